@@ -1,0 +1,386 @@
+"""Benchmark: DOF/s of assemble + Dirichlet + Jacobi-PCG to a 1e-10 relative
+residual on one GB300, FP32-refined (FP32 iterations + FP64 reliable updates)
+beside plain FP64, on the P2 diffusion+mass tetrahedral workload
+(TetrahedronMesh box of 64^3 cubes, 1,572,864 cells, 2,146,689 dofs; interior
+nodes jittered +-0.2h; lognormal(0,1) per-cell diffusion; reaction 1; f = 1;
+u = 0 on the boundary; quadrature index 4).
+
+One step = symbolic CSR pattern + numeric assembly + right-hand side +
+Dirichlet elimination + PCG, with the mesh, dof map and coefficients already in
+HBM (``value``); ``e2e`` repeats the step through the public API starting from
+pinned host arrays (upload, mesh topology, dof numbering, boundary flags,
+the step, and the solution copied back).  Inputs (a 0.7 GB FP64 matrix) are
+larger than the 129 MB L2, so no L2 flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--n 64]
+
+Under torchrun every rank runs an independent replica (the path does not
+shard across GPUs; see the design notes); ``value`` is the total dofs solved per
+second over all ranks, with the slowest rank's time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "DOF/s assemble+PCG to 1e-10 rel res, FP32-refined vs FP64 on GB300; serve p50/p99"
+RTOL = 1e-10
+Q = 4
+CPU_SAMPLE_N = 24
+MAXIT = 20000
+
+
+def read_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("uuid,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, uuid=None):
+        self.uuid = uuid
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        rows = [[p.strip() for p in ln.split(",")] for ln in self.lines]
+        rows = [r for r in rows if len(r) >= 8]
+        uuids = sorted({r[0] for r in rows})
+        want = None
+        if self.uuid:
+            key = self.uuid.replace("GPU-", "").lower()
+            for u in uuids:
+                if key and (key in u.lower() or u.lower().replace("gpu-", "") in key):
+                    want = u
+        if want is None and len(uuids) == 1:
+            want = uuids[0]
+        if want is None:
+            return None
+        for parts in rows:
+            if parts[0] != want:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+def build_problem(torch, F, node_np, cell_np, kappa_np, dev):
+    node = torch.as_tensor(node_np, device=dev)
+    cell = torch.as_tensor(cell_np, device=dev)
+    kappa = torch.as_tensor(kappa_np, device=dev)
+    mesh = F.TetrahedronMesh(node, cell)
+    space = F.LagrangeFESpace(mesh, p=2)
+    space.cell_to_dof()
+    from fealpy_gb300.fem import DirichletBC
+    bc = DirichletBC(space, gd=0.0)
+    return mesh, space, kappa, bc
+
+
+def solve_step(torch, F, space, kappa, bc, mode, profile=False):
+    """symbolic + numeric assembly + RHS + Dirichlet + PCG; returns (x, info, A)."""
+    from fealpy_gb300.fem import BilinearForm, LinearForm, ScalarDiffusionIntegrator, ScalarMassIntegrator
+    from fealpy_gb300.fem import ScalarSourceIntegrator
+    space._cache.clear()
+    bf = BilinearForm(space)
+    bf.add_integrator(ScalarDiffusionIntegrator(coef=kappa, q=Q), ScalarMassIntegrator(coef=1.0, q=Q))
+    A = bf.assembly(emit_f32=(mode == "mixed"))
+    lf = LinearForm(space)
+    lf.add_integrator(ScalarSourceIntegrator(1.0, q=Q))
+    Fv = lf.assembly()
+    A2, F2 = bc.apply(A, Fv)
+    if mode == "mixed":
+        A2._f32 = A2.values.to(torch.float32)
+        x, info = F.cg_mixed(A2, F2, rtol=RTOL, maxit=MAXIT, returninfo=True, profile=profile)
+    else:
+        M = F.JacobiPreconditioner().apply(A2)
+        x, info = F.cg(A2, F2, M=M, atol=0.0, rtol=RTOL, maxit=MAXIT, returninfo=True, stop="residual",
+                       profile=profile)
+    return x, info, A2, F2
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+    import fealpy_gb300 as F
+    from fealpy_gb300 import _lib
+    from fealpy_gb300.workloads import diffusion_mass_tet_box
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    n = args.n
+    node_np, cell_np, kappa_np = diffusion_mass_tet_box(n)
+    mesh, space, kappa, bc = build_problem(torch, F, node_np, cell_np, kappa_np, dev)
+    gdof = space.number_of_global_dofs()
+    stream = torch.cuda.current_stream(dev)
+
+    def barrier():
+        torch.cuda.synchronize(dev)
+        if world > 1:
+            dist.barrier()
+
+    def max_over_ranks(v):
+        if world == 1:
+            return v
+        t = torch.tensor([v], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    results = {}
+    for mode in ("fp64", "mixed"):
+        for _ in range(args.warmup):
+            solve_step(torch, F, space, kappa, bc, mode)
+        barrier()
+        sampler = ClockSampler(getattr(torch.cuda.get_device_properties(dev), "uuid", None) and
+                               str(torch.cuda.get_device_properties(dev).uuid)) if mode == "mixed" else None
+        if sampler:
+            sampler.start()
+            time.sleep(0.3)
+        launches0 = _lib.launch_count()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        barrier()
+        ev0.record(stream)
+        infos = []
+        for _ in range(args.steps):
+            x, info, A2, F2 = solve_step(torch, F, space, kappa, bc, mode, profile=True)
+            infos.append(info)
+        ev1.record(stream)
+        barrier()
+        ms = ev0.elapsed_time(ev1)
+        clocks = sampler.stop() if sampler else None
+        launches = _lib.launch_count() - launches0
+        ms = max_over_ranks(ms)
+        r = F2 - A2 @ x
+        relres = float(torch.linalg.norm(r) / torch.linalg.norm(F2))
+        kms = sum(i["kernel_ms"] for i in infos)
+        kl = sum(i["kernel_launches"] for i in infos)
+        results[mode] = {"ms": ms, "ms_per_step": ms / args.steps, "x": x, "relres": relres,
+                         "niter": infos[-1]["niter"], "n_updates": infos[-1].get("n_updates", 0),
+                         "kernel_ms_avg": kms / max(kl, 1), "kernel_launches": kl, "launches": launches,
+                         "clocks": clocks, "nnz": A2.nnz, "n": gdof}
+
+    x64 = results["fp64"]["x"]
+    xm = results["mixed"]["x"]
+    err = float(torch.max(torch.abs(xm - x64)) / torch.max(torch.abs(x64)))
+
+    # e2e: from pinned host arrays through the public API, solution back to host
+    node_h = torch.as_tensor(node_np).pin_memory()
+    cell_h = torch.as_tensor(cell_np).pin_memory()
+    kappa_h = torch.as_tensor(kappa_np).pin_memory()
+    x_h = torch.empty(gdof, dtype=torch.float64).pin_memory()
+
+    def e2e_step():
+        nd = node_h.to(dev, non_blocking=True)
+        cl = cell_h.to(dev, non_blocking=True)
+        kp = kappa_h.to(dev, non_blocking=True)
+        m = F.TetrahedronMesh(nd, cl)
+        sp_ = F.LagrangeFESpace(m, p=2)
+        from fealpy_gb300.fem import DirichletBC
+        bc_ = DirichletBC(sp_, gd=0.0)
+        x, info, _, _ = solve_step(torch, F, sp_, kp, bc_, "mixed")
+        x_h.copy_(x, non_blocking=True)
+        torch.cuda.synchronize(dev)
+
+    e2e_step()
+    barrier()
+    t0 = time.perf_counter()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    e2e_steps = max(1, min(args.steps, 3))
+    for _ in range(e2e_steps):
+        e2e_step()
+    e1.record(stream)
+    barrier()
+    e2e_ms = max_over_ranks(max(e0.elapsed_time(e1), (time.perf_counter() - t0) * 1e3))
+    h2d = node_np.nbytes + cell_np.nbytes + kappa_np.nbytes
+    d2h = gdof * 8
+
+    peak, peak_kind = read_peaks()
+    mixed = results["mixed"]
+    fp64 = results["fp64"]
+    value = world * gdof / (mixed["ms_per_step"] / 1e3)
+    # dominant kernel: the fused FP32 PCG SpMV (p = z + beta p_old, Ap = A p, p.Ap)
+    nnz = mixed["nnz"]
+    bytes_per_launch = nnz * (4 + 4) + gdof * (8 + 4 * 4)
+    achieved = bytes_per_launch / (mixed["kernel_ms_avg"] / 1e3) / 1e9 if mixed["kernel_ms_avg"] > 0 else 0.0
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tp):
+        try:
+            traffic = json.load(open(tp)).get("pcg_spmv_f32_bytes_per_launch_at_n64")
+        except Exception:
+            traffic = None
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(CPU_SAMPLE_N, repeats=3)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "DOF/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": mixed["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+            "data": "synthetic (seeded jittered tet box, lognormal coefficients)",
+            "config": {"workload": f"P2 diffusion+mass TetrahedronMesh box {n}^3 (C2)", "cells": int(cell_np.shape[0]),
+                       "gdof": gdof, "nnz": nnz, "quadrature": Q, "rtol": RTOL,
+                       "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{world}"},
+            "fp32_refined": {"ms_per_step": mixed["ms_per_step"], "dof_per_s": value, "cg_iters": mixed["niter"],
+                             "reliable_updates": mixed["n_updates"], "true_relres": mixed["relres"],
+                             "max_rel_err_vs_fp64": err},
+            "fp64": {"ms_per_step": fp64["ms_per_step"], "dof_per_s": world * gdof / (fp64["ms_per_step"] / 1e3),
+                     "cg_iters": fp64["niter"], "true_relres": fp64["relres"]},
+            "speedup_fp32_refined_vs_fp64": fp64["ms_per_step"] / mixed["ms_per_step"],
+            "e2e": {"value": world * gdof * e2e_steps / (e2e_ms / 1e3), "unit": "DOF/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "steps": e2e_steps},
+            "gpu_launches": mixed["launches"],
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak if peak else None, "traffic": traffic,
+                         "kernel": "pcg_spmv_kernel<float> (fused p-update + SpMV + p.Ap)",
+                         "algorithmic_bytes_per_launch": bytes_per_launch,
+                         "avg_launch_ms": mixed["kernel_ms_avg"], "peak_source": peak_kind},
+            "clocks": mixed["clocks"],
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+# CPU reference (the oracle: numpy/scipy restatement of the reference path)
+# ---------------------------------------------------------------------------
+def oracle_step(n):
+    from oracle import fem_oracle as O
+    from fealpy_gb300.workloads import diffusion_mass_tet_box
+    node, cell, kappa = diffusion_mass_tet_box(n)
+    t0 = time.perf_counter()
+    out = O.poisson_pipeline(node, cell, 2, kappa=kappa, rho=1.0, q=Q, rtol=RTOL)
+    dt = time.perf_counter() - t0
+    return out["n"], dt, out["info"]["niter"]
+
+
+def cpu_baseline(n, repeats=3):
+    times = []
+    gdof = niter = 0
+    for _ in range(repeats):
+        gdof, dt, niter = oracle_step(n)
+        times.append(dt)
+    t = statistics.median(times)
+    return {"value": gdof / t, "unit": "DOF/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": f"P2 diffusion+mass tet box {n}^3 ({gdof} dofs, {niter} PCG iterations), median of {repeats}; "
+                      f"numpy/scipy oracle restating the reference numpy path (einsum, lexsort+add.at coalesce, "
+                      f"scipy csr_matvec CG)",
+            "seconds_per_sample": t}
+
+
+def run_reference(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    n = CPU_SAMPLE_N
+    for _ in range(args.warmup):
+        oracle_step(n)
+    times = []
+    gdof = niter = 0
+    for _ in range(args.steps):
+        gdof, dt, niter = oracle_step(n)
+        times.append(dt)
+    tot = sum(times)
+    value = gdof * len(times) / tot
+    line = {"metric": METRIC, "value": value, "unit": "DOF/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": tot / len(times) * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded jittered tet box)",
+            "impl": "reference",
+            "config": {"workload": f"P2 diffusion+mass TetrahedronMesh box (C2 family), bounded host sample {n}^3",
+                       "gdof": gdof, "quadrature": Q, "rtol": RTOL},
+            "cpu_baseline": {"value": value, "unit": "DOF/s", "cores": os.cpu_count(), "kind": "port",
+                             "sample": f"{n}^3 P2 tet box ({gdof} dofs, {niter} PCG iterations) per step"},
+            "e2e": {"value": value, "unit": "DOF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=64)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

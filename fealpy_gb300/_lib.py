@@ -1,0 +1,199 @@
+"""ctypes binding of ``libfealpy_gb300.so`` (the C ABI in ``include/fealpy_gb300.h``).
+
+This module is the only place that touches the shared library.  It loads the
+in-tree build, declares every entry point's signature, maps status codes to the
+exception types FEALPy raises (``ValueError`` for bad arguments,
+``RuntimeError`` for everything found while running), and provides the small
+amount of plumbing the host code needs: raw device pointers of torch tensors,
+the current CUDA stream, and workspaces carved from torch's caching allocator.
+
+There is no fallback: if the library is missing or no CUDA device is present,
+every call raises.
+"""
+import ctypes
+import os
+import threading
+
+import torch
+
+from . import _build
+
+_LOCK = threading.Lock()
+_LIB = None
+
+c_i32 = ctypes.c_int32
+c_i64 = ctypes.c_int64
+c_sz = ctypes.c_size_t
+c_dbl = ctypes.c_double
+c_vp = ctypes.c_void_p
+
+FGB_F32 = 0
+FGB_F64 = 1
+
+FGB_CH_MEASURE = 0
+FGB_CH_METRIC = 1
+FGB_CH_GRAD = 16
+FGB_MAX_CHANNELS = 16
+
+STATUS_NAMES = {
+    0: "ok", 1: "invalid argument", 2: "workspace missing or too small", 3: "index out of range",
+    4: "contribution outside the CSR pattern", 5: "non-finite value", 6: "CG breakdown (matrix not SPD)",
+    7: "CUDA error", 8: "size exceeds a fixed kernel limit",
+}
+
+PCG_REASONS = {0: "running", 1: "atol", 2: "rtol", 3: "maxit", 4: "zero rhs", 5: "breakdown", 6: "nonfinite"}
+
+
+class PcgInfo(ctypes.Structure):
+    _fields_ = [("niter", c_i64), ("residual", c_dbl), ("b_norm", c_dbl), ("true_relres", c_dbl),
+                ("reason", c_i32), ("n_updates", c_i32), ("launches", c_i64), ("kernel_ms", c_dbl),
+                ("kernel_launches", c_i64)]
+
+
+# name: (restype, [argtypes])
+_SIGNATURES = {
+    "fgb_status_string": (ctypes.c_char_p, [c_i32]),
+    "fgb_abi_version": (c_i32, []),
+    "fgb_scan_workspace_bytes": (c_sz, [c_i64]),
+    "fgb_exclusive_scan_i32": (c_i32, [c_vp, c_i64, c_vp, c_vp, c_sz, c_vp]),
+    "fgb_adjacency_workspace_bytes": (c_sz, [c_i64]),
+    "fgb_adjacency_build": (c_i32, [c_i64, c_i32, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_sz, c_vp]),
+    "fgb_pattern_workspace_bytes": (c_sz, [c_i64]),
+    "fgb_pattern_count": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_i32, c_vp, c_vp, c_vp, c_sz, c_vp]),
+    "fgb_pattern_fill": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_i32, c_vp, c_vp, c_vp, c_vp, c_sz, c_vp]),
+    "fgb_pattern_expand_blocks": (c_i32, [c_i64, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "fgb_cell_factors": (c_i32, [c_i32, c_i64, c_vp, c_vp, c_i32, c_vp, c_vp, c_vp, c_vp, c_i32, c_vp, c_vp, c_vp]),
+    "fgb_assemble_workspace_bytes": (c_sz, [c_i64]),
+    "fgb_assemble_scalar": (c_i32, [c_i32, c_i64, c_vp, c_vp, c_vp, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp,
+                                    c_vp, c_vp, c_vp, c_sz, c_vp]),
+    "fgb_assemble_elasticity_p1": (c_i32, [c_i32, c_i32, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp,
+                                           c_vp, c_vp, c_vp, c_sz, c_vp]),
+    "fgb_dirichlet_count": (c_i32, [c_i32, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "fgb_dirichlet_fill": (c_i32, [c_i32, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "fgb_csr_spmv": (c_i32, [c_i32, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_i32, c_vp]),
+    "fgb_csr_diagonal": (c_i32, [c_i32, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "fgb_pcg_workspace_bytes": (c_sz, [c_i64]),
+    "fgb_pcg_f64": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_dbl, c_dbl, c_i64, c_i32, c_i32, c_i32,
+                            c_i32, c_vp, c_sz, ctypes.POINTER(PcgInfo), c_vp]),
+    "fgb_pcg_mixed_workspace_bytes": (c_sz, [c_i64]),
+    "fgb_pcg_mixed": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_dbl, c_dbl, c_i64, c_i32, c_i32,
+                              c_i32, c_vp, c_sz, ctypes.POINTER(PcgInfo), c_vp]),
+    "fgb_gather_sum": (c_i32, [c_i32, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp]),
+}
+
+
+def library_path() -> str:
+    return _build.LIB_PATH
+
+
+def lib():
+    """Load (building first if absent) and return the ctypes library handle."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    with _LOCK:
+        if _LIB is None:
+            path = library_path()
+            if not os.path.exists(path):
+                _build.build()
+            handle = ctypes.CDLL(path)
+            for name, (res, args) in _SIGNATURES.items():
+                fn = getattr(handle, name)
+                fn.restype = res
+                fn.argtypes = args
+            _LIB = handle
+    return _LIB
+
+
+def exported_symbols():
+    return sorted(_SIGNATURES)
+
+
+class FgbError(RuntimeError):
+    def __init__(self, fn, code):
+        self.code = code
+        super().__init__(f"{fn} failed: {STATUS_NAMES.get(code, 'unknown')} (status {code})")
+
+
+def check(fn_name, code):
+    if code != 0:
+        if code == 1:
+            raise ValueError(f"{fn_name}: invalid argument (status 1)")
+        raise FgbError(fn_name, code)
+
+
+# Kernels each entry point launches per call (the solvers report theirs in
+# fgb_pcg_info.launches).  Used to count this library's launches in a region.
+KERNELS_PER_CALL = {
+    "fgb_cell_factors": 1, "fgb_adjacency_build": 6, "fgb_pattern_count": 5, "fgb_pattern_fill": 2,
+    "fgb_pattern_expand_blocks": 2, "fgb_assemble_scalar": 2, "fgb_assemble_elasticity_p1": 2,
+    "fgb_dirichlet_count": 1, "fgb_exclusive_scan_i32": 3, "fgb_dirichlet_fill": 1, "fgb_csr_spmv": 1,
+    "fgb_csr_diagonal": 1, "fgb_gather_sum": 1,
+}
+
+_launches = [0]
+
+
+def launch_count() -> int:
+    """Kernels launched by this library in this process so far."""
+    return _launches[0]
+
+
+def add_launches(n: int):
+    _launches[0] += int(n)
+
+
+def call(name, *args):
+    """Call an entry point and raise on a non-zero status."""
+    code = getattr(lib(), name)(*args)
+    check(name, code)
+    _launches[0] += KERNELS_PER_CALL.get(name, 0)
+    return code
+
+
+# ---------------------------------------------------------------------------
+# device plumbing
+# ---------------------------------------------------------------------------
+def require_cuda(t: torch.Tensor, name: str = "tensor"):
+    if not isinstance(t, torch.Tensor) or t.device.type != "cuda":
+        raise ValueError(f"{name} must be a CUDA tensor (fealpy_gb300 runs on the GPU only)")
+    return t
+
+
+def ptr(t):
+    """Raw device pointer of a contiguous CUDA tensor (None -> NULL)."""
+    if t is None:
+        return None
+    if t.device.type != "cuda":
+        raise ValueError("expected a CUDA tensor")
+    if not t.is_contiguous():
+        raise ValueError("expected a contiguous tensor")
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def stream_ptr(device=None):
+    return ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+
+
+def dtype_code(dtype) -> int:
+    if dtype == torch.float64:
+        return FGB_F64
+    if dtype == torch.float32:
+        return FGB_F32
+    raise ValueError(f"unsupported floating dtype {dtype}")
+
+
+def workspace(nbytes: int, device) -> torch.Tensor:
+    """Scratch buffer from torch's caching allocator (256-byte aligned)."""
+    nbytes = max(int(nbytes), 256)
+    return torch.empty(nbytes, dtype=torch.uint8, device=device)
+
+
+def status_word(device) -> torch.Tensor:
+    return torch.zeros(1, dtype=torch.int32, device=device)
+
+
+def check_status_word(fn_name: str, st: torch.Tensor):
+    code = int(st.item())
+    if code != 0:
+        raise FgbError(fn_name, code)

@@ -1,0 +1,132 @@
+// Dirichlet boundary conditions by symmetric elimination on a canonical CSR.
+//
+// FEALPy's DirichletBC.apply (fealpy/fem/dirichlet_bc.py:101-229) first forms
+// f - A u_D with one SpMV and overwrites f on boundary dofs, then drops every
+// CSR entry whose row or column is a boundary dof (mask + cumsum, _mul) and
+// adds a unit diagonal on boundary rows through CSRTensor.add -> COO -> tocsr
+// (which leaves the columns of each row in argsort order).  Here one warp per
+// row does both vector and matrix work in two passes (count, then fill after a
+// scan of the new row lengths) and emits the rows in canonical column order.
+
+#include "fgb_common.cuh"
+
+namespace fgb {
+
+template <typename T>
+__global__ void dirichlet_count_kernel(int64_t n, const int64_t* __restrict__ indptr, const int32_t* __restrict__ indices,
+                                       const T* __restrict__ values, const uint8_t* __restrict__ is_bd,
+                                       const T* __restrict__ f, const T* __restrict__ u_bd, T* __restrict__ f_out,
+                                       int32_t* __restrict__ row_nnz) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
+  const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+  for (int64_t i = warp; i < n; i += nwarps) {
+    if (is_bd[i]) {
+      if (lane == 0) {
+        if (f_out) f_out[i] = u_bd[i];
+        row_nnz[i] = 1;
+      }
+      continue;
+    }
+    // f - A uh over the whole row, as FEALPy's f - A.matmul(uh): uh is zero off
+    // the boundary unless the caller passed interior values in it
+    const int64_t s = indptr[i], e = indptr[i + 1];
+    T acc = T(0);
+    int cnt = 0;
+    for (int64_t k = s + lane; k < e; k += 32) {
+      const int32_t j = indices[k];
+      if (f_out) acc += values[k] * u_bd[j];
+      if (!is_bd[j]) ++cnt;
+    }
+    cnt = warp_sum(cnt);
+    if (f_out) acc = warp_sum(acc);
+    if (lane == 0) {
+      row_nnz[i] = cnt;
+      if (f_out) f_out[i] = f[i] - acc;
+    }
+  }
+}
+
+template <typename T>
+__global__ void dirichlet_fill_kernel(int64_t n, const int64_t* __restrict__ indptr, const int32_t* __restrict__ indices,
+                                      const T* __restrict__ values, const uint8_t* __restrict__ is_bd,
+                                      const int64_t* __restrict__ new_indptr, int32_t* __restrict__ new_indices,
+                                      T* __restrict__ new_values) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
+  const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+  for (int64_t i = warp; i < n; i += nwarps) {
+    const int64_t o = new_indptr[i];
+    if (is_bd[i]) {
+      if (lane == 0) {
+        new_indices[o] = static_cast<int32_t>(i);
+        new_values[o] = T(1);
+      }
+      continue;
+    }
+    const int64_t s = indptr[i], e = indptr[i + 1];
+    int64_t run = 0;
+    for (int64_t base = s; base < e; base += 32) {
+      const int64_t k = base + lane;
+      bool keep = false;
+      int32_t j = 0;
+      if (k < e) {
+        j = indices[k];
+        keep = !is_bd[j];
+      }
+      const unsigned ball = __ballot_sync(0xffffffffu, keep);
+      if (keep) {
+        const int64_t pos = o + run + __popc(ball & ((1u << lane) - 1u));
+        new_indices[pos] = j;
+        new_values[pos] = values[k];
+      }
+      run += __popc(ball);
+    }
+  }
+}
+
+}  // namespace fgb
+
+using namespace fgb;
+
+extern "C" {
+
+int32_t fgb_dirichlet_count(int32_t dtype, int64_t n, const int64_t* indptr, const int32_t* indices,
+                            const void* values, const uint8_t* is_bd, const void* f, const void* u_bd, void* f_out,
+                            int32_t* row_nnz, void* stream) {
+  if (n <= 0 || !indptr || !indices || !is_bd || !row_nnz) return FGB_ERR_ARG;
+  if (f_out && (!values || !f || !u_bd)) return FGB_ERR_ARG;
+  cudaStream_t st = as_stream(stream);
+  const int grid = grid_for(n * 32, 256, kNumSMs * 16);
+  if (dtype == FGB_F64)
+    dirichlet_count_kernel<double><<<grid, 256, 0, st>>>(n, indptr, indices, static_cast<const double*>(values), is_bd,
+                                                         static_cast<const double*>(f), static_cast<const double*>(u_bd),
+                                                         static_cast<double*>(f_out), row_nnz);
+  else if (dtype == FGB_F32)
+    dirichlet_count_kernel<float><<<grid, 256, 0, st>>>(n, indptr, indices, static_cast<const float*>(values), is_bd,
+                                                        static_cast<const float*>(f), static_cast<const float*>(u_bd),
+                                                        static_cast<float*>(f_out), row_nnz);
+  else
+    return FGB_ERR_ARG;
+  return launch_status();
+}
+
+int32_t fgb_dirichlet_fill(int32_t dtype, int64_t n, const int64_t* indptr, const int32_t* indices, const void* values,
+                           const uint8_t* is_bd, const int64_t* new_indptr, int32_t* new_indices, void* new_values,
+                           void* stream) {
+  if (n <= 0 || !indptr || !indices || !values || !is_bd || !new_indptr || !new_indices || !new_values)
+    return FGB_ERR_ARG;
+  cudaStream_t st = as_stream(stream);
+  const int grid = grid_for(n * 32, 256, kNumSMs * 16);
+  if (dtype == FGB_F64)
+    dirichlet_fill_kernel<double><<<grid, 256, 0, st>>>(n, indptr, indices, static_cast<const double*>(values), is_bd,
+                                                        new_indptr, new_indices, static_cast<double*>(new_values));
+  else if (dtype == FGB_F32)
+    dirichlet_fill_kernel<float><<<grid, 256, 0, st>>>(n, indptr, indices, static_cast<const float*>(values), is_bd,
+                                                       new_indptr, new_indices, static_cast<float*>(new_values));
+  else
+    return FGB_ERR_ARG;
+  return launch_status();
+}
+
+}  // extern "C"

@@ -1,0 +1,196 @@
+"""``BilinearForm`` / ``LinearForm`` with FEALPy's interface
+(``fealpy/fem/form.py``, ``bilinear_form.py``, ``linear_form.py``).
+
+``BilinearForm.assembly`` runs the symbolic phase (dof adjacency + canonical
+CSR pattern) and the numeric phase (factor kernel + row-gather assembly) on the
+GPU and returns a :class:`~fealpy_gb300.sparse.CSRTensor` whose pattern equals
+FEALPy's coalesced CSR and whose values match it to rounding.
+"""
+from typing import Optional, Sequence
+
+import torch
+
+from ..functionspace import TensorFunctionSpace
+from ..sparse import CSRTensor
+from .. import _lib
+from .. import kernels as K
+from .integrators import (ElasticityPlan, GroupIntegrator, Integrator, ScalarPlan, VectorSourceIntegrator)
+
+__all__ = ["BilinearForm", "LinearForm", "symbolic_structure"]
+
+
+def symbolic_structure(c2d: torch.Tensor, n_dof: int, status: Optional[torch.Tensor] = None):
+    """(adj_ptr, adj, indptr, indices) for a cell-to-dof map."""
+    st = _lib.status_word(c2d.device) if status is None else status
+    adj_ptr, adj, _ = K.build_adjacency(c2d, n_dof, st)
+    indptr, indices = K.build_pattern(adj_ptr, adj, c2d, n_dof, st)
+    return adj_ptr, adj, indptr, indices
+
+
+class _Form:
+    def __init__(self, *space, batch_size: int = 0):
+        if len(space) == 0:
+            raise ValueError("No space is given.")
+        if isinstance(space[0], Sequence):
+            space = tuple(space[0])
+        if len(space) != 1:
+            raise NotImplementedError("forms over two different spaces are not provided")
+        if batch_size != 0:
+            raise NotImplementedError("batched forms are not provided")
+        self._spaces = space
+        self.integrators = {}
+        self.splitters = {}
+        self._cursor = 0
+        self.batch_size = batch_size
+
+    @property
+    def space(self):
+        return self._spaces[0]
+
+    def __len__(self):
+        return len(self.integrators)
+
+    def add_integrator(self, *I, region=None, splitter=None, group=None):
+        if len(I) == 0:
+            return self
+        if len(I) == 1 and isinstance(I[0], (list, tuple)):
+            I = tuple(I[0])
+        if len(I) == 1:
+            I = I[0]
+            if region is not None:
+                I.set_region(region)
+        else:
+            I = GroupIntegrator(*I, region=region)
+        group = f"_group_{self._cursor}" if group is None else group
+        self._cursor += 1
+        if group in self.integrators:
+            self.integrators[group] = self.integrators[group] + I
+        else:
+            self.integrators[group] = I
+        # cell chunking (UniformSplitter) has no effect on a row-gather assembly
+        self.splitters[group] = splitter
+        return self
+
+    def __lshift__(self, other):
+        if isinstance(other, Integrator):
+            return self.add_integrator(other)
+        return NotImplemented
+
+
+class BilinearForm(_Form):
+    _M = None
+
+    def __init__(self, *space, batch_size: int = 0, reuse_pattern: bool = False):
+        super().__init__(*space, batch_size=batch_size)
+        self.reuse_pattern = reuse_pattern
+        s = self.space
+        n = s.number_of_global_dofs()
+        self.sparse_shape = (n, n)
+
+    @property
+    def shape(self):
+        return self.sparse_shape
+
+    def _plan(self):
+        plans = [it.plan(self.space) for it in self.integrators.values()]
+        if not plans:
+            raise RuntimeError("no integrator added to the form")
+        out = plans[0]
+        for p in plans[1:]:
+            if isinstance(out, ScalarPlan) and isinstance(p, ScalarPlan):
+                out = out + p
+            else:
+                raise NotImplementedError("only several scalar integrators can share one form")
+        return out
+
+    def _symbolic(self, space, c2d, n):
+        key = ("symbolic", n)
+        cache = getattr(space, "_cache", {})
+        if self.reuse_pattern and key in cache:
+            return cache[key]
+        out = symbolic_structure(c2d, n)
+        if self.reuse_pattern:
+            cache[key] = out
+        return out
+
+    def assembly(self, *, format="csr", dtype=torch.float64, emit_f32: bool = False) -> CSRTensor:
+        """Assemble the global matrix.  ``dtype`` float64 (default) or float32
+        selects the arithmetic of the factor and assembly kernels;
+        ``emit_f32`` also stores a float copy of float64 values on the result
+        (used by the mixed-precision solver)."""
+        if format not in ("csr", "coo"):
+            raise ValueError(f"Unsupported format {format}.")
+        if format == "coo":
+            raise NotImplementedError("the GB300 path emits CSR")
+        space = self.space
+        plan = self._plan()
+        status = _lib.status_word(space.device)
+        if isinstance(plan, ScalarPlan):
+            c2d = space.cell_to_dof()
+            n = space.number_of_global_dofs()
+            adj_ptr, adj, indptr, indices = self._symbolic(space, c2d, n)
+            mesh = space.mesh
+            fac = K.cell_factors(mesh, plan.channels, plan.coef_matrix(), dtype, status)
+            tab = torch.as_tensor(plan.tables, dtype=dtype, device=space.device)
+            values, v32 = K.assemble_scalar(adj_ptr, adj, c2d, tab, fac, indptr, indices,
+                                            values_f32=emit_f32 and dtype == torch.float64, status=status)
+        elif isinstance(plan, ElasticityPlan):
+            ss = space.scalar_space
+            mesh = ss.mesh
+            cell = mesh.cell
+            NN = mesh.number_of_nodes()
+            adj_ptr, adj, nptr, nidx = self._symbolic(ss, cell, NN)
+            indptr, indices = K.expand_blocks(NN, plan.gd, space.dof_priority, nptr, nidx)
+            n = space.number_of_global_dofs()
+            fac = K.cell_factors(mesh, plan.channels, plan.coef_matrix(), dtype, status)
+            values, v32 = K.assemble_elasticity_p1(plan.gd, adj_ptr, adj, cell, fac, nptr, nidx, indptr,
+                                                   indices.numel(), values_f32=emit_f32 and dtype == torch.float64,
+                                                   status=status)
+        else:
+            raise NotImplementedError
+        _lib.check_status_word("assembly", status)
+        M = CSRTensor(indptr, indices, values, (n, n))
+        if v32 is not None:
+            M._f32 = v32
+        self._M = M
+        return M
+
+    def __matmul__(self, u):
+        if self._M is None:
+            self.assembly()
+        return self._M @ u
+
+    def mult(self, x, out=None):
+        return self @ x
+
+
+class LinearForm(_Form):
+    """Right-hand-side vector: cell vectors from the source integrators, summed
+    into dofs by the deterministic adjacency gather."""
+
+    def __init__(self, *space, batch_size: int = 0):
+        super().__init__(*space, batch_size=batch_size)
+        self._V = None
+
+    def assembly(self, *, format="dense") -> torch.Tensor:
+        space = self.space
+        local = None
+        for it in self.integrators.values():
+            ints = it.ints if isinstance(it, GroupIntegrator) else [it]
+            for i in ints:
+                v = i.assembly(space)
+                local = v if local is None else local + v
+        if local is None:
+            raise RuntimeError("no integrator added to the form")
+        c2d = space.cell_to_dof()
+        n = space.number_of_global_dofs()
+        key = ("adjacency", n)
+        cache = space._cache
+        if key not in cache:
+            st = _lib.status_word(space.device)
+            adj_ptr, adj, _ = K.build_adjacency(c2d, n, st)
+            _lib.check_status_word("adjacency", st)
+            cache[key] = (adj_ptr, adj)
+        adj_ptr, adj = cache[key]
+        self._V = K.gather_sum(adj_ptr, adj, local.to(torch.float64).contiguous())
+        return self._V

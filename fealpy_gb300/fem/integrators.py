@@ -1,0 +1,387 @@
+"""Integrators with FEALPy's interface (``fealpy/fem/integrator.py``,
+``scalar_diffusion_integrator.py``, ``scalar_mass_integrator.py``,
+``linear_elasticity_integrator.py``, ``scalar_source_integrator.py``).
+
+An operator integrator here does not build local matrices on the assembly
+path.  It describes its local matrix as ``sum_t factor_t(cell) * table_t`` (a
+*plan*): the factors are per-cell geometric quantities computed by the
+``fgb_cell_factors`` kernel (signed measure, Jacobian-inverse metric, times the
+coefficient) and the tables are mesh-independent contractions of the basis
+gradients with the integrator's own quadrature rule.  ``BilinearForm`` merges
+the plans of all integrators on a space into a single factor launch and a
+single CSR assembly launch.  ``assembly(space)`` still returns the
+(NC, ldof, ldof) local matrices for callers that want them.
+"""
+from typing import List, Optional, Tuple
+
+import numpy as np
+import torch
+
+from .. import _lib
+from .. import simplex as sx
+from ..functionspace import TensorFunctionSpace
+from .. import kernels as K
+
+__all__ = ["Integrator", "GroupIntegrator", "ScalarDiffusionIntegrator", "ScalarMassIntegrator",
+           "LinearElasticityIntegrator", "ScalarSourceIntegrator", "VectorSourceIntegrator", "ScalarPlan",
+           "ElasticityPlan"]
+
+_S = slice(None)
+
+
+def _is_full(index) -> bool:
+    return index is None or (isinstance(index, slice) and index == slice(None))
+
+
+class ScalarPlan:
+    """Local matrix = sum_t factor_t(c) * tables[t]; channel t = (kind, coef_row, scale)."""
+
+    def __init__(self, channels: List[Tuple[int, int, float]], coefs: List[torch.Tensor], tables: np.ndarray):
+        self.channels = channels
+        self.coefs = coefs
+        self.tables = tables
+
+    def __add__(self, other: "ScalarPlan") -> "ScalarPlan":
+        off = len(self.coefs)
+        ch = list(self.channels) + [(k, (c + off) if c >= 0 else -1, s) for k, c, s in other.channels]
+        return ScalarPlan(ch, self.coefs + other.coefs, np.concatenate([self.tables, other.tables], axis=0))
+
+    def coef_matrix(self):
+        return torch.stack(self.coefs, 0) if self.coefs else None
+
+
+class ElasticityPlan:
+    """P1 elasticity: factor channels = grad(lambda_{1..GD}) then |T| D00, |T| D_lambda, |T| D_mu."""
+
+    def __init__(self, gd: int, channels, coefs):
+        self.gd = gd
+        self.channels = channels
+        self.coefs = coefs
+
+    def coef_matrix(self):
+        return torch.stack(self.coefs, 0) if self.coefs else None
+
+
+def _cell_coefficient(coef, space, q: int) -> Tuple[float, Optional[torch.Tensor]]:
+    """(scale, per-cell array or None) from a FEALPy CoefLike.  Coefficients must
+    be constant on each cell; a callable is evaluated at the quadrature points
+    and accepted when its values agree across each cell's points."""
+    mesh = space.mesh
+    NC = mesh.number_of_cells()
+    if coef is None:
+        return 1.0, None
+    if isinstance(coef, (int, float)):
+        return float(coef), None
+    if isinstance(coef, torch.Tensor):
+        if coef.numel() == 1:
+            return float(coef.reshape(-1)[0].item()), None
+        if coef.ndim == 1 and coef.shape[0] == NC:
+            return 1.0, coef.to(device=mesh.device, dtype=torch.float64)
+        if coef.ndim == 2 and coef.shape[0] == NC:
+            val = coef.to(device=mesh.device, dtype=torch.float64)
+            if bool(torch.all(val == val[:, :1])):
+                return 1.0, val[:, 0].contiguous()
+        raise NotImplementedError("coefficients must be constant per cell: scalar, (NC,) or (NC, NQ) with equal "
+                                  "values along the quadrature axis")
+    if isinstance(coef, np.ndarray):
+        return _cell_coefficient(torch.as_tensor(coef, device=mesh.device), space, q)
+    if callable(coef):
+        bcs, _ = mesh.quadrature_formula(q).get_quadrature_points_and_weights()
+        if getattr(coef, "coordtype", "barycentric") == "cartesian":
+            val = coef(mesh.bc_to_point(bcs))
+        else:
+            val = coef(torch.as_tensor(bcs, device=mesh.device), index=_S)
+        return _cell_coefficient(torch.as_tensor(val, device=mesh.device), space, q)
+    raise TypeError(f"coef should be int, float, TensorLike or callable, but got {type(coef)}")
+
+
+class Integrator:
+    """Base class: region handling, data cache switch and ``+`` grouping."""
+    etype = "cell"
+
+    def __init__(self, keep_data: bool = False):
+        self._region = None
+        self._cache = {}
+        self._keep_data = keep_data
+
+    def keep_data(self, status_on=True):
+        self._keep_data = status_on
+        if not status_on:
+            self._cache.clear()
+        return self
+
+    def clear(self):
+        self._cache.clear()
+
+    def set_region(self, region):
+        self._region = region
+        self.clear()
+        return self
+
+    def get_region(self):
+        return self._region
+
+    def _check_region(self):
+        if self._region is not None or not _is_full(getattr(self, "index", None)):
+            raise NotImplementedError("integration over a sub-region of cells is not provided on the GB300 path")
+
+    def __add__(self, other):
+        if isinstance(other, Integrator):
+            return GroupIntegrator(self, other)
+        return NotImplemented
+
+    __iadd__ = __add__
+
+    def __call__(self, *args, **kwargs):
+        return self.assembly(*args, **kwargs)
+
+    def to_global_dof(self, space, /, indices=None):
+        c2d = space.cell_to_dof()
+        return c2d if indices is None else c2d[indices]
+
+    def __repr__(self):
+        return self.__class__.__name__
+
+
+class _OperatorIntegrator(Integrator):
+    def plan(self, space):
+        raise NotImplementedError
+
+    def assembly(self, space, /, indices=None):
+        """Local matrices (NC, ldof, ldof), FP64 (a convenience; the CSR path
+        never materialises them)."""
+        plan = self.plan(space)
+        if isinstance(plan, ElasticityPlan):
+            raise NotImplementedError("local elasticity matrices are only formed inside the CSR kernel")
+        mesh = space.mesh
+        f = K.cell_factors(mesh, plan.channels, plan.coef_matrix(), torch.float64)
+        tab = torch.as_tensor(plan.tables, dtype=torch.float64, device=mesh.device)
+        out = torch.einsum("ct,tij->cij", f, tab)
+        return out if indices is None else out[indices]
+
+
+class ScalarDiffusionIntegrator(_OperatorIntegrator):
+    """``(coef grad u, grad v)`` on simplex Lagrange spaces."""
+
+    def __init__(self, coef=None, q: Optional[int] = None, *, region=None, batched: bool = False, method=None):
+        super().__init__()
+        if batched:
+            raise NotImplementedError("batched coefficients are not provided")
+        if method not in (None, "fast"):
+            raise NotImplementedError(f"assembly variant {method!r} is not provided on the GB300 path")
+        self.coef = coef
+        self.q = q
+        self.batched = batched
+        self.set_region(region)
+
+    def plan(self, space) -> ScalarPlan:
+        self._check_region()
+        mesh = space.mesh
+        TD = mesh.TD
+        q = space.p + 3 if self.q is None else self.q
+        scale, arr = _cell_coefficient(self.coef, space, q)
+        coefs = [arr] if arr is not None else []
+        ci = 0 if arr is not None else -1
+        ch = [(_lib.FGB_CH_METRIC + k * 3 + l, ci, scale) for k, l in sx.metric_pairs(TD)]
+        return ScalarPlan(ch, coefs, sx.diffusion_tables(TD, space.p, q))
+
+
+class ScalarMassIntegrator(_OperatorIntegrator):
+    """``(coef u, v)`` on simplex Lagrange spaces."""
+
+    def __init__(self, coef=None, q: Optional[int] = None, *, index=_S, batched: bool = False, method=None):
+        super().__init__()
+        if batched:
+            raise NotImplementedError("batched coefficients are not provided")
+        if method is not None:
+            raise NotImplementedError(f"assembly variant {method!r} is not provided on the GB300 path")
+        self.coef = coef
+        self.q = q
+        self.index = index
+
+    def plan(self, space) -> ScalarPlan:
+        self._check_region()
+        mesh = space.mesh
+        q = space.p + 3 if self.q is None else self.q
+        scale, arr = _cell_coefficient(self.coef, space, q)
+        coefs = [arr] if arr is not None else []
+        ch = [(_lib.FGB_CH_MEASURE, 0 if arr is not None else -1, scale)]
+        return ScalarPlan(ch, coefs, sx.mass_table(mesh.TD, space.p, q))
+
+
+class LinearElasticityIntegrator(_OperatorIntegrator):
+    """Linear elasticity on a ``TensorFunctionSpace`` of P1 Lagrange functions,
+    interleaved components (``dof_priority=False``)."""
+
+    def __init__(self, material, q: Optional[int] = None, *, index=_S, method=None):
+        super().__init__()
+        if method not in (None, "assembly"):
+            raise NotImplementedError(f"assembly variant {method!r} is not provided on the GB300 path")
+        self.material = material
+        self.q = q
+        self.index = index
+
+    def plan(self, space) -> ElasticityPlan:
+        self._check_region()
+        if not isinstance(space, TensorFunctionSpace):
+            raise TypeError("LinearElasticityIntegrator needs a TensorFunctionSpace")
+        ss = space.scalar_space
+        mesh = ss.mesh
+        gd = mesh.GD
+        if ss.p != 1:
+            raise NotImplementedError("the GB300 elasticity kernel covers P1 spaces")
+        if space.dof_priority:
+            raise NotImplementedError("the GB300 elasticity kernel covers the interleaved layout (shape=(-1, GD))")
+        q = ss.p + 3 if self.q is None else self.q
+        _, ws = mesh.quadrature_formula(q).get_quadrature_points_and_weights()
+        wsum = float(np.sum(ws))
+        D = torch.as_tensor(self.material.elastic_matrix(), dtype=torch.float64, device=mesh.device)
+        if D.ndim != 4 or D.shape[1] != 1:
+            raise ValueError(f"elastic matrix must be (NC or 1, 1, {2 * gd}, {2 * gd})")
+        if gd == 3:
+            d01, dmu = D[:, 0, 0, 1], D[:, 0, 5, 5]
+            d00 = 2.0 * dmu + d01
+        else:
+            d00, d01, dmu = D[:, 0, 0, 0], D[:, 0, 0, 1], D[:, 0, 2, 2]
+        chans = [(_lib.FGB_CH_GRAD + k * 3 + a, -1, 1.0) for k in range(gd) for a in range(gd)]
+        coefs = []
+        for v in (d00, d01, dmu):
+            if v.numel() == 1:
+                chans.append((_lib.FGB_CH_MEASURE, -1, float(v.item()) * wsum))
+            else:
+                chans.append((_lib.FGB_CH_MEASURE, len(coefs), wsum))
+                coefs.append(v.contiguous())
+        return ElasticityPlan(gd, chans, coefs)
+
+
+class GroupIntegrator(Integrator):
+    """Several integrators sharing one dof map; their local matrices add."""
+
+    def __init__(self, *ints, region=None):
+        super().__init__()
+        self.ints = []
+        if not ints:
+            raise ValueError("No integrators provided.")
+        for it in ints:
+            if isinstance(it, GroupIntegrator):
+                self.ints.extend(it.ints)
+            elif isinstance(it, Integrator):
+                self.ints.append(it)
+            else:
+                raise TypeError(f"Unsupported type {type(it).__name__} found in the inputs.")
+        if region is not None:
+            self.set_region(region)
+
+    def __iter__(self):
+        return iter(self.ints)
+
+    def __len__(self):
+        return len(self.ints)
+
+    def __getitem__(self, i):
+        return self.ints[i]
+
+    def __iadd__(self, other):
+        if isinstance(other, GroupIntegrator):
+            self.ints.extend(other.ints)
+        elif isinstance(other, Integrator):
+            self.ints.append(other)
+        else:
+            return NotImplemented
+        return self
+
+    def set_region(self, region):
+        for it in self.ints:
+            it.set_region(region)
+        return super().set_region(region)
+
+    def to_global_dof(self, space, /, indices=None):
+        return self.ints[0].to_global_dof(space, indices)
+
+    def plan(self, space):
+        plans = [it.plan(space) for it in self.ints]
+        out = plans[0]
+        for p in plans[1:]:
+            if not (isinstance(out, ScalarPlan) and isinstance(p, ScalarPlan)):
+                raise NotImplementedError("only scalar integrators can be grouped")
+            out = out + p
+        return out
+
+    def assembly(self, space, /, indices=None):
+        out = self.ints[0].assembly(space, indices)
+        for it in self.ints[1:]:
+            out = out + it.assembly(space, indices)
+        return out
+
+
+# ---------------------------------------------------------------------------
+# source integrators (right-hand sides)
+# ---------------------------------------------------------------------------
+def _source_values(source, mesh, bcs):
+    """Source values at quadrature points: (NC, NQ) or broadcastable."""
+    if isinstance(source, (int, float)):
+        return float(source)
+    if isinstance(source, torch.Tensor):
+        return source.to(device=mesh.device, dtype=torch.float64)
+    if callable(source):
+        if getattr(source, "coordtype", "barycentric") == "cartesian":
+            return torch.as_tensor(source(mesh.bc_to_point(bcs)), dtype=torch.float64, device=mesh.device)
+        return torch.as_tensor(source(torch.as_tensor(bcs, device=mesh.device), index=_S), dtype=torch.float64,
+                               device=mesh.device)
+    raise TypeError(f"source should be int, float, TensorLike or callable, but got {type(source)}")
+
+
+class ScalarSourceIntegrator(Integrator):
+    """``(f, v)`` (``fealpy/fem/scalar_source_integrator.py:13-90``)."""
+
+    def __init__(self, source=None, q: Optional[int] = None, *, region=None, batched: bool = False, method=None):
+        super().__init__()
+        self.source = source
+        self.q = q
+        self.set_region(region)
+
+    def assembly(self, space, /, indices=None) -> torch.Tensor:
+        self._check_region()
+        mesh = space.mesh
+        q = space.p + 3 if self.q is None else self.q
+        bcs, ws = mesh.quadrature_formula(q).get_quadrature_points_and_weights()
+        cm = mesh.entity_measure("cell")
+        phi = torch.as_tensor(sx.shape_function(bcs, space.p), device=mesh.device)       # (NQ, ldof)
+        w = torch.as_tensor(ws, device=mesh.device)
+        f = _source_values(self.source, mesh, bcs)
+        if isinstance(f, float):
+            return torch.einsum("c,q,qi->ci", cm, w, phi) * f
+        if f.ndim == 1 and f.shape[0] == mesh.number_of_cells():
+            f = f[:, None].expand(-1, len(ws))
+        return torch.einsum("c,q,qi,cq->ci", cm, w, phi, f)
+
+
+class VectorSourceIntegrator(Integrator):
+    """``(f, v)`` for a vector source on a TensorFunctionSpace (interleaved)."""
+
+    def __init__(self, source=None, q: Optional[int] = None, *, region=None, method=None):
+        super().__init__()
+        self.source = source
+        self.q = q
+        self.set_region(region)
+
+    def assembly(self, space, /, indices=None) -> torch.Tensor:
+        self._check_region()
+        ss = space.scalar_space
+        mesh = ss.mesh
+        gd = space.dof_numel
+        q = ss.p + 3 if self.q is None else self.q
+        bcs, ws = mesh.quadrature_formula(q).get_quadrature_points_and_weights()
+        cm = mesh.entity_measure("cell")
+        phi = torch.as_tensor(sx.shape_function(bcs, ss.p), device=mesh.device)
+        w = torch.as_tensor(ws, device=mesh.device)
+        f = self.source
+        if callable(f):
+            f = _source_values(f, mesh, bcs)                      # (NC, NQ, gd)
+        else:
+            f = torch.as_tensor(f, dtype=torch.float64, device=mesh.device).reshape(1, 1, gd)
+            f = f.expand(mesh.number_of_cells(), len(ws), gd)
+        loc = torch.einsum("c,q,qi,cqd->cid", cm, w, phi, f)       # (NC, ldof, gd)
+        if space.dof_priority:
+            loc = loc.transpose(1, 2)
+        return loc.reshape(loc.shape[0], -1)

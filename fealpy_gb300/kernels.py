@@ -1,0 +1,220 @@
+"""Host wrappers of the assembly, boundary-condition and solver entry points.
+
+Each function takes and returns torch CUDA tensors, allocates outputs and
+workspaces through torch's caching allocator, launches on the current stream
+and maps a non-zero status to an exception.  Nothing here computes on the CPU.
+"""
+import ctypes
+from typing import List, Optional, Sequence, Tuple
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import call, ptr, stream_ptr, workspace, status_word, check_status_word, dtype_code
+
+__all__ = ["cell_factors", "build_adjacency", "build_pattern", "assemble_scalar", "assemble_elasticity_p1",
+           "expand_blocks", "dirichlet_apply", "csr_spmv", "csr_diagonal", "pcg_f64", "pcg_mixed", "gather_sum"]
+
+
+def _dev(mesh_or_tensor):
+    d = mesh_or_tensor.device
+    if d.type != "cuda":
+        raise ValueError("the assembly path needs the mesh on a CUDA device")
+    return d
+
+
+def cell_factors(mesh, channels: Sequence[Tuple[int, int, float]], coef: Optional[torch.Tensor],
+                 out_dtype=torch.float64, status: Optional[torch.Tensor] = None) -> torch.Tensor:
+    """(NC, nch) factor channels, see ``fgb_cell_factors``.  ``channels`` is a
+    list of ``(kind, coef_row or -1, scale)``; ``coef`` is (n_coef, NC) float64."""
+    dev = _dev(mesh.node)
+    NC = mesh.number_of_cells()
+    nch = len(channels)
+    if nch == 0 or nch > _lib.FGB_MAX_CHANNELS:
+        raise ValueError(f"between 1 and {_lib.FGB_MAX_CHANNELS} factor channels are supported, got {nch}")
+    out = torch.empty((NC, nch), dtype=out_dtype, device=dev)
+    if NC == 0:
+        return out
+    kinds = (ctypes.c_int32 * nch)(*[int(c[0]) for c in channels])
+    coefs = (ctypes.c_int32 * nch)(*[int(c[1]) for c in channels])
+    scales = (ctypes.c_double * nch)(*[float(c[2]) for c in channels])
+    if coef is not None:
+        coef = coef.to(device=dev, dtype=torch.float64).contiguous()
+    own = status is None
+    st = status_word(dev) if own else status
+    call("fgb_cell_factors", mesh.TD, NC, ptr(mesh.node), ptr(mesh.cell), nch, kinds, coefs, scales, ptr(coef),
+         dtype_code(out_dtype), ptr(out), ptr(st), stream_ptr(dev))
+    if own:
+        check_status_word("fgb_cell_factors", st)
+    return out
+
+
+def build_adjacency(c2d: torch.Tensor, n_dof: int, status: torch.Tensor):
+    """dof -> sorted (cell*ldof + local) adjacency."""
+    dev = _dev(c2d)
+    c2d = c2d.contiguous()
+    NC, ldof = c2d.shape
+    adj_ptr = torch.empty(n_dof + 1, dtype=torch.int64, device=dev)
+    adj = torch.empty(max(NC * ldof, 1), dtype=torch.int32, device=dev)
+    max_deg = torch.zeros(1, dtype=torch.int32, device=dev)
+    lib = _lib.lib()
+    ws = workspace(lib.fgb_adjacency_workspace_bytes(n_dof), dev)
+    call("fgb_adjacency_build", NC, ldof, ptr(c2d), n_dof, ptr(adj_ptr), ptr(adj), ptr(max_deg), ptr(status),
+         ptr(ws), ws.numel(), stream_ptr(dev))
+    return adj_ptr, adj, max_deg
+
+
+def build_pattern(adj_ptr, adj, c2d, n_dof: int, status: torch.Tensor):
+    """Canonical CSR pattern (indptr int64, indices int32).  One host sync (nnz)."""
+    dev = _dev(c2d)
+    ldof = c2d.shape[1]
+    lib = _lib.lib()
+    ws = workspace(lib.fgb_pattern_workspace_bytes(n_dof), dev)
+    indptr = torch.empty(n_dof + 1, dtype=torch.int64, device=dev)
+    call("fgb_pattern_count", n_dof, ptr(adj_ptr), ptr(adj), ptr(c2d), ldof, ptr(indptr), ptr(status), ptr(ws),
+         ws.numel(), stream_ptr(dev))
+    nnz = int(indptr[n_dof].item())
+    check_status_word("fgb_pattern_count", status)
+    indices = torch.empty(max(nnz, 1), dtype=torch.int32, device=dev)
+    call("fgb_pattern_fill", n_dof, ptr(adj_ptr), ptr(adj), ptr(c2d), ldof, ptr(indptr), ptr(indices), ptr(status),
+         ptr(ws), ws.numel(), stream_ptr(dev))
+    return indptr, indices[:nnz]
+
+
+def expand_blocks(n_node: int, bs: int, dof_priority: bool, indptr, indices):
+    dev = _dev(indptr)
+    nnz_s = indices.numel()
+    out_ptr = torch.empty(n_node * bs + 1, dtype=torch.int64, device=dev)
+    out_idx = torch.empty(max(nnz_s * bs * bs, 1), dtype=torch.int32, device=dev)
+    call("fgb_pattern_expand_blocks", n_node, bs, int(bool(dof_priority)), ptr(indptr), ptr(indices), ptr(out_ptr),
+         ptr(out_idx), stream_ptr(dev))
+    return out_ptr, out_idx[: nnz_s * bs * bs]
+
+
+def assemble_scalar(adj_ptr, adj, c2d, tables: torch.Tensor, factors: torch.Tensor, indptr, indices,
+                    values_f32: bool = False, status: Optional[torch.Tensor] = None):
+    dev = _dev(c2d)
+    n_dof = adj_ptr.numel() - 1
+    ldof = c2d.shape[1]
+    dtype = factors.dtype
+    nt = tables.shape[0]
+    if tables.shape[1:] != (ldof, ldof) or factors.shape[1] != nt:
+        raise ValueError("table/factor shapes do not match")
+    values = torch.empty(indices.numel(), dtype=dtype, device=dev)
+    v32 = torch.empty(indices.numel(), dtype=torch.float32, device=dev) if values_f32 else None
+    lib = _lib.lib()
+    ws = workspace(lib.fgb_assemble_workspace_bytes(n_dof), dev)
+    own = status is None
+    st = status_word(dev) if own else status
+    call("fgb_assemble_scalar", dtype_code(dtype), n_dof, ptr(adj_ptr), ptr(adj), ptr(c2d), ldof, nt,
+         ptr(tables.to(dev, dtype).contiguous()), ptr(factors.contiguous()), ptr(indptr), ptr(indices), ptr(values),
+         ptr(v32), ptr(st), ptr(ws), ws.numel(), stream_ptr(dev))
+    if own:
+        check_status_word("fgb_assemble_scalar", st)
+    return values, v32
+
+
+def assemble_elasticity_p1(gd, adj_ptr, adj, cell, factors, node_indptr, node_indices, indptr, nnz,
+                           values_f32: bool = False, status: Optional[torch.Tensor] = None):
+    dev = _dev(cell)
+    n_node = adj_ptr.numel() - 1
+    dtype = factors.dtype
+    values = torch.empty(nnz, dtype=dtype, device=dev)
+    v32 = torch.empty(nnz, dtype=torch.float32, device=dev) if values_f32 else None
+    lib = _lib.lib()
+    ws = workspace(lib.fgb_assemble_workspace_bytes(n_node), dev)
+    own = status is None
+    st = status_word(dev) if own else status
+    call("fgb_assemble_elasticity_p1", dtype_code(dtype), gd, n_node, ptr(adj_ptr), ptr(adj), ptr(cell),
+         ptr(factors.contiguous()), ptr(node_indptr), ptr(node_indices), ptr(indptr), ptr(values), ptr(v32), ptr(st),
+         ptr(ws), ws.numel(), stream_ptr(dev))
+    if own:
+        check_status_word("fgb_assemble_elasticity_p1", st)
+    return values, v32
+
+
+def dirichlet_apply(indptr, indices, values, is_bd: torch.Tensor, f: Optional[torch.Tensor],
+                    uh: Optional[torch.Tensor], matrix: bool = True):
+    """Returns (new_indptr, new_indices, new_values, f_new); entries not asked for are None."""
+    dev = _dev(indptr)
+    n = indptr.numel() - 1
+    dt = values.dtype
+    isb = is_bd.to(device=dev, dtype=torch.uint8).contiguous()
+    row_nnz = torch.empty(n, dtype=torch.int32, device=dev)
+    f_out = None
+    if f is not None:
+        f_out = torch.empty(n, dtype=dt, device=dev)
+        f = f.to(dev, dt).contiguous()
+        uh = uh.to(dev, dt).contiguous()
+    call("fgb_dirichlet_count", dtype_code(dt), n, ptr(indptr), ptr(indices), ptr(values), ptr(isb), ptr(f), ptr(uh),
+         ptr(f_out), ptr(row_nnz), stream_ptr(dev))
+    if not matrix:
+        return None, None, None, f_out
+    lib = _lib.lib()
+    ws = workspace(lib.fgb_scan_workspace_bytes(n), dev)
+    new_ptr = torch.empty(n + 1, dtype=torch.int64, device=dev)
+    call("fgb_exclusive_scan_i32", ptr(row_nnz), n, ptr(new_ptr), ptr(ws), ws.numel(), stream_ptr(dev))
+    nnz = int(new_ptr[n].item())
+    new_idx = torch.empty(max(nnz, 1), dtype=torch.int32, device=dev)
+    new_val = torch.empty(max(nnz, 1), dtype=dt, device=dev)
+    call("fgb_dirichlet_fill", dtype_code(dt), n, ptr(indptr), ptr(indices), ptr(values), ptr(isb), ptr(new_ptr),
+         ptr(new_idx), ptr(new_val), stream_ptr(dev))
+    return new_ptr, new_idx[:nnz], new_val[:nnz], f_out
+
+
+def csr_spmv(indptr, indices, values, x, lanes: int = 0, out: Optional[torch.Tensor] = None):
+    dev = _dev(indptr)
+    n = indptr.numel() - 1
+    x = x.to(dev, values.dtype).contiguous()
+    y = out if out is not None else torch.empty(n, dtype=values.dtype, device=dev)
+    call("fgb_csr_spmv", dtype_code(values.dtype), n, ptr(indptr), ptr(indices), ptr(values), ptr(x), ptr(y), lanes,
+         stream_ptr(dev))
+    return y
+
+
+def csr_diagonal(indptr, indices, values):
+    dev = _dev(indptr)
+    n = indptr.numel() - 1
+    d = torch.empty(n, dtype=values.dtype, device=dev)
+    dinv = torch.empty(n, dtype=values.dtype, device=dev)
+    call("fgb_csr_diagonal", dtype_code(values.dtype), n, ptr(indptr), ptr(indices), ptr(values), ptr(d), ptr(dinv),
+         stream_ptr(dev))
+    return d, dinv
+
+
+def pcg_f64(indptr, indices, values, dinv, b, x, atol, rtol, maxit, check_every=16, lanes=0, norm=0, profile=False):
+    dev = _dev(indptr)
+    n = indptr.numel() - 1
+    lib = _lib.lib()
+    ws = workspace(lib.fgb_pcg_workspace_bytes(n), dev)
+    info = _lib.PcgInfo()
+    call("fgb_pcg_f64", n, ptr(indptr), ptr(indices), ptr(values), ptr(dinv), ptr(b), ptr(x), float(atol),
+         float(rtol), int(maxit), int(check_every), int(lanes), int(norm), int(bool(profile)), ptr(ws), ws.numel(),
+         ctypes.byref(info), stream_ptr(dev))
+    _lib.add_launches(info.launches)
+    return info
+
+
+def pcg_mixed(indptr, indices, values64, values32, dinv64, b, x, rtol, delta=0.1, maxit=100000, check_every=32,
+              lanes=0, profile=False):
+    dev = _dev(indptr)
+    n = indptr.numel() - 1
+    lib = _lib.lib()
+    ws = workspace(lib.fgb_pcg_mixed_workspace_bytes(n), dev)
+    info = _lib.PcgInfo()
+    call("fgb_pcg_mixed", n, ptr(indptr), ptr(indices), ptr(values64), ptr(values32), ptr(dinv64), ptr(b), ptr(x),
+         float(rtol), float(delta), int(maxit), int(check_every), int(lanes), int(bool(profile)), ptr(ws),
+         ws.numel(), ctypes.byref(info), stream_ptr(dev))
+    _lib.add_launches(info.launches)
+    return info
+
+
+def gather_sum(adj_ptr, adj, local: torch.Tensor, out: Optional[torch.Tensor] = None):
+    """out[i] = sum of local.flat[adj[k]] over i's adjacency (deterministic)."""
+    dev = _dev(adj_ptr)
+    n = adj_ptr.numel() - 1
+    local = local.contiguous()
+    y = out if out is not None else torch.empty(n, dtype=local.dtype, device=dev)
+    call("fgb_gather_sum", dtype_code(local.dtype), n, ptr(adj_ptr), ptr(adj), ptr(local), ptr(y), stream_ptr(dev))
+    return y

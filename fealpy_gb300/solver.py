@@ -1,0 +1,104 @@
+"""Jacobi-preconditioned CG with FEALPy's interface (``fealpy/solver/cg.py:14-123``)
+and its FP32-refined variant.
+
+``cg`` keeps the reference iteration exactly (same recurrences, same stopping
+rule on ``sqrt(r.z)``, ``info = {'residual', 'niter'}``) but runs it as two
+fused GPU kernels per iteration with all scalars on the device.
+``cg_mixed`` runs the iterations in FP32 and restores FP64 accuracy with
+reliable updates (FP64 residual recomputation) until the true relative
+residual ``||b - A x|| / ||b||`` reaches ``rtol``.
+"""
+import logging
+from typing import Optional
+
+import torch
+
+from .sparse import CSRTensor
+from . import kernels as K
+
+__all__ = ["cg", "cg_mixed", "JacobiPreconditioner"]
+
+logger = logging.getLogger("fealpy_gb300")
+
+
+class JacobiPreconditioner:
+    """``M = diag(A)^-1`` as a diagonal CSRTensor
+    (``fealpy/solver/iterative_solver_manger.py:273-280``)."""
+
+    def apply(self, A: CSRTensor) -> CSRTensor:
+        d = A.diags()
+        M = CSRTensor(d.crow, d.col, 1.0 / d.values, A.shape)
+        return M
+
+
+def _diag_inv_of(M):
+    if M is None:
+        return None
+    if isinstance(M, CSRTensor) and M.is_diagonal():
+        return M.values.contiguous()
+    raise NotImplementedError("cg on the GB300 path takes M=None or a diagonal CSRTensor (Jacobi)")
+
+
+def _info_dict(info, extra=None):
+    out = {"residual": info.residual, "niter": int(info.niter), "reason": int(info.reason),
+           "launches": int(info.launches), "kernel_ms": float(info.kernel_ms),
+           "kernel_launches": int(info.kernel_launches)}
+    if extra:
+        out.update(extra)
+    return out
+
+
+def cg(A, b: torch.Tensor, x0: Optional[torch.Tensor] = None, M=None, *, batch_first: bool = False,
+       atol: float = 1e-12, rtol: float = 1e-8, maxit: Optional[int] = 10000, returninfo: bool = False,
+       check_every: int = 16, lanes_per_row: int = 0, stop: str = "preconditioned", profile: bool = False):
+    """Solve ``A x = b`` by (preconditioned) CG; see module docstring.
+
+    ``stop='preconditioned'`` (default) is FEALPy's test on ``sqrt(r.z)``;
+    ``stop='residual'`` tests the 2-norm of the iterated residual instead.
+    ``profile`` records CUDA-event times of the SpMV kernel into the info."""
+    if not isinstance(b, torch.Tensor):
+        raise AssertionError("b must be a Tensor")
+    if b.ndim not in (1, 2):
+        raise ValueError("b must be a 1D or 2D dense tensor")
+    if x0 is not None and x0.shape != b.shape:
+        raise ValueError("x0 and b must have the same shape")
+    if not isinstance(A, CSRTensor):
+        raise NotImplementedError("cg on the GB300 path takes a CSRTensor matrix")
+    if b.ndim == 2:
+        raise NotImplementedError("multi-right-hand-side cg is not provided on the GB300 path")
+    dinv = _diag_inv_of(M)
+    b = b.to(dtype=torch.float64).contiguous()
+    x = torch.zeros_like(b) if x0 is None else x0.to(torch.float64).clone()
+    if stop not in ("preconditioned", "residual"):
+        raise ValueError("stop must be 'preconditioned' or 'residual'")
+    info = K.pcg_f64(A.crow, A.col, A.values.to(torch.float64), dinv, b, x, atol, rtol,
+                     maxit if maxit is not None else 2 ** 62, check_every, lanes_per_row,
+                     0 if stop == "preconditioned" else 1, profile)
+    out = _info_dict(info)
+    reason = info.reason
+    if reason == 3:
+        logger.info(f"CG: failed, stopped by maxit ({maxit}).")
+    if returninfo:
+        return x, out
+    return x
+
+
+def cg_mixed(A: CSRTensor, b: torch.Tensor, x0: Optional[torch.Tensor] = None, M=None, *, rtol: float = 1e-10,
+             delta: float = 0.1, maxit: int = 100000, returninfo: bool = False, check_every: int = 32,
+             lanes_per_row: int = 0, profile: bool = False):
+    """FP32 Jacobi-PCG iterations with FP64 reliable updates; stops on the true
+    FP64 relative residual.  ``M`` must be None (Jacobi from ``A`` is used) or
+    the diagonal CSR of ``JacobiPreconditioner``."""
+    if not isinstance(A, CSRTensor):
+        raise NotImplementedError("cg_mixed takes a CSRTensor matrix")
+    dinv = _diag_inv_of(M)
+    if dinv is None:
+        dinv = A.diagonal_inverse()
+    b = b.to(dtype=torch.float64).contiguous()
+    x = torch.zeros_like(b) if x0 is None else x0.to(torch.float64).clone()
+    info = K.pcg_mixed(A.crow, A.col, A.values, A.values_f32(), dinv, b, x, rtol, delta, maxit, check_every,
+                       lanes_per_row, profile)
+    out = _info_dict(info, {"relres": info.true_relres, "n_updates": int(info.n_updates)})
+    if returninfo:
+        return x, out
+    return x

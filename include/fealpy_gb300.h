@@ -1,0 +1,240 @@
+/*
+ * fealpy_gb300.h -- C ABI of the GB300 (sm_103a) kernels behind the FEALPy
+ * Lagrange assemble + Dirichlet + Jacobi-PCG path.
+ *
+ * Every entry point:
+ *   - takes device pointers (unless the name ends in _host), plain sizes and a
+ *     cudaStream_t passed as `void* stream`, and is stream-ordered;
+ *   - returns an int status (FGB_OK == 0); conditions found on the device are
+ *     written into the caller's `int32_t* status` device word (max of codes);
+ *   - never allocates device memory: scratch comes from a caller workspace
+ *     sized by the matching *_workspace_bytes() query, and the library never
+ *     frees caller memory;
+ *   - never traps or aborts; it keeps no global mutable state.
+ *
+ * Index conventions follow FEALPy: cell-to-dof maps are int32 (NC, ldof)
+ * row-major, CSR row pointers are int64 (FEALPy's `crow` dtype after
+ * bincount+cumsum, fealpy/sparse/coo_tensor.py:144-146), CSR column indices
+ * are int32.  Every CSR produced here is canonical: rows ascending, columns
+ * strictly ascending, duplicates summed.
+ */
+#ifndef FEALPY_GB300_H
+#define FEALPY_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum fgb_status_code {
+  FGB_OK = 0,
+  FGB_ERR_ARG = 1,        /* bad argument (sizes, null pointers, dtype)      */
+  FGB_ERR_WORKSPACE = 2,  /* workspace missing or smaller than queried       */
+  FGB_ERR_INDEX = 3,      /* an index read on the device was out of range    */
+  FGB_ERR_PATTERN = 4,    /* a contribution's column is missing from the CSR */
+  FGB_ERR_NONFINITE = 5,  /* NaN/Inf met (degenerate cell, NaN coefficient)  */
+  FGB_ERR_BREAKDOWN = 6,  /* CG breakdown: p.Ap <= 0 (matrix not SPD)        */
+  FGB_ERR_CUDA = 7,       /* a CUDA launch or copy failed                    */
+  FGB_ERR_CAPACITY = 8    /* a size exceeds a documented fixed limit         */
+};
+
+enum fgb_dtype { FGB_F32 = 0, FGB_F64 = 1 };
+
+/* Stop reasons reported by the PCG solvers (fgb_pcg_info.reason). */
+enum fgb_pcg_reason {
+  FGB_PCG_RUNNING = 0,
+  FGB_PCG_ATOL = 1,     /* sqrt(r.z) < atol                                  */
+  FGB_PCG_RTOL = 2,     /* sqrt(r.z) < rtol*||b|| (or true residual, mixed)  */
+  FGB_PCG_MAXIT = 3,    /* iteration limit reached                           */
+  FGB_PCG_ZERO_RHS = 4, /* ||b|| < 1e-15: x = 0 returned                     */
+  FGB_PCG_BREAKDOWN = 5,
+  FGB_PCG_NONFINITE = 6
+};
+
+typedef struct fgb_pcg_info {
+  int64_t niter;      /* CG iterations performed                            */
+  double residual;    /* sqrt(r.z) at exit (FEALPy's `info['residual']`)    */
+  double b_norm;      /* ||b||_2                                            */
+  double true_relres; /* ||b - A x||_2/||b||_2 in FP64 (mixed solver), else -1 */
+  int32_t reason;     /* enum fgb_pcg_reason                                */
+  int32_t n_updates;  /* mixed solver: FP64 residual replacements performed */
+  int64_t launches;   /* kernels launched by the call                       */
+  double kernel_ms;   /* profile != 0: summed CUDA-event time of the SpMV   */
+                      /* kernel of the iterations that did work             */
+  int64_t kernel_launches; /* number of SpMV launches summed in kernel_ms   */
+} fgb_pcg_info;
+
+/* Cell-factor channel kinds for fgb_cell_factors (k, l, a in 0..TD-1):
+ *   FGB_CH_MEASURE            signed cell measure |T| (simplex_measure)
+ *   FGB_CH_METRIC + k*3 + l   |T| * grad(lambda_{k+1}) . grad(lambda_{l+1})
+ *   FGB_CH_GRAD   + k*3 + a   d lambda_{k+1} / d x_a                      */
+enum fgb_channel { FGB_CH_MEASURE = 0, FGB_CH_METRIC = 1, FGB_CH_GRAD = 16 };
+#define FGB_MAX_CHANNELS 16
+
+const char* fgb_status_string(int32_t status);
+int32_t fgb_abi_version(void);
+
+/* Exclusive scan of n int32 counts into n+1 int64 offsets (out[0] = 0).
+ * Building block of COOTensor.tocsr's bincount+cumsum
+ * (fealpy/sparse/coo_tensor.py:144-146). */
+size_t fgb_scan_workspace_bytes(int64_t n);
+int32_t fgb_exclusive_scan_i32(const int32_t* in, int64_t n, int64_t* out, void* workspace,
+                               size_t workspace_bytes, void* stream);
+
+/* ---- symbolic assembly ------------------------------------------------- */
+
+/* dof -> (cell, local index) adjacency, sorted by cell then local index:
+ * adj_ptr (n_dof+1, int64), adj (n_cell*ldof, int32, packed cell*ldof+li).
+ * This is the grouping that FEALPy's stable lexsort in COOTensor.coalesce
+ * (fealpy/sparse/coo_tensor.py:184-200) imposes on the COO triplets built by
+ * BilinearForm._scalar_assembly (fealpy/fem/bilinear_form.py:46-75).
+ * Also writes the maximum adjacency length to max_degree (device int32). */
+size_t fgb_adjacency_workspace_bytes(int64_t n_dof);
+int32_t fgb_adjacency_build(int64_t n_cell, int32_t ldof, const int32_t* cell2dof, int64_t n_dof,
+                            int64_t* adj_ptr, int32_t* adj, int32_t* max_degree, int32_t* status,
+                            void* workspace, size_t workspace_bytes, void* stream);
+
+/* Canonical CSR pattern of sum_c P_c^T K_c P_c: row i holds the sorted union
+ * of the dofs of the cells around dof i.  Replaces the index half of
+ * COOTensor.coalesce + tocsr (fealpy/sparse/coo_tensor.py:137-157,184-213).
+ * count: writes indptr (n_dof+1) via an internal scan; fill: writes indices. */
+size_t fgb_pattern_workspace_bytes(int64_t n_dof);
+int32_t fgb_pattern_count(int64_t n_dof, const int64_t* adj_ptr, const int32_t* adj,
+                          const int32_t* cell2dof, int32_t ldof, int64_t* indptr, int32_t* status,
+                          void* workspace, size_t workspace_bytes, void* stream);
+int32_t fgb_pattern_fill(int64_t n_dof, const int64_t* adj_ptr, const int32_t* adj,
+                         const int32_t* cell2dof, int32_t ldof, const int64_t* indptr,
+                         int32_t* indices, int32_t* status, void* workspace,
+                         size_t workspace_bytes, void* stream);
+
+/* Block expansion of a scalar pattern for vector spaces: bs components per
+ * node; interleaved (3*node+comp, TensorFunctionSpace(space,(-1,GD)),
+ * fealpy/functionspace/tensor_space.py:29-31) when dof_priority == 0, else
+ * component-major (comp*n_node+node).  out_indptr has bs*n_node+1 entries. */
+int32_t fgb_pattern_expand_blocks(int64_t n_node, int32_t bs, int32_t dof_priority,
+                                  const int64_t* indptr, const int32_t* indices,
+                                  int64_t* out_indptr, int32_t* out_indices, void* stream);
+
+/* ---- numeric assembly -------------------------------------------------- */
+
+/* Per-cell geometric factors (affine simplex, TD = 2 or 3, GD = TD): the
+ * signed measure and Jacobian-inverse metric that FEALPy's simplex_measure,
+ * triangle/tetrahedron_grad_lambda compute (fealpy/backend/numpy_backend.py:
+ * 414-421, 587-598, 620-629), evaluated in FP64 and written as n_channel
+ * columns of factors (n_cell, n_channel) in out_dtype.  Channel j is
+ *   value(kind_j) * scale_j * (coef_index_j >= 0 ? coef[coef_index_j*n_cell + c] : 1).
+ * chan_*_host are host arrays of n_channel <= FGB_MAX_CHANNELS entries. */
+int32_t fgb_cell_factors(int32_t td, int64_t n_cell, const double* node, const int32_t* cell,
+                         int32_t n_channel, const int32_t* chan_kind_host,
+                         const int32_t* chan_coef_host, const double* chan_scale_host,
+                         const double* coef, int32_t out_dtype, void* factors, int32_t* status,
+                         void* stream);
+
+/* Scalar Lagrange assembly straight into CSR values (no local-matrix
+ * materialisation, no atomics): K_c[i][j] = sum_t factors[c][t]*tables[t][i][j],
+ * which equals FEALPy's bilinear_integral einsum over quadrature points for
+ * ScalarDiffusionIntegrator / ScalarMassIntegrator / their GroupIntegrator
+ * (fealpy/functional.py:68-106, fealpy/fem/scalar_diffusion_integrator.py:54-63,
+ * fealpy/fem/scalar_mass_integrator.py:47-54, fealpy/fem/integrator.py:361-378)
+ * when coefficients are constant per cell.  Contributions to each CSR entry
+ * are summed in (cell, local index) order.  values_f32 (optional) receives a
+ * float copy.  dtype selects double or float tables/factors/values.
+ * ldof <= 32; tables (n_table, ldof, ldof). */
+size_t fgb_assemble_workspace_bytes(int64_t n_rows);
+int32_t fgb_assemble_scalar(int32_t dtype, int64_t n_dof, const int64_t* adj_ptr,
+                            const int32_t* adj, const int32_t* cell2dof, int32_t ldof,
+                            int32_t n_table, const void* tables, const void* factors,
+                            const int64_t* indptr, const int32_t* indices, void* values,
+                            float* values_f32, int32_t* status, void* workspace,
+                            size_t workspace_bytes, void* stream);
+
+/* P1 linear elasticity, interleaved vector dofs (LinearElasticityIntegrator
+ * default variant, fealpy/fem/linear_elasticity_integrator.py:60-181, the
+ * dof_priority=False branch).  adj/adj_ptr is the node->(cell, vertex)
+ * adjacency, node_indptr/node_indices the scalar node pattern, indptr/indices
+ * the expanded vector pattern (fgb_pattern_expand_blocks, dof_priority 0).
+ * factors (n_cell, gd*gd + 3): grad(lambda_{1..gd}) components, then
+ * |T|*D00, |T|*D_lambda, |T|*D_mu with D00 = 2*D55+D01 (3-D) or D[0,0]
+ * (2-D), D_lambda = D01, D_mu = D55 (3-D) or D22 (2-D). */
+int32_t fgb_assemble_elasticity_p1(int32_t dtype, int32_t gd, int64_t n_node,
+                                   const int64_t* adj_ptr, const int32_t* adj,
+                                   const int32_t* cell, const void* factors,
+                                   const int64_t* node_indptr, const int32_t* node_indices,
+                                   const int64_t* indptr, void* values, float* values_f32,
+                                   int32_t* status, void* workspace, size_t workspace_bytes,
+                                   void* stream);
+
+/* Cell vectors to a global vector: out[i] = sum over the adjacency of dof i
+ * (cell order) of local[cell*ldof + li].  Replaces the index_add scatter of
+ * LinearForm._scalar_assembly (fealpy/fem/linear_form.py:36-86). */
+int32_t fgb_gather_sum(int32_t dtype, int64_t n, const int64_t* adj_ptr, const int32_t* adj,
+                       const void* local, void* out, void* stream);
+
+/* ---- Dirichlet boundary conditions ------------------------------------- */
+
+/* DirichletBC.apply (fealpy/fem/dirichlet_bc.py:101-229): given is_bd (uint8,
+ * n), the boundary values u_bd (n, zero off the boundary) and f:
+ *   count: f_out = f - A u_bd off the boundary, f_out[bd] = u_bd[bd];
+ *          row_nnz (n, int32) = kept entries per row (1 on boundary rows);
+ *   fill:  new_indices/new_values of the eliminated matrix (boundary rows and
+ *          columns removed, unit diagonal on boundary rows), in canonical order
+ *          given new_indptr = exclusive scan of row_nnz. */
+int32_t fgb_dirichlet_count(int32_t dtype, int64_t n, const int64_t* indptr, const int32_t* indices,
+                            const void* values, const uint8_t* is_bd, const void* f,
+                            const void* u_bd, void* f_out, int32_t* row_nnz, void* stream);
+int32_t fgb_dirichlet_fill(int32_t dtype, int64_t n, const int64_t* indptr, const int32_t* indices,
+                           const void* values, const uint8_t* is_bd, const int64_t* new_indptr,
+                           int32_t* new_indices, void* new_values, void* stream);
+
+/* ---- sparse kernels and solvers ----------------------------------------- */
+
+/* y = A x for a CSR matrix (CSRTensor.matmul -> bm.csr_spmm,
+ * fealpy/sparse/csr_tensor.py:411-452, fealpy/backend/numpy_backend.py:181-199).
+ * lanes_per_row in {0 (auto), 1, 2, 4, 8, 16, 32}. */
+int32_t fgb_csr_spmv(int32_t dtype, int64_t n_row, const int64_t* indptr, const int32_t* indices,
+                     const void* values, const void* x, void* y, int32_t lanes_per_row,
+                     void* stream);
+
+/* diag(A) and 1/diag(A) (CSRTensor.diags + JacobiPreconditioner.apply,
+ * fealpy/sparse/csr_tensor.py:467-475, fealpy/solver/iterative_solver_manger.py:
+ * 273-280).  A missing diagonal yields 0 and 1/0 = inf, as in FEALPy. */
+int32_t fgb_csr_diagonal(int32_t dtype, int64_t n, const int64_t* indptr, const int32_t* indices,
+                         const void* values, void* diag, void* diag_inv, void* stream);
+
+/* Jacobi-preconditioned CG in FP64 with FEALPy's iteration and stopping rule
+ * (fealpy/solver/cg.py:76-123): stop when sqrt(r.z) < atol or
+ * < rtol*||b||_2 or after maxit iterations.  diag_inv == NULL means no
+ * preconditioner.  x holds x0 on entry and the solution on exit.  Blocking:
+ * the host polls a device flag every check_every iterations.  norm == 0
+ * monitors FEALPy's sqrt(r.z); norm == 1 monitors the 2-norm of the iterated
+ * residual instead.  lanes_per_row as in fgb_csr_spmv (0 = auto, >= 2).
+ * profile != 0 brackets every SpMV launch with CUDA events (kernel_ms). */
+size_t fgb_pcg_workspace_bytes(int64_t n);
+int32_t fgb_pcg_f64(int64_t n, const int64_t* indptr, const int32_t* indices, const double* values,
+                    const double* diag_inv, const double* b, double* x, double atol, double rtol,
+                    int64_t maxit, int32_t check_every, int32_t lanes_per_row, int32_t norm,
+                    int32_t profile, void* workspace, size_t workspace_bytes,
+                    fgb_pcg_info* info_host, void* stream);
+
+/* Mixed precision: Jacobi-PCG iterations in FP32 on values32 (FP32 SpMV,
+ * dots and updates) with FP64 reliable updates: whenever the FP32 residual
+ * has dropped by `delta` since the last update (or looks converged), the
+ * FP32 correction is added to the FP64 iterate and the residual is recomputed
+ * as b - A x with values64 in FP64.  Stops when that true residual satisfies
+ * ||b - A x||_2 <= rtol*||b||_2.  No FEALPy counterpart: this is the
+ * FP32-refined variant of fealpy/solver/cg.py. */
+size_t fgb_pcg_mixed_workspace_bytes(int64_t n);
+int32_t fgb_pcg_mixed(int64_t n, const int64_t* indptr, const int32_t* indices,
+                      const double* values64, const float* values32, const double* diag_inv64,
+                      const double* b, double* x, double rtol, double delta, int64_t maxit,
+                      int32_t check_every, int32_t lanes_per_row, int32_t profile,
+                      void* workspace, size_t workspace_bytes, fgb_pcg_info* info_host,
+                      void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FEALPY_GB300_H */

@@ -1,0 +1,209 @@
+"""Generate the golden fixtures of ``tests/golden/*.npz`` by running the reference
+FEALPy (numpy backend, unmodified) through its public API.
+
+Run in an environment where the reference checkout is importable:
+
+    python tests/golden/make_golden.py /path/to/fealpy-checkout
+
+The fixtures hold only inputs and outputs of the reference (meshes, dof maps,
+local matrices, CSR matrices, vectors, iteration counts, quadrature tables and
+the reference's own known-answer data), never its source.  Every random input
+is seeded here and stored in the fixture, so tests read it back instead of
+regenerating it.
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def canonical(crow, col, val):
+    """Sort the columns inside each row (the reference's tocsr may leave them in
+    unstable-argsort order); returns (crow, col, val) in canonical order."""
+    crow = np.asarray(crow, dtype=np.int64)
+    col = np.asarray(col)
+    val = np.asarray(val)
+    row = np.repeat(np.arange(len(crow) - 1), np.diff(crow))
+    order = np.lexsort((col, row))
+    return crow, col[order].astype(np.int32), val[order]
+
+
+def jitter(node, is_bd, h, amp, rng):
+    out = node.copy()
+    d = rng.uniform(-amp * h, amp * h, size=node.shape)
+    out[~is_bd] += d[~is_bd]
+    return out
+
+
+def main(ref_root):
+    sys.path.insert(0, HERE)
+    import refshim
+    refshim.install(ref_root)
+    from fealpy.backend import backend_manager as bm
+    bm.set_backend("numpy")
+    from fealpy.mesh import TriangleMesh, TetrahedronMesh
+    from fealpy.functionspace import LagrangeFESpace, TensorFunctionSpace
+    from fealpy.fem import (BilinearForm, LinearForm, ScalarDiffusionIntegrator, ScalarMassIntegrator,
+                            LinearElasticityIntegrator, ScalarSourceIntegrator, VectorSourceIntegrator, DirichletBC)
+    from fealpy.solver import cg
+    from fealpy.material import LinearElasticMaterial
+    from fealpy.sparse import CSRTensor
+    from fealpy.quadrature import TriangleQuadrature, TetrahedronQuadrature
+    from fealpy.decorator import cartesian
+
+    def jacobi(A):
+        d = A.diags()
+        return CSRTensor(d.crow, d.col, 1.0 / d.values, A.shape)
+
+    # ------------------------------------------------------------------ C1
+    mesh = TriangleMesh.from_box([0, 1, 0, 1], 64, 64)
+    space = LagrangeFESpace(mesh, p=1)
+
+    @cartesian
+    def solution(p):
+        return np.sin(np.pi * p[..., 0]) * np.sin(np.pi * p[..., 1])
+
+    @cartesian
+    def source(p):
+        return 2 * np.pi ** 2 * solution(p)
+
+    bf = BilinearForm(space)
+    bf.add_integrator(ScalarDiffusionIntegrator(coef=1, q=3))
+    A = bf.assembly()
+    lf = LinearForm(space)
+    lf.add_integrator(ScalarSourceIntegrator(source, q=3))
+    F = lf.assembly()
+    bc = DirichletBC(space, gd=solution)
+    A2, F2 = bc.apply(A, F)
+    uh, info = cg(A2, F2, M=jacobi(A2), atol=1e-30, rtol=1e-10, returninfo=True)
+    c0, c1, c2 = canonical(A.crow, A.col, A.values)
+    p0, p1, p2 = canonical(A2.crow, A2.col, A2.values)
+    np.savez_compressed(os.path.join(HERE, "c1_poisson_tri_p1_64.npz"),
+                        node=mesh.node, cell=mesh.cell, cell2dof=space.cell_to_dof(),
+                        crow=c0, col=c1, val=c2, F=F, is_bd=bc.is_boundary_dof,
+                        bc_crow=p0, bc_col=p1, bc_val=p2, bc_F=F2, uh=uh,
+                        niter=np.int64(info["niter"]), residual=np.float64(info["residual"]))
+    print("C1", A.nnz, A2.nnz, info["niter"])
+
+    # ------------------------------------------- small jittered scalar cases
+    rng = np.random.default_rng(20251204)
+    cases = {}
+    for tag, (kind, dims, p, q) in {
+        "tri_p1": ("tri", (4, 3), 1, None), "tri_p2": ("tri", (4, 3), 2, None), "tri_p3": ("tri", (3, 3), 3, None),
+        "tet_p1": ("tet", (3, 2, 2), 1, None), "tet_p2": ("tet", (2, 2, 2), 2, 4),
+    }.items():
+        if kind == "tri":
+            m0 = TriangleMesh.from_box([0, 1, 0, 1], *dims)
+            h = 1.0 / max(dims)
+            node = jitter(m0.node, m0.boundary_node_flag(), h, 0.15, rng)
+            mesh = TriangleMesh(node, m0.cell)
+        else:
+            m0 = TetrahedronMesh.from_box([0, 1, 0, 1, 0, 1], *dims)
+            h = 1.0 / max(dims)
+            node = jitter(m0.node, m0.boundary_node_flag(), h, 0.2, rng)
+            mesh = TetrahedronMesh(node, m0.cell)
+        space = LagrangeFESpace(mesh, p=p)
+        NC = mesh.number_of_cells()
+        kappa = np.exp(rng.normal(0.0, 1.0, NC))
+        rho = 1.0
+        di = ScalarDiffusionIntegrator(coef=kappa, q=q)
+        mi = ScalarMassIntegrator(coef=rho, q=q)
+        Kd = di.assembly(space)
+        Km = mi.assembly(space)
+        bf = BilinearForm(space)
+        bf.add_integrator(ScalarDiffusionIntegrator(coef=kappa, q=q), ScalarMassIntegrator(coef=rho, q=q))
+        A = bf.assembly()
+        f = rng.normal(size=space.number_of_global_dofs())
+        gdv = rng.normal(size=space.number_of_global_dofs())
+        bc = DirichletBC(space, gd=gdv)
+        A2, F2 = bc.apply(A, f.copy())
+        uh, info = cg(A2, F2, M=jacobi(A2), atol=1e-30, rtol=1e-10, returninfo=True)
+        c0, c1, c2 = canonical(A.crow, A.col, A.values)
+        p0, p1, p2 = canonical(A2.crow, A2.col, A2.values)
+        np.savez_compressed(os.path.join(HERE, f"small_{tag}.npz"),
+                            node=mesh.node, cell=mesh.cell, p=np.int64(p), q=np.int64(-1 if q is None else q),
+                            kappa=kappa, cell2dof=space.cell_to_dof(), edge=mesh.edge, face2cell=mesh.face2cell,
+                            ipoints=space.interpolation_points(), K_diff=Kd, K_mass=Km,
+                            crow=c0, col=c1, val=c2, f=f, gd=gdv, is_bd=bc.is_boundary_dof,
+                            bc_crow=p0, bc_col=p1, bc_val=p2, bc_F=F2, uh=uh, niter=np.int64(info["niter"]),
+                            residual=np.float64(info["residual"]))
+        print(tag, A.nnz, A2.nnz, info["niter"])
+
+    # ------------------------------------------------ P1 elasticity (tets)
+    m0 = TetrahedronMesh.from_box([0, 1, 0, 1, 0, 1], 4, 3, 3)
+    node = jitter(m0.node, m0.boundary_node_flag(), 0.25, 0.2, rng)
+    mesh = TetrahedronMesh(node, m0.cell)
+    NC = mesh.number_of_cells()
+    scale = np.exp(rng.normal(0.0, 0.5, NC))
+
+    class ScaledMaterial(LinearElasticMaterial):
+        def __init__(self, s, **kw):
+            super().__init__(**kw)
+            self._s = s
+
+        def elastic_matrix(self, bcs=None):
+            return self._s[:, None, None, None] * super().elastic_matrix(bcs)
+
+    mat = ScaledMaterial(scale, name="m", lame_lambda=1.0, shear_modulus=0.5)
+    ts = TensorFunctionSpace(LagrangeFESpace(mesh, p=1), (-1, 3))
+    KK = LinearElasticityIntegrator(mat, q=4).assembly(ts)
+    bf = BilinearForm(ts)
+    bf.add_integrator(LinearElasticityIntegrator(mat, q=4))
+    A = bf.assembly()
+    lf = LinearForm(ts)
+    @cartesian
+    def body_force(p):
+        out = np.zeros(p.shape[:-1] + (3,), dtype=np.float64)
+        out[..., 2] = -1.0
+        return out
+
+    lf.add_integrator(VectorSourceIntegrator(source=body_force, q=4))
+    F = lf.assembly()
+
+    @cartesian
+    def clamp(p):
+        return np.abs(p[..., 0]) < 1e-12
+
+    @cartesian
+    def zero_disp(p):
+        return np.zeros(p.shape[:-1] + (3,), dtype=np.float64)
+
+    bc = DirichletBC(ts, gd=zero_disp, threshold=clamp)
+    A2, F2 = bc.apply(A, F)
+    uh, info = cg(A2, F2, M=jacobi(A2), atol=1e-30, rtol=1e-10, returninfo=True)
+    c0, c1, c2 = canonical(A.crow, A.col, A.values)
+    p0, p1, p2 = canonical(A2.crow, A2.col, A2.values)
+    np.savez_compressed(os.path.join(HERE, "small_elasticity_tet_p1.npz"),
+                        node=mesh.node, cell=mesh.cell, scale=scale, cell2dof=ts.cell_to_dof(), KK=KK,
+                        crow=c0, col=c1, val=c2, F=F, is_bd=bc.is_boundary_dof,
+                        bc_crow=p0, bc_col=p1, bc_val=p2, bc_F=F2, uh=uh, niter=np.int64(info["niter"]))
+    print("elasticity", A.nnz, A2.nnz, info["niter"])
+
+    # ------------------------------------------- reference known answers
+    sys.path.insert(0, os.path.join(ref_root, "test", "fem"))
+    import scalar_diffusion_integrator_data as sdd
+    import scalar_mass_integrator_data as smd
+    dd = sdd.triangle_mesh_one_box[0]
+    md = smd.triangle_mesh_one_box[0]
+    np.savez_compressed(os.path.join(HERE, "reference_known_answers.npz"),
+                        diffusion_args=np.asarray(dd["args"][0] + [dd["args"][1], dd["args"][2]], dtype=np.float64),
+                        diffusion_cell_matrix=np.asarray(dd["assembly_cell_matrix"]),
+                        mass_args=np.asarray(md["args"][0] + [md["args"][1], md["args"][2]], dtype=np.float64),
+                        mass_cell_matrix=np.asarray(md["assembly_cell_matrix"]))
+
+    # ------------------------------------------------- quadrature tables
+    tabs = {}
+    for q in range(1, 10):
+        b, w = TriangleQuadrature(q).get_quadrature_points_and_weights()
+        tabs[f"tri_{q}_bcs"], tabs[f"tri_{q}_ws"] = np.asarray(b), np.asarray(w)
+    for q in range(1, 8):
+        b, w = TetrahedronQuadrature(q).get_quadrature_points_and_weights()
+        tabs[f"tet_{q}_bcs"], tabs[f"tet_{q}_ws"] = np.asarray(b), np.asarray(w)
+    np.savez_compressed(os.path.join(HERE, "quadrature_tables.npz"), **tabs)
+    print("done")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("FEALPY_REFERENCE", "/root/reference"))

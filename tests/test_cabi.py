@@ -1,0 +1,49 @@
+"""The C-ABI library builds for sm_103a, loads, and exports every entry point
+declared in include/fealpy_gb300.h (no GPU compute calls here)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from fealpy_gb300 import _build, _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_symbols():
+    text = open(os.path.join(ROOT, "include", "fealpy_gb300.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(fgb_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol():
+    path = _build.build()
+    lib = ctypes.CDLL(path)
+    missing = [s for s in header_symbols() if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+def test_binding_covers_header():
+    assert set(header_symbols()) == set(_lib.exported_symbols())
+
+
+def test_host_only_entry_points():
+    lib = _lib.lib()
+    assert lib.fgb_abi_version() == 1
+    assert lib.fgb_status_string(0) == b"ok"
+    assert b"pattern" in lib.fgb_status_string(4)
+    assert lib.fgb_pcg_workspace_bytes(1000) >= 5 * 8 * 1000
+    assert lib.fgb_scan_workspace_bytes(10) > 0
+
+
+def test_argument_validation_without_gpu():
+    lib = _lib.lib()
+    # invalid sizes are rejected before any CUDA call
+    assert lib.fgb_csr_spmv(1, 0, None, None, None, None, None, 0, None) == 1
+    assert lib.fgb_cell_factors(4, 10, None, None, 1, None, None, None, None, 1, None, None, None) == 1
+    assert lib.fgb_pcg_f64(0, None, None, None, None, None, None, 0.0, 0.0, 1, 1, 0, 0, 0, None, 0, None, None) == 1
+
+
+def test_build_targets_sm103a():
+    assert "arch=compute_103a,code=sm_103a" in " ".join(_build.ARCH_FLAGS)

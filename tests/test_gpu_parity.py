@@ -1,0 +1,276 @@
+"""GPU parity: the sm_103a path through the public API (and so through the C
+ABI) against the reference fixtures and the CPU oracle.
+
+Tolerances: CSR indptr/indices bit-exact (canonical order); values, right-hand
+sides and boundary-modified vectors within 1e-12 relative (max-norm relative to
+the array's max-norm); CG iteration counts within +-1 of the reference;
+solutions within 1e-9 relative of the reference's solution."""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+VAL_TOL = 1e-12
+
+
+def cuda():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch.device("cuda:0")
+
+
+def load(golden_dir, name):
+    return np.load(os.path.join(golden_dir, name))
+
+
+def rel_err(a, b):
+    a = a.detach().cpu().numpy() if isinstance(a, torch.Tensor) else np.asarray(a)
+    b = np.asarray(b)
+    return np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
+
+
+def same(a, b):
+    a = a.detach().cpu().numpy() if isinstance(a, torch.Tensor) else np.asarray(a)
+    return a.shape == np.asarray(b).shape and np.array_equal(a, np.asarray(b))
+
+
+def test_c1_poisson_full_path(golden_dir):
+    dev = cuda()
+    import fealpy_gb300 as F
+    from fealpy_gb300.fem import (BilinearForm, LinearForm, ScalarDiffusionIntegrator, ScalarSourceIntegrator,
+                                  DirichletBC)
+    z = load(golden_dir, "c1_poisson_tri_p1_64.npz")
+    mesh = F.TriangleMesh.from_box([0, 1, 0, 1], 64, 64, device=dev)
+    assert same(mesh.node, z["node"]) and same(mesh.cell, z["cell"])
+    space = F.LagrangeFESpace(mesh, p=1)
+
+    def solution(p):
+        return torch.sin(np.pi * p[..., 0]) * torch.sin(np.pi * p[..., 1])
+    solution.coordtype = "cartesian"
+
+    def source(p):
+        return 2 * np.pi ** 2 * solution(p)
+    source.coordtype = "cartesian"
+
+    bf = BilinearForm(space)
+    bf.add_integrator(ScalarDiffusionIntegrator(coef=1, q=3))
+    A = bf.assembly()
+    assert same(A.crow, z["crow"]) and same(A.col, z["col"])
+    assert rel_err(A.values, z["val"]) < VAL_TOL
+    lf = LinearForm(space)
+    lf.add_integrator(ScalarSourceIntegrator(source, q=3))
+    Fv = lf.assembly()
+    assert rel_err(Fv, z["F"]) < VAL_TOL
+    bc = DirichletBC(space, gd=solution)
+    assert same(bc.is_boundary_dof, z["is_bd"])
+    A2, F2 = bc.apply(A, Fv)
+    assert same(A2.crow, z["bc_crow"]) and same(A2.col, z["bc_col"])
+    assert rel_err(A2.values, z["bc_val"]) < VAL_TOL
+    assert rel_err(F2, z["bc_F"]) < VAL_TOL
+    M = F.JacobiPreconditioner().apply(A2)
+    uh, info = F.cg(A2, F2, M=M, atol=1e-30, rtol=1e-10, returninfo=True)
+    assert abs(info["niter"] - int(z["niter"])) <= 1
+    assert rel_err(uh, z["uh"]) < 1e-9
+
+
+@pytest.mark.parametrize("tag", ["tri_p1", "tri_p2", "tri_p3", "tet_p1", "tet_p2"])
+def test_small_cases(golden_dir, tag):
+    dev = cuda()
+    import fealpy_gb300 as F
+    from fealpy_gb300.fem import BilinearForm, ScalarDiffusionIntegrator, ScalarMassIntegrator, DirichletBC
+    z = load(golden_dir, f"small_{tag}.npz")
+    node = torch.as_tensor(z["node"], device=dev)
+    cell = torch.as_tensor(z["cell"], dtype=torch.int32, device=dev)
+    mesh = (F.TriangleMesh if z["cell"].shape[1] == 3 else F.TetrahedronMesh)(node, cell)
+    p = int(z["p"])
+    q = None if int(z["q"]) < 0 else int(z["q"])
+    space = F.LagrangeFESpace(mesh, p)
+    kappa = torch.as_tensor(z["kappa"], device=dev)
+    # local matrices through the integrator API
+    Kd = ScalarDiffusionIntegrator(coef=kappa, q=q).assembly(space)
+    assert rel_err(Kd, z["K_diff"]) < VAL_TOL
+    Km = ScalarMassIntegrator(coef=1.0, q=q).assembly(space)
+    assert rel_err(Km, z["K_mass"]) < VAL_TOL
+    bf = BilinearForm(space)
+    bf.add_integrator(ScalarDiffusionIntegrator(coef=kappa, q=q), ScalarMassIntegrator(coef=1.0, q=q))
+    A = bf.assembly()
+    assert same(A.crow, z["crow"]) and same(A.col, z["col"])
+    assert rel_err(A.values, z["val"]) < VAL_TOL
+    gd = torch.as_tensor(z["gd"], device=dev)
+    bc = DirichletBC(space, gd=gd)
+    assert same(bc.is_boundary_dof, z["is_bd"])
+    A2, F2 = bc.apply(A, torch.as_tensor(z["f"], device=dev))
+    assert same(A2.crow, z["bc_crow"]) and same(A2.col, z["bc_col"])
+    assert rel_err(A2.values, z["bc_val"]) < VAL_TOL
+    assert rel_err(F2, z["bc_F"]) < VAL_TOL
+    uh, info = F.cg(A2, F2, M=F.JacobiPreconditioner().apply(A2), atol=1e-30, rtol=1e-10, returninfo=True)
+    assert abs(info["niter"] - int(z["niter"])) <= 1
+    assert rel_err(uh, z["uh"]) < 1e-8
+
+
+def test_elasticity_p1(golden_dir):
+    dev = cuda()
+    import fealpy_gb300 as F
+    from fealpy_gb300.fem import BilinearForm, LinearForm, LinearElasticityIntegrator, VectorSourceIntegrator, DirichletBC
+    z = load(golden_dir, "small_elasticity_tet_p1.npz")
+    mesh = F.TetrahedronMesh(torch.as_tensor(z["node"], device=dev),
+                             torch.as_tensor(z["cell"], dtype=torch.int32, device=dev))
+    ts = F.TensorFunctionSpace(F.LagrangeFESpace(mesh, 1), (-1, 3))
+    mat = F.LinearElasticMaterial("m", lame_lambda=1.0, shear_modulus=0.5,
+                                  cell_scale=torch.as_tensor(z["scale"], device=dev))
+    bf = BilinearForm(ts)
+    bf.add_integrator(LinearElasticityIntegrator(mat, q=4))
+    A = bf.assembly()
+    assert same(A.crow, z["crow"]) and same(A.col, z["col"])
+    assert rel_err(A.values, z["val"]) < VAL_TOL
+    lf = LinearForm(ts)
+    lf.add_integrator(VectorSourceIntegrator(source=[0.0, 0.0, -1.0], q=4))
+    Fv = lf.assembly()
+    assert rel_err(Fv, z["F"]) < VAL_TOL
+    clamp = lambda x: torch.abs(x[..., 0]) < 1e-12
+    bc = DirichletBC(ts, gd=0.0, threshold=clamp)
+    assert same(bc.is_boundary_dof, z["is_bd"])
+    A2, F2 = bc.apply(A, Fv)
+    assert same(A2.crow, z["bc_crow"]) and same(A2.col, z["bc_col"])
+    assert rel_err(A2.values, z["bc_val"]) < VAL_TOL
+    assert rel_err(F2, z["bc_F"]) < VAL_TOL
+    uh, info = F.cg(A2, F2, M=F.JacobiPreconditioner().apply(A2), atol=1e-30, rtol=1e-10, returninfo=True)
+    assert abs(info["niter"] - int(z["niter"])) <= 1
+    assert rel_err(uh, z["uh"]) < 1e-8
+
+
+def test_spmv_all_lane_widths(golden_dir):
+    dev = cuda()
+    from fealpy_gb300 import kernels as K
+    import scipy.sparse as sp
+    z = load(golden_dir, "small_tet_p2.npz")
+    crow, col, val = z["crow"], z["col"], z["val"]
+    n = len(crow) - 1
+    x = np.random.default_rng(0).normal(size=n)
+    ref = sp.csr_matrix((val, col, crow), shape=(n, n)) @ x
+    t = lambda a, dt=None: torch.as_tensor(a, device=dev, dtype=dt)
+    for lanes in (0, 1, 2, 4, 8, 16, 32):
+        y = K.csr_spmv(t(crow), t(col), t(val), t(x), lanes)
+        assert rel_err(y, ref) < 1e-14
+        y32 = K.csr_spmv(t(crow), t(col), t(val, torch.float32), t(x, torch.float32), lanes)
+        assert rel_err(y32, ref) < 1e-5
+
+
+def test_determinism_bitwise(golden_dir):
+    dev = cuda()
+    import fealpy_gb300 as F
+    from fealpy_gb300.fem import BilinearForm, ScalarDiffusionIntegrator, ScalarMassIntegrator
+    mesh = F.TetrahedronMesh.from_box([0, 1, 0, 1, 0, 1], 6, 5, 4, device=dev)
+    space = F.LagrangeFESpace(mesh, 2)
+    kappa = torch.rand(mesh.number_of_cells(), device=dev, dtype=torch.float64) + 0.5
+    vals = []
+    for _ in range(2):
+        bf = BilinearForm(space)
+        bf.add_integrator(ScalarDiffusionIntegrator(coef=kappa, q=4), ScalarMassIntegrator(q=4))
+        vals.append(bf.assembly())
+    assert torch.equal(vals[0].crow, vals[1].crow) and torch.equal(vals[0].col, vals[1].col)
+    assert torch.equal(vals[0].values, vals[1].values)
+
+
+def test_high_valence_rows_take_the_wide_path():
+    """A fan of 300 triangles around one vertex: that row (301 entries) exceeds
+    the first-pass capacity of the pattern and assembly kernels."""
+    dev = cuda()
+    import fealpy_gb300 as F
+    from fealpy_gb300.fem import BilinearForm, ScalarDiffusionIntegrator
+    from oracle import fem_oracle as O
+    m = 300
+    ang = np.linspace(0, 2 * np.pi, m, endpoint=False)
+    node = np.concatenate([[[0.0, 0.0]], np.c_[np.cos(ang), np.sin(ang)]], axis=0)
+    cell = np.array([[0, 1 + k, 1 + (k + 1) % m] for k in range(m)], dtype=np.int32)
+    mesh = F.TriangleMesh(torch.as_tensor(node, device=dev), torch.as_tensor(cell, device=dev))
+    space = F.LagrangeFESpace(mesh, 2)
+    bf = BilinearForm(space)
+    bf.add_integrator(ScalarDiffusionIntegrator(q=4))
+    A = bf.assembly()
+    topo = O.construct(cell)
+    c2d = O.cell_to_dof(cell, topo, node.shape[0], 2)
+    n = O.n_global_dofs(cell, topo, node.shape[0], 2)
+    crow, col, val = O.coalesce_to_csr(c2d, O.diffusion_local(node, cell, 2, 4), n)
+    assert same(A.crow, crow) and same(A.col, col)
+    assert rel_err(A.values, val) < VAL_TOL
+
+
+def test_mixed_precision_reaches_fp64_accuracy():
+    dev = cuda()
+    import fealpy_gb300 as F
+    from fealpy_gb300.fem import BilinearForm, ScalarDiffusionIntegrator, ScalarMassIntegrator, DirichletBC
+    mesh = F.TetrahedronMesh.from_box([0, 1, 0, 1, 0, 1], 12, 12, 12, device=dev)
+    space = F.LagrangeFESpace(mesh, 2)
+    g = torch.Generator(device="cpu").manual_seed(0)
+    kappa = torch.exp(torch.randn(mesh.number_of_cells(), generator=g, dtype=torch.float64)).to(dev)
+    bf = BilinearForm(space)
+    bf.add_integrator(ScalarDiffusionIntegrator(coef=kappa, q=4), ScalarMassIntegrator(coef=1.0, q=4))
+    A = bf.assembly(emit_f32=True)
+    n = space.number_of_global_dofs()
+    A2, F2 = DirichletBC(space, gd=0.0).apply(A, torch.ones(n, dtype=torch.float64, device=dev))
+    x64, i64 = F.cg(A2, F2, M=F.JacobiPreconditioner().apply(A2), atol=1e-30, rtol=1e-12, returninfo=True)
+    xm, im = F.cg_mixed(A2, F2, rtol=1e-10, returninfo=True)
+    r = F2 - A2 @ xm
+    rel = float(torch.linalg.norm(r) / torch.linalg.norm(F2))
+    assert rel <= 1e-10 * 1.0001, rel
+    assert abs(rel - im["relres"]) <= 1e-3 * rel + 1e-16
+    err = float(torch.max(torch.abs(xm - x64)) / torch.max(torch.abs(x64)))
+    assert err < 1e-8, err
+    assert im["n_updates"] >= 1
+
+
+def test_cg_edge_cases():
+    dev = cuda()
+    import fealpy_gb300 as F
+    from fealpy_gb300.fem import BilinearForm, ScalarDiffusionIntegrator, DirichletBC
+    mesh = F.TriangleMesh.from_box([0, 1, 0, 1], 8, 8, device=dev)
+    space = F.LagrangeFESpace(mesh, 1)
+    bf = BilinearForm(space)
+    bf.add_integrator(ScalarDiffusionIntegrator())
+    A = bf.assembly()
+    n = space.number_of_global_dofs()
+    A2, F2 = DirichletBC(space, gd=0.0).apply(A, torch.ones(n, dtype=torch.float64, device=dev))
+    # zero right-hand side: x = 0 and no iteration
+    x, info = F.cg(A2, torch.zeros(n, dtype=torch.float64, device=dev), x0=torch.ones(n, dtype=torch.float64, device=dev),
+                   returninfo=True)
+    assert info["niter"] == 0 and float(torch.abs(x).max()) == 0.0
+    # iteration limit
+    x, info = F.cg(A2, F2, M=F.JacobiPreconditioner().apply(A2), atol=1e-30, rtol=1e-30, maxit=5, returninfo=True)
+    assert info["niter"] == 5
+    # a negative definite matrix is reported, not silently iterated
+    neg = A2.mul(-1.0)
+    with pytest.raises(RuntimeError):
+        F.cg(neg, F2, rtol=1e-10)
+
+
+def test_full_size_properties():
+    """Size-independent checks on a 32^3 P2 tetrahedral case: diffusion rows sum
+    to zero, the mass matrix integrates 1 to |Omega| = 1, A is symmetric."""
+    dev = cuda()
+    import fealpy_gb300 as F
+    from fealpy_gb300.fem import BilinearForm, ScalarDiffusionIntegrator, ScalarMassIntegrator
+    mesh = F.TetrahedronMesh.from_box([0, 1, 0, 1, 0, 1], 32, 32, 32, device=dev)
+    space = F.LagrangeFESpace(mesh, 2)
+    n = space.number_of_global_dofs()
+    one = torch.ones(n, dtype=torch.float64, device=dev)
+    bf = BilinearForm(space)
+    bf.add_integrator(ScalarDiffusionIntegrator(q=4))
+    A = bf.assembly()
+    scale = float(A.values.abs().max())
+    assert float((A @ one).abs().max()) < 1e-12 * scale * 30
+    bm = BilinearForm(space)
+    bm.add_integrator(ScalarMassIntegrator(q=4))
+    M = bm.assembly()
+    assert abs(float(M.values.sum()) - 1.0) < 1e-12
+    d = A.to_dense() if n < 20000 else None
+    # symmetry via a random bilinear form: y^T A x == x^T A y
+    g = torch.Generator(device="cpu").manual_seed(1)
+    x = torch.randn(n, generator=g, dtype=torch.float64).to(dev)
+    y = torch.randn(n, generator=g, dtype=torch.float64).to(dev)
+    a = float(torch.dot(y, A @ x))
+    b = float(torch.dot(x, A @ y))
+    assert abs(a - b) <= 1e-12 * max(abs(a), 1.0) * 10

@@ -1,0 +1,114 @@
+"""Host-side logic of the package on CPU tensors (no GPU): mesh topology, dof
+numbering, boundary dofs and the factor x table decomposition the assembly
+kernels evaluate, all checked against the reference's fixtures."""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from fealpy_gb300 import simplex as sx
+from fealpy_gb300.mesh import TriangleMesh, TetrahedronMesh
+from fealpy_gb300.functionspace import LagrangeFESpace, TensorFunctionSpace
+
+
+def load(golden_dir, name):
+    return np.load(os.path.join(golden_dir, name))
+
+
+def make_mesh(node, cell):
+    node_t = torch.as_tensor(node)
+    cell_t = torch.as_tensor(cell, dtype=torch.int32)
+    return (TriangleMesh if cell.shape[1] == 3 else TetrahedronMesh)(node_t, cell_t)
+
+
+def kernel_factors_numpy(node, cell):
+    """What fgb_cell_factors computes: signed measure, grad(lambda_{1..TD})."""
+    TD = cell.shape[1] - 1
+    x = node[cell]
+    J = np.stack([x[:, k + 1] - x[:, 0] for k in range(TD)], axis=-1)   # J[c, a, k]
+    det = np.linalg.det(J)
+    inv = np.linalg.inv(J)                                               # inv[c, k, a]
+    measure = det / (2.0 if TD == 2 else 6.0)
+    return measure, inv
+
+
+@pytest.mark.parametrize("tag", ["tri_p1", "tri_p2", "tri_p3", "tet_p1", "tet_p2"])
+def test_topology_dofs_and_boundary(golden_dir, tag):
+    z = load(golden_dir, f"small_{tag}.npz")
+    mesh = make_mesh(z["node"], z["cell"])
+    p = int(z["p"])
+    assert np.array_equal(mesh.edge.numpy(), z["edge"])
+    assert np.array_equal(mesh.face2cell.numpy(), z["face2cell"])
+    space = LagrangeFESpace(mesh, p)
+    assert np.array_equal(space.cell_to_dof().numpy(), z["cell2dof"])
+    assert space.number_of_global_dofs() == z["f"].shape[0]
+    assert np.array_equal(space.is_boundary_dof().numpy(), z["is_bd"])
+    assert np.allclose(space.interpolation_points().numpy(), z["ipoints"], atol=1e-15, rtol=0)
+
+
+@pytest.mark.parametrize("tag", ["tri_p1", "tri_p2", "tri_p3", "tet_p1", "tet_p2"])
+def test_factor_table_decomposition(golden_dir, tag):
+    """sum_t factor_t * table_t reproduces the reference's quadrature local matrices."""
+    z = load(golden_dir, f"small_{tag}.npz")
+    node, cell, p = z["node"], z["cell"], int(z["p"])
+    TD = cell.shape[1] - 1
+    q = p + 3 if int(z["q"]) < 0 else int(z["q"])
+    measure, inv = kernel_factors_numpy(node, cell)
+    pairs = sx.metric_pairs(TD)
+    G = np.stack([measure * np.einsum("ca,ca->c", inv[:, k], inv[:, l]) for k, l in pairs], axis=1)
+    Kd = np.einsum("ct,tij->cij", G * z["kappa"][:, None], sx.diffusion_tables(TD, p, q))
+    Km = np.einsum("c,tij->cij", measure, sx.mass_table(TD, p, q))
+    scale = np.max(np.abs(z["K_diff"]))
+    assert np.max(np.abs(Kd - z["K_diff"])) / scale < 1e-12
+    assert np.max(np.abs(Km - z["K_mass"])) / np.max(np.abs(z["K_mass"])) < 1e-12
+
+
+def test_elasticity_host_logic(golden_dir):
+    z = load(golden_dir, "small_elasticity_tet_p1.npz")
+    node, cell, s = z["node"], z["cell"], z["scale"]
+    mesh = make_mesh(node, cell)
+    ts = TensorFunctionSpace(LagrangeFESpace(mesh, 1), (-1, 3))
+    assert np.array_equal(ts.cell_to_dof().numpy(), z["cell2dof"])
+    clamp = lambda x: torch.abs(x[..., 0]) < 1e-12
+    assert np.array_equal(ts.is_boundary_dof(threshold=clamp, method=None).numpy(), z["is_bd"])
+    # the per-(row block, column block) formula of the elasticity kernel
+    measure, inv = kernel_factors_numpy(node, cell)
+    g = np.concatenate([-inv.sum(axis=1, keepdims=True), inv], axis=1)   # (NC, 4, 3) grad lambda
+    _, ws = mesh.quadrature_formula(4).get_quadrature_points_and_weights()
+    wsum = ws.sum()
+    lam, mu = 1.0 * s * measure * wsum, 0.5 * s * measure * wsum
+    d00 = 2 * mu + lam
+    NC = cell.shape[0]
+    KK = np.zeros((NC, 12, 12))
+    for a in range(3):
+        for b in range(3):
+            gi, gj = g[:, :, None, :], g[:, None, :, :]
+            if a == b:
+                dot = np.einsum("cid,cjd->cij", g, g)
+                blk = d00[:, None, None] * gi[..., a] * gj[..., a] + mu[:, None, None] * (dot - gi[..., a] * gj[..., a])
+            else:
+                blk = lam[:, None, None] * gi[..., a] * gj[..., b] + mu[:, None, None] * gi[..., b] * gj[..., a]
+            KK[:, a::3, b::3] = blk
+    assert np.max(np.abs(KK - z["KK"])) / np.max(np.abs(z["KK"])) < 1e-12
+
+
+def test_c1_mesh_bitwise(golden_dir):
+    z = load(golden_dir, "c1_poisson_tri_p1_64.npz")
+    mesh = TriangleMesh.from_box([0, 1, 0, 1], 64, 64)
+    assert np.array_equal(mesh.node.numpy(), z["node"])
+    assert np.array_equal(mesh.cell.numpy(), z["cell"])
+    space = LagrangeFESpace(mesh, 1)
+    assert np.array_equal(space.is_boundary_dof().numpy(), z["is_bd"])
+
+
+def test_tet_from_box_matches_oracle():
+    from oracle import fem_oracle as O
+    node, cell = O.tet_from_box([0, 1, 0, 1, 0, 1], 3, 2, 2)
+    mesh = TetrahedronMesh.from_box([0, 1, 0, 1, 0, 1], 3, 2, 2)
+    assert np.array_equal(mesh.node.numpy(), node)
+    assert np.array_equal(mesh.cell.numpy(), cell)
+    topo = O.construct(cell)
+    assert np.array_equal(mesh.edge.numpy(), topo["edge"])
+    assert np.array_equal(mesh.face.numpy(), topo["face"])
+    assert np.array_equal(mesh.cell_to_ipoint(2).numpy(), O.cell_to_dof(cell, topo, node.shape[0], 2))
