@@ -189,7 +189,8 @@ def run_ours(args):
         return float(t.item())
 
     results = {}
-    for mode in ("fp64", "mixed"):
+    modes = [m for m in args.modes.split(",") if m]
+    for mode in modes:
         for _ in range(args.warmup):
             solve_step(torch, F, space, kappa, bc, mode)
         barrier()
@@ -222,6 +223,14 @@ def run_ours(args):
                          "kernel_ms_avg": kms / max(kl, 1), "kernel_launches": kl, "launches": launches,
                          "clocks": clocks, "nnz": A2.nnz, "n": gdof}
 
+    if set(modes) != {"fp64", "mixed"} or args.no_e2e:
+        # profiling run: report the per-mode timings on stderr only
+        for m, r in results.items():
+            print(f"[profile run] {m}: {r['ms_per_step']:.3f} ms/step, {r['niter']} iterations, "
+                  f"relres {r['relres']:.3e}, spmv avg {r['kernel_ms_avg'] * 1e3:.1f} us", file=sys.stderr)
+        if world > 1:
+            dist.destroy_process_group()
+        return
     x64 = results["fp64"]["x"]
     xm = results["mixed"]["x"]
     err = float(torch.max(torch.abs(xm - x64)) / torch.max(torch.abs(x64)))
@@ -373,6 +382,9 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=64)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--modes", default="fp64,mixed",
+                    help="solver modes to time (a single-mode run is for profiling and prints no JSON line)")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)

@@ -79,7 +79,23 @@ _SIGNATURES = {
     "fgb_pcg_mixed": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_dbl, c_dbl, c_i64, c_i32, c_i32,
                               c_i32, c_vp, c_sz, ctypes.POINTER(PcgInfo), c_vp]),
     "fgb_gather_sum": (c_i32, [c_i32, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "fgb_sell_slots": (c_i64, [c_i64]),
+    "fgb_sell_workspace_bytes": (c_sz, [c_i64]),
+    "fgb_sell_plan": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_vp, c_sz, c_vp]),
+    "fgb_sell_fill": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "fgb_sell_spmv": (c_i32, [c_i32, ctypes.c_void_p, c_vp, c_vp, c_vp]),
+    "fgb_pcg_sell_workspace_bytes": (c_sz, [c_i64]),
+    "fgb_pcg_sell_f64": (c_i32, [ctypes.c_void_p, c_vp, c_vp, c_vp, c_dbl, c_dbl, c_i64, c_i32, c_i32, c_i32, c_i32,
+                                 c_vp, c_sz, ctypes.POINTER(PcgInfo), c_vp]),
+    "fgb_pcg_sell_mixed": (c_i32, [ctypes.c_void_p, c_vp, c_vp, c_vp, c_dbl, c_dbl, c_i64, c_i32, c_i32, c_i32,
+                                   c_vp, c_sz, ctypes.POINTER(PcgInfo), c_vp]),
 }
+
+
+class SellDesc(ctypes.Structure):
+    """``fgb_sell`` (include/fealpy_gb300.h)."""
+    _fields_ = [("n", c_i64), ("n_slices", c_i64), ("slice_ptr", c_vp), ("perm", c_vp), ("col", c_vp),
+                ("val64", c_vp), ("val32", c_vp)]
 
 
 def library_path() -> str:
@@ -128,7 +144,7 @@ KERNELS_PER_CALL = {
     "fgb_cell_factors": 1, "fgb_adjacency_build": 6, "fgb_pattern_count": 5, "fgb_pattern_fill": 2,
     "fgb_pattern_expand_blocks": 2, "fgb_assemble_scalar": 2, "fgb_assemble_elasticity_p1": 2,
     "fgb_dirichlet_count": 1, "fgb_exclusive_scan_i32": 3, "fgb_dirichlet_fill": 1, "fgb_csr_spmv": 1,
-    "fgb_csr_diagonal": 1, "fgb_gather_sum": 1,
+    "fgb_csr_diagonal": 1, "fgb_gather_sum": 1, "fgb_sell_plan": 4, "fgb_sell_fill": 1, "fgb_sell_spmv": 1,
 }
 
 _launches = [0]

@@ -1,0 +1,781 @@
+// SELL-32 (sliced ELLPACK, rows sorted by length inside windows of 256 rows)
+// copy of a CSR matrix, its SpMV, and the Jacobi-PCG solvers that iterate on it.
+//
+// Why: the CG time is the SpMV, and a CSR SpMV with a few lanes per row keeps
+// too few bytes in flight to cover HBM latency (rows here hold 10-80 entries).
+// In SELL-32 a warp owns 32 rows; entry k of those rows sits in one 128-byte
+// line (column-major inside the slice), so every load instruction of the warp
+// is a full coalesced line, each lane accumulates its own row with no shuffles,
+// and the k-loop is unrolled so several lines per warp are in flight.  Sorting
+// rows by length inside 256-row windows keeps the zero padding small while
+// preserving locality of the gathered vector entries.
+//
+// The solvers keep every vector in the original row order; only the matrix is
+// permuted (slot -> row map `perm`).  Two drivers are provided: host polling of
+// a device flag (as in krylov.cu) and a CUDA graph whose while-conditional node
+// runs the iteration body on the device until a loop-control kernel clears the
+// condition (converged, breakdown, iteration limit, or a hard trip cap).
+
+#include "fgb_common.cuh"
+
+#include <climits>
+#include <cmath>
+#include <cstring>
+
+namespace fgb {
+
+constexpr int kSellC = 32;        // rows per slice (one warp)
+constexpr int kSellWindow = 256;  // rows sorted together
+constexpr int kSellThreads = 256;
+constexpr int kSellMaxBlocks = kNumSMs * 8;
+
+struct SellView {
+  int64_t n, n_slices;
+  const int64_t* slice_ptr;
+  const int32_t* perm;
+  const int32_t* col;
+};
+
+// -------------------------------------------------------------- construction
+__global__ void sell_sort_windows(int64_t n, const int64_t* __restrict__ indptr, int32_t* __restrict__ perm,
+                                  int32_t* __restrict__ slice_entries) {
+  __shared__ unsigned long long key[kSellWindow];
+  const int64_t base = static_cast<int64_t>(blockIdx.x) * kSellWindow;
+  const int64_t row = base + threadIdx.x;
+  int len = -1;
+  if (row < n) len = static_cast<int>(indptr[row + 1] - indptr[row]);
+  // ascending on (INT_MAX - len, local row): longest rows first, padding rows
+  // (len = -1) last, ties in row order
+  const unsigned long long hi = static_cast<unsigned long long>(static_cast<long long>(INT_MAX) - len);
+  key[threadIdx.x] = (hi << 32) | static_cast<unsigned long long>(threadIdx.x);
+  __syncthreads();
+  for (int k = 2; k <= kSellWindow; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      const int t = threadIdx.x, u = t ^ j;
+      if (u > t) {
+        unsigned long long a = key[t], b = key[u];
+        bool up = (t & k) == 0;
+        if ((a > b) == up) { key[t] = b; key[u] = a; }
+      }
+      __syncthreads();
+    }
+  }
+  const unsigned long long kk = key[threadIdx.x];
+  const int slen = static_cast<int>(static_cast<long long>(INT_MAX) - static_cast<long long>(kk >> 32));
+  const int64_t full = base + static_cast<int64_t>(kk & 0xffffffffu);
+  const int64_t slot = base + threadIdx.x;
+  perm[slot] = (slen >= 0 && full < n) ? static_cast<int32_t>(full) : -1;
+  // the first slot of a slice holds its longest row: that is the slice width
+  if ((threadIdx.x & 31) == 0) slice_entries[slot / kSellC] = kSellC * (slen > 0 ? slen : 0);
+}
+
+__global__ void sell_fill_kernel(int64_t n_slices, const int64_t* __restrict__ slice_ptr,
+                                 const int32_t* __restrict__ perm, const int64_t* __restrict__ indptr,
+                                 const int32_t* __restrict__ indices, const double* __restrict__ v64,
+                                 const float* __restrict__ v32, int32_t* __restrict__ scol, double* __restrict__ s64,
+                                 float* __restrict__ s32) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
+  const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+  for (int64_t s = warp; s < n_slices; s += nwarps) {
+    const int64_t base = slice_ptr[s];
+    const int w = static_cast<int>((slice_ptr[s + 1] - base) / kSellC);
+    const int32_t row = perm[s * kSellC + lane];
+    int64_t rs = 0;
+    int len = 0;
+    if (row >= 0) { rs = indptr[row]; len = static_cast<int>(indptr[row + 1] - rs); }
+    for (int k = 0; k < w; ++k) {
+      const int64_t pos = base + static_cast<int64_t>(k) * kSellC + lane;
+      const bool real = k < len;
+      scol[pos] = real ? indices[rs + k] : (row >= 0 ? row : 0);
+      if (s64) s64[pos] = real ? v64[rs + k] : 0.0;
+      if (s32) s32[pos] = real ? (v64 ? static_cast<float>(v64[rs + k]) : v32[rs + k]) : 0.0f;
+    }
+  }
+}
+
+// ------------------------------------------------------------------- SpMV
+template <typename T>
+__global__ void __launch_bounds__(kSellThreads) sell_spmv_kernel(SellView A, const T* __restrict__ val,
+                                                                 const T* __restrict__ x, T* __restrict__ y) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
+  const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+  for (int64_t s = warp; s < A.n_slices; s += nwarps) {
+    const int64_t base = A.slice_ptr[s] + lane;
+    const int w = static_cast<int>((A.slice_ptr[s + 1] - A.slice_ptr[s]) >> 5);
+    T acc = T(0);
+    int k = 0;
+    for (; k + 4 <= w; k += 4) {
+      int32_t j[4];
+      T v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        j[u] = ld_stream(A.col + base + static_cast<int64_t>(k + u) * kSellC);
+        v[u] = ld_stream(val + base + static_cast<int64_t>(k + u) * kSellC);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) acc += v[u] * __ldg(x + j[u]);
+    }
+    for (; k < w; ++k) {
+      const int64_t p = base + static_cast<int64_t>(k) * kSellC;
+      acc += ld_stream(val + p) * __ldg(x + ld_stream(A.col + p));
+    }
+    const int32_t row = A.perm[s * kSellC + lane];
+    if (row >= 0) y[row] = acc;
+  }
+}
+
+// ------------------------------------------------------------ PCG kernels
+struct SellPcgState {
+  double rz, rz_prev, rr, alpha, beta, b_norm, tol, atol, resid, r_upd, true_rel;
+  long long niter, maxit, trips, trip_cap;
+  int done, need_update, n_updates, norm_rr;
+  unsigned int counter[4];
+};
+
+// Last-block-done deterministic reduction of two FP64 partials per block.
+__device__ bool sell_last_block(double v0, double v1, double* partials, unsigned int* counter, double* out0,
+                                double* out1) {
+  __shared__ double red[kSellThreads / 32];
+  __shared__ bool am_last;
+  double s0 = block_sum(v0, red);
+  __syncthreads();
+  double s1 = block_sum(v1, red);
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = s0;
+    partials[kSellMaxBlocks + blockIdx.x] = s1;
+    __threadfence();
+    unsigned int t = atomicAdd(counter, 1u);
+    am_last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!am_last) return false;
+  __threadfence();
+  double a = 0.0, b = 0.0;
+  for (int k = threadIdx.x; k < static_cast<int>(gridDim.x); k += blockDim.x) {
+    a += __ldcg(partials + k);
+    b += __ldcg(partials + kSellMaxBlocks + k);
+  }
+  __syncthreads();
+  a = block_sum(a, red);
+  __syncthreads();
+  b = block_sum(b, red);
+  if (threadIdx.x == 0) { *out0 = a; *out1 = b; *counter = 0u; }
+  return true;
+}
+
+// acc_row = sum_k val * (z[j] + beta p_old[j]) over one SELL row (lane), unrolled.
+template <typename T>
+__device__ __forceinline__ T sell_row_dot_p(const SellView& A, const T* __restrict__ val, int64_t base, int w,
+                                            const T* __restrict__ z, const T* __restrict__ p_old, T beta) {
+  T acc = T(0);
+  int k = 0;
+  for (; k + 4 <= w; k += 4) {
+    int32_t j[4];
+    T v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      j[u] = ld_stream(A.col + base + static_cast<int64_t>(k + u) * kSellC);
+      v[u] = ld_stream(val + base + static_cast<int64_t>(k + u) * kSellC);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) acc += v[u] * (z[j[u]] + beta * p_old[j[u]]);
+  }
+  for (; k < w; ++k) {
+    const int64_t p = base + static_cast<int64_t>(k) * kSellC;
+    const int32_t j = ld_stream(A.col + p);
+    acc += ld_stream(val + p) * (z[j] + beta * p_old[j]);
+  }
+  return acc;
+}
+
+template <typename T>
+__device__ __forceinline__ T sell_row_dot_x(const SellView& A, const T* __restrict__ val, int64_t base, int w,
+                                            const T* __restrict__ x) {
+  T acc = T(0);
+  int k = 0;
+  for (; k + 4 <= w; k += 4) {
+    int32_t j[4];
+    T v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      j[u] = ld_stream(A.col + base + static_cast<int64_t>(k + u) * kSellC);
+      v[u] = ld_stream(val + base + static_cast<int64_t>(k + u) * kSellC);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) acc += v[u] * x[j[u]];
+  }
+  for (; k < w; ++k) {
+    const int64_t p = base + static_cast<int64_t>(k) * kSellC;
+    acc += ld_stream(val + p) * x[ld_stream(A.col + p)];
+  }
+  return acc;
+}
+
+#define SELL_WARP_LOOP(A)                                                                   \
+  const int lane = threadIdx.x & 31;                                                        \
+  const int64_t warp0 = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5; \
+  const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;               \
+  for (int64_t s = warp0; s < (A).n_slices; s += nwarps)
+
+// r = b - A x ; z = Dinv r ; p = z ; rz, b.b   (T = FP64 state)
+template <typename T>
+__global__ void __launch_bounds__(kSellThreads) sell_pcg_init(SellView A, const T* __restrict__ val,
+                                                              const T* __restrict__ dinv, const T* __restrict__ b,
+                                                              const T* __restrict__ x, T* __restrict__ r,
+                                                              T* __restrict__ z, T* __restrict__ p, double* partials,
+                                                              SellPcgState* st) {
+  double rz = 0.0, bb = 0.0;
+  SELL_WARP_LOOP(A) {
+    const int64_t base = A.slice_ptr[s] + lane;
+    const int w = static_cast<int>((A.slice_ptr[s + 1] - A.slice_ptr[s]) >> 5);
+    const T acc = sell_row_dot_x(A, val, base, w, x);
+    const int32_t row = A.perm[s * kSellC + lane];
+    if (row >= 0) {
+      const T bi = b[row];
+      const T ri = bi - acc;
+      const T zi = dinv ? dinv[row] * ri : ri;
+      r[row] = ri; z[row] = zi; p[row] = zi;
+      rz += static_cast<double>(ri) * static_cast<double>(zi);
+      bb += static_cast<double>(bi) * static_cast<double>(bi);
+    }
+  }
+  double trz, tbb;
+  if (sell_last_block(rz, bb, partials, &st->counter[0], &trz, &tbb) && threadIdx.x == 0) {
+    st->rz = trz;
+    st->rr = trz;
+    st->b_norm = sqrt(tbb);
+    st->beta = 0.0;
+    st->niter = 0;
+    st->n_updates = 0;
+    st->need_update = 0;
+    if (st->b_norm < 1e-15) st->done = FGB_PCG_ZERO_RHS;
+  }
+}
+
+// kernel A: p_new = z + beta p_old ; Ap = A p_new ; alpha = rz / p_new.Ap
+template <typename T>
+__global__ void __launch_bounds__(kSellThreads) sell_pcg_spmv(SellView A, const T* __restrict__ val,
+                                                              const T* __restrict__ z, const T* __restrict__ p_old,
+                                                              T* __restrict__ p_new, T* __restrict__ Ap,
+                                                              double* partials, SellPcgState* st) {
+  if (st->done) return;
+  const T beta = static_cast<T>(st->beta);
+  double pap = 0.0;
+  SELL_WARP_LOOP(A) {
+    const int64_t base = A.slice_ptr[s] + lane;
+    const int w = static_cast<int>((A.slice_ptr[s + 1] - A.slice_ptr[s]) >> 5);
+    const T acc = sell_row_dot_p(A, val, base, w, z, p_old, beta);
+    const int32_t row = A.perm[s * kSellC + lane];
+    if (row >= 0) {
+      const T pi = z[row] + beta * p_old[row];
+      p_new[row] = pi;
+      Ap[row] = acc;
+      pap += static_cast<double>(pi) * static_cast<double>(acc);
+    }
+  }
+  double tpap, unused;
+  if (sell_last_block(pap, 0.0, partials, &st->counter[1], &tpap, &unused) && threadIdx.x == 0) {
+    if (!(tpap > 0.0) || !isfinite(tpap)) {
+      st->done = isfinite(tpap) ? FGB_PCG_BREAKDOWN : FGB_PCG_NONFINITE;
+      st->alpha = 0.0;
+    } else {
+      st->alpha = st->rz / tpap;
+    }
+  }
+}
+
+// kernel B (FP64 solver)
+__global__ void __launch_bounds__(kSellThreads) sell_pcg_update_f64(int64_t n, const double* __restrict__ dinv,
+                                                                    const double* __restrict__ p,
+                                                                    const double* __restrict__ Ap,
+                                                                    double* __restrict__ x, double* __restrict__ r,
+                                                                    double* __restrict__ z, double* partials,
+                                                                    SellPcgState* st) {
+  if (st->done) return;
+  const double alpha = st->alpha;
+  double rz = 0.0, rr = 0.0;
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const double pi = p[i];
+    x[i] += alpha * pi;
+    const double ri = r[i] - alpha * Ap[i];
+    const double zi = dinv ? dinv[i] * ri : ri;
+    r[i] = ri;
+    z[i] = zi;
+    rz += ri * zi;
+    rr += ri * ri;
+  }
+  double trz, trr;
+  if (sell_last_block(rz, rr, partials, &st->counter[2], &trz, &trr) && threadIdx.x == 0) {
+    st->niter += 1;
+    const double res = st->norm_rr ? sqrt(trr) : sqrt(trz);
+    st->resid = res;
+    st->rr = trr;
+    if (!isfinite(res)) st->done = FGB_PCG_NONFINITE;
+    else if (res < st->atol) st->done = FGB_PCG_ATOL;
+    else if (res < st->tol) st->done = FGB_PCG_RTOL;
+    else if (st->niter >= st->maxit) st->done = FGB_PCG_MAXIT;
+    st->rz_prev = st->rz;
+    st->beta = trz / st->rz;
+    st->rz = trz;
+  }
+}
+
+// kernel B (mixed solver): FP32 updates, decides whether a reliable update is due
+__global__ void __launch_bounds__(kSellThreads) sell_mixed_update(int64_t n, const float* __restrict__ dinv,
+                                                                  const float* __restrict__ p,
+                                                                  const float* __restrict__ Ap, float* __restrict__ y,
+                                                                  float* __restrict__ r, float* __restrict__ z,
+                                                                  double* partials, SellPcgState* st, double delta) {
+  if (st->done) return;
+  const float alpha = static_cast<float>(st->alpha);
+  double rz = 0.0, rr = 0.0;
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    y[i] += alpha * p[i];
+    const float ri = r[i] - alpha * Ap[i];
+    const float zi = dinv[i] * ri;
+    r[i] = ri;
+    z[i] = zi;
+    rz += static_cast<double>(ri) * static_cast<double>(zi);
+    rr += static_cast<double>(ri) * static_cast<double>(ri);
+  }
+  double trz, trr;
+  if (sell_last_block(rz, rr, partials, &st->counter[2], &trz, &trr) && threadIdx.x == 0) {
+    st->niter += 1;
+    const double res = sqrt(trr);
+    st->resid = res;
+    st->rr = trr;
+    if (!isfinite(res)) st->done = FGB_PCG_NONFINITE;
+    else st->need_update = (res < delta * st->r_upd) || (res < st->tol) || (st->niter >= st->maxit);
+    st->rz_prev = st->rz;
+    st->beta = trz / st->rz;
+    st->rz = trz;
+  }
+}
+
+// reliable update part 1: x += y, y = 0 (own rows)
+__global__ void sell_mixed_fold(int64_t n, double* __restrict__ x, float* __restrict__ y, const SellPcgState* st,
+                                int first) {
+  if (!first && (st->done || !st->need_update)) return;
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    x[i] += static_cast<double>(y[i]);
+    y[i] = 0.0f;
+  }
+}
+
+// reliable update part 2: r64 = b - A64 x, true residual test
+__global__ void __launch_bounds__(kSellThreads) sell_mixed_residual(SellView A, const double* __restrict__ val,
+                                                                    const double* __restrict__ b,
+                                                                    const double* __restrict__ x,
+                                                                    double* __restrict__ r64, double* partials,
+                                                                    SellPcgState* st, int first) {
+  if (!first && (st->done || !st->need_update)) return;
+  double rr = 0.0;
+  SELL_WARP_LOOP(A) {
+    const int64_t base = A.slice_ptr[s] + lane;
+    const int w = static_cast<int>((A.slice_ptr[s + 1] - A.slice_ptr[s]) >> 5);
+    const double acc = sell_row_dot_x(A, val, base, w, x);
+    const int32_t row = A.perm[s * kSellC + lane];
+    if (row >= 0) {
+      const double ri = b[row] - acc;
+      r64[row] = ri;
+      rr += ri * ri;
+    }
+  }
+  double trr, unused;
+  if (sell_last_block(rr, 0.0, partials, &st->counter[3], &trr, &unused) && threadIdx.x == 0) {
+    const double nrm = sqrt(trr);
+    st->true_rel = st->b_norm > 0.0 ? nrm / st->b_norm : 0.0;
+    st->resid = nrm;
+    if (!first) st->n_updates += 1;
+    if (!isfinite(nrm)) st->done = FGB_PCG_NONFINITE;
+    else if (nrm <= st->tol) st->done = FGB_PCG_RTOL;
+    else if (st->niter >= st->maxit) st->done = FGB_PCG_MAXIT;
+  }
+}
+
+// reliable update part 3: r = float(r64), z = Dinv r ; restart p on the first call
+__global__ void __launch_bounds__(kSellThreads) sell_mixed_replace(int64_t n, const double* __restrict__ dinv64,
+                                                                   const double* __restrict__ r64,
+                                                                   float* __restrict__ r, float* __restrict__ z,
+                                                                   float* __restrict__ p, float* __restrict__ dinv32,
+                                                                   double* partials, SellPcgState* st, int first) {
+  if (!first && (st->done || !st->need_update)) return;
+  double rz = 0.0, rr = 0.0;
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const float ri = static_cast<float>(r64[i]);
+    const float di = first ? static_cast<float>(dinv64[i]) : dinv32[i];
+    if (first) dinv32[i] = di;
+    const float zi = di * ri;
+    r[i] = ri;
+    z[i] = zi;
+    if (first) p[i] = zi;
+    rz += static_cast<double>(ri) * static_cast<double>(zi);
+    rr += static_cast<double>(ri) * static_cast<double>(ri);
+  }
+  double trz, trr;
+  if (sell_last_block(rz, rr, partials, &st->counter[0], &trz, &trr) && threadIdx.x == 0) {
+    st->beta = first ? 0.0 : trz / st->rz_prev;
+    st->rz = trz;
+    st->rr = trr;
+    st->r_upd = sqrt(trr);
+    st->need_update = 0;
+  }
+}
+
+// Loop control of the graph driver: one thread.  Clears the while condition
+// when the solve is finished, and in any case after trip_cap body executions,
+// so the device loop always ends.
+__global__ void sell_loop_ctl(SellPcgState* st, cudaGraphConditionalHandle handle) {
+  st->trips += 1;
+  if (st->trips >= st->trip_cap && !st->done) st->done = FGB_PCG_MAXIT;
+  if (st->done) cudaGraphSetConditional(handle, 0);
+}
+
+}  // namespace fgb
+
+using namespace fgb;
+
+namespace {
+
+int sell_grid(int64_t n_slices) { return grid_for(n_slices * 32, kSellThreads, kSellMaxBlocks); }
+int vec_grid(int64_t n) { return grid_for(n, kSellThreads, kSellMaxBlocks); }
+
+SellView view_of(const fgb_sell* A) { return SellView{A->n, A->n_slices, A->slice_ptr, A->perm, A->col}; }
+
+struct EventPairs {
+  bool on;
+  int cap;
+  cudaEvent_t* ev = nullptr;
+  double ms = 0.0;
+  int64_t launches = 0;
+  EventPairs(bool enable, int c) : on(enable), cap(c) {
+    if (!on) return;
+    ev = new cudaEvent_t[2 * cap];
+    for (int k = 0; k < 2 * cap; ++k) cudaEventCreate(&ev[k]);
+  }
+  ~EventPairs() {
+    if (!ev) return;
+    for (int k = 0; k < 2 * cap; ++k) cudaEventDestroy(ev[k]);
+    delete[] ev;
+  }
+  cudaEvent_t a(int k) const { return on ? ev[2 * k] : nullptr; }
+  cudaEvent_t b(int k) const { return on ? ev[2 * k + 1] : nullptr; }
+  void collect(int64_t executed) {
+    if (!on) return;
+    for (int64_t k = 0; k < executed && k < cap; ++k) {
+      float t = 0.f;
+      if (cudaEventElapsedTime(&t, ev[2 * k], ev[2 * k + 1]) == cudaSuccess) { ms += t; ++launches; }
+    }
+  }
+};
+
+struct F64Work {
+  SellPcgState* st;
+  double* partials;
+  double *r, *z, *p0, *p1, *Ap;
+};
+
+struct MixedWork {
+  SellPcgState* st;
+  double* partials;
+  float *r, *z, *p0, *p1, *Ap, *y, *dinv32;
+  double* r64;
+};
+
+bool carve_f64(Carver& cv, int64_t n, F64Work& w) {
+  w.st = cv.take<SellPcgState>(1);
+  w.partials = cv.take<double>(2 * kSellMaxBlocks);
+  w.r = cv.take<double>(n); w.z = cv.take<double>(n); w.p0 = cv.take<double>(n); w.p1 = cv.take<double>(n);
+  w.Ap = cv.take<double>(n);
+  return cv.ok;
+}
+
+bool carve_mixed(Carver& cv, int64_t n, MixedWork& w) {
+  w.st = cv.take<SellPcgState>(1);
+  w.partials = cv.take<double>(2 * kSellMaxBlocks);
+  w.r = cv.take<float>(n); w.z = cv.take<float>(n); w.p0 = cv.take<float>(n); w.p1 = cv.take<float>(n);
+  w.Ap = cv.take<float>(n); w.y = cv.take<float>(n); w.dinv32 = cv.take<float>(n);
+  w.r64 = cv.take<double>(n);
+  return cv.ok;
+}
+
+// one CG iteration (FP64): ping-pong p by parity
+void f64_body(const SellView& A, const double* val, const double* dinv, double* x, F64Work& w, int parity,
+              cudaEvent_t e0, cudaEvent_t e1, cudaStream_t s) {
+  double* p_old = parity ? w.p1 : w.p0;
+  double* p_new = parity ? w.p0 : w.p1;
+  if (e0) cudaEventRecord(e0, s);
+  sell_pcg_spmv<double><<<sell_grid(A.n_slices), kSellThreads, 0, s>>>(A, val, w.z, p_old, p_new, w.Ap, w.partials, w.st);
+  if (e1) cudaEventRecord(e1, s);
+  sell_pcg_update_f64<<<vec_grid(A.n), kSellThreads, 0, s>>>(A.n, dinv, p_new, w.Ap, x, w.r, w.z, w.partials, w.st);
+}
+
+void mixed_body(const SellView& A, const float* val32, const double* val64, const double* dinv64, const double* b,
+                double* x, MixedWork& w, double delta, int parity, cudaEvent_t e0, cudaEvent_t e1, cudaStream_t s) {
+  float* p_old = parity ? w.p1 : w.p0;
+  float* p_new = parity ? w.p0 : w.p1;
+  if (e0) cudaEventRecord(e0, s);
+  sell_pcg_spmv<float><<<sell_grid(A.n_slices), kSellThreads, 0, s>>>(A, val32, w.z, p_old, p_new, w.Ap, w.partials, w.st);
+  if (e1) cudaEventRecord(e1, s);
+  sell_mixed_update<<<vec_grid(A.n), kSellThreads, 0, s>>>(A.n, w.dinv32, p_new, w.Ap, w.y, w.r, w.z, w.partials, w.st, delta);
+  sell_mixed_fold<<<vec_grid(A.n), kSellThreads, 0, s>>>(A.n, x, w.y, w.st, 0);
+  sell_mixed_residual<<<sell_grid(A.n_slices), kSellThreads, 0, s>>>(A, val64, b, x, w.r64, w.partials, w.st, 0);
+  sell_mixed_replace<<<vec_grid(A.n), kSellThreads, 0, s>>>(A.n, dinv64, w.r64, w.r, w.z, p_new, w.dinv32, w.partials, w.st, 0);
+}
+
+template <typename Body>
+int graph_loop(Body body_two_iters, SellPcgState* st, cudaStream_t s, int64_t* launches) {
+  // Build: while(cond) { two iterations ; loop_ctl }.  Two iterations per trip
+  // keep the p ping-pong parity fixed inside the body.
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t ge = nullptr;
+  cudaGraphConditionalHandle h;
+  int rc = FGB_OK;
+  if (cudaGraphCreate(&g, 0) != cudaSuccess) return FGB_ERR_CUDA;
+  if (cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault) != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return FGB_ERR_CUDA;
+  }
+  cudaGraphNodeParams cp = {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = h;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t node;
+  if (cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp) != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return FGB_ERR_CUDA;
+  }
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  cudaStream_t cs;
+  cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+  if (cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+    rc = FGB_ERR_CUDA;
+  } else {
+    body_two_iters(cs);
+    sell_loop_ctl<<<1, 1, 0, cs>>>(st, h);
+    cudaGraph_t out = nullptr;
+    if (cudaStreamEndCapture(cs, &out) != cudaSuccess) rc = FGB_ERR_CUDA;
+  }
+  if (rc == FGB_OK && cudaGraphInstantiate(&ge, g, 0) != cudaSuccess) rc = FGB_ERR_CUDA;
+  if (rc == FGB_OK && cudaGraphLaunch(ge, s) != cudaSuccess) rc = FGB_ERR_CUDA;
+  if (rc == FGB_OK && cudaStreamSynchronize(s) != cudaSuccess) rc = FGB_ERR_CUDA;
+  if (ge) cudaGraphExecDestroy(ge);
+  cudaGraphDestroy(g);
+  cudaStreamDestroy(cs);
+  (void)launches;
+  return rc;
+}
+
+int read_state(SellPcgState* d, SellPcgState* h, cudaStream_t s) {
+  if (cudaMemcpyAsync(h, d, sizeof(SellPcgState), cudaMemcpyDeviceToHost, s) != cudaSuccess) return FGB_ERR_CUDA;
+  if (cudaStreamSynchronize(s) != cudaSuccess) return FGB_ERR_CUDA;
+  return FGB_OK;
+}
+
+int set_tol(SellPcgState* d, double tol, cudaStream_t s) {
+  return cudaMemcpyAsync(reinterpret_cast<char*>(d) + offsetof(SellPcgState, tol), &tol, sizeof(double),
+                         cudaMemcpyHostToDevice, s) == cudaSuccess ? FGB_OK : FGB_ERR_CUDA;
+}
+
+int finish(int done) {
+  return done == FGB_PCG_BREAKDOWN ? FGB_ERR_BREAKDOWN : (done == FGB_PCG_NONFINITE ? FGB_ERR_NONFINITE : FGB_OK);
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t fgb_sell_workspace_bytes(int64_t n) {
+  const int64_t ns = (n + kSellC - 1) / kSellC;
+  return align_up(static_cast<size_t>(ns) * sizeof(int32_t)) + scan_workspace_bytes(ns);
+}
+
+int64_t fgb_sell_slots(int64_t n) {
+  return ((n + kSellWindow - 1) / kSellWindow) * kSellWindow;
+}
+
+int32_t fgb_sell_plan(int64_t n, const int64_t* indptr, int32_t* perm, int64_t* slice_ptr, void* workspace,
+                      size_t workspace_bytes, void* stream) {
+  if (n <= 0 || !indptr || !perm || !slice_ptr) return FGB_ERR_ARG;
+  if (n >= (int64_t(1) << 31)) return FGB_ERR_CAPACITY;
+  if (!workspace || workspace_bytes < fgb_sell_workspace_bytes(n)) return FGB_ERR_WORKSPACE;
+  cudaStream_t st = as_stream(stream);
+  const int64_t windows = (n + kSellWindow - 1) / kSellWindow;
+  const int64_t slices = windows * (kSellWindow / kSellC);
+  Carver cv(workspace, workspace_bytes);
+  int32_t* entries = cv.take<int32_t>(slices);
+  void* scan_ws = cv.base + cv.off;
+  size_t scan_bytes = workspace_bytes - cv.off;
+  sell_sort_windows<<<static_cast<unsigned>(windows), kSellWindow, 0, st>>>(n, indptr, perm, entries);
+  return exclusive_scan_i32_to_i64(entries, slices, slice_ptr, scan_ws, scan_bytes, st);
+}
+
+int32_t fgb_sell_fill(int64_t n, const int64_t* indptr, const int32_t* indices, const double* values64,
+                      const float* values32, const int32_t* perm, const int64_t* slice_ptr, int32_t* col,
+                      double* val64, float* val32, void* stream) {
+  if (n <= 0 || !indptr || !indices || !perm || !slice_ptr || !col) return FGB_ERR_ARG;
+  if ((val64 && !values64) || (val32 && !values64 && !values32)) return FGB_ERR_ARG;
+  const int64_t slices = fgb_sell_slots(n) / kSellC;
+  sell_fill_kernel<<<grid_for(slices * 32, 256, kNumSMs * 16), 256, 0, as_stream(stream)>>>(
+      slices, slice_ptr, perm, indptr, indices, values64, values32, col, val64, val32);
+  return launch_status();
+}
+
+int32_t fgb_sell_spmv(int32_t dtype, const fgb_sell* A, const void* x, void* y, void* stream) {
+  if (!A || !x || !y || A->n <= 0) return FGB_ERR_ARG;
+  SellView v = view_of(A);
+  cudaStream_t st = as_stream(stream);
+  if (dtype == FGB_F64) {
+    if (!A->val64) return FGB_ERR_ARG;
+    sell_spmv_kernel<double><<<sell_grid(v.n_slices), kSellThreads, 0, st>>>(v, A->val64, static_cast<const double*>(x),
+                                                                            static_cast<double*>(y));
+  } else if (dtype == FGB_F32) {
+    if (!A->val32) return FGB_ERR_ARG;
+    sell_spmv_kernel<float><<<sell_grid(v.n_slices), kSellThreads, 0, st>>>(v, A->val32, static_cast<const float*>(x),
+                                                                           static_cast<float*>(y));
+  } else {
+    return FGB_ERR_ARG;
+  }
+  return launch_status();
+}
+
+size_t fgb_pcg_sell_workspace_bytes(int64_t n) {
+  // sized for the larger (mixed) layout
+  return align_up(sizeof(SellPcgState)) + align_up(2 * kSellMaxBlocks * sizeof(double)) +
+         5 * align_up(static_cast<size_t>(n) * sizeof(double)) + 7 * align_up(static_cast<size_t>(n) * sizeof(float));
+}
+
+int32_t fgb_pcg_sell_f64(const fgb_sell* A, const double* diag_inv, const double* b, double* x, double atol,
+                         double rtol, int64_t maxit, int32_t check_every, int32_t norm, int32_t use_graph,
+                         int32_t profile, void* workspace, size_t workspace_bytes, fgb_pcg_info* info,
+                         void* stream) {
+  if (!A || A->n <= 0 || !A->val64 || !b || !x || maxit <= 0) return FGB_ERR_ARG;
+  if (!workspace || workspace_bytes < fgb_pcg_sell_workspace_bytes(A->n)) return FGB_ERR_WORKSPACE;
+  if (check_every <= 0) check_every = 16;
+  if (use_graph) profile = 0;
+  cudaStream_t s = as_stream(stream);
+  SellView v = view_of(A);
+  const int64_t n = A->n;
+  Carver cv(workspace, workspace_bytes);
+  F64Work w;
+  if (!carve_f64(cv, n, w)) return FGB_ERR_WORKSPACE;
+  SellPcgState h{};
+  h.atol = atol;
+  h.maxit = maxit;
+  h.norm_rr = norm;
+  h.trip_cap = maxit / 2 + 2;
+  int64_t launches = 0;
+  cudaMemcpyAsync(w.st, &h, sizeof(SellPcgState), cudaMemcpyHostToDevice, s);
+  sell_pcg_init<double><<<sell_grid(v.n_slices), kSellThreads, 0, s>>>(v, A->val64, diag_inv, b, x, w.r, w.z, w.p0,
+                                                                       w.partials, w.st);
+  ++launches;
+  int rc = read_state(w.st, &h, s);
+  if (rc) return rc;
+  EventPairs prof(profile != 0, check_every);
+  if (h.done == FGB_PCG_ZERO_RHS) {
+    cudaMemsetAsync(x, 0, n * sizeof(double), s);
+  } else {
+    if ((rc = set_tol(w.st, rtol * h.b_norm, s))) return rc;
+    if (use_graph) {
+      rc = graph_loop([&](cudaStream_t cs) {
+        f64_body(v, A->val64, diag_inv, x, w, 0, nullptr, nullptr, cs);
+        f64_body(v, A->val64, diag_inv, x, w, 1, nullptr, nullptr, cs);
+      }, w.st, s, &launches);
+      if (rc) return rc;
+      if ((rc = read_state(w.st, &h, s))) return rc;
+      launches += 5 * ((h.niter + 1) / 2 + 1);
+    } else {
+      int64_t it = 0;
+      while (true) {
+        const int64_t before = h.niter;
+        for (int k = 0; k < check_every; ++k, ++it) f64_body(v, A->val64, diag_inv, x, w, static_cast<int>(it & 1), prof.a(k), prof.b(k), s);
+        launches += 2 * check_every;
+        if (cudaGetLastError() != cudaSuccess) return FGB_ERR_CUDA;
+        if ((rc = read_state(w.st, &h, s))) return rc;
+        prof.collect(h.niter - before);
+        if (h.done) break;
+      }
+    }
+  }
+  if (info) {
+    info->niter = h.niter; info->residual = h.resid; info->b_norm = h.b_norm; info->true_relres = -1.0;
+    info->reason = h.done; info->n_updates = 0; info->launches = launches; info->kernel_ms = prof.ms;
+    info->kernel_launches = prof.launches;
+  }
+  return finish(h.done);
+}
+
+int32_t fgb_pcg_sell_mixed(const fgb_sell* A, const double* diag_inv64, const double* b, double* x, double rtol,
+                           double delta, int64_t maxit, int32_t check_every, int32_t use_graph, int32_t profile,
+                           void* workspace, size_t workspace_bytes, fgb_pcg_info* info, void* stream) {
+  if (!A || A->n <= 0 || !A->val64 || !A->val32 || !diag_inv64 || !b || !x || maxit <= 0) return FGB_ERR_ARG;
+  if (!(delta > 0.0 && delta < 1.0)) return FGB_ERR_ARG;
+  if (!workspace || workspace_bytes < fgb_pcg_sell_workspace_bytes(A->n)) return FGB_ERR_WORKSPACE;
+  if (check_every <= 0) check_every = 16;
+  if (use_graph) profile = 0;
+  cudaStream_t s = as_stream(stream);
+  SellView v = view_of(A);
+  const int64_t n = A->n;
+  Carver cv(workspace, workspace_bytes);
+  MixedWork w;
+  if (!carve_mixed(cv, n, w)) return FGB_ERR_WORKSPACE;
+  SellPcgState h{};
+  h.maxit = maxit;
+  h.norm_rr = 1;
+  h.trip_cap = maxit / 2 + 2;
+  int64_t launches = 0;
+  cudaMemcpyAsync(w.st, &h, sizeof(SellPcgState), cudaMemcpyHostToDevice, s);
+  cudaMemsetAsync(w.y, 0, n * sizeof(float), s);
+  // ||b|| from the init kernel (r, z, p all alias r64: it stores the same value thrice)
+  sell_pcg_init<double><<<sell_grid(v.n_slices), kSellThreads, 0, s>>>(v, A->val64, nullptr, b, x, w.r64, w.r64,
+                                                                       w.r64, w.partials, w.st);
+  ++launches;
+  int rc = read_state(w.st, &h, s);
+  if (rc) return rc;
+  EventPairs prof(profile != 0, check_every);
+  if (h.done == FGB_PCG_ZERO_RHS) {
+    cudaMemsetAsync(x, 0, n * sizeof(double), s);
+  } else {
+    if ((rc = set_tol(w.st, rtol * h.b_norm, s))) return rc;
+    sell_mixed_residual<<<sell_grid(v.n_slices), kSellThreads, 0, s>>>(v, A->val64, b, x, w.r64, w.partials, w.st, 1);
+    sell_mixed_replace<<<vec_grid(n), kSellThreads, 0, s>>>(n, diag_inv64, w.r64, w.r, w.z, w.p0, w.dinv32, w.partials,
+                                                          w.st, 1);
+    launches += 2;
+    if (use_graph) {
+      rc = graph_loop([&](cudaStream_t cs) {
+        mixed_body(v, A->val32, A->val64, diag_inv64, b, x, w, delta, 0, nullptr, nullptr, cs);
+        mixed_body(v, A->val32, A->val64, diag_inv64, b, x, w, delta, 1, nullptr, nullptr, cs);
+      }, w.st, s, &launches);
+      if (rc) return rc;
+      if ((rc = read_state(w.st, &h, s))) return rc;
+      launches += 11 * ((h.niter + 1) / 2 + 1);
+    } else {
+      int64_t it = 0;
+      while (true) {
+        const int64_t before = h.niter;
+        for (int k = 0; k < check_every; ++k, ++it)
+          mixed_body(v, A->val32, A->val64, diag_inv64, b, x, w, delta, static_cast<int>(it & 1), prof.a(k), prof.b(k), s);
+        launches += 5 * check_every;
+        if (cudaGetLastError() != cudaSuccess) return FGB_ERR_CUDA;
+        if ((rc = read_state(w.st, &h, s))) return rc;
+        prof.collect(h.niter - before);
+        if (h.done) break;
+      }
+    }
+  }
+  if (info) {
+    info->niter = h.niter; info->residual = h.resid; info->b_norm = h.b_norm; info->true_relres = h.true_rel;
+    info->reason = h.done; info->n_updates = h.n_updates; info->launches = launches; info->kernel_ms = prof.ms;
+    info->kernel_launches = prof.launches;
+  }
+  return finish(h.done);
+}
+
+}  // extern "C"

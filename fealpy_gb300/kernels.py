@@ -218,3 +218,72 @@ def gather_sum(adj_ptr, adj, local: torch.Tensor, out: Optional[torch.Tensor] = 
     y = out if out is not None else torch.empty(n, dtype=local.dtype, device=dev)
     call("fgb_gather_sum", dtype_code(local.dtype), n, ptr(adj_ptr), ptr(adj), ptr(local), ptr(y), stream_ptr(dev))
     return y
+
+
+class SellMatrix:
+    """Device SELL-32 copy of a CSR matrix (tensors kept alive here) and the
+    ``fgb_sell`` descriptor pointing at them."""
+
+    def __init__(self, n, n_slices, slice_ptr, perm, col, val64, val32):
+        self.n, self.n_slices = n, n_slices
+        self.slice_ptr, self.perm, self.col, self.val64, self.val32 = slice_ptr, perm, col, val64, val32
+        self.desc = _lib.SellDesc(n, n_slices, slice_ptr.data_ptr(), perm.data_ptr(), col.data_ptr(),
+                                  val64.data_ptr() if val64 is not None else None,
+                                  val32.data_ptr() if val32 is not None else None)
+
+    @property
+    def padded_nnz(self):
+        return self.col.numel()
+
+
+def sell_build(indptr, indices, values64=None, values32=None, want64=True, want32=False) -> SellMatrix:
+    """SELL-32 copy of a CSR matrix (one host read for the padded size)."""
+    dev = _dev(indptr)
+    n = indptr.numel() - 1
+    lib = _lib.lib()
+    slots = int(lib.fgb_sell_slots(n))
+    n_slices = slots // 32
+    perm = torch.empty(slots, dtype=torch.int32, device=dev)
+    slice_ptr = torch.empty(n_slices + 1, dtype=torch.int64, device=dev)
+    ws = workspace(lib.fgb_sell_workspace_bytes(n), dev)
+    call("fgb_sell_plan", n, ptr(indptr), ptr(perm), ptr(slice_ptr), ptr(ws), ws.numel(), stream_ptr(dev))
+    total = int(slice_ptr[n_slices].item())
+    col = torch.empty(max(total, 1), dtype=torch.int32, device=dev)
+    v64 = torch.empty(max(total, 1), dtype=torch.float64, device=dev) if want64 else None
+    v32 = torch.empty(max(total, 1), dtype=torch.float32, device=dev) if want32 else None
+    call("fgb_sell_fill", n, ptr(indptr), ptr(indices), ptr(values64), ptr(values32), ptr(perm), ptr(slice_ptr),
+         ptr(col), ptr(v64), ptr(v32), stream_ptr(dev))
+    return SellMatrix(n, n_slices, slice_ptr, perm, col, v64, v32)
+
+
+def sell_spmv(S: SellMatrix, x, dtype=torch.float64):
+    dev = S.col.device
+    y = torch.empty(S.n, dtype=dtype, device=dev)
+    x = x.to(dev, dtype).contiguous()
+    call("fgb_sell_spmv", dtype_code(dtype), ctypes.byref(S.desc), ptr(x), ptr(y), stream_ptr(dev))
+    return y
+
+
+def pcg_sell_f64(S: SellMatrix, dinv, b, x, atol, rtol, maxit, check_every=16, norm=0, graph=True, profile=False):
+    dev = S.col.device
+    lib = _lib.lib()
+    ws = workspace(lib.fgb_pcg_sell_workspace_bytes(S.n), dev)
+    info = _lib.PcgInfo()
+    call("fgb_pcg_sell_f64", ctypes.byref(S.desc), ptr(dinv), ptr(b), ptr(x), float(atol), float(rtol), int(maxit),
+         int(check_every), int(norm), int(bool(graph)), int(bool(profile)), ptr(ws), ws.numel(), ctypes.byref(info),
+         stream_ptr(dev))
+    _lib.add_launches(info.launches)
+    return info
+
+
+def pcg_sell_mixed(S: SellMatrix, dinv64, b, x, rtol, delta=0.1, maxit=100000, check_every=32, graph=True,
+                   profile=False):
+    dev = S.col.device
+    lib = _lib.lib()
+    ws = workspace(lib.fgb_pcg_sell_workspace_bytes(S.n), dev)
+    info = _lib.PcgInfo()
+    call("fgb_pcg_sell_mixed", ctypes.byref(S.desc), ptr(dinv64), ptr(b), ptr(x), float(rtol), float(delta),
+         int(maxit), int(check_every), int(bool(graph)), int(bool(profile)), ptr(ws), ws.numel(), ctypes.byref(info),
+         stream_ptr(dev))
+    _lib.add_launches(info.launches)
+    return info

@@ -48,14 +48,28 @@ def _info_dict(info, extra=None):
     return out
 
 
+def _sell_of(A: CSRTensor, want32: bool):
+    """SELL-32 copy of A for the solvers (cached on the matrix)."""
+    S = getattr(A, "_sell", None)
+    if S is None or (want32 and S.val32 is None):
+        v32 = A._f32 if (want32 and A._f32 is not None) else None
+        S = K.sell_build(A.crow, A.col, A.values.to(torch.float64).contiguous(), v32, want64=True, want32=want32)
+        A._sell = S
+    return S
+
+
 def cg(A, b: torch.Tensor, x0: Optional[torch.Tensor] = None, M=None, *, batch_first: bool = False,
        atol: float = 1e-12, rtol: float = 1e-8, maxit: Optional[int] = 10000, returninfo: bool = False,
-       check_every: int = 16, lanes_per_row: int = 0, stop: str = "preconditioned", profile: bool = False):
+       check_every: int = 16, lanes_per_row: int = 0, stop: str = "preconditioned", profile: bool = False,
+       solver_format: str = "sell", graph: bool = True):
     """Solve ``A x = b`` by (preconditioned) CG; see module docstring.
 
     ``stop='preconditioned'`` (default) is FEALPy's test on ``sqrt(r.z)``;
     ``stop='residual'`` tests the 2-norm of the iterated residual instead.
-    ``profile`` records CUDA-event times of the SpMV kernel into the info."""
+    ``solver_format='sell'`` (default) iterates on a SELL-32 copy of ``A``
+    ('csr' iterates on the CSR arrays); ``graph`` runs the iterations as a
+    device-side CUDA-graph loop.  ``profile`` records CUDA-event times of the
+    SpMV kernel into the info (host-polled loop)."""
     if not isinstance(b, torch.Tensor):
         raise AssertionError("b must be a Tensor")
     if b.ndim not in (1, 2):
@@ -66,17 +80,23 @@ def cg(A, b: torch.Tensor, x0: Optional[torch.Tensor] = None, M=None, *, batch_f
         raise NotImplementedError("cg on the GB300 path takes a CSRTensor matrix")
     if b.ndim == 2:
         raise NotImplementedError("multi-right-hand-side cg is not provided on the GB300 path")
+    if stop not in ("preconditioned", "residual"):
+        raise ValueError("stop must be 'preconditioned' or 'residual'")
     dinv = _diag_inv_of(M)
     b = b.to(dtype=torch.float64).contiguous()
     x = torch.zeros_like(b) if x0 is None else x0.to(torch.float64).clone()
-    if stop not in ("preconditioned", "residual"):
-        raise ValueError("stop must be 'preconditioned' or 'residual'")
-    info = K.pcg_f64(A.crow, A.col, A.values.to(torch.float64), dinv, b, x, atol, rtol,
-                     maxit if maxit is not None else 2 ** 62, check_every, lanes_per_row,
-                     0 if stop == "preconditioned" else 1, profile)
+    maxit = maxit if maxit is not None else 2 ** 62
+    norm = 0 if stop == "preconditioned" else 1
+    if solver_format == "sell":
+        S = _sell_of(A, want32=False)
+        info = K.pcg_sell_f64(S, dinv, b, x, atol, rtol, maxit, check_every, norm, graph and not profile, profile)
+    elif solver_format == "csr":
+        info = K.pcg_f64(A.crow, A.col, A.values.to(torch.float64), dinv, b, x, atol, rtol, maxit, check_every,
+                         lanes_per_row, norm, profile)
+    else:
+        raise ValueError("solver_format must be 'sell' or 'csr'")
     out = _info_dict(info)
-    reason = info.reason
-    if reason == 3:
+    if info.reason == 3:
         logger.info(f"CG: failed, stopped by maxit ({maxit}).")
     if returninfo:
         return x, out
@@ -85,7 +105,7 @@ def cg(A, b: torch.Tensor, x0: Optional[torch.Tensor] = None, M=None, *, batch_f
 
 def cg_mixed(A: CSRTensor, b: torch.Tensor, x0: Optional[torch.Tensor] = None, M=None, *, rtol: float = 1e-10,
              delta: float = 0.1, maxit: int = 100000, returninfo: bool = False, check_every: int = 32,
-             lanes_per_row: int = 0, profile: bool = False):
+             lanes_per_row: int = 0, profile: bool = False, solver_format: str = "sell", graph: bool = True):
     """FP32 Jacobi-PCG iterations with FP64 reliable updates; stops on the true
     FP64 relative residual.  ``M`` must be None (Jacobi from ``A`` is used) or
     the diagonal CSR of ``JacobiPreconditioner``."""
@@ -96,8 +116,14 @@ def cg_mixed(A: CSRTensor, b: torch.Tensor, x0: Optional[torch.Tensor] = None, M
         dinv = A.diagonal_inverse()
     b = b.to(dtype=torch.float64).contiguous()
     x = torch.zeros_like(b) if x0 is None else x0.to(torch.float64).clone()
-    info = K.pcg_mixed(A.crow, A.col, A.values, A.values_f32(), dinv, b, x, rtol, delta, maxit, check_every,
-                       lanes_per_row, profile)
+    if solver_format == "sell":
+        S = _sell_of(A, want32=True)
+        info = K.pcg_sell_mixed(S, dinv, b, x, rtol, delta, maxit, check_every, graph and not profile, profile)
+    elif solver_format == "csr":
+        info = K.pcg_mixed(A.crow, A.col, A.values, A.values_f32(), dinv, b, x, rtol, delta, maxit, check_every,
+                           lanes_per_row, profile)
+    else:
+        raise ValueError("solver_format must be 'sell' or 'csr'")
     out = _info_dict(info, {"relres": info.true_relres, "n_updates": int(info.n_updates)})
     if returninfo:
         return x, out

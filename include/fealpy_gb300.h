@@ -233,6 +233,48 @@ int32_t fgb_pcg_mixed(int64_t n, const int64_t* indptr, const int32_t* indices,
                       void* workspace, size_t workspace_bytes, fgb_pcg_info* info_host,
                       void* stream);
 
+/* ---- SELL-32 solver copy ------------------------------------------------- */
+
+/* Sliced-ELLPACK copy of a CSR matrix used by the SELL solvers: slices of 32
+ * rows (rows sorted by length inside windows of 256), entries column-major
+ * inside a slice, zero padding.  perm maps slot -> row (-1 = padding). */
+typedef struct fgb_sell {
+  int64_t n;                /* rows                                           */
+  int64_t n_slices;         /* fgb_sell_slots(n) / 32                         */
+  const int64_t* slice_ptr; /* n_slices + 1 entry offsets                     */
+  const int32_t* perm;      /* fgb_sell_slots(n) slot -> row                  */
+  const int32_t* col;       /* slice_ptr[n_slices] column indices             */
+  const double* val64;      /* FP64 values (optional)                         */
+  const float* val32;       /* FP32 values (optional)                         */
+} fgb_sell;
+
+/* No FEALPy counterpart: a solver-side layout of CSRTensor (the matrix the
+ * reference hands to fealpy/solver/cg.py).  plan: perm + slice_ptr (one
+ * host read of slice_ptr[n_slices] then sizes col/val); fill: col/val. */
+int64_t fgb_sell_slots(int64_t n);
+size_t fgb_sell_workspace_bytes(int64_t n);
+int32_t fgb_sell_plan(int64_t n, const int64_t* indptr, int32_t* perm, int64_t* slice_ptr,
+                      void* workspace, size_t workspace_bytes, void* stream);
+int32_t fgb_sell_fill(int64_t n, const int64_t* indptr, const int32_t* indices,
+                      const double* values64, const float* values32, const int32_t* perm,
+                      const int64_t* slice_ptr, int32_t* col, double* val64, float* val32,
+                      void* stream);
+int32_t fgb_sell_spmv(int32_t dtype, const fgb_sell* A, const void* x, void* y, void* stream);
+
+/* Jacobi-PCG on a SELL copy: same iteration, stopping rules and info as
+ * fgb_pcg_f64 / fgb_pcg_mixed.  use_graph != 0 runs the iterations as a CUDA
+ * graph with a device-side while loop (no host polling; profile ignored). */
+size_t fgb_pcg_sell_workspace_bytes(int64_t n);
+int32_t fgb_pcg_sell_f64(const fgb_sell* A, const double* diag_inv, const double* b, double* x,
+                         double atol, double rtol, int64_t maxit, int32_t check_every,
+                         int32_t norm, int32_t use_graph, int32_t profile, void* workspace,
+                         size_t workspace_bytes, fgb_pcg_info* info_host, void* stream);
+int32_t fgb_pcg_sell_mixed(const fgb_sell* A, const double* diag_inv64, const double* b,
+                           double* x, double rtol, double delta, int64_t maxit,
+                           int32_t check_every, int32_t use_graph, int32_t profile,
+                           void* workspace, size_t workspace_bytes, fgb_pcg_info* info_host,
+                           void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -274,3 +274,42 @@ def test_full_size_properties():
     a = float(torch.dot(y, A @ x))
     b = float(torch.dot(x, A @ y))
     assert abs(a - b) <= 1e-12 * max(abs(a), 1.0) * 10
+
+
+def test_sell_copy_spmv_and_solver_drivers(golden_dir):
+    """The SELL-32 solver copy: SpMV against scipy, and the graph-driven loop
+    against the host-polled loop (same kernels, bitwise-equal iterates)."""
+    dev = cuda()
+    import scipy.sparse as sp
+    import fealpy_gb300 as F
+    from fealpy_gb300 import kernels as K
+    from fealpy_gb300.sparse import CSRTensor
+    for name in ("small_tet_p2.npz", "small_tri_p3.npz", "c1_poisson_tri_p1_64.npz"):
+        z = load(golden_dir, name)
+        crow, col, val = z["crow"], z["col"], z["val"]
+        n = len(crow) - 1
+        t = lambda a, dt=None: torch.as_tensor(a, device=dev, dtype=dt)
+        S = K.sell_build(t(crow), t(col), t(val), None, want64=True, want32=True)
+        assert S.padded_nnz >= len(col)
+        x = np.random.default_rng(1).normal(size=n)
+        ref = sp.csr_matrix((val, col, crow), shape=(n, n)) @ x
+        assert rel_err(K.sell_spmv(S, t(x), torch.float64), ref) < 1e-14
+        assert rel_err(K.sell_spmv(S, t(x, torch.float32), torch.float32), ref) < 1e-5
+    z = load(golden_dir, "c1_poisson_tri_p1_64.npz")
+    A = CSRTensor(torch.as_tensor(z["bc_crow"], device=dev), torch.as_tensor(z["bc_col"], device=dev),
+                  torch.as_tensor(z["bc_val"], device=dev), (len(z["bc_crow"]) - 1,) * 2)
+    b = torch.as_tensor(z["bc_F"], device=dev)
+    M = F.JacobiPreconditioner().apply(A)
+    xs = {}
+    for fmt, graph in (("sell", True), ("sell", False), ("csr", False)):
+        x, info = F.cg(A, b, M=M, atol=1e-30, rtol=1e-10, returninfo=True, solver_format=fmt, graph=graph)
+        assert abs(info["niter"] - int(z["niter"])) <= 1, (fmt, graph, info["niter"])
+        assert rel_err(x, z["uh"]) < 1e-9
+        xs[(fmt, graph)] = x
+    assert torch.equal(xs[("sell", True)], xs[("sell", False)])
+    xm = {}
+    for graph in (True, False):
+        x, info = F.cg_mixed(A, b, rtol=1e-10, returninfo=True, graph=graph)
+        assert info["relres"] <= 1e-10 and rel_err(x, z["uh"]) < 1e-8
+        xm[graph] = (x, info["niter"])
+    assert xm[True][1] == xm[False][1] and torch.equal(xm[True][0], xm[False][0])
