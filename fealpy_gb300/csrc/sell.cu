@@ -25,7 +25,16 @@
 namespace fgb {
 
 constexpr int kSellC = 32;        // rows per slice (one warp)
+constexpr int kSellPack = 4;      // consecutive entries of a row stored contiguously
 constexpr int kSellWindow = 256;  // rows sorted together
+
+// Offset of entry k of lane (row slot) `lane` inside its slice: packs of 4
+// entries per lane, lanes interleaved pack by pack, so that pack q of the
+// warp is one contiguous 512-byte (FP32) run and each lane loads its 4
+// entries with a single 16-byte vector load.
+__host__ __device__ __forceinline__ int64_t sell_pos(int lane, int k) {
+  return static_cast<int64_t>(k >> 2) * (kSellC * kSellPack) + lane * kSellPack + (k & 3);
+}
 constexpr int kSellThreads = 256;
 constexpr int kSellMaxBlocks = kNumSMs * 8;
 
@@ -65,8 +74,12 @@ __global__ void sell_sort_windows(int64_t n, const int64_t* __restrict__ indptr,
   const int64_t full = base + static_cast<int64_t>(kk & 0xffffffffu);
   const int64_t slot = base + threadIdx.x;
   perm[slot] = (slen >= 0 && full < n) ? static_cast<int32_t>(full) : -1;
-  // the first slot of a slice holds its longest row: that is the slice width
-  if ((threadIdx.x & 31) == 0) slice_entries[slot / kSellC] = kSellC * (slen > 0 ? slen : 0);
+  // the first slot of a slice holds its longest row: that is the slice width,
+  // rounded up to whole packs of kSellPack entries
+  if ((threadIdx.x & 31) == 0) {
+    const int w = slen > 0 ? slen : 0;
+    slice_entries[slot / kSellC] = kSellC * ((w + kSellPack - 1) / kSellPack) * kSellPack;
+  }
 }
 
 __global__ void sell_fill_kernel(int64_t n_slices, const int64_t* __restrict__ slice_ptr,
@@ -85,7 +98,7 @@ __global__ void sell_fill_kernel(int64_t n_slices, const int64_t* __restrict__ s
     int len = 0;
     if (row >= 0) { rs = indptr[row]; len = static_cast<int>(indptr[row + 1] - rs); }
     for (int k = 0; k < w; ++k) {
-      const int64_t pos = base + static_cast<int64_t>(k) * kSellC + lane;
+      const int64_t pos = base + sell_pos(lane, k);
       const bool real = k < len;
       scol[pos] = real ? indices[rs + k] : (row >= 0 ? row : 0);
       if (s64) s64[pos] = real ? v64[rs + k] : 0.0;
@@ -95,32 +108,105 @@ __global__ void sell_fill_kernel(int64_t n_slices, const int64_t* __restrict__ s
 }
 
 // ------------------------------------------------------------------- SpMV
+// One pack (4 entries of this lane's row): 16-byte streaming loads of the
+// columns and values, then the gathers.
+struct Pack4F {
+  int4 c;
+  float4 v;
+};
+struct Pack4D {
+  int4 c;
+  double2 v01, v23;
+};
+
+__device__ __forceinline__ Pack4F load_pack(const int32_t* col, const float* val, int64_t sbase, int lane, int q) {
+  const int64_t off = sbase + static_cast<int64_t>(q) * (kSellC * kSellPack) + lane * kSellPack;
+  Pack4F p;
+  p.c = __ldcs(reinterpret_cast<const int4*>(col + off));
+  p.v = __ldcs(reinterpret_cast<const float4*>(val + off));
+  return p;
+}
+
+__device__ __forceinline__ Pack4D load_pack(const int32_t* col, const double* val, int64_t sbase, int lane, int q) {
+  const int64_t off = sbase + static_cast<int64_t>(q) * (kSellC * kSellPack) + lane * kSellPack;
+  Pack4D p;
+  p.c = __ldcs(reinterpret_cast<const int4*>(col + off));
+  p.v01 = __ldcs(reinterpret_cast<const double2*>(val + off));
+  p.v23 = __ldcs(reinterpret_cast<const double2*>(val + off + 2));
+  return p;
+}
+
+template <typename T, typename G>
+__device__ __forceinline__ T pack_dot(const Pack4F& p, const G& g, T acc) {
+  acc += p.v.x * g(p.c.x);
+  acc += p.v.y * g(p.c.y);
+  acc += p.v.z * g(p.c.z);
+  acc += p.v.w * g(p.c.w);
+  return acc;
+}
+
+template <typename T, typename G>
+__device__ __forceinline__ T pack_dot(const Pack4D& p, const G& g, T acc) {
+  acc += p.v01.x * g(p.c.x);
+  acc += p.v01.y * g(p.c.y);
+  acc += p.v23.x * g(p.c.z);
+  acc += p.v23.y * g(p.c.w);
+  return acc;
+}
+
+template <typename T> struct PackOf;
+template <> struct PackOf<float> { using type = Pack4F; };
+template <> struct PackOf<double> { using type = Pack4D; };
+
+// Row of slot `lane` of the slice starting at sbase with width w (a multiple of
+// 4): sum over entries, in entry order, of val * g(col).  Two packs per trip
+// keep 32 (FP32) or 48 (FP64) bytes of matrix per lane in flight.
+template <typename T, typename G>
+__device__ __forceinline__ T sell_row(const int32_t* __restrict__ col, const T* __restrict__ val, int64_t sbase, int w,
+                                      int lane, const G& g) {
+  using P = typename PackOf<T>::type;
+  const int nq = w / kSellPack;
+  T acc = T(0);
+  int q = 0;
+  for (; q + 2 <= nq; q += 2) {
+    const P a = load_pack(col, val, sbase, lane, q);
+    const P b = load_pack(col, val, sbase, lane, q + 1);
+    acc = pack_dot<T>(a, g, acc);
+    acc = pack_dot<T>(b, g, acc);
+  }
+  if (q < nq) {
+    const P a = load_pack(col, val, sbase, lane, q);
+    acc = pack_dot<T>(a, g, acc);
+  }
+  return acc;
+}
+
+template <typename T>
+struct GatherX {
+  const T* __restrict__ x;
+  __device__ __forceinline__ T operator()(int32_t j) const { return x[j]; }
+};
+
+// p_new[j] = z[j] + beta * p_old[j], formed on the fly for every gathered column
+template <typename T>
+struct GatherP {
+  const T* __restrict__ z;
+  const T* __restrict__ p;
+  T beta;
+  __device__ __forceinline__ T operator()(int32_t j) const { return z[j] + beta * p[j]; }
+};
+
 template <typename T>
 __global__ void __launch_bounds__(kSellThreads) sell_spmv_kernel(SellView A, const T* __restrict__ val,
                                                                  const T* __restrict__ x, T* __restrict__ y) {
   const int lane = threadIdx.x & 31;
   const int64_t warp = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
   const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+  const GatherX<T> g{x};
   for (int64_t s = warp; s < A.n_slices; s += nwarps) {
-    const int64_t base = A.slice_ptr[s] + lane;
-    const int w = static_cast<int>((A.slice_ptr[s + 1] - A.slice_ptr[s]) >> 5);
-    T acc = T(0);
-    int k = 0;
-    for (; k + 4 <= w; k += 4) {
-      int32_t j[4];
-      T v[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        j[u] = ld_stream(A.col + base + static_cast<int64_t>(k + u) * kSellC);
-        v[u] = ld_stream(val + base + static_cast<int64_t>(k + u) * kSellC);
-      }
-#pragma unroll
-      for (int u = 0; u < 4; ++u) acc += v[u] * __ldg(x + j[u]);
-    }
-    for (; k < w; ++k) {
-      const int64_t p = base + static_cast<int64_t>(k) * kSellC;
-      acc += ld_stream(val + p) * __ldg(x + ld_stream(A.col + p));
-    }
+    const int64_t sbase = A.slice_ptr[s];
+    const int w = static_cast<int>((A.slice_ptr[s + 1] - sbase) >> 5);
+    const T acc = sell_row(A.col, val, sbase, w, lane, g);
     const int32_t row = A.perm[s * kSellC + lane];
     if (row >= 0) y[row] = acc;
   }
@@ -165,52 +251,19 @@ __device__ bool sell_last_block(double v0, double v1, double* partials, unsigned
   return true;
 }
 
-// acc_row = sum_k val * (z[j] + beta p_old[j]) over one SELL row (lane), unrolled.
+// Row of the calling lane: `base` is slice_ptr[s] + lane (as in the callers).
 template <typename T>
 __device__ __forceinline__ T sell_row_dot_p(const SellView& A, const T* __restrict__ val, int64_t base, int w,
                                             const T* __restrict__ z, const T* __restrict__ p_old, T beta) {
-  T acc = T(0);
-  int k = 0;
-  for (; k + 4 <= w; k += 4) {
-    int32_t j[4];
-    T v[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      j[u] = ld_stream(A.col + base + static_cast<int64_t>(k + u) * kSellC);
-      v[u] = ld_stream(val + base + static_cast<int64_t>(k + u) * kSellC);
-    }
-#pragma unroll
-    for (int u = 0; u < 4; ++u) acc += v[u] * (z[j[u]] + beta * p_old[j[u]]);
-  }
-  for (; k < w; ++k) {
-    const int64_t p = base + static_cast<int64_t>(k) * kSellC;
-    const int32_t j = ld_stream(A.col + p);
-    acc += ld_stream(val + p) * (z[j] + beta * p_old[j]);
-  }
-  return acc;
+  const int lane = threadIdx.x & 31;
+  return sell_row(A.col, val, base - lane, w, lane, GatherP<T>{z, p_old, beta});
 }
 
 template <typename T>
 __device__ __forceinline__ T sell_row_dot_x(const SellView& A, const T* __restrict__ val, int64_t base, int w,
                                             const T* __restrict__ x) {
-  T acc = T(0);
-  int k = 0;
-  for (; k + 4 <= w; k += 4) {
-    int32_t j[4];
-    T v[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      j[u] = ld_stream(A.col + base + static_cast<int64_t>(k + u) * kSellC);
-      v[u] = ld_stream(val + base + static_cast<int64_t>(k + u) * kSellC);
-    }
-#pragma unroll
-    for (int u = 0; u < 4; ++u) acc += v[u] * x[j[u]];
-  }
-  for (; k < w; ++k) {
-    const int64_t p = base + static_cast<int64_t>(k) * kSellC;
-    acc += ld_stream(val + p) * x[ld_stream(A.col + p)];
-  }
-  return acc;
+  const int lane = threadIdx.x & 31;
+  return sell_row(A.col, val, base - lane, w, lane, GatherX<T>{x});
 }
 
 #define SELL_WARP_LOOP(A)                                                                   \
