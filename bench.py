@@ -133,25 +133,43 @@ def build_problem(torch, F, node_np, cell_np, kappa_np, dev):
     return mesh, space, kappa, bc
 
 
-def solve_step(torch, F, space, kappa, bc, mode, profile=False):
-    """symbolic + numeric assembly + RHS + Dirichlet + PCG; returns (x, info, A)."""
+STAGES = ("assembly (pattern + values)", "rhs", "dirichlet", "solver copy (SELL)", "pcg")
+
+
+def solve_step(torch, F, space, kappa, bc, mode, profile=False, marks=None):
+    """symbolic + numeric assembly + RHS + Dirichlet + PCG; returns (x, info, A, F).
+    ``marks``: optional list receiving a CUDA event after each stage."""
     from fealpy_gb300.fem import BilinearForm, LinearForm, ScalarDiffusionIntegrator, ScalarMassIntegrator
     from fealpy_gb300.fem import ScalarSourceIntegrator
+    from fealpy_gb300.solver import _sell_of
+
+    def mark():
+        if marks is not None:
+            e = torch.cuda.Event(enable_timing=True)
+            e.record()
+            marks.append(e)
+
+    mark()
     space._cache.clear()
     bf = BilinearForm(space)
     bf.add_integrator(ScalarDiffusionIntegrator(coef=kappa, q=Q), ScalarMassIntegrator(coef=1.0, q=Q))
-    A = bf.assembly(emit_f32=(mode == "mixed"))
+    A = bf.assembly()
+    mark()
     lf = LinearForm(space)
     lf.add_integrator(ScalarSourceIntegrator(1.0, q=Q))
     Fv = lf.assembly()
+    mark()
     A2, F2 = bc.apply(A, Fv)
+    mark()
+    _sell_of(A2, want32=(mode == "mixed"))
+    mark()
     if mode == "mixed":
-        A2._f32 = A2.values.to(torch.float32)
         x, info = F.cg_mixed(A2, F2, rtol=RTOL, maxit=MAXIT, returninfo=True, profile=profile)
     else:
         M = F.JacobiPreconditioner().apply(A2)
         x, info = F.cg(A2, F2, M=M, atol=0.0, rtol=RTOL, maxit=MAXIT, returninfo=True, stop="residual",
                        profile=profile)
+    mark()
     return x, info, A2, F2
 
 
@@ -218,19 +236,24 @@ def run_ours(args):
         relres = float(torch.linalg.norm(r) / torch.linalg.norm(F2))
         # SpMV kernel duration: one more solve with CUDA events around every
         # SpMV launch (host-polled loop, same kernels as the graph loop)
-        _, pinfo, _, _ = solve_step(torch, F, space, kappa, bc, mode, profile=True)
+        marks = []
+        _, pinfo, _, _ = solve_step(torch, F, space, kappa, bc, mode, profile=True, marks=marks)
+        torch.cuda.synchronize(dev)
+        stages = {name: marks[k].elapsed_time(marks[k + 1]) for k, name in enumerate(STAGES)}
         kms = pinfo["kernel_ms"]
         kl = pinfo["kernel_launches"]
         results[mode] = {"ms": ms, "ms_per_step": ms / args.steps, "x": x, "relres": relres,
                          "niter": infos[-1]["niter"], "n_updates": infos[-1].get("n_updates", 0),
                          "kernel_ms_avg": kms / max(kl, 1), "kernel_launches": kl, "launches": launches,
+                         "other_ms_avg": pinfo["other_ms"] / max(kl, 1), "stages_ms": stages,
                          "clocks": clocks, "nnz": A2.nnz, "n": gdof}
 
     if set(modes) != {"fp64", "mixed"} or args.no_e2e:
         # profiling run: report the per-mode timings on stderr only
         for m, r in results.items():
             print(f"[profile run] {m}: {r['ms_per_step']:.3f} ms/step, {r['niter']} iterations, "
-                  f"relres {r['relres']:.3e}, spmv avg {r['kernel_ms_avg'] * 1e3:.1f} us", file=sys.stderr)
+                  f"relres {r['relres']:.3e}, spmv avg {r['kernel_ms_avg'] * 1e3:.1f} us, rest of iteration "
+                  f"{r['other_ms_avg'] * 1e3:.1f} us, stages {json.dumps(r['stages_ms'])}", file=sys.stderr)
         if world > 1:
             dist.destroy_process_group()
         return
@@ -304,9 +327,11 @@ def run_ours(args):
                        "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{world}"},
             "fp32_refined": {"ms_per_step": mixed["ms_per_step"], "dof_per_s": value, "cg_iters": mixed["niter"],
                              "reliable_updates": mixed["n_updates"], "true_relres": mixed["relres"],
-                             "max_rel_err_vs_fp64": err},
+                             "max_rel_err_vs_fp64": err, "stages_ms": mixed["stages_ms"],
+                             "spmv_us": mixed["kernel_ms_avg"] * 1e3, "rest_of_iteration_us": mixed["other_ms_avg"] * 1e3},
             "fp64": {"ms_per_step": fp64["ms_per_step"], "dof_per_s": world * gdof / (fp64["ms_per_step"] / 1e3),
-                     "cg_iters": fp64["niter"], "true_relres": fp64["relres"]},
+                     "cg_iters": fp64["niter"], "true_relres": fp64["relres"], "stages_ms": fp64["stages_ms"],
+                     "spmv_us": fp64["kernel_ms_avg"] * 1e3, "rest_of_iteration_us": fp64["other_ms_avg"] * 1e3},
             "speedup_fp32_refined_vs_fp64": fp64["ms_per_step"] / mixed["ms_per_step"],
             "e2e": {"value": world * gdof * e2e_steps / (e2e_ms / 1e3), "unit": "DOF/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "steps": e2e_steps},

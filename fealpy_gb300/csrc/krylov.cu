@@ -546,6 +546,7 @@ int run_pcg_f64(int64_t n, const int64_t* indptr, const int32_t* indices, const 
     info->launches = launches;
     info->kernel_ms = prof.ms;
     info->kernel_launches = prof.launches;
+    info->other_ms = 0.0;
   }
   return finish_status(h.done);
 }
@@ -618,6 +619,7 @@ int run_pcg_mixed(int64_t n, const int64_t* indptr, const int32_t* indices, cons
     info->launches = launches;
     info->kernel_ms = prof.ms;
     info->kernel_launches = prof.launches;
+    info->other_ms = 0.0;
   }
   return finish_status(h.done);
 }

@@ -501,29 +501,38 @@ int vec_grid(int64_t n) { return grid_for(n, kSellThreads, kSellMaxBlocks); }
 
 SellView view_of(const fgb_sell* A) { return SellView{A->n, A->n_slices, A->slice_ptr, A->perm, A->col}; }
 
+// CUDA events before the SpMV, after the SpMV and after the rest of each
+// iteration of a host-polled chunk; only iterations that did work (counted by
+// the device iteration counter) are summed.
 struct EventPairs {
   bool on;
   int cap;
   cudaEvent_t* ev = nullptr;
-  double ms = 0.0;
+  double ms = 0.0, other = 0.0;
   int64_t launches = 0;
   EventPairs(bool enable, int c) : on(enable), cap(c) {
     if (!on) return;
-    ev = new cudaEvent_t[2 * cap];
-    for (int k = 0; k < 2 * cap; ++k) cudaEventCreate(&ev[k]);
+    ev = new cudaEvent_t[3 * cap];
+    for (int k = 0; k < 3 * cap; ++k) cudaEventCreate(&ev[k]);
   }
   ~EventPairs() {
     if (!ev) return;
-    for (int k = 0; k < 2 * cap; ++k) cudaEventDestroy(ev[k]);
+    for (int k = 0; k < 3 * cap; ++k) cudaEventDestroy(ev[k]);
     delete[] ev;
   }
-  cudaEvent_t a(int k) const { return on ? ev[2 * k] : nullptr; }
-  cudaEvent_t b(int k) const { return on ? ev[2 * k + 1] : nullptr; }
+  cudaEvent_t a(int k) const { return on ? ev[3 * k] : nullptr; }
+  cudaEvent_t b(int k) const { return on ? ev[3 * k + 1] : nullptr; }
+  cudaEvent_t c(int k) const { return on ? ev[3 * k + 2] : nullptr; }
   void collect(int64_t executed) {
     if (!on) return;
     for (int64_t k = 0; k < executed && k < cap; ++k) {
-      float t = 0.f;
-      if (cudaEventElapsedTime(&t, ev[2 * k], ev[2 * k + 1]) == cudaSuccess) { ms += t; ++launches; }
+      float t = 0.f, u = 0.f;
+      if (cudaEventElapsedTime(&t, ev[3 * k], ev[3 * k + 1]) == cudaSuccess &&
+          cudaEventElapsedTime(&u, ev[3 * k + 1], ev[3 * k + 2]) == cudaSuccess) {
+        ms += t;
+        other += u;
+        ++launches;
+      }
     }
   }
 };
@@ -560,17 +569,19 @@ bool carve_mixed(Carver& cv, int64_t n, MixedWork& w) {
 
 // one CG iteration (FP64): ping-pong p by parity
 void f64_body(const SellView& A, const double* val, const double* dinv, double* x, F64Work& w, int parity,
-              cudaEvent_t e0, cudaEvent_t e1, cudaStream_t s) {
+              cudaEvent_t e0, cudaEvent_t e1, cudaEvent_t e2, cudaStream_t s) {
   double* p_old = parity ? w.p1 : w.p0;
   double* p_new = parity ? w.p0 : w.p1;
   if (e0) cudaEventRecord(e0, s);
   sell_pcg_spmv<double><<<sell_grid(A.n_slices), kSellThreads, 0, s>>>(A, val, w.z, p_old, p_new, w.Ap, w.partials, w.st);
   if (e1) cudaEventRecord(e1, s);
   sell_pcg_update_f64<<<vec_grid(A.n), kSellThreads, 0, s>>>(A.n, dinv, p_new, w.Ap, x, w.r, w.z, w.partials, w.st);
+  if (e2) cudaEventRecord(e2, s);
 }
 
 void mixed_body(const SellView& A, const float* val32, const double* val64, const double* dinv64, const double* b,
-                double* x, MixedWork& w, double delta, int parity, cudaEvent_t e0, cudaEvent_t e1, cudaStream_t s) {
+                double* x, MixedWork& w, double delta, int parity, cudaEvent_t e0, cudaEvent_t e1, cudaEvent_t e2,
+                cudaStream_t s) {
   float* p_old = parity ? w.p1 : w.p0;
   float* p_new = parity ? w.p0 : w.p1;
   if (e0) cudaEventRecord(e0, s);
@@ -580,6 +591,7 @@ void mixed_body(const SellView& A, const float* val32, const double* val64, cons
   sell_mixed_fold<<<vec_grid(A.n), kSellThreads, 0, s>>>(A.n, x, w.y, w.st, 0);
   sell_mixed_residual<<<sell_grid(A.n_slices), kSellThreads, 0, s>>>(A, val64, b, x, w.r64, w.partials, w.st, 0);
   sell_mixed_replace<<<vec_grid(A.n), kSellThreads, 0, s>>>(A.n, dinv64, w.r64, w.r, w.z, p_new, w.dinv32, w.partials, w.st, 0);
+  if (e2) cudaEventRecord(e2, s);
 }
 
 template <typename Body>
@@ -738,8 +750,8 @@ int32_t fgb_pcg_sell_f64(const fgb_sell* A, const double* diag_inv, const double
     if ((rc = set_tol(w.st, rtol * h.b_norm, s))) return rc;
     if (use_graph) {
       rc = graph_loop([&](cudaStream_t cs) {
-        f64_body(v, A->val64, diag_inv, x, w, 0, nullptr, nullptr, cs);
-        f64_body(v, A->val64, diag_inv, x, w, 1, nullptr, nullptr, cs);
+        f64_body(v, A->val64, diag_inv, x, w, 0, nullptr, nullptr, nullptr, cs);
+        f64_body(v, A->val64, diag_inv, x, w, 1, nullptr, nullptr, nullptr, cs);
       }, w.st, s, &launches);
       if (rc) return rc;
       if ((rc = read_state(w.st, &h, s))) return rc;
@@ -748,7 +760,7 @@ int32_t fgb_pcg_sell_f64(const fgb_sell* A, const double* diag_inv, const double
       int64_t it = 0;
       while (true) {
         const int64_t before = h.niter;
-        for (int k = 0; k < check_every; ++k, ++it) f64_body(v, A->val64, diag_inv, x, w, static_cast<int>(it & 1), prof.a(k), prof.b(k), s);
+        for (int k = 0; k < check_every; ++k, ++it) f64_body(v, A->val64, diag_inv, x, w, static_cast<int>(it & 1), prof.a(k), prof.b(k), prof.c(k), s);
         launches += 2 * check_every;
         if (cudaGetLastError() != cudaSuccess) return FGB_ERR_CUDA;
         if ((rc = read_state(w.st, &h, s))) return rc;
@@ -761,6 +773,7 @@ int32_t fgb_pcg_sell_f64(const fgb_sell* A, const double* diag_inv, const double
     info->niter = h.niter; info->residual = h.resid; info->b_norm = h.b_norm; info->true_relres = -1.0;
     info->reason = h.done; info->n_updates = 0; info->launches = launches; info->kernel_ms = prof.ms;
     info->kernel_launches = prof.launches;
+    info->other_ms = prof.other;
   }
   return finish(h.done);
 }
@@ -803,8 +816,8 @@ int32_t fgb_pcg_sell_mixed(const fgb_sell* A, const double* diag_inv64, const do
     launches += 2;
     if (use_graph) {
       rc = graph_loop([&](cudaStream_t cs) {
-        mixed_body(v, A->val32, A->val64, diag_inv64, b, x, w, delta, 0, nullptr, nullptr, cs);
-        mixed_body(v, A->val32, A->val64, diag_inv64, b, x, w, delta, 1, nullptr, nullptr, cs);
+        mixed_body(v, A->val32, A->val64, diag_inv64, b, x, w, delta, 0, nullptr, nullptr, nullptr, cs);
+        mixed_body(v, A->val32, A->val64, diag_inv64, b, x, w, delta, 1, nullptr, nullptr, nullptr, cs);
       }, w.st, s, &launches);
       if (rc) return rc;
       if ((rc = read_state(w.st, &h, s))) return rc;
@@ -814,7 +827,8 @@ int32_t fgb_pcg_sell_mixed(const fgb_sell* A, const double* diag_inv64, const do
       while (true) {
         const int64_t before = h.niter;
         for (int k = 0; k < check_every; ++k, ++it)
-          mixed_body(v, A->val32, A->val64, diag_inv64, b, x, w, delta, static_cast<int>(it & 1), prof.a(k), prof.b(k), s);
+          mixed_body(v, A->val32, A->val64, diag_inv64, b, x, w, delta, static_cast<int>(it & 1), prof.a(k), prof.b(k),
+                     prof.c(k), s);
         launches += 5 * check_every;
         if (cudaGetLastError() != cudaSuccess) return FGB_ERR_CUDA;
         if ((rc = read_state(w.st, &h, s))) return rc;
@@ -827,6 +841,7 @@ int32_t fgb_pcg_sell_mixed(const fgb_sell* A, const double* diag_inv64, const do
     info->niter = h.niter; info->residual = h.resid; info->b_norm = h.b_norm; info->true_relres = h.true_rel;
     info->reason = h.done; info->n_updates = h.n_updates; info->launches = launches; info->kernel_ms = prof.ms;
     info->kernel_launches = prof.launches;
+    info->other_ms = prof.other;
   }
   return finish(h.done);
 }
