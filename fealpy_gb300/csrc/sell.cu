@@ -307,8 +307,13 @@ __global__ void __launch_bounds__(kSellThreads) sell_pcg_init(SellView A, const 
   }
 }
 
-// kernel A: p_new = z + beta p_old ; Ap = A p_new ; alpha = rz / p_new.Ap
-template <typename T>
+// kernel A: Ap = A p ; alpha = rz / p.Ap.  FUSED: p_new = z + beta p_old is
+// formed on the fly for every gathered column (one launch fewer per iteration;
+// used in FP32, where the extra FMA per entry is free).  Not FUSED: p has been
+// updated in place by sell_p_update beforehand (used in FP64, where the FMA
+// rate of this part is low enough that a second FMA per entry would cost more
+// than the extra streaming pass over p).
+template <typename T, bool FUSED>
 __global__ void __launch_bounds__(kSellThreads) sell_pcg_spmv(SellView A, const T* __restrict__ val,
                                                               const T* __restrict__ z, const T* __restrict__ p_old,
                                                               T* __restrict__ p_new, T* __restrict__ Ap,
@@ -319,11 +324,16 @@ __global__ void __launch_bounds__(kSellThreads) sell_pcg_spmv(SellView A, const 
   SELL_WARP_LOOP(A) {
     const int64_t base = A.slice_ptr[s] + lane;
     const int w = static_cast<int>((A.slice_ptr[s + 1] - A.slice_ptr[s]) >> 5);
-    const T acc = sell_row_dot_p(A, val, base, w, z, p_old, beta);
+    const T acc = FUSED ? sell_row_dot_p(A, val, base, w, z, p_old, beta) : sell_row_dot_x(A, val, base, w, p_old);
     const int32_t row = A.perm[s * kSellC + lane];
     if (row >= 0) {
-      const T pi = z[row] + beta * p_old[row];
-      p_new[row] = pi;
+      T pi;
+      if (FUSED) {
+        pi = z[row] + beta * p_old[row];
+        p_new[row] = pi;
+      } else {
+        pi = p_old[row];
+      }
       Ap[row] = acc;
       pap += static_cast<double>(pi) * static_cast<double>(acc);
     }
@@ -337,6 +347,33 @@ __global__ void __launch_bounds__(kSellThreads) sell_pcg_spmv(SellView A, const 
       st->alpha = st->rz / tpap;
     }
   }
+}
+
+// ||b|| (mixed solver set-up); marks a zero right-hand side
+__global__ void __launch_bounds__(kSellThreads) sell_bnorm(int64_t n, const double* __restrict__ b, double* partials,
+                                                           SellPcgState* st) {
+  double bb = 0.0;
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    bb += b[i] * b[i];
+  double tbb, unused;
+  if (sell_last_block(bb, 0.0, partials, &st->counter[0], &tbb, &unused) && threadIdx.x == 0) {
+    st->b_norm = sqrt(tbb);
+    st->niter = 0;
+    st->n_updates = 0;
+    st->need_update = 0;
+    if (st->b_norm < 1e-15) st->done = FGB_PCG_ZERO_RHS;
+  }
+}
+
+// p = z + beta p, in place (FP64 solver, before kernel A)
+__global__ void __launch_bounds__(kSellThreads) sell_p_update(int64_t n, const double* __restrict__ z,
+                                                              double* __restrict__ p, const SellPcgState* st) {
+  if (st->done) return;
+  const double beta = st->beta;
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    p[i] = z[i] + beta * p[i];
 }
 
 // kernel B (FP64 solver)
@@ -376,19 +413,21 @@ __global__ void __launch_bounds__(kSellThreads) sell_pcg_update_f64(int64_t n, c
   }
 }
 
-// kernel B (mixed solver): FP32 updates, decides whether a reliable update is due
+// kernel B (mixed solver): x += alpha p in FP64, r -= alpha Ap and z = Dinv r in
+// FP32; decides whether a reliable update is due.
 __global__ void __launch_bounds__(kSellThreads) sell_mixed_update(int64_t n, const float* __restrict__ dinv,
                                                                   const float* __restrict__ p,
-                                                                  const float* __restrict__ Ap, float* __restrict__ y,
+                                                                  const float* __restrict__ Ap, double* __restrict__ x,
                                                                   float* __restrict__ r, float* __restrict__ z,
                                                                   double* partials, SellPcgState* st, double delta) {
   if (st->done) return;
-  const float alpha = static_cast<float>(st->alpha);
+  const double alpha = st->alpha;
+  const float alpha32 = static_cast<float>(alpha);
   double rz = 0.0, rr = 0.0;
   for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
        i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-    y[i] += alpha * p[i];
-    const float ri = r[i] - alpha * Ap[i];
+    x[i] += alpha * static_cast<double>(p[i]);
+    const float ri = r[i] - alpha32 * Ap[i];
     const float zi = dinv[i] * ri;
     r[i] = ri;
     z[i] = zi;
@@ -409,38 +448,39 @@ __global__ void __launch_bounds__(kSellThreads) sell_mixed_update(int64_t n, con
   }
 }
 
-// reliable update part 1: x += y, y = 0 (own rows)
-__global__ void sell_mixed_fold(int64_t n, double* __restrict__ x, float* __restrict__ y, const SellPcgState* st,
-                                int first) {
-  if (!first && (st->done || !st->need_update)) return;
-  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
-       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-    x[i] += static_cast<double>(y[i]);
-    y[i] = 0.0f;
-  }
-}
-
-// reliable update part 2: r64 = b - A64 x, true residual test
-__global__ void __launch_bounds__(kSellThreads) sell_mixed_residual(SellView A, const double* __restrict__ val,
+// Reliable update (only when due, or first = 1 at the start): r64 = b - A64 x
+// with the FP64 values in FP64, true residual test, then r = float(r64),
+// z = Dinv r and beta from the replaced residual.  The first call also builds
+// the FP32 inverse diagonal and starts the direction p = z.
+__global__ void __launch_bounds__(kSellThreads) sell_mixed_reliable(SellView A, const double* __restrict__ val,
                                                                     const double* __restrict__ b,
                                                                     const double* __restrict__ x,
-                                                                    double* __restrict__ r64, double* partials,
-                                                                    SellPcgState* st, int first) {
+                                                                    const double* __restrict__ dinv64,
+                                                                    float* __restrict__ dinv32, float* __restrict__ r,
+                                                                    float* __restrict__ z, float* __restrict__ p,
+                                                                    double* partials, SellPcgState* st, int first) {
   if (!first && (st->done || !st->need_update)) return;
-  double rr = 0.0;
+  double rr64 = 0.0, rz = 0.0;
   SELL_WARP_LOOP(A) {
     const int64_t base = A.slice_ptr[s] + lane;
     const int w = static_cast<int>((A.slice_ptr[s + 1] - A.slice_ptr[s]) >> 5);
     const double acc = sell_row_dot_x(A, val, base, w, x);
     const int32_t row = A.perm[s * kSellC + lane];
     if (row >= 0) {
-      const double ri = b[row] - acc;
-      r64[row] = ri;
-      rr += ri * ri;
+      const double r64 = b[row] - acc;
+      rr64 += r64 * r64;
+      const float di = first ? static_cast<float>(dinv64[row]) : dinv32[row];
+      if (first) dinv32[row] = di;
+      const float ri = static_cast<float>(r64);
+      const float zi = di * ri;
+      r[row] = ri;
+      z[row] = zi;
+      if (first) p[row] = zi;
+      rz += static_cast<double>(ri) * static_cast<double>(zi);
     }
   }
-  double trr, unused;
-  if (sell_last_block(rr, 0.0, partials, &st->counter[3], &trr, &unused) && threadIdx.x == 0) {
+  double trr, trz;
+  if (sell_last_block(rr64, rz, partials, &st->counter[3], &trr, &trz) && threadIdx.x == 0) {
     const double nrm = sqrt(trr);
     st->true_rel = st->b_norm > 0.0 ? nrm / st->b_norm : 0.0;
     st->resid = nrm;
@@ -448,35 +488,10 @@ __global__ void __launch_bounds__(kSellThreads) sell_mixed_residual(SellView A, 
     if (!isfinite(nrm)) st->done = FGB_PCG_NONFINITE;
     else if (nrm <= st->tol) st->done = FGB_PCG_RTOL;
     else if (st->niter >= st->maxit) st->done = FGB_PCG_MAXIT;
-  }
-}
-
-// reliable update part 3: r = float(r64), z = Dinv r ; restart p on the first call
-__global__ void __launch_bounds__(kSellThreads) sell_mixed_replace(int64_t n, const double* __restrict__ dinv64,
-                                                                   const double* __restrict__ r64,
-                                                                   float* __restrict__ r, float* __restrict__ z,
-                                                                   float* __restrict__ p, float* __restrict__ dinv32,
-                                                                   double* partials, SellPcgState* st, int first) {
-  if (!first && (st->done || !st->need_update)) return;
-  double rz = 0.0, rr = 0.0;
-  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
-       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-    const float ri = static_cast<float>(r64[i]);
-    const float di = first ? static_cast<float>(dinv64[i]) : dinv32[i];
-    if (first) dinv32[i] = di;
-    const float zi = di * ri;
-    r[i] = ri;
-    z[i] = zi;
-    if (first) p[i] = zi;
-    rz += static_cast<double>(ri) * static_cast<double>(zi);
-    rr += static_cast<double>(ri) * static_cast<double>(ri);
-  }
-  double trz, trr;
-  if (sell_last_block(rz, rr, partials, &st->counter[0], &trz, &trr) && threadIdx.x == 0) {
     st->beta = first ? 0.0 : trz / st->rz_prev;
     st->rz = trz;
     st->rr = trr;
-    st->r_upd = sqrt(trr);
+    st->r_upd = nrm;
     st->need_update = 0;
   }
 }
@@ -546,8 +561,7 @@ struct F64Work {
 struct MixedWork {
   SellPcgState* st;
   double* partials;
-  float *r, *z, *p0, *p1, *Ap, *y, *dinv32;
-  double* r64;
+  float *r, *z, *p0, *p1, *Ap, *dinv32;
 };
 
 bool carve_f64(Carver& cv, int64_t n, F64Work& w) {
@@ -562,35 +576,37 @@ bool carve_mixed(Carver& cv, int64_t n, MixedWork& w) {
   w.st = cv.take<SellPcgState>(1);
   w.partials = cv.take<double>(2 * kSellMaxBlocks);
   w.r = cv.take<float>(n); w.z = cv.take<float>(n); w.p0 = cv.take<float>(n); w.p1 = cv.take<float>(n);
-  w.Ap = cv.take<float>(n); w.y = cv.take<float>(n); w.dinv32 = cv.take<float>(n);
-  w.r64 = cv.take<double>(n);
+  w.Ap = cv.take<float>(n); w.dinv32 = cv.take<float>(n);
   return cv.ok;
 }
 
-// one CG iteration (FP64): ping-pong p by parity
+// one CG iteration (FP64): p = z + beta p in place, then Ap, then the updates
 void f64_body(const SellView& A, const double* val, const double* dinv, double* x, F64Work& w, int parity,
               cudaEvent_t e0, cudaEvent_t e1, cudaEvent_t e2, cudaStream_t s) {
-  double* p_old = parity ? w.p1 : w.p0;
-  double* p_new = parity ? w.p0 : w.p1;
+  (void)parity;
+  sell_p_update<<<vec_grid(A.n), kSellThreads, 0, s>>>(A.n, w.z, w.p0, w.st);
   if (e0) cudaEventRecord(e0, s);
-  sell_pcg_spmv<double><<<sell_grid(A.n_slices), kSellThreads, 0, s>>>(A, val, w.z, p_old, p_new, w.Ap, w.partials, w.st);
+  sell_pcg_spmv<double, false><<<sell_grid(A.n_slices), kSellThreads, 0, s>>>(A, val, w.z, w.p0, nullptr, w.Ap,
+                                                                             w.partials, w.st);
   if (e1) cudaEventRecord(e1, s);
-  sell_pcg_update_f64<<<vec_grid(A.n), kSellThreads, 0, s>>>(A.n, dinv, p_new, w.Ap, x, w.r, w.z, w.partials, w.st);
+  sell_pcg_update_f64<<<vec_grid(A.n), kSellThreads, 0, s>>>(A.n, dinv, w.p0, w.Ap, x, w.r, w.z, w.partials, w.st);
   if (e2) cudaEventRecord(e2, s);
 }
 
+// one CG iteration (mixed): ping-pong p by parity (the fused SpMV writes p_new)
 void mixed_body(const SellView& A, const float* val32, const double* val64, const double* dinv64, const double* b,
                 double* x, MixedWork& w, double delta, int parity, cudaEvent_t e0, cudaEvent_t e1, cudaEvent_t e2,
                 cudaStream_t s) {
   float* p_old = parity ? w.p1 : w.p0;
   float* p_new = parity ? w.p0 : w.p1;
   if (e0) cudaEventRecord(e0, s);
-  sell_pcg_spmv<float><<<sell_grid(A.n_slices), kSellThreads, 0, s>>>(A, val32, w.z, p_old, p_new, w.Ap, w.partials, w.st);
+  sell_pcg_spmv<float, true><<<sell_grid(A.n_slices), kSellThreads, 0, s>>>(A, val32, w.z, p_old, p_new, w.Ap,
+                                                                           w.partials, w.st);
   if (e1) cudaEventRecord(e1, s);
-  sell_mixed_update<<<vec_grid(A.n), kSellThreads, 0, s>>>(A.n, w.dinv32, p_new, w.Ap, w.y, w.r, w.z, w.partials, w.st, delta);
-  sell_mixed_fold<<<vec_grid(A.n), kSellThreads, 0, s>>>(A.n, x, w.y, w.st, 0);
-  sell_mixed_residual<<<sell_grid(A.n_slices), kSellThreads, 0, s>>>(A, val64, b, x, w.r64, w.partials, w.st, 0);
-  sell_mixed_replace<<<vec_grid(A.n), kSellThreads, 0, s>>>(A.n, dinv64, w.r64, w.r, w.z, p_new, w.dinv32, w.partials, w.st, 0);
+  sell_mixed_update<<<vec_grid(A.n), kSellThreads, 0, s>>>(A.n, w.dinv32, p_new, w.Ap, x, w.r, w.z, w.partials, w.st,
+                                                           delta);
+  sell_mixed_reliable<<<sell_grid(A.n_slices), kSellThreads, 0, s>>>(A, val64, b, x, dinv64, w.dinv32, w.r, w.z,
+                                                                     nullptr, w.partials, w.st, 0);
   if (e2) cudaEventRecord(e2, s);
 }
 
@@ -755,13 +771,13 @@ int32_t fgb_pcg_sell_f64(const fgb_sell* A, const double* diag_inv, const double
       }, w.st, s, &launches);
       if (rc) return rc;
       if ((rc = read_state(w.st, &h, s))) return rc;
-      launches += 5 * ((h.niter + 1) / 2 + 1);
+      launches += 7 * ((h.niter + 1) / 2 + 1);
     } else {
       int64_t it = 0;
       while (true) {
         const int64_t before = h.niter;
         for (int k = 0; k < check_every; ++k, ++it) f64_body(v, A->val64, diag_inv, x, w, static_cast<int>(it & 1), prof.a(k), prof.b(k), prof.c(k), s);
-        launches += 2 * check_every;
+        launches += 3 * check_every;
         if (cudaGetLastError() != cudaSuccess) return FGB_ERR_CUDA;
         if ((rc = read_state(w.st, &h, s))) return rc;
         prof.collect(h.niter - before);
@@ -798,10 +814,7 @@ int32_t fgb_pcg_sell_mixed(const fgb_sell* A, const double* diag_inv64, const do
   h.trip_cap = maxit / 2 + 2;
   int64_t launches = 0;
   cudaMemcpyAsync(w.st, &h, sizeof(SellPcgState), cudaMemcpyHostToDevice, s);
-  cudaMemsetAsync(w.y, 0, n * sizeof(float), s);
-  // ||b|| from the init kernel (r, z, p all alias r64: it stores the same value thrice)
-  sell_pcg_init<double><<<sell_grid(v.n_slices), kSellThreads, 0, s>>>(v, A->val64, nullptr, b, x, w.r64, w.r64,
-                                                                       w.r64, w.partials, w.st);
+  sell_bnorm<<<vec_grid(n), kSellThreads, 0, s>>>(n, b, w.partials, w.st);
   ++launches;
   int rc = read_state(w.st, &h, s);
   if (rc) return rc;
@@ -810,10 +823,10 @@ int32_t fgb_pcg_sell_mixed(const fgb_sell* A, const double* diag_inv64, const do
     cudaMemsetAsync(x, 0, n * sizeof(double), s);
   } else {
     if ((rc = set_tol(w.st, rtol * h.b_norm, s))) return rc;
-    sell_mixed_residual<<<sell_grid(v.n_slices), kSellThreads, 0, s>>>(v, A->val64, b, x, w.r64, w.partials, w.st, 1);
-    sell_mixed_replace<<<vec_grid(n), kSellThreads, 0, s>>>(n, diag_inv64, w.r64, w.r, w.z, w.p0, w.dinv32, w.partials,
-                                                          w.st, 1);
-    launches += 2;
+    // initial residual in FP64, its FP32 copy, z and p = z
+    sell_mixed_reliable<<<sell_grid(v.n_slices), kSellThreads, 0, s>>>(v, A->val64, b, x, diag_inv64, w.dinv32, w.r,
+                                                                       w.z, w.p0, w.partials, w.st, 1);
+    ++launches;
     if (use_graph) {
       rc = graph_loop([&](cudaStream_t cs) {
         mixed_body(v, A->val32, A->val64, diag_inv64, b, x, w, delta, 0, nullptr, nullptr, nullptr, cs);
@@ -821,7 +834,7 @@ int32_t fgb_pcg_sell_mixed(const fgb_sell* A, const double* diag_inv64, const do
       }, w.st, s, &launches);
       if (rc) return rc;
       if ((rc = read_state(w.st, &h, s))) return rc;
-      launches += 11 * ((h.niter + 1) / 2 + 1);
+      launches += 7 * ((h.niter + 1) / 2 + 1);
     } else {
       int64_t it = 0;
       while (true) {
@@ -829,7 +842,7 @@ int32_t fgb_pcg_sell_mixed(const fgb_sell* A, const double* diag_inv64, const do
         for (int k = 0; k < check_every; ++k, ++it)
           mixed_body(v, A->val32, A->val64, diag_inv64, b, x, w, delta, static_cast<int>(it & 1), prof.a(k), prof.b(k),
                      prof.c(k), s);
-        launches += 5 * check_every;
+        launches += 3 * check_every;
         if (cudaGetLastError() != cudaSuccess) return FGB_ERR_CUDA;
         if ((rc = read_state(w.st, &h, s))) return rc;
         prof.collect(h.niter - before);
