@@ -419,7 +419,8 @@ __global__ void __launch_bounds__(kSellThreads) sell_mixed_update(int64_t n, con
                                                                   const float* __restrict__ p,
                                                                   const float* __restrict__ Ap, double* __restrict__ x,
                                                                   float* __restrict__ r, float* __restrict__ z,
-                                                                  double* partials, SellPcgState* st, double delta) {
+                                                                  double* partials, SellPcgState* st, double delta,
+                                                                  cudaGraphConditionalHandle hif, int set_if) {
   if (st->done) return;
   const double alpha = st->alpha;
   const float alpha32 = static_cast<float>(alpha);
@@ -445,6 +446,8 @@ __global__ void __launch_bounds__(kSellThreads) sell_mixed_update(int64_t n, con
     st->rz_prev = st->rz;
     st->beta = trz / st->rz;
     st->rz = trz;
+    // graph driver: run the reliable-update node only when it is due
+    if (set_if) cudaGraphSetConditional(hif, (st->need_update && !st->done) ? 1u : 0u);
   }
 }
 
@@ -520,35 +523,86 @@ SellView view_of(const fgb_sell* A) { return SellView{A->n, A->n_slices, A->slic
 // iteration of a host-polled chunk; only iterations that did work (counted by
 // the device iteration counter) are summed.
 struct EventPairs {
+  static constexpr int kPer = 5;  // body start, before SpMV, after SpMV, after update, body end
   bool on;
   int cap;
   cudaEvent_t* ev = nullptr;
-  double ms = 0.0, other = 0.0;
+  double ms = 0.0, other = 0.0, extra = 0.0;
   int64_t launches = 0;
   EventPairs(bool enable, int c) : on(enable), cap(c) {
     if (!on) return;
-    ev = new cudaEvent_t[3 * cap];
-    for (int k = 0; k < 3 * cap; ++k) cudaEventCreate(&ev[k]);
+    ev = new cudaEvent_t[kPer * cap];
+    for (int k = 0; k < kPer * cap; ++k) cudaEventCreate(&ev[k]);
   }
   ~EventPairs() {
     if (!ev) return;
-    for (int k = 0; k < 3 * cap; ++k) cudaEventDestroy(ev[k]);
+    for (int k = 0; k < kPer * cap; ++k) cudaEventDestroy(ev[k]);
     delete[] ev;
   }
-  cudaEvent_t a(int k) const { return on ? ev[3 * k] : nullptr; }
-  cudaEvent_t b(int k) const { return on ? ev[3 * k + 1] : nullptr; }
-  cudaEvent_t c(int k) const { return on ? ev[3 * k + 2] : nullptr; }
+  cudaEvent_t at(int k, int j) const { return on ? ev[kPer * k + j] : nullptr; }
+  const cudaEvent_t* of(int k) const { return on ? ev + kPer * k : nullptr; }
+  // spmv = t2 - t1, update = t3 - t2, extra = (t1 - t0) + (t4 - t3)
   void collect(int64_t executed) {
     if (!on) return;
     for (int64_t k = 0; k < executed && k < cap; ++k) {
-      float t = 0.f, u = 0.f;
-      if (cudaEventElapsedTime(&t, ev[3 * k], ev[3 * k + 1]) == cudaSuccess &&
-          cudaEventElapsedTime(&u, ev[3 * k + 1], ev[3 * k + 2]) == cudaSuccess) {
-        ms += t;
-        other += u;
+      float d[4];
+      bool ok = true;
+      for (int j = 0; j < 4; ++j) ok = ok && cudaEventElapsedTime(&d[j], ev[kPer * k + j], ev[kPer * k + j + 1]) == cudaSuccess;
+      if (ok) {
+        ms += d[1];
+        other += d[2];
+        extra += d[0] + d[3];
         ++launches;
       }
     }
+  }
+};
+
+inline void rec(const cudaEvent_t* e, int j, cudaStream_t s) {
+  if (e) cudaEventRecord(e[j], s);
+}
+
+// Capture state of the while-loop body.  add_if() appends an IF conditional
+// node (condition `hif`, set on the device by the update kernel) whose body
+// is whatever `fn` launches on the stream it is given.
+struct CaptureCtx {
+  cudaStream_t cs = nullptr;
+  cudaGraphConditionalHandle hif = 0;
+  bool ok = true;
+
+  template <typename Fn>
+  void add_if(Fn fn) {
+    cudaStreamCaptureStatus status;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    if (cudaStreamGetCaptureInfo(cs, &status, nullptr, &g, &deps, nullptr, &nd) != cudaSuccess ||
+        status != cudaStreamCaptureStatusActive) {
+      ok = false;
+      return;
+    }
+    cudaGraphNodeParams p = {};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = hif;
+    p.conditional.type = cudaGraphCondTypeIf;
+    p.conditional.size = 1;
+    cudaGraphNode_t node;
+    if (cudaGraphAddNode(&node, g, deps, nullptr, nd, &p) != cudaSuccess) { ok = false; return; }
+    if (cudaStreamUpdateCaptureDependencies(cs, &node, nullptr, 1, cudaStreamSetCaptureDependencies) != cudaSuccess) {
+      ok = false;
+      return;
+    }
+    cudaStream_t bs;
+    cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking);
+    if (cudaStreamBeginCaptureToGraph(bs, p.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                      cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+      ok = false;
+    } else {
+      fn(bs);
+      cudaGraph_t out = nullptr;
+      if (cudaStreamEndCapture(bs, &out) != cudaSuccess) ok = false;
+    }
+    cudaStreamDestroy(bs);
   }
 };
 
@@ -582,32 +636,42 @@ bool carve_mixed(Carver& cv, int64_t n, MixedWork& w) {
 
 // one CG iteration (FP64): p = z + beta p in place, then Ap, then the updates
 void f64_body(const SellView& A, const double* val, const double* dinv, double* x, F64Work& w, int parity,
-              cudaEvent_t e0, cudaEvent_t e1, cudaEvent_t e2, cudaStream_t s) {
+              const cudaEvent_t* ev, cudaStream_t s) {
   (void)parity;
+  rec(ev, 0, s);
   sell_p_update<<<vec_grid(A.n), kSellThreads, 0, s>>>(A.n, w.z, w.p0, w.st);
-  if (e0) cudaEventRecord(e0, s);
+  rec(ev, 1, s);
   sell_pcg_spmv<double, false><<<sell_grid(A.n_slices), kSellThreads, 0, s>>>(A, val, w.z, w.p0, nullptr, w.Ap,
                                                                              w.partials, w.st);
-  if (e1) cudaEventRecord(e1, s);
+  rec(ev, 2, s);
   sell_pcg_update_f64<<<vec_grid(A.n), kSellThreads, 0, s>>>(A.n, dinv, w.p0, w.Ap, x, w.r, w.z, w.partials, w.st);
-  if (e2) cudaEventRecord(e2, s);
+  rec(ev, 3, s);
+  rec(ev, 4, s);
 }
 
-// one CG iteration (mixed): ping-pong p by parity (the fused SpMV writes p_new)
+// one CG iteration (mixed): ping-pong p by parity (the fused SpMV writes p_new).
+// With a capture context the reliable update becomes an IF node of the graph;
+// otherwise it is launched every iteration and returns at once when not due.
 void mixed_body(const SellView& A, const float* val32, const double* val64, const double* dinv64, const double* b,
-                double* x, MixedWork& w, double delta, int parity, cudaEvent_t e0, cudaEvent_t e1, cudaEvent_t e2,
-                cudaStream_t s) {
+                double* x, MixedWork& w, double delta, int parity, const cudaEvent_t* ev, cudaStream_t s,
+                CaptureCtx* ctx = nullptr) {
   float* p_old = parity ? w.p1 : w.p0;
   float* p_new = parity ? w.p0 : w.p1;
-  if (e0) cudaEventRecord(e0, s);
+  rec(ev, 0, s);
+  rec(ev, 1, s);
   sell_pcg_spmv<float, true><<<sell_grid(A.n_slices), kSellThreads, 0, s>>>(A, val32, w.z, p_old, p_new, w.Ap,
                                                                            w.partials, w.st);
-  if (e1) cudaEventRecord(e1, s);
+  rec(ev, 2, s);
   sell_mixed_update<<<vec_grid(A.n), kSellThreads, 0, s>>>(A.n, w.dinv32, p_new, w.Ap, x, w.r, w.z, w.partials, w.st,
-                                                           delta);
-  sell_mixed_reliable<<<sell_grid(A.n_slices), kSellThreads, 0, s>>>(A, val64, b, x, dinv64, w.dinv32, w.r, w.z,
-                                                                     nullptr, w.partials, w.st, 0);
-  if (e2) cudaEventRecord(e2, s);
+                                                           delta, ctx ? ctx->hif : 0, ctx ? 1 : 0);
+  rec(ev, 3, s);
+  auto reliable = [&](cudaStream_t rs) {
+    sell_mixed_reliable<<<sell_grid(A.n_slices), kSellThreads, 0, rs>>>(A, val64, b, x, dinv64, w.dinv32, w.r, w.z,
+                                                                        nullptr, w.partials, w.st, 0);
+  };
+  if (ctx) ctx->add_if(reliable);
+  else reliable(s);
+  rec(ev, 4, s);
 }
 
 template <typename Body>
@@ -634,16 +698,21 @@ int graph_loop(Body body_two_iters, SellPcgState* st, cudaStream_t s, int64_t* l
     return FGB_ERR_CUDA;
   }
   cudaGraph_t body = cp.conditional.phGraph_out[0];
-  cudaStream_t cs;
-  cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
-  if (cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+  CaptureCtx ctx;
+  if (cudaGraphConditionalHandleCreate(&ctx.hif, body, 0, cudaGraphCondAssignDefault) != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return FGB_ERR_CUDA;
+  }
+  cudaStreamCreateWithFlags(&ctx.cs, cudaStreamNonBlocking);
+  if (cudaStreamBeginCaptureToGraph(ctx.cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
     rc = FGB_ERR_CUDA;
   } else {
-    body_two_iters(cs);
-    sell_loop_ctl<<<1, 1, 0, cs>>>(st, h);
+    body_two_iters(ctx);
+    sell_loop_ctl<<<1, 1, 0, ctx.cs>>>(st, h);
     cudaGraph_t out = nullptr;
-    if (cudaStreamEndCapture(cs, &out) != cudaSuccess) rc = FGB_ERR_CUDA;
+    if (cudaStreamEndCapture(ctx.cs, &out) != cudaSuccess || !ctx.ok) rc = FGB_ERR_CUDA;
   }
+  cudaStream_t cs = ctx.cs;
   if (rc == FGB_OK && cudaGraphInstantiate(&ge, g, 0) != cudaSuccess) rc = FGB_ERR_CUDA;
   if (rc == FGB_OK && cudaGraphLaunch(ge, s) != cudaSuccess) rc = FGB_ERR_CUDA;
   if (rc == FGB_OK && cudaStreamSynchronize(s) != cudaSuccess) rc = FGB_ERR_CUDA;
@@ -765,9 +834,9 @@ int32_t fgb_pcg_sell_f64(const fgb_sell* A, const double* diag_inv, const double
   } else {
     if ((rc = set_tol(w.st, rtol * h.b_norm, s))) return rc;
     if (use_graph) {
-      rc = graph_loop([&](cudaStream_t cs) {
-        f64_body(v, A->val64, diag_inv, x, w, 0, nullptr, nullptr, nullptr, cs);
-        f64_body(v, A->val64, diag_inv, x, w, 1, nullptr, nullptr, nullptr, cs);
+      rc = graph_loop([&](CaptureCtx& c) {
+        f64_body(v, A->val64, diag_inv, x, w, 0, nullptr, c.cs);
+        f64_body(v, A->val64, diag_inv, x, w, 1, nullptr, c.cs);
       }, w.st, s, &launches);
       if (rc) return rc;
       if ((rc = read_state(w.st, &h, s))) return rc;
@@ -776,7 +845,7 @@ int32_t fgb_pcg_sell_f64(const fgb_sell* A, const double* diag_inv, const double
       int64_t it = 0;
       while (true) {
         const int64_t before = h.niter;
-        for (int k = 0; k < check_every; ++k, ++it) f64_body(v, A->val64, diag_inv, x, w, static_cast<int>(it & 1), prof.a(k), prof.b(k), prof.c(k), s);
+        for (int k = 0; k < check_every; ++k, ++it) f64_body(v, A->val64, diag_inv, x, w, static_cast<int>(it & 1), prof.of(k), s);
         launches += 3 * check_every;
         if (cudaGetLastError() != cudaSuccess) return FGB_ERR_CUDA;
         if ((rc = read_state(w.st, &h, s))) return rc;
@@ -790,6 +859,7 @@ int32_t fgb_pcg_sell_f64(const fgb_sell* A, const double* diag_inv, const double
     info->reason = h.done; info->n_updates = 0; info->launches = launches; info->kernel_ms = prof.ms;
     info->kernel_launches = prof.launches;
     info->other_ms = prof.other;
+    info->extra_ms = prof.extra;
   }
   return finish(h.done);
 }
@@ -828,20 +898,20 @@ int32_t fgb_pcg_sell_mixed(const fgb_sell* A, const double* diag_inv64, const do
                                                                        w.z, w.p0, w.partials, w.st, 1);
     ++launches;
     if (use_graph) {
-      rc = graph_loop([&](cudaStream_t cs) {
-        mixed_body(v, A->val32, A->val64, diag_inv64, b, x, w, delta, 0, nullptr, nullptr, nullptr, cs);
-        mixed_body(v, A->val32, A->val64, diag_inv64, b, x, w, delta, 1, nullptr, nullptr, nullptr, cs);
+      rc = graph_loop([&](CaptureCtx& c) {
+        mixed_body(v, A->val32, A->val64, diag_inv64, b, x, w, delta, 0, nullptr, c.cs, &c);
+        mixed_body(v, A->val32, A->val64, diag_inv64, b, x, w, delta, 1, nullptr, c.cs, &c);
       }, w.st, s, &launches);
       if (rc) return rc;
       if ((rc = read_state(w.st, &h, s))) return rc;
-      launches += 7 * ((h.niter + 1) / 2 + 1);
+      // per trip: 2 x (SpMV + update) + loop control; reliable updates when due
+      launches += 5 * ((h.niter + 1) / 2 + 1) + h.n_updates;
     } else {
       int64_t it = 0;
       while (true) {
         const int64_t before = h.niter;
         for (int k = 0; k < check_every; ++k, ++it)
-          mixed_body(v, A->val32, A->val64, diag_inv64, b, x, w, delta, static_cast<int>(it & 1), prof.a(k), prof.b(k),
-                     prof.c(k), s);
+          mixed_body(v, A->val32, A->val64, diag_inv64, b, x, w, delta, static_cast<int>(it & 1), prof.of(k), s);
         launches += 3 * check_every;
         if (cudaGetLastError() != cudaSuccess) return FGB_ERR_CUDA;
         if ((rc = read_state(w.st, &h, s))) return rc;
@@ -855,6 +925,7 @@ int32_t fgb_pcg_sell_mixed(const fgb_sell* A, const double* diag_inv64, const do
     info->reason = h.done; info->n_updates = h.n_updates; info->launches = launches; info->kernel_ms = prof.ms;
     info->kernel_launches = prof.launches;
     info->other_ms = prof.other;
+    info->extra_ms = prof.extra;
   }
   return finish(h.done);
 }

@@ -201,9 +201,8 @@ __global__ void adjacency_sort(int64_t n_dof, const int64_t* __restrict__ adj_pt
 // ---------------------------------------------------------------------------
 // row pattern
 // ---------------------------------------------------------------------------
-constexpr int kPatWarps = 8;        // warps per block, first pass
-constexpr int kPatCap = 512;        // candidates per warp held in shared memory, first pass
-constexpr int kPatBigCap = 8192;    // second pass, one warp per block (32 KB)
+constexpr int kPatWarps = 8;        // warps per block, first pass (hash set per warp)
+constexpr int kPatBigCap = 8192;    // second pass (bitonic over all candidates), one warp per block (32 KB)
 
 __device__ __forceinline__ int next_pow2(int x) {
   int p = 32;
@@ -274,18 +273,93 @@ __device__ bool pattern_row(int64_t i, int mode, const int64_t* __restrict__ adj
   return true;
 }
 
+// First-pass row builder: the candidates are inserted into a per-warp
+// open-addressing hash set in shared memory (kHashSlots slots), the distinct
+// columns are compacted and only those (at most kHashMaxUnique) are sorted.
+// For a P2 tetrahedral row that is ~240 candidates but <= 65 distinct columns,
+// so the sort is 4-8x smaller than sorting all candidates.  Returns false when
+// the row has more distinct columns than kHashMaxUnique (the bitonic pass 2
+// handles it).  The result does not depend on insertion order.
+constexpr int kHashSlots = 256;
+constexpr int kHashMaxUnique = 128;
+
+__device__ bool pattern_row_hash(int64_t i, int mode, const int64_t* __restrict__ adj_ptr,
+                                 const int32_t* __restrict__ adj, const int32_t* __restrict__ c2d, int ldof,
+                                 int32_t* __restrict__ row_cnt, const int64_t* __restrict__ indptr,
+                                 int32_t* __restrict__ indices, int32_t* tab, int32_t* srt) {
+  const int lane = threadIdx.x & 31;
+  const int64_t s = adj_ptr[i];
+  const int m = static_cast<int>(adj_ptr[i + 1] - s) * ldof;
+  for (int t = lane; t < kHashSlots; t += 32) tab[t] = -1;
+  __syncwarp();
+  bool full = false;
+  for (int base = 0; base < m; base += 32) {
+    const int t = base + lane;
+    if (t < m) {
+      const int k = t / ldof, j = t - k * ldof;
+      const int32_t c = adj[s + k] / ldof;
+      const int32_t v = c2d[static_cast<int64_t>(c) * ldof + j];
+      const unsigned h = (static_cast<unsigned>(v) * 2654435761u) >> 24;  // 8 bits
+      int pr = 0;
+      for (; pr < kHashSlots; ++pr) {
+        const int32_t old = atomicCAS(tab + ((h + pr) & (kHashSlots - 1)), -1, v);
+        if (old == -1 || old == v) break;
+      }
+      if (pr == kHashSlots) full = true;
+    }
+  }
+  __syncwarp();
+  if (__any_sync(0xffffffffu, full)) return false;
+  int u = 0;
+  for (int base = 0; base < kHashSlots; base += 32) {
+    const int32_t v = tab[base + lane];
+    const bool keep = v >= 0;
+    const unsigned ball = __ballot_sync(0xffffffffu, keep);
+    const int pos = u + __popc(ball & ((1u << lane) - 1u));
+    if (keep && pos < kHashMaxUnique) srt[pos] = v;
+    u += __popc(ball);
+  }
+  if (u > kHashMaxUnique) return false;
+  const int np2 = next_pow2(u > 0 ? u : 1);
+  for (int t = u + lane; t < np2; t += 32) srt[t] = INT_MAX;
+  __syncwarp();
+  for (int k = 2; k <= np2; k <<= 1) {
+    for (int jj = k >> 1; jj > 0; jj >>= 1) {
+      for (int t = lane; t < np2; t += 32) {
+        const int w = t ^ jj;
+        if (w > t) {
+          const int32_t a = srt[t], b = srt[w];
+          const bool up = (t & k) == 0;
+          if ((a > b) == up) { srt[t] = b; srt[w] = a; }
+        }
+      }
+      __syncwarp();
+    }
+  }
+  if (mode == 0) {
+    if (lane == 0) row_cnt[i] = u;
+  } else {
+    const int64_t out0 = indptr[i];
+    for (int t = lane; t < u; t += 32) indices[out0 + t] = srt[t];
+  }
+  __syncwarp();
+  return true;
+}
+
 __global__ void __launch_bounds__(kPatWarps * 32) pattern_pass1(int64_t n_dof, int mode, const int64_t* __restrict__ adj_ptr,
                                                                 const int32_t* __restrict__ adj, const int32_t* __restrict__ c2d,
                                                                 int ldof, int32_t* __restrict__ row_cnt,
                                                                 const int64_t* __restrict__ indptr, int32_t* __restrict__ indices,
                                                                 int32_t* __restrict__ ovf, int32_t* __restrict__ ovf_len) {
-  __shared__ int32_t sbuf[kPatWarps * kPatCap];
+  __shared__ int32_t stab[kPatWarps * kHashSlots];
+  __shared__ int32_t ssrt[kPatWarps * kHashMaxUnique];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  int32_t* buf = sbuf + wib * kPatCap;
+  int32_t* tab = stab + wib * kHashSlots;
+  int32_t* srt = ssrt + wib * kHashMaxUnique;
   const int64_t warp = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
   const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
   for (int64_t i = warp; i < n_dof; i += nwarps) {
-    bool done = pattern_row(i, mode, adj_ptr, adj, c2d, ldof, row_cnt, indptr, indices, buf, kPatCap);
+    bool done = pattern_row_hash(i, mode, adj_ptr, adj, c2d, ldof, row_cnt, indptr, indices, tab, srt);
     if (!done && lane == 0) {
       int slot = atomicAdd(ovf_len, 1);
       ovf[slot] = static_cast<int32_t>(i);

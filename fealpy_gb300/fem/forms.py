@@ -19,11 +19,21 @@ from .integrators import (ElasticityPlan, GroupIntegrator, Integrator, ScalarPla
 __all__ = ["BilinearForm", "LinearForm", "symbolic_structure"]
 
 
-def symbolic_structure(c2d: torch.Tensor, n_dof: int, status: Optional[torch.Tensor] = None):
+def _mark(marks, label):
+    """Record a CUDA event labelled `label` into `marks` (timing instrumentation)."""
+    if marks is not None:
+        e = torch.cuda.Event(enable_timing=True)
+        e.record()
+        marks.append((label, e))
+
+
+def symbolic_structure(c2d: torch.Tensor, n_dof: int, status: Optional[torch.Tensor] = None, marks=None):
     """(adj_ptr, adj, indptr, indices) for a cell-to-dof map."""
     st = _lib.status_word(c2d.device) if status is None else status
     adj_ptr, adj, _ = K.build_adjacency(c2d, n_dof, st)
+    _mark(marks, "adjacency")
     indptr, indices = K.build_pattern(adj_ptr, adj, c2d, n_dof, st)
+    _mark(marks, "pattern")
     return adj_ptr, adj, indptr, indices
 
 
@@ -103,21 +113,22 @@ class BilinearForm(_Form):
                 raise NotImplementedError("only several scalar integrators can share one form")
         return out
 
-    def _symbolic(self, space, c2d, n):
+    def _symbolic(self, space, c2d, n, marks=None):
         key = ("symbolic", n)
         cache = getattr(space, "_cache", {})
         if self.reuse_pattern and key in cache:
             return cache[key]
-        out = symbolic_structure(c2d, n)
+        out = symbolic_structure(c2d, n, marks=marks)
         if self.reuse_pattern:
             cache[key] = out
         return out
 
-    def assembly(self, *, format="csr", dtype=torch.float64, emit_f32: bool = False) -> CSRTensor:
+    def assembly(self, *, format="csr", dtype=torch.float64, emit_f32: bool = False, marks=None) -> CSRTensor:
         """Assemble the global matrix.  ``dtype`` float64 (default) or float32
         selects the arithmetic of the factor and assembly kernels;
         ``emit_f32`` also stores a float copy of float64 values on the result
-        (used by the mixed-precision solver)."""
+        (used by the mixed-precision solver).  ``marks`` (a list) receives
+        labelled CUDA events after each sub-stage (instrumentation)."""
         if format not in ("csr", "coo"):
             raise ValueError(f"Unsupported format {format}.")
         if format == "coo":
@@ -125,27 +136,32 @@ class BilinearForm(_Form):
         space = self.space
         plan = self._plan()
         status = _lib.status_word(space.device)
+        _mark(marks, "start")
         if isinstance(plan, ScalarPlan):
             c2d = space.cell_to_dof()
             n = space.number_of_global_dofs()
-            adj_ptr, adj, indptr, indices = self._symbolic(space, c2d, n)
+            adj_ptr, adj, indptr, indices = self._symbolic(space, c2d, n, marks)
             mesh = space.mesh
             fac = K.cell_factors(mesh, plan.channels, plan.coef_matrix(), dtype, status)
+            _mark(marks, "factors")
             tab = torch.as_tensor(plan.tables, dtype=dtype, device=space.device)
             values, v32 = K.assemble_scalar(adj_ptr, adj, c2d, tab, fac, indptr, indices,
                                             values_f32=emit_f32 and dtype == torch.float64, status=status)
+            _mark(marks, "values")
         elif isinstance(plan, ElasticityPlan):
             ss = space.scalar_space
             mesh = ss.mesh
             cell = mesh.cell
             NN = mesh.number_of_nodes()
-            adj_ptr, adj, nptr, nidx = self._symbolic(ss, cell, NN)
+            adj_ptr, adj, nptr, nidx = self._symbolic(ss, cell, NN, marks)
             indptr, indices = K.expand_blocks(NN, plan.gd, space.dof_priority, nptr, nidx)
             n = space.number_of_global_dofs()
             fac = K.cell_factors(mesh, plan.channels, plan.coef_matrix(), dtype, status)
+            _mark(marks, "factors")
             values, v32 = K.assemble_elasticity_p1(plan.gd, adj_ptr, adj, cell, fac, nptr, nidx, indptr,
                                                    indices.numel(), values_f32=emit_f32 and dtype == torch.float64,
                                                    status=status)
+            _mark(marks, "values")
         else:
             raise NotImplementedError
         _lib.check_status_word("assembly", status)

@@ -64,8 +64,10 @@ typedef struct fgb_pcg_info {
   double kernel_ms;   /* profile != 0: summed CUDA-event time of the SpMV   */
                       /* kernel of the iterations that did work             */
   int64_t kernel_launches; /* number of SpMV launches summed in kernel_ms   */
-  double other_ms;    /* profile != 0: CUDA-event time of the rest of those */
-                      /* iterations (vector updates, reliable updates)      */
+  double other_ms;    /* profile != 0: CUDA-event time of the vector-update */
+                      /* kernel of those iterations                         */
+  double extra_ms;    /* profile != 0: time of the remaining kernels of     */
+                      /* those iterations (p update, reliable-update check) */
 } fgb_pcg_info;
 
 /* Cell-factor channel kinds for fgb_cell_factors (k, l, a in 0..TD-1):
