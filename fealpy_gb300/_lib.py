@@ -47,7 +47,8 @@ PCG_REASONS = {0: "running", 1: "atol", 2: "rtol", 3: "maxit", 4: "zero rhs", 5:
 class PcgInfo(ctypes.Structure):
     _fields_ = [("niter", c_i64), ("residual", c_dbl), ("b_norm", c_dbl), ("true_relres", c_dbl),
                 ("reason", c_i32), ("n_updates", c_i32), ("launches", c_i64), ("kernel_ms", c_dbl),
-                ("kernel_launches", c_i64), ("other_ms", c_dbl), ("extra_ms", c_dbl)]
+                ("kernel_launches", c_i64), ("other_ms", c_dbl), ("extra_ms", c_dbl), ("graph", c_i32),
+                ("reserved", c_i32)]
 
 
 # name: (restype, [argtypes])

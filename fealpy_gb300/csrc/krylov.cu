@@ -548,6 +548,8 @@ int run_pcg_f64(int64_t n, const int64_t* indptr, const int32_t* indices, const 
     info->kernel_launches = prof.launches;
     info->other_ms = 0.0;
     info->extra_ms = 0.0;
+    info->graph = 0;
+    info->reserved = 0;
   }
   return finish_status(h.done);
 }
@@ -622,6 +624,8 @@ int run_pcg_mixed(int64_t n, const int64_t* indptr, const int32_t* indices, cons
     info->kernel_launches = prof.launches;
     info->other_ms = 0.0;
     info->extra_ms = 0.0;
+    info->graph = 0;
+    info->reserved = 0;
   }
   return finish_status(h.done);
 }

@@ -674,8 +674,13 @@ void mixed_body(const SellView& A, const float* val32, const double* val64, cons
   rec(ev, 4, s);
 }
 
+// Returns FGB_OK after the graph ran to completion.  *launched tells the caller
+// whether anything was submitted: when graph construction fails before the
+// launch (a feature missing in the driver), the caller falls back to the
+// host-polled loop, which runs the same kernels.
 template <typename Body>
-int graph_loop(Body body_two_iters, SellPcgState* st, cudaStream_t s, int64_t* launches) {
+int graph_loop(Body body_two_iters, SellPcgState* st, cudaStream_t s, bool need_if, bool* launched) {
+  *launched = false;
   // Build: while(cond) { two iterations ; loop_ctl }.  Two iterations per trip
   // keep the p ping-pong parity fixed inside the body.
   cudaGraph_t g = nullptr;
@@ -699,7 +704,7 @@ int graph_loop(Body body_two_iters, SellPcgState* st, cudaStream_t s, int64_t* l
   }
   cudaGraph_t body = cp.conditional.phGraph_out[0];
   CaptureCtx ctx;
-  if (cudaGraphConditionalHandleCreate(&ctx.hif, body, 0, cudaGraphCondAssignDefault) != cudaSuccess) {
+  if (need_if && cudaGraphConditionalHandleCreate(&ctx.hif, body, 0, cudaGraphCondAssignDefault) != cudaSuccess) {
     cudaGraphDestroy(g);
     return FGB_ERR_CUDA;
   }
@@ -714,12 +719,15 @@ int graph_loop(Body body_two_iters, SellPcgState* st, cudaStream_t s, int64_t* l
   }
   cudaStream_t cs = ctx.cs;
   if (rc == FGB_OK && cudaGraphInstantiate(&ge, g, 0) != cudaSuccess) rc = FGB_ERR_CUDA;
-  if (rc == FGB_OK && cudaGraphLaunch(ge, s) != cudaSuccess) rc = FGB_ERR_CUDA;
-  if (rc == FGB_OK && cudaStreamSynchronize(s) != cudaSuccess) rc = FGB_ERR_CUDA;
+  if (rc != FGB_OK) cudaGetLastError();  // clear a non-sticky API error before falling back
+  if (rc == FGB_OK) {
+    *launched = true;
+    if (cudaGraphLaunch(ge, s) != cudaSuccess) rc = FGB_ERR_CUDA;
+    else if (cudaStreamSynchronize(s) != cudaSuccess) rc = FGB_ERR_CUDA;
+  }
   if (ge) cudaGraphExecDestroy(ge);
   cudaGraphDestroy(g);
   cudaStreamDestroy(cs);
-  (void)launches;
   return rc;
 }
 
@@ -829,19 +837,28 @@ int32_t fgb_pcg_sell_f64(const fgb_sell* A, const double* diag_inv, const double
   int rc = read_state(w.st, &h, s);
   if (rc) return rc;
   EventPairs prof(profile != 0, check_every);
+  int used_graph = 0;
   if (h.done == FGB_PCG_ZERO_RHS) {
     cudaMemsetAsync(x, 0, n * sizeof(double), s);
   } else {
     if ((rc = set_tol(w.st, rtol * h.b_norm, s))) return rc;
+    bool graphed = false;
     if (use_graph) {
+      bool launched = false;
       rc = graph_loop([&](CaptureCtx& c) {
         f64_body(v, A->val64, diag_inv, x, w, 0, nullptr, c.cs);
         f64_body(v, A->val64, diag_inv, x, w, 1, nullptr, c.cs);
-      }, w.st, s, &launches);
-      if (rc) return rc;
-      if ((rc = read_state(w.st, &h, s))) return rc;
-      launches += 7 * ((h.niter + 1) / 2 + 1);
-    } else {
+      }, w.st, s, false, &launched);
+      if (rc && launched) return rc;
+      if (rc == FGB_OK) {
+        graphed = true;
+        used_graph = 1;
+        if ((rc = read_state(w.st, &h, s))) return rc;
+        launches += 7 * ((h.niter + 1) / 2 + 1);
+      }
+      rc = FGB_OK;
+    }
+    if (!graphed) {
       int64_t it = 0;
       while (true) {
         const int64_t before = h.niter;
@@ -860,6 +877,8 @@ int32_t fgb_pcg_sell_f64(const fgb_sell* A, const double* diag_inv, const double
     info->kernel_launches = prof.launches;
     info->other_ms = prof.other;
     info->extra_ms = prof.extra;
+    info->graph = used_graph;
+    info->reserved = 0;
   }
   return finish(h.done);
 }
@@ -889,6 +908,7 @@ int32_t fgb_pcg_sell_mixed(const fgb_sell* A, const double* diag_inv64, const do
   int rc = read_state(w.st, &h, s);
   if (rc) return rc;
   EventPairs prof(profile != 0, check_every);
+  int used_graph = 0;
   if (h.done == FGB_PCG_ZERO_RHS) {
     cudaMemsetAsync(x, 0, n * sizeof(double), s);
   } else {
@@ -897,16 +917,24 @@ int32_t fgb_pcg_sell_mixed(const fgb_sell* A, const double* diag_inv64, const do
     sell_mixed_reliable<<<sell_grid(v.n_slices), kSellThreads, 0, s>>>(v, A->val64, b, x, diag_inv64, w.dinv32, w.r,
                                                                        w.z, w.p0, w.partials, w.st, 1);
     ++launches;
+    bool graphed = false;
     if (use_graph) {
+      bool launched = false;
       rc = graph_loop([&](CaptureCtx& c) {
         mixed_body(v, A->val32, A->val64, diag_inv64, b, x, w, delta, 0, nullptr, c.cs, &c);
         mixed_body(v, A->val32, A->val64, diag_inv64, b, x, w, delta, 1, nullptr, c.cs, &c);
-      }, w.st, s, &launches);
-      if (rc) return rc;
-      if ((rc = read_state(w.st, &h, s))) return rc;
-      // per trip: 2 x (SpMV + update) + loop control; reliable updates when due
-      launches += 5 * ((h.niter + 1) / 2 + 1) + h.n_updates;
-    } else {
+      }, w.st, s, true, &launched);
+      if (rc && launched) return rc;
+      if (rc == FGB_OK) {
+        graphed = true;
+        used_graph = 1;
+        if ((rc = read_state(w.st, &h, s))) return rc;
+        // per trip: 2 x (SpMV + update) + loop control; reliable updates when due
+        launches += 5 * ((h.niter + 1) / 2 + 1) + h.n_updates;
+      }
+      rc = FGB_OK;
+    }
+    if (!graphed) {
       int64_t it = 0;
       while (true) {
         const int64_t before = h.niter;
@@ -926,6 +954,8 @@ int32_t fgb_pcg_sell_mixed(const fgb_sell* A, const double* diag_inv64, const do
     info->kernel_launches = prof.launches;
     info->other_ms = prof.other;
     info->extra_ms = prof.extra;
+    info->graph = used_graph;
+    info->reserved = 0;
   }
   return finish(h.done);
 }
