@@ -250,7 +250,8 @@ def run_ours(args):
                          "kernel_ms_avg": kms / max(kl, 1), "kernel_launches": kl, "launches": launches,
                          "other_ms_avg": pinfo["other_ms"] / max(kl, 1),
                          "extra_ms_avg": pinfo["extra_ms"] / max(kl, 1), "stages_ms": stages,
-                         "clocks": clocks, "nnz": A2.nnz, "n": gdof}
+                         "clocks": clocks, "nnz": A2.nnz, "n": gdof,
+                         "sell_launch": list(A2._sell.launch) if getattr(A2, "_sell", None) is not None else None}
 
     if set(modes) != {"fp64", "mixed"} or args.no_e2e:
         # profiling run: report the per-mode timings on stderr only
@@ -334,11 +335,13 @@ def run_ours(args):
                              "reliable_updates": mixed["n_updates"], "true_relres": mixed["relres"],
                              "max_rel_err_vs_fp64": err, "stages_ms": mixed["stages_ms"],
                              "spmv_us": mixed["kernel_ms_avg"] * 1e3, "update_us": mixed["other_ms_avg"] * 1e3,
-                             "other_kernels_us": mixed["extra_ms_avg"] * 1e3},
+                             "other_kernels_us": mixed["extra_ms_avg"] * 1e3,
+                             "sell_launch_threads_blocks": mixed["sell_launch"]},
             "fp64": {"ms_per_step": fp64["ms_per_step"], "dof_per_s": world * gdof / (fp64["ms_per_step"] / 1e3),
                      "cg_iters": fp64["niter"], "true_relres": fp64["relres"], "stages_ms": fp64["stages_ms"],
                      "spmv_us": fp64["kernel_ms_avg"] * 1e3, "update_us": fp64["other_ms_avg"] * 1e3,
-                     "other_kernels_us": fp64["extra_ms_avg"] * 1e3},
+                     "other_kernels_us": fp64["extra_ms_avg"] * 1e3,
+                     "sell_launch_threads_blocks": fp64["sell_launch"]},
             "speedup_fp32_refined_vs_fp64": fp64["ms_per_step"] / mixed["ms_per_step"],
             "e2e": {"value": world * gdof * e2e_steps / (e2e_ms / 1e3), "unit": "DOF/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "steps": e2e_steps},

@@ -96,7 +96,7 @@ _SIGNATURES = {
 class SellDesc(ctypes.Structure):
     """``fgb_sell`` (include/fealpy_gb300.h)."""
     _fields_ = [("n", c_i64), ("n_slices", c_i64), ("slice_ptr", c_vp), ("perm", c_vp), ("col", c_vp),
-                ("val64", c_vp), ("val32", c_vp)]
+                ("val64", c_vp), ("val32", c_vp), ("threads", c_i32), ("blocks", c_i32)]
 
 
 def library_path() -> str:

@@ -43,7 +43,34 @@ struct SellView {
   const int64_t* slice_ptr;
   const int32_t* perm;
   const int32_t* col;
+  int threads;  // launch shape of the slice kernels (0: defaults)
+  int blocks;
 };
+
+// Launch shapes.  Vector kernels: one 1024-thread block per SM (fewer blocks
+// shorten the tail of the deterministic block reduction).  Slice kernels: the
+// shape carried by the SELL descriptor (chosen by the autotuner), else 256
+// threads and up to 8 blocks per SM.
+struct Launch {
+  int blocks, threads;
+};
+
+inline Launch vec_launch(int64_t n) {
+  const int64_t b = (n + 1023) / 1024;
+  return {static_cast<int>(b < 1 ? 1 : (b > kNumSMs ? kNumSMs : b)), 1024};
+}
+
+inline Launch slice_launch(const SellView& A) {
+  const int t = A.threads > 0 ? A.threads : kSellThreads;
+  const int cap = A.blocks > 0 ? A.blocks : kSellMaxBlocks;
+  int64_t b = (A.n_slices * 32 + t - 1) / t;
+  if (b < 1) b = 1;
+  if (b > cap) b = cap;
+  return {static_cast<int>(b), t};
+}
+
+#define SLICE_LAUNCH(A, s) slice_launch(A).blocks, slice_launch(A).threads, 0, s
+#define VEC_LAUNCH(n, s) vec_launch(n).blocks, vec_launch(n).threads, 0, s
 
 // -------------------------------------------------------------- construction
 __global__ void sell_sort_windows(int64_t n, const int64_t* __restrict__ indptr, int32_t* __restrict__ perm,
@@ -197,7 +224,7 @@ struct GatherP {
 };
 
 template <typename T>
-__global__ void __launch_bounds__(kSellThreads) sell_spmv_kernel(SellView A, const T* __restrict__ val,
+__global__ void __launch_bounds__(1024, 1) sell_spmv_kernel(SellView A, const T* __restrict__ val,
                                                                  const T* __restrict__ x, T* __restrict__ y) {
   const int lane = threadIdx.x & 31;
   const int64_t warp = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
@@ -223,7 +250,7 @@ struct SellPcgState {
 // Last-block-done deterministic reduction of two FP64 partials per block.
 __device__ bool sell_last_block(double v0, double v1, double* partials, unsigned int* counter, double* out0,
                                 double* out1) {
-  __shared__ double red[kSellThreads / 32];
+  __shared__ double red[32];  // one slot per warp of a block of up to 1024 threads
   __shared__ bool am_last;
   double s0 = block_sum(v0, red);
   __syncthreads();
@@ -274,7 +301,7 @@ __device__ __forceinline__ T sell_row_dot_x(const SellView& A, const T* __restri
 
 // r = b - A x ; z = Dinv r ; p = z ; rz, b.b   (T = FP64 state)
 template <typename T>
-__global__ void __launch_bounds__(kSellThreads) sell_pcg_init(SellView A, const T* __restrict__ val,
+__global__ void __launch_bounds__(1024, 1) sell_pcg_init(SellView A, const T* __restrict__ val,
                                                               const T* __restrict__ dinv, const T* __restrict__ b,
                                                               const T* __restrict__ x, T* __restrict__ r,
                                                               T* __restrict__ z, T* __restrict__ p, double* partials,
@@ -314,7 +341,7 @@ __global__ void __launch_bounds__(kSellThreads) sell_pcg_init(SellView A, const 
 // rate of this part is low enough that a second FMA per entry would cost more
 // than the extra streaming pass over p).
 template <typename T, bool FUSED>
-__global__ void __launch_bounds__(kSellThreads) sell_pcg_spmv(SellView A, const T* __restrict__ val,
+__global__ void __launch_bounds__(1024, 1) sell_pcg_spmv(SellView A, const T* __restrict__ val,
                                                               const T* __restrict__ z, const T* __restrict__ p_old,
                                                               T* __restrict__ p_new, T* __restrict__ Ap,
                                                               double* partials, SellPcgState* st) {
@@ -350,7 +377,7 @@ __global__ void __launch_bounds__(kSellThreads) sell_pcg_spmv(SellView A, const 
 }
 
 // ||b|| (mixed solver set-up); marks a zero right-hand side
-__global__ void __launch_bounds__(kSellThreads) sell_bnorm(int64_t n, const double* __restrict__ b, double* partials,
+__global__ void __launch_bounds__(1024, 1) sell_bnorm(int64_t n, const double* __restrict__ b, double* partials,
                                                            SellPcgState* st) {
   double bb = 0.0;
   for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
@@ -367,7 +394,7 @@ __global__ void __launch_bounds__(kSellThreads) sell_bnorm(int64_t n, const doub
 }
 
 // p = z + beta p, in place (FP64 solver, before kernel A)
-__global__ void __launch_bounds__(kSellThreads) sell_p_update(int64_t n, const double* __restrict__ z,
+__global__ void __launch_bounds__(1024, 1) sell_p_update(int64_t n, const double* __restrict__ z,
                                                               double* __restrict__ p, const SellPcgState* st) {
   if (st->done) return;
   const double beta = st->beta;
@@ -377,7 +404,7 @@ __global__ void __launch_bounds__(kSellThreads) sell_p_update(int64_t n, const d
 }
 
 // kernel B (FP64 solver)
-__global__ void __launch_bounds__(kSellThreads) sell_pcg_update_f64(int64_t n, const double* __restrict__ dinv,
+__global__ void __launch_bounds__(1024, 1) sell_pcg_update_f64(int64_t n, const double* __restrict__ dinv,
                                                                     const double* __restrict__ p,
                                                                     const double* __restrict__ Ap,
                                                                     double* __restrict__ x, double* __restrict__ r,
@@ -413,30 +440,34 @@ __global__ void __launch_bounds__(kSellThreads) sell_pcg_update_f64(int64_t n, c
   }
 }
 
-// kernel B (mixed solver): x += alpha p in FP64, r -= alpha Ap and z = Dinv r in
-// FP32; decides whether a reliable update is due.
-__global__ void __launch_bounds__(kSellThreads) sell_mixed_update(int64_t n, const float* __restrict__ dinv,
+// kernel B (mixed solver): y += alpha p, r -= alpha Ap and z = Dinv r in FP32;
+// decides whether a reliable update is due.  y is the FP32 correction to the
+// FP64 iterate x accumulated since the last reliable update (x_true = x + y;
+// it is folded into x before each reliable update and at the end), so the
+// loop streams no FP64 vector.  Per-thread dot partials are FP32 (a thread
+// sums about n / (blocks * threads) terms); blocks and the grid add in FP64.
+__global__ void __launch_bounds__(1024, 1) sell_mixed_update(int64_t n, const float* __restrict__ dinv,
                                                                   const float* __restrict__ p,
-                                                                  const float* __restrict__ Ap, double* __restrict__ x,
+                                                                  const float* __restrict__ Ap, float* __restrict__ y,
                                                                   float* __restrict__ r, float* __restrict__ z,
                                                                   double* partials, SellPcgState* st, double delta,
                                                                   cudaGraphConditionalHandle hif, int set_if) {
   if (st->done) return;
-  const double alpha = st->alpha;
-  const float alpha32 = static_cast<float>(alpha);
-  double rz = 0.0, rr = 0.0;
+  const float alpha32 = static_cast<float>(st->alpha);
+  float rz = 0.0f, rr = 0.0f;
   for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
        i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-    x[i] += alpha * static_cast<double>(p[i]);
+    y[i] += alpha32 * p[i];
     const float ri = r[i] - alpha32 * Ap[i];
     const float zi = dinv[i] * ri;
     r[i] = ri;
     z[i] = zi;
-    rz += static_cast<double>(ri) * static_cast<double>(zi);
-    rr += static_cast<double>(ri) * static_cast<double>(ri);
+    rz += ri * zi;
+    rr += ri * ri;
   }
   double trz, trr;
-  if (sell_last_block(rz, rr, partials, &st->counter[2], &trz, &trr) && threadIdx.x == 0) {
+  if (sell_last_block(static_cast<double>(rz), static_cast<double>(rr), partials, &st->counter[2], &trz, &trr) &&
+      threadIdx.x == 0) {
     st->niter += 1;
     const double res = sqrt(trr);
     st->resid = res;
@@ -451,11 +482,23 @@ __global__ void __launch_bounds__(kSellThreads) sell_mixed_update(int64_t n, con
   }
 }
 
+// x += y ; y = 0 (mixed solver): before a reliable update when one is due, and
+// unconditionally (force = 1) when the solve ends.
+__global__ void __launch_bounds__(1024, 1) sell_mixed_fold(int64_t n, double* __restrict__ x, float* __restrict__ y,
+                                                        const SellPcgState* st, int force) {
+  if (!force && (st->done || !st->need_update)) return;
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    x[i] += static_cast<double>(y[i]);
+    y[i] = 0.0f;
+  }
+}
+
 // Reliable update (only when due, or first = 1 at the start): r64 = b - A64 x
 // with the FP64 values in FP64, true residual test, then r = float(r64),
 // z = Dinv r and beta from the replaced residual.  The first call also builds
 // the FP32 inverse diagonal and starts the direction p = z.
-__global__ void __launch_bounds__(kSellThreads) sell_mixed_reliable(SellView A, const double* __restrict__ val,
+__global__ void __launch_bounds__(1024, 1) sell_mixed_reliable(SellView A, const double* __restrict__ val,
                                                                     const double* __restrict__ b,
                                                                     const double* __restrict__ x,
                                                                     const double* __restrict__ dinv64,
@@ -514,10 +557,14 @@ using namespace fgb;
 
 namespace {
 
-int sell_grid(int64_t n_slices) { return grid_for(n_slices * 32, kSellThreads, kSellMaxBlocks); }
-int vec_grid(int64_t n) { return grid_for(n, kSellThreads, kSellMaxBlocks); }
+SellView view_of(const fgb_sell* A) {
+  return SellView{A->n, A->n_slices, A->slice_ptr, A->perm, A->col, A->threads, A->blocks};
+}
 
-SellView view_of(const fgb_sell* A) { return SellView{A->n, A->n_slices, A->slice_ptr, A->perm, A->col}; }
+bool launch_ok(const fgb_sell* A) {
+  return A->threads >= 0 && A->threads <= 1024 && A->threads % 32 == 0 && A->blocks >= 0 &&
+         A->blocks <= kSellMaxBlocks;
+}
 
 // CUDA events before the SpMV, after the SpMV and after the rest of each
 // iteration of a host-polled chunk; only iterations that did work (counted by
@@ -562,16 +609,25 @@ inline void rec(const cudaEvent_t* e, int j, cudaStream_t s) {
   if (e) cudaEventRecord(e[j], s);
 }
 
-// Capture state of the while-loop body.  add_if() appends an IF conditional
-// node (condition `hif`, set on the device by the update kernel) whose body
-// is whatever `fn` launches on the stream it is given.
+// Capture state of the while-loop body.  new_handle() makes a condition
+// handle on the body graph; add_if() appends an IF conditional node on that
+// handle (set on the device by an earlier kernel of the body) whose body is
+// whatever `fn` launches on the stream it is given.  Each IF node needs its
+// own handle: a second conditional node on a handle is rejected.
 struct CaptureCtx {
   cudaStream_t cs = nullptr;
-  cudaGraphConditionalHandle hif = 0;
+  cudaGraph_t body = nullptr;
   bool ok = true;
 
+  cudaGraphConditionalHandle new_handle() {
+    cudaGraphConditionalHandle h = 0;
+    if (cudaGraphConditionalHandleCreate(&h, body, 0, cudaGraphCondAssignDefault) != cudaSuccess) ok = false;
+    return h;
+  }
+
   template <typename Fn>
-  void add_if(Fn fn) {
+  void add_if(cudaGraphConditionalHandle hif, Fn fn) {
+    if (!ok) return;
     cudaStreamCaptureStatus status;
     cudaGraph_t g = nullptr;
     const cudaGraphNode_t* deps = nullptr;
@@ -615,7 +671,7 @@ struct F64Work {
 struct MixedWork {
   SellPcgState* st;
   double* partials;
-  float *r, *z, *p0, *p1, *Ap, *dinv32;
+  float *r, *z, *p0, *p1, *Ap, *dinv32, *y;
 };
 
 bool carve_f64(Carver& cv, int64_t n, F64Work& w) {
@@ -630,7 +686,7 @@ bool carve_mixed(Carver& cv, int64_t n, MixedWork& w) {
   w.st = cv.take<SellPcgState>(1);
   w.partials = cv.take<double>(2 * kSellMaxBlocks);
   w.r = cv.take<float>(n); w.z = cv.take<float>(n); w.p0 = cv.take<float>(n); w.p1 = cv.take<float>(n);
-  w.Ap = cv.take<float>(n); w.dinv32 = cv.take<float>(n);
+  w.Ap = cv.take<float>(n); w.dinv32 = cv.take<float>(n); w.y = cv.take<float>(n);
   return cv.ok;
 }
 
@@ -639,12 +695,11 @@ void f64_body(const SellView& A, const double* val, const double* dinv, double* 
               const cudaEvent_t* ev, cudaStream_t s) {
   (void)parity;
   rec(ev, 0, s);
-  sell_p_update<<<vec_grid(A.n), kSellThreads, 0, s>>>(A.n, w.z, w.p0, w.st);
+  sell_p_update<<<VEC_LAUNCH(A.n, s)>>>(A.n, w.z, w.p0, w.st);
   rec(ev, 1, s);
-  sell_pcg_spmv<double, false><<<sell_grid(A.n_slices), kSellThreads, 0, s>>>(A, val, w.z, w.p0, nullptr, w.Ap,
-                                                                             w.partials, w.st);
+  sell_pcg_spmv<double, false><<<SLICE_LAUNCH(A, s)>>>(A, val, w.z, w.p0, nullptr, w.Ap, w.partials, w.st);
   rec(ev, 2, s);
-  sell_pcg_update_f64<<<vec_grid(A.n), kSellThreads, 0, s>>>(A.n, dinv, w.p0, w.Ap, x, w.r, w.z, w.partials, w.st);
+  sell_pcg_update_f64<<<VEC_LAUNCH(A.n, s)>>>(A.n, dinv, w.p0, w.Ap, x, w.r, w.z, w.partials, w.st);
   rec(ev, 3, s);
   rec(ev, 4, s);
 }
@@ -657,19 +712,20 @@ void mixed_body(const SellView& A, const float* val32, const double* val64, cons
                 CaptureCtx* ctx = nullptr) {
   float* p_old = parity ? w.p1 : w.p0;
   float* p_new = parity ? w.p0 : w.p1;
+  const cudaGraphConditionalHandle hif = ctx ? ctx->new_handle() : 0;
   rec(ev, 0, s);
   rec(ev, 1, s);
-  sell_pcg_spmv<float, true><<<sell_grid(A.n_slices), kSellThreads, 0, s>>>(A, val32, w.z, p_old, p_new, w.Ap,
-                                                                           w.partials, w.st);
+  sell_pcg_spmv<float, true><<<SLICE_LAUNCH(A, s)>>>(A, val32, w.z, p_old, p_new, w.Ap, w.partials, w.st);
   rec(ev, 2, s);
-  sell_mixed_update<<<vec_grid(A.n), kSellThreads, 0, s>>>(A.n, w.dinv32, p_new, w.Ap, x, w.r, w.z, w.partials, w.st,
-                                                           delta, ctx ? ctx->hif : 0, ctx ? 1 : 0);
+  sell_mixed_update<<<VEC_LAUNCH(A.n, s)>>>(A.n, w.dinv32, p_new, w.Ap, w.y, w.r, w.z, w.partials, w.st, delta, hif,
+                                            ctx ? 1 : 0);
   rec(ev, 3, s);
   auto reliable = [&](cudaStream_t rs) {
-    sell_mixed_reliable<<<sell_grid(A.n_slices), kSellThreads, 0, rs>>>(A, val64, b, x, dinv64, w.dinv32, w.r, w.z,
-                                                                        nullptr, w.partials, w.st, 0);
+    sell_mixed_fold<<<VEC_LAUNCH(A.n, rs)>>>(A.n, x, w.y, w.st, 0);
+    sell_mixed_reliable<<<SLICE_LAUNCH(A, rs)>>>(A, val64, b, x, dinv64, w.dinv32, w.r, w.z, nullptr, w.partials,
+                                                 w.st, 0);
   };
-  if (ctx) ctx->add_if(reliable);
+  if (ctx) ctx->add_if(hif, reliable);
   else reliable(s);
   rec(ev, 4, s);
 }
@@ -679,7 +735,7 @@ void mixed_body(const SellView& A, const float* val32, const double* val64, cons
 // launch (a feature missing in the driver), the caller falls back to the
 // host-polled loop, which runs the same kernels.
 template <typename Body>
-int graph_loop(Body body_two_iters, SellPcgState* st, cudaStream_t s, bool need_if, bool* launched) {
+int graph_loop(Body body_two_iters, SellPcgState* st, cudaStream_t s, bool* launched) {
   *launched = false;
   // Build: while(cond) { two iterations ; loop_ctl }.  Two iterations per trip
   // keep the p ping-pong parity fixed inside the body.
@@ -704,10 +760,7 @@ int graph_loop(Body body_two_iters, SellPcgState* st, cudaStream_t s, bool need_
   }
   cudaGraph_t body = cp.conditional.phGraph_out[0];
   CaptureCtx ctx;
-  if (need_if && cudaGraphConditionalHandleCreate(&ctx.hif, body, 0, cudaGraphCondAssignDefault) != cudaSuccess) {
-    cudaGraphDestroy(g);
-    return FGB_ERR_CUDA;
-  }
+  ctx.body = body;
   cudaStreamCreateWithFlags(&ctx.cs, cudaStreamNonBlocking);
   if (cudaStreamBeginCaptureToGraph(ctx.cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
     rc = FGB_ERR_CUDA;
@@ -787,17 +840,17 @@ int32_t fgb_sell_fill(int64_t n, const int64_t* indptr, const int32_t* indices, 
 }
 
 int32_t fgb_sell_spmv(int32_t dtype, const fgb_sell* A, const void* x, void* y, void* stream) {
-  if (!A || !x || !y || A->n <= 0) return FGB_ERR_ARG;
+  if (!A || !x || !y || A->n <= 0 || !launch_ok(A)) return FGB_ERR_ARG;
   SellView v = view_of(A);
   cudaStream_t st = as_stream(stream);
   if (dtype == FGB_F64) {
     if (!A->val64) return FGB_ERR_ARG;
-    sell_spmv_kernel<double><<<sell_grid(v.n_slices), kSellThreads, 0, st>>>(v, A->val64, static_cast<const double*>(x),
-                                                                            static_cast<double*>(y));
+    sell_spmv_kernel<double><<<SLICE_LAUNCH(v, st)>>>(v, A->val64, static_cast<const double*>(x),
+                                                      static_cast<double*>(y));
   } else if (dtype == FGB_F32) {
     if (!A->val32) return FGB_ERR_ARG;
-    sell_spmv_kernel<float><<<sell_grid(v.n_slices), kSellThreads, 0, st>>>(v, A->val32, static_cast<const float*>(x),
-                                                                           static_cast<float*>(y));
+    sell_spmv_kernel<float><<<SLICE_LAUNCH(v, st)>>>(v, A->val32, static_cast<const float*>(x),
+                                                     static_cast<float*>(y));
   } else {
     return FGB_ERR_ARG;
   }
@@ -814,7 +867,7 @@ int32_t fgb_pcg_sell_f64(const fgb_sell* A, const double* diag_inv, const double
                          double rtol, int64_t maxit, int32_t check_every, int32_t norm, int32_t use_graph,
                          int32_t profile, void* workspace, size_t workspace_bytes, fgb_pcg_info* info,
                          void* stream) {
-  if (!A || A->n <= 0 || !A->val64 || !b || !x || maxit <= 0) return FGB_ERR_ARG;
+  if (!A || A->n <= 0 || !A->val64 || !b || !x || maxit <= 0 || !launch_ok(A)) return FGB_ERR_ARG;
   if (!workspace || workspace_bytes < fgb_pcg_sell_workspace_bytes(A->n)) return FGB_ERR_WORKSPACE;
   if (check_every <= 0) check_every = 16;
   if (use_graph) profile = 0;
@@ -831,8 +884,7 @@ int32_t fgb_pcg_sell_f64(const fgb_sell* A, const double* diag_inv, const double
   h.trip_cap = maxit / 2 + 2;
   int64_t launches = 0;
   cudaMemcpyAsync(w.st, &h, sizeof(SellPcgState), cudaMemcpyHostToDevice, s);
-  sell_pcg_init<double><<<sell_grid(v.n_slices), kSellThreads, 0, s>>>(v, A->val64, diag_inv, b, x, w.r, w.z, w.p0,
-                                                                       w.partials, w.st);
+  sell_pcg_init<double><<<SLICE_LAUNCH(v, s)>>>(v, A->val64, diag_inv, b, x, w.r, w.z, w.p0, w.partials, w.st);
   ++launches;
   int rc = read_state(w.st, &h, s);
   if (rc) return rc;
@@ -848,7 +900,7 @@ int32_t fgb_pcg_sell_f64(const fgb_sell* A, const double* diag_inv, const double
       rc = graph_loop([&](CaptureCtx& c) {
         f64_body(v, A->val64, diag_inv, x, w, 0, nullptr, c.cs);
         f64_body(v, A->val64, diag_inv, x, w, 1, nullptr, c.cs);
-      }, w.st, s, false, &launched);
+      }, w.st, s, &launched);
       if (rc && launched) return rc;
       if (rc == FGB_OK) {
         graphed = true;
@@ -886,7 +938,8 @@ int32_t fgb_pcg_sell_f64(const fgb_sell* A, const double* diag_inv, const double
 int32_t fgb_pcg_sell_mixed(const fgb_sell* A, const double* diag_inv64, const double* b, double* x, double rtol,
                            double delta, int64_t maxit, int32_t check_every, int32_t use_graph, int32_t profile,
                            void* workspace, size_t workspace_bytes, fgb_pcg_info* info, void* stream) {
-  if (!A || A->n <= 0 || !A->val64 || !A->val32 || !diag_inv64 || !b || !x || maxit <= 0) return FGB_ERR_ARG;
+  if (!A || A->n <= 0 || !A->val64 || !A->val32 || !diag_inv64 || !b || !x || maxit <= 0 || !launch_ok(A))
+    return FGB_ERR_ARG;
   if (!(delta > 0.0 && delta < 1.0)) return FGB_ERR_ARG;
   if (!workspace || workspace_bytes < fgb_pcg_sell_workspace_bytes(A->n)) return FGB_ERR_WORKSPACE;
   if (check_every <= 0) check_every = 16;
@@ -903,7 +956,8 @@ int32_t fgb_pcg_sell_mixed(const fgb_sell* A, const double* diag_inv64, const do
   h.trip_cap = maxit / 2 + 2;
   int64_t launches = 0;
   cudaMemcpyAsync(w.st, &h, sizeof(SellPcgState), cudaMemcpyHostToDevice, s);
-  sell_bnorm<<<vec_grid(n), kSellThreads, 0, s>>>(n, b, w.partials, w.st);
+  sell_bnorm<<<VEC_LAUNCH(n, s)>>>(n, b, w.partials, w.st);
+  cudaMemsetAsync(w.y, 0, n * sizeof(float), s);
   ++launches;
   int rc = read_state(w.st, &h, s);
   if (rc) return rc;
@@ -914,8 +968,8 @@ int32_t fgb_pcg_sell_mixed(const fgb_sell* A, const double* diag_inv64, const do
   } else {
     if ((rc = set_tol(w.st, rtol * h.b_norm, s))) return rc;
     // initial residual in FP64, its FP32 copy, z and p = z
-    sell_mixed_reliable<<<sell_grid(v.n_slices), kSellThreads, 0, s>>>(v, A->val64, b, x, diag_inv64, w.dinv32, w.r,
-                                                                       w.z, w.p0, w.partials, w.st, 1);
+    sell_mixed_reliable<<<SLICE_LAUNCH(v, s)>>>(v, A->val64, b, x, diag_inv64, w.dinv32, w.r, w.z, w.p0, w.partials,
+                                                w.st, 1);
     ++launches;
     bool graphed = false;
     if (use_graph) {
@@ -923,14 +977,14 @@ int32_t fgb_pcg_sell_mixed(const fgb_sell* A, const double* diag_inv64, const do
       rc = graph_loop([&](CaptureCtx& c) {
         mixed_body(v, A->val32, A->val64, diag_inv64, b, x, w, delta, 0, nullptr, c.cs, &c);
         mixed_body(v, A->val32, A->val64, diag_inv64, b, x, w, delta, 1, nullptr, c.cs, &c);
-      }, w.st, s, true, &launched);
+      }, w.st, s, &launched);
       if (rc && launched) return rc;
       if (rc == FGB_OK) {
         graphed = true;
         used_graph = 1;
         if ((rc = read_state(w.st, &h, s))) return rc;
-        // per trip: 2 x (SpMV + update) + loop control; reliable updates when due
-        launches += 5 * ((h.niter + 1) / 2 + 1) + h.n_updates;
+        // per trip: 2 x (SpMV + update) + loop control; fold + reliable update when due
+        launches += 5 * ((h.niter + 1) / 2 + 1) + 2 * h.n_updates;
       }
       rc = FGB_OK;
     }
@@ -940,13 +994,18 @@ int32_t fgb_pcg_sell_mixed(const fgb_sell* A, const double* diag_inv64, const do
         const int64_t before = h.niter;
         for (int k = 0; k < check_every; ++k, ++it)
           mixed_body(v, A->val32, A->val64, diag_inv64, b, x, w, delta, static_cast<int>(it & 1), prof.of(k), s);
-        launches += 3 * check_every;
+        launches += 4 * check_every;
         if (cudaGetLastError() != cudaSuccess) return FGB_ERR_CUDA;
         if ((rc = read_state(w.st, &h, s))) return rc;
         prof.collect(h.niter - before);
         if (h.done) break;
       }
     }
+    // the FP32 correction left over when the loop ended without a final
+    // reliable update (breakdown, non-finite values, trip cap)
+    sell_mixed_fold<<<VEC_LAUNCH(n, s)>>>(n, x, w.y, w.st, 1);
+    ++launches;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return FGB_ERR_CUDA;
   }
   if (info) {
     info->niter = h.niter; info->residual = h.resid; info->b_norm = h.b_norm; info->true_relres = h.true_rel;

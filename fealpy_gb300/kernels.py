@@ -229,11 +229,55 @@ class SellMatrix:
         self.slice_ptr, self.perm, self.col, self.val64, self.val32 = slice_ptr, perm, col, val64, val32
         self.desc = _lib.SellDesc(n, n_slices, slice_ptr.data_ptr(), perm.data_ptr(), col.data_ptr(),
                                   val64.data_ptr() if val64 is not None else None,
-                                  val32.data_ptr() if val32 is not None else None)
+                                  val32.data_ptr() if val32 is not None else None, 0, 0)
 
     @property
     def padded_nnz(self):
         return self.col.numel()
+
+    def set_launch(self, threads: int = 0, blocks: int = 0):
+        """Launch shape of the slice kernels (0, 0 = library defaults)."""
+        if threads and (threads % 32 or not 32 <= threads <= 1024):
+            raise ValueError("threads must be a multiple of 32 in [32, 1024]")
+        if blocks and not 1 <= blocks <= SELL_MAX_BLOCKS:
+            raise ValueError(f"blocks must be in [1, {SELL_MAX_BLOCKS}]")
+        self.desc.threads, self.desc.blocks = int(threads), int(blocks)
+
+    @property
+    def launch(self):
+        return int(self.desc.threads), int(self.desc.blocks)
+
+
+SELL_MAX_BLOCKS = 152 * 8
+# (threads, blocks cap) candidates of the slice-kernel autotuner: 8, 4, 2 and
+# 1 resident 256/512/1024-thread blocks per SM, plus grid-stride variants
+SELL_LAUNCH_CANDIDATES = ((256, 1216), (512, 608), (1024, 304), (1024, 152), (256, 608), (128, 1216))
+
+
+def sell_autotune(S: SellMatrix, dtype=torch.float32, reps: int = 20, candidates=SELL_LAUNCH_CANDIDATES):
+    """Pick the launch shape of the slice kernels by timing the SELL SpMV with
+    CUDA events on the current stream (after one warm-up call per shape).
+    Sets it on ``S`` and returns ``{(threads, blocks): microseconds}``."""
+    dev = S.col.device
+    x = torch.rand(S.n, dtype=dtype, device=dev)
+    y = torch.empty(S.n, dtype=dtype, device=dev)
+    code = dtype_code(dtype)
+    s = torch.cuda.current_stream(dev)
+    times = {}
+    for t, b in candidates:
+        S.set_launch(t, b)
+        call("fgb_sell_spmv", code, ctypes.byref(S.desc), ptr(x), ptr(y), stream_ptr(dev))
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(reps):
+            call("fgb_sell_spmv", code, ctypes.byref(S.desc), ptr(x), ptr(y), stream_ptr(dev))
+        e1.record(s)
+        e1.synchronize()
+        times[(t, b)] = 1000.0 * e0.elapsed_time(e1) / reps
+    best = min(times, key=times.get)
+    S.set_launch(*best)
+    return times
 
 
 def sell_build(indptr, indices, values64=None, values32=None, want64=True, want32=False) -> SellMatrix:

@@ -49,13 +49,30 @@ def _info_dict(info, extra=None):
     return out
 
 
-def _sell_of(A: CSRTensor, want32: bool):
-    """SELL-32 copy of A for the solvers (cached on the matrix)."""
+# Launch shape of the SELL slice kernels per (rows, padded entries, value
+# type), found once by timing the candidates (kernels.sell_autotune) and
+# reused for every later matrix of the same size.
+_LAUNCH_CACHE = {}
+
+
+def _sell_of(A: CSRTensor, want32: bool, tune: bool = True):
+    """SELL-32 copy of A for the solvers (cached on the matrix), with its
+    launch shape from the autotuner cache."""
     S = getattr(A, "_sell", None)
     if S is None or (want32 and S.val32 is None):
         v32 = A._f32 if (want32 and A._f32 is not None) else None
         S = K.sell_build(A.crow, A.col, A.values.to(torch.float64).contiguous(), v32, want64=True, want32=want32)
         A._sell = S
+        if tune:
+            dt = torch.float32 if want32 else torch.float64
+            key = (S.n, S.padded_nnz, dt)
+            shape = _LAUNCH_CACHE.get(key)
+            if shape is None:
+                times = K.sell_autotune(S, dt)
+                shape = min(times, key=times.get)
+                _LAUNCH_CACHE[key] = shape
+                logger.info(f"SELL launch shape for n={S.n}: {shape} ({times[shape]:.1f} us per SpMV)")
+            S.set_launch(*shape)
     return S
 
 

@@ -252,6 +252,9 @@ typedef struct fgb_sell {
   const int32_t* col;       /* slice_ptr[n_slices] column indices             */
   const double* val64;      /* FP64 values (optional)                         */
   const float* val32;       /* FP32 values (optional)                         */
+  int32_t threads;          /* launch shape of the slice kernels (SpMV, PCG   */
+  int32_t blocks;           /* residual/SpMV steps); 0 = defaults.  threads a */
+                            /* multiple of 32 in [32, 1024], blocks <= 1216   */
 } fgb_sell;
 
 /* No FEALPy counterpart: a solver-side layout of CSRTensor (the matrix the

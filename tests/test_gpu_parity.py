@@ -311,5 +311,37 @@ def test_sell_copy_spmv_and_solver_drivers(golden_dir):
     for graph in (True, False):
         x, info = F.cg_mixed(A, b, rtol=1e-10, returninfo=True, graph=graph)
         assert info["relres"] <= 1e-10 and rel_err(x, z["uh"]) < 1e-8
+        assert info["graph"] == graph, info
         xm[graph] = (x, info["niter"])
     assert xm[True][1] == xm[False][1] and torch.equal(xm[True][0], xm[False][0])
+
+
+def test_sell_launch_shapes_and_autotune(golden_dir):
+    """Every launch shape of the slice kernels gives the same SpMV bit for bit
+    (a lane owns its row whatever the grid) and a converged solve; the
+    autotuner times all candidates and keeps the fastest."""
+    dev = cuda()
+    import fealpy_gb300 as F
+    from fealpy_gb300 import kernels as K
+    from fealpy_gb300.sparse import CSRTensor
+    z = load(golden_dir, "c1_poisson_tri_p1_64.npz")
+    A = CSRTensor(torch.as_tensor(z["bc_crow"], device=dev), torch.as_tensor(z["bc_col"], device=dev),
+                  torch.as_tensor(z["bc_val"], device=dev), (len(z["bc_crow"]) - 1,) * 2)
+    b = torch.as_tensor(z["bc_F"], device=dev)
+    S = K.sell_build(A.crow, A.col, A.values, None, want64=True, want32=True)
+    x = torch.as_tensor(np.random.default_rng(3).normal(size=A.shape[0]), device=dev)
+    y0 = K.sell_spmv(S, x, torch.float64)
+    for shape in K.SELL_LAUNCH_CANDIDATES + ((32, 1), (96, 7)):
+        S.set_launch(*shape)
+        assert torch.equal(K.sell_spmv(S, x, torch.float64), y0), shape
+    with pytest.raises(ValueError):
+        S.set_launch(100, 1)
+    with pytest.raises(ValueError):
+        S.set_launch(256, K.SELL_MAX_BLOCKS + 1)
+    times = K.sell_autotune(S, torch.float32, reps=3)
+    assert set(times) == set(K.SELL_LAUNCH_CANDIDATES) and S.launch == min(times, key=times.get)
+    A._sell = S
+    for shape in ((32, 1), S.launch):
+        S.set_launch(*shape)
+        xs, info = F.cg_mixed(A, b, rtol=1e-10, returninfo=True)
+        assert info["relres"] <= 1e-10 and rel_err(xs, z["uh"]) < 1e-8, (shape, info)
