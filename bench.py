@@ -136,7 +136,7 @@ def build_problem(torch, F, node_np, cell_np, kappa_np, dev):
 STAGES = ("assembly (pattern + values)", "rhs", "dirichlet", "solver copy (SELL)", "pcg")
 
 
-def solve_step(torch, F, space, kappa, bc, mode, profile=False, marks=None, asm_marks=None):
+def solve_step(torch, F, space, kappa, bc, mode, profile=False, marks=None, asm_marks=None, graph=True):
     """symbolic + numeric assembly + RHS + Dirichlet + PCG; returns (x, info, A, F).
     ``marks``: optional list receiving a CUDA event after each stage;
     ``asm_marks``: optional list receiving labelled events inside the assembly."""
@@ -165,11 +165,11 @@ def solve_step(torch, F, space, kappa, bc, mode, profile=False, marks=None, asm_
     _sell_of(A2, want32=(mode == "mixed"))
     mark()
     if mode == "mixed":
-        x, info = F.cg_mixed(A2, F2, rtol=RTOL, maxit=MAXIT, returninfo=True, profile=profile)
+        x, info = F.cg_mixed(A2, F2, rtol=RTOL, maxit=MAXIT, returninfo=True, profile=profile, graph=graph)
     else:
         M = F.JacobiPreconditioner().apply(A2)
         x, info = F.cg(A2, F2, M=M, atol=0.0, rtol=RTOL, maxit=MAXIT, returninfo=True, stop="residual",
-                       profile=profile)
+                       profile=profile, graph=graph)
     mark()
     return x, info, A2, F2
 
@@ -211,7 +211,7 @@ def run_ours(args):
     modes = [m for m in args.modes.split(",") if m]
     for mode in modes:
         for _ in range(args.warmup):
-            solve_step(torch, F, space, kappa, bc, mode)
+            solve_step(torch, F, space, kappa, bc, mode, graph=not args.no_graph)
         barrier()
         sampler = ClockSampler(getattr(torch.cuda.get_device_properties(dev), "uuid", None) and
                                str(torch.cuda.get_device_properties(dev).uuid)) if mode == "mixed" else None
@@ -227,7 +227,7 @@ def run_ours(args):
         # NVTX range "timed_<mode>" lets a profiler capture exactly the timed steps
         torch.cuda.nvtx.range_push(f"timed_{mode}")
         for _ in range(args.steps):
-            x, info, A2, F2 = solve_step(torch, F, space, kappa, bc, mode, profile=False)
+            x, info, A2, F2 = solve_step(torch, F, space, kappa, bc, mode, profile=False, graph=not args.no_graph)
             infos.append(info)
         ev1.record(stream)
         torch.cuda.nvtx.range_pop()
@@ -315,7 +315,7 @@ def run_ours(args):
     achieved = bytes_per_launch / (mixed["kernel_ms_avg"] / 1e3) / 1e9 if mixed["kernel_ms_avg"] > 0 else 0.0
     traffic = None
     tp = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tp):
+    if os.path.exists(tp) and n == 64:
         try:
             traffic = json.load(open(tp)).get("pcg_spmv_f32_bytes_per_launch_at_n64")
         except Exception:
@@ -428,6 +428,9 @@ def main():
     ap.add_argument("--modes", default="fp64,mixed",
                     help="solver modes to time (a single-mode run is for profiling and prints no JSON line)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
+    ap.add_argument("--no-graph", action="store_true",
+                    help="host-polled solver loop instead of the CUDA-graph loop (profiling runs: a profiler "
+                         "cannot capture kernels inside a graph that has conditional nodes)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
