@@ -76,6 +76,8 @@ _SIGNATURES = {
     "fgb_pcg_workspace_bytes": (c_sz, [c_i64]),
     "fgb_pcg_f64": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_dbl, c_dbl, c_i64, c_i32, c_i32, c_i32,
                             c_i32, c_vp, c_sz, ctypes.POINTER(PcgInfo), c_vp]),
+    "fgb_pcg_f64_noalloc": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_dbl, c_dbl, c_i64, c_i32, c_i32,
+                                    c_i32, ctypes.POINTER(PcgInfo), c_vp]),
     "fgb_pcg_mixed_workspace_bytes": (c_sz, [c_i64]),
     "fgb_pcg_mixed": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_dbl, c_dbl, c_i64, c_i32, c_i32,
                               c_i32, c_vp, c_sz, ctypes.POINTER(PcgInfo), c_vp]),

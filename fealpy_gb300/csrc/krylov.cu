@@ -21,6 +21,7 @@
 
 #include <cmath>
 #include <cstring>
+#include <mutex>
 
 namespace fgb {
 
@@ -718,6 +719,62 @@ int32_t fgb_pcg_f64(int64_t n, const int64_t* indptr, const int32_t* indices, co
     case 32: return run_pcg_f64<32>(n, indptr, indices, values, diag_inv, b, x, atol, rtol, maxit, check_every, norm, profile, cv, info_host, s);
     default: return FGB_ERR_ARG;
   }
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// FP64 Jacobi-PCG without any allocation: the solver's scratch (state block,
+// reduction partials and the r, z, p, p', Ap vectors) lives in one static
+// device array of this library instead of a caller workspace.
+namespace {
+
+constexpr size_t cx_align(size_t b) { return (b + 255) / 256 * 256; }
+
+// Same layout and size as fgb_pcg_workspace_bytes(FGB_PCG_NOALLOC_MAX_ROWS):
+// 5 FP64 vectors of 65,536 rows + state + partials, about 2.6 MB.
+constexpr size_t kNoAllocScratchBytes = cx_align(sizeof(PcgState)) + cx_align(2 * kPcgMaxBlocks * sizeof(double)) +
+                                        5 * cx_align(static_cast<size_t>(FGB_PCG_NOALLOC_MAX_ROWS) * sizeof(double));
+
+__device__ __align__(256) unsigned char g_pcg_noalloc_scratch[kNoAllocScratchBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+// Device address of the static scratch on the current device, looked up once
+// per device (the lookup may load this library's device code on that device).
+int noalloc_scratch(void** out) {
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return FGB_ERR_CUDA;
+  if (dev >= kNoAllocMaxDevices) return FGB_ERR_CAPACITY;
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_pcg_noalloc_scratch) != cudaSuccess || !p) return FGB_ERR_CUDA;
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return FGB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t fgb_pcg_f64_noalloc(int64_t n, const int64_t* indptr, const int32_t* indices, const double* values,
+                            const double* diag_inv, const double* b, double* x, double atol, double rtol,
+                            int64_t maxit, int32_t check_every, int32_t lanes_per_row, int32_t norm,
+                            fgb_pcg_info* info_host, void* stream) {
+  if (n <= 0 || !indptr || !indices || !values || !b || !x || maxit <= 0) return FGB_ERR_ARG;
+  if (n > FGB_PCG_NOALLOC_MAX_ROWS) return FGB_ERR_CAPACITY;
+  if (fgb_pcg_workspace_bytes(n) > kNoAllocScratchBytes) return FGB_ERR_CAPACITY;
+  void* scratch = nullptr;
+  const int rc = noalloc_scratch(&scratch);
+  if (rc != FGB_OK) return rc;
+  // profile = 0: the event-timing option creates CUDA events, so it is not offered here
+  return fgb_pcg_f64(n, indptr, indices, values, diag_inv, b, x, atol, rtol, maxit, check_every, lanes_per_row, norm,
+                     0, scratch, kNoAllocScratchBytes, info_host, stream);
 }
 
 size_t fgb_pcg_mixed_workspace_bytes(int64_t n) {

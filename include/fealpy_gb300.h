@@ -224,6 +224,30 @@ int32_t fgb_pcg_f64(int64_t n, const int64_t* indptr, const int32_t* indices, co
                     int32_t profile, void* workspace, size_t workspace_bytes,
                     fgb_pcg_info* info_host, void* stream);
 
+/* fgb_pcg_f64 without a workspace, for callers that cannot allocate device
+ * memory at the point of the solve: a host code whose device memory is
+ * handed out by its own pool or capped in advance, a plain C/Fortran caller
+ * with no allocator of its own, or a loop that must not call cudaMalloc
+ * (which may synchronise the whole device).  No counterpart in FEALPy.
+ *
+ * Same arguments, iteration, stopping rules and info as fgb_pcg_f64 (no
+ * profile option).  The scratch is one static device array of this library
+ * sized for FGB_PCG_NOALLOC_MAX_ROWS rows (about 2.6 MB); larger n returns
+ * FGB_ERR_CAPACITY before any device work.  The caller zeroes nothing: each
+ * call writes the solver state (with its block-arrival counters, which must
+ * start at zero) before the first kernel, and every vector is written before
+ * it is read.  The first call on a device looks up the array's device address
+ * (and may load this library's device code): make it once per device, with
+ * that device current, before any stream capture.  The scratch is shared by
+ * all calls on a device, so calls that overlap in time (two host threads, or
+ * two streams) race on it: serialise them. */
+#define FGB_PCG_NOALLOC_MAX_ROWS 65536
+int32_t fgb_pcg_f64_noalloc(int64_t n, const int64_t* indptr, const int32_t* indices,
+                            const double* values, const double* diag_inv, const double* b,
+                            double* x, double atol, double rtol, int64_t maxit,
+                            int32_t check_every, int32_t lanes_per_row, int32_t norm,
+                            fgb_pcg_info* info_host, void* stream);
+
 /* Mixed precision: Jacobi-PCG iterations in FP32 on values32 (FP32 SpMV,
  * dots and updates) with FP64 reliable updates: whenever the FP32 residual
  * has dropped by `delta` since the last update (or looks converged), the
