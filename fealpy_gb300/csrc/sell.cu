@@ -37,7 +37,6 @@ __host__ __device__ __forceinline__ int64_t sell_pos(int lane, int k) {
 }
 constexpr int kSellThreads = 256;
 constexpr int kSellMaxBlocks = kNumSMs * 8;
-constexpr int kSellMaxWarps = kSellMaxBlocks * 32;  // blocks <= kSellMaxBlocks, threads <= 1024
 
 struct SellView {
   int64_t n, n_slices;
@@ -77,8 +76,8 @@ inline Launch slice_launch(const SellView& A) {
 
 #define SLICE_LAUNCH(A, s) slice_launch(A).blocks, slice_launch(A).threads, 0, s
 
-// warps of a slice-kernel launch (one p.Ap partial each)
-inline int slice_warps(const SellView& A) { return slice_launch(A).blocks * (slice_launch(A).threads / 32); }
+// blocks of a slice-kernel launch (one p.Ap partial each)
+inline int slice_blocks(const SellView& A) { return slice_launch(A).blocks; }
 #define VEC_LAUNCH(n, s) vec_launch(n).blocks, vec_launch(n).threads, 0, s
 
 // -------------------------------------------------------------- construction
@@ -350,18 +349,25 @@ __global__ void __launch_bounds__(1024, 1) sell_pcg_init(SellView A, const T* __
   }
 }
 
-// p.Ap of the SpMV step: the sum of its per-warp partials, formed by every
+// p.Ap of the SpMV step: the sum of its per-block partials, formed by every
 // block of the consuming kernel in the same order, so that all blocks hold the
-// bitwise-same value without a grid-wide reduction in the SpMV kernel (a block
-// reduction there makes every warp of a block wait for its slowest one, and
-// the last-block pass adds a serial tail: together about 10% of the SpMV).
-__device__ double sum_warp_partials(const double* wpart, int nwp) {
+// bitwise-same value without a grid-wide reduction in the SpMV kernel (the
+// last-block pass there adds a serial tail of a few microseconds).  Eight
+// independent loads per thread and trip keep the L2 round trips few.
+__device__ double sum_block_partials(const double* bpart, int nwp) {
   __shared__ double red[32];
   __shared__ double total;
-  double a = 0.0;
-  for (int k = threadIdx.x; k < nwp; k += blockDim.x) a += __ldcg(wpart + k);
-  a = block_sum(a, red);
-  if (threadIdx.x == 0) total = a;
+  double a[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  const int T = blockDim.x;
+  int k = threadIdx.x;
+  for (; k + 7 * T < nwp; k += 8 * T) {
+#pragma unroll
+    for (int u = 0; u < 8; ++u) a[u] += __ldcg(bpart + k + u * T);
+  }
+  for (; k < nwp; k += T) a[0] += __ldcg(bpart + k);
+  double v = ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
+  v = block_sum(v, red);
+  if (threadIdx.x == 0) total = v;
   __syncthreads();
   return total;
 }
@@ -379,8 +385,8 @@ __device__ __forceinline__ bool block_done(const SellPcgState* st) {
 // alpha = rz / p.Ap for the update kernels; false (and the solve marked done
 // by block 0) on breakdown or non-finite values, in which case every block
 // returns without touching the vectors.
-__device__ bool step_alpha(const double* wpart, int nwp, SellPcgState* st, double* alpha) {
-  const double pap = sum_warp_partials(wpart, nwp);
+__device__ bool step_alpha(const double* bpart, int nwp, SellPcgState* st, double* alpha) {
+  const double pap = sum_block_partials(bpart, nwp);
   if (!(pap > 0.0) || !isfinite(pap)) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
       st->done = isfinite(pap) ? FGB_PCG_BREAKDOWN : FGB_PCG_NONFINITE;
@@ -392,7 +398,7 @@ __device__ bool step_alpha(const double* wpart, int nwp, SellPcgState* st, doubl
   return true;
 }
 
-// kernel A: Ap = A p and per-warp partials of p.Ap.  FUSED: p_new = z + beta p_old is
+// kernel A: Ap = A p and per-block partials of p.Ap.  FUSED: p_new = z + beta p_old is
 // formed on the fly for every gathered column (one launch fewer per iteration;
 // used in FP32, where the extra FMA per entry is free).  Not FUSED: p has been
 // updated in place by sell_p_update beforehand (used in FP64, where the FMA
@@ -402,7 +408,13 @@ template <typename T, bool FUSED>
 __global__ void __launch_bounds__(1024, 1) sell_pcg_spmv(SellView A, const T* __restrict__ val,
                                                               const T* __restrict__ z, const T* __restrict__ p_old,
                                                               T* __restrict__ p_new, T* __restrict__ Ap,
-                                                              double* wpart, const SellPcgState* st) {
+                                                              double* bpart, const SellPcgState* st) {
+  // per-block combination of the warps' p.Ap without a block barrier at the
+  // end: the last warp of the block to arrive adds the warps' slots in order
+  __shared__ double wslot[32];
+  __shared__ unsigned int arrivals;
+  if (threadIdx.x == 0) arrivals = 0u;
+  __syncthreads();
   if (st->done) return;
   const T beta = static_cast<T>(st->beta);
   double pap = 0.0;
@@ -424,7 +436,18 @@ __global__ void __launch_bounds__(1024, 1) sell_pcg_spmv(SellView A, const T* __
     }
   }
   pap = warp_sum(pap);
-  if (lane == 0) wpart[warp0] = pap;
+  if (lane == 0) {
+    const unsigned int nw = blockDim.x >> 5;
+    wslot[threadIdx.x >> 5] = pap;
+    __threadfence_block();
+    if (atomicAdd(&arrivals, 1u) == nw - 1) {
+      __threadfence_block();
+      const volatile double* ws = wslot;
+      double t = 0.0;
+      for (unsigned int k = 0; k < nw; ++k) t += ws[k];
+      bpart[blockIdx.x] = t;
+    }
+  }
 }
 
 // ||b|| (mixed solver set-up); marks a zero right-hand side
@@ -459,11 +482,11 @@ __global__ void __launch_bounds__(1024, 1) sell_pcg_update_f64(int64_t n, const 
                                                                     const double* __restrict__ p,
                                                                     const double* __restrict__ Ap,
                                                                     double* __restrict__ x, double* __restrict__ r,
-                                                                    double* __restrict__ z, const double* wpart,
+                                                                    double* __restrict__ z, const double* bpart,
                                                                     int nwp, double* partials, SellPcgState* st) {
   if (block_done(st)) return;
   double alpha;
-  if (!step_alpha(wpart, nwp, st, &alpha)) return;
+  if (!step_alpha(bpart, nwp, st, &alpha)) return;
   double rz = 0.0, rr = 0.0;
   for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
        i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
@@ -502,12 +525,12 @@ __global__ void __launch_bounds__(1024, 1) sell_mixed_update(int64_t n, const fl
                                                                   const float* __restrict__ p,
                                                                   const float* __restrict__ Ap, float* __restrict__ y,
                                                                   float* __restrict__ r, float* __restrict__ z,
-                                                                  const double* wpart, int nwp, double* partials,
+                                                                  const double* bpart, int nwp, double* partials,
                                                                   SellPcgState* st, double delta,
                                                                   cudaGraphConditionalHandle hif, int set_if) {
   if (block_done(st)) return;
   double alpha;
-  if (!step_alpha(wpart, nwp, st, &alpha)) return;
+  if (!step_alpha(bpart, nwp, st, &alpha)) return;
   const float alpha32 = static_cast<float>(alpha);
   float rz = 0.0f, rr = 0.0f;
   for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
@@ -720,21 +743,21 @@ struct CaptureCtx {
 struct F64Work {
   SellPcgState* st;
   double* partials;
-  double* wpart;  // per-warp partials of the SpMV step
+  double* bpart;  // per-block p.Ap partials of the SpMV step
   double *r, *z, *p0, *p1, *Ap;
 };
 
 struct MixedWork {
   SellPcgState* st;
   double* partials;
-  double* wpart;
+  double* bpart;
   float *r, *z, *p0, *p1, *Ap, *dinv32, *y;
 };
 
 bool carve_f64(Carver& cv, int64_t n, F64Work& w) {
   w.st = cv.take<SellPcgState>(1);
   w.partials = cv.take<double>(2 * kSellMaxBlocks);
-  w.wpart = cv.take<double>(kSellMaxWarps);
+  w.bpart = cv.take<double>(kSellMaxBlocks);
   w.r = cv.take<double>(n); w.z = cv.take<double>(n); w.p0 = cv.take<double>(n); w.p1 = cv.take<double>(n);
   w.Ap = cv.take<double>(n);
   return cv.ok;
@@ -743,7 +766,7 @@ bool carve_f64(Carver& cv, int64_t n, F64Work& w) {
 bool carve_mixed(Carver& cv, int64_t n, MixedWork& w) {
   w.st = cv.take<SellPcgState>(1);
   w.partials = cv.take<double>(2 * kSellMaxBlocks);
-  w.wpart = cv.take<double>(kSellMaxWarps);
+  w.bpart = cv.take<double>(kSellMaxBlocks);
   w.r = cv.take<float>(n); w.z = cv.take<float>(n); w.p0 = cv.take<float>(n); w.p1 = cv.take<float>(n);
   w.Ap = cv.take<float>(n); w.dinv32 = cv.take<float>(n); w.y = cv.take<float>(n);
   return cv.ok;
@@ -756,9 +779,9 @@ void f64_body(const SellView& A, const double* val, const double* dinv, double* 
   rec(ev, 0, s);
   sell_p_update<<<VEC_LAUNCH(A.n, s)>>>(A.n, w.z, w.p0, w.st);
   rec(ev, 1, s);
-  sell_pcg_spmv<double, false><<<SLICE_LAUNCH(A, s)>>>(A, val, w.z, w.p0, nullptr, w.Ap, w.wpart, w.st);
+  sell_pcg_spmv<double, false><<<SLICE_LAUNCH(A, s)>>>(A, val, w.z, w.p0, nullptr, w.Ap, w.bpart, w.st);
   rec(ev, 2, s);
-  sell_pcg_update_f64<<<VEC_LAUNCH(A.n, s)>>>(A.n, dinv, w.p0, w.Ap, x, w.r, w.z, w.wpart, slice_warps(A),
+  sell_pcg_update_f64<<<VEC_LAUNCH(A.n, s)>>>(A.n, dinv, w.p0, w.Ap, x, w.r, w.z, w.bpart, slice_blocks(A),
                                               w.partials, w.st);
   rec(ev, 3, s);
   rec(ev, 4, s);
@@ -775,9 +798,9 @@ void mixed_body(const SellView& A, const float* val32, const double* val64, cons
   const cudaGraphConditionalHandle hif = ctx ? ctx->new_handle() : 0;
   rec(ev, 0, s);
   rec(ev, 1, s);
-  sell_pcg_spmv<float, true><<<SLICE_LAUNCH(A, s)>>>(A, val32, w.z, p_old, p_new, w.Ap, w.wpart, w.st);
+  sell_pcg_spmv<float, true><<<SLICE_LAUNCH(A, s)>>>(A, val32, w.z, p_old, p_new, w.Ap, w.bpart, w.st);
   rec(ev, 2, s);
-  sell_mixed_update<<<VEC_LAUNCH(A.n, s)>>>(A.n, w.dinv32, p_new, w.Ap, w.y, w.r, w.z, w.wpart, slice_warps(A),
+  sell_mixed_update<<<VEC_LAUNCH(A.n, s)>>>(A.n, w.dinv32, p_new, w.Ap, w.y, w.r, w.z, w.bpart, slice_blocks(A),
                                             w.partials, w.st, delta, hif, ctx ? 1 : 0);
   rec(ev, 3, s);
   auto reliable = [&](cudaStream_t rs) {
@@ -920,7 +943,7 @@ int32_t fgb_sell_spmv(int32_t dtype, const fgb_sell* A, const void* x, void* y, 
 size_t fgb_pcg_sell_workspace_bytes(int64_t n) {
   // sized for the larger (mixed) layout
   return align_up(sizeof(SellPcgState)) + align_up(2 * kSellMaxBlocks * sizeof(double)) +
-         align_up(kSellMaxWarps * sizeof(double)) + 5 * align_up(static_cast<size_t>(n) * sizeof(double)) +
+         align_up(kSellMaxBlocks * sizeof(double)) + 5 * align_up(static_cast<size_t>(n) * sizeof(double)) +
          7 * align_up(static_cast<size_t>(n) * sizeof(float));
 }
 
