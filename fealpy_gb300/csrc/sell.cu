@@ -201,11 +201,13 @@ template <> struct PackOf<double> { using type = Pack4D; };
 template <typename T> struct PacksPerTrip { static constexpr int value = 2; };
 template <> struct PacksPerTrip<float> { static constexpr int value = 4; };
 
-template <typename T, typename G>
-__device__ __forceinline__ T sell_row(const int32_t* __restrict__ col, const T* __restrict__ val, int64_t sbase, int w,
-                                      int lane, const G& g) {
-  using P = typename PackOf<T>::type;
-  constexpr int U = PacksPerTrip<T>::value;
+// V: stored value type, T: accumulation type (FP32 values of an FP32-assembled
+// matrix are accumulated in FP64 by the reliable update).
+template <typename V, typename T, typename G>
+__device__ __forceinline__ T sell_row_acc(const int32_t* __restrict__ col, const V* __restrict__ val, int64_t sbase,
+                                          int w, int lane, const G& g) {
+  using P = typename PackOf<V>::type;
+  constexpr int U = PacksPerTrip<V>::value;
   const int nq = w / kSellPack;
   T acc = T(0);
   int q = 0;
@@ -221,6 +223,12 @@ __device__ __forceinline__ T sell_row(const int32_t* __restrict__ col, const T* 
     acc = pack_dot<T>(a, g, acc);
   }
   return acc;
+}
+
+template <typename T, typename G>
+__device__ __forceinline__ T sell_row(const int32_t* __restrict__ col, const T* __restrict__ val, int64_t sbase, int w,
+                                      int lane, const G& g) {
+  return sell_row_acc<T, T, G>(col, val, sbase, w, lane, g);
 }
 
 template <typename T>
@@ -572,11 +580,13 @@ __global__ void __launch_bounds__(1024, 1) sell_mixed_fold(int64_t n, double* __
   }
 }
 
-// Reliable update (only when due, or first = 1 at the start): r64 = b - A64 x
-// with the FP64 values in FP64, true residual test, then r = float(r64),
-// z = Dinv r and beta from the replaced residual.  The first call also builds
-// the FP32 inverse diagonal and starts the direction p = z.
-__global__ void __launch_bounds__(1024, 1) sell_mixed_reliable(SellView A, const double* __restrict__ val,
+// Reliable update (only when due, or first = 1 at the start): r64 = b - A x in
+// FP64 arithmetic (V = double: the FP64 values; V = float: the values of an
+// FP32-assembled matrix, the operator the solve is for), true residual test,
+// then r = float(r64), z = Dinv r and beta from the replaced residual.  The
+// first call also builds the FP32 inverse diagonal and starts p = z.
+template <typename V>
+__global__ void __launch_bounds__(1024, 1) sell_mixed_reliable(SellView A, const V* __restrict__ val,
                                                                     const double* __restrict__ b,
                                                                     const double* __restrict__ x,
                                                                     const double* __restrict__ dinv64,
@@ -588,7 +598,7 @@ __global__ void __launch_bounds__(1024, 1) sell_mixed_reliable(SellView A, const
   SELL_WARP_LOOP(A) {
     const int64_t base = A.slice_ptr[s] + lane;
     const int w = static_cast<int>((A.slice_ptr[s + 1] - A.slice_ptr[s]) >> 5);
-    const double acc = sell_row_dot_x(A, val, base, w, x);
+    const double acc = sell_row_acc<V, double>(A.col, val, base - lane, w, lane, GatherX<double>{x});
     const int32_t row = A.perm[s * kSellC + lane];
     if (row >= 0) {
       const double r64 = b[row] - acc;
@@ -805,8 +815,12 @@ void mixed_body(const SellView& A, const float* val32, const double* val64, cons
   rec(ev, 3, s);
   auto reliable = [&](cudaStream_t rs) {
     sell_mixed_fold<<<VEC_LAUNCH(A.n, rs)>>>(A.n, x, w.y, w.st, 0);
-    sell_mixed_reliable<<<SLICE_LAUNCH(A, rs)>>>(A, val64, b, x, dinv64, w.dinv32, w.r, w.z, nullptr, w.partials,
-                                                 w.st, 0);
+    if (val64)
+      sell_mixed_reliable<double><<<SLICE_LAUNCH(A, rs)>>>(A, val64, b, x, dinv64, w.dinv32, w.r, w.z, nullptr,
+                                                           w.partials, w.st, 0);
+    else
+      sell_mixed_reliable<float><<<SLICE_LAUNCH(A, rs)>>>(A, val32, b, x, dinv64, w.dinv32, w.r, w.z, nullptr,
+                                                          w.partials, w.st, 0);
   };
   if (ctx) ctx->add_if(hif, reliable);
   else reliable(s);
@@ -1022,8 +1036,7 @@ int32_t fgb_pcg_sell_f64(const fgb_sell* A, const double* diag_inv, const double
 int32_t fgb_pcg_sell_mixed(const fgb_sell* A, const double* diag_inv64, const double* b, double* x, double rtol,
                            double delta, int64_t maxit, int32_t check_every, int32_t use_graph, int32_t profile,
                            void* workspace, size_t workspace_bytes, fgb_pcg_info* info, void* stream) {
-  if (!A || A->n <= 0 || !A->val64 || !A->val32 || !diag_inv64 || !b || !x || maxit <= 0 || !launch_ok(A))
-    return FGB_ERR_ARG;
+  if (!A || A->n <= 0 || !A->val32 || !diag_inv64 || !b || !x || maxit <= 0 || !launch_ok(A)) return FGB_ERR_ARG;
   if (!(delta > 0.0 && delta < 1.0)) return FGB_ERR_ARG;
   if (!workspace || workspace_bytes < fgb_pcg_sell_workspace_bytes(A->n)) return FGB_ERR_WORKSPACE;
   if (check_every <= 0) check_every = 16;
@@ -1052,8 +1065,12 @@ int32_t fgb_pcg_sell_mixed(const fgb_sell* A, const double* diag_inv64, const do
   } else {
     if ((rc = set_tol(w.st, rtol * h.b_norm, s))) return rc;
     // initial residual in FP64, its FP32 copy, z and p = z
-    sell_mixed_reliable<<<SLICE_LAUNCH(v, s)>>>(v, A->val64, b, x, diag_inv64, w.dinv32, w.r, w.z, w.p0, w.partials,
-                                                w.st, 1);
+    if (A->val64)
+      sell_mixed_reliable<double><<<SLICE_LAUNCH(v, s)>>>(v, A->val64, b, x, diag_inv64, w.dinv32, w.r, w.z, w.p0,
+                                                          w.partials, w.st, 1);
+    else
+      sell_mixed_reliable<float><<<SLICE_LAUNCH(v, s)>>>(v, A->val32, b, x, diag_inv64, w.dinv32, w.r, w.z, w.p0,
+                                                         w.partials, w.st, 1);
     ++launches;
     bool graphed = false;
     if (use_graph) {

@@ -59,9 +59,13 @@ def _sell_of(A: CSRTensor, want32: bool, tune: bool = True):
     """SELL-32 copy of A for the solvers (cached on the matrix), with its
     launch shape from the autotuner cache."""
     S = getattr(A, "_sell", None)
-    if S is None or (want32 and S.val32 is None):
-        v32 = A._f32 if (want32 and A._f32 is not None) else None
-        S = K.sell_build(A.crow, A.col, A.values.to(torch.float64).contiguous(), v32, want64=True, want32=want32)
+    if S is None or (want32 and S.val32 is None) or (not want32 and S.val64 is None):
+        if A.values.dtype == torch.float32 and want32:
+            # FP32-assembled operator: the FP32 values are the matrix (no FP64 copy)
+            S = K.sell_build(A.crow, A.col, None, A.values.contiguous(), want64=False, want32=True)
+        else:
+            v32 = A._f32 if (want32 and A._f32 is not None) else None
+            S = K.sell_build(A.crow, A.col, A.values.to(torch.float64).contiguous(), v32, want64=True, want32=want32)
         A._sell = S
         if tune:
             dt = torch.float32 if want32 else torch.float64
@@ -125,19 +129,29 @@ def cg_mixed(A: CSRTensor, b: torch.Tensor, x0: Optional[torch.Tensor] = None, M
              delta: float = 0.1, maxit: int = 100000, returninfo: bool = False, check_every: int = 32,
              lanes_per_row: int = 0, profile: bool = False, solver_format: str = "sell", graph: bool = True):
     """FP32 Jacobi-PCG iterations with FP64 reliable updates; stops on the true
-    FP64 relative residual.  ``M`` must be None (Jacobi from ``A`` is used) or
-    the diagonal CSR of ``JacobiPreconditioner``."""
+    relative residual computed in FP64 arithmetic.  ``M`` must be None (Jacobi
+    from ``A`` is used) or the diagonal CSR of ``JacobiPreconditioner``.
+
+    An FP64 ``A`` keeps its FP64 values for the residual recomputation (the
+    FP32 copy only drives the iterations).  An FP32 ``A`` (assembled with
+    ``dtype=torch.float32``) is the operator itself: the residual is formed
+    from its FP32 values in FP64 arithmetic, so the solve reaches ``rtol`` for
+    that operator, and the difference to the FP64-assembled solution is the
+    assembly's FP32 rounding."""
     if not isinstance(A, CSRTensor):
         raise NotImplementedError("cg_mixed takes a CSRTensor matrix")
     dinv = _diag_inv_of(M)
     if dinv is None:
         dinv = A.diagonal_inverse()
+    dinv = dinv.to(torch.float64).contiguous()
     b = b.to(dtype=torch.float64).contiguous()
     x = torch.zeros_like(b) if x0 is None else x0.to(torch.float64).clone()
     if solver_format == "sell":
         S = _sell_of(A, want32=True)
         info = K.pcg_sell_mixed(S, dinv, b, x, rtol, delta, maxit, check_every, graph and not profile, profile)
     elif solver_format == "csr":
+        if A.values.dtype != torch.float64:
+            raise NotImplementedError("solver_format='csr' cg_mixed needs an FP64 matrix")
         info = K.pcg_mixed(A.crow, A.col, A.values, A.values_f32(), dinv, b, x, rtol, delta, maxit, check_every,
                            lanes_per_row, profile)
     else:

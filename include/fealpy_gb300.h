@@ -296,7 +296,10 @@ int32_t fgb_sell_spmv(int32_t dtype, const fgb_sell* A, const void* x, void* y, 
 
 /* Jacobi-PCG on a SELL copy: same iteration, stopping rules and info as
  * fgb_pcg_f64 / fgb_pcg_mixed.  use_graph != 0 runs the iterations as a CUDA
- * graph with a device-side while loop (no host polling; profile ignored). */
+ * graph with a device-side while loop (no host polling; profile ignored).
+ * fgb_pcg_sell_mixed needs val32; its FP64 residual recomputation uses val64
+ * when present, else the FP32 values themselves (an FP32-assembled operator,
+ * accumulated in FP64), and then solves that operator to rtol. */
 size_t fgb_pcg_sell_workspace_bytes(int64_t n);
 int32_t fgb_pcg_sell_f64(const fgb_sell* A, const double* diag_inv, const double* b, double* x,
                          double atol, double rtol, int64_t maxit, int32_t check_every,

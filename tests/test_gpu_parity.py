@@ -223,6 +223,44 @@ def test_mixed_precision_reaches_fp64_accuracy():
     assert im["n_updates"] >= 1
 
 
+def test_fp32_assembly_refined_solve():
+    """FP32 cell-local assembly + FP32 inner CG + FP64 refinement: the FP32
+    matrix equals the FP64 one rounded (to FP32 accumulation accuracy), the
+    refinement reaches 1e-10 on the FP32 operator (residual in FP64
+    arithmetic), and the solution's error against the FP64-assembled solve is
+    of the order of FP32 rounding (stated bound 1e-5 relative, max norm)."""
+    dev = cuda()
+    import fealpy_gb300 as F
+    from fealpy_gb300.fem import BilinearForm, ScalarDiffusionIntegrator, ScalarMassIntegrator, DirichletBC
+    mesh = F.TetrahedronMesh.from_box([0, 1, 0, 1, 0, 1], 12, 12, 12, device=dev)
+    space = F.LagrangeFESpace(mesh, 2)
+    g = torch.Generator(device="cpu").manual_seed(0)
+    kappa = torch.exp(torch.randn(mesh.number_of_cells(), generator=g, dtype=torch.float64)).to(dev)
+    mats = {}
+    for dt in (torch.float64, torch.float32):
+        bf = BilinearForm(space)
+        bf.add_integrator(ScalarDiffusionIntegrator(coef=kappa, q=4), ScalarMassIntegrator(coef=1.0, q=4))
+        mats[dt] = bf.assembly(dtype=dt)
+    A64, A32 = mats[torch.float64], mats[torch.float32]
+    assert A32.values.dtype == torch.float32
+    assert torch.equal(A64.crow, A32.crow) and torch.equal(A64.col, A32.col)
+    assert rel_err(A32.values.double(), A64.values.cpu().numpy()) < 1e-6
+    n = space.number_of_global_dofs()
+    bc = DirichletBC(space, gd=0.0)
+    f = torch.ones(n, dtype=torch.float64, device=dev)
+    B64, F64 = bc.apply(A64, f)
+    B32, F32 = bc.apply(A32, f)
+    x64 = F.cg(B64, F64, M=F.JacobiPreconditioner().apply(B64), atol=1e-30, rtol=1e-12)
+    xm, im = F.cg_mixed(B32, F32, rtol=1e-10, returninfo=True)
+    Bd = F.CSRTensor(B32.crow, B32.col, B32.values.double(), B32.shape)
+    r = F32.double() - Bd @ xm
+    rel = float(torch.linalg.norm(r) / torch.linalg.norm(F32.double()))
+    assert rel <= 1e-10 * 1.0001, rel
+    assert im["relres"] <= 1e-10 and im["graph"]
+    err = float(torch.max(torch.abs(xm - x64)) / torch.max(torch.abs(x64)))
+    assert err < 1e-5, err
+
+
 def test_cg_edge_cases():
     dev = cuda()
     import fealpy_gb300 as F
