@@ -92,7 +92,33 @@ _SIGNATURES = {
                                  c_vp, c_sz, ctypes.POINTER(PcgInfo), c_vp]),
     "fgb_pcg_sell_mixed": (c_i32, [ctypes.c_void_p, c_vp, c_vp, c_vp, c_dbl, c_dbl, c_i64, c_i32, c_i32, c_i32,
                                    c_vp, c_sz, ctypes.POINTER(PcgInfo), c_vp]),
+    "fgb_batch_bytes": (c_sz, [c_i32, c_i32, c_i32]),
+    "fgb_batch_create": (c_i32, [c_i32, c_i32, c_i32, c_i32, c_vp, c_sz, ctypes.POINTER(c_vp)]),
+    "fgb_batch_destroy": (c_i32, [c_vp]),
+    "fgb_batch_set": (c_i32, [c_vp, c_i32, c_vp, c_i32, c_vp, c_vp, c_i32, c_vp, c_vp, c_vp]),
+    "fgb_batch_admit": (c_i32, [c_vp, c_i32, c_vp, c_vp, c_vp, c_dbl, c_vp]),
+    "fgb_batch_run": (c_i32, [c_vp, c_i64, c_i32, c_vp, ctypes.POINTER(c_i32), ctypes.POINTER(c_i32), c_vp]),
+    "fgb_batch_retire": (c_i32, [c_vp, c_i32, c_vp, c_vp]),
+    "fgb_batch_spmv": (c_i32, [c_vp, c_vp, c_vp, c_vp]),
 }
+
+
+class BatchSystem(ctypes.Structure):
+    """``fgb_batch_system`` (include/fealpy_gb300.h)."""
+    _fields_ = [("n", c_i64), ("n_slices", c_i64)] + [(k, c_vp) for k in (
+        "slice_ptr", "perm", "col", "val32", "val64", "dinv64", "b", "x", "r", "z", "p0", "p1", "Ap", "y", "dinv32")]
+
+
+class BatchState(ctypes.Structure):
+    """``fgb_batch_state``."""
+    _fields_ = [(k, c_dbl) for k in ("rz", "rz_prev", "rr", "alpha", "beta", "b_norm", "tol", "resid", "r_upd",
+                                     "true_rel", "delta")] + [("niter", c_i64), ("maxit", c_i64)] + [
+        (k, c_i32) for k in ("active", "done", "need_update", "n_updates", "parity", "reserved")]
+
+
+class BatchTile(ctypes.Structure):
+    """``fgb_batch_tile``."""
+    _fields_ = [("sys", c_i32), ("begin", c_i32), ("end", c_i32), ("reserved", c_i32)]
 
 
 class SellDesc(ctypes.Structure):

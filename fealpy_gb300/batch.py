@@ -1,0 +1,255 @@
+"""Batched FP32-refined Jacobi-PCG over many independent systems, with
+continuous batching (no FEALPy counterpart: FEALPy's ``fealpy/solver/cg.py``
+solves one system per call; this solves many at once on one GPU).
+
+Every system keeps its own SELL-32 copy, FP64 solution and FP32 Krylov
+vectors resident on the device.  The solver holds a fixed number of slots;
+``add`` places a system into a free slot, ``step`` admits the pending systems,
+runs the loop (one CUDA graph with a device-side while node) for at most a
+given number of iterations, and retires every system that finished.  Systems
+can be added between steps while others are in flight (continuous batching).
+
+Each system's iterates depend only on that system: all its reductions run
+over its own tiles in a fixed order, so a system solved alone and inside any
+mix gives the same bits.
+"""
+import ctypes
+from typing import Dict, List, Optional
+
+import numpy as np
+import torch
+
+from . import _lib
+from . import kernels as K
+from ._lib import call, ptr, stream_ptr
+from .sparse import CSRTensor
+
+__all__ = ["BatchSolver", "BatchResult"]
+
+
+class BatchResult:
+    """Outcome of one system: FP64 solution and its solve record."""
+
+    def __init__(self, key, x, niter, relres, reason, n_updates):
+        self.key, self.x, self.niter, self.relres, self.reason, self.n_updates = key, x, niter, relres, reason, n_updates
+
+    def info(self):
+        return {"niter": self.niter, "relres": self.relres, "reason": self.reason, "n_updates": self.n_updates}
+
+
+class _Slot:
+    def __init__(self, key, S, dinv64, b, x, vecs, rtol, maxit):
+        self.key, self.S, self.dinv64, self.b, self.x, self.vecs = key, S, dinv64, b, x, vecs
+        self.rtol, self.maxit = rtol, maxit
+        self.admitted = False
+
+
+class BatchSolver:
+    """Continuous-batching mixed-precision PCG.
+
+    ``slices_per_tile`` / ``rows_per_tile`` / ``slice_threads`` set the work
+    split of the batched kernels (see :func:`autotune`)."""
+
+    def __init__(self, max_systems: int = 256, *, max_slice_tiles: int = 1 << 16, max_row_tiles: int = 1 << 16,
+                 slices_per_tile: int = 16, rows_per_tile: int = 4096, slice_threads: int = 256,
+                 delta: float = 0.1, device=None):
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self.max_systems = int(max_systems)
+        self.max_slice_tiles, self.max_row_tiles = int(max_slice_tiles), int(max_row_tiles)
+        self.slices_per_tile, self.rows_per_tile = int(slices_per_tile), int(rows_per_tile)
+        self.slice_threads = int(slice_threads)
+        self.delta = float(delta)
+        lib = _lib.lib()
+        nbytes = int(lib.fgb_batch_bytes(self.max_systems, self.max_slice_tiles, self.max_row_tiles))
+        if nbytes == 0:
+            raise ValueError("invalid batch capacities")
+        self._buf = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
+        h = ctypes.c_void_p()
+        call("fgb_batch_create", self.max_systems, self.max_slice_tiles, self.max_row_tiles, self.slice_threads,
+             ptr(self._buf), nbytes, ctypes.byref(h))
+        self._h = h
+        self._slots: List[Optional[_Slot]] = [None] * self.max_systems
+        self._dirty = True
+        self._n_table = 0
+        self.launches = 0
+        self.used_graph = False
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                _lib.lib().fgb_batch_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    # ------------------------------------------------------------ systems
+    def free_slots(self) -> int:
+        return sum(1 for s in self._slots if s is None)
+
+    def active(self) -> int:
+        return self.max_systems - self.free_slots()
+
+    @staticmethod
+    def resident_bytes(n: int, nnz_padded: int, fp64_values: bool) -> int:
+        """Device bytes one system keeps resident (SELL copy + vectors)."""
+        return nnz_padded * (4 + 4 + (8 if fp64_values else 0)) + n * (8 + 8 + 8 + 7 * 4) + (n // 32 + 2) * 12
+
+    def add(self, A: CSRTensor, b: torch.Tensor, x0: Optional[torch.Tensor] = None, *, rtol: float = 1e-10,
+            maxit: int = 100000, key=None) -> int:
+        """Place ``A x = b`` in a free slot (admitted at the next ``step``);
+        returns the slot.  An FP32 ``A`` is its own operator; an FP64 ``A``
+        keeps FP64 values for the residual recomputation."""
+        if not isinstance(A, CSRTensor):
+            raise NotImplementedError("BatchSolver takes CSRTensor matrices")
+        try:
+            slot = self._slots.index(None)
+        except ValueError:
+            raise RuntimeError("no free slot in the batch") from None
+        n = A.shape[0]
+        if A.values.dtype == torch.float32:
+            S = K.sell_build(A.crow, A.col, None, A.values.contiguous(), want64=False, want32=True)
+        else:
+            S = K.sell_build(A.crow, A.col, A.values.to(torch.float64).contiguous(), None, want64=True, want32=True)
+        dinv64 = A.diagonal_inverse().to(torch.float64).contiguous()
+        b64 = b.to(self.device, torch.float64).contiguous()
+        x = torch.zeros(n, dtype=torch.float64, device=self.device) if x0 is None else \
+            x0.to(self.device, torch.float64).clone()
+        vecs = torch.empty((7, n), dtype=torch.float32, device=self.device)
+        self._slots[slot] = _Slot(slot if key is None else key, S, dinv64, b64, x, vecs, float(rtol), int(maxit))
+        self._dirty = True
+        return slot
+
+    # ------------------------------------------------------------ tables
+    def _tiles(self, sizes, per_tile, attr):
+        tiles, ptr_ = [], [0]
+        for s, lim in enumerate(sizes):
+            for a in range(0, lim, per_tile):
+                tiles.append((s, a, min(a + per_tile, lim), 0))
+            ptr_.append(len(tiles))
+        return tiles, ptr_
+
+    def _sync_tables(self):
+        used = [i for i, s in enumerate(self._slots) if s is not None]
+        n_sys = (max(used) + 1) if used else 0
+        systems = (_lib.BatchSystem * max(n_sys, 1))()
+        slice_sizes, row_sizes = [], []
+        for i in range(n_sys):
+            sl = self._slots[i]
+            if sl is None:
+                slice_sizes.append(0)
+                row_sizes.append(0)
+                continue
+            S, v = sl.S, sl.vecs
+            d = systems[i]
+            d.n, d.n_slices = S.n, S.n_slices
+            d.slice_ptr, d.perm, d.col = S.slice_ptr.data_ptr(), S.perm.data_ptr(), S.col.data_ptr()
+            d.val32 = S.val32.data_ptr()
+            d.val64 = S.val64.data_ptr() if S.val64 is not None else None
+            d.dinv64, d.b, d.x = sl.dinv64.data_ptr(), sl.b.data_ptr(), sl.x.data_ptr()
+            d.r, d.z, d.p0, d.p1, d.Ap, d.y, d.dinv32 = (v[k].data_ptr() for k in range(7))
+            slice_sizes.append(S.n_slices)
+            row_sizes.append(S.n)
+        st, sp = self._tiles(slice_sizes, self.slices_per_tile, "slices")
+        vt, vp = self._tiles(row_sizes, self.rows_per_tile, "rows")
+        if len(st) > self.max_slice_tiles or len(vt) > self.max_row_tiles:
+            raise RuntimeError("batch tile capacity exceeded: raise max_slice_tiles / max_row_tiles")
+        sta = (_lib.BatchTile * max(len(st), 1))(*[_lib.BatchTile(*t) for t in st])
+        vta = (_lib.BatchTile * max(len(vt), 1))(*[_lib.BatchTile(*t) for t in vt])
+        spa = (ctypes.c_int32 * (n_sys + 1))(*sp)
+        vpa = (ctypes.c_int32 * (n_sys + 1))(*vp)
+        call("fgb_batch_set", self._h, n_sys, systems, len(st), sta, spa, len(vt), vta, vpa,
+             stream_ptr(self.device))
+        self._n_table = n_sys
+        self._dirty = False
+
+    # ------------------------------------------------------------ running
+    def step(self, max_iterations: int = 1 << 40, graph: bool = True) -> List[BatchResult]:
+        """Admit pending systems, iterate all unfinished ones for at most
+        ``max_iterations`` iterations, retire and return those that finished."""
+        stream = stream_ptr(self.device)
+        pending = [i for i, s in enumerate(self._slots) if s is not None and not s.admitted]
+        if self._dirty:
+            self._sync_tables()
+        if pending:
+            n = len(pending)
+            slots = (ctypes.c_int32 * n)(*pending)
+            rt = (ctypes.c_double * n)(*[self._slots[i].rtol for i in pending])
+            mx = (ctypes.c_int64 * n)(*[self._slots[i].maxit for i in pending])
+            call("fgb_batch_admit", self._h, n, slots, rt, mx, self.delta, stream)
+            self.launches += 5
+            for i in pending:
+                self._slots[i].admitted = True
+        if self._n_table == 0:
+            return []
+        states = (_lib.BatchState * self._n_table)()
+        running = ctypes.c_int32()
+        graphed = ctypes.c_int32()
+        call("fgb_batch_run", self._h, int(max_iterations), int(bool(graph)), states, ctypes.byref(running),
+             ctypes.byref(graphed), stream)
+        self.used_graph = bool(graphed.value)
+        done = [i for i in range(self._n_table) if self._slots[i] is not None and states[i].done != 0]
+        out = []
+        if done:
+            arr = (ctypes.c_int32 * len(done))(*done)
+            call("fgb_batch_retire", self._h, len(done), arr, stream)
+            for i in done:
+                sl, stt = self._slots[i], states[i]
+                if stt.done == 4:  # zero right-hand side: x = 0
+                    sl.x.zero_()
+                out.append(BatchResult(sl.key, sl.x, int(stt.niter), float(stt.true_rel), int(stt.done),
+                                       int(stt.n_updates)))
+                self._slots[i] = None
+            self._dirty = True
+        return out
+
+    def solve_all(self, graph: bool = True) -> Dict[object, BatchResult]:
+        """Run until every system in the batch has finished."""
+        res = {}
+        while self.active():
+            for r in self.step(graph=graph):
+                res[r.key] = r
+        return res
+
+    # ------------------------------------------------------------ tuning
+    def spmv_time_us(self, reps: int = 10) -> float:
+        """Mean time of one batched FP32 SpMV over every system in the table."""
+        if self._dirty:
+            self._sync_tables()
+        n = self._n_table
+        xs = (ctypes.c_void_p * max(n, 1))()
+        ys = (ctypes.c_void_p * max(n, 1))()
+        keep = []
+        for i in range(n):
+            sl = self._slots[i]
+            if sl is None:
+                continue
+            x = torch.ones(sl.S.n, dtype=torch.float32, device=self.device)
+            y = torch.empty_like(x)
+            keep += [x, y]
+            xs[i], ys[i] = x.data_ptr(), y.data_ptr()
+        stream = stream_ptr(self.device)
+        s = torch.cuda.current_stream(self.device)
+        call("fgb_batch_spmv", self._h, xs, ys, stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(reps):
+            call("fgb_batch_spmv", self._h, xs, ys, stream)
+        e1.record(s)
+        e1.synchronize()
+        return 1000.0 * e0.elapsed_time(e1) / reps
+
+
+def autotune(systems, candidates=((8, 128), (16, 256), (32, 256), (64, 512), (16, 512), (128, 1024)),
+             device=None, **kw) -> Dict[tuple, float]:
+    """Choose (slices per tile, threads per block) of the batched slice
+    kernels by timing the batched SpMV of ``systems`` (a list of (A, b)) for
+    each candidate; returns {candidate: microseconds}."""
+    times = {}
+    for spt, thr in candidates:
+        bs = BatchSolver(max(len(systems), 1), slices_per_tile=spt, slice_threads=thr, device=device, **kw)
+        for A, b in systems:
+            bs.add(A, b)
+        times[(spt, thr)] = bs.spmv_time_us()
+        del bs
+    return times

@@ -1,0 +1,697 @@
+// Batched FP32-refined Jacobi-PCG: many independent systems (each with its own
+// SELL-32x4 copy and Krylov vectors) iterate together.  One iteration is four
+// kernels over tile lists plus a reliable-update branch:
+//
+//   slice tiles: Ap = A p_new with p_new = z + beta p_old formed per gathered
+//                column; per-tile partials of p.Ap
+//   systems    : alpha = rz / p.Ap per system (sum of its tiles, in order)
+//   row tiles  : y += alpha p, r -= alpha Ap, z = Dinv r; per-tile r.z, r.r
+//   control    : per system rz, rr, beta, stopping test, reliable update due?;
+//                any update due -> IF branch; nothing running -> end of loop
+//   IF branch  : x += y (row tiles), r64 = b - A x in FP64 arithmetic and the
+//                replaced r, z (slice tiles), true residual test (systems)
+//
+// Every reduction of a system adds its own tiles in tile order, and a
+// system's tiles depend only on its own sizes, so its iterates are the same
+// whatever else is in the batch.  Systems join (fgb_batch_admit) and leave
+// (fgb_batch_retire) between runs; the graph reads the tables from fixed
+// device addresses, so it is captured once per handle.
+
+#include "fgb_common.cuh"
+#include "sell_rows.cuh"
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <new>
+
+namespace fgb {
+
+constexpr int kBatchRowThreads = 512;
+constexpr int kBatchRowBlocks = 2 * kNumSMs;
+constexpr int kBatchSliceBlocks = 8 * kNumSMs;
+
+struct BatchCtl {
+  long long trips, trip_limit, if_trips;
+  int any_update, running;
+  int any_acc, running_acc;  // accumulated over the blocks of batch_control
+  unsigned int arrived;
+  int pad;
+};
+
+// Per-system sums of tile partials: one warp per system, lanes take every
+// 32nd tile and the warp adds them in a fixed tree, so the result does not
+// depend on timing.  `stride` partials per tile, component `c`.
+__device__ __forceinline__ double tile_sum(const double* __restrict__ part, int t0, int t1, int stride, int c) {
+  double v = 0.0;
+  for (int t = t0 + (threadIdx.x & 31); t < t1; t += 32) v += part[stride * t + c];
+  return warp_sum(v);
+}
+
+__device__ __forceinline__ int warp_system() { return (blockIdx.x * blockDim.x + threadIdx.x) >> 5; }
+
+// ---------------------------------------------------------------- kernels
+// Slice tiles: Ap, p_new and the tile's p.Ap.
+__global__ void __launch_bounds__(1024, 1) batch_spmv_step(const fgb_batch_system* __restrict__ sys,
+                                                           const fgb_batch_state* __restrict__ st,
+                                                           const fgb_batch_tile* __restrict__ tiles,
+                                                           const int32_t* __restrict__ n_tiles, double* spart) {
+  __shared__ double red[32];
+  const int nt = *n_tiles;
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+  for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+    const fgb_batch_tile tile = tiles[t];
+    const fgb_batch_state& S = st[tile.sys];
+    if (!S.active || S.done || S.need_update) {  // need_update: admission pending
+      if (threadIdx.x == 0) spart[t] = 0.0;
+      continue;
+    }
+    const fgb_batch_system& A = sys[tile.sys];
+    const float beta = static_cast<float>(S.beta);
+    const float* p_old = S.parity ? A.p1 : A.p0;
+    float* p_new = S.parity ? A.p0 : A.p1;
+    const GatherP<float> g{A.z, p_old, beta};
+    double pap = 0.0;
+    for (int64_t s = tile.begin + wib; s < tile.end; s += wpb) {
+      const int64_t sbase = A.slice_ptr[s];
+      const int w = static_cast<int>((A.slice_ptr[s + 1] - sbase) >> 5);
+      const float acc = sell_row(A.col, A.val32, sbase, w, lane, g);
+      const int32_t row = A.perm[s * kSellC + lane];
+      if (row >= 0) {
+        const float pi = A.z[row] + beta * p_old[row];
+        p_new[row] = pi;
+        A.Ap[row] = acc;
+        pap += static_cast<double>(pi) * static_cast<double>(acc);
+      }
+    }
+    const double b = block_sum(pap, red);
+    if (threadIdx.x == 0) spart[t] = b;
+    __syncthreads();
+  }
+}
+
+// Systems (a warp each): alpha = rz / p.Ap.
+__global__ void batch_alpha(int32_t n_sys, fgb_batch_state* st, const int32_t* __restrict__ tile_ptr,
+                            const double* __restrict__ spart) {
+  const int s = warp_system();
+  if (s >= n_sys) return;
+  fgb_batch_state& S = st[s];
+  if (!S.active || S.done || S.need_update) return;
+  const double pap = tile_sum(spart, tile_ptr[s], tile_ptr[s + 1], 1, 0);
+  if ((threadIdx.x & 31) != 0) return;
+  if (!(pap > 0.0) || !isfinite(pap)) {
+    S.done = isfinite(pap) ? FGB_PCG_BREAKDOWN : FGB_PCG_NONFINITE;
+    S.alpha = 0.0;
+  } else {
+    S.alpha = S.rz / pap;
+  }
+}
+
+// Row tiles: the FP32 updates and the tile's r.z, r.r.
+__global__ void __launch_bounds__(1024, 1) batch_update(const fgb_batch_system* __restrict__ sys,
+                                                        const fgb_batch_state* __restrict__ st,
+                                                        const fgb_batch_tile* __restrict__ tiles,
+                                                        const int32_t* __restrict__ n_tiles, double* vpart) {
+  __shared__ double red[32];
+  const int nt = *n_tiles;
+  for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+    const fgb_batch_tile tile = tiles[t];
+    const fgb_batch_state& S = st[tile.sys];
+    if (!S.active || S.done || S.need_update) {
+      if (threadIdx.x == 0) { vpart[2 * t] = 0.0; vpart[2 * t + 1] = 0.0; }
+      continue;
+    }
+    const fgb_batch_system& A = sys[tile.sys];
+    const float alpha = static_cast<float>(S.alpha);
+    const float* __restrict__ p = S.parity ? A.p0 : A.p1;  // written by the SpMV step
+    float rz = 0.0f, rr = 0.0f;
+    for (int i = tile.begin + threadIdx.x; i < tile.end; i += blockDim.x) {
+      A.y[i] += alpha * p[i];
+      const float ri = A.r[i] - alpha * A.Ap[i];
+      const float zi = A.dinv32[i] * ri;
+      A.r[i] = ri;
+      A.z[i] = zi;
+      rz += ri * zi;
+      rr += ri * ri;
+    }
+    const double a = block_sum(static_cast<double>(rz), red);
+    __syncthreads();
+    const double b = block_sum(static_cast<double>(rr), red);
+    if (threadIdx.x == 0) { vpart[2 * t] = a; vpart[2 * t + 1] = b; }
+    __syncthreads();
+  }
+}
+
+// Systems (a warp each): rz, rr, beta, stopping test and whether a reliable
+// update is due; the last block to finish sets the graph conditions.
+__global__ void batch_control(int32_t n_sys, fgb_batch_state* st, const int32_t* __restrict__ tile_ptr,
+                              const double* __restrict__ vpart, BatchCtl* ctl, cudaGraphConditionalHandle h_if,
+                              cudaGraphConditionalHandle h_while, int graph) {
+  __shared__ bool last;
+  int any = 0, running = 0;
+  const int s = warp_system();
+  if (s < n_sys) {
+    fgb_batch_state& S = st[s];
+    if (S.active && !S.done) {
+      if (S.need_update) {
+        running = 1;
+      } else {
+        const double rz = tile_sum(vpart, tile_ptr[s], tile_ptr[s + 1], 2, 0);
+        const double rr = tile_sum(vpart, tile_ptr[s], tile_ptr[s + 1], 2, 1);
+        if ((threadIdx.x & 31) == 0) {
+          S.niter += 1;
+          const double res = sqrt(rr);
+          S.resid = res;
+          S.rr = rr;
+          if (!isfinite(res)) {
+            S.done = FGB_PCG_NONFINITE;
+          } else {
+            S.need_update = (res < S.delta * S.r_upd) || (res < S.tol) || (S.niter >= S.maxit);
+            S.rz_prev = S.rz;
+            S.beta = rz / S.rz;
+            S.rz = rz;
+            S.parity ^= 1;
+          }
+          any = S.need_update && !S.done;
+          running = !S.done;
+        }
+      }
+    }
+  }
+  any = __syncthreads_or(any);
+  running = __syncthreads_or(running);
+  if (threadIdx.x == 0) {
+    if (any) atomicOr(&ctl->any_acc, 1);
+    if (running) atomicOr(&ctl->running_acc, 1);
+    __threadfence();
+    last = atomicAdd(&ctl->arrived, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last || threadIdx.x != 0) return;
+  __threadfence();
+  const int a = atomicOr(&ctl->any_acc, 0), r = atomicOr(&ctl->running_acc, 0);
+  ctl->any_acc = 0;
+  ctl->running_acc = 0;
+  ctl->arrived = 0u;
+  ctl->trips += 1;
+  ctl->if_trips += a ? 1 : 0;
+  ctl->any_update = a;
+  ctl->running = r;
+  if (graph) {
+    cudaGraphSetConditional(h_if, a ? 1u : 0u);
+    if (!r || ctl->trips >= ctl->trip_limit) cudaGraphSetConditional(h_while, 0u);
+  }
+}
+
+// Row tiles of systems with an update due (or all given slots when force):
+// x += y, y = 0.  Admission (need_update == 2) instead zeroes y and forms the
+// per-tile partials of b.b.
+__global__ void __launch_bounds__(1024, 1) batch_fold(const fgb_batch_system* __restrict__ sys,
+                                                      const fgb_batch_state* __restrict__ st,
+                                                      const fgb_batch_tile* __restrict__ tiles,
+                                                      const int32_t* __restrict__ n_tiles,
+                                                      const int32_t* __restrict__ force, double* vpart) {
+  __shared__ double red[32];
+  const int nt = *n_tiles;
+  for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+    const fgb_batch_tile tile = tiles[t];
+    const fgb_batch_state& S = st[tile.sys];
+    const bool forced = force && force[tile.sys];
+    const int mode = S.active ? S.need_update : 0;
+    const fgb_batch_system& A = sys[tile.sys];
+    if (forced || (mode == 1 && !S.done)) {
+      for (int i = tile.begin + threadIdx.x; i < tile.end; i += blockDim.x) {
+        A.x[i] += static_cast<double>(A.y[i]);
+        A.y[i] = 0.0f;
+      }
+    } else if (mode == 2 && !S.done) {
+      double bb = 0.0;
+      for (int i = tile.begin + threadIdx.x; i < tile.end; i += blockDim.x) {
+        A.y[i] = 0.0f;
+        bb += A.b[i] * A.b[i];
+      }
+      const double v = block_sum(bb, red);
+      if (threadIdx.x == 0) vpart[2 * t] = v;
+      __syncthreads();
+    }
+  }
+}
+
+// Admission: ||b||, tol = rtol * ||b|| (rtol was stored in tol), zero rhs.
+__global__ void batch_bnorm(int32_t n_sys, fgb_batch_state* st, const int32_t* __restrict__ tile_ptr,
+                            const double* __restrict__ vpart) {
+  const int s = warp_system();
+  if (s >= n_sys) return;
+  fgb_batch_state& S = st[s];
+  if (!S.active || S.done || S.need_update != 2) return;
+  const double bb = tile_sum(vpart, tile_ptr[s], tile_ptr[s + 1], 2, 0);
+  if ((threadIdx.x & 31) != 0) return;
+  S.b_norm = sqrt(bb);
+  S.tol = S.tol * S.b_norm;
+  if (S.b_norm < 1e-15) S.done = FGB_PCG_ZERO_RHS;
+}
+
+// Slice tiles of systems with an update due (1) or admitted (2): r64 = b - A x
+// in FP64 arithmetic, r = float(r64), z = Dinv r; per-tile r64.r64 and r.z.
+// Admission also builds the FP32 inverse diagonal and starts p_old = z.
+template <typename V>
+__device__ void reliable_tile(const fgb_batch_system& A, const fgb_batch_state& S, const V* __restrict__ val,
+                              const fgb_batch_tile& tile, int mode, double* rr_out, double* rz_out) {
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+  double rr64 = 0.0, rz = 0.0;
+  float* p_old = S.parity ? A.p1 : A.p0;
+  for (int64_t s = tile.begin + wib; s < tile.end; s += wpb) {
+    const int64_t sbase = A.slice_ptr[s];
+    const int w = static_cast<int>((A.slice_ptr[s + 1] - sbase) >> 5);
+    const double acc = sell_row_acc<V, double>(A.col, val, sbase, w, lane, GatherX<double>{A.x});
+    const int32_t row = A.perm[s * kSellC + lane];
+    if (row >= 0) {
+      const double r64 = A.b[row] - acc;
+      rr64 += r64 * r64;
+      float di;
+      if (mode == 2) {
+        di = static_cast<float>(A.dinv64[row]);
+        A.dinv32[row] = di;
+      } else {
+        di = A.dinv32[row];
+      }
+      const float ri = static_cast<float>(r64);
+      const float zi = di * ri;
+      A.r[row] = ri;
+      A.z[row] = zi;
+      if (mode == 2) p_old[row] = zi;
+      rz += static_cast<double>(ri) * static_cast<double>(zi);
+    }
+  }
+  *rr_out = rr64;
+  *rz_out = rz;
+}
+
+__global__ void __launch_bounds__(1024, 1) batch_reliable(const fgb_batch_system* __restrict__ sys,
+                                                          const fgb_batch_state* __restrict__ st,
+                                                          const fgb_batch_tile* __restrict__ tiles,
+                                                          const int32_t* __restrict__ n_tiles, double* rpart) {
+  __shared__ double red[32];
+  const int nt = *n_tiles;
+  for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+    const fgb_batch_tile tile = tiles[t];
+    const fgb_batch_state& S = st[tile.sys];
+    const int mode = S.active && !S.done ? S.need_update : 0;
+    if (!mode) continue;
+    const fgb_batch_system& A = sys[tile.sys];
+    double rr, rz;
+    if (A.val64) reliable_tile<double>(A, S, A.val64, tile, mode, &rr, &rz);
+    else reliable_tile<float>(A, S, A.val32, tile, mode, &rr, &rz);
+    const double a = block_sum(rr, red);
+    __syncthreads();
+    const double b = block_sum(rz, red);
+    if (threadIdx.x == 0) { rpart[2 * t] = a; rpart[2 * t + 1] = b; }
+    __syncthreads();
+  }
+}
+
+// Systems with an update due or admitted: true residual test, beta from the
+// replaced residual.
+__global__ void batch_reliable_fin(int32_t n_sys, fgb_batch_state* st, const int32_t* __restrict__ tile_ptr,
+                                   const double* __restrict__ rpart) {
+  const int s = warp_system();
+  if (s >= n_sys) return;
+  fgb_batch_state& S = st[s];
+  const int mode = S.active && !S.done ? S.need_update : 0;
+  if (!mode) return;
+  const double rr = tile_sum(rpart, tile_ptr[s], tile_ptr[s + 1], 2, 0);
+  const double rz = tile_sum(rpart, tile_ptr[s], tile_ptr[s + 1], 2, 1);
+  if ((threadIdx.x & 31) != 0) return;
+  const double nrm = sqrt(rr);
+  S.true_rel = S.b_norm > 0.0 ? nrm / S.b_norm : 0.0;
+  S.resid = nrm;
+  if (mode == 1) S.n_updates += 1;
+  if (!isfinite(nrm)) S.done = FGB_PCG_NONFINITE;
+  else if (nrm <= S.tol) S.done = FGB_PCG_RTOL;
+  else if (S.niter >= S.maxit) S.done = FGB_PCG_MAXIT;
+  S.beta = mode == 2 ? 0.0 : rz / S.rz_prev;
+  S.rz = rz;
+  S.rr = rr;
+  S.r_upd = nrm;
+  S.need_update = 0;
+}
+
+// Retirement: slots flagged in `force` become inactive; flags cleared.
+__global__ void batch_deactivate(int32_t n_sys, fgb_batch_state* st, int32_t* force) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n_sys || !force[s]) return;
+  st[s].active = 0;
+  force[s] = 0;
+}
+
+// y_s = A_s x_s (FP32) over slice tiles; the autotuner's timing kernel.
+__global__ void __launch_bounds__(1024, 1) batch_spmv_plain(const fgb_batch_system* __restrict__ sys,
+                                                            const fgb_batch_tile* __restrict__ tiles,
+                                                            const int32_t* __restrict__ n_tiles,
+                                                            const float* const* __restrict__ xs,
+                                                            float* const* __restrict__ ys) {
+  const int nt = *n_tiles;
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+  for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+    const fgb_batch_tile tile = tiles[t];
+    const fgb_batch_system& A = sys[tile.sys];
+    const GatherX<float> g{xs[tile.sys]};
+    float* y = ys[tile.sys];
+    for (int64_t s = tile.begin + wib; s < tile.end; s += wpb) {
+      const int64_t sbase = A.slice_ptr[s];
+      const int w = static_cast<int>((A.slice_ptr[s + 1] - sbase) >> 5);
+      const float acc = sell_row(A.col, A.val32, sbase, w, lane, g);
+      const int32_t row = A.perm[s * kSellC + lane];
+      if (row >= 0) y[row] = acc;
+    }
+  }
+}
+
+}  // namespace fgb
+
+using namespace fgb;
+
+// ------------------------------------------------------------------ host side
+struct fgb_batch {
+  int32_t max_sys, max_st, max_vt, slice_threads;
+  int32_t n_sys = 0, n_st = 0, n_vt = 0;
+  fgb_batch_system* sys;
+  fgb_batch_state* st;
+  fgb_batch_tile *stiles, *vtiles;
+  int32_t *stile_ptr, *vtile_ptr, *n_stiles, *n_vtiles, *force;
+  double *spart, *vpart, *rpart;
+  BatchCtl* ctl;
+  const float** xs;
+  float** ys;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  bool graph_failed = false;
+};
+
+namespace {
+
+size_t batch_layout(int32_t ms, int32_t mst, int32_t mvt, fgb_batch* b, void* base, size_t bytes) {
+  Carver cv(base, bytes);
+  auto sys = cv.take<fgb_batch_system>(ms);
+  auto st = cv.take<fgb_batch_state>(ms);
+  auto stiles = cv.take<fgb_batch_tile>(mst);
+  auto vtiles = cv.take<fgb_batch_tile>(mvt);
+  auto sptr = cv.take<int32_t>(ms + 1);
+  auto vptr = cv.take<int32_t>(ms + 1);
+  auto counts = cv.take<int32_t>(2);
+  auto force = cv.take<int32_t>(ms);
+  auto spart = cv.take<double>(mst);
+  auto vpart = cv.take<double>(2 * static_cast<size_t>(mvt));
+  auto rpart = cv.take<double>(2 * static_cast<size_t>(mst));
+  auto ctl = cv.take<BatchCtl>(1);
+  auto xs = cv.take<const float*>(ms);
+  auto ys = cv.take<float*>(ms);
+  if (b) {
+    b->sys = sys; b->st = st; b->stiles = stiles; b->vtiles = vtiles; b->stile_ptr = sptr; b->vtile_ptr = vptr;
+    b->n_stiles = counts; b->n_vtiles = counts + 1; b->force = force; b->spart = spart; b->vpart = vpart;
+    b->rpart = rpart; b->ctl = ctl; b->xs = xs; b->ys = ys;
+  }
+  return cv.ok ? cv.off : 0;
+}
+
+int sys_blocks(int32_t n) { return (n + 255) / 256; }
+int warp_sys_blocks(int32_t n) { return (n * 32 + 255) / 256; }  // one warp per system
+int slice_grid(const fgb_batch* b) { return b->max_st < kBatchSliceBlocks ? b->max_st : kBatchSliceBlocks; }
+int row_grid(const fgb_batch* b) { return b->max_vt < kBatchRowBlocks ? b->max_vt : kBatchRowBlocks; }
+
+void launch_iteration(fgb_batch* b, cudaStream_t s, int graph, cudaGraphConditionalHandle h_if,
+                      cudaGraphConditionalHandle h_while) {
+  batch_spmv_step<<<slice_grid(b), b->slice_threads, 0, s>>>(b->sys, b->st, b->stiles, b->n_stiles, b->spart);
+  batch_alpha<<<warp_sys_blocks(b->max_sys), 256, 0, s>>>(b->max_sys, b->st, b->stile_ptr, b->spart);
+  batch_update<<<row_grid(b), kBatchRowThreads, 0, s>>>(b->sys, b->st, b->vtiles, b->n_vtiles, b->vpart);
+  batch_control<<<warp_sys_blocks(b->max_sys), 256, 0, s>>>(b->max_sys, b->st, b->vtile_ptr, b->vpart, b->ctl, h_if, h_while,
+                                               graph);
+}
+
+void launch_reliable(fgb_batch* b, cudaStream_t s) {
+  batch_fold<<<row_grid(b), kBatchRowThreads, 0, s>>>(b->sys, b->st, b->vtiles, b->n_vtiles, nullptr, b->vpart);
+  batch_reliable<<<slice_grid(b), b->slice_threads, 0, s>>>(b->sys, b->st, b->stiles, b->n_stiles, b->rpart);
+  batch_reliable_fin<<<warp_sys_blocks(b->max_sys), 256, 0, s>>>(b->max_sys, b->st, b->stile_ptr, b->rpart);
+}
+
+// while (running && trips < limit) { iteration ; if (update due) reliable }
+int build_graph(fgb_batch* b) {
+  cudaGraph_t g = nullptr;
+  if (cudaGraphCreate(&g, 0) != cudaSuccess) return FGB_ERR_CUDA;
+  cudaGraphConditionalHandle hw, hif;
+  int rc = FGB_OK;
+  cudaStream_t cs = nullptr;
+  do {
+    if (cudaGraphConditionalHandleCreate(&hw, g, 1, cudaGraphCondAssignDefault) != cudaSuccess) { rc = FGB_ERR_CUDA; break; }
+    cudaGraphNodeParams wp = {};
+    wp.type = cudaGraphNodeTypeConditional;
+    wp.conditional.handle = hw;
+    wp.conditional.type = cudaGraphCondTypeWhile;
+    wp.conditional.size = 1;
+    cudaGraphNode_t wnode;
+    if (cudaGraphAddNode(&wnode, g, nullptr, nullptr, 0, &wp) != cudaSuccess) { rc = FGB_ERR_CUDA; break; }
+    cudaGraph_t body = wp.conditional.phGraph_out[0];
+    if (cudaGraphConditionalHandleCreate(&hif, body, 0, cudaGraphCondAssignDefault) != cudaSuccess) { rc = FGB_ERR_CUDA; break; }
+    if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) { rc = FGB_ERR_CUDA; cs = nullptr; break; }
+    if (cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+      rc = FGB_ERR_CUDA;
+      break;
+    }
+    launch_iteration(b, cs, 1, hif, hw);
+    // IF node on hif after the control kernel
+    cudaStreamCaptureStatus status;
+    cudaGraph_t cg = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    bool ok = cudaStreamGetCaptureInfo(cs, &status, nullptr, &cg, &deps, nullptr, &nd) == cudaSuccess &&
+              status == cudaStreamCaptureStatusActive;
+    cudaGraphNodeParams ip = {};
+    cudaGraphNode_t inode;
+    if (ok) {
+      ip.type = cudaGraphNodeTypeConditional;
+      ip.conditional.handle = hif;
+      ip.conditional.type = cudaGraphCondTypeIf;
+      ip.conditional.size = 1;
+      ok = cudaGraphAddNode(&inode, cg, deps, nullptr, nd, &ip) == cudaSuccess &&
+           cudaStreamUpdateCaptureDependencies(cs, &inode, nullptr, 1, cudaStreamSetCaptureDependencies) == cudaSuccess;
+    }
+    cudaGraph_t out = nullptr;
+    const bool ended = cudaStreamEndCapture(cs, &out) == cudaSuccess;
+    if (!ok || !ended) { rc = FGB_ERR_CUDA; break; }
+    cudaStream_t bs = nullptr;
+    if (cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking) != cudaSuccess) { rc = FGB_ERR_CUDA; break; }
+    if (cudaStreamBeginCaptureToGraph(bs, ip.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                      cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+      rc = FGB_ERR_CUDA;
+    } else {
+      launch_reliable(b, bs);
+      cudaGraph_t o2 = nullptr;
+      if (cudaStreamEndCapture(bs, &o2) != cudaSuccess) rc = FGB_ERR_CUDA;
+    }
+    cudaStreamDestroy(bs);
+    if (rc) break;
+    if (cudaGraphInstantiate(&b->exec, g, 0) != cudaSuccess) { b->exec = nullptr; rc = FGB_ERR_CUDA; break; }
+  } while (false);
+  if (cs) cudaStreamDestroy(cs);
+  if (rc) {
+    cudaGraphDestroy(g);
+    cudaGetLastError();
+    return rc;
+  }
+  b->graph = g;
+  return FGB_OK;
+}
+
+bool valid_tiles(int32_t n_sys, const fgb_batch_system* sys, int32_t nt, const fgb_batch_tile* tiles,
+                 const int32_t* ptr, bool slices) {
+  if (ptr[0] != 0 || ptr[n_sys] != nt) return false;
+  for (int32_t s = 0; s < n_sys; ++s) {
+    if (ptr[s + 1] < ptr[s]) return false;
+    const int64_t lim = slices ? sys[s].n_slices : sys[s].n;
+    for (int32_t t = ptr[s]; t < ptr[s + 1]; ++t) {
+      if (tiles[t].sys != s || tiles[t].begin < 0 || tiles[t].begin >= tiles[t].end || tiles[t].end > lim) return false;
+    }
+  }
+  return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t fgb_batch_bytes(int32_t max_sys, int32_t max_slice_tiles, int32_t max_row_tiles) {
+  if (max_sys <= 0 || max_slice_tiles <= 0 || max_row_tiles <= 0) return 0;
+  // sizes only: an aligned stand-in base address that is never dereferenced
+  void* probe = reinterpret_cast<void*>(static_cast<uintptr_t>(256));
+  return batch_layout(max_sys, max_slice_tiles, max_row_tiles, nullptr, probe, static_cast<size_t>(1) << 40);
+}
+
+int32_t fgb_batch_create(int32_t max_sys, int32_t max_slice_tiles, int32_t max_row_tiles, int32_t slice_threads,
+                         void* device_buffer, size_t bytes, fgb_batch** out) {
+  if (!out || max_sys <= 0 || max_slice_tiles <= 0 || max_row_tiles <= 0) return FGB_ERR_ARG;
+  if (slice_threads < 64 || slice_threads > 1024 || slice_threads % 32) return FGB_ERR_ARG;
+  if (!device_buffer || bytes < fgb_batch_bytes(max_sys, max_slice_tiles, max_row_tiles)) return FGB_ERR_WORKSPACE;
+  fgb_batch* b = new (std::nothrow) fgb_batch;
+  if (!b) return FGB_ERR_CAPACITY;
+  b->max_sys = max_sys; b->max_st = max_slice_tiles; b->max_vt = max_row_tiles; b->slice_threads = slice_threads;
+  if (batch_layout(max_sys, max_slice_tiles, max_row_tiles, b, device_buffer, bytes) == 0) {
+    delete b;
+    return FGB_ERR_WORKSPACE;
+  }
+  // every slot inactive, no tiles, zero force flags
+  if (cudaMemset(device_buffer, 0, bytes) != cudaSuccess) { delete b; return FGB_ERR_CUDA; }
+  *out = b;
+  return FGB_OK;
+}
+
+int32_t fgb_batch_destroy(fgb_batch* b) {
+  if (!b) return FGB_ERR_ARG;
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  delete b;
+  return FGB_OK;
+}
+
+int32_t fgb_batch_set(fgb_batch* b, int32_t n_sys, const fgb_batch_system* systems, int32_t n_slice_tiles,
+                      const fgb_batch_tile* slice_tiles, const int32_t* slice_tile_ptr, int32_t n_row_tiles,
+                      const fgb_batch_tile* row_tiles, const int32_t* row_tile_ptr, void* stream) {
+  if (!b || n_sys < 0 || n_sys > b->max_sys || n_slice_tiles < 0 || n_slice_tiles > b->max_st || n_row_tiles < 0 ||
+      n_row_tiles > b->max_vt)
+    return FGB_ERR_ARG;
+  if (n_sys > 0 && (!systems || !slice_tile_ptr || !row_tile_ptr)) return FGB_ERR_ARG;
+  for (int32_t s = 0; s < n_sys; ++s) {
+    const fgb_batch_system& A = systems[s];
+    if (A.n <= 0) continue;  // an empty slot: it must own no tiles
+    if (A.n >= (int64_t(1) << 31) || A.n_slices != fgb_sell_slots(A.n) / kSellC || !A.slice_ptr || !A.perm ||
+        !A.col || !A.val32 || !A.dinv64 || !A.b || !A.x || !A.r || !A.z || !A.p0 || !A.p1 || !A.Ap || !A.y ||
+        !A.dinv32)
+      return FGB_ERR_ARG;
+  }
+  if (n_sys > 0 && (!valid_tiles(n_sys, systems, n_slice_tiles, slice_tiles, slice_tile_ptr, true) ||
+                    !valid_tiles(n_sys, systems, n_row_tiles, row_tiles, row_tile_ptr, false)))
+    return FGB_ERR_ARG;
+  cudaStream_t s = as_stream(stream);
+  // tile pointers padded to max_sys + 1 entries (the kernels walk every slot)
+  int32_t* sp = new (std::nothrow) int32_t[2 * (b->max_sys + 1) + 2];
+  if (!sp) return FGB_ERR_CAPACITY;
+  int32_t* vp = sp + (b->max_sys + 1);
+  for (int32_t k = 0; k <= b->max_sys; ++k) {
+    sp[k] = n_sys > 0 ? slice_tile_ptr[k < n_sys ? k : n_sys] : 0;
+    vp[k] = n_sys > 0 ? row_tile_ptr[k < n_sys ? k : n_sys] : 0;
+  }
+  int32_t* counts = vp + (b->max_sys + 1);
+  counts[0] = n_slice_tiles;
+  counts[1] = n_row_tiles;
+  bool ok = true;
+  if (n_sys > 0) ok = ok && cudaMemcpyAsync(b->sys, systems, n_sys * sizeof(fgb_batch_system), cudaMemcpyHostToDevice, s) == cudaSuccess;
+  if (n_slice_tiles > 0)
+    ok = ok && cudaMemcpyAsync(b->stiles, slice_tiles, n_slice_tiles * sizeof(fgb_batch_tile), cudaMemcpyHostToDevice, s) == cudaSuccess;
+  if (n_row_tiles > 0)
+    ok = ok && cudaMemcpyAsync(b->vtiles, row_tiles, n_row_tiles * sizeof(fgb_batch_tile), cudaMemcpyHostToDevice, s) == cudaSuccess;
+  ok = ok && cudaMemcpyAsync(b->stile_ptr, sp, (b->max_sys + 1) * sizeof(int32_t), cudaMemcpyHostToDevice, s) == cudaSuccess;
+  ok = ok && cudaMemcpyAsync(b->vtile_ptr, vp, (b->max_sys + 1) * sizeof(int32_t), cudaMemcpyHostToDevice, s) == cudaSuccess;
+  ok = ok && cudaMemcpyAsync(b->n_stiles, counts, 2 * sizeof(int32_t), cudaMemcpyHostToDevice, s) == cudaSuccess;
+  ok = ok && cudaStreamSynchronize(s) == cudaSuccess;  // the host arrays are freed below
+  delete[] sp;
+  if (!ok) return FGB_ERR_CUDA;
+  b->n_sys = n_sys; b->n_st = n_slice_tiles; b->n_vt = n_row_tiles;
+  return FGB_OK;
+}
+
+int32_t fgb_batch_admit(fgb_batch* b, int32_t n, const int32_t* slots, const double* rtol, const int64_t* maxit,
+                        double delta, void* stream) {
+  if (!b || n < 0 || (n > 0 && (!slots || !rtol || !maxit))) return FGB_ERR_ARG;
+  if (!(delta > 0.0 && delta < 1.0)) return FGB_ERR_ARG;
+  cudaStream_t s = as_stream(stream);
+  for (int32_t k = 0; k < n; ++k) {
+    if (slots[k] < 0 || slots[k] >= b->n_sys || !(rtol[k] > 0.0) || maxit[k] <= 0) return FGB_ERR_ARG;
+    fgb_batch_state h;
+    std::memset(&h, 0, sizeof(h));
+    h.tol = rtol[k];  // batch_bnorm turns it into rtol * ||b||
+    h.delta = delta;
+    h.maxit = maxit[k];
+    h.active = 1;
+    h.need_update = 2;
+    if (cudaMemcpyAsync(b->st + slots[k], &h, sizeof(h), cudaMemcpyHostToDevice, s) != cudaSuccess) return FGB_ERR_CUDA;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return FGB_ERR_CUDA;  // h lives on this stack frame
+  }
+  if (n == 0) return FGB_OK;
+  batch_fold<<<row_grid(b), kBatchRowThreads, 0, s>>>(b->sys, b->st, b->vtiles, b->n_vtiles, nullptr, b->vpart);
+  batch_bnorm<<<warp_sys_blocks(b->max_sys), 256, 0, s>>>(b->max_sys, b->st, b->vtile_ptr, b->vpart);
+  batch_reliable<<<slice_grid(b), b->slice_threads, 0, s>>>(b->sys, b->st, b->stiles, b->n_stiles, b->rpart);
+  batch_reliable_fin<<<warp_sys_blocks(b->max_sys), 256, 0, s>>>(b->max_sys, b->st, b->stile_ptr, b->rpart);
+  return launch_status();
+}
+
+int32_t fgb_batch_run(fgb_batch* b, int64_t trip_limit, int32_t use_graph, fgb_batch_state* states_host,
+                      int32_t* running, int32_t* used_graph, void* stream) {
+  if (!b || trip_limit <= 0) return FGB_ERR_ARG;
+  cudaStream_t s = as_stream(stream);
+  BatchCtl c{};
+  c.trip_limit = trip_limit;
+  if (cudaMemcpyAsync(b->ctl, &c, sizeof(c), cudaMemcpyHostToDevice, s) != cudaSuccess) return FGB_ERR_CUDA;
+  bool graphed = false;
+  if (use_graph && !b->graph_failed) {
+    if (!b->exec && build_graph(b) != FGB_OK) b->graph_failed = true;
+    if (b->exec) {
+      if (cudaGraphLaunch(b->exec, s) != cudaSuccess) return FGB_ERR_CUDA;
+      graphed = true;
+    }
+  }
+  if (!graphed) {
+    // host-driven: the same kernels, the reliable branch launched every trip
+    // (its kernels return at once for systems without an update due)
+    const int chunk = 16;
+    while (true) {
+      for (int k = 0; k < chunk; ++k) {
+        launch_iteration(b, s, 0, 0, 0);
+        launch_reliable(b, s);
+      }
+      if (cudaGetLastError() != cudaSuccess) return FGB_ERR_CUDA;
+      if (cudaMemcpyAsync(&c, b->ctl, sizeof(c), cudaMemcpyDeviceToHost, s) != cudaSuccess) return FGB_ERR_CUDA;
+      if (cudaStreamSynchronize(s) != cudaSuccess) return FGB_ERR_CUDA;
+      if (!c.running || c.trips >= trip_limit) break;
+    }
+  }
+  if (cudaMemcpyAsync(&c, b->ctl, sizeof(c), cudaMemcpyDeviceToHost, s) != cudaSuccess) return FGB_ERR_CUDA;
+  if (states_host && b->n_sys > 0 &&
+      cudaMemcpyAsync(states_host, b->st, b->n_sys * sizeof(fgb_batch_state), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    return FGB_ERR_CUDA;
+  if (cudaStreamSynchronize(s) != cudaSuccess) return FGB_ERR_CUDA;
+  if (running) *running = c.running;
+  if (used_graph) *used_graph = graphed ? 1 : 0;
+  return FGB_OK;
+}
+
+int32_t fgb_batch_retire(fgb_batch* b, int32_t n, const int32_t* slots, void* stream) {
+  if (!b || n < 0 || (n > 0 && !slots)) return FGB_ERR_ARG;
+  if (n == 0) return FGB_OK;
+  cudaStream_t s = as_stream(stream);
+  int32_t* flags = new (std::nothrow) int32_t[b->max_sys];
+  if (!flags) return FGB_ERR_CAPACITY;
+  std::memset(flags, 0, sizeof(int32_t) * b->max_sys);
+  for (int32_t k = 0; k < n; ++k) {
+    if (slots[k] < 0 || slots[k] >= b->n_sys) { delete[] flags; return FGB_ERR_ARG; }
+    flags[slots[k]] = 1;
+  }
+  bool ok = cudaMemcpyAsync(b->force, flags, sizeof(int32_t) * b->max_sys, cudaMemcpyHostToDevice, s) == cudaSuccess;
+  ok = ok && cudaStreamSynchronize(s) == cudaSuccess;
+  delete[] flags;
+  if (!ok) return FGB_ERR_CUDA;
+  batch_fold<<<row_grid(b), kBatchRowThreads, 0, s>>>(b->sys, b->st, b->vtiles, b->n_vtiles, b->force, b->vpart);
+  batch_deactivate<<<sys_blocks(b->max_sys), 256, 0, s>>>(b->max_sys, b->st, b->force);
+  return launch_status();
+}
+
+int32_t fgb_batch_spmv(fgb_batch* b, const float* const* x, float* const* y, void* stream) {
+  if (!b || (b->n_sys > 0 && (!x || !y))) return FGB_ERR_ARG;
+  if (b->n_sys == 0) return FGB_OK;
+  cudaStream_t s = as_stream(stream);
+  bool ok = cudaMemcpyAsync(b->xs, x, b->n_sys * sizeof(float*), cudaMemcpyHostToDevice, s) == cudaSuccess &&
+            cudaMemcpyAsync(b->ys, y, b->n_sys * sizeof(float*), cudaMemcpyHostToDevice, s) == cudaSuccess;
+  if (!ok) return FGB_ERR_CUDA;
+  batch_spmv_plain<<<slice_grid(b), b->slice_threads, 0, s>>>(b->sys, b->stiles, b->n_stiles, b->xs, b->ys);
+  return launch_status();
+}
+
+}  // extern "C"

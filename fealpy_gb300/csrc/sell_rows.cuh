@@ -1,0 +1,129 @@
+// SELL-32x4 layout and the per-lane row kernels shared by the single-system
+// solvers (sell.cu) and the batched solver (batch.cu).
+//
+// Slices of 32 rows (one warp); entry k of the row of lane `lane` sits at
+// sell_pos(lane, k) inside its slice: packs of 4 consecutive entries per lane,
+// lanes interleaved pack by pack, so that every pack of a warp is one
+// contiguous run and each lane loads its 4 entries with a single 16-byte load.
+#pragma once
+
+#include "fgb_common.cuh"
+
+namespace fgb {
+
+constexpr int kSellC = 32;        // rows per slice (one warp)
+constexpr int kSellPack = 4;      // consecutive entries of a row stored contiguously
+constexpr int kSellWindow = 256;  // rows sorted together
+
+// Offset of entry k of lane (row slot) `lane` inside its slice: packs of 4
+// entries per lane, lanes interleaved pack by pack, so that pack q of the
+// warp is one contiguous 512-byte (FP32) run and each lane loads its 4
+// entries with a single 16-byte vector load.
+__host__ __device__ __forceinline__ int64_t sell_pos(int lane, int k) {
+  return static_cast<int64_t>(k >> 2) * (kSellC * kSellPack) + lane * kSellPack + (k & 3);
+}
+
+// One pack (4 entries of this lane's row): 16-byte streaming loads of the
+// columns and values, then the gathers.
+struct Pack4F {
+  int4 c;
+  float4 v;
+};
+struct Pack4D {
+  int4 c;
+  double2 v01, v23;
+};
+
+__device__ __forceinline__ Pack4F load_pack(const int32_t* col, const float* val, int64_t sbase, int lane, int q) {
+  const int64_t off = sbase + static_cast<int64_t>(q) * (kSellC * kSellPack) + lane * kSellPack;
+  Pack4F p;
+  p.c = __ldcs(reinterpret_cast<const int4*>(col + off));
+  p.v = __ldcs(reinterpret_cast<const float4*>(val + off));
+  return p;
+}
+
+__device__ __forceinline__ Pack4D load_pack(const int32_t* col, const double* val, int64_t sbase, int lane, int q) {
+  const int64_t off = sbase + static_cast<int64_t>(q) * (kSellC * kSellPack) + lane * kSellPack;
+  Pack4D p;
+  p.c = __ldcs(reinterpret_cast<const int4*>(col + off));
+  p.v01 = __ldcs(reinterpret_cast<const double2*>(val + off));
+  p.v23 = __ldcs(reinterpret_cast<const double2*>(val + off + 2));
+  return p;
+}
+
+template <typename T, typename G>
+__device__ __forceinline__ T pack_dot(const Pack4F& p, const G& g, T acc) {
+  acc += p.v.x * g(p.c.x);
+  acc += p.v.y * g(p.c.y);
+  acc += p.v.z * g(p.c.z);
+  acc += p.v.w * g(p.c.w);
+  return acc;
+}
+
+template <typename T, typename G>
+__device__ __forceinline__ T pack_dot(const Pack4D& p, const G& g, T acc) {
+  acc += p.v01.x * g(p.c.x);
+  acc += p.v01.y * g(p.c.y);
+  acc += p.v23.x * g(p.c.z);
+  acc += p.v23.y * g(p.c.w);
+  return acc;
+}
+
+template <typename T> struct PackOf;
+template <> struct PackOf<float> { using type = Pack4F; };
+template <> struct PackOf<double> { using type = Pack4D; };
+
+// Row of slot `lane` of the slice starting at sbase with width w (a multiple of
+// 4): sum over entries, in entry order, of val * g(col).  All loads of a trip
+// are issued before its gathers: four packs per trip in FP32 (128 bytes of
+// matrix per lane in flight), two in FP64 (96 bytes; four would not fit in
+// the 64 registers of a 1024-thread block).
+template <typename T> struct PacksPerTrip { static constexpr int value = 2; };
+template <> struct PacksPerTrip<float> { static constexpr int value = 4; };
+
+// V: stored value type, T: accumulation type (FP32 values of an FP32-assembled
+// matrix are accumulated in FP64 by the reliable update).
+template <typename V, typename T, typename G>
+__device__ __forceinline__ T sell_row_acc(const int32_t* __restrict__ col, const V* __restrict__ val, int64_t sbase,
+                                          int w, int lane, const G& g) {
+  using P = typename PackOf<V>::type;
+  constexpr int U = PacksPerTrip<V>::value;
+  const int nq = w / kSellPack;
+  T acc = T(0);
+  int q = 0;
+  for (; q + U <= nq; q += U) {
+    P a[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) a[u] = load_pack(col, val, sbase, lane, q + u);
+#pragma unroll
+    for (int u = 0; u < U; ++u) acc = pack_dot<T>(a[u], g, acc);
+  }
+  for (; q < nq; ++q) {
+    const P a = load_pack(col, val, sbase, lane, q);
+    acc = pack_dot<T>(a, g, acc);
+  }
+  return acc;
+}
+
+template <typename T, typename G>
+__device__ __forceinline__ T sell_row(const int32_t* __restrict__ col, const T* __restrict__ val, int64_t sbase, int w,
+                                      int lane, const G& g) {
+  return sell_row_acc<T, T, G>(col, val, sbase, w, lane, g);
+}
+
+template <typename T>
+struct GatherX {
+  const T* __restrict__ x;
+  __device__ __forceinline__ T operator()(int32_t j) const { return x[j]; }
+};
+
+// p_new[j] = z[j] + beta * p_old[j], formed on the fly for every gathered column
+template <typename T>
+struct GatherP {
+  const T* __restrict__ z;
+  const T* __restrict__ p;
+  T beta;
+  __device__ __forceinline__ T operator()(int32_t j) const { return z[j] + beta * p[j]; }
+};
+
+}  // namespace fgb

@@ -311,6 +311,90 @@ int32_t fgb_pcg_sell_mixed(const fgb_sell* A, const double* diag_inv64, const do
                            void* workspace, size_t workspace_bytes, fgb_pcg_info* info_host,
                            void* stream);
 
+/* ---- batched FP32-refined Jacobi-PCG over many systems ------------------ */
+
+/* No FEALPy counterpart: FEALPy solves one system per fealpy/solver/cg.py
+ * call.  Here many independent systems (meshes of uneven size and degree,
+ * each with its own SELL copy and Krylov vectors) advance together: every
+ * kernel of an iteration walks a list of tiles (a tile = one system's range
+ * of slices or rows), every dot product is reduced per system in a fixed
+ * order (so a system's iterates do not depend on the other systems in the
+ * batch), and the loop runs as one CUDA graph with a device-side while node.
+ * Systems are admitted into free slots and retired between runs (continuous
+ * batching).  Same iteration, reliable updates and stopping rule as
+ * fgb_pcg_sell_mixed, per system. */
+typedef struct fgb_batch_system {
+  int64_t n;                /* rows                                        */
+  int64_t n_slices;         /* SELL slices (fgb_sell_slots(n) / 32)        */
+  const int64_t* slice_ptr; /* SELL copy of the matrix (fgb_sell fields)   */
+  const int32_t* perm;
+  const int32_t* col;
+  const float* val32;       /* required                                    */
+  const double* val64;      /* optional: FP64 residual values              */
+  const double* dinv64;     /* 1 / diag(A)                                 */
+  const double* b;          /* right-hand side (FP64)                      */
+  double* x;                /* x0 on admission, the solution on retirement */
+  float* r;                 /* n floats each, owned by the caller          */
+  float* z;
+  float* p0;
+  float* p1;
+  float* Ap;
+  float* y;
+  float* dinv32;
+} fgb_batch_system;
+
+/* Per-system state (device array; read back by fgb_batch_run). */
+typedef struct fgb_batch_state {
+  double rz, rz_prev, rr, alpha, beta, b_norm, tol, resid, r_upd, true_rel, delta;
+  int64_t niter, maxit;
+  int32_t active;      /* 1 while the system takes part in the loop       */
+  int32_t done;        /* FGB_PCG_* reason once finished, 0 while running */
+  int32_t need_update; /* 1: reliable update due, 2: admission pending    */
+  int32_t n_updates;
+  int32_t parity;      /* which of p0/p1 holds the current direction      */
+  int32_t reserved;
+} fgb_batch_state;
+
+/* A tile: rows or slices [begin, end) of system `sys`.  Tiles of a system
+ * are consecutive in their list; tile_ptr[s]..tile_ptr[s+1] are its tiles. */
+typedef struct fgb_batch_tile {
+  int32_t sys, begin, end, reserved;
+} fgb_batch_tile;
+
+typedef struct fgb_batch fgb_batch; /* opaque: device tables + the graph    */
+
+size_t fgb_batch_bytes(int32_t max_sys, int32_t max_slice_tiles, int32_t max_row_tiles);
+/* device_buffer (fgb_batch_bytes bytes, caller-owned) holds the tables, the
+ * states and the per-tile partials.  slice_threads: threads per block of the
+ * slice kernels (a multiple of 32 in [64, 1024]). */
+int32_t fgb_batch_create(int32_t max_sys, int32_t max_slice_tiles, int32_t max_row_tiles,
+                         int32_t slice_threads, void* device_buffer, size_t bytes,
+                         fgb_batch** out);
+int32_t fgb_batch_destroy(fgb_batch* batch);
+/* Replace the system table and both tile lists (host arrays, copied). */
+int32_t fgb_batch_set(fgb_batch* batch, int32_t n_sys, const fgb_batch_system* systems,
+                      int32_t n_slice_tiles, const fgb_batch_tile* slice_tiles,
+                      const int32_t* slice_tile_ptr, int32_t n_row_tiles,
+                      const fgb_batch_tile* row_tiles, const int32_t* row_tile_ptr,
+                      void* stream);
+/* Admit systems (slot ids): reset their state, then ||b||, the initial FP64
+ * residual, z and p on the device. */
+int32_t fgb_batch_admit(fgb_batch* batch, int32_t n, const int32_t* slots, const double* rtol,
+                        const int64_t* maxit, double delta, void* stream);
+/* Iterate all admitted, unfinished systems for at most trip_limit
+ * iterations (use_graph: one graph launch; else one launch per kernel) and
+ * copy the first n_sys states to states_host.  *running: systems still
+ * unfinished. */
+int32_t fgb_batch_run(fgb_batch* batch, int64_t trip_limit, int32_t use_graph,
+                      fgb_batch_state* states_host, int32_t* running, int32_t* used_graph,
+                      void* stream);
+/* Retire systems: add the pending FP32 correction into x, zero x of a zero
+ * right-hand side, and mark the slots inactive. */
+int32_t fgb_batch_retire(fgb_batch* batch, int32_t n, const int32_t* slots, void* stream);
+/* y_s = A_s x_s in FP32 for every system of the table (x, y: per-system
+ * device pointers, host arrays of n_sys entries); used by the autotuner. */
+int32_t fgb_batch_spmv(fgb_batch* batch, const float* const* x, float* const* y, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

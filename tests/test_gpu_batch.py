@@ -1,0 +1,117 @@
+"""Batched FP32-refined PCG (fealpy_gb300.batch): every system of a batch
+reaches the true relative residual 1e-10, agrees with the single-system FP64
+solve, and gives the same bits alone and inside any mix, whether it joins
+at the start or while others are in flight (continuous batching)."""
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-10
+
+
+def cuda():
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA device")
+    return torch.device("cuda", 0)
+
+
+def _poisson(F, mesh, p, seed, dtype=torch.float64):
+    from fealpy_gb300.fem import BilinearForm, ScalarDiffusionIntegrator, ScalarMassIntegrator, DirichletBC
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    NC = mesh.number_of_cells()
+    kappa = torch.exp(torch.randn(NC, generator=g, dtype=torch.float64)).to(mesh.node.device)
+    space = F.LagrangeFESpace(mesh, p)
+    bf = BilinearForm(space)
+    bf.add_integrator(ScalarDiffusionIntegrator(coef=kappa, q=p + 2), ScalarMassIntegrator(coef=1.0, q=p + 2))
+    A = bf.assembly(dtype=dtype)
+    n = space.number_of_global_dofs()
+    f = torch.rand(n, generator=g, dtype=torch.float64).to(mesh.node.device)
+    return DirichletBC(space, gd=0.0).apply(A, f)
+
+
+def _systems(dev):
+    import fealpy_gb300 as F
+    out = []
+    for k, (nx, p) in enumerate([(8, 1), (20, 2), (13, 3), (40, 1), (6, 2)]):
+        m = F.TriangleMesh.from_box([0, 1, 0, 1], nx, nx, device=dev)
+        out.append(_poisson(F, m, p, k))
+    m = F.TetrahedronMesh.from_box([0, 1, 0, 1, 0, 1], 6, 5, 4, device=dev)
+    out.append(_poisson(F, m, 1, 9))
+    return out
+
+
+def _residual(A, b, x):
+    import fealpy_gb300 as F
+    Ad = F.CSRTensor(A.crow, A.col, A.values.to(torch.float64), A.shape)
+    bd = b.to(torch.float64)
+    return float(torch.linalg.norm(bd - Ad @ x) / torch.linalg.norm(bd))
+
+
+def test_batch_converges_and_matches_fp64():
+    dev = cuda()
+    import fealpy_gb300 as F
+    from fealpy_gb300.batch import BatchSolver
+    systems = _systems(dev)
+    bs = BatchSolver(8, slices_per_tile=4, rows_per_tile=512)
+    for k, (A, b) in enumerate(systems):
+        bs.add(A, b, rtol=RTOL, key=k)
+    res = bs.solve_all()
+    assert sorted(res) == list(range(len(systems)))
+    assert bs.used_graph
+    for k, (A, b) in enumerate(systems):
+        r = res[k]
+        assert r.reason == 2, (k, r.info())
+        rel = _residual(A, b, r.x)
+        assert rel <= RTOL * 1.0001 and abs(rel - r.relres) <= 1e-3 * rel, (k, rel, r.relres)
+        x64 = F.cg(A, b, M=F.JacobiPreconditioner().apply(A), atol=1e-30, rtol=1e-13)
+        err = float((r.x - x64).abs().max() / x64.abs().max())
+        assert err < 1e-8, (k, err)
+
+
+def test_batch_solo_equals_mix_and_late_admission():
+    dev = cuda()
+    from fealpy_gb300.batch import BatchSolver
+    systems = _systems(dev)
+    cfg = dict(slices_per_tile=4, rows_per_tile=512)
+    solo = {}
+    for k, (A, b) in enumerate(systems):
+        bs = BatchSolver(2, **cfg)
+        bs.add(A, b, rtol=RTOL, key=k)
+        solo[k] = bs.solve_all()[k]
+    # mix: half start together, the rest join while the first ones run
+    bs = BatchSolver(4, **cfg)
+    res, waiting = {}, list(range(len(systems)))
+    for k in waiting[:3]:
+        bs.add(*systems[k], rtol=RTOL, key=k)
+    waiting = waiting[3:]
+    while bs.active() or waiting:
+        for r in bs.step(max_iterations=7):
+            res[r.key] = r
+        while waiting and bs.free_slots():
+            k = waiting.pop(0)
+            bs.add(*systems[k], rtol=RTOL, key=k)
+    for k in solo:
+        assert res[k].niter == solo[k].niter, (k, res[k].niter, solo[k].niter)
+        assert torch.equal(res[k].x, solo[k].x), k
+    # host-driven loop: same kernels, same bits
+    bs = BatchSolver(8, **cfg)
+    for k, (A, b) in enumerate(systems):
+        bs.add(A, b, rtol=RTOL, key=k)
+    polled = bs.solve_all(graph=False)
+    for k in solo:
+        assert torch.equal(polled[k].x, solo[k].x), k
+
+
+def test_batch_fp32_operators_and_autotune():
+    dev = cuda()
+    import fealpy_gb300 as F
+    from fealpy_gb300.batch import BatchSolver, autotune
+    m = F.TriangleMesh.from_box([0, 1, 0, 1], 24, 24, device=dev)
+    A32, b32 = _poisson(F, m, 2, 3, dtype=torch.float32)
+    bs = BatchSolver(2)
+    bs.add(A32, b32, rtol=RTOL, key="a")
+    r = bs.solve_all()["a"]
+    assert r.reason == 2 and _residual(A32, b32, r.x) <= RTOL * 1.0001
+    times = autotune([(A32, b32)], candidates=((8, 128), (16, 256)))
+    assert set(times) == {(8, 128), (16, 256)} and all(t > 0 for t in times.values())
