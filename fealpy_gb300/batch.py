@@ -52,12 +52,13 @@ class BatchSolver:
 
     def __init__(self, max_systems: int = 256, *, max_slice_tiles: int = 1 << 16, max_row_tiles: int = 1 << 16,
                  slices_per_tile: int = 16, rows_per_tile: int = 4096, slice_threads: int = 256,
-                 delta: float = 0.1, device=None):
+                 max_tiles_per_system: int = 256, delta: float = 0.1, device=None):
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         self.max_systems = int(max_systems)
         self.max_slice_tiles, self.max_row_tiles = int(max_slice_tiles), int(max_row_tiles)
         self.slices_per_tile, self.rows_per_tile = int(slices_per_tile), int(rows_per_tile)
         self.slice_threads = int(slice_threads)
+        self.max_tiles_per_system = int(max_tiles_per_system)
         self.delta = float(delta)
         lib = _lib.lib()
         nbytes = int(lib.fgb_batch_bytes(self.max_systems, self.max_slice_tiles, self.max_row_tiles))
@@ -122,10 +123,14 @@ class BatchSolver:
 
     # ------------------------------------------------------------ tables
     def _tiles(self, sizes, per_tile, attr):
+        """Tiles of each system: ``per_tile`` slices (rows), widened so that a
+        system has at most ``max_tiles_per_system`` tiles (its per-system
+        sums stay short); depends on the system's own size only."""
         tiles, ptr_ = [], [0]
         for s, lim in enumerate(sizes):
-            for a in range(0, lim, per_tile):
-                tiles.append((s, a, min(a + per_tile, lim), 0))
+            step = max(per_tile, -(-lim // self.max_tiles_per_system))
+            for a in range(0, lim, step):
+                tiles.append((s, a, min(a + step, lim), 0))
             ptr_.append(len(tiles))
         return tiles, ptr_
 
