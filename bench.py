@@ -521,6 +521,8 @@ def run_batched(args):
                        "gdof": gdof, "rtol": RTOL, "autotune_us": {f"{a}x{b}": t for (a, b), t in times.items()},
                        "slices_per_tile": spt, "slice_threads": thr},
             "solve_ms": solve_ms, "assembly_ms": ms - solve_ms, "graph": bs.used_graph,
+            "fp64_continuations": bs.fallbacks,
+            "fp64_iterations": sum(getattr(res[k], "fp64_iterations", 0) for k in res),
             "max_true_relres": max(rel), "iters_max": max(iters), "iters_mean": sum(iters) / len(iters),
             "max_rel_err_vs_fp64_sample": max(err), "gpu_launches": (_lib.launch_count() - l0) // args.steps}
     print(json.dumps(line), flush=True)

@@ -41,7 +41,8 @@ STATUS_NAMES = {
     7: "CUDA error", 8: "size exceeds a fixed kernel limit",
 }
 
-PCG_REASONS = {0: "running", 1: "atol", 2: "rtol", 3: "maxit", 4: "zero rhs", 5: "breakdown", 6: "nonfinite"}
+PCG_REASONS = {0: "running", 1: "atol", 2: "rtol", 3: "maxit", 4: "zero rhs", 5: "breakdown", 6: "nonfinite",
+               7: "stagnated"}
 
 
 class PcgInfo(ctypes.Structure):
@@ -106,14 +107,16 @@ _SIGNATURES = {
 class BatchSystem(ctypes.Structure):
     """``fgb_batch_system`` (include/fealpy_gb300.h)."""
     _fields_ = [("n", c_i64), ("n_slices", c_i64)] + [(k, c_vp) for k in (
-        "slice_ptr", "perm", "col", "val32", "val64", "dinv64", "b", "x", "r", "z", "p0", "p1", "Ap", "y", "dinv32")]
+        "slice_ptr", "perm", "col", "val32", "val64", "dinv64", "b", "x", "r", "z", "p0", "p1", "Ap", "y",
+        "dinv32")] + [("fp64", c_i32), ("reserved", c_i32)]
 
 
 class BatchState(ctypes.Structure):
     """``fgb_batch_state``."""
     _fields_ = [(k, c_dbl) for k in ("rz", "rz_prev", "rr", "alpha", "beta", "b_norm", "tol", "resid", "r_upd",
                                      "true_rel", "delta")] + [("niter", c_i64), ("maxit", c_i64)] + [
-        (k, c_i32) for k in ("active", "done", "need_update", "n_updates", "parity", "reserved")]
+        (k, c_i32) for k in ("active", "done", "need_update", "n_updates", "parity", "stall")] + [
+        ("r_best", c_dbl), ("last_upd", c_i64), ("max_gap", c_i64)]
 
 
 class BatchTile(ctypes.Structure):

@@ -32,16 +32,18 @@ class BatchResult:
 
     def __init__(self, key, x, niter, relres, reason, n_updates):
         self.key, self.x, self.niter, self.relres, self.reason, self.n_updates = key, x, niter, relres, reason, n_updates
+        self.fp64_iterations = 0  # of niter, those run in FP64 after an FP32 stagnation
 
     def info(self):
         return {"niter": self.niter, "relres": self.relres, "reason": self.reason, "n_updates": self.n_updates}
 
 
 class _Slot:
-    def __init__(self, key, S, dinv64, b, x, vecs, rtol, maxit):
+    def __init__(self, key, S, dinv64, b, x, vecs, rtol, maxit, fp64, A):
         self.key, self.S, self.dinv64, self.b, self.x, self.vecs = key, S, dinv64, b, x, vecs
-        self.rtol, self.maxit = rtol, maxit
+        self.rtol, self.maxit, self.fp64, self.A = rtol, maxit, fp64, A
         self.admitted = False
+        self.iters_before = 0  # FP32 iterations spent before an FP64 continuation
 
 
 class BatchSolver:
@@ -74,6 +76,7 @@ class BatchSolver:
         self._n_table = 0
         self.launches = 0
         self.used_graph = False
+        self.fallbacks = 0  # systems continued in FP64 after their FP32 iterations stagnated
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -97,10 +100,12 @@ class BatchSolver:
         return nnz_padded * (4 + 4 + (8 if fp64_values else 0)) + n * (8 + 8 + 8 + 7 * 4) + (n // 32 + 2) * 12
 
     def add(self, A: CSRTensor, b: torch.Tensor, x0: Optional[torch.Tensor] = None, *, rtol: float = 1e-10,
-            maxit: int = 100000, key=None) -> int:
+            maxit: int = 100000, key=None, fp64: bool = False) -> int:
         """Place ``A x = b`` in a free slot (admitted at the next ``step``);
         returns the slot.  An FP32 ``A`` is its own operator; an FP64 ``A``
-        keeps FP64 values for the residual recomputation."""
+        keeps FP64 values for the residual recomputation.  ``fp64``: iterate
+        in FP64 (plain FP64 PCG with the same stopping rule).  An FP32 system
+        that stagnates is continued in FP64 from its current iterate."""
         if not isinstance(A, CSRTensor):
             raise NotImplementedError("BatchSolver takes CSRTensor matrices")
         try:
@@ -108,7 +113,9 @@ class BatchSolver:
         except ValueError:
             raise RuntimeError("no free slot in the batch") from None
         n = A.shape[0]
-        if A.values.dtype == torch.float32:
+        if fp64:
+            S = K.sell_build(A.crow, A.col, A.values.to(torch.float64).contiguous(), None, want64=True, want32=False)
+        elif A.values.dtype == torch.float32:
             S = K.sell_build(A.crow, A.col, None, A.values.contiguous(), want64=False, want32=True)
         else:
             S = K.sell_build(A.crow, A.col, A.values.to(torch.float64).contiguous(), None, want64=True, want32=True)
@@ -116,8 +123,9 @@ class BatchSolver:
         b64 = b.to(self.device, torch.float64).contiguous()
         x = torch.zeros(n, dtype=torch.float64, device=self.device) if x0 is None else \
             x0.to(self.device, torch.float64).clone()
-        vecs = torch.empty((7, n), dtype=torch.float32, device=self.device)
-        self._slots[slot] = _Slot(slot if key is None else key, S, dinv64, b64, x, vecs, float(rtol), int(maxit))
+        vecs = torch.empty((7, n), dtype=torch.float64 if fp64 else torch.float32, device=self.device)
+        self._slots[slot] = _Slot(slot if key is None else key, S, dinv64, b64, x, vecs, float(rtol), int(maxit),
+                                  bool(fp64), A)
         self._dirty = True
         return slot
 
@@ -149,8 +157,9 @@ class BatchSolver:
             d = systems[i]
             d.n, d.n_slices = S.n, S.n_slices
             d.slice_ptr, d.perm, d.col = S.slice_ptr.data_ptr(), S.perm.data_ptr(), S.col.data_ptr()
-            d.val32 = S.val32.data_ptr()
+            d.val32 = S.val32.data_ptr() if S.val32 is not None else None
             d.val64 = S.val64.data_ptr() if S.val64 is not None else None
+            d.fp64 = 1 if sl.fp64 else 0
             d.dinv64, d.b, d.x = sl.dinv64.data_ptr(), sl.b.data_ptr(), sl.x.data_ptr()
             d.r, d.z, d.p0, d.p1, d.Ap, d.y, d.dinv32 = (v[k].data_ptr() for k in range(7))
             slice_sizes.append(S.n_slices)
@@ -198,13 +207,23 @@ class BatchSolver:
         if done:
             arr = (ctypes.c_int32 * len(done))(*done)
             call("fgb_batch_retire", self._h, len(done), arr, stream)
+            restart = []
             for i in done:
                 sl, stt = self._slots[i], states[i]
+                self._slots[i] = None
+                if stt.done == 7:  # FP32 iterations stagnated: continue in FP64 from x
+                    restart.append((sl, int(stt.niter), int(stt.n_updates)))
+                    continue
                 if stt.done == 4:  # zero right-hand side: x = 0
                     sl.x.zero_()
-                out.append(BatchResult(sl.key, sl.x, int(stt.niter), float(stt.true_rel), int(stt.done),
-                                       int(stt.n_updates)))
-                self._slots[i] = None
+                res = BatchResult(sl.key, sl.x, sl.iters_before + int(stt.niter), float(stt.true_rel),
+                                  int(stt.done), int(stt.n_updates))
+                res.fp64_iterations = int(stt.niter) if sl.fp64 and sl.iters_before else 0
+                out.append(res)
+            for sl, it, nu in restart:
+                self.fallbacks += 1
+                slot = self.add(sl.A, sl.b, sl.x, rtol=sl.rtol, maxit=max(sl.maxit - it, 1), key=sl.key, fp64=True)
+                self._slots[slot].iters_before = sl.iters_before + it
             self._dirty = True
         return out
 

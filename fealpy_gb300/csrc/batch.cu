@@ -51,6 +51,44 @@ __device__ __forceinline__ double tile_sum(const double* __restrict__ part, int 
 __device__ __forceinline__ int warp_system() { return (blockIdx.x * blockDim.x + threadIdx.x) >> 5; }
 
 // ---------------------------------------------------------------- kernels
+// Vector type of a system: float (FP32 iterations) or double (fp64 systems).
+template <typename T> struct Vec;
+template <> struct Vec<float> {
+  __device__ static const float* val(const fgb_batch_system& A) { return A.val32; }
+  __device__ static const float* dinv(const fgb_batch_system& A) { return static_cast<const float*>(A.dinv32); }
+};
+template <> struct Vec<double> {
+  __device__ static const double* val(const fgb_batch_system& A) { return A.val64; }
+  __device__ static const double* dinv(const fgb_batch_system& A) { return A.dinv64; }
+};
+template <typename T> __device__ __forceinline__ T* vp(void* p) { return static_cast<T*>(p); }
+
+// One slice tile: Ap, p_new = z + beta p_old, and the tile's p.Ap (per thread).
+template <typename T>
+__device__ double spmv_tile(const fgb_batch_system& A, const fgb_batch_state& S, const fgb_batch_tile& tile) {
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+  const T beta = static_cast<T>(S.beta);
+  const T* z = vp<T>(A.z);
+  const T* p_old = vp<T>(S.parity ? A.p1 : A.p0);
+  T* p_new = vp<T>(S.parity ? A.p0 : A.p1);
+  T* Ap = vp<T>(A.Ap);
+  const GatherP<T> g{z, p_old, beta};
+  double pap = 0.0;
+  for (int64_t s = tile.begin + wib; s < tile.end; s += wpb) {
+    const int64_t sbase = A.slice_ptr[s];
+    const int w = static_cast<int>((A.slice_ptr[s + 1] - sbase) >> 5);
+    const T acc = sell_row(A.col, Vec<T>::val(A), sbase, w, lane, g);
+    const int32_t row = A.perm[s * kSellC + lane];
+    if (row >= 0) {
+      const T pi = z[row] + beta * p_old[row];
+      p_new[row] = pi;
+      Ap[row] = acc;
+      pap += static_cast<double>(pi) * static_cast<double>(acc);
+    }
+  }
+  return pap;
+}
+
 // Slice tiles: Ap, p_new and the tile's p.Ap.
 __global__ void __launch_bounds__(1024, 1) batch_spmv_step(const fgb_batch_system* __restrict__ sys,
                                                            const fgb_batch_state* __restrict__ st,
@@ -58,7 +96,6 @@ __global__ void __launch_bounds__(1024, 1) batch_spmv_step(const fgb_batch_syste
                                                            const int32_t* __restrict__ n_tiles, double* spart) {
   __shared__ double red[32];
   const int nt = *n_tiles;
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
   for (int t = blockIdx.x; t < nt; t += gridDim.x) {
     const fgb_batch_tile tile = tiles[t];
     const fgb_batch_state& S = st[tile.sys];
@@ -67,23 +104,7 @@ __global__ void __launch_bounds__(1024, 1) batch_spmv_step(const fgb_batch_syste
       continue;
     }
     const fgb_batch_system& A = sys[tile.sys];
-    const float beta = static_cast<float>(S.beta);
-    const float* p_old = S.parity ? A.p1 : A.p0;
-    float* p_new = S.parity ? A.p0 : A.p1;
-    const GatherP<float> g{A.z, p_old, beta};
-    double pap = 0.0;
-    for (int64_t s = tile.begin + wib; s < tile.end; s += wpb) {
-      const int64_t sbase = A.slice_ptr[s];
-      const int w = static_cast<int>((A.slice_ptr[s + 1] - sbase) >> 5);
-      const float acc = sell_row(A.col, A.val32, sbase, w, lane, g);
-      const int32_t row = A.perm[s * kSellC + lane];
-      if (row >= 0) {
-        const float pi = A.z[row] + beta * p_old[row];
-        p_new[row] = pi;
-        A.Ap[row] = acc;
-        pap += static_cast<double>(pi) * static_cast<double>(acc);
-      }
-    }
+    const double pap = A.fp64 ? spmv_tile<double>(A, S, tile) : spmv_tile<float>(A, S, tile);
     const double b = block_sum(pap, red);
     if (threadIdx.x == 0) spart[t] = b;
     __syncthreads();
@@ -107,7 +128,33 @@ __global__ void batch_alpha(int32_t n_sys, fgb_batch_state* st, const int32_t* _
   }
 }
 
-// Row tiles: the FP32 updates and the tile's r.z, r.r.
+// One row tile: y += alpha p, r -= alpha Ap, z = Dinv r; per-thread r.z, r.r
+// (accumulated in the vector type, combined in FP64 by the block).
+template <typename T>
+__device__ void update_tile(const fgb_batch_system& A, const fgb_batch_state& S, const fgb_batch_tile& tile,
+                            double* rz_out, double* rr_out) {
+  const T alpha = static_cast<T>(S.alpha);
+  const T* __restrict__ p = vp<T>(S.parity ? A.p0 : A.p1);  // written by the SpMV step
+  const T* __restrict__ Ap = vp<T>(A.Ap);
+  const T* __restrict__ dinv = Vec<T>::dinv(A);
+  T* __restrict__ y = vp<T>(A.y);
+  T* __restrict__ r = vp<T>(A.r);
+  T* __restrict__ z = vp<T>(A.z);
+  T rz = T(0), rr = T(0);
+  for (int i = tile.begin + threadIdx.x; i < tile.end; i += blockDim.x) {
+    y[i] += alpha * p[i];
+    const T ri = r[i] - alpha * Ap[i];
+    const T zi = dinv[i] * ri;
+    r[i] = ri;
+    z[i] = zi;
+    rz += ri * zi;
+    rr += ri * ri;
+  }
+  *rz_out = static_cast<double>(rz);
+  *rr_out = static_cast<double>(rr);
+}
+
+// Row tiles: the updates and the tile's r.z, r.r.
 __global__ void __launch_bounds__(1024, 1) batch_update(const fgb_batch_system* __restrict__ sys,
                                                         const fgb_batch_state* __restrict__ st,
                                                         const fgb_batch_tile* __restrict__ tiles,
@@ -122,31 +169,25 @@ __global__ void __launch_bounds__(1024, 1) batch_update(const fgb_batch_system* 
       continue;
     }
     const fgb_batch_system& A = sys[tile.sys];
-    const float alpha = static_cast<float>(S.alpha);
-    const float* __restrict__ p = S.parity ? A.p0 : A.p1;  // written by the SpMV step
-    float rz = 0.0f, rr = 0.0f;
-    for (int i = tile.begin + threadIdx.x; i < tile.end; i += blockDim.x) {
-      A.y[i] += alpha * p[i];
-      const float ri = A.r[i] - alpha * A.Ap[i];
-      const float zi = A.dinv32[i] * ri;
-      A.r[i] = ri;
-      A.z[i] = zi;
-      rz += ri * zi;
-      rr += ri * ri;
-    }
-    const double a = block_sum(static_cast<double>(rz), red);
+    double rz, rr;
+    if (A.fp64) update_tile<double>(A, S, tile, &rz, &rr);
+    else update_tile<float>(A, S, tile, &rz, &rr);
+    const double a = block_sum(rz, red);
     __syncthreads();
-    const double b = block_sum(static_cast<double>(rr), red);
+    const double b = block_sum(rr, red);
     if (threadIdx.x == 0) { vpart[2 * t] = a; vpart[2 * t + 1] = b; }
     __syncthreads();
   }
 }
 
 // Systems (a warp each): rz, rr, beta, stopping test and whether a reliable
-// update is due; the last block to finish sets the graph conditions.
+// update is due; the last block to finish sets the graph conditions.  An FP32
+// system also gets a check of its true residual when the gap since its last
+// reliable update has grown well past the longest earlier gap (a plateau).
 __global__ void batch_control(int32_t n_sys, fgb_batch_state* st, const int32_t* __restrict__ tile_ptr,
-                              const double* __restrict__ vpart, BatchCtl* ctl, cudaGraphConditionalHandle h_if,
-                              cudaGraphConditionalHandle h_while, int graph) {
+                              const double* __restrict__ vpart, const fgb_batch_system* __restrict__ sys,
+                              BatchCtl* ctl, cudaGraphConditionalHandle h_if, cudaGraphConditionalHandle h_while,
+                              int graph) {
   __shared__ bool last;
   int any = 0, running = 0;
   const int s = warp_system();
@@ -166,7 +207,10 @@ __global__ void batch_control(int32_t n_sys, fgb_batch_state* st, const int32_t*
           if (!isfinite(res)) {
             S.done = FGB_PCG_NONFINITE;
           } else {
-            S.need_update = (res < S.delta * S.r_upd) || (res < S.tol) || (S.niter >= S.maxit);
+            const long long gap = S.niter - S.last_upd;
+            const long long slack = S.max_gap / 2 > 100 ? S.max_gap / 2 : 100;
+            const bool plateau = !sys[s].fp64 && S.max_gap > 0 && gap > S.max_gap + slack;
+            S.need_update = (res < S.delta * S.r_upd) || (res < S.tol) || (S.niter >= S.maxit) || plateau;
             S.rz_prev = S.rz;
             S.beta = rz / S.rz;
             S.rz = rz;
@@ -203,6 +247,26 @@ __global__ void batch_control(int32_t n_sys, fgb_batch_state* st, const int32_t*
   }
 }
 
+template <typename T>
+__device__ void fold_tile(const fgb_batch_system& A, const fgb_batch_tile& tile) {
+  T* y = vp<T>(A.y);
+  for (int i = tile.begin + threadIdx.x; i < tile.end; i += blockDim.x) {
+    A.x[i] += static_cast<double>(y[i]);
+    y[i] = T(0);
+  }
+}
+
+template <typename T>
+__device__ double admit_tile(const fgb_batch_system& A, const fgb_batch_tile& tile) {
+  T* y = vp<T>(A.y);
+  double bb = 0.0;
+  for (int i = tile.begin + threadIdx.x; i < tile.end; i += blockDim.x) {
+    y[i] = T(0);
+    bb += A.b[i] * A.b[i];
+  }
+  return bb;
+}
+
 // Row tiles of systems with an update due (or all given slots when force):
 // x += y, y = 0.  Admission (need_update == 2) instead zeroes y and forms the
 // per-tile partials of b.b.
@@ -220,16 +284,10 @@ __global__ void __launch_bounds__(1024, 1) batch_fold(const fgb_batch_system* __
     const int mode = S.active ? S.need_update : 0;
     const fgb_batch_system& A = sys[tile.sys];
     if (forced || (mode == 1 && !S.done)) {
-      for (int i = tile.begin + threadIdx.x; i < tile.end; i += blockDim.x) {
-        A.x[i] += static_cast<double>(A.y[i]);
-        A.y[i] = 0.0f;
-      }
+      if (A.fp64) fold_tile<double>(A, tile);
+      else fold_tile<float>(A, tile);
     } else if (mode == 2 && !S.done) {
-      double bb = 0.0;
-      for (int i = tile.begin + threadIdx.x; i < tile.end; i += blockDim.x) {
-        A.y[i] = 0.0f;
-        bb += A.b[i] * A.b[i];
-      }
+      const double bb = A.fp64 ? admit_tile<double>(A, tile) : admit_tile<float>(A, tile);
       const double v = block_sum(bb, red);
       if (threadIdx.x == 0) vpart[2 * t] = v;
       __syncthreads();
@@ -252,14 +310,17 @@ __global__ void batch_bnorm(int32_t n_sys, fgb_batch_state* st, const int32_t* _
 }
 
 // Slice tiles of systems with an update due (1) or admitted (2): r64 = b - A x
-// in FP64 arithmetic, r = float(r64), z = Dinv r; per-tile r64.r64 and r.z.
-// Admission also builds the FP32 inverse diagonal and starts p_old = z.
-template <typename V>
+// in FP64 arithmetic (V: the stored values), r = T(r64), z = Dinv r; per-tile
+// r64.r64 and r.z.  Admission of an FP32 system also builds its FP32 inverse
+// diagonal; admission starts p_old = z.
+template <typename V, typename T>
 __device__ void reliable_tile(const fgb_batch_system& A, const fgb_batch_state& S, const V* __restrict__ val,
                               const fgb_batch_tile& tile, int mode, double* rr_out, double* rz_out) {
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
   double rr64 = 0.0, rz = 0.0;
-  float* p_old = S.parity ? A.p1 : A.p0;
+  T* p_old = vp<T>(S.parity ? A.p1 : A.p0);
+  T* r = vp<T>(A.r);
+  T* z = vp<T>(A.z);
   for (int64_t s = tile.begin + wib; s < tile.end; s += wpb) {
     const int64_t sbase = A.slice_ptr[s];
     const int w = static_cast<int>((A.slice_ptr[s + 1] - sbase) >> 5);
@@ -268,17 +329,19 @@ __device__ void reliable_tile(const fgb_batch_system& A, const fgb_batch_state& 
     if (row >= 0) {
       const double r64 = A.b[row] - acc;
       rr64 += r64 * r64;
-      float di;
-      if (mode == 2) {
-        di = static_cast<float>(A.dinv64[row]);
-        A.dinv32[row] = di;
+      T di;
+      if (sizeof(T) == 8) {
+        di = static_cast<T>(A.dinv64[row]);
+      } else if (mode == 2) {
+        di = static_cast<T>(A.dinv64[row]);
+        vp<T>(A.dinv32)[row] = di;
       } else {
-        di = A.dinv32[row];
+        di = vp<T>(A.dinv32)[row];
       }
-      const float ri = static_cast<float>(r64);
-      const float zi = di * ri;
-      A.r[row] = ri;
-      A.z[row] = zi;
+      const T ri = static_cast<T>(r64);
+      const T zi = di * ri;
+      r[row] = ri;
+      z[row] = zi;
       if (mode == 2) p_old[row] = zi;
       rz += static_cast<double>(ri) * static_cast<double>(zi);
     }
@@ -300,8 +363,9 @@ __global__ void __launch_bounds__(1024, 1) batch_reliable(const fgb_batch_system
     if (!mode) continue;
     const fgb_batch_system& A = sys[tile.sys];
     double rr, rz;
-    if (A.val64) reliable_tile<double>(A, S, A.val64, tile, mode, &rr, &rz);
-    else reliable_tile<float>(A, S, A.val32, tile, mode, &rr, &rz);
+    if (A.fp64) reliable_tile<double, double>(A, S, A.val64, tile, mode, &rr, &rz);
+    else if (A.val64) reliable_tile<double, float>(A, S, A.val64, tile, mode, &rr, &rz);
+    else reliable_tile<float, float>(A, S, A.val32, tile, mode, &rr, &rz);
     const double a = block_sum(rr, red);
     __syncthreads();
     const double b = block_sum(rz, red);
@@ -311,9 +375,11 @@ __global__ void __launch_bounds__(1024, 1) batch_reliable(const fgb_batch_system
 }
 
 // Systems with an update due or admitted: true residual test, beta from the
-// replaced residual.
+// replaced residual.  An FP32 system whose true residual has not halved over
+// two consecutive checks stops as FGB_PCG_STAGNATED (its condition number is
+// beyond what FP32 iterations resolve); the caller continues it in FP64.
 __global__ void batch_reliable_fin(int32_t n_sys, fgb_batch_state* st, const int32_t* __restrict__ tile_ptr,
-                                   const double* __restrict__ rpart) {
+                                   const double* __restrict__ rpart, const fgb_batch_system* __restrict__ sys) {
   const int s = warp_system();
   if (s >= n_sys) return;
   fgb_batch_state& S = st[s];
@@ -325,10 +391,25 @@ __global__ void batch_reliable_fin(int32_t n_sys, fgb_batch_state* st, const int
   const double nrm = sqrt(rr);
   S.true_rel = S.b_norm > 0.0 ? nrm / S.b_norm : 0.0;
   S.resid = nrm;
-  if (mode == 1) S.n_updates += 1;
+  if (mode == 1) {
+    S.n_updates += 1;
+    const long long gap = S.niter - S.last_upd;
+    if (gap > S.max_gap) S.max_gap = gap;
+    S.last_upd = S.niter;
+    if (nrm < 0.5 * S.r_best) {
+      S.r_best = nrm;
+      S.stall = 0;
+    } else {
+      S.stall += 1;
+    }
+  } else {
+    S.r_best = nrm;
+    S.last_upd = S.niter;
+  }
   if (!isfinite(nrm)) S.done = FGB_PCG_NONFINITE;
   else if (nrm <= S.tol) S.done = FGB_PCG_RTOL;
   else if (S.niter >= S.maxit) S.done = FGB_PCG_MAXIT;
+  else if (!sys[s].fp64 && S.stall >= 2) S.done = FGB_PCG_STAGNATED;
   S.beta = mode == 2 ? 0.0 : rz / S.rz_prev;
   S.rz = rz;
   S.rr = rr;
@@ -355,6 +436,7 @@ __global__ void __launch_bounds__(1024, 1) batch_spmv_plain(const fgb_batch_syst
   for (int t = blockIdx.x; t < nt; t += gridDim.x) {
     const fgb_batch_tile tile = tiles[t];
     const fgb_batch_system& A = sys[tile.sys];
+    if (A.fp64) continue;
     const GatherX<float> g{xs[tile.sys]};
     float* y = ys[tile.sys];
     for (int64_t s = tile.begin + wib; s < tile.end; s += wpb) {
@@ -424,14 +506,14 @@ void launch_iteration(fgb_batch* b, cudaStream_t s, int graph, cudaGraphConditio
   batch_spmv_step<<<slice_grid(b), b->slice_threads, 0, s>>>(b->sys, b->st, b->stiles, b->n_stiles, b->spart);
   batch_alpha<<<warp_sys_blocks(b->max_sys), 256, 0, s>>>(b->max_sys, b->st, b->stile_ptr, b->spart);
   batch_update<<<row_grid(b), kBatchRowThreads, 0, s>>>(b->sys, b->st, b->vtiles, b->n_vtiles, b->vpart);
-  batch_control<<<warp_sys_blocks(b->max_sys), 256, 0, s>>>(b->max_sys, b->st, b->vtile_ptr, b->vpart, b->ctl, h_if, h_while,
+  batch_control<<<warp_sys_blocks(b->max_sys), 256, 0, s>>>(b->max_sys, b->st, b->vtile_ptr, b->vpart, b->sys, b->ctl, h_if, h_while,
                                                graph);
 }
 
 void launch_reliable(fgb_batch* b, cudaStream_t s) {
   batch_fold<<<row_grid(b), kBatchRowThreads, 0, s>>>(b->sys, b->st, b->vtiles, b->n_vtiles, nullptr, b->vpart);
   batch_reliable<<<slice_grid(b), b->slice_threads, 0, s>>>(b->sys, b->st, b->stiles, b->n_stiles, b->rpart);
-  batch_reliable_fin<<<warp_sys_blocks(b->max_sys), 256, 0, s>>>(b->max_sys, b->st, b->stile_ptr, b->rpart);
+  batch_reliable_fin<<<warp_sys_blocks(b->max_sys), 256, 0, s>>>(b->max_sys, b->st, b->stile_ptr, b->rpart, b->sys);
 }
 
 // while (running && trips < limit) { iteration ; if (update due) reliable }
@@ -563,9 +645,9 @@ int32_t fgb_batch_set(fgb_batch* b, int32_t n_sys, const fgb_batch_system* syste
     const fgb_batch_system& A = systems[s];
     if (A.n <= 0) continue;  // an empty slot: it must own no tiles
     if (A.n >= (int64_t(1) << 31) || A.n_slices != fgb_sell_slots(A.n) / kSellC || !A.slice_ptr || !A.perm ||
-        !A.col || !A.val32 || !A.dinv64 || !A.b || !A.x || !A.r || !A.z || !A.p0 || !A.p1 || !A.Ap || !A.y ||
-        !A.dinv32)
+        !A.col || !A.dinv64 || !A.b || !A.x || !A.r || !A.z || !A.p0 || !A.p1 || !A.Ap || !A.y)
       return FGB_ERR_ARG;
+    if (A.fp64 ? !A.val64 : (!A.val32 || !A.dinv32)) return FGB_ERR_ARG;
   }
   if (n_sys > 0 && (!valid_tiles(n_sys, systems, n_slice_tiles, slice_tiles, slice_tile_ptr, true) ||
                     !valid_tiles(n_sys, systems, n_row_tiles, row_tiles, row_tile_ptr, false)))
@@ -619,7 +701,7 @@ int32_t fgb_batch_admit(fgb_batch* b, int32_t n, const int32_t* slots, const dou
   batch_fold<<<row_grid(b), kBatchRowThreads, 0, s>>>(b->sys, b->st, b->vtiles, b->n_vtiles, nullptr, b->vpart);
   batch_bnorm<<<warp_sys_blocks(b->max_sys), 256, 0, s>>>(b->max_sys, b->st, b->vtile_ptr, b->vpart);
   batch_reliable<<<slice_grid(b), b->slice_threads, 0, s>>>(b->sys, b->st, b->stiles, b->n_stiles, b->rpart);
-  batch_reliable_fin<<<warp_sys_blocks(b->max_sys), 256, 0, s>>>(b->max_sys, b->st, b->stile_ptr, b->rpart);
+  batch_reliable_fin<<<warp_sys_blocks(b->max_sys), 256, 0, s>>>(b->max_sys, b->st, b->stile_ptr, b->rpart, b->sys);
   return launch_status();
 }
 

@@ -50,7 +50,9 @@ enum fgb_pcg_reason {
   FGB_PCG_MAXIT = 3,    /* iteration limit reached                           */
   FGB_PCG_ZERO_RHS = 4, /* ||b|| < 1e-15: x = 0 returned                     */
   FGB_PCG_BREAKDOWN = 5,
-  FGB_PCG_NONFINITE = 6
+  FGB_PCG_NONFINITE = 6,
+  FGB_PCG_STAGNATED = 7 /* batched FP32 iterations stopped improving the    */
+                        /* true residual (x holds the best iterate so far)  */
 };
 
 typedef struct fgb_pcg_info {
@@ -329,18 +331,21 @@ typedef struct fgb_batch_system {
   const int64_t* slice_ptr; /* SELL copy of the matrix (fgb_sell fields)   */
   const int32_t* perm;
   const int32_t* col;
-  const float* val32;       /* required                                    */
-  const double* val64;      /* optional: FP64 residual values              */
+  const float* val32;       /* FP32 values (required unless fp64)          */
+  const double* val64;      /* FP64 values (required if fp64, else optional */
+                            /* for the residual recomputation)             */
   const double* dinv64;     /* 1 / diag(A)                                 */
   const double* b;          /* right-hand side (FP64)                      */
   double* x;                /* x0 on admission, the solution on retirement */
-  float* r;                 /* n floats each, owned by the caller          */
-  float* z;
-  float* p0;
-  float* p1;
-  float* Ap;
-  float* y;
-  float* dinv32;
+  void* r;                  /* Krylov vectors, n entries each, owned by    */
+  void* z;                  /* the caller: float, or double when fp64      */
+  void* p0;
+  void* p1;
+  void* Ap;
+  void* y;
+  void* dinv32;             /* float inverse diagonal (unused when fp64)   */
+  int32_t fp64;             /* 1: this system iterates in FP64             */
+  int32_t reserved;
 } fgb_batch_system;
 
 /* Per-system state (device array; read back by fgb_batch_run). */
@@ -352,7 +357,10 @@ typedef struct fgb_batch_state {
   int32_t need_update; /* 1: reliable update due, 2: admission pending    */
   int32_t n_updates;
   int32_t parity;      /* which of p0/p1 holds the current direction      */
-  int32_t reserved;
+  int32_t stall;       /* true-residual checks without a 2x improvement   */
+  double r_best;       /* best true residual norm so far                  */
+  int64_t last_upd;    /* iteration of the last reliable update           */
+  int64_t max_gap;     /* longest interval between reliable updates       */
 } fgb_batch_state;
 
 /* A tile: rows or slices [begin, end) of system `sys`.  Tiles of a system

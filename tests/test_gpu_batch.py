@@ -115,3 +115,41 @@ def test_batch_fp32_operators_and_autotune():
     assert r.reason == 2 and _residual(A32, b32, r.x) <= RTOL * 1.0001
     times = autotune([(A32, b32)], candidates=((8, 128), (16, 256)))
     assert set(times) == {(8, 128), (16, 256)} and all(t > 0 for t in times.values())
+
+
+def _laplace_1d(n, dev, dtype):
+    """Tridiagonal 1-D Laplacian (condition number ~ 0.4 n^2), b = 1."""
+    import fealpy_gb300 as F
+    rows, cols, vals = [], [], []
+    for i in range(n):
+        for j, v in ((i - 1, -1.0), (i, 2.0), (i + 1, -1.0)):
+            if 0 <= j < n:
+                rows.append(i)
+                cols.append(j)
+                vals.append(v)
+    crow = torch.zeros(n + 1, dtype=torch.int64)
+    crow[1:] = torch.cumsum(torch.bincount(torch.tensor(rows), minlength=n), 0)
+    A = F.CSRTensor(crow.to(dev), torch.tensor(cols, dtype=torch.int32, device=dev),
+                    torch.tensor(vals, dtype=dtype, device=dev), (n, n))
+    return A, torch.ones(n, dtype=torch.float64, device=dev)
+
+
+def test_batch_fp64_systems_and_stagnation_continuation():
+    """An FP64 system of the batch follows plain FP64 PCG; an ill-conditioned
+    FP32 system either converges or is continued in FP64 after stagnating,
+    and always ends at the 1e-10 true residual."""
+    dev = cuda()
+    import fealpy_gb300 as F
+    from fealpy_gb300.batch import BatchSolver
+    (A, b) = _systems(dev)[1]
+    L, lb = _laplace_1d(6000, dev, torch.float32)
+    bs = BatchSolver(4)
+    bs.add(A, b, rtol=RTOL, key="fp64", fp64=True)
+    bs.add(L, lb, rtol=RTOL, key="ill", maxit=200000)
+    res = bs.solve_all()
+    r = res["fp64"]
+    assert r.reason == 2 and _residual(A, b, r.x) <= RTOL * 1.0001
+    x64 = F.cg(A, b, M=F.JacobiPreconditioner().apply(A), atol=0.0, rtol=RTOL, stop="residual", returninfo=True)
+    assert abs(r.niter - x64[1]["niter"]) <= 2, (r.niter, x64[1]["niter"])
+    q = res["ill"]
+    assert q.reason == 2 and _residual(L, lb, q.x) <= RTOL * 1.0001, (q.info(), bs.fallbacks)
