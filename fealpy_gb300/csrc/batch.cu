@@ -209,8 +209,10 @@ __global__ void batch_control(int32_t n_sys, fgb_batch_state* st, const int32_t*
           } else {
             const long long gap = S.niter - S.last_upd;
             const long long slack = S.max_gap / 2 > 100 ? S.max_gap / 2 : 100;
-            const bool plateau = !sys[s].fp64 && S.max_gap > 0 && gap > S.max_gap + slack;
-            S.need_update = (res < S.delta * S.r_upd) || (res < S.tol) || (S.niter >= S.maxit) || plateau;
+            // before any residual-triggered update: a first check after 1000 iterations
+            const bool plateau = !sys[s].fp64 && (S.max_gap > 0 ? gap > S.max_gap + slack : gap > 1000);
+            const bool due = (res < S.delta * S.r_upd) || (res < S.tol) || (S.niter >= S.maxit);
+            S.need_update = due ? 1 : (plateau ? 3 : 0);  // 3: a check of the true residual
             S.rz_prev = S.rz;
             S.beta = rz / S.rz;
             S.rz = rz;
@@ -283,7 +285,7 @@ __global__ void __launch_bounds__(1024, 1) batch_fold(const fgb_batch_system* __
     const bool forced = force && force[tile.sys];
     const int mode = S.active ? S.need_update : 0;
     const fgb_batch_system& A = sys[tile.sys];
-    if (forced || (mode == 1 && !S.done)) {
+    if (forced || ((mode == 1 || mode == 3) && !S.done)) {
       if (A.fp64) fold_tile<double>(A, tile);
       else fold_tile<float>(A, tile);
     } else if (mode == 2 && !S.done) {
@@ -391,10 +393,12 @@ __global__ void batch_reliable_fin(int32_t n_sys, fgb_batch_state* st, const int
   const double nrm = sqrt(rr);
   S.true_rel = S.b_norm > 0.0 ? nrm / S.b_norm : 0.0;
   S.resid = nrm;
-  if (mode == 1) {
+  if (mode != 2) {
     S.n_updates += 1;
+    // the longest gap between updates triggered by the residual estimate
+    // (not by a check) sets when the next check is due
     const long long gap = S.niter - S.last_upd;
-    if (gap > S.max_gap) S.max_gap = gap;
+    if (mode == 1 && gap > S.max_gap) S.max_gap = gap;
     S.last_upd = S.niter;
     if (nrm < 0.5 * S.r_best) {
       S.r_best = nrm;

@@ -354,7 +354,8 @@ typedef struct fgb_batch_state {
   int64_t niter, maxit;
   int32_t active;      /* 1 while the system takes part in the loop       */
   int32_t done;        /* FGB_PCG_* reason once finished, 0 while running */
-  int32_t need_update; /* 1: reliable update due, 2: admission pending    */
+  int32_t need_update; /* 1: reliable update due, 2: admission pending,   */
+                       /* 3: true-residual check on a plateau            */
   int32_t n_updates;
   int32_t parity;      /* which of p0/p1 holds the current direction      */
   int32_t stall;       /* true-residual checks without a 2x improvement   */
