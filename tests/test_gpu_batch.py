@@ -118,7 +118,8 @@ def test_batch_fp32_operators_and_autotune():
 
 
 def _laplace_1d(n, dev, dtype):
-    """Tridiagonal 1-D Laplacian (condition number ~ 0.4 n^2), b = 1."""
+    """Tridiagonal 1-D Laplacian (condition number ~ 0.4 n^2), random b (a
+    constant b would let CG end early by symmetry)."""
     import fealpy_gb300 as F
     rows, cols, vals = [], [], []
     for i in range(n):
@@ -131,7 +132,8 @@ def _laplace_1d(n, dev, dtype):
     crow[1:] = torch.cumsum(torch.bincount(torch.tensor(rows), minlength=n), 0)
     A = F.CSRTensor(crow.to(dev), torch.tensor(cols, dtype=torch.int32, device=dev),
                     torch.tensor(vals, dtype=dtype, device=dev), (n, n))
-    return A, torch.ones(n, dtype=torch.float64, device=dev)
+    g = torch.Generator(device="cpu").manual_seed(n)
+    return A, torch.rand(n, generator=g, dtype=torch.float64).to(dev)
 
 
 def test_batch_fp64_systems_and_stagnation_continuation():
@@ -142,7 +144,7 @@ def test_batch_fp64_systems_and_stagnation_continuation():
     import fealpy_gb300 as F
     from fealpy_gb300.batch import BatchSolver
     (A, b) = _systems(dev)[1]
-    L, lb = _laplace_1d(6000, dev, torch.float32)
+    L, lb = _laplace_1d(3000, dev, torch.float32)
     bs = BatchSolver(4)
     bs.add(A, b, rtol=RTOL, key="fp64", fp64=True)
     bs.add(L, lb, rtol=RTOL, key="ill", maxit=200000)
