@@ -211,7 +211,9 @@ __global__ void batch_control(int32_t n_sys, fgb_batch_state* st, const int32_t*
             const long long slack = S.max_gap / 2 > 100 ? S.max_gap / 2 : 100;
             // before any residual-triggered update: a first check after 1000 iterations
             const bool plateau = !sys[s].fp64 && (S.max_gap > 0 ? gap > S.max_gap + slack : gap > 1000);
-            const bool due = (res < S.delta * S.r_upd) || (res < S.tol) || (S.niter >= S.maxit);
+            // FP64 systems run plain FP64 PCG: the true residual is formed only
+            // to confirm convergence (or at the iteration limit)
+            const bool due = (!sys[s].fp64 && res < S.delta * S.r_upd) || (res < S.tol) || (S.niter >= S.maxit);
             S.need_update = due ? 1 : (plateau ? 3 : 0);  // 3: a check of the true residual
             S.rz_prev = S.rz;
             S.beta = rz / S.rz;
