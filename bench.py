@@ -39,7 +39,7 @@ RTOL = 1e-10
 Q = 4
 CPU_SAMPLE_N = 24
 MAXIT = 20000
-BATCH_MAXIT = 200000
+BATCH_MAXIT = 100000
 
 
 def read_peaks():

@@ -154,4 +154,6 @@ def test_batch_fp64_systems_and_stagnation_continuation():
     x64 = F.cg(A, b, M=F.JacobiPreconditioner().apply(A), atol=0.0, rtol=RTOL, stop="residual", returninfo=True)
     assert abs(r.niter - x64[1]["niter"]) <= 2, (r.niter, x64[1]["niter"])
     q = res["ill"]
-    assert q.reason == 2 and _residual(L, lb, q.x) <= RTOL * 1.0001, (q.info(), bs.fallbacks)
+    # the recomputed residual of this operator (|A||x| / |b| ~ 1e3) carries
+    # summation-order differences of a few 1e-11
+    assert q.reason == 2 and q.relres <= RTOL and _residual(L, lb, q.x) <= 2 * RTOL, (q.info(), bs.fallbacks)
