@@ -211,7 +211,7 @@ class BatchSolver:
             for i in done:
                 sl, stt = self._slots[i], states[i]
                 self._slots[i] = None
-                if stt.done == 7:  # FP32 iterations stagnated: continue in FP64 from x
+                if stt.done == 7 and not sl.fp64:  # FP32 iterations stagnated: continue in FP64 from x
                     restart.append((sl, int(stt.niter), int(stt.n_updates)))
                     continue
                 if stt.done == 4:  # zero right-hand side: x = 0

@@ -29,7 +29,6 @@ namespace fgb {
 
 constexpr int kBatchRowThreads = 512;
 constexpr int kBatchRowBlocks = 2 * kNumSMs;
-constexpr int kBatchSliceBlocks = 8 * kNumSMs;
 
 struct BatchCtl {
   long long trips, trip_limit, if_trips;
@@ -415,7 +414,7 @@ __global__ void batch_reliable_fin(int32_t n_sys, fgb_batch_state* st, const int
   if (!isfinite(nrm)) S.done = FGB_PCG_NONFINITE;
   else if (nrm <= S.tol) S.done = FGB_PCG_RTOL;
   else if (S.niter >= S.maxit) S.done = FGB_PCG_MAXIT;
-  else if (!sys[s].fp64 && S.stall >= 2) S.done = FGB_PCG_STAGNATED;
+  else if (S.stall >= (sys[s].fp64 ? 3 : 2)) S.done = FGB_PCG_STAGNATED;  // FP64: attainable accuracy
   S.beta = mode == 2 ? 0.0 : rz / S.rz_prev;
   S.rz = rz;
   S.rr = rr;
@@ -504,7 +503,13 @@ size_t batch_layout(int32_t ms, int32_t mst, int32_t mvt, fgb_batch* b, void* ba
 
 int sys_blocks(int32_t n) { return (n + 255) / 256; }
 int warp_sys_blocks(int32_t n) { return (n * 32 + 255) / 256; }  // one warp per system
-int slice_grid(const fgb_batch* b) { return b->max_st < kBatchSliceBlocks ? b->max_st : kBatchSliceBlocks; }
+// The tile loops are persistent: as many blocks as stay resident at once (the
+// slice kernels use up to 64 registers a thread, so 1024 threads per SM), so
+// that no block of a later wave holds a tile back.
+int slice_grid(const fgb_batch* b) {
+  const int resident = kNumSMs * (1024 / b->slice_threads > 0 ? 1024 / b->slice_threads : 1);
+  return b->max_st < resident ? b->max_st : resident;
+}
 int row_grid(const fgb_batch* b) { return b->max_vt < kBatchRowBlocks ? b->max_vt : kBatchRowBlocks; }
 
 void launch_iteration(fgb_batch* b, cudaStream_t s, int graph, cudaGraphConditionalHandle h_if,

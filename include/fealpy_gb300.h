@@ -51,8 +51,9 @@ enum fgb_pcg_reason {
   FGB_PCG_ZERO_RHS = 4, /* ||b|| < 1e-15: x = 0 returned                     */
   FGB_PCG_BREAKDOWN = 5,
   FGB_PCG_NONFINITE = 6,
-  FGB_PCG_STAGNATED = 7 /* batched FP32 iterations stopped improving the    */
-                        /* true residual (x holds the best iterate so far)  */
+  FGB_PCG_STAGNATED = 7 /* batched solver: the true residual stopped        */
+                        /* improving (FP32 iterations: continue in FP64;    */
+                        /* FP64: the attainable accuracy is above rtol)     */
 };
 
 typedef struct fgb_pcg_info {
