@@ -1,0 +1,52 @@
+"""Serving loop (fealpy_gb300.serving): requests arriving over time are
+admitted into the running batch as slots and memory free up, every result
+meets the 1e-10 true residual, and each result is the same (bit for bit)
+alone and in the mix."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def cuda():
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA device")
+    return torch.device("cuda", 0)
+
+
+def _stream():
+    from fealpy_gb300.workloads import serving_requests
+    # a short stream of small requests at a high arrival rate, so that many
+    # arrive while others are still iterating
+    return serving_requests(24, rate=400.0, seed=11, dof_range=(3e2, 2e4))
+
+
+def test_serving_mix_equals_solo_and_converges():
+    dev = cuda()
+    from fealpy_gb300.serving import SolveServer, poisson_request_problem
+    from fealpy_gb300.batch import BatchSolver
+    reqs = _stream()
+    srv = SolveServer(max_slots=6, chunk=16, device=dev)
+    out = srv.run(reqs, keep_solutions=True)
+    assert out["n"] == len(reqs) and out["p99_s"] >= out["p50_s"] > 0
+    assert out["max_relres"] <= 1e-10 * 1.0001
+    assert srv.resident == 0 and srv.peak_resident > 0
+    for i, r in enumerate(reqs):
+        A, b = poisson_request_problem(r, dev)
+        bs = BatchSolver(1, max_slice_tiles=1 << 17, max_row_tiles=1 << 17, device=dev)
+        bs.add(A, b, rtol=1e-10, maxit=100000, key=0)
+        solo = bs.solve_all()[0]
+        assert np.array_equal(solo.x.cpu().numpy(), out["solutions"][i]), i
+
+
+def test_serving_memory_budget_limits_admission():
+    dev = cuda()
+    from fealpy_gb300.serving import SolveServer, resident_estimate
+    reqs = _stream()[:8]
+    # a budget of a little more than the largest request: one at a time
+    big = max(resident_estimate(r["dofs"], 20 * r["dofs"], False) for r in reqs)
+    srv = SolveServer(max_slots=8, chunk=16, hbm_budget=1.2 * big, device=dev)
+    out = srv.run(reqs)
+    assert out["n"] == len(reqs) and out["max_relres"] <= 1e-10 * 1.0001
+    assert srv.peak_resident <= 1.2 * big
