@@ -332,6 +332,11 @@ def run_ours(args):
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(CPU_SAMPLE_N, repeats=3)
 
+    # a short sample of the serving stream (the full sweep: --workload serving)
+    serving = None
+    if rank == 0 and world == 1 and not args.no_serving:
+        serving = serving_sample(torch, dev, args.serve_sample)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "DOF/s", "n_gpus": world, "steps": args.steps,
@@ -363,6 +368,7 @@ def run_ours(args):
                          "avg_launch_ms": mixed["kernel_ms_avg"], "peak_source": peak_kind},
             "clocks": mixed["clocks"],
             "cpu_baseline": cpu,
+            "serving": serving,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -537,6 +543,24 @@ def run_batched(args):
 # ---------------------------------------------------------------------------
 # serving workload: Poisson arrivals, continuous batching under a memory budget
 # ---------------------------------------------------------------------------
+def serving_sample(torch, dev, count, rate=200.0):
+    """p50/p99 latency and throughput of a short request stream, FP32-refined
+    and plain FP64 (continuous batching, 150 GB budget, 256 slots)."""
+    from fealpy_gb300.serving import SolveServer, poisson_request_problem
+    from fealpy_gb300.workloads import serving_requests
+    reqs = serving_requests(count, rate=rate, seed=3)
+    out = {"requests": count, "arrival_rate_rps": rate, "workload": "C4 stream (70% tri P1/P2, 30% tet P1, "
+                                                                    "1e3-2e6 dofs)"}
+    SolveServer(max_slots=8, device=dev).run(serving_requests(4, rate=1e6, seed=99, dof_range=(1e3, 1e4)))
+    for prec in ("mixed", "fp64"):
+        srv = SolveServer(hbm_budget=150e9, max_slots=256, chunk=64, fp64=(prec == "fp64"), device=dev)
+        r = srv.run(reqs, poisson_request_problem)
+        out[prec] = {"p50_ms": r["p50_s"] * 1e3, "p99_ms": r["p99_s"] * 1e3, "throughput_rps": r["throughput_rps"],
+                     "dofs_per_s": r["dofs_per_s"], "max_relres": r["max_relres"],
+                     "fp64_continuations": r["fp64_continuations"]}
+    return out
+
+
 def run_serving(args):
     import torch
     from fealpy_gb300.serving import SolveServer, poisson_request_problem
@@ -593,6 +617,8 @@ def main():
     ap.add_argument("--serve-count", type=int, default=200, help="requests per arrival rate")
     ap.add_argument("--serve-rates", default="50,200,1000")
     ap.add_argument("--serve-chunk", type=int, default=64)
+    ap.add_argument("--serve-sample", type=int, default=32, help="requests of the serving sample in the default run")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving sample of the default run")
     args = ap.parse_args()
     if args.workload == "batched" and args.impl == "ours":
         run_batched(args)
