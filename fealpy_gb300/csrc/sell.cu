@@ -155,6 +155,12 @@ struct SellPcgState {
   long long niter, maxit, trips, trip_cap;
   int done, need_update, n_updates, norm_rr;
   unsigned int counter[4];
+  // mixed solver, plateau detection: best true residual, reliable updates in a
+  // row without halving it, iteration of the last update, longest gap between
+  // updates triggered by the residual estimate
+  double r_best;
+  long long last_upd, max_gap;
+  int stall, pad;
 };
 
 // Last-block-done deterministic reduction of two FP64 partials per block.
@@ -446,7 +452,15 @@ __global__ void __launch_bounds__(1024, 1) sell_mixed_update(int64_t n, const fl
     st->resid = res;
     st->rr = trr;
     if (!isfinite(res)) st->done = FGB_PCG_NONFINITE;
-    else st->need_update = (res < delta * st->r_upd) || (res < st->tol) || (st->niter >= st->maxit);
+    else {
+      // a check of the true residual when the gap since the last update has
+      // grown well past the longest earlier one (FP32 iterations on a plateau)
+      const long long gap = st->niter - st->last_upd;
+      const long long slack = st->max_gap / 2 > 100 ? st->max_gap / 2 : 100;
+      const bool plateau = st->max_gap > 0 ? gap > st->max_gap + slack : gap > 1000;
+      const bool due = (res < delta * st->r_upd) || (res < st->tol) || (st->niter >= st->maxit);
+      st->need_update = due ? 1 : (plateau ? 3 : 0);
+    }
     st->rz_prev = st->rz;
     st->beta = trz / st->rz;
     st->rz = trz;
@@ -505,10 +519,25 @@ __global__ void __launch_bounds__(1024, 1) sell_mixed_reliable(SellView A, const
     const double nrm = sqrt(trr);
     st->true_rel = st->b_norm > 0.0 ? nrm / st->b_norm : 0.0;
     st->resid = nrm;
-    if (!first) st->n_updates += 1;
+    if (!first) {
+      st->n_updates += 1;
+      const long long gap = st->niter - st->last_upd;
+      if (st->need_update == 1 && gap > st->max_gap) st->max_gap = gap;
+      st->last_upd = st->niter;
+      if (nrm < 0.5 * st->r_best) {
+        st->r_best = nrm;
+        st->stall = 0;
+      } else {
+        st->stall += 1;
+      }
+    } else {
+      st->r_best = nrm;
+      st->last_upd = 0;
+    }
     if (!isfinite(nrm)) st->done = FGB_PCG_NONFINITE;
     else if (nrm <= st->tol) st->done = FGB_PCG_RTOL;
     else if (st->niter >= st->maxit) st->done = FGB_PCG_MAXIT;
+    else if (st->stall >= 2) st->done = FGB_PCG_STAGNATED;  // the caller continues in FP64
     st->beta = first ? 0.0 : trz / st->rz_prev;
     st->rz = trz;
     st->rr = trr;

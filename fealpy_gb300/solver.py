@@ -156,7 +156,20 @@ def cg_mixed(A: CSRTensor, b: torch.Tensor, x0: Optional[torch.Tensor] = None, M
                            lanes_per_row, profile)
     else:
         raise ValueError("solver_format must be 'sell' or 'csr'")
-    out = _info_dict(info, {"relres": info.true_relres, "n_updates": int(info.n_updates)})
+    out = _info_dict(info, {"relres": info.true_relres, "n_updates": int(info.n_updates), "fp64_iterations": 0})
+    if info.reason == 7:
+        # the FP32 iterations stopped improving the true residual (a condition
+        # number beyond FP32): continue with FP64 PCG from the current iterate
+        logger.info(f"cg_mixed: FP32 iterations stagnated at relres {info.true_relres:.2e}; continuing in FP64")
+        dinv64 = dinv if dinv is not None else A.diagonal_inverse().to(torch.float64)
+        M64 = CSRTensor(torch.arange(A.shape[0] + 1, device=x.device), torch.arange(A.shape[0], device=x.device,
+                        dtype=torch.int32), dinv64, A.shape)
+        x, i64 = cg(A, b, x0=x, M=M64, atol=0.0, rtol=rtol, maxit=max(maxit - int(info.niter), 1), returninfo=True,
+                    stop="residual", graph=graph)
+        Ad = CSRTensor(A.crow, A.col, A.values.to(torch.float64), A.shape)
+        rel = float(torch.linalg.norm(b - Ad @ x) / torch.linalg.norm(b))
+        out.update({"niter": out["niter"] + i64["niter"], "reason": i64["reason"], "relres": rel,
+                    "fp64_iterations": i64["niter"], "graph": out["graph"] and i64["graph"]})
     if returninfo:
         return x, out
     return x

@@ -51,9 +51,10 @@ enum fgb_pcg_reason {
   FGB_PCG_ZERO_RHS = 4, /* ||b|| < 1e-15: x = 0 returned                     */
   FGB_PCG_BREAKDOWN = 5,
   FGB_PCG_NONFINITE = 6,
-  FGB_PCG_STAGNATED = 7 /* batched solver: the true residual stopped        */
-                        /* improving (FP32 iterations: continue in FP64;    */
-                        /* FP64: the attainable accuracy is above rtol)     */
+  FGB_PCG_STAGNATED = 7 /* the true residual stopped improving: FP32       */
+                        /* iterations (fgb_pcg_sell_mixed, batched): the    */
+                        /* caller continues in FP64 from x; batched FP64:   */
+                        /* the attainable accuracy is above rtol            */
 };
 
 typedef struct fgb_pcg_info {

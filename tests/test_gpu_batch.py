@@ -157,3 +157,14 @@ def test_batch_fp64_systems_and_stagnation_continuation():
     # the recomputed residual of this operator (|A||x| / |b| ~ 1e3) carries
     # summation-order differences of a few 1e-11
     assert q.reason == 2 and q.relres <= RTOL and _residual(L, lb, q.x) <= 2 * RTOL, (q.info(), bs.fallbacks)
+
+
+def test_cg_mixed_continues_in_fp64_after_stagnation():
+    """The single-system FP32-refined solver on an operator beyond FP32
+    (condition number ~4e6) ends at the 1e-10 true residual, continuing in
+    FP64 if its FP32 iterations stall."""
+    dev = cuda()
+    import fealpy_gb300 as F
+    L, lb = _laplace_1d(3000, dev, torch.float32)
+    x, info = F.cg_mixed(L, lb, rtol=RTOL, maxit=200000, returninfo=True)
+    assert info["reason"] == 2 and _residual(L, lb, x) <= 2 * RTOL, info
