@@ -164,12 +164,27 @@ def cg_mixed(A: CSRTensor, b: torch.Tensor, x0: Optional[torch.Tensor] = None, M
         dinv64 = dinv if dinv is not None else A.diagonal_inverse().to(torch.float64)
         M64 = CSRTensor(torch.arange(A.shape[0] + 1, device=x.device), torch.arange(A.shape[0], device=x.device,
                         dtype=torch.int32), dinv64, A.shape)
-        x, i64 = cg(A, b, x0=x, M=M64, atol=0.0, rtol=rtol, maxit=max(maxit - int(info.niter), 1), returninfo=True,
-                    stop="residual", graph=graph)
         Ad = CSRTensor(A.crow, A.col, A.values.to(torch.float64), A.shape)
-        rel = float(torch.linalg.norm(b - Ad @ x) / torch.linalg.norm(b))
-        out.update({"niter": out["niter"] + i64["niter"], "reason": i64["reason"], "relres": rel,
-                    "fp64_iterations": i64["niter"], "graph": out["graph"] and i64["graph"]})
+        bn = float(torch.linalg.norm(b))
+        left, its, rel, reason, best = max(maxit - int(info.niter), 1), 0, float(info.true_relres), 3, None
+        # FP64 PCG restarted from the current iterate until the true residual
+        # (formed in FP64) meets rtol; each restart re-forms r = b - A x, so the
+        # drift of the iterated residual cannot end the solve early
+        for _ in range(8):
+            x, i64 = cg(A, b, x0=x, M=M64, atol=0.0, rtol=rtol, maxit=left, returninfo=True, stop="residual",
+                        graph=graph)
+            its += i64["niter"]
+            left -= i64["niter"]
+            new = float(torch.linalg.norm(b - Ad @ x)) / bn
+            if new <= rtol:
+                rel, reason = new, 2
+                break
+            if left <= 0 or new > 0.5 * rel:
+                rel, reason = new, (3 if left <= 0 else 7)
+                break
+            rel = new
+        out.update({"niter": out["niter"] + its, "reason": reason, "relres": rel, "fp64_iterations": its,
+                    "graph": out["graph"] and i64["graph"]})
     if returninfo:
         return x, out
     return x
