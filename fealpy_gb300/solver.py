@@ -166,7 +166,7 @@ def cg_mixed(A: CSRTensor, b: torch.Tensor, x0: Optional[torch.Tensor] = None, M
                         dtype=torch.int32), dinv64, A.shape)
         Ad = CSRTensor(A.crow, A.col, A.values.to(torch.float64), A.shape)
         bn = float(torch.linalg.norm(b))
-        left, its, rel, reason, best = max(maxit - int(info.niter), 1), 0, float(info.true_relres), 3, None
+        left, its, rel, reason = max(maxit - int(info.niter), 1), 0, float(info.true_relres), 3
         # FP64 PCG restarted from the current iterate until the true residual
         # (formed in FP64) meets rtol; each restart re-forms r = b - A x, so the
         # drift of the iterated residual cannot end the solve early
