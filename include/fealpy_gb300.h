@@ -11,6 +11,9 @@
  *     sized by the matching *_workspace_bytes() query, and the library never
  *     frees caller memory;
  *   - never traps or aborts; it keeps no global mutable state.
+ * Two documented exceptions: fgb_pcg_f64_noalloc uses a static device array
+ * of the library instead of a workspace, and an fgb_batch handle (host
+ * object created by fgb_batch_create) owns the CUDA graph it captures.
  *
  * Index conventions follow FEALPy: cell-to-dof maps are int32 (NC, ldof)
  * row-major, CSR row pointers are int64 (FEALPy's `crow` dtype after
