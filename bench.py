@@ -543,6 +543,74 @@ def run_batched(args):
 # ---------------------------------------------------------------------------
 # serving workload: Poisson arrivals, continuous batching under a memory budget
 # ---------------------------------------------------------------------------
+def run_elasticity(args):
+    """P1 vector linear elasticity on an n^3 tetrahedral box (default 128^3:
+    12,582,912 cells, 6,440,067 dofs): lambda = 1, mu = 0.5 scaled per cell by
+    exp(N(0, 0.5)), clamped at x = 0, body force (0, 0, -1), q = 4, rtol 1e-8;
+    FP32-refined iterations (FP64 operator) beside plain FP64."""
+    import torch
+    import fealpy_gb300 as F
+    from fealpy_gb300.fem import BilinearForm, LinearForm, LinearElasticityIntegrator, VectorSourceIntegrator
+    from fealpy_gb300.fem import DirichletBC
+    from fealpy_gb300.workloads import elasticity_tet_box
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    n = args.elast_n
+    node_np, cell_np, scale_np = elasticity_tet_box(n)
+    mesh = F.TetrahedronMesh(torch.as_tensor(node_np, device=dev), torch.as_tensor(cell_np, device=dev))
+    ts = F.TensorFunctionSpace(F.LagrangeFESpace(mesh, 1), (-1, 3))
+    mat = F.LinearElasticMaterial("m", lame_lambda=1.0, shear_modulus=0.5,
+                                  cell_scale=torch.as_tensor(scale_np, device=dev))
+    bc = DirichletBC(ts, gd=0.0, threshold=lambda x: torch.abs(x[..., 0]) < 1e-12)
+    gdof = ts.number_of_global_dofs()
+    rtol = 1e-8
+
+    def step(mode):
+        bf = BilinearForm(ts)
+        bf.add_integrator(LinearElasticityIntegrator(mat, q=4))
+        A = bf.assembly()
+        lf = LinearForm(ts)
+        lf.add_integrator(VectorSourceIntegrator(source=[0.0, 0.0, -1.0], q=4))
+        A2, F2 = bc.apply(A, lf.assembly())
+        if mode == "mixed":
+            x, info = F.cg_mixed(A2, F2, rtol=rtol, maxit=200000, returninfo=True)
+        else:
+            x, info = F.cg(A2, F2, M=F.JacobiPreconditioner().apply(A2), atol=0.0, rtol=rtol, maxit=200000,
+                           returninfo=True, stop="residual")
+        return x, info, A2, F2
+
+    res = {}
+    for mode in ("mixed", "fp64"):
+        for _ in range(args.warmup):
+            step(mode)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            x, info, A2, F2 = step(mode)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        r = F2 - A2 @ x
+        res[mode] = {"ms_per_step": ms, "dof_per_s": gdof / (ms / 1e3), "cg_iters": info["niter"],
+                     "true_relres": float(torch.linalg.norm(r) / torch.linalg.norm(F2)),
+                     "fp64_iterations": info.get("fp64_iterations", info["niter"] if mode == "fp64" else 0),
+                     "x": x, "nnz": A2.nnz}
+    err = float((res["mixed"]["x"] - res["fp64"]["x"]).abs().max() / res["fp64"]["x"].abs().max())
+    for m in res:
+        res[m].pop("x")
+    line = {"metric": "DOF/s assemble+PCG to 1e-8 rel res, P1 vector elasticity (C5)",
+            "value": res["mixed"]["dof_per_s"], "unit": "DOF/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": res["mixed"]["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+            "data": "synthetic (seeded per-cell material scale)",
+            "config": {"workload": f"LinearElasticityIntegrator P1 TetrahedronMesh box {n}^3 (C5)",
+                       "cells": int(cell_np.shape[0]), "gdof": gdof, "rtol": rtol, "quadrature": 4},
+            "fp32_refined": res["mixed"], "fp64": res["fp64"], "max_rel_err_vs_fp64": err,
+            "speedup_fp32_refined_vs_fp64": res["fp64"]["ms_per_step"] / res["mixed"]["ms_per_step"]}
+    print(json.dumps(line), flush=True)
+
+
 def serving_sample(torch, dev, count, rate=200.0):
     """p50/p99 latency and throughput of a short request stream, FP32-refined
     and plain FP64 (continuous batching, 150 GB budget, 256 slots)."""
@@ -610,9 +678,10 @@ def main():
     ap.add_argument("--no-graph", action="store_true",
                     help="host-polled solver loop instead of the CUDA-graph loop (profiling runs: a profiler "
                          "cannot capture kernels inside a graph that has conditional nodes)")
-    ap.add_argument("--workload", choices=["c2", "batched", "serving"], default="c2",
+    ap.add_argument("--workload", choices=["c2", "batched", "serving", "elasticity"], default="c2",
                     help="c2: the P2 tet box (default, the headline line); batched: 256 uneven triangle meshes; "
-                         "serving: the request stream")
+                         "serving: the request stream; elasticity: P1 vector elasticity on a tet box")
+    ap.add_argument("--elast-n", type=int, default=128)
     ap.add_argument("--batch-count", type=int, default=256)
     ap.add_argument("--serve-count", type=int, default=200, help="requests per arrival rate")
     ap.add_argument("--serve-rates", default="50,200,1000")
@@ -625,6 +694,9 @@ def main():
         return
     if args.workload == "serving" and args.impl == "ours":
         run_serving(args)
+        return
+    if args.workload == "elasticity" and args.impl == "ours":
+        run_elasticity(args)
         return
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
