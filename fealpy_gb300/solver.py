@@ -179,7 +179,7 @@ def cg_mixed(A: CSRTensor, b: torch.Tensor, x0: Optional[torch.Tensor] = None, M
             if new <= rtol:
                 rel, reason = new, 2
                 break
-            if left <= 0 or new > 0.5 * rel:
+            if left <= 0 or new > 0.9 * rel:
                 rel, reason = new, (3 if left <= 0 else 7)
                 break
             rel = new
