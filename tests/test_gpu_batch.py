@@ -161,10 +161,12 @@ def test_batch_fp64_systems_and_stagnation_continuation():
 
 def test_cg_mixed_continues_in_fp64_after_stagnation():
     """The single-system FP32-refined solver on an operator beyond FP32
-    (condition number ~4e6) ends at the 1e-10 true residual, continuing in
-    FP64 if its FP32 iterations stall."""
+    (condition number ~4e6) continues in FP64 when its FP32 iterations stall
+    and ends at 1e-10 or at the attainable accuracy of this operator (its
+    FP64 residual floor is about 1.2e-10: then reason 7, 'stagnated')."""
     dev = cuda()
     import fealpy_gb300 as F
     L, lb = _laplace_1d(3000, dev, torch.float32)
     x, info = F.cg_mixed(L, lb, rtol=RTOL, maxit=200000, returninfo=True)
-    assert info["reason"] == 2 and _residual(L, lb, x) <= 2 * RTOL, info
+    assert info["fp64_iterations"] > 0, info
+    assert info["reason"] in (2, 7) and _residual(L, lb, x) <= 2 * RTOL, info
