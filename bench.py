@@ -123,6 +123,21 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # our arm
 # ---------------------------------------------------------------------------
+def replica_max(torch, dist, v, world, dev):
+    """The slowest rank's time: every rank solves its own replica (the path
+    has no data exchange between GPUs), so the job ends with the slowest."""
+    if world == 1:
+        return v
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(gdof, world, ms_per_step):
+    """Whole-job DOF/s: all ranks' dofs over the slowest rank's step time."""
+    return world * gdof / (ms_per_step / 1e3)
+
+
 def build_problem(torch, F, node_np, cell_np, kappa_np, dev):
     node = torch.as_tensor(node_np, device=dev)
     cell = torch.as_tensor(cell_np, device=dev)
@@ -205,11 +220,7 @@ def run_ours(args):
             dist.barrier()
 
     def max_over_ranks(v):
-        if world == 1:
-            return v
-        t = torch.tensor([v], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return replica_max(torch, dist, v, world, dev)
 
     results = {}
     modes = [m for m in args.modes.split(",") if m]
@@ -313,7 +324,7 @@ def run_ours(args):
     peak, peak_kind = read_peaks()
     mixed = results["mixed"]
     fp64 = results["fp64"]
-    value = world * gdof / (mixed["ms_per_step"] / 1e3)
+    value = replica_value(gdof, world, mixed["ms_per_step"])
     # dominant kernel: the fused FP32 PCG SpMV (p = z + beta p_old, Ap = A p, p.Ap)
     nnz = mixed["nnz"]
     # values + columns of the real entries, the slot->row map, z and p_old read
