@@ -63,6 +63,8 @@ _SIGNATURES = {
     "fgb_pattern_workspace_bytes": (c_sz, [c_i64]),
     "fgb_pattern_count": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_i32, c_vp, c_vp, c_vp, c_sz, c_vp]),
     "fgb_pattern_fill": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_i32, c_vp, c_vp, c_vp, c_vp, c_sz, c_vp]),
+    "fgb_pattern_build": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_i32, c_i64, c_vp, c_vp, c_sz, c_vp, c_vp, c_sz, c_vp]),
+    "fgb_pattern_compact": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_sz, c_vp]),
     "fgb_pattern_expand_blocks": (c_i32, [c_i64, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "fgb_cell_factors": (c_i32, [c_i32, c_i64, c_vp, c_vp, c_i32, c_vp, c_vp, c_vp, c_vp, c_i32, c_vp, c_vp, c_vp]),
     "fgb_assemble_workspace_bytes": (c_sz, [c_i64]),
@@ -173,7 +175,7 @@ def check(fn_name, code):
 # Kernels each entry point launches per call (the solvers report theirs in
 # fgb_pcg_info.launches).  Used to count this library's launches in a region.
 KERNELS_PER_CALL = {
-    "fgb_cell_factors": 1, "fgb_adjacency_build": 6, "fgb_pattern_count": 5, "fgb_pattern_fill": 2,
+    "fgb_cell_factors": 1, "fgb_adjacency_build": 6, "fgb_pattern_count": 5, "fgb_pattern_fill": 2, "fgb_pattern_build": 5, "fgb_pattern_compact": 2,
     "fgb_pattern_expand_blocks": 2, "fgb_assemble_scalar": 2, "fgb_assemble_elasticity_p1": 2,
     "fgb_dirichlet_count": 1, "fgb_exclusive_scan_i32": 3, "fgb_dirichlet_fill": 1, "fgb_csr_spmv": 1,
     "fgb_csr_diagonal": 1, "fgb_gather_sum": 1, "fgb_sell_plan": 4, "fgb_sell_fill": 1, "fgb_sell_spmv": 1,

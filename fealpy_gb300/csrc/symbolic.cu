@@ -283,10 +283,31 @@ __device__ bool pattern_row(int64_t i, int mode, const int64_t* __restrict__ adj
 constexpr int kHashSlots = 256;
 constexpr int kHashMaxUnique = 128;
 
+// Ascending sort of one value per lane across the warp (bitonic network on
+// registers, 15 shuffle steps).
+__device__ __forceinline__ int32_t warp_sort32(int32_t v) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      const int32_t o = __shfl_xor_sync(0xffffffffu, v, j);
+      const bool up = (lane & k) == 0;
+      const bool low = (lane & j) == 0;
+      v = (low == up) ? min(v, o) : max(v, o);
+    }
+  }
+  return v;
+}
+
+// mode 0: count (row_cnt); 1: write the sorted row into indices at indptr[i];
+// 2: count and stage the sorted row at stage[adj_ptr[i] * ldof] (its upper
+// bound of entries), so that the values need no second pass.
 __device__ bool pattern_row_hash(int64_t i, int mode, const int64_t* __restrict__ adj_ptr,
                                  const int32_t* __restrict__ adj, const int32_t* __restrict__ c2d, int ldof,
                                  int32_t* __restrict__ row_cnt, const int64_t* __restrict__ indptr,
-                                 int32_t* __restrict__ indices, int32_t* tab, int32_t* srt) {
+                                 int32_t* __restrict__ indices, int32_t* __restrict__ stage, int32_t* tab,
+                                 int32_t* srt) {
   const int lane = threadIdx.x & 31;
   const int64_t s = adj_ptr[i];
   const int m = static_cast<int>(adj_ptr[i + 1] - s) * ldof;
@@ -320,6 +341,17 @@ __device__ bool pattern_row_hash(int64_t i, int mode, const int64_t* __restrict_
     u += __popc(ball);
   }
   if (u > kHashMaxUnique) return false;
+  if (u <= 32) {
+    __syncwarp();
+    const int32_t v = warp_sort32(lane < u ? srt[lane] : INT_MAX);
+    if (mode == 0 || mode == 2) {
+      if (lane == 0) row_cnt[i] = u;
+    }
+    if (mode == 1 && lane < u) indices[indptr[i] + lane] = v;
+    if (mode == 2 && lane < u) stage[adj_ptr[i] * ldof + lane] = v;
+    __syncwarp();
+    return true;
+  }
   const int np2 = next_pow2(u > 0 ? u : 1);
   for (int t = u + lane; t < np2; t += 32) srt[t] = INT_MAX;
   __syncwarp();
@@ -336,11 +368,15 @@ __device__ bool pattern_row_hash(int64_t i, int mode, const int64_t* __restrict_
       __syncwarp();
     }
   }
-  if (mode == 0) {
+  if (mode == 0 || mode == 2) {
     if (lane == 0) row_cnt[i] = u;
-  } else {
+  }
+  if (mode == 1) {
     const int64_t out0 = indptr[i];
     for (int t = lane; t < u; t += 32) indices[out0 + t] = srt[t];
+  } else if (mode == 2) {
+    const int64_t out0 = adj_ptr[i] * ldof;
+    for (int t = lane; t < u; t += 32) stage[out0 + t] = srt[t];
   }
   __syncwarp();
   return true;
@@ -350,7 +386,8 @@ __global__ void __launch_bounds__(kPatWarps * 32) pattern_pass1(int64_t n_dof, i
                                                                 const int32_t* __restrict__ adj, const int32_t* __restrict__ c2d,
                                                                 int ldof, int32_t* __restrict__ row_cnt,
                                                                 const int64_t* __restrict__ indptr, int32_t* __restrict__ indices,
-                                                                int32_t* __restrict__ ovf, int32_t* __restrict__ ovf_len) {
+                                                                int32_t* __restrict__ ovf, int32_t* __restrict__ ovf_len,
+                                                                int32_t* __restrict__ stage) {
   __shared__ int32_t stab[kPatWarps * kHashSlots];
   __shared__ int32_t ssrt[kPatWarps * kHashMaxUnique];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -359,11 +396,28 @@ __global__ void __launch_bounds__(kPatWarps * 32) pattern_pass1(int64_t n_dof, i
   const int64_t warp = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
   const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
   for (int64_t i = warp; i < n_dof; i += nwarps) {
-    bool done = pattern_row_hash(i, mode, adj_ptr, adj, c2d, ldof, row_cnt, indptr, indices, tab, srt);
+    bool done = pattern_row_hash(i, mode, adj_ptr, adj, c2d, ldof, row_cnt, indptr, indices, stage, tab, srt);
     if (!done && lane == 0) {
       int slot = atomicAdd(ovf_len, 1);
       ovf[slot] = static_cast<int32_t>(i);
+      if (mode == 2) stage[adj_ptr[i] * ldof] = -1;  // this row is not staged: pass 2 writes it
     }
+  }
+}
+
+// Staged rows -> indices (warp per row); rows marked -1 are left to pass 2.
+__global__ void pattern_compact(int64_t n_dof, const int64_t* __restrict__ adj_ptr, int ldof,
+                                const int64_t* __restrict__ indptr, const int32_t* __restrict__ stage,
+                                int32_t* __restrict__ indices) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
+  const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+  for (int64_t i = warp; i < n_dof; i += nwarps) {
+    const int64_t o = indptr[i];
+    const int len = static_cast<int>(indptr[i + 1] - o);
+    const int64_t src = adj_ptr[i] * ldof;
+    if (len == 0 || stage[src] < 0) continue;  // empty row (no staged slot to read) / row left to pass 2
+    for (int t = lane; t < len; t += 32) indices[o + t] = stage[src + t];
   }
 }
 
@@ -471,7 +525,7 @@ static int pattern_launch(int mode, int64_t n_dof, const int64_t* adj_ptr, const
                           int32_t* ovf_len, int32_t* status, cudaStream_t st) {
   cudaMemsetAsync(ovf_len, 0, sizeof(int32_t), st);
   pattern_pass1<<<grid_for(n_dof * 32, kPatWarps * 32, kNumSMs * 8), kPatWarps * 32, 0, st>>>(
-      n_dof, mode, adj_ptr, adj, c2d, ldof, row_cnt, indptr, indices, ovf, ovf_len);
+      n_dof, mode, adj_ptr, adj, c2d, ldof, row_cnt, indptr, indices, ovf, ovf_len, nullptr);
   cudaFuncSetAttribute(pattern_pass2, cudaFuncAttributeMaxDynamicSharedMemorySize, kPatBigCap * 4);
   pattern_pass2<<<kNumSMs, 32, kPatBigCap * 4, st>>>(mode, adj_ptr, adj, c2d, ldof, row_cnt, indptr, indices, ovf,
                                                      ovf_len, status);
@@ -510,6 +564,49 @@ int32_t fgb_pattern_fill(int64_t n_dof, const int64_t* adj_ptr, const int32_t* a
   int32_t* ovf = cv.take<int32_t>(n_dof);
   int32_t* ovf_len = cv.take<int32_t>(1);
   return pattern_launch(1, n_dof, adj_ptr, adj, cell2dof, ldof, nullptr, indptr, indices, ovf, ovf_len, status, st);
+}
+
+int32_t fgb_pattern_build(int64_t n_dof, const int64_t* adj_ptr, const int32_t* adj, const int32_t* cell2dof,
+                          int32_t ldof, int64_t n_adj, int64_t* indptr, int32_t* stage, size_t stage_bytes,
+                          int32_t* status, void* workspace, size_t workspace_bytes, void* stream) {
+  if (n_dof <= 0 || ldof <= 0 || n_adj <= 0 || !adj_ptr || !adj || !cell2dof || !indptr || !stage) return FGB_ERR_ARG;
+  if (stage_bytes < static_cast<size_t>(n_adj) * ldof * sizeof(int32_t)) return FGB_ERR_WORKSPACE;
+  if (workspace == nullptr || workspace_bytes < fgb_pattern_workspace_bytes(n_dof)) return FGB_ERR_WORKSPACE;
+  cudaStream_t st = as_stream(stream);
+  Carver cv(workspace, workspace_bytes);
+  int32_t* cnt = cv.take<int32_t>(n_dof);
+  int32_t* ovf = cv.take<int32_t>(n_dof);
+  int32_t* ovf_len = cv.take<int32_t>(1);
+  void* scan_ws = cv.base + cv.off;
+  size_t scan_bytes = workspace_bytes - cv.off;
+  cudaMemsetAsync(ovf_len, 0, sizeof(int32_t), st);
+  pattern_pass1<<<grid_for(n_dof * 32, kPatWarps * 32, kNumSMs * 8), kPatWarps * 32, 0, st>>>(
+      n_dof, 2, adj_ptr, adj, cell2dof, ldof, cnt, nullptr, nullptr, ovf, ovf_len, stage);
+  cudaFuncSetAttribute(pattern_pass2, cudaFuncAttributeMaxDynamicSharedMemorySize, kPatBigCap * 4);
+  pattern_pass2<<<kNumSMs, 32, kPatBigCap * 4, st>>>(0, adj_ptr, adj, cell2dof, ldof, cnt, nullptr, nullptr, ovf,
+                                                     ovf_len, status);
+  const int rc = launch_status();
+  if (rc != FGB_OK) return rc;
+  return exclusive_scan_i32_to_i64(cnt, n_dof, indptr, scan_ws, scan_bytes, st);
+}
+
+int32_t fgb_pattern_compact(int64_t n_dof, const int64_t* adj_ptr, const int32_t* adj, const int32_t* cell2dof,
+                            int32_t ldof, const int64_t* indptr, const int32_t* stage, int32_t* indices,
+                            int32_t* status, void* workspace, size_t workspace_bytes, void* stream) {
+  if (n_dof <= 0 || ldof <= 0 || !adj_ptr || !adj || !cell2dof || !indptr || !stage || !indices) return FGB_ERR_ARG;
+  if (workspace == nullptr || workspace_bytes < fgb_pattern_workspace_bytes(n_dof)) return FGB_ERR_WORKSPACE;
+  cudaStream_t st = as_stream(stream);
+  Carver cv(workspace, workspace_bytes);
+  cv.take<int32_t>(n_dof);
+  int32_t* ovf = cv.take<int32_t>(n_dof);
+  int32_t* ovf_len = cv.take<int32_t>(1);
+  pattern_compact<<<grid_for(n_dof * 32, 256, kNumSMs * 16), 256, 0, st>>>(n_dof, adj_ptr, ldof, indptr, stage,
+                                                                          indices);
+  // rows that did not fit the hash pass (listed by fgb_pattern_build in the same workspace)
+  cudaFuncSetAttribute(pattern_pass2, cudaFuncAttributeMaxDynamicSharedMemorySize, kPatBigCap * 4);
+  pattern_pass2<<<kNumSMs, 32, kPatBigCap * 4, st>>>(1, adj_ptr, adj, cell2dof, ldof, nullptr, indptr, indices, ovf,
+                                                     ovf_len, status);
+  return launch_status();
 }
 
 int32_t fgb_pattern_expand_blocks(int64_t n_node, int32_t bs, int32_t dof_priority, const int64_t* indptr,

@@ -72,13 +72,17 @@ def build_pattern(adj_ptr, adj, c2d, n_dof: int, status: torch.Tensor):
     lib = _lib.lib()
     ws = workspace(lib.fgb_pattern_workspace_bytes(n_dof), dev)
     indptr = torch.empty(n_dof + 1, dtype=torch.int64, device=dev)
-    call("fgb_pattern_count", n_dof, ptr(adj_ptr), ptr(adj), ptr(c2d), ldof, ptr(indptr), ptr(status), ptr(ws),
-         ws.numel(), stream_ptr(dev))
+    n_adj = int(adj.numel())
+    # one hashed pass that stages every sorted row (n_adj * ldof int32 of
+    # scratch), then a copy into the exact-size indices
+    stage = torch.empty(max(n_adj * ldof, 1), dtype=torch.int32, device=dev)
+    call("fgb_pattern_build", n_dof, ptr(adj_ptr), ptr(adj), ptr(c2d), ldof, n_adj, ptr(indptr), ptr(stage),
+         stage.numel() * 4, ptr(status), ptr(ws), ws.numel(), stream_ptr(dev))
     nnz = int(indptr[n_dof].item())
-    check_status_word("fgb_pattern_count", status)
+    check_status_word("fgb_pattern_build", status)
     indices = torch.empty(max(nnz, 1), dtype=torch.int32, device=dev)
-    call("fgb_pattern_fill", n_dof, ptr(adj_ptr), ptr(adj), ptr(c2d), ldof, ptr(indptr), ptr(indices), ptr(status),
-         ptr(ws), ws.numel(), stream_ptr(dev))
+    call("fgb_pattern_compact", n_dof, ptr(adj_ptr), ptr(adj), ptr(c2d), ldof, ptr(indptr), ptr(stage),
+         ptr(indices), ptr(status), ptr(ws), ws.numel(), stream_ptr(dev))
     return indptr, indices[:nnz]
 
 

@@ -122,6 +122,21 @@ int32_t fgb_pattern_fill(int64_t n_dof, const int64_t* adj_ptr, const int32_t* a
                          int32_t* indices, int32_t* status, void* workspace,
                          size_t workspace_bytes, void* stream);
 
+/* The same pattern in one pass over the rows: build hashes and sorts every
+ * row once, staging it at stage[adj_ptr[i] * ldof] (stage: n_adj * ldof
+ * int32, n_adj = adj_ptr[n_dof]), and writes indptr; compact then copies the
+ * staged rows into indices (after the caller has read nnz = indptr[n_dof]).
+ * Both take the same workspace, which carries the list of rows too long for
+ * the hash pass from build to compact. */
+int32_t fgb_pattern_build(int64_t n_dof, const int64_t* adj_ptr, const int32_t* adj,
+                          const int32_t* cell2dof, int32_t ldof, int64_t n_adj, int64_t* indptr,
+                          int32_t* stage, size_t stage_bytes, int32_t* status, void* workspace,
+                          size_t workspace_bytes, void* stream);
+int32_t fgb_pattern_compact(int64_t n_dof, const int64_t* adj_ptr, const int32_t* adj,
+                            const int32_t* cell2dof, int32_t ldof, const int64_t* indptr,
+                            const int32_t* stage, int32_t* indices, int32_t* status,
+                            void* workspace, size_t workspace_bytes, void* stream);
+
 /* Block expansion of a scalar pattern for vector spaces: bs components per
  * node; interleaved (3*node+comp, TensorFunctionSpace(space,(-1,GD)),
  * fealpy/functionspace/tensor_space.py:29-31) when dof_priority == 0, else
