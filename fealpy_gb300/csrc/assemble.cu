@@ -112,13 +112,16 @@ struct RowSmem {
   int ncopy;   // independent accumulator copies per warp
 };
 
-template <typename T>
+// LDOF > 0: the local dof count as a compile-time constant (divisions by it
+// become multiply-shifts); LDOF == 0: taken from `ldof_rt`.
+template <typename T, int LDOF>
 __device__ bool assemble_scalar_row(int64_t i, const int64_t* __restrict__ adj_ptr, const int32_t* __restrict__ adj,
-                                    const int32_t* __restrict__ c2d, int ldof, int nt, const T* __restrict__ tab,
+                                    const int32_t* __restrict__ c2d, int ldof_rt, int nt, const T* __restrict__ tab,
                                     const T* __restrict__ factors, const int64_t* __restrict__ indptr,
                                     const int32_t* __restrict__ indices, T* __restrict__ values,
                                     float* __restrict__ values32, int32_t* cols, T* acc, int cap, int ncopy,
                                     int32_t* status) {
+  const int ldof = LDOF > 0 ? LDOF : ldof_rt;
   const int lane = threadIdx.x & 31;
   const int64_t base = indptr[i];
   const int L = static_cast<int>(indptr[i + 1] - base);
@@ -158,7 +161,7 @@ __device__ bool assemble_scalar_row(int64_t i, const int64_t* __restrict__ adj_p
 }
 
 // Dynamic shared memory layout: tables (nt*ldof*ldof T) | per warp: acc (ncopy*cap T) | cols (cap int32)
-template <typename T>
+template <typename T, int LDOF>
 __global__ void assemble_scalar_kernel(int64_t n_rows, const int32_t* __restrict__ row_list,
                                        const int32_t* __restrict__ row_list_len, const int64_t* __restrict__ adj_ptr,
                                        const int32_t* __restrict__ adj, const int32_t* __restrict__ c2d, int ldof,
@@ -181,8 +184,8 @@ __global__ void assemble_scalar_kernel(int64_t n_rows, const int32_t* __restrict
   const int64_t nwarps = static_cast<int64_t>(gridDim.x) * wpb;
   for (int64_t r = warp; r < n; r += nwarps) {
     const int64_t i = row_list ? row_list[r] : r;
-    bool done = assemble_scalar_row<T>(i, adj_ptr, adj, c2d, ldof, nt, tab, factors, indptr, indices, values, values32,
-                                       cols, acc, cap, ncopy, status);
+    bool done = assemble_scalar_row<T, LDOF>(i, adj_ptr, adj, c2d, ldof, nt, tab, factors, indptr, indices, values,
+                                             values32, cols, acc, cap, ncopy, status);
     if (!done && lane == 0) {
       if (ovf) { int slot = atomicAdd(ovf_len, 1); ovf[slot] = static_cast<int32_t>(i); }
       else set_status(status, FGB_ERR_CAPACITY);
@@ -334,16 +337,21 @@ int launch_scalar(int64_t n_dof, const int64_t* adj_ptr, const int32_t* adj, con
   const size_t per_warp2 = align_up(static_cast<size_t>(kAsmBigCap) * sizeof(T) + kAsmBigCap * 4, 16);
   const size_t smem2 = tab_bytes + per_warp2;
   if (smem1 > kMaxDynSmem || smem2 > kMaxDynSmem) return FGB_ERR_CAPACITY;
-  cudaFuncSetAttribute(assemble_scalar_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       static_cast<int>(smem2 > smem1 ? smem2 : smem1));
+  auto kern = assemble_scalar_kernel<T, 0>;
+  switch (ldof) {
+    case 3: kern = assemble_scalar_kernel<T, 3>; break;
+    case 4: kern = assemble_scalar_kernel<T, 4>; break;
+    case 6: kern = assemble_scalar_kernel<T, 6>; break;
+    case 10: kern = assemble_scalar_kernel<T, 10>; break;
+    default: break;
+  }
+  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem2 > smem1 ? smem2 : smem1));
   cudaMemsetAsync(ovf_len, 0, sizeof(int32_t), st);
   const int grid1 = grid_for(n_dof, kAsmWarps, kNumSMs * 16);
-  assemble_scalar_kernel<T><<<grid1, kAsmWarps * 32, smem1, st>>>(n_dof, nullptr, nullptr, adj_ptr, adj, c2d, ldof, nt,
-                                                                  tables, factors, indptr, indices, values, values32,
-                                                                  kAsmCap, ncopy, ovf, ovf_len, status);
-  assemble_scalar_kernel<T><<<kNumSMs, 32, smem2, st>>>(n_dof, ovf, ovf_len, adj_ptr, adj, c2d, ldof, nt, tables,
-                                                        factors, indptr, indices, values, values32, kAsmBigCap, 1,
-                                                        nullptr, nullptr, status);
+  kern<<<grid1, kAsmWarps * 32, smem1, st>>>(n_dof, nullptr, nullptr, adj_ptr, adj, c2d, ldof, nt, tables, factors,
+                                             indptr, indices, values, values32, kAsmCap, ncopy, ovf, ovf_len, status);
+  kern<<<kNumSMs, 32, smem2, st>>>(n_dof, ovf, ovf_len, adj_ptr, adj, c2d, ldof, nt, tables, factors, indptr, indices,
+                                   values, values32, kAsmBigCap, 1, nullptr, nullptr, status);
   return launch_status();
 }
 
