@@ -482,6 +482,26 @@ def batched_step(torch, F, probs, dtype, bs_kw, marks=None):
     return res, systems, bs
 
 
+def cpu_sample_batched(meshes, budget_s=15.0, max_dofs=80000):
+    """The oracle port of the reference numpy path, one mesh after another
+    (the reference has no batched solve), on the smallest meshes of the
+    batch until about ``budget_s`` of host time: DOF/s of that sample."""
+    from oracle import fem_oracle as O
+    order = sorted(range(len(meshes)), key=lambda k: (meshes[k]["p"] * meshes[k]["nx"]) ** 2)
+    dofs, t, used = 0, 0.0, 0
+    for k in order:
+        m = meshes[k]
+        if (m["p"] * m["nx"] + 1) ** 2 > max_dofs or t > budget_s:
+            break
+        t0 = time.perf_counter()
+        out = O.poisson_pipeline(m["node"], m["cell"], m["p"], kappa=m["kappa"], q=m["p"] + 3, rtol=RTOL)
+        t += time.perf_counter() - t0
+        dofs += out["n"]
+        used += 1
+    return {"value": dofs / t if t > 0 else None, "unit": "DOF/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": f"{used} smallest meshes of the batch solved one after another ({dofs} dofs, {t:.1f} s)"}
+
+
 def run_batched(args):
     import torch
     import fealpy_gb300 as F
@@ -547,7 +567,8 @@ def run_batched(args):
             "fp64_continuations": bs.fallbacks,
             "fp64_iterations": sum(getattr(res[k], "fp64_iterations", 0) for k in res),
             "max_true_relres": max(rel), "iters_max": max(iters), "iters_mean": sum(iters) / len(iters),
-            "max_rel_err_vs_fp64_sample": max(err), "gpu_launches": (_lib.launch_count() - l0) // args.steps}
+            "max_rel_err_vs_fp64_sample": max(err), "gpu_launches": (_lib.launch_count() - l0) // args.steps,
+            "cpu_baseline": None if args.no_cpu_baseline else cpu_sample_batched(meshes)}
     print(json.dumps(line), flush=True)
 
 
@@ -640,6 +661,35 @@ def serving_sample(torch, dev, count, rate=200.0):
     return out
 
 
+def cpu_sample_serving(reqs, budget_s=15.0, max_dofs=60000):
+    """Sequential FIFO replay of the stream's smallest requests with the oracle
+    port of the reference numpy path (one solve after another, no overlap):
+    DOF/s and seconds per request of that sample."""
+    from oracle import fem_oracle as O
+    from fealpy_gb300.workloads import tri_box_arrays, tet_box_arrays, jitter_interior
+    small = sorted((r for r in reqs if r["dofs"] <= max_dofs), key=lambda r: r["t"])
+    dofs, t, used = 0, 0.0, 0
+    for r in small:
+        if t > budget_s:
+            break
+        n = r["n"]
+        if r["kind"] == "tri":
+            node, cell = tri_box_arrays(n, n)
+            node = jitter_interior(node, 1.0 / n, 0.15, seed=r["seed"])
+        else:
+            node, cell = tet_box_arrays(n, n, n)
+            node = jitter_interior(node, 1.0 / n, 0.2, seed=r["seed"])
+        kappa = np.exp(np.random.default_rng(r["seed"]).normal(0.0, 1.0, cell.shape[0]))
+        t0 = time.perf_counter()
+        out = O.poisson_pipeline(node, cell, r["p"], kappa=kappa, q=r["p"] + 2, rtol=RTOL)
+        t += time.perf_counter() - t0
+        dofs += out["n"]
+        used += 1
+    return {"value": dofs / t if t > 0 else None, "unit": "DOF/s", "cores": os.cpu_count(), "kind": "port",
+            "seconds_per_request": t / max(used, 1),
+            "sample": f"{used} requests of <= {max_dofs} dofs replayed one after another ({dofs} dofs, {t:.1f} s)"}
+
+
 def run_serving(args):
     import torch
     from fealpy_gb300.serving import SolveServer, poisson_request_problem
@@ -671,7 +721,9 @@ def run_serving(args):
             "config": {"workload": "70% tri P1/P2, 30% tet P1, 1e3-2e6 dofs log-uniform (C4)",
                        "requests_per_rate": args.serve_count, "hbm_budget_gb": 150, "slots": 256,
                        "chunk_iterations": args.serve_chunk},
-            "sweep": rows}
+            "sweep": rows,
+            "cpu_baseline": None if args.no_cpu_baseline else cpu_sample_serving(
+                serving_requests(args.serve_count, rate=50.0, seed=3))}
     print(json.dumps(line), flush=True)
 
 
