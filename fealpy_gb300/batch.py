@@ -16,7 +16,6 @@ mix gives the same bits.
 import ctypes
 from typing import Dict, List, Optional
 
-import numpy as np
 import torch
 
 from . import _lib

@@ -16,7 +16,7 @@ arrival time; p50/p99 over all requests and the throughput (requests/s over
 the whole stream) are reported by :meth:`SolveServer.run`.
 """
 import time
-from typing import Callable, Dict, List, Optional
+from typing import Callable, Dict, List
 
 import numpy as np
 import torch
