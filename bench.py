@@ -457,7 +457,7 @@ def batched_setup(torch, F, meshes, dev):
     return probs
 
 
-def batched_step(torch, F, probs, dtype, bs_kw, marks=None):
+def batched_step(torch, F, probs, dtype, bs_kw, marks=None, fp64=False):
     """Assemble every problem (diffusion with the checkerboard coefficient,
     quadrature p + 3, f = 1, u = 0) and solve all of them in one batch."""
     from fealpy_gb300.fem import BilinearForm, LinearForm, ScalarDiffusionIntegrator, ScalarSourceIntegrator
@@ -472,7 +472,7 @@ def batched_step(torch, F, probs, dtype, bs_kw, marks=None):
         lf = LinearForm(space)
         lf.add_integrator(ScalarSourceIntegrator(1.0, q=p + 3))
         A2, F2 = bc.apply(A, lf.assembly())
-        bs.add(A2, F2, rtol=RTOL, maxit=BATCH_MAXIT, key=k)
+        bs.add(A2, F2, rtol=RTOL, maxit=BATCH_MAXIT, key=k, fp64=fp64)
         systems.append((A2, F2))
     if marks is not None:
         e = torch.cuda.Event(enable_timing=True)
@@ -532,7 +532,7 @@ def run_batched(args):
     marks = []
     e0.record()
     for _ in range(args.steps):
-        res, systems, bs = batched_step(torch, F, probs, asm_dtype, kw, marks)
+        res, systems, bs = batched_step(torch, F, probs, asm_dtype, kw, marks, fp64=args.batch_precision == "fp64")
     e1.record()
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / args.steps
@@ -561,6 +561,7 @@ def run_batched(args):
             "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
             "data": "synthetic (seeded meshes, checkerboard coefficients)",
             "config": {"workload": f"{len(probs)} TriangleMesh boxes nx log-uniform [16,512], p in {{1,2,3}} (C3)",
+                       "iterations": args.batch_precision,
                        "gdof": gdof, "rtol": RTOL, "autotune_us": {f"{a}x{b}": t for (a, b), t in times.items()},
                        "slices_per_tile": spt, "slice_threads": thr},
             "solve_ms": solve_ms, "assembly_ms": ms - solve_ms, "graph": bs.used_graph,
@@ -746,6 +747,8 @@ def main():
                          "serving: the request stream; elasticity: P1 vector elasticity on a tet box")
     ap.add_argument("--elast-n", type=int, default=128)
     ap.add_argument("--batch-count", type=int, default=256)
+    ap.add_argument("--batch-precision", choices=["mixed", "fp64"], default="mixed",
+                    help="iterations of the batched solve: FP32 with FP64 refinement (default) or plain FP64")
     ap.add_argument("--serve-count", type=int, default=200, help="requests per arrival rate")
     ap.add_argument("--serve-rates", default="50,200,1000")
     ap.add_argument("--serve-chunk", type=int, default=64)
