@@ -208,8 +208,12 @@ __global__ void batch_control(int32_t n_sys, fgb_batch_state* st, const int32_t*
           } else {
             const long long gap = S.niter - S.last_upd;
             const long long slack = S.max_gap / 2 > 100 ? S.max_gap / 2 : 100;
-            // before any residual-triggered update: a first check after 1000 iterations
-            const bool plateau = !sys[s].fp64 && (S.max_gap > 0 ? gap > S.max_gap + slack : gap > 1000);
+            // before any residual-triggered update: a first check after 1000
+            // iterations; FP64 systems (no residual-triggered updates) are checked
+            // every 5000 iterations, so a residual that stalls above rtol ends
+            // after three checks instead of at the iteration limit
+            const bool plateau = sys[s].fp64 ? gap > 5000
+                                             : (S.max_gap > 0 ? gap > S.max_gap + slack : gap > 1000);
             // FP64 systems run plain FP64 PCG: the true residual is formed only
             // to confirm convergence (or at the iteration limit)
             const bool due = (!sys[s].fp64 && res < S.delta * S.r_upd) || (res < S.tol) || (S.niter >= S.maxit);
