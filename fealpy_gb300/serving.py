@@ -40,10 +40,27 @@ def resident_estimate(n: int, nnz: int, fp64: bool) -> int:
 def poisson_request_problem(req: dict, device, dtype=torch.float64):
     """Build the system of one serving request on the device: a jittered
     TriangleMesh box (P1/P2) or TetrahedronMesh box (P1), lognormal(0, 1)
-    per-cell coefficient, f = 1, u = 0 on the boundary.  Returns (A, b)."""
+    per-cell coefficient, f = 1, u = 0 on the boundary; or, for kind
+    'elast', P1 vector elasticity on a tetrahedral box (lambda = 1, mu = 0.5
+    scaled per cell by a lognormal(0, 0.5) factor, clamped at x = 0, body
+    force (0, 0, -1)).  Returns (A, b)."""
     from . import TriangleMesh, TetrahedronMesh, LagrangeFESpace
     from .fem import BilinearForm, LinearForm, ScalarDiffusionIntegrator, ScalarSourceIntegrator, DirichletBC
     g = torch.Generator(device="cpu").manual_seed(int(req["seed"]))
+    if req["kind"] == "elast":
+        from . import TensorFunctionSpace, LinearElasticMaterial
+        from .fem import LinearElasticityIntegrator, VectorSourceIntegrator
+        n = int(req["n"])
+        mesh = TetrahedronMesh.from_box([0, 1, 0, 1, 0, 1], n, n, n, device=device)
+        scale = torch.exp(0.5 * torch.randn(mesh.number_of_cells(), generator=g, dtype=torch.float64)).to(device)
+        ts = TensorFunctionSpace(LagrangeFESpace(mesh, 1), (-1, 3))
+        mat = LinearElasticMaterial("m", lame_lambda=1.0, shear_modulus=0.5, cell_scale=scale)
+        bf = BilinearForm(ts)
+        bf.add_integrator(LinearElasticityIntegrator(mat, q=4))
+        lf = LinearForm(ts)
+        lf.add_integrator(VectorSourceIntegrator(source=[0.0, 0.0, -1.0], q=4))
+        bc = DirichletBC(ts, gd=0.0, threshold=lambda x: torch.abs(x[..., 0]) < 1e-12)
+        return bc.apply(bf.assembly(dtype=dtype), lf.assembly())
     n, p = int(req["n"]), int(req["p"])
     if req["kind"] == "tri":
         mesh = TriangleMesh.from_box([0, 1, 0, 1], n, n, device=device)

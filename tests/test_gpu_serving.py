@@ -18,8 +18,11 @@ def cuda():
 def _stream():
     from fealpy_gb300.workloads import serving_requests
     # a short stream of small requests at a high arrival rate, so that many
-    # arrive while others are still iterating
-    return serving_requests(24, rate=400.0, seed=11, dof_range=(3e2, 2e4))
+    # arrive while others are still iterating; two of them elasticity solves
+    reqs = serving_requests(24, rate=400.0, seed=11, dof_range=(3e2, 2e4))
+    for k, n in ((5, 6), (13, 8)):
+        reqs[k].update({"kind": "elast", "n": n, "p": 1, "dofs": 3 * (n + 1) ** 3})
+    return reqs
 
 
 def test_serving_mix_equals_solo_and_converges():
