@@ -16,6 +16,7 @@ mix gives the same bits.
 import ctypes
 from typing import Dict, List, Optional
 
+import numpy as np
 import torch
 
 from . import _lib
@@ -43,6 +44,7 @@ class _Slot:
         self.rtol, self.maxit, self.fp64, self.A = rtol, maxit, fp64, A
         self.admitted = False
         self.iters_before = 0  # FP32 iterations spent before an FP64 continuation
+        self.tiles = None      # cached (slice tile bounds, row tile bounds)
 
 
 class BatchSolver:
@@ -129,28 +131,38 @@ class BatchSolver:
         return slot
 
     # ------------------------------------------------------------ tables
-    def _tiles(self, sizes, per_tile, attr):
-        """Tiles of each system: ``per_tile`` slices (rows), widened so that a
-        system has at most ``max_tiles_per_system`` tiles (its per-system
-        sums stay short); depends on the system's own size only."""
-        tiles, ptr_ = [], [0]
-        for s, lim in enumerate(sizes):
-            step = max(per_tile, -(-lim // self.max_tiles_per_system))
-            for a in range(0, lim, step):
-                tiles.append((s, a, min(a + step, lim), 0))
-            ptr_.append(len(tiles))
-        return tiles, ptr_
+    def _tile_bounds(self, lim, per_tile):
+        """(begin, end) of one system's tiles: ``per_tile`` slices (rows),
+        widened so that the system has at most ``max_tiles_per_system`` tiles
+        (its per-system sums stay short).  Depends on the system only."""
+        step = max(per_tile, -(-lim // self.max_tiles_per_system))
+        b = np.arange(0, lim, step, dtype=np.int32)
+        return np.stack([b, np.minimum(b + step, lim).astype(np.int32)], axis=1)
+
+    def _tiles(self, parts):
+        """Tile array (sys, begin, end, 0) int32 and tile pointers of the
+        table from each slot's cached bounds (None for an empty slot)."""
+        rows, ptr_ = [], [0]
+        for s, bnd in enumerate(parts):
+            if bnd is not None and len(bnd):
+                t = np.zeros((len(bnd), 4), dtype=np.int32)
+                t[:, 0] = s
+                t[:, 1:3] = bnd
+                rows.append(t)
+            ptr_.append(ptr_[-1] + (0 if bnd is None else len(bnd)))
+        tiles = np.ascontiguousarray(np.concatenate(rows) if rows else np.zeros((1, 4), dtype=np.int32))
+        return tiles, np.asarray(ptr_, dtype=np.int32), ptr_[-1]
 
     def _sync_tables(self):
         used = [i for i, s in enumerate(self._slots) if s is not None]
         n_sys = (max(used) + 1) if used else 0
         systems = (_lib.BatchSystem * max(n_sys, 1))()
-        slice_sizes, row_sizes = [], []
+        slice_parts, row_parts = [], []
         for i in range(n_sys):
             sl = self._slots[i]
             if sl is None:
-                slice_sizes.append(0)
-                row_sizes.append(0)
+                slice_parts.append(None)
+                row_parts.append(None)
                 continue
             S, v = sl.S, sl.vecs
             d = systems[i]
@@ -161,18 +173,18 @@ class BatchSolver:
             d.fp64 = 1 if sl.fp64 else 0
             d.dinv64, d.b, d.x = sl.dinv64.data_ptr(), sl.b.data_ptr(), sl.x.data_ptr()
             d.r, d.z, d.p0, d.p1, d.Ap, d.y, d.dinv32 = (v[k].data_ptr() for k in range(7))
-            slice_sizes.append(S.n_slices)
-            row_sizes.append(S.n)
-        st, sp = self._tiles(slice_sizes, self.slices_per_tile, "slices")
-        vt, vp = self._tiles(row_sizes, self.rows_per_tile, "rows")
-        if len(st) > self.max_slice_tiles or len(vt) > self.max_row_tiles:
+            if sl.tiles is None:
+                sl.tiles = (self._tile_bounds(S.n_slices, self.slices_per_tile),
+                            self._tile_bounds(S.n, self.rows_per_tile))
+            slice_parts.append(sl.tiles[0])
+            row_parts.append(sl.tiles[1])
+        sta, spa, nst = self._tiles(slice_parts)
+        vta, vpa, nvt = self._tiles(row_parts)
+        if nst > self.max_slice_tiles or nvt > self.max_row_tiles:
             raise RuntimeError("batch tile capacity exceeded: raise max_slice_tiles / max_row_tiles")
-        sta = (_lib.BatchTile * max(len(st), 1))(*[_lib.BatchTile(*t) for t in st])
-        vta = (_lib.BatchTile * max(len(vt), 1))(*[_lib.BatchTile(*t) for t in vt])
-        spa = (ctypes.c_int32 * (n_sys + 1))(*sp)
-        vpa = (ctypes.c_int32 * (n_sys + 1))(*vp)
-        call("fgb_batch_set", self._h, n_sys, systems, len(st), sta, spa, len(vt), vta, vpa,
-             stream_ptr(self.device))
+        vp_ = ctypes.c_void_p
+        call("fgb_batch_set", self._h, n_sys, systems, nst, vp_(sta.ctypes.data), vp_(spa.ctypes.data), nvt,
+             vp_(vta.ctypes.data), vp_(vpa.ctypes.data), stream_ptr(self.device))
         self._n_table = n_sys
         self._dirty = False
 
