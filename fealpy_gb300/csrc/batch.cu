@@ -382,8 +382,8 @@ __global__ void __launch_bounds__(1024, 1) batch_reliable(const fgb_batch_system
 }
 
 // Systems with an update due or admitted: true residual test, beta from the
-// replaced residual.  An FP32 system whose true residual has not halved over
-// two consecutive checks stops as FGB_PCG_STAGNATED (its condition number is
+// replaced residual.  An FP32 system whose true residual has not halved since
+// the previous check stops as FGB_PCG_STAGNATED (its condition number is
 // beyond what FP32 iterations resolve); the caller continues it in FP64.
 __global__ void batch_reliable_fin(int32_t n_sys, fgb_batch_state* st, const int32_t* __restrict__ tile_ptr,
                                    const double* __restrict__ rpart, const fgb_batch_system* __restrict__ sys) {
@@ -418,7 +418,7 @@ __global__ void batch_reliable_fin(int32_t n_sys, fgb_batch_state* st, const int
   if (!isfinite(nrm)) S.done = FGB_PCG_NONFINITE;
   else if (nrm <= S.tol) S.done = FGB_PCG_RTOL;
   else if (S.niter >= S.maxit) S.done = FGB_PCG_MAXIT;
-  else if (S.stall >= (sys[s].fp64 ? 3 : 2)) S.done = FGB_PCG_STAGNATED;  // FP64: attainable accuracy
+  else if (S.stall >= (sys[s].fp64 ? 3 : 1)) S.done = FGB_PCG_STAGNATED;  // FP64: attainable accuracy
   S.beta = mode == 2 ? 0.0 : rz / S.rz_prev;
   S.rz = rz;
   S.rr = rr;

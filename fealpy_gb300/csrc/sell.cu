@@ -537,7 +537,7 @@ __global__ void __launch_bounds__(1024, 1) sell_mixed_reliable(SellView A, const
     if (!isfinite(nrm)) st->done = FGB_PCG_NONFINITE;
     else if (nrm <= st->tol) st->done = FGB_PCG_RTOL;
     else if (st->niter >= st->maxit) st->done = FGB_PCG_MAXIT;
-    else if (st->stall >= 2) st->done = FGB_PCG_STAGNATED;  // the caller continues in FP64
+    else if (st->stall >= 1) st->done = FGB_PCG_STAGNATED;  // the caller continues in FP64
     st->beta = first ? 0.0 : trz / st->rz_prev;
     st->rz = trz;
     st->rr = trr;
