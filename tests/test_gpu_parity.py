@@ -383,3 +383,37 @@ def test_sell_launch_shapes_and_autotune(golden_dir):
         S.set_launch(*shape)
         xs, info = F.cg_mixed(A, b, rtol=1e-10, returninfo=True)
         assert info["relres"] <= 1e-10 and rel_err(xs, z["uh"]) < 1e-8, (shape, info)
+
+
+def test_elasticity_fp32_assembly_and_refined_solve(golden_dir):
+    """P1 elasticity assembled in FP32 (factors from FP64 geometry): the
+    pattern equals the FP64 one bit for bit, values within FP32 rounding, and
+    the FP32-refined solve of it meets 1e-10 on that operator."""
+    dev = cuda()
+    import fealpy_gb300 as F
+    from fealpy_gb300.fem import BilinearForm, LinearForm, LinearElasticityIntegrator, VectorSourceIntegrator
+    from fealpy_gb300.fem import DirichletBC
+    z = load(golden_dir, "small_elasticity_tet_p1.npz")
+    mesh = F.TetrahedronMesh(torch.as_tensor(z["node"], device=dev),
+                             torch.as_tensor(z["cell"], dtype=torch.int32, device=dev))
+    ts = F.TensorFunctionSpace(F.LagrangeFESpace(mesh, 1), (-1, 3))
+    mat = F.LinearElasticMaterial("m", lame_lambda=1.0, shear_modulus=0.5,
+                                  cell_scale=torch.as_tensor(z["scale"], device=dev))
+    out = {}
+    for dt in (torch.float64, torch.float32):
+        bf = BilinearForm(ts)
+        bf.add_integrator(LinearElasticityIntegrator(mat, q=4))
+        out[dt] = bf.assembly(dtype=dt)
+    A64, A32 = out[torch.float64], out[torch.float32]
+    assert A32.values.dtype == torch.float32
+    assert torch.equal(A64.crow, A32.crow) and torch.equal(A64.col, A32.col)
+    assert rel_err(A32.values.double(), A64.values.cpu().numpy()) < 1e-6
+    lf = LinearForm(ts)
+    lf.add_integrator(VectorSourceIntegrator(source=[0.0, 0.0, -1.0], q=4))
+    bc = DirichletBC(ts, gd=0.0, threshold=lambda x: torch.abs(x[..., 0]) < 1e-12)
+    B, f = bc.apply(A32, lf.assembly())
+    x, info = F.cg_mixed(B, f, rtol=1e-10, returninfo=True)
+    Bd = F.CSRTensor(B.crow, B.col, B.values.double(), B.shape)
+    rel = float(torch.linalg.norm(f.double() - Bd @ x) / torch.linalg.norm(f.double()))
+    assert info["reason"] == 2 and rel <= 1e-10 * 1.0001, (info, rel)
+    assert rel_err(x, z["uh"]) < 1e-4
