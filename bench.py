@@ -457,7 +457,7 @@ def batched_setup(torch, F, meshes, dev):
     return probs
 
 
-def batched_step(torch, F, probs, dtype, bs_kw, marks=None, fp64=False):
+def batched_step(torch, F, probs, dtype, bs_kw, marks=None, fp64=False, graph=True):
     """Assemble every problem (diffusion with the checkerboard coefficient,
     quadrature p + 3, f = 1, u = 0) and solve all of them in one batch."""
     from fealpy_gb300.fem import BilinearForm, LinearForm, ScalarDiffusionIntegrator, ScalarSourceIntegrator
@@ -478,7 +478,7 @@ def batched_step(torch, F, probs, dtype, bs_kw, marks=None, fp64=False):
         e = torch.cuda.Event(enable_timing=True)
         e.record()
         marks.append(e)
-    res = bs.solve_all()
+    res = bs.solve_all(graph=graph)
     return res, systems, bs
 
 
@@ -531,9 +531,12 @@ def run_batched(args):
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     marks = []
     e0.record()
+    torch.cuda.nvtx.range_push("timed_batched")
     for _ in range(args.steps):
-        res, systems, bs = batched_step(torch, F, probs, asm_dtype, kw, marks, fp64=args.batch_precision == "fp64")
+        res, systems, bs = batched_step(torch, F, probs, asm_dtype, kw, marks, fp64=args.batch_precision == "fp64",
+                                        graph=not args.no_graph)
     e1.record()
+    torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / args.steps
     solve_ms = marks[-1].elapsed_time(e1)
