@@ -54,8 +54,8 @@ class BatchSolver:
     split of the batched kernels (see :func:`autotune`)."""
 
     def __init__(self, max_systems: int = 256, *, max_slice_tiles: int = 1 << 16, max_row_tiles: int = 1 << 16,
-                 slices_per_tile: int = 16, rows_per_tile: int = 4096, slice_threads: int = 256,
-                 max_tiles_per_system: int = 256, delta: float = 0.1, device=None):
+                 slices_per_tile: int = 8, rows_per_tile: int = 1024, slice_threads: int = 256,
+                 max_tiles_per_system: int = 16384, delta: float = 0.1, device=None):
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         self.max_systems = int(max_systems)
         self.max_slice_tiles, self.max_row_tiles = int(max_slice_tiles), int(max_row_tiles)
@@ -275,7 +275,7 @@ class BatchSolver:
         return 1000.0 * e0.elapsed_time(e1) / reps
 
 
-def autotune(systems, candidates=((8, 128), (16, 256), (32, 256), (64, 512), (16, 512), (128, 1024)),
+def autotune(systems, candidates=((4, 256), (8, 256), (16, 256), (8, 512), (16, 512), (8, 1024)),
              device=None, **kw) -> Dict[tuple, float]:
     """Choose (slices per tile, threads per block) of the batched slice
     kernels by timing the batched SpMV of ``systems`` (a list of (A, b)) for

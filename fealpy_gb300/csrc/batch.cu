@@ -1,6 +1,9 @@
 // Batched FP32-refined Jacobi-PCG: many independent systems (each with its own
 // SELL-32x4 copy and Krylov vectors) iterate together.  One iteration is four
-// kernels over tile lists plus a reliable-update branch:
+// kernels over tile lists plus a reliable-update branch.  A tile (a few slices
+// or ~1000 rows of one system) is processed by one warp, which takes the next
+// tile with an atomic ticket: no block barriers in the tile loops, and the
+// load balances itself however uneven the systems are.
 //
 //   slice tiles: Ap = A p_new with p_new = z + beta p_old formed per gathered
 //                column; per-tile partials of p.Ap
@@ -35,19 +38,32 @@ struct BatchCtl {
   int any_update, running;
   int any_acc, running_acc;  // accumulated over the blocks of batch_control
   unsigned int arrived;
+  // tile tickets of the tile kernels (SpMV, update, fold, reliable): each warp
+  // takes the next tile with one atomic; the kernel that follows in stream
+  // order puts the ticket back to 0
+  unsigned int ticket[4];
   int pad;
 };
 
-// Per-system sums of tile partials: one warp per system, lanes take every
-// 32nd tile and the warp adds them in a fixed tree, so the result does not
-// depend on timing.  `stride` partials per tile, component `c`.
-__device__ __forceinline__ double tile_sum(const double* __restrict__ part, int t0, int t1, int stride, int c) {
-  double v = 0.0;
-  for (int t = t0 + (threadIdx.x & 31); t < t1; t += 32) v += part[stride * t + c];
-  return warp_sum(v);
+enum { kTicketSpmv = 0, kTicketUpdate = 1, kTicketFold = 2, kTicketReliable = 3 };
+
+// The next tile for the calling warp (all lanes get the same index).
+__device__ __forceinline__ int next_tile(unsigned int* ticket) {
+  unsigned int t = 0;
+  if ((threadIdx.x & 31) == 0) t = atomicAdd(ticket, 1u);
+  return static_cast<int>(__shfl_sync(0xffffffffu, t, 0));
 }
 
-__device__ __forceinline__ int warp_system() { return (blockIdx.x * blockDim.x + threadIdx.x) >> 5; }
+// Per-system sums of tile partials: a block per system; thread k adds tiles
+// k, k + blockDim, ... and the block adds the threads in a fixed tree, so the
+// result does not depend on timing.  Valid in thread 0.  `stride` partials per
+// tile, component `c`.
+__device__ __forceinline__ double tile_sum(const double* __restrict__ part, int t0, int t1, int stride, int c,
+                                           double* red) {
+  double v = 0.0;
+  for (int t = t0 + threadIdx.x; t < t1; t += blockDim.x) v += part[stride * t + c];
+  return block_sum(v, red);
+}
 
 // ---------------------------------------------------------------- kernels
 // Vector type of a system: float (FP32 iterations) or double (fp64 systems).
@@ -62,10 +78,10 @@ template <> struct Vec<double> {
 };
 template <typename T> __device__ __forceinline__ T* vp(void* p) { return static_cast<T*>(p); }
 
-// One slice tile: Ap, p_new = z + beta p_old, and the tile's p.Ap (per thread).
+// One slice tile, one warp: Ap, p_new = z + beta p_old, and the lane's p.Ap.
 template <typename T>
 __device__ double spmv_tile(const fgb_batch_system& A, const fgb_batch_state& S, const fgb_batch_tile& tile) {
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+  const int lane = threadIdx.x & 31;
   const T beta = static_cast<T>(S.beta);
   const T* z = vp<T>(A.z);
   const T* p_old = vp<T>(S.parity ? A.p1 : A.p0);
@@ -73,7 +89,7 @@ __device__ double spmv_tile(const fgb_batch_system& A, const fgb_batch_state& S,
   T* Ap = vp<T>(A.Ap);
   const GatherP<T> g{z, p_old, beta};
   double pap = 0.0;
-  for (int64_t s = tile.begin + wib; s < tile.end; s += wpb) {
+  for (int64_t s = tile.begin; s < tile.end; ++s) {
     const int64_t sbase = A.slice_ptr[s];
     const int w = static_cast<int>((A.slice_ptr[s + 1] - sbase) >> 5);
     const T acc = sell_row(A.col, Vec<T>::val(A), sbase, w, lane, g);
@@ -88,37 +104,39 @@ __device__ double spmv_tile(const fgb_batch_system& A, const fgb_batch_state& S,
   return pap;
 }
 
-// Slice tiles: Ap, p_new and the tile's p.Ap.
+// Slice tiles (a warp each, taken by ticket): Ap, p_new and the tile's p.Ap.
 __global__ void __launch_bounds__(1024, 1) batch_spmv_step(const fgb_batch_system* __restrict__ sys,
                                                            const fgb_batch_state* __restrict__ st,
                                                            const fgb_batch_tile* __restrict__ tiles,
-                                                           const int32_t* __restrict__ n_tiles, double* spart) {
-  __shared__ double red[32];
+                                                           const int32_t* __restrict__ n_tiles, double* spart,
+                                                           BatchCtl* ctl) {
   const int nt = *n_tiles;
-  for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+  while (true) {
+    const int t = next_tile(&ctl->ticket[kTicketSpmv]);
+    if (t >= nt) break;
     const fgb_batch_tile tile = tiles[t];
     const fgb_batch_state& S = st[tile.sys];
-    if (!S.active || S.done || S.need_update) {  // need_update: admission pending
-      if (threadIdx.x == 0) spart[t] = 0.0;
-      continue;
+    double pap = 0.0;
+    if (S.active && !S.done && !S.need_update) {  // need_update: admission pending
+      const fgb_batch_system& A = sys[tile.sys];
+      pap = A.fp64 ? spmv_tile<double>(A, S, tile) : spmv_tile<float>(A, S, tile);
     }
-    const fgb_batch_system& A = sys[tile.sys];
-    const double pap = A.fp64 ? spmv_tile<double>(A, S, tile) : spmv_tile<float>(A, S, tile);
-    const double b = block_sum(pap, red);
-    if (threadIdx.x == 0) spart[t] = b;
-    __syncthreads();
+    pap = warp_sum(pap);
+    if ((threadIdx.x & 31) == 0) spart[t] = pap;
   }
 }
 
-// Systems (a warp each): alpha = rz / p.Ap.
+// Systems (a block each): alpha = rz / p.Ap.  Also returns the SpMV ticket.
 __global__ void batch_alpha(int32_t n_sys, fgb_batch_state* st, const int32_t* __restrict__ tile_ptr,
-                            const double* __restrict__ spart) {
-  const int s = warp_system();
+                            const double* __restrict__ spart, BatchCtl* ctl) {
+  __shared__ double red[32];
+  if (blockIdx.x == 0 && threadIdx.x == 0) ctl->ticket[kTicketSpmv] = 0u;
+  const int s = blockIdx.x;
   if (s >= n_sys) return;
   fgb_batch_state& S = st[s];
   if (!S.active || S.done || S.need_update) return;
-  const double pap = tile_sum(spart, tile_ptr[s], tile_ptr[s + 1], 1, 0);
-  if ((threadIdx.x & 31) != 0) return;
+  const double pap = tile_sum(spart, tile_ptr[s], tile_ptr[s + 1], 1, 0, red);
+  if (threadIdx.x != 0) return;
   if (!(pap > 0.0) || !isfinite(pap)) {
     S.done = isfinite(pap) ? FGB_PCG_BREAKDOWN : FGB_PCG_NONFINITE;
     S.alpha = 0.0;
@@ -127,8 +145,8 @@ __global__ void batch_alpha(int32_t n_sys, fgb_batch_state* st, const int32_t* _
   }
 }
 
-// One row tile: y += alpha p, r -= alpha Ap, z = Dinv r; per-thread r.z, r.r
-// (accumulated in the vector type, combined in FP64 by the block).
+// One row tile, one warp: y += alpha p, r -= alpha Ap, z = Dinv r; the lane's
+// r.z, r.r (accumulated in the vector type).
 template <typename T>
 __device__ void update_tile(const fgb_batch_system& A, const fgb_batch_state& S, const fgb_batch_tile& tile,
                             double* rz_out, double* rr_out) {
@@ -140,7 +158,7 @@ __device__ void update_tile(const fgb_batch_system& A, const fgb_batch_state& S,
   T* __restrict__ r = vp<T>(A.r);
   T* __restrict__ z = vp<T>(A.z);
   T rz = T(0), rr = T(0);
-  for (int i = tile.begin + threadIdx.x; i < tile.end; i += blockDim.x) {
+  for (int i = tile.begin + (threadIdx.x & 31); i < tile.end; i += 32) {
     y[i] += alpha * p[i];
     const T ri = r[i] - alpha * Ap[i];
     const T zi = dinv[i] * ri;
@@ -153,52 +171,52 @@ __device__ void update_tile(const fgb_batch_system& A, const fgb_batch_state& S,
   *rr_out = static_cast<double>(rr);
 }
 
-// Row tiles: the updates and the tile's r.z, r.r.
+// Row tiles (a warp each, by ticket): the updates and the tile's r.z, r.r.
 __global__ void __launch_bounds__(1024, 1) batch_update(const fgb_batch_system* __restrict__ sys,
                                                         const fgb_batch_state* __restrict__ st,
                                                         const fgb_batch_tile* __restrict__ tiles,
-                                                        const int32_t* __restrict__ n_tiles, double* vpart) {
-  __shared__ double red[32];
+                                                        const int32_t* __restrict__ n_tiles, double* vpart,
+                                                        BatchCtl* ctl) {
   const int nt = *n_tiles;
-  for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+  while (true) {
+    const int t = next_tile(&ctl->ticket[kTicketUpdate]);
+    if (t >= nt) break;
     const fgb_batch_tile tile = tiles[t];
     const fgb_batch_state& S = st[tile.sys];
-    if (!S.active || S.done || S.need_update) {
-      if (threadIdx.x == 0) { vpart[2 * t] = 0.0; vpart[2 * t + 1] = 0.0; }
-      continue;
+    double rz = 0.0, rr = 0.0;
+    if (S.active && !S.done && !S.need_update) {
+      const fgb_batch_system& A = sys[tile.sys];
+      if (A.fp64) update_tile<double>(A, S, tile, &rz, &rr);
+      else update_tile<float>(A, S, tile, &rz, &rr);
     }
-    const fgb_batch_system& A = sys[tile.sys];
-    double rz, rr;
-    if (A.fp64) update_tile<double>(A, S, tile, &rz, &rr);
-    else update_tile<float>(A, S, tile, &rz, &rr);
-    const double a = block_sum(rz, red);
-    __syncthreads();
-    const double b = block_sum(rr, red);
-    if (threadIdx.x == 0) { vpart[2 * t] = a; vpart[2 * t + 1] = b; }
-    __syncthreads();
+    rz = warp_sum(rz);
+    rr = warp_sum(rr);
+    if ((threadIdx.x & 31) == 0) { vpart[2 * t] = rz; vpart[2 * t + 1] = rr; }
   }
 }
 
-// Systems (a warp each): rz, rr, beta, stopping test and whether a reliable
-// update is due; the last block to finish sets the graph conditions.  An FP32
-// system also gets a check of its true residual when the gap since its last
-// reliable update has grown well past the longest earlier gap (a plateau).
+// Systems (a block each): rz, rr, beta, stopping test and whether a reliable
+// update (or a check of the true residual) is due; the last block to finish
+// sets the graph conditions.  Also returns the update ticket.
 __global__ void batch_control(int32_t n_sys, fgb_batch_state* st, const int32_t* __restrict__ tile_ptr,
                               const double* __restrict__ vpart, const fgb_batch_system* __restrict__ sys,
                               BatchCtl* ctl, cudaGraphConditionalHandle h_if, cudaGraphConditionalHandle h_while,
                               int graph) {
+  __shared__ double red[32];
   __shared__ bool last;
+  if (blockIdx.x == 0 && threadIdx.x == 0) ctl->ticket[kTicketUpdate] = 0u;
   int any = 0, running = 0;
-  const int s = warp_system();
+  const int s = blockIdx.x;
   if (s < n_sys) {
     fgb_batch_state& S = st[s];
     if (S.active && !S.done) {
       if (S.need_update) {
         running = 1;
       } else {
-        const double rz = tile_sum(vpart, tile_ptr[s], tile_ptr[s + 1], 2, 0);
-        const double rr = tile_sum(vpart, tile_ptr[s], tile_ptr[s + 1], 2, 1);
-        if ((threadIdx.x & 31) == 0) {
+        const double rz = tile_sum(vpart, tile_ptr[s], tile_ptr[s + 1], 2, 0, red);
+        __syncthreads();
+        const double rr = tile_sum(vpart, tile_ptr[s], tile_ptr[s + 1], 2, 1, red);
+        if (threadIdx.x == 0) {
           S.niter += 1;
           const double res = sqrt(rr);
           S.resid = res;
@@ -229,8 +247,6 @@ __global__ void batch_control(int32_t n_sys, fgb_batch_state* st, const int32_t*
       }
     }
   }
-  any = __syncthreads_or(any);
-  running = __syncthreads_or(running);
   if (threadIdx.x == 0) {
     if (any) atomicOr(&ctl->any_acc, 1);
     if (running) atomicOr(&ctl->running_acc, 1);
@@ -257,7 +273,7 @@ __global__ void batch_control(int32_t n_sys, fgb_batch_state* st, const int32_t*
 template <typename T>
 __device__ void fold_tile(const fgb_batch_system& A, const fgb_batch_tile& tile) {
   T* y = vp<T>(A.y);
-  for (int i = tile.begin + threadIdx.x; i < tile.end; i += blockDim.x) {
+  for (int i = tile.begin + (threadIdx.x & 31); i < tile.end; i += 32) {
     A.x[i] += static_cast<double>(y[i]);
     y[i] = T(0);
   }
@@ -267,24 +283,26 @@ template <typename T>
 __device__ double admit_tile(const fgb_batch_system& A, const fgb_batch_tile& tile) {
   T* y = vp<T>(A.y);
   double bb = 0.0;
-  for (int i = tile.begin + threadIdx.x; i < tile.end; i += blockDim.x) {
+  for (int i = tile.begin + (threadIdx.x & 31); i < tile.end; i += 32) {
     y[i] = T(0);
     bb += A.b[i] * A.b[i];
   }
   return bb;
 }
 
-// Row tiles of systems with an update due (or all given slots when force):
-// x += y, y = 0.  Admission (need_update == 2) instead zeroes y and forms the
-// per-tile partials of b.b.
+// Row tiles (a warp each, by ticket) of systems with an update due (or all
+// given slots when force): x += y, y = 0.  Admission (need_update == 2)
+// instead zeroes y and forms the per-tile partials of b.b.
 __global__ void __launch_bounds__(1024, 1) batch_fold(const fgb_batch_system* __restrict__ sys,
                                                       const fgb_batch_state* __restrict__ st,
                                                       const fgb_batch_tile* __restrict__ tiles,
                                                       const int32_t* __restrict__ n_tiles,
-                                                      const int32_t* __restrict__ force, double* vpart) {
-  __shared__ double red[32];
+                                                      const int32_t* __restrict__ force, double* vpart,
+                                                      BatchCtl* ctl) {
   const int nt = *n_tiles;
-  for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+  while (true) {
+    const int t = next_tile(&ctl->ticket[kTicketFold]);
+    if (t >= nt) break;
     const fgb_batch_tile tile = tiles[t];
     const fgb_batch_state& S = st[tile.sys];
     const bool forced = force && force[tile.sys];
@@ -294,41 +312,43 @@ __global__ void __launch_bounds__(1024, 1) batch_fold(const fgb_batch_system* __
       if (A.fp64) fold_tile<double>(A, tile);
       else fold_tile<float>(A, tile);
     } else if (mode == 2 && !S.done) {
-      const double bb = A.fp64 ? admit_tile<double>(A, tile) : admit_tile<float>(A, tile);
-      const double v = block_sum(bb, red);
-      if (threadIdx.x == 0) vpart[2 * t] = v;
-      __syncthreads();
+      double bb = A.fp64 ? admit_tile<double>(A, tile) : admit_tile<float>(A, tile);
+      bb = warp_sum(bb);
+      if ((threadIdx.x & 31) == 0) vpart[2 * t] = bb;
     }
   }
 }
 
 // Admission: ||b||, tol = rtol * ||b|| (rtol was stored in tol), zero rhs.
+// Also returns the fold ticket.
 __global__ void batch_bnorm(int32_t n_sys, fgb_batch_state* st, const int32_t* __restrict__ tile_ptr,
-                            const double* __restrict__ vpart) {
-  const int s = warp_system();
+                            const double* __restrict__ vpart, BatchCtl* ctl) {
+  __shared__ double red[32];
+  if (blockIdx.x == 0 && threadIdx.x == 0) ctl->ticket[kTicketFold] = 0u;
+  const int s = blockIdx.x;
   if (s >= n_sys) return;
   fgb_batch_state& S = st[s];
   if (!S.active || S.done || S.need_update != 2) return;
-  const double bb = tile_sum(vpart, tile_ptr[s], tile_ptr[s + 1], 2, 0);
-  if ((threadIdx.x & 31) != 0) return;
+  const double bb = tile_sum(vpart, tile_ptr[s], tile_ptr[s + 1], 2, 0, red);
+  if (threadIdx.x != 0) return;
   S.b_norm = sqrt(bb);
   S.tol = S.tol * S.b_norm;
   if (S.b_norm < 1e-15) S.done = FGB_PCG_ZERO_RHS;
 }
 
-// Slice tiles of systems with an update due (1) or admitted (2): r64 = b - A x
-// in FP64 arithmetic (V: the stored values), r = T(r64), z = Dinv r; per-tile
-// r64.r64 and r.z.  Admission of an FP32 system also builds its FP32 inverse
-// diagonal; admission starts p_old = z.
+// One slice tile, one warp, of a system with an update due (1, 3) or admitted
+// (2): r64 = b - A x in FP64 arithmetic (V: the stored values), r = T(r64),
+// z = Dinv r; the lane's r64.r64 and r.z.  Admission of an FP32 system also
+// builds its FP32 inverse diagonal; admission starts p_old = z.
 template <typename V, typename T>
 __device__ void reliable_tile(const fgb_batch_system& A, const fgb_batch_state& S, const V* __restrict__ val,
                               const fgb_batch_tile& tile, int mode, double* rr_out, double* rz_out) {
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+  const int lane = threadIdx.x & 31;
   double rr64 = 0.0, rz = 0.0;
   T* p_old = vp<T>(S.parity ? A.p1 : A.p0);
   T* r = vp<T>(A.r);
   T* z = vp<T>(A.z);
-  for (int64_t s = tile.begin + wib; s < tile.end; s += wpb) {
+  for (int64_t s = tile.begin; s < tile.end; ++s) {
     const int64_t sbase = A.slice_ptr[s];
     const int w = static_cast<int>((A.slice_ptr[s + 1] - sbase) >> 5);
     const double acc = sell_row_acc<V, double>(A.col, val, sbase, w, lane, GatherX<double>{A.x});
@@ -360,10 +380,12 @@ __device__ void reliable_tile(const fgb_batch_system& A, const fgb_batch_state& 
 __global__ void __launch_bounds__(1024, 1) batch_reliable(const fgb_batch_system* __restrict__ sys,
                                                           const fgb_batch_state* __restrict__ st,
                                                           const fgb_batch_tile* __restrict__ tiles,
-                                                          const int32_t* __restrict__ n_tiles, double* rpart) {
-  __shared__ double red[32];
+                                                          const int32_t* __restrict__ n_tiles, double* rpart,
+                                                          BatchCtl* ctl) {
   const int nt = *n_tiles;
-  for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+  while (true) {
+    const int t = next_tile(&ctl->ticket[kTicketReliable]);
+    if (t >= nt) break;
     const fgb_batch_tile tile = tiles[t];
     const fgb_batch_state& S = st[tile.sys];
     const int mode = S.active && !S.done ? S.need_update : 0;
@@ -373,28 +395,34 @@ __global__ void __launch_bounds__(1024, 1) batch_reliable(const fgb_batch_system
     if (A.fp64) reliable_tile<double, double>(A, S, A.val64, tile, mode, &rr, &rz);
     else if (A.val64) reliable_tile<double, float>(A, S, A.val64, tile, mode, &rr, &rz);
     else reliable_tile<float, float>(A, S, A.val32, tile, mode, &rr, &rz);
-    const double a = block_sum(rr, red);
-    __syncthreads();
-    const double b = block_sum(rz, red);
-    if (threadIdx.x == 0) { rpart[2 * t] = a; rpart[2 * t + 1] = b; }
-    __syncthreads();
+    rr = warp_sum(rr);
+    rz = warp_sum(rz);
+    if ((threadIdx.x & 31) == 0) { rpart[2 * t] = rr; rpart[2 * t + 1] = rz; }
   }
 }
 
-// Systems with an update due or admitted: true residual test, beta from the
-// replaced residual.  An FP32 system whose true residual has not halved since
-// the previous check stops as FGB_PCG_STAGNATED (its condition number is
-// beyond what FP32 iterations resolve); the caller continues it in FP64.
+// Systems (a block each) with an update due or admitted: true residual test,
+// beta from the replaced residual.  An FP32 system whose true residual has not
+// halved since the previous check stops as FGB_PCG_STAGNATED (its condition
+// number is beyond what FP32 iterations resolve); the caller continues it in
+// FP64.  Also returns the fold and reliable tickets.
 __global__ void batch_reliable_fin(int32_t n_sys, fgb_batch_state* st, const int32_t* __restrict__ tile_ptr,
-                                   const double* __restrict__ rpart, const fgb_batch_system* __restrict__ sys) {
-  const int s = warp_system();
+                                   const double* __restrict__ rpart, const fgb_batch_system* __restrict__ sys,
+                                   BatchCtl* ctl) {
+  __shared__ double red[32];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    ctl->ticket[kTicketFold] = 0u;
+    ctl->ticket[kTicketReliable] = 0u;
+  }
+  const int s = blockIdx.x;
   if (s >= n_sys) return;
   fgb_batch_state& S = st[s];
   const int mode = S.active && !S.done ? S.need_update : 0;
   if (!mode) return;
-  const double rr = tile_sum(rpart, tile_ptr[s], tile_ptr[s + 1], 2, 0);
-  const double rz = tile_sum(rpart, tile_ptr[s], tile_ptr[s + 1], 2, 1);
-  if ((threadIdx.x & 31) != 0) return;
+  const double rr = tile_sum(rpart, tile_ptr[s], tile_ptr[s + 1], 2, 0, red);
+  __syncthreads();
+  const double rz = tile_sum(rpart, tile_ptr[s], tile_ptr[s + 1], 2, 1, red);
+  if (threadIdx.x != 0) return;
   const double nrm = sqrt(rr);
   S.true_rel = S.b_norm > 0.0 ? nrm / S.b_norm : 0.0;
   S.resid = nrm;
@@ -426,29 +454,33 @@ __global__ void batch_reliable_fin(int32_t n_sys, fgb_batch_state* st, const int
   S.need_update = 0;
 }
 
-// Retirement: slots flagged in `force` become inactive; flags cleared.
-__global__ void batch_deactivate(int32_t n_sys, fgb_batch_state* st, int32_t* force) {
+// Retirement: slots flagged in `force` become inactive; flags cleared.  Also
+// returns the fold ticket (retirement runs batch_fold first).
+__global__ void batch_deactivate(int32_t n_sys, fgb_batch_state* st, int32_t* force, BatchCtl* ctl) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s == 0) ctl->ticket[kTicketFold] = 0u;
   if (s >= n_sys || !force[s]) return;
   st[s].active = 0;
   force[s] = 0;
 }
 
-// y_s = A_s x_s (FP32) over slice tiles; the autotuner's timing kernel.
+// y_s = A_s x_s (FP32) over slice tiles, a warp per tile (tiles dealt out
+// round-robin); the autotuner's timing kernel.
 __global__ void __launch_bounds__(1024, 1) batch_spmv_plain(const fgb_batch_system* __restrict__ sys,
                                                             const fgb_batch_tile* __restrict__ tiles,
                                                             const int32_t* __restrict__ n_tiles,
                                                             const float* const* __restrict__ xs,
                                                             float* const* __restrict__ ys) {
   const int nt = *n_tiles;
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
-  for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+  const int lane = threadIdx.x & 31;
+  const int w0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+  for (int t = w0; t < nt; t += nw) {
     const fgb_batch_tile tile = tiles[t];
     const fgb_batch_system& A = sys[tile.sys];
     if (A.fp64) continue;
     const GatherX<float> g{xs[tile.sys]};
     float* y = ys[tile.sys];
-    for (int64_t s = tile.begin + wib; s < tile.end; s += wpb) {
+    for (int64_t s = tile.begin; s < tile.end; ++s) {
       const int64_t sbase = A.slice_ptr[s];
       const int w = static_cast<int>((A.slice_ptr[s + 1] - sbase) >> 5);
       const float acc = sell_row(A.col, A.val32, sbase, w, lane, g);
@@ -506,7 +538,7 @@ size_t batch_layout(int32_t ms, int32_t mst, int32_t mvt, fgb_batch* b, void* ba
 }
 
 int sys_blocks(int32_t n) { return (n + 255) / 256; }
-int warp_sys_blocks(int32_t n) { return (n * 32 + 255) / 256; }  // one warp per system
+constexpr int kSysThreads = 256;  // a block per system for the per-system sums
 // The tile loops are persistent: as many blocks as stay resident at once (the
 // slice kernels use up to 64 registers a thread, so 1024 threads per SM), so
 // that no block of a later wave holds a tile back.
@@ -518,17 +550,21 @@ int row_grid(const fgb_batch* b) { return b->max_vt < kBatchRowBlocks ? b->max_v
 
 void launch_iteration(fgb_batch* b, cudaStream_t s, int graph, cudaGraphConditionalHandle h_if,
                       cudaGraphConditionalHandle h_while) {
-  batch_spmv_step<<<slice_grid(b), b->slice_threads, 0, s>>>(b->sys, b->st, b->stiles, b->n_stiles, b->spart);
-  batch_alpha<<<warp_sys_blocks(b->max_sys), 256, 0, s>>>(b->max_sys, b->st, b->stile_ptr, b->spart);
-  batch_update<<<row_grid(b), kBatchRowThreads, 0, s>>>(b->sys, b->st, b->vtiles, b->n_vtiles, b->vpart);
-  batch_control<<<warp_sys_blocks(b->max_sys), 256, 0, s>>>(b->max_sys, b->st, b->vtile_ptr, b->vpart, b->sys, b->ctl, h_if, h_while,
+  batch_spmv_step<<<slice_grid(b), b->slice_threads, 0, s>>>(b->sys, b->st, b->stiles, b->n_stiles, b->spart,
+                                                              b->ctl);
+  batch_alpha<<<b->max_sys, kSysThreads, 0, s>>>(b->max_sys, b->st, b->stile_ptr, b->spart, b->ctl);
+  batch_update<<<row_grid(b), kBatchRowThreads, 0, s>>>(b->sys, b->st, b->vtiles, b->n_vtiles, b->vpart, b->ctl);
+  batch_control<<<b->max_sys, kSysThreads, 0, s>>>(b->max_sys, b->st, b->vtile_ptr, b->vpart, b->sys, b->ctl, h_if, h_while,
                                                graph);
 }
 
 void launch_reliable(fgb_batch* b, cudaStream_t s) {
-  batch_fold<<<row_grid(b), kBatchRowThreads, 0, s>>>(b->sys, b->st, b->vtiles, b->n_vtiles, nullptr, b->vpart);
-  batch_reliable<<<slice_grid(b), b->slice_threads, 0, s>>>(b->sys, b->st, b->stiles, b->n_stiles, b->rpart);
-  batch_reliable_fin<<<warp_sys_blocks(b->max_sys), 256, 0, s>>>(b->max_sys, b->st, b->stile_ptr, b->rpart, b->sys);
+  batch_fold<<<row_grid(b), kBatchRowThreads, 0, s>>>(b->sys, b->st, b->vtiles, b->n_vtiles, nullptr, b->vpart,
+                                                      b->ctl);
+  batch_reliable<<<slice_grid(b), b->slice_threads, 0, s>>>(b->sys, b->st, b->stiles, b->n_stiles, b->rpart,
+                                                            b->ctl);
+  batch_reliable_fin<<<b->max_sys, kSysThreads, 0, s>>>(b->max_sys, b->st, b->stile_ptr, b->rpart, b->sys,
+                                                         b->ctl);
 }
 
 // while (running && trips < limit) { iteration ; if (update due) reliable }
@@ -713,10 +749,13 @@ int32_t fgb_batch_admit(fgb_batch* b, int32_t n, const int32_t* slots, const dou
     if (cudaStreamSynchronize(s) != cudaSuccess) return FGB_ERR_CUDA;  // h lives on this stack frame
   }
   if (n == 0) return FGB_OK;
-  batch_fold<<<row_grid(b), kBatchRowThreads, 0, s>>>(b->sys, b->st, b->vtiles, b->n_vtiles, nullptr, b->vpart);
-  batch_bnorm<<<warp_sys_blocks(b->max_sys), 256, 0, s>>>(b->max_sys, b->st, b->vtile_ptr, b->vpart);
-  batch_reliable<<<slice_grid(b), b->slice_threads, 0, s>>>(b->sys, b->st, b->stiles, b->n_stiles, b->rpart);
-  batch_reliable_fin<<<warp_sys_blocks(b->max_sys), 256, 0, s>>>(b->max_sys, b->st, b->stile_ptr, b->rpart, b->sys);
+  batch_fold<<<row_grid(b), kBatchRowThreads, 0, s>>>(b->sys, b->st, b->vtiles, b->n_vtiles, nullptr, b->vpart,
+                                                      b->ctl);
+  batch_bnorm<<<b->max_sys, kSysThreads, 0, s>>>(b->max_sys, b->st, b->vtile_ptr, b->vpart, b->ctl);
+  batch_reliable<<<slice_grid(b), b->slice_threads, 0, s>>>(b->sys, b->st, b->stiles, b->n_stiles, b->rpart,
+                                                            b->ctl);
+  batch_reliable_fin<<<b->max_sys, kSysThreads, 0, s>>>(b->max_sys, b->st, b->stile_ptr, b->rpart, b->sys,
+                                                         b->ctl);
   return launch_status();
 }
 
@@ -775,8 +814,9 @@ int32_t fgb_batch_retire(fgb_batch* b, int32_t n, const int32_t* slots, void* st
   ok = ok && cudaStreamSynchronize(s) == cudaSuccess;
   delete[] flags;
   if (!ok) return FGB_ERR_CUDA;
-  batch_fold<<<row_grid(b), kBatchRowThreads, 0, s>>>(b->sys, b->st, b->vtiles, b->n_vtiles, b->force, b->vpart);
-  batch_deactivate<<<sys_blocks(b->max_sys), 256, 0, s>>>(b->max_sys, b->st, b->force);
+  batch_fold<<<row_grid(b), kBatchRowThreads, 0, s>>>(b->sys, b->st, b->vtiles, b->n_vtiles, b->force, b->vpart,
+                                                      b->ctl);
+  batch_deactivate<<<sys_blocks(b->max_sys), 256, 0, s>>>(b->max_sys, b->st, b->force, b->ctl);
   return launch_status();
 }
 

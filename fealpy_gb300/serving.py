@@ -95,7 +95,7 @@ class SolveServer:
                                                                                    torch.cuda.current_device())
         self.hbm_budget, self.max_slots, self.chunk = float(hbm_budget), int(max_slots), int(chunk)
         self.fp64, self.rtol, self.maxit = bool(fp64), float(rtol), int(maxit)
-        kw = dict(max_slice_tiles=1 << 17, max_row_tiles=1 << 17)
+        kw = dict(max_slice_tiles=1 << 18, max_row_tiles=1 << 18)
         kw.update(batch_kw)
         self.batch = BatchSolver(self.max_slots, device=self.device, **kw)
         self.resident = 0
