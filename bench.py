@@ -518,7 +518,9 @@ def run_batched(args):
     meshes = batched_tri_meshes(args.batch_count)
     probs = batched_setup(torch, F, meshes, dev)
     gdof = sum(pr[0].number_of_global_dofs() for pr in probs)
-    kw = dict(max_slice_tiles=1 << 18, max_row_tiles=1 << 18)
+    # tile capacity for the finest candidate split (4 slices of 32 rows per
+    # tile) plus one partial tile per system
+    kw = dict(max_slice_tiles=gdof // 128 + 2 * len(probs) + 1024, max_row_tiles=1 << 18)
     # autotune the slice tiling on the first step's systems
     res, systems, _ = batched_step(torch, F, probs, asm_dtype, kw)
     times = autotune(systems[:64], device=dev, **kw)

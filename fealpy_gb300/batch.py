@@ -95,6 +95,24 @@ class BatchSolver:
     def active(self) -> int:
         return self.max_systems - self.free_slots()
 
+    def _n_tiles(self, lim, per_tile):
+        step = max(per_tile, -(-lim // self.max_tiles_per_system))
+        return -(-lim // step)
+
+    def fits(self, n: int) -> bool:
+        """Whether a free slot and the tile tables have room for one more
+        system of ``n`` rows next to the systems already placed."""
+        if self.free_slots() == 0:
+            return False
+        st = vt = 0
+        for sl in self._slots:
+            if sl is not None:
+                st += self._n_tiles(sl.S.n_slices, self.slices_per_tile)
+                vt += self._n_tiles(sl.S.n, self.rows_per_tile)
+        st += self._n_tiles(int(_lib.lib().fgb_sell_slots(n)) // 32, self.slices_per_tile)
+        vt += self._n_tiles(n, self.rows_per_tile)
+        return st <= self.max_slice_tiles and vt <= self.max_row_tiles
+
     @staticmethod
     def resident_bytes(n: int, nnz_padded: int, fp64_values: bool) -> int:
         """Device bytes one system keeps resident (SELL copy + vectors)."""

@@ -105,7 +105,7 @@ class SolveServer:
     def admit(self, key, A, b) -> bool:
         """Admit one assembled request if a slot and the budget allow."""
         need = resident_estimate(A.shape[0], A.nnz, self.fp64)
-        if self.batch.free_slots() == 0 or self.resident + need > self.hbm_budget:
+        if not self.batch.fits(A.shape[0]) or self.resident + need > self.hbm_budget:
             return False
         self.batch.add(A, b, rtol=self.rtol, maxit=self.maxit, key=key, fp64=self.fp64)
         self._bytes[key] = need
