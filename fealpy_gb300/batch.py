@@ -133,11 +133,13 @@ class BatchSolver:
             raise RuntimeError("no free slot in the batch") from None
         n = A.shape[0]
         if fp64:
-            S = K.sell_build(A.crow, A.col, A.values.to(torch.float64).contiguous(), None, want64=True, want32=False)
+            S = K.sell_build(A.crow, A.col, A.values.to(torch.float64).contiguous(), None, want64=True, want32=False,
+                             d16=False)
         elif A.values.dtype == torch.float32:
-            S = K.sell_build(A.crow, A.col, None, A.values.contiguous(), want64=False, want32=True)
+            S = K.sell_build(A.crow, A.col, None, A.values.contiguous(), want64=False, want32=True, d16=False)
         else:
-            S = K.sell_build(A.crow, A.col, A.values.to(torch.float64).contiguous(), None, want64=True, want32=True)
+            S = K.sell_build(A.crow, A.col, A.values.to(torch.float64).contiguous(), None, want64=True, want32=True,
+                             d16=False)
         dinv64 = A.diagonal_inverse().to(torch.float64).contiguous()
         b64 = b.to(self.device, torch.float64).contiguous()
         x = torch.zeros(n, dtype=torch.float64, device=self.device) if x0 is None else \

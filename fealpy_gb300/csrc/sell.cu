@@ -22,6 +22,7 @@
 #include <climits>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 
 namespace fgb {
 
@@ -35,7 +36,29 @@ struct SellView {
   const int32_t* col;
   int threads;  // launch shape of the slice kernels (0: defaults)
   int blocks;
+  const uint16_t* col16;  // delta-coded columns (then col is unused) or null
+  const int32_t* col0;    // first column of every slot's row (delta-coded copies)
 };
+
+// Row of slot (s, lane): sum over entries of val * g(col), for either column
+// format.  The slice width is a multiple of 4 entries.
+template <bool D16, typename V, typename T, typename G>
+__device__ __forceinline__ T slice_row(const SellView& A, const V* __restrict__ val, int64_t s, int lane,
+                                       const G& g) {
+  const int64_t sbase = A.slice_ptr[s];
+  const int w = static_cast<int>((A.slice_ptr[s + 1] - sbase) >> 5);
+  if constexpr (D16)
+    return sell_row_acc_d16<V, T>(A.col16, A.col0[s * kSellC + lane], val, sbase, w, lane, g);
+  else
+    return sell_row_acc<V, T>(A.col, val, sbase, w, lane, g);
+}
+
+// Launch `f(std::integral_constant<bool, D16>)` for the column format of A.
+template <typename F>
+void with_cols(const SellView& A, F&& f) {
+  if (A.col16) f(std::true_type{});
+  else f(std::false_type{});
+}
 
 // Launch shapes.  Vector kernels: two 512-thread blocks per SM (few blocks
 // shorten the tail of the deterministic block reduction; measured at 2.1M rows:
@@ -69,6 +92,11 @@ inline Launch slice_launch(const SellView& A) {
 // blocks of a slice-kernel launch (one p.Ap partial each)
 inline int slice_blocks(const SellView& A) { return slice_launch(A).blocks; }
 #define VEC_LAUNCH(n, s) vec_launch(n).blocks, vec_launch(n).threads, 0, s
+
+// both pointers 16-byte aligned (vector kernels take 16-byte accesses then)
+__device__ __forceinline__ bool aligned16(const void* a, const void* b) {
+  return ((reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(b)) & 15u) == 0;
+}
 
 // -------------------------------------------------------------- construction
 __global__ void sell_sort_windows(int64_t n, const int64_t* __restrict__ indptr, int32_t* __restrict__ perm,
@@ -133,7 +161,7 @@ __global__ void sell_fill_kernel(int64_t n_slices, const int64_t* __restrict__ s
 }
 
 // ------------------------------------------------------------------- SpMV
-template <typename T>
+template <typename T, bool D16>
 __global__ void __launch_bounds__(1024, 1) sell_spmv_kernel(SellView A, const T* __restrict__ val,
                                                                  const T* __restrict__ x, T* __restrict__ y) {
   const int lane = threadIdx.x & 31;
@@ -141,9 +169,7 @@ __global__ void __launch_bounds__(1024, 1) sell_spmv_kernel(SellView A, const T*
   const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
   const GatherX<T> g{x};
   for (int64_t s = warp; s < A.n_slices; s += nwarps) {
-    const int64_t sbase = A.slice_ptr[s];
-    const int w = static_cast<int>((A.slice_ptr[s + 1] - sbase) >> 5);
-    const T acc = sell_row(A.col, val, sbase, w, lane, g);
+    const T acc = slice_row<D16, T, T>(A, val, s, lane, g);
     const int32_t row = A.perm[s * kSellC + lane];
     if (row >= 0) y[row] = acc;
   }
@@ -163,50 +189,60 @@ struct SellPcgState {
   int stall, pad;
 };
 
-// Last-block-done deterministic reduction of two FP64 partials per block.
-__device__ bool sell_last_block(double v0, double v1, double* partials, unsigned int* counter, double* out0,
-                                double* out1) {
-  __shared__ double red[32];  // one slot per warp of a block of up to 1024 threads
-  __shared__ bool am_last;
-  double s0 = block_sum(v0, red);
+// Last-block-done deterministic reduction of two partials per thread (T =
+// float: FP32 per-thread and per-warp sums, as in the FP32 iterations; T =
+// double: FP64 throughout).  Per block: warp shuffles, one barrier, then warp
+// 0 alone adds the warps' sums in FP64, publishes the block's partials and
+// takes a ticket; warp 0 of the last block loads all partials (unrolled, a
+// round trip per 320 blocks) and adds them in block order.  FP64 arithmetic is
+// kept to a few lanes: its rate on this part is a small fraction of FP32.  The
+// totals are valid in thread 0 of the last block, the only thread that returns
+// true.  Must be the last block-wide step of the calling kernel: warps other
+// than 0 return at once.
+template <typename T>
+__device__ bool sell_last_block(T v0, T v1, double* partials, unsigned int* counter, double* out0, double* out1) {
+  __shared__ double2 ws[32];  // one slot per warp of a block of up to 1024 threads
+  constexpr int kPer = 10;    // partials per lane and round trip
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  v0 = warp_sum(v0);
+  v1 = warp_sum(v1);
+  if (lane == 0) ws[wid] = make_double2(static_cast<double>(v0), static_cast<double>(v1));
   __syncthreads();
-  double s1 = block_sum(v1, red);
-  if (threadIdx.x == 0) {
-    partials[blockIdx.x] = s0;
-    partials[kSellMaxBlocks + blockIdx.x] = s1;
+  if (wid != 0) return false;
+  const int nw = (blockDim.x + 31) >> 5;
+  double2 t = lane < nw ? ws[lane] : make_double2(0.0, 0.0);
+  t.x = warp_sum(t.x);
+  t.y = warp_sum(t.y);
+  unsigned int ticket = 0u;
+  if (lane == 0) {
+    partials[blockIdx.x] = t.x;
+    partials[kSellMaxBlocks + blockIdx.x] = t.y;
     __threadfence();
-    unsigned int t = atomicAdd(counter, 1u);
-    am_last = (t == gridDim.x - 1);
+    ticket = atomicAdd(counter, 1u);
   }
-  __syncthreads();
-  if (!am_last) return false;
+  ticket = __shfl_sync(0xffffffffu, ticket, 0);
+  if (ticket != gridDim.x - 1) return false;
   __threadfence();
+  const int nb = static_cast<int>(gridDim.x);
   double a = 0.0, b = 0.0;
-  for (int k = threadIdx.x; k < static_cast<int>(gridDim.x); k += blockDim.x) {
-    a += __ldcg(partials + k);
-    b += __ldcg(partials + kSellMaxBlocks + k);
+  for (int base = 0; base < nb; base += 32 * kPer) {
+    double pa[kPer], pb[kPer];
+#pragma unroll
+    for (int u = 0; u < kPer; ++u) {
+      const int k = base + lane + 32 * u;
+      pa[u] = k < nb ? __ldcg(partials + k) : 0.0;
+      pb[u] = k < nb ? __ldcg(partials + kSellMaxBlocks + k) : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < kPer; ++u) {
+      a += pa[u];
+      b += pb[u];
+    }
   }
-  __syncthreads();
-  a = block_sum(a, red);
-  __syncthreads();
-  b = block_sum(b, red);
-  if (threadIdx.x == 0) { *out0 = a; *out1 = b; *counter = 0u; }
-  return true;
-}
-
-// Row of the calling lane: `base` is slice_ptr[s] + lane (as in the callers).
-template <typename T>
-__device__ __forceinline__ T sell_row_dot_p(const SellView& A, const T* __restrict__ val, int64_t base, int w,
-                                            const T* __restrict__ z, const T* __restrict__ p_old, T beta) {
-  const int lane = threadIdx.x & 31;
-  return sell_row(A.col, val, base - lane, w, lane, GatherP<T>{z, p_old, beta});
-}
-
-template <typename T>
-__device__ __forceinline__ T sell_row_dot_x(const SellView& A, const T* __restrict__ val, int64_t base, int w,
-                                            const T* __restrict__ x) {
-  const int lane = threadIdx.x & 31;
-  return sell_row(A.col, val, base - lane, w, lane, GatherX<T>{x});
+  a = warp_sum(a);
+  b = warp_sum(b);
+  if (lane == 0) { *out0 = a; *out1 = b; *counter = 0u; }
+  return lane == 0;
 }
 
 #define SELL_WARP_LOOP(A)                                                                   \
@@ -216,7 +252,7 @@ __device__ __forceinline__ T sell_row_dot_x(const SellView& A, const T* __restri
   for (int64_t s = warp0; s < (A).n_slices; s += nwarps)
 
 // r = b - A x ; z = Dinv r ; p = z ; rz, b.b   (T = FP64 state)
-template <typename T>
+template <typename T, bool D16>
 __global__ void __launch_bounds__(1024, 1) sell_pcg_init(SellView A, const T* __restrict__ val,
                                                               const T* __restrict__ dinv, const T* __restrict__ b,
                                                               const T* __restrict__ x, T* __restrict__ r,
@@ -224,9 +260,7 @@ __global__ void __launch_bounds__(1024, 1) sell_pcg_init(SellView A, const T* __
                                                               SellPcgState* st) {
   double rz = 0.0, bb = 0.0;
   SELL_WARP_LOOP(A) {
-    const int64_t base = A.slice_ptr[s] + lane;
-    const int w = static_cast<int>((A.slice_ptr[s + 1] - A.slice_ptr[s]) >> 5);
-    const T acc = sell_row_dot_x(A, val, base, w, x);
+    const T acc = slice_row<D16, T, T>(A, val, s, lane, GatherX<T>{x});
     const int32_t row = A.perm[s * kSellC + lane];
     if (row >= 0) {
       const T bi = b[row];
@@ -250,53 +284,50 @@ __global__ void __launch_bounds__(1024, 1) sell_pcg_init(SellView A, const T* __
   }
 }
 
-// p.Ap of the SpMV step: the sum of its per-block partials, formed by every
-// block of the consuming kernel in the same order, so that all blocks hold the
-// bitwise-same value without a grid-wide reduction in the SpMV kernel (the
-// last-block pass there adds a serial tail of a few microseconds).  Eight
-// independent loads per thread and trip keep the L2 round trips few.
-__device__ double sum_block_partials(const double* bpart, int nwp) {
-  __shared__ double red[32];
-  __shared__ double total;
-  double a[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-  const int T = blockDim.x;
-  int k = threadIdx.x;
-  for (; k + 7 * T < nwp; k += 8 * T) {
+// alpha = rz / p.Ap for the update kernels.  p.Ap is the sum of the SpMV
+// step's per-block partials, formed by warp 0 of every block of the consuming
+// kernel in the same order, so that all blocks hold the bitwise-same value
+// without a grid-wide reduction in the SpMV kernel (a last-block pass there
+// adds a serial tail of a few microseconds).  Warp 0 loads the partials
+// unrolled (a round trip per 608), adds them and lane 0 divides, so that the
+// FP64 work stays on one warp; it also reads the done flag (block 0 may set it
+// on breakdown while other blocks start), and one barrier hands both to the
+// block, so that all its threads take the same branch; the other warps issue
+// their first vector loads meanwhile.  Returns false (and block 0 marks the
+// solve done) on breakdown or non-finite values, or when the solve has already
+// ended: the block then returns without touching the vectors.
+__device__ bool block_alpha(const double* bpart, int nwp, SellPcgState* st, double* alpha) {
+  __shared__ double sh_alpha;
+  __shared__ int sh_ok;
+  constexpr int kPer = 19;
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    double acc = 0.0;
+    for (int base = 0; base < nwp; base += 32 * kPer) {
+      double v[kPer];
 #pragma unroll
-    for (int u = 0; u < 8; ++u) a[u] += __ldcg(bpart + k + u * T);
-  }
-  for (; k < nwp; k += T) a[0] += __ldcg(bpart + k);
-  double v = ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
-  v = block_sum(v, red);
-  if (threadIdx.x == 0) total = v;
-  __syncthreads();
-  return total;
-}
-
-// The done flag as one value for the whole block: in the update kernels block 0
-// may set it (breakdown) while other blocks start, and all threads of a block
-// must take the same branch before the block reductions.
-__device__ __forceinline__ bool block_done(const SellPcgState* st) {
-  __shared__ int d;
-  if (threadIdx.x == 0) d = *reinterpret_cast<const volatile int*>(&st->done);
-  __syncthreads();
-  return d != 0;
-}
-
-// alpha = rz / p.Ap for the update kernels; false (and the solve marked done
-// by block 0) on breakdown or non-finite values, in which case every block
-// returns without touching the vectors.
-__device__ bool step_alpha(const double* bpart, int nwp, SellPcgState* st, double* alpha) {
-  const double pap = sum_block_partials(bpart, nwp);
-  if (!(pap > 0.0) || !isfinite(pap)) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-      st->done = isfinite(pap) ? FGB_PCG_BREAKDOWN : FGB_PCG_NONFINITE;
-      st->alpha = 0.0;
+      for (int u = 0; u < kPer; ++u) {
+        const int k = base + lane + 32 * u;
+        v[u] = k < nwp ? __ldcg(bpart + k) : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < kPer; ++u) acc += v[u];
     }
-    return false;
+    const double pap = warp_sum(acc);
+    if (lane == 0) {
+      const int done = *reinterpret_cast<const volatile int*>(&st->done);
+      const bool ok = !done && pap > 0.0 && isfinite(pap);
+      if (!done && !ok && blockIdx.x == 0) {
+        st->done = isfinite(pap) ? FGB_PCG_BREAKDOWN : FGB_PCG_NONFINITE;
+        st->alpha = 0.0;
+      }
+      sh_ok = ok ? 1 : 0;
+      sh_alpha = ok ? st->rz / pap : 0.0;
+    }
   }
-  *alpha = st->rz / pap;
-  return true;
+  __syncthreads();
+  *alpha = sh_alpha;
+  return sh_ok != 0;
 }
 
 // kernel A: Ap = A p and per-block partials of p.Ap.  FUSED: p_new = z + beta p_old is
@@ -305,7 +336,7 @@ __device__ bool step_alpha(const double* bpart, int nwp, SellPcgState* st, doubl
 // updated in place by sell_p_update beforehand (used in FP64, where the FMA
 // rate of this part is low enough that a second FMA per entry would cost more
 // than the extra streaming pass over p).
-template <typename T, bool FUSED>
+template <typename T, bool FUSED, bool D16>
 __global__ void __launch_bounds__(1024, 1) sell_pcg_spmv(SellView A, const T* __restrict__ val,
                                                               const T* __restrict__ z, const T* __restrict__ p_old,
                                                               T* __restrict__ p_new, T* __restrict__ Ap,
@@ -318,11 +349,13 @@ __global__ void __launch_bounds__(1024, 1) sell_pcg_spmv(SellView A, const T* __
   __syncthreads();
   if (st->done) return;
   const T beta = static_cast<T>(st->beta);
-  double pap = 0.0;
+  // p.Ap partials in T per thread and warp (FP32 in the FP32 iterations: FP64
+  // arithmetic runs at a small fraction of the FP32 rate on this part), FP64
+  // from the warp sums on
+  T pap = T(0);
   SELL_WARP_LOOP(A) {
-    const int64_t base = A.slice_ptr[s] + lane;
-    const int w = static_cast<int>((A.slice_ptr[s + 1] - A.slice_ptr[s]) >> 5);
-    const T acc = FUSED ? sell_row_dot_p(A, val, base, w, z, p_old, beta) : sell_row_dot_x(A, val, base, w, p_old);
+    const T acc = FUSED ? slice_row<D16, T, T>(A, val, s, lane, GatherP<T>{z, p_old, beta})
+                        : slice_row<D16, T, T>(A, val, s, lane, GatherX<T>{p_old});
     const int32_t row = A.perm[s * kSellC + lane];
     if (row >= 0) {
       T pi;
@@ -333,13 +366,13 @@ __global__ void __launch_bounds__(1024, 1) sell_pcg_spmv(SellView A, const T* __
         pi = p_old[row];
       }
       Ap[row] = acc;
-      pap += static_cast<double>(pi) * static_cast<double>(acc);
+      pap += pi * acc;
     }
   }
   pap = warp_sum(pap);
   if (lane == 0) {
     const unsigned int nw = blockDim.x >> 5;
-    wslot[threadIdx.x >> 5] = pap;
+    wslot[threadIdx.x >> 5] = static_cast<double>(pap);
     __threadfence_block();
     if (atomicAdd(&arrivals, 1u) == nw - 1) {
       __threadfence_block();
@@ -368,31 +401,72 @@ __global__ void __launch_bounds__(1024, 1) sell_bnorm(int64_t n, const double* _
   }
 }
 
-// p = z + beta p, in place (FP64 solver, before kernel A)
+// p = z + beta p, in place (FP64 solver, before kernel A); 16-byte accesses
+// when both vectors are 16-byte aligned, the odd last row by thread 0
 __global__ void __launch_bounds__(1024, 1) sell_p_update(int64_t n, const double* __restrict__ z,
                                                               double* __restrict__ p, const SellPcgState* st) {
   if (st->done) return;
   const double beta = st->beta;
-  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
-       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
-    p[i] = z[i] + beta * p[i];
+  const int64_t tid = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  const int64_t n2 = aligned16(z, p) ? n >> 1 : 0;
+  const double2* Z = reinterpret_cast<const double2*>(z);
+  double2* P = reinterpret_cast<double2*>(p);
+  for (int64_t g = tid; g < n2; g += stride) {
+    const double2 zv = Z[g];
+    double2 pv = P[g];
+    pv.x = zv.x + beta * pv.x;
+    pv.y = zv.y + beta * pv.y;
+    P[g] = pv;
+  }
+  for (int64_t i = 2 * n2 + tid; i < n; i += stride) p[i] = z[i] + beta * p[i];
 }
 
-// kernel B (FP64 solver)
+// kernel B (FP64 solver).  Rows in pairs (16-byte accesses) when every vector
+// is 16-byte aligned; the first trip's loads are issued before alpha is known
+// (its sum over the SpMV partials ends in a block barrier).
 __global__ void __launch_bounds__(1024, 1) sell_pcg_update_f64(int64_t n, const double* __restrict__ dinv,
                                                                     const double* __restrict__ p,
                                                                     const double* __restrict__ Ap,
                                                                     double* __restrict__ x, double* __restrict__ r,
                                                                     double* __restrict__ z, const double* bpart,
                                                                     int nwp, double* partials, SellPcgState* st) {
-  if (block_done(st)) return;
+  const int64_t tid = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  const bool vec = aligned16(p, Ap) && aligned16(x, r) && aligned16(z, dinv ? dinv : z);
+  const int64_t n2 = vec ? n >> 1 : 0;
+  const double2* P = reinterpret_cast<const double2*>(p);
+  const double2* AP = reinterpret_cast<const double2*>(Ap);
+  double2* X = reinterpret_cast<double2*>(x);
+  double2* R = reinterpret_cast<double2*>(r);
+  double2* Z = reinterpret_cast<double2*>(z);
+  const double2* D = reinterpret_cast<const double2*>(dinv);
+  int64_t g = tid;
+  double2 pv, av, xv, rv, dv = make_double2(1.0, 1.0);
+  auto load = [&](int64_t gg) {
+    pv = P[gg]; av = AP[gg]; xv = X[gg]; rv = R[gg];
+    if (dinv) dv = __ldg(D + gg);
+  };
+  if (g < n2) load(g);
   double alpha;
-  if (!step_alpha(bpart, nwp, st, &alpha)) return;
+  if (!block_alpha(bpart, nwp, st, &alpha)) return;
   double rz = 0.0, rr = 0.0;
-  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
-       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-    const double pi = p[i];
-    x[i] += alpha * pi;
+  while (g < n2) {
+    xv.x += alpha * pv.x;
+    xv.y += alpha * pv.y;
+    rv.x -= alpha * av.x;
+    rv.y -= alpha * av.y;
+    const double2 zv = make_double2(dv.x * rv.x, dv.y * rv.y);
+    X[g] = xv;
+    R[g] = rv;
+    Z[g] = zv;
+    rz += rv.x * zv.x + rv.y * zv.y;
+    rr += rv.x * rv.x + rv.y * rv.y;
+    g += stride;
+    if (g < n2) load(g);
+  }
+  for (int64_t i = 2 * n2 + tid; i < n; i += stride) {
+    x[i] += alpha * p[i];
     const double ri = r[i] - alpha * Ap[i];
     const double zi = dinv ? dinv[i] * ri : ri;
     r[i] = ri;
@@ -429,13 +503,42 @@ __global__ void __launch_bounds__(1024, 1) sell_mixed_update(int64_t n, const fl
                                                                   const double* bpart, int nwp, double* partials,
                                                                   SellPcgState* st, double delta,
                                                                   cudaGraphConditionalHandle hif, int set_if) {
-  if (block_done(st)) return;
+  const int64_t tid = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  const bool vec = aligned16(p, Ap) && aligned16(y, r) && aligned16(z, dinv);
+  const int64_t n4 = vec ? n >> 2 : 0;
+  const float4* P = reinterpret_cast<const float4*>(p);
+  const float4* AP = reinterpret_cast<const float4*>(Ap);
+  float4* Y = reinterpret_cast<float4*>(y);
+  float4* R = reinterpret_cast<float4*>(r);
+  float4* Z = reinterpret_cast<float4*>(z);
+  const float4* D = reinterpret_cast<const float4*>(dinv);
+  // rows in fours (16-byte accesses); the first trip's loads are issued
+  // before alpha is known (its sum over the SpMV partials ends in a block
+  // barrier)
+  int64_t g = tid;
+  float4 pv, av, yv, rv, dv;
+  auto load = [&](int64_t gg) {
+    pv = P[gg]; av = AP[gg]; yv = Y[gg]; rv = R[gg]; dv = __ldg(D + gg);
+  };
+  if (g < n4) load(g);
   double alpha;
-  if (!step_alpha(bpart, nwp, st, &alpha)) return;
+  if (!block_alpha(bpart, nwp, st, &alpha)) return;
   const float alpha32 = static_cast<float>(alpha);
   float rz = 0.0f, rr = 0.0f;
-  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
-       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+  while (g < n4) {
+    yv.x += alpha32 * pv.x; yv.y += alpha32 * pv.y; yv.z += alpha32 * pv.z; yv.w += alpha32 * pv.w;
+    rv.x -= alpha32 * av.x; rv.y -= alpha32 * av.y; rv.z -= alpha32 * av.z; rv.w -= alpha32 * av.w;
+    const float4 zv = make_float4(dv.x * rv.x, dv.y * rv.y, dv.z * rv.z, dv.w * rv.w);
+    Y[g] = yv;
+    R[g] = rv;
+    Z[g] = zv;
+    rz += (rv.x * zv.x + rv.y * zv.y) + (rv.z * zv.z + rv.w * zv.w);
+    rr += (rv.x * rv.x + rv.y * rv.y) + (rv.z * rv.z + rv.w * rv.w);
+    g += stride;
+    if (g < n4) load(g);
+  }
+  for (int64_t i = 4 * n4 + tid; i < n; i += stride) {
     y[i] += alpha32 * p[i];
     const float ri = r[i] - alpha32 * Ap[i];
     const float zi = dinv[i] * ri;
@@ -445,7 +548,7 @@ __global__ void __launch_bounds__(1024, 1) sell_mixed_update(int64_t n, const fl
     rr += ri * ri;
   }
   double trz, trr;
-  if (sell_last_block(static_cast<double>(rz), static_cast<double>(rr), partials, &st->counter[2], &trz, &trr) &&
+  if (sell_last_block(rz, rr, partials, &st->counter[2], &trz, &trr) &&
       threadIdx.x == 0) {
     st->niter += 1;
     const double res = sqrt(trr);
@@ -486,7 +589,7 @@ __global__ void __launch_bounds__(1024, 1) sell_mixed_fold(int64_t n, double* __
 // FP32-assembled matrix, the operator the solve is for), true residual test,
 // then r = float(r64), z = Dinv r and beta from the replaced residual.  The
 // first call also builds the FP32 inverse diagonal and starts p = z.
-template <typename V>
+template <typename V, bool D16>
 __global__ void __launch_bounds__(1024, 1) sell_mixed_reliable(SellView A, const V* __restrict__ val,
                                                                     const double* __restrict__ b,
                                                                     const double* __restrict__ x,
@@ -497,9 +600,7 @@ __global__ void __launch_bounds__(1024, 1) sell_mixed_reliable(SellView A, const
   if (!first && (st->done || !st->need_update)) return;
   double rr64 = 0.0, rz = 0.0;
   SELL_WARP_LOOP(A) {
-    const int64_t base = A.slice_ptr[s] + lane;
-    const int w = static_cast<int>((A.slice_ptr[s + 1] - A.slice_ptr[s]) >> 5);
-    const double acc = sell_row_acc<V, double>(A.col, val, base - lane, w, lane, GatherX<double>{x});
+    const double acc = slice_row<D16, V, double>(A, val, s, lane, GatherX<double>{x});
     const int32_t row = A.perm[s * kSellC + lane];
     if (row >= 0) {
       const double r64 = b[row] - acc;
@@ -562,7 +663,7 @@ using namespace fgb;
 namespace {
 
 SellView view_of(const fgb_sell* A) {
-  return SellView{A->n, A->n_slices, A->slice_ptr, A->perm, A->col, A->threads, A->blocks};
+  return SellView{A->n, A->n_slices, A->slice_ptr, A->perm, A->col, A->threads, A->blocks, A->col16, A->col0};
 }
 
 bool launch_ok(const fgb_sell* A) {
@@ -705,7 +806,10 @@ void f64_body(const SellView& A, const double* val, const double* dinv, double* 
   rec(ev, 0, s);
   sell_p_update<<<VEC_LAUNCH(A.n, s)>>>(A.n, w.z, w.p0, w.st);
   rec(ev, 1, s);
-  sell_pcg_spmv<double, false><<<SLICE_LAUNCH(A, s)>>>(A, val, w.z, w.p0, nullptr, w.Ap, w.bpart, w.st);
+  with_cols(A, [&](auto d16) {
+    sell_pcg_spmv<double, false, decltype(d16)::value>
+        <<<SLICE_LAUNCH(A, s)>>>(A, val, w.z, w.p0, nullptr, w.Ap, w.bpart, w.st);
+  });
   rec(ev, 2, s);
   sell_pcg_update_f64<<<VEC_LAUNCH(A.n, s)>>>(A.n, dinv, w.p0, w.Ap, x, w.r, w.z, w.bpart, slice_blocks(A),
                                               w.partials, w.st);
@@ -724,19 +828,25 @@ void mixed_body(const SellView& A, const float* val32, const double* val64, cons
   const cudaGraphConditionalHandle hif = ctx ? ctx->new_handle() : 0;
   rec(ev, 0, s);
   rec(ev, 1, s);
-  sell_pcg_spmv<float, true><<<SLICE_LAUNCH(A, s)>>>(A, val32, w.z, p_old, p_new, w.Ap, w.bpart, w.st);
+  with_cols(A, [&](auto d16) {
+    sell_pcg_spmv<float, true, decltype(d16)::value>
+        <<<SLICE_LAUNCH(A, s)>>>(A, val32, w.z, p_old, p_new, w.Ap, w.bpart, w.st);
+  });
   rec(ev, 2, s);
   sell_mixed_update<<<VEC_LAUNCH(A.n, s)>>>(A.n, w.dinv32, p_new, w.Ap, w.y, w.r, w.z, w.bpart, slice_blocks(A),
                                             w.partials, w.st, delta, hif, ctx ? 1 : 0);
   rec(ev, 3, s);
   auto reliable = [&](cudaStream_t rs) {
     sell_mixed_fold<<<VEC_LAUNCH(A.n, rs)>>>(A.n, x, w.y, w.st, 0);
-    if (val64)
-      sell_mixed_reliable<double><<<SLICE_LAUNCH(A, rs)>>>(A, val64, b, x, dinv64, w.dinv32, w.r, w.z, nullptr,
-                                                           w.partials, w.st, 0);
-    else
-      sell_mixed_reliable<float><<<SLICE_LAUNCH(A, rs)>>>(A, val32, b, x, dinv64, w.dinv32, w.r, w.z, nullptr,
-                                                          w.partials, w.st, 0);
+    with_cols(A, [&](auto d16) {
+      constexpr bool D = decltype(d16)::value;
+      if (val64)
+        sell_mixed_reliable<double, D><<<SLICE_LAUNCH(A, rs)>>>(A, val64, b, x, dinv64, w.dinv32, w.r, w.z,
+                                                                nullptr, w.partials, w.st, 0);
+      else
+        sell_mixed_reliable<float, D><<<SLICE_LAUNCH(A, rs)>>>(A, val32, b, x, dinv64, w.dinv32, w.r, w.z,
+                                                               nullptr, w.partials, w.st, 0);
+    });
   };
   if (ctx) ctx->add_if(hif, reliable);
   else reliable(s);
@@ -858,12 +968,16 @@ int32_t fgb_sell_spmv(int32_t dtype, const fgb_sell* A, const void* x, void* y, 
   cudaStream_t st = as_stream(stream);
   if (dtype == FGB_F64) {
     if (!A->val64) return FGB_ERR_ARG;
-    sell_spmv_kernel<double><<<SLICE_LAUNCH(v, st)>>>(v, A->val64, static_cast<const double*>(x),
-                                                      static_cast<double*>(y));
+    with_cols(v, [&](auto d16) {
+      sell_spmv_kernel<double, decltype(d16)::value>
+          <<<SLICE_LAUNCH(v, st)>>>(v, A->val64, static_cast<const double*>(x), static_cast<double*>(y));
+    });
   } else if (dtype == FGB_F32) {
     if (!A->val32) return FGB_ERR_ARG;
-    sell_spmv_kernel<float><<<SLICE_LAUNCH(v, st)>>>(v, A->val32, static_cast<const float*>(x),
-                                                     static_cast<float*>(y));
+    with_cols(v, [&](auto d16) {
+      sell_spmv_kernel<float, decltype(d16)::value>
+          <<<SLICE_LAUNCH(v, st)>>>(v, A->val32, static_cast<const float*>(x), static_cast<float*>(y));
+    });
   } else {
     return FGB_ERR_ARG;
   }
@@ -898,7 +1012,10 @@ int32_t fgb_pcg_sell_f64(const fgb_sell* A, const double* diag_inv, const double
   h.trip_cap = maxit / 2 + 2;
   int64_t launches = 0;
   cudaMemcpyAsync(w.st, &h, sizeof(SellPcgState), cudaMemcpyHostToDevice, s);
-  sell_pcg_init<double><<<SLICE_LAUNCH(v, s)>>>(v, A->val64, diag_inv, b, x, w.r, w.z, w.p0, w.partials, w.st);
+  with_cols(v, [&](auto d16) {
+    sell_pcg_init<double, decltype(d16)::value>
+        <<<SLICE_LAUNCH(v, s)>>>(v, A->val64, diag_inv, b, x, w.r, w.z, w.p0, w.partials, w.st);
+  });
   ++launches;
   int rc = read_state(w.st, &h, s);
   if (rc) return rc;
@@ -981,12 +1098,15 @@ int32_t fgb_pcg_sell_mixed(const fgb_sell* A, const double* diag_inv64, const do
   } else {
     if ((rc = set_tol(w.st, rtol * h.b_norm, s))) return rc;
     // initial residual in FP64, its FP32 copy, z and p = z
-    if (A->val64)
-      sell_mixed_reliable<double><<<SLICE_LAUNCH(v, s)>>>(v, A->val64, b, x, diag_inv64, w.dinv32, w.r, w.z, w.p0,
-                                                          w.partials, w.st, 1);
-    else
-      sell_mixed_reliable<float><<<SLICE_LAUNCH(v, s)>>>(v, A->val32, b, x, diag_inv64, w.dinv32, w.r, w.z, w.p0,
-                                                         w.partials, w.st, 1);
+    with_cols(v, [&](auto d16) {
+      constexpr bool D = decltype(d16)::value;
+      if (A->val64)
+        sell_mixed_reliable<double, D><<<SLICE_LAUNCH(v, s)>>>(v, A->val64, b, x, diag_inv64, w.dinv32, w.r, w.z,
+                                                               w.p0, w.partials, w.st, 1);
+      else
+        sell_mixed_reliable<float, D><<<SLICE_LAUNCH(v, s)>>>(v, A->val32, b, x, diag_inv64, w.dinv32, w.r, w.z,
+                                                              w.p0, w.partials, w.st, 1);
+    });
     ++launches;
     bool graphed = false;
     if (use_graph) {

@@ -111,6 +111,95 @@ __device__ __forceinline__ T sell_row(const int32_t* __restrict__ col, const T* 
   return sell_row_acc<T, T, G>(col, val, sbase, w, lane, g);
 }
 
+// ------------------------------------------------ delta-coded column indices
+// Columns of a row sorted ascending and stored as 16-bit steps: the column of
+// entry k is c0 + d[0] + ... + d[k] (c0 per slot, the row's first column;
+// d = 0 for the first entry and for padding, which therefore gathers the
+// last real column again, with a zero value).  A step above 65535 is bridged
+// by zero-valued entries of step 65535.  2 bytes per entry instead of 4.
+struct Pack4FH {
+  uint2 d;
+  float4 v;
+};
+struct Pack4DH {
+  uint2 d;
+  double2 v01, v23;
+};
+
+__device__ __forceinline__ Pack4FH load_pack_d16(const uint16_t* d16, const float* val, int64_t sbase, int lane,
+                                                 int q) {
+  const int64_t off = sbase + static_cast<int64_t>(q) * (kSellC * kSellPack) + lane * kSellPack;
+  Pack4FH p;
+  p.d = __ldcs(reinterpret_cast<const uint2*>(d16 + off));
+  p.v = __ldcs(reinterpret_cast<const float4*>(val + off));
+  return p;
+}
+
+__device__ __forceinline__ Pack4DH load_pack_d16(const uint16_t* d16, const double* val, int64_t sbase, int lane,
+                                                 int q) {
+  const int64_t off = sbase + static_cast<int64_t>(q) * (kSellC * kSellPack) + lane * kSellPack;
+  Pack4DH p;
+  p.d = __ldcs(reinterpret_cast<const uint2*>(d16 + off));
+  p.v01 = __ldcs(reinterpret_cast<const double2*>(val + off));
+  p.v23 = __ldcs(reinterpret_cast<const double2*>(val + off + 2));
+  return p;
+}
+
+template <typename T, typename G>
+__device__ __forceinline__ T pack_dot_d16(const Pack4FH& p, const G& g, int32_t& c, T acc) {
+  c += static_cast<int32_t>(p.d.x & 0xffffu);
+  acc += p.v.x * g(c);
+  c += static_cast<int32_t>(p.d.x >> 16);
+  acc += p.v.y * g(c);
+  c += static_cast<int32_t>(p.d.y & 0xffffu);
+  acc += p.v.z * g(c);
+  c += static_cast<int32_t>(p.d.y >> 16);
+  acc += p.v.w * g(c);
+  return acc;
+}
+
+template <typename T, typename G>
+__device__ __forceinline__ T pack_dot_d16(const Pack4DH& p, const G& g, int32_t& c, T acc) {
+  c += static_cast<int32_t>(p.d.x & 0xffffu);
+  acc += p.v01.x * g(c);
+  c += static_cast<int32_t>(p.d.x >> 16);
+  acc += p.v01.y * g(c);
+  c += static_cast<int32_t>(p.d.y & 0xffffu);
+  acc += p.v23.x * g(c);
+  c += static_cast<int32_t>(p.d.y >> 16);
+  acc += p.v23.y * g(c);
+  return acc;
+}
+
+template <typename T> struct PackD16Of;
+template <> struct PackD16Of<float> { using type = Pack4FH; };
+template <> struct PackD16Of<double> { using type = Pack4DH; };
+
+// As sell_row_acc, with delta-coded columns starting from c0.
+template <typename V, typename T, typename G>
+__device__ __forceinline__ T sell_row_acc_d16(const uint16_t* __restrict__ d16, int32_t c0,
+                                              const V* __restrict__ val, int64_t sbase, int w, int lane,
+                                              const G& g) {
+  using P = typename PackD16Of<V>::type;
+  constexpr int U = PacksPerTrip<V>::value;
+  const int nq = w / kSellPack;
+  T acc = T(0);
+  int32_t c = c0;
+  int q = 0;
+  for (; q + U <= nq; q += U) {
+    P a[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) a[u] = load_pack_d16(d16, val, sbase, lane, q + u);
+#pragma unroll
+    for (int u = 0; u < U; ++u) acc = pack_dot_d16<T>(a[u], g, c, acc);
+  }
+  for (; q < nq; ++q) {
+    const P a = load_pack_d16(d16, val, sbase, lane, q);
+    acc = pack_dot_d16<T>(a, g, c, acc);
+  }
+  return acc;
+}
+
 template <typename T>
 struct GatherX {
   const T* __restrict__ x;

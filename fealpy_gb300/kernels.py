@@ -226,18 +226,57 @@ def gather_sum(adj_ptr, adj, local: torch.Tensor, out: Optional[torch.Tensor] = 
 
 class SellMatrix:
     """Device SELL-32 copy of a CSR matrix (tensors kept alive here) and the
-    ``fgb_sell`` descriptor pointing at them."""
+    ``fgb_sell`` descriptor pointing at them.
 
-    def __init__(self, n, n_slices, slice_ptr, perm, col, val64, val32):
+    With 4-byte columns (``col``) the copy is in the matrix's own numbering.
+    The delta-coded copy (``col16`` + ``col0``) is of P A P^T for the
+    locality renumbering ``order`` (new row k = old row order[k]); the solver
+    and SpMV wrappers below permute vectors into and out of that numbering."""
+
+    def __init__(self, n, n_slices, slice_ptr, perm, col, val64, val32, col16=None, col0=None, order=None,
+                 nnz=None):
         self.n, self.n_slices = n, n_slices
         self.slice_ptr, self.perm, self.col, self.val64, self.val32 = slice_ptr, perm, col, val64, val32
-        self.desc = _lib.SellDesc(n, n_slices, slice_ptr.data_ptr(), perm.data_ptr(), col.data_ptr(),
+        self.col16, self.col0, self.order, self.nnz = col16, col0, order, nnz
+        self.desc = _lib.SellDesc(n, n_slices, slice_ptr.data_ptr(), perm.data_ptr(),
+                                  col.data_ptr() if col is not None else None,
                                   val64.data_ptr() if val64 is not None else None,
-                                  val32.data_ptr() if val32 is not None else None, 0, 0)
+                                  val32.data_ptr() if val32 is not None else None, 0, 0,
+                                  col16.data_ptr() if col16 is not None else None,
+                                  col0.data_ptr() if col0 is not None else None)
+
+    @property
+    def d16(self) -> bool:
+        return self.col16 is not None
+
+    @property
+    def device(self):
+        return self.slice_ptr.device
 
     @property
     def padded_nnz(self):
-        return self.col.numel()
+        return (self.col16 if self.col16 is not None else self.col).numel()
+
+    def to_inner(self, v: torch.Tensor) -> torch.Tensor:
+        """A vector in the copy's numbering (a new tensor when renumbered)."""
+        if self.order is None or v is None:
+            return v
+        v = v.contiguous()
+        out = torch.empty_like(v)
+        call("fgb_permute", dtype_code(v.dtype), self.n, ptr(self.order), ptr(v), ptr(out), 0, stream_ptr(v.device))
+        return out
+
+    def to_outer(self, v: torch.Tensor, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+        """Back to the matrix's own numbering (into ``out`` if given)."""
+        if self.order is None:
+            if out is not None and out is not v:
+                out.copy_(v)
+                return out
+            return v
+        res = out if out is not None else torch.empty_like(v)
+        call("fgb_permute", dtype_code(v.dtype), self.n, ptr(self.order), ptr(v.contiguous()), ptr(res), 1,
+             stream_ptr(v.device))
+        return res
 
     def set_launch(self, threads: int = 0, blocks: int = 0):
         """Launch shape of the slice kernels (0, 0 = library defaults)."""
@@ -262,7 +301,7 @@ def sell_autotune(S: SellMatrix, dtype=torch.float32, reps: int = 20, candidates
     """Pick the launch shape of the slice kernels by timing the SELL SpMV with
     CUDA events on the current stream (after one warm-up call per shape).
     Sets it on ``S`` and returns ``{(threads, blocks): microseconds}``."""
-    dev = S.col.device
+    dev = S.device
     x = torch.rand(S.n, dtype=dtype, device=dev)
     y = torch.empty(S.n, dtype=dtype, device=dev)
     code = dtype_code(dtype)
@@ -284,11 +323,23 @@ def sell_autotune(S: SellMatrix, dtype=torch.float32, reps: int = 20, candidates
     return times
 
 
-def sell_build(indptr, indices, values64=None, values32=None, want64=True, want32=False) -> SellMatrix:
-    """SELL-32 copy of a CSR matrix (one host read for the padded size)."""
+# A delta-coded copy is kept when its entries (with bridges) are at most this
+# many times the nonzeros: 6 bytes per entry against 8.
+D16_MAX_GROWTH = 1.25
+
+
+def sell_build(indptr, indices, values64=None, values32=None, want64=True, want32=False,
+               d16: Optional[bool] = None) -> SellMatrix:
+    """SELL-32 copy of a CSR matrix.  ``d16``: True = delta-coded columns of
+    the renumbered matrix, False = 4-byte columns, None = delta-coded when
+    the bridges add at most 25% entries (two host reads for the sizes)."""
     dev = _dev(indptr)
     n = indptr.numel() - 1
     lib = _lib.lib()
+    if d16 is None or d16:
+        S = _sell_build_d16(indptr, indices, values64, values32, want64, want32, force=bool(d16))
+        if S is not None:
+            return S
     slots = int(lib.fgb_sell_slots(n))
     n_slices = slots // 32
     perm = torch.empty(slots, dtype=torch.int32, device=dev)
@@ -301,37 +352,89 @@ def sell_build(indptr, indices, values64=None, values32=None, want64=True, want3
     v32 = torch.empty(max(total, 1), dtype=torch.float32, device=dev) if want32 else None
     call("fgb_sell_fill", n, ptr(indptr), ptr(indices), ptr(values64), ptr(values32), ptr(perm), ptr(slice_ptr),
          ptr(col), ptr(v64), ptr(v32), stream_ptr(dev))
-    return SellMatrix(n, n_slices, slice_ptr, perm, col, v64, v32)
+    return SellMatrix(n, n_slices, slice_ptr, perm, col, v64, v32, nnz=indices.numel())
+
+
+def _sell_build_d16(indptr, indices, values64, values32, want64, want32, force=False,
+                    renumber=True) -> Optional[SellMatrix]:
+    """Delta-coded copy of P A P^T (None when not worth it and not forced).
+    ``renumber=False`` keeps the matrix's own numbering (columns must be
+    ascending in every row; steps above 65535 are bridged)."""
+    dev = _dev(indptr)
+    n = indptr.numel() - 1
+    nnz = indices.numel()
+    lib = _lib.lib()
+    s = stream_ptr(dev)
+    ws = workspace(max(lib.fgb_sell_d16_workspace_bytes(n), lib.fgb_sell_workspace_bytes(n)), dev)
+    if renumber:
+        order = torch.empty(n, dtype=torch.int32, device=dev)
+        inv = torch.empty(n, dtype=torch.int32, device=dev)
+        call("fgb_sell_renumber", n, ptr(indptr), ptr(indices), ptr(order), ptr(inv), ptr(ws), ws.numel(), s)
+        p_indptr = torch.empty(n + 1, dtype=torch.int64, device=dev)
+        p_indices = torch.empty(max(nnz, 1), dtype=torch.int32, device=dev)
+        p64 = torch.empty(max(nnz, 1), dtype=torch.float64, device=dev) if want64 else None
+        p32 = torch.empty(max(nnz, 1), dtype=torch.float32, device=dev) if want32 else None
+        call("fgb_csr_permute", n, ptr(indptr), ptr(indices), ptr(values64), ptr(values32), ptr(order), ptr(inv),
+             ptr(p_indptr), ptr(p_indices), ptr(p64), ptr(p32), ptr(ws), ws.numel(), s)
+        del inv
+    else:
+        order, p_indptr, p_indices, p64, p32 = None, indptr, indices, values64, values32
+    b_indptr = torch.empty(n + 1, dtype=torch.int64, device=dev)
+    call("fgb_sell_d16_indptr", n, ptr(p_indptr), ptr(p_indices), ptr(b_indptr), ptr(ws), ws.numel(), s)
+    if not force and int(b_indptr[n].item()) > D16_MAX_GROWTH * max(nnz, 1):
+        return None
+    slots = int(lib.fgb_sell_slots(n))
+    n_slices = slots // 32
+    perm = torch.empty(slots, dtype=torch.int32, device=dev)
+    slice_ptr = torch.empty(n_slices + 1, dtype=torch.int64, device=dev)
+    call("fgb_sell_plan", n, ptr(b_indptr), ptr(perm), ptr(slice_ptr), ptr(ws), ws.numel(), s)
+    total = int(slice_ptr[n_slices].item())
+    col0 = torch.empty(slots, dtype=torch.int32, device=dev)
+    col16 = torch.empty(max(total, 4), dtype=torch.int16, device=dev)
+    v64 = torch.empty(max(total, 1), dtype=torch.float64, device=dev) if want64 else None
+    v32 = torch.empty(max(total, 1), dtype=torch.float32, device=dev) if want32 else None
+    call("fgb_sell_fill_d16", n, ptr(p_indptr), ptr(p_indices), ptr(p64), ptr(p32), ptr(perm), ptr(slice_ptr),
+         ptr(col0), ptr(col16), ptr(v64), ptr(v32), s)
+    return SellMatrix(n, n_slices, slice_ptr, perm, None, v64, v32, col16=col16, col0=col0, order=order, nnz=nnz)
 
 
 def sell_spmv(S: SellMatrix, x, dtype=torch.float64):
-    dev = S.col.device
+    """y = A x in the matrix's own numbering."""
+    dev = S.device
+    x = S.to_inner(x.to(dev, dtype).contiguous())
     y = torch.empty(S.n, dtype=dtype, device=dev)
-    x = x.to(dev, dtype).contiguous()
     call("fgb_sell_spmv", dtype_code(dtype), ctypes.byref(S.desc), ptr(x), ptr(y), stream_ptr(dev))
-    return y
+    return S.to_outer(y)
 
 
 def pcg_sell_f64(S: SellMatrix, dinv, b, x, atol, rtol, maxit, check_every=16, norm=0, graph=True, profile=False):
-    dev = S.col.device
+    """Jacobi-PCG in FP64 on the SELL copy; dinv, b and x (updated in place)
+    in the matrix's own numbering."""
+    dev = S.device
     lib = _lib.lib()
     ws = workspace(lib.fgb_pcg_sell_workspace_bytes(S.n), dev)
     info = _lib.PcgInfo()
-    call("fgb_pcg_sell_f64", ctypes.byref(S.desc), ptr(dinv), ptr(b), ptr(x), float(atol), float(rtol), int(maxit),
+    di, bi, xi = S.to_inner(dinv), S.to_inner(b), S.to_inner(x)
+    call("fgb_pcg_sell_f64", ctypes.byref(S.desc), ptr(di), ptr(bi), ptr(xi), float(atol), float(rtol), int(maxit),
          int(check_every), int(norm), int(bool(graph)), int(bool(profile)), ptr(ws), ws.numel(), ctypes.byref(info),
          stream_ptr(dev))
+    S.to_outer(xi, out=x)
     _lib.add_launches(info.launches)
     return info
 
 
 def pcg_sell_mixed(S: SellMatrix, dinv64, b, x, rtol, delta=0.1, maxit=100000, check_every=32, graph=True,
                    profile=False):
-    dev = S.col.device
+    """FP32 Jacobi-PCG with FP64 reliable updates on the SELL copy; dinv64, b
+    and x (updated in place) in the matrix's own numbering."""
+    dev = S.device
     lib = _lib.lib()
     ws = workspace(lib.fgb_pcg_sell_workspace_bytes(S.n), dev)
     info = _lib.PcgInfo()
-    call("fgb_pcg_sell_mixed", ctypes.byref(S.desc), ptr(dinv64), ptr(b), ptr(x), float(rtol), float(delta),
+    di, bi, xi = S.to_inner(dinv64), S.to_inner(b), S.to_inner(x)
+    call("fgb_pcg_sell_mixed", ctypes.byref(S.desc), ptr(di), ptr(bi), ptr(xi), float(rtol), float(delta),
          int(maxit), int(check_every), int(bool(graph)), int(bool(profile)), ptr(ws), ws.numel(), ctypes.byref(info),
          stream_ptr(dev))
+    S.to_outer(xi, out=x)
     _lib.add_launches(info.launches)
     return info

@@ -53,6 +53,10 @@ def _info_dict(info, extra=None):
 # type), found once by timing the candidates (kernels.sell_autotune) and
 # reused for every later matrix of the same size.
 _LAUNCH_CACHE = {}
+# column format of the solvers' SELL copies: None = delta-coded columns of the
+# renumbered matrix where the bridges add at most 25% entries, False = 4-byte
+# columns, True = delta-coded always
+SELL_D16: Optional[bool] = None
 
 
 def _sell_of(A: CSRTensor, want32: bool, tune: bool = True):
@@ -62,14 +66,15 @@ def _sell_of(A: CSRTensor, want32: bool, tune: bool = True):
     if S is None or (want32 and S.val32 is None) or (not want32 and S.val64 is None):
         if A.values.dtype == torch.float32 and want32:
             # FP32-assembled operator: the FP32 values are the matrix (no FP64 copy)
-            S = K.sell_build(A.crow, A.col, None, A.values.contiguous(), want64=False, want32=True)
+            S = K.sell_build(A.crow, A.col, None, A.values.contiguous(), want64=False, want32=True, d16=SELL_D16)
         else:
             v32 = A._f32 if (want32 and A._f32 is not None) else None
-            S = K.sell_build(A.crow, A.col, A.values.to(torch.float64).contiguous(), v32, want64=True, want32=want32)
+            S = K.sell_build(A.crow, A.col, A.values.to(torch.float64).contiguous(), v32, want64=True, want32=want32,
+                             d16=SELL_D16)
         A._sell = S
         if tune:
             dt = torch.float32 if want32 else torch.float64
-            key = (S.n, S.padded_nnz, dt)
+            key = (S.n, S.padded_nnz, dt, S.d16)
             shape = _LAUNCH_CACHE.get(key)
             if shape is None:
                 times = K.sell_autotune(S, dt)

@@ -301,6 +301,9 @@ typedef struct fgb_sell {
   int32_t threads;          /* launch shape of the slice kernels (SpMV, PCG   */
   int32_t blocks;           /* residual/SpMV steps); 0 = defaults.  threads a */
                             /* multiple of 32 in [32, 1024], blocks <= 1216   */
+  const uint16_t* col16;    /* delta-coded columns (col unused) or NULL:      */
+  const int32_t* col0;      /* column of entry k = col0[slot] + sum of the    */
+                            /* steps col16 up to k (fgb_sell_fill_d16)        */
 } fgb_sell;
 
 /* No FEALPy counterpart: a solver-side layout of CSRTensor (the matrix the
@@ -315,6 +318,36 @@ int32_t fgb_sell_fill(int64_t n, const int64_t* indptr, const int32_t* indices,
                       const int64_t* slice_ptr, int32_t* col, double* val64, float* val32,
                       void* stream);
 int32_t fgb_sell_spmv(int32_t dtype, const fgb_sell* A, const void* x, void* y, void* stream);
+
+/* Delta-coded SELL copy: 2-byte column steps instead of 4-byte columns, for
+ * a matrix renumbered so that the steps are small.  No FEALPy counterpart
+ * (solver-side layout, as above); the solve is the same Jacobi-PCG on
+ * P A P^T with b, x and the inverse diagonal permuted alike.
+ *   renumber: order[k] = old index of new row k: rows sorted by (smallest
+ *     column, row), which interleaves the node, edge, face and cell dofs of
+ *     FEALPy's numbering by location (identity when a group of equal keys
+ *     exceeds 64 rows); inv = its inverse.
+ *   csr_permute: rows order[k] of the CSR with columns inv[col], ascending.
+ *   d16_indptr: row pointer of the row lengths including the zero-valued
+ *     bridge entries that split steps above 65535 (for fgb_sell_plan).
+ *   fill_d16: col0/col16 and values of the plan's slots.
+ *   permute: dst[k] = src[order[k]] (scatter = 0) or dst[order[k]] = src[k]. */
+size_t fgb_sell_d16_workspace_bytes(int64_t n);
+int32_t fgb_sell_renumber(int64_t n, const int64_t* indptr, const int32_t* indices, int32_t* order,
+                          int32_t* inv, void* workspace, size_t workspace_bytes, void* stream);
+int32_t fgb_csr_permute(int64_t n, const int64_t* indptr, const int32_t* indices, const double* values64,
+                        const float* values32, const int32_t* order, const int32_t* inv,
+                        int64_t* new_indptr, int32_t* new_indices, double* new_values64,
+                        float* new_values32, void* workspace, size_t workspace_bytes, void* stream);
+int32_t fgb_sell_d16_indptr(int64_t n, const int64_t* indptr, const int32_t* indices,
+                            int64_t* bridged_indptr, void* workspace, size_t workspace_bytes,
+                            void* stream);
+int32_t fgb_sell_fill_d16(int64_t n, const int64_t* indptr, const int32_t* indices,
+                          const double* values64, const float* values32, const int32_t* perm,
+                          const int64_t* slice_ptr, int32_t* col0, uint16_t* col16, double* val64,
+                          float* val32, void* stream);
+int32_t fgb_permute(int32_t dtype, int64_t n, const int32_t* order, const void* src, void* dst,
+                    int32_t scatter, void* stream);
 
 /* Jacobi-PCG on a SELL copy: same iteration, stopping rules and info as
  * fgb_pcg_f64 / fgb_pcg_mixed.  use_graph != 0 runs the iterations as a CUDA

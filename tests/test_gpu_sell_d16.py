@@ -1,0 +1,149 @@
+"""Delta-coded SELL copy (fealpy_gb300.kernels.sell_build(d16=True)): the
+locality renumbering is a permutation and deterministic, the renumbered copy
+multiplies like the CSR matrix (FP64 within 1e-14 of scipy; FP32 within
+1e-5), steps above 65535 are bridged, rows above the shared-memory stage and
+key groups above 64 rows take their fallbacks, and the solvers on the
+renumbered copy give the solution in the caller's numbering."""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def cuda():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch.device("cuda:0")
+
+
+def rel_err(a, b):
+    a = a.detach().cpu().numpy() if isinstance(a, torch.Tensor) else np.asarray(a)
+    b = np.asarray(b)
+    return np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
+
+
+def _spd(n, extra_cols, seed=0):
+    """Symmetric diagonally dominant CSR: a 1-D Laplacian plus symmetric
+    couplings (i, j) for the given extra column offsets (wrapped)."""
+    import scipy.sparse as sp
+    rng = np.random.default_rng(seed)
+    rows, cols = [np.arange(n - 1)], [np.arange(1, n)]
+    for off in extra_cols:
+        i = np.arange(n)
+        j = (i + off) % n
+        keep = i < j
+        rows.append(i[keep])
+        cols.append(j[keep])
+    r = np.concatenate(rows)
+    c = np.concatenate(cols)
+    v = -rng.uniform(0.1, 1.0, size=r.size)
+    A = sp.coo_matrix((np.concatenate([v, v]), (np.concatenate([r, c]), np.concatenate([c, r]))), shape=(n, n)).tocsr()
+    A.sum_duplicates()
+    d = np.asarray(-A.sum(axis=1)).ravel() + 1.0
+    A = (A + sp.diags(d)).tocsr()
+    A.sort_indices()
+    return A
+
+
+def _build(A, dev, d16, want32=True):
+    from fealpy_gb300 import kernels as K
+    t = lambda a: torch.as_tensor(a, device=dev)
+    return K.sell_build(t(A.indptr.astype(np.int64)), t(A.indices.astype(np.int32)), t(A.data), None, want64=True,
+                        want32=want32, d16=d16)
+
+
+def _check_spmv(S, A, dev):
+    from fealpy_gb300 import kernels as K
+    x = np.random.default_rng(5).normal(size=A.shape[0])
+    ref = A @ x
+    assert rel_err(K.sell_spmv(S, torch.as_tensor(x, device=dev), torch.float64), ref) < 1e-14
+    assert rel_err(K.sell_spmv(S, torch.as_tensor(x, device=dev, dtype=torch.float32), torch.float32), ref) < 1e-5
+
+
+def test_d16_golden_matrices_match_csr(golden_dir):
+    dev = cuda()
+    import scipy.sparse as sp
+    for name in ("small_tet_p2.npz", "small_tri_p3.npz", "c1_poisson_tri_p1_64.npz"):
+        z = np.load(os.path.join(golden_dir, name))
+        n = len(z["crow"]) - 1
+        A = sp.csr_matrix((z["val"], z["col"], z["crow"]), shape=(n, n))
+        S = _build(A, dev, True)
+        assert S.d16 and S.order is not None and S.padded_nnz >= A.nnz
+        order = S.order.cpu().numpy()
+        assert np.array_equal(np.sort(order), np.arange(n))
+        S2 = _build(A, dev, True)
+        assert torch.equal(S.order, S2.order) and torch.equal(S.col16, S2.col16) and torch.equal(S.val64, S2.val64)
+        _check_spmv(S, A, dev)
+
+
+def test_d16_bridges_long_rows_and_identity_fallback():
+    dev = cuda()
+    import scipy.sparse as sp
+    from fealpy_gb300 import kernels as K
+    # couplings 150000 apart in a 400000-row matrix: the renumbering puts the
+    # coupled rows next to each other; kept in its own numbering, every
+    # coupled row needs two bridges
+    A = _spd(400000, [150000])
+    S = _build(A, dev, True)
+    assert S.order is not None and S.padded_nnz >= A.nnz
+    _check_spmv(S, A, dev)
+    t = lambda a: torch.as_tensor(a, device=dev)
+    S = K._sell_build_d16(t(A.indptr.astype(np.int64)), t(A.indices.astype(np.int32)), t(A.data), None, True, True,
+                          force=True, renumber=False)
+    assert S.order is None and S.padded_nnz >= A.nnz + 2 * 250000
+    _check_spmv(S, A, dev)
+    # one row with 3000 entries (above the 1024-entry stage) and its column
+    B = _spd(20000, [7]).tolil()
+    cols = np.arange(0, 20000, 7)[:3000]
+    B[5, cols] = -1e-3
+    B[cols, 5] = -1e-3
+    B = B.tocsr()
+    B = (B + sp.diags(np.abs(B).sum(axis=1).A.ravel())).tocsr()
+    B.sort_indices()
+    _check_spmv(_build(B, dev, True), B, dev)
+    # an arrow matrix: every row's smallest column is 0 (one key group of all
+    # rows), so the renumbering falls back to the identity
+    n = 5000
+    C = sp.lil_matrix((n, n))
+    C.setdiag(float(n))
+    C[0, :] = 1.0
+    C[:, 0] = 1.0
+    C[0, 0] = float(n) * 2
+    C = C.tocsr()
+    C.sort_indices()
+    S = _build(C, dev, True)
+    assert np.array_equal(S.order.cpu().numpy(), np.arange(n))
+    _check_spmv(S, C, dev)
+
+
+def test_d16_solvers_match_int32_columns(golden_dir):
+    """cg (FP64) and cg_mixed on the renumbered copy: same stopping test,
+    solution in the caller's numbering, within 1e-9 of the 4-byte-column
+    solve."""
+    dev = cuda()
+    import fealpy_gb300 as F
+    from fealpy_gb300 import solver as SV
+    from fealpy_gb300.sparse import CSRTensor
+    z = np.load(os.path.join(golden_dir, "c1_poisson_tri_p1_64.npz"))
+    out = {}
+    old = SV.SELL_D16
+    try:
+        for mode in (False, True):
+            SV.SELL_D16 = mode
+            A = CSRTensor(torch.as_tensor(z["bc_crow"], device=dev), torch.as_tensor(z["bc_col"], device=dev),
+                          torch.as_tensor(z["bc_val"], device=dev), (len(z["bc_crow"]) - 1,) * 2)
+            b = torch.as_tensor(z["bc_F"], device=dev)
+            x64, i64 = F.cg(A, b, M=F.JacobiPreconditioner().apply(A), atol=1e-30, rtol=1e-10, returninfo=True)
+            assert A._sell.d16 == mode
+            xm, im = F.cg_mixed(A, b, rtol=1e-10, returninfo=True)
+            assert im["relres"] <= 1e-10
+            out[mode] = (x64, i64["niter"], xm)
+    finally:
+        SV.SELL_D16 = old
+    assert abs(out[True][1] - out[False][1]) <= 1
+    assert rel_err(out[True][0], out[False][0].cpu().numpy()) < 1e-9
+    assert rel_err(out[True][2], out[False][2].cpu().numpy()) < 1e-8
+    assert rel_err(out[True][0], z["uh"]) < 1e-9
