@@ -208,6 +208,8 @@ def run_ours(args):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
 
+    from fealpy_gb300 import solver as SV
+    SV.SELL_D16 = {"auto": None, "i32": False, "d16": True}[args.sell_cols]
     n = args.n
     node_np, cell_np, kappa_np = diffusion_mass_tet_box(n)
     mesh, space, kappa, bc = build_problem(torch, F, node_np, cell_np, kappa_np, dev)
@@ -272,14 +274,16 @@ def run_ours(args):
                          "other_ms_avg": pinfo["other_ms"] / max(kl, 1),
                          "extra_ms_avg": pinfo["extra_ms"] / max(kl, 1), "stages_ms": stages,
                          "clocks": clocks, "nnz": A2.nnz, "n": gdof,
-                         "sell_launch": list(A2._sell.launch) if getattr(A2, "_sell", None) is not None else None}
+                         "sell_launch": list(A2._sell.launch) if getattr(A2, "_sell", None) is not None else None,
+                         "sell_cols": ("d16" if A2._sell.d16 else "i32") if getattr(A2, "_sell", None) is not None
+                         else None}
 
     if set(modes) != {"fp64", "mixed"} or args.no_e2e:
         # profiling run: report the per-mode timings on stderr only
         for m, r in results.items():
             print(f"[profile run] {m}: {r['ms_per_step']:.3f} ms/step, {r['niter']} iterations, "
                   f"relres {r['relres']:.3e}, spmv avg {r['kernel_ms_avg'] * 1e3:.1f} us, update "
-                  f"{r['other_ms_avg'] * 1e3:.1f} us, other {r['extra_ms_avg'] * 1e3:.1f} us, "
+                  f"{r['other_ms_avg'] * 1e3:.1f} us, other {r['extra_ms_avg'] * 1e3:.1f} us, cols {r['sell_cols']}, "
                   f"stages {json.dumps(r['stages_ms'])}", file=sys.stderr)
         if world > 1:
             dist.destroy_process_group()
@@ -327,15 +331,18 @@ def run_ours(args):
     value = replica_value(gdof, world, mixed["ms_per_step"])
     # dominant kernel: the fused FP32 PCG SpMV (p = z + beta p_old, Ap = A p, p.Ap)
     nnz = mixed["nnz"]
-    # values + columns of the real entries, the slot->row map, z and p_old read
-    # once, p_new and Ap written once (FP32 vectors)
-    bytes_per_launch = nnz * (4 + 4) + gdof * (4 + 4 * 4)
+    # values + columns of the real entries (4-byte columns, or 2-byte steps plus
+    # a first column per row), the slot->row map, z and p_old read once, p_new
+    # and Ap written once (FP32 vectors)
+    d16 = mixed["sell_cols"] == "d16"
+    bytes_per_launch = nnz * (4 + 2) + gdof * (4 + 4 + 4 * 4) if d16 else nnz * (4 + 4) + gdof * (4 + 4 * 4)
     achieved = bytes_per_launch / (mixed["kernel_ms_avg"] / 1e3) / 1e9 if mixed["kernel_ms_avg"] > 0 else 0.0
     traffic = None
     tp = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tp) and n == 64:
         try:
-            traffic = json.load(open(tp)).get("pcg_spmv_f32_bytes_per_launch_at_n64")
+            traffic = json.load(open(tp)).get("pcg_spmv_f32_d16_bytes_per_launch_at_n64" if d16 else
+                                              "pcg_spmv_f32_bytes_per_launch_at_n64")
         except Exception:
             traffic = None
 
@@ -362,19 +369,20 @@ def run_ours(args):
                              "max_rel_err_vs_fp64": err, "stages_ms": mixed["stages_ms"],
                              "spmv_us": mixed["kernel_ms_avg"] * 1e3, "update_us": mixed["other_ms_avg"] * 1e3,
                              "other_kernels_us": mixed["extra_ms_avg"] * 1e3,
-                             "sell_launch_threads_blocks": mixed["sell_launch"]},
+                             "sell_launch_threads_blocks": mixed["sell_launch"], "sell_columns": mixed["sell_cols"]},
             "fp64": {"ms_per_step": fp64["ms_per_step"], "dof_per_s": world * gdof / (fp64["ms_per_step"] / 1e3),
                      "cg_iters": fp64["niter"], "true_relres": fp64["relres"], "stages_ms": fp64["stages_ms"],
                      "spmv_us": fp64["kernel_ms_avg"] * 1e3, "update_us": fp64["other_ms_avg"] * 1e3,
                      "other_kernels_us": fp64["extra_ms_avg"] * 1e3,
-                     "sell_launch_threads_blocks": fp64["sell_launch"]},
+                     "sell_launch_threads_blocks": fp64["sell_launch"], "sell_columns": fp64["sell_cols"]},
             "speedup_fp32_refined_vs_fp64": fp64["ms_per_step"] / mixed["ms_per_step"],
             "e2e": {"value": world * gdof * e2e_steps / (e2e_ms / 1e3), "unit": "DOF/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "steps": e2e_steps},
             "gpu_launches": mixed["launches"],
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak if peak else None, "traffic": traffic,
-                         "kernel": "sell_pcg_spmv<float> (SELL-32; fused p-update + SpMV + p.Ap)",
+                         "kernel": "sell_pcg_spmv<float> (SELL-32" + (", 16-bit column steps" if d16 else "") +
+                                   "; fused p-update + SpMV + p.Ap)",
                          "algorithmic_bytes_per_launch": bytes_per_launch,
                          "avg_launch_ms": mixed["kernel_ms_avg"], "peak_source": peak_kind},
             "clocks": mixed["clocks"],
@@ -759,6 +767,8 @@ def main():
     ap.add_argument("--serve-chunk", type=int, default=64)
     ap.add_argument("--serve-sample", type=int, default=32, help="requests of the serving sample in the default run")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving sample of the default run")
+    ap.add_argument("--sell-cols", choices=["auto", "i32", "d16"], default="auto",
+                    help="column format of the solvers' SELL copies (auto: 16-bit steps where they fit)")
     args = ap.parse_args()
     if args.workload == "batched" and args.impl == "ours":
         run_batched(args)
