@@ -767,7 +767,7 @@ def main():
     ap.add_argument("--serve-chunk", type=int, default=64)
     ap.add_argument("--serve-sample", type=int, default=32, help="requests of the serving sample in the default run")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving sample of the default run")
-    ap.add_argument("--sell-cols", choices=["auto", "i32", "d16"], default="auto",
+    ap.add_argument("--sell-cols", choices=["auto", "i32", "d16"], default="i32",
                     help="column format of the solvers' SELL copies (auto: 16-bit steps where they fit)")
     args = ap.parse_args()
     if args.workload == "batched" and args.impl == "ours":

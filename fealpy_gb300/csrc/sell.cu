@@ -331,11 +331,12 @@ __device__ bool block_alpha(const double* bpart, int nwp, SellPcgState* st, doub
 }
 
 // kernel A: Ap = A p and per-block partials of p.Ap.  FUSED: p_new = z + beta p_old is
-// formed on the fly for every gathered column (one launch fewer per iteration;
-// used in FP32, where the extra FMA per entry is free).  Not FUSED: p has been
-// updated in place by sell_p_update beforehand (used in FP64, where the FMA
-// rate of this part is low enough that a second FMA per entry would cost more
-// than the extra streaming pass over p).
+// formed on the fly for every gathered column (one launch fewer per iteration,
+// but two gathers per entry).  Not FUSED: p has been updated in place by the
+// p-update kernel beforehand.  Both solvers use the unfused form: measured on
+// the P2 64^3 system (57.6 M nonzeros, FP32) the fused SpMV takes 95 us, the
+// plain one 79 us, and the p update a few microseconds; in FP64 the second
+// FMA per entry would also cost FP64 issue slots.
 template <typename T, bool FUSED, bool D16>
 __global__ void __launch_bounds__(1024, 1) sell_pcg_spmv(SellView A, const T* __restrict__ val,
                                                               const T* __restrict__ z, const T* __restrict__ p_old,
@@ -420,6 +421,29 @@ __global__ void __launch_bounds__(1024, 1) sell_p_update(int64_t n, const double
     P[g] = pv;
   }
   for (int64_t i = 2 * n2 + tid; i < n; i += stride) p[i] = z[i] + beta * p[i];
+}
+
+// p = z + beta p, in place (mixed solver, before kernel A); four rows per
+// thread and trip (16-byte accesses) when both vectors are 16-byte aligned
+__global__ void __launch_bounds__(1024, 1) sell_p_update_f32(int64_t n, const float* __restrict__ z,
+                                                                  float* __restrict__ p, const SellPcgState* st) {
+  if (st->done) return;
+  const float beta = static_cast<float>(st->beta);
+  const int64_t tid = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  const int64_t n4 = aligned16(z, p) ? n >> 2 : 0;
+  const float4* Z = reinterpret_cast<const float4*>(z);
+  float4* P = reinterpret_cast<float4*>(p);
+  for (int64_t g = tid; g < n4; g += stride) {
+    const float4 zv = Z[g];
+    float4 pv = P[g];
+    pv.x = zv.x + beta * pv.x;
+    pv.y = zv.y + beta * pv.y;
+    pv.z = zv.z + beta * pv.z;
+    pv.w = zv.w + beta * pv.w;
+    P[g] = pv;
+  }
+  for (int64_t i = 4 * n4 + tid; i < n; i += stride) p[i] = z[i] + beta * p[i];
 }
 
 // kernel B (FP64 solver).  Rows in pairs (16-byte accesses) when every vector
@@ -771,21 +795,21 @@ struct F64Work {
   SellPcgState* st;
   double* partials;
   double* bpart;  // per-block p.Ap partials of the SpMV step
-  double *r, *z, *p0, *p1, *Ap;
+  double *r, *z, *p0, *Ap;
 };
 
 struct MixedWork {
   SellPcgState* st;
   double* partials;
   double* bpart;
-  float *r, *z, *p0, *p1, *Ap, *dinv32, *y;
+  float *r, *z, *p0, *Ap, *dinv32, *y;
 };
 
 bool carve_f64(Carver& cv, int64_t n, F64Work& w) {
   w.st = cv.take<SellPcgState>(1);
   w.partials = cv.take<double>(2 * kSellMaxBlocks);
   w.bpart = cv.take<double>(kSellMaxBlocks);
-  w.r = cv.take<double>(n); w.z = cv.take<double>(n); w.p0 = cv.take<double>(n); w.p1 = cv.take<double>(n);
+  w.r = cv.take<double>(n); w.z = cv.take<double>(n); w.p0 = cv.take<double>(n);
   w.Ap = cv.take<double>(n);
   return cv.ok;
 }
@@ -794,7 +818,7 @@ bool carve_mixed(Carver& cv, int64_t n, MixedWork& w) {
   w.st = cv.take<SellPcgState>(1);
   w.partials = cv.take<double>(2 * kSellMaxBlocks);
   w.bpart = cv.take<double>(kSellMaxBlocks);
-  w.r = cv.take<float>(n); w.z = cv.take<float>(n); w.p0 = cv.take<float>(n); w.p1 = cv.take<float>(n);
+  w.r = cv.take<float>(n); w.z = cv.take<float>(n); w.p0 = cv.take<float>(n);
   w.Ap = cv.take<float>(n); w.dinv32 = cv.take<float>(n); w.y = cv.take<float>(n);
   return cv.ok;
 }
@@ -817,23 +841,26 @@ void f64_body(const SellView& A, const double* val, const double* dinv, double* 
   rec(ev, 4, s);
 }
 
-// one CG iteration (mixed): ping-pong p by parity (the fused SpMV writes p_new).
-// With a capture context the reliable update becomes an IF node of the graph;
-// otherwise it is launched every iteration and returns at once when not due.
+// one CG iteration (mixed): p = z + beta p in place, then Ap, then the
+// updates (p lives in w.p0; the parity argument is kept for the two-iteration
+// graph body).  With a capture context the reliable update becomes an IF node
+// of the graph; otherwise it is launched every iteration and returns at once
+// when not due.
 void mixed_body(const SellView& A, const float* val32, const double* val64, const double* dinv64, const double* b,
                 double* x, MixedWork& w, double delta, int parity, const cudaEvent_t* ev, cudaStream_t s,
                 CaptureCtx* ctx = nullptr) {
-  float* p_old = parity ? w.p1 : w.p0;
-  float* p_new = parity ? w.p0 : w.p1;
+  (void)parity;
+  float* p = w.p0;
   const cudaGraphConditionalHandle hif = ctx ? ctx->new_handle() : 0;
   rec(ev, 0, s);
+  sell_p_update_f32<<<VEC_LAUNCH(A.n, s)>>>(A.n, w.z, p, w.st);
   rec(ev, 1, s);
   with_cols(A, [&](auto d16) {
-    sell_pcg_spmv<float, true, decltype(d16)::value>
-        <<<SLICE_LAUNCH(A, s)>>>(A, val32, w.z, p_old, p_new, w.Ap, w.bpart, w.st);
+    sell_pcg_spmv<float, false, decltype(d16)::value>
+        <<<SLICE_LAUNCH(A, s)>>>(A, val32, w.z, p, nullptr, w.Ap, w.bpart, w.st);
   });
   rec(ev, 2, s);
-  sell_mixed_update<<<VEC_LAUNCH(A.n, s)>>>(A.n, w.dinv32, p_new, w.Ap, w.y, w.r, w.z, w.bpart, slice_blocks(A),
+  sell_mixed_update<<<VEC_LAUNCH(A.n, s)>>>(A.n, w.dinv32, p, w.Ap, w.y, w.r, w.z, w.bpart, slice_blocks(A),
                                             w.partials, w.st, delta, hif, ctx ? 1 : 0);
   rec(ev, 3, s);
   auto reliable = [&](cudaStream_t rs) {
@@ -987,8 +1014,8 @@ int32_t fgb_sell_spmv(int32_t dtype, const fgb_sell* A, const void* x, void* y, 
 size_t fgb_pcg_sell_workspace_bytes(int64_t n) {
   // sized for the larger (mixed) layout
   return align_up(sizeof(SellPcgState)) + align_up(2 * kSellMaxBlocks * sizeof(double)) +
-         align_up(kSellMaxBlocks * sizeof(double)) + 5 * align_up(static_cast<size_t>(n) * sizeof(double)) +
-         7 * align_up(static_cast<size_t>(n) * sizeof(float));
+         align_up(kSellMaxBlocks * sizeof(double)) + 4 * align_up(static_cast<size_t>(n) * sizeof(double)) +
+         6 * align_up(static_cast<size_t>(n) * sizeof(float));
 }
 
 int32_t fgb_pcg_sell_f64(const fgb_sell* A, const double* diag_inv, const double* b, double* x, double atol,
@@ -1120,8 +1147,9 @@ int32_t fgb_pcg_sell_mixed(const fgb_sell* A, const double* diag_inv64, const do
         graphed = true;
         used_graph = 1;
         if ((rc = read_state(w.st, &h, s))) return rc;
-        // per trip: 2 x (SpMV + update) + loop control; fold + reliable update when due
-        launches += 5 * ((h.niter + 1) / 2 + 1) + 2 * h.n_updates;
+        // per trip: 2 x (p update + SpMV + update) + loop control; fold + reliable
+        // update when due
+        launches += 7 * ((h.niter + 1) / 2 + 1) + 2 * h.n_updates;
       }
       rc = FGB_OK;
     }
@@ -1131,7 +1159,7 @@ int32_t fgb_pcg_sell_mixed(const fgb_sell* A, const double* diag_inv64, const do
         const int64_t before = h.niter;
         for (int k = 0; k < check_every; ++k, ++it)
           mixed_body(v, A->val32, A->val64, diag_inv64, b, x, w, delta, static_cast<int>(it & 1), prof.of(k), s);
-        launches += 4 * check_every;
+        launches += 5 * check_every;
         if (cudaGetLastError() != cudaSuccess) return FGB_ERR_CUDA;
         if ((rc = read_state(w.st, &h, s))) return rc;
         prof.collect(h.niter - before);

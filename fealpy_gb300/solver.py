@@ -53,10 +53,12 @@ def _info_dict(info, extra=None):
 # type), found once by timing the candidates (kernels.sell_autotune) and
 # reused for every later matrix of the same size.
 _LAUNCH_CACHE = {}
-# column format of the solvers' SELL copies: None = delta-coded columns of the
-# renumbered matrix where the bridges add at most 25% entries, False = 4-byte
-# columns, True = delta-coded always
-SELL_D16: Optional[bool] = None
+# column format of the solvers' SELL copies: False = 4-byte columns (default:
+# measured faster on the P2 64^3 system, where the renumbering the 2-byte
+# steps need costs more gather locality than the 25% fewer matrix bytes
+# save), None = delta-coded columns of the renumbered matrix where the bridges
+# add at most 25% entries, True = delta-coded always
+SELL_D16: Optional[bool] = False
 
 
 def _sell_of(A: CSRTensor, want32: bool, tune: bool = True):
