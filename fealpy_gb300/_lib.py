@@ -115,7 +115,7 @@ _SIGNATURES = {
 class BatchSystem(ctypes.Structure):
     """``fgb_batch_system`` (include/fealpy_gb300.h)."""
     _fields_ = [("n", c_i64), ("n_slices", c_i64)] + [(k, c_vp) for k in (
-        "slice_ptr", "perm", "col", "val32", "val64", "dinv64", "b", "x", "r", "z", "p0", "p1", "Ap", "y",
+        "slice_ptr", "perm", "col", "val32", "val64", "dinv64", "b", "x", "r", "z", "p", "Ap", "y",
         "dinv32")] + [("fp64", c_i32), ("reserved", c_i32)]
 
 
@@ -123,7 +123,7 @@ class BatchState(ctypes.Structure):
     """``fgb_batch_state``."""
     _fields_ = [(k, c_dbl) for k in ("rz", "rz_prev", "rr", "alpha", "beta", "b_norm", "tol", "resid", "r_upd",
                                      "true_rel", "delta")] + [("niter", c_i64), ("maxit", c_i64)] + [
-        (k, c_i32) for k in ("active", "done", "need_update", "n_updates", "parity", "stall")] + [
+        (k, c_i32) for k in ("active", "done", "need_update", "n_updates", "reserved", "stall")] + [
         ("r_best", c_dbl), ("last_upd", c_i64), ("max_gap", c_i64)]
 
 

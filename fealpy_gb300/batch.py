@@ -116,7 +116,7 @@ class BatchSolver:
     @staticmethod
     def resident_bytes(n: int, nnz_padded: int, fp64_values: bool) -> int:
         """Device bytes one system keeps resident (SELL copy + vectors)."""
-        return nnz_padded * (4 + 4 + (8 if fp64_values else 0)) + n * (8 + 8 + 8 + 7 * 4) + (n // 32 + 2) * 12
+        return nnz_padded * (4 + 4 + (8 if fp64_values else 0)) + n * (8 + 8 + 8 + 6 * 4) + (n // 32 + 2) * 12
 
     def add(self, A: CSRTensor, b: torch.Tensor, x0: Optional[torch.Tensor] = None, *, rtol: float = 1e-10,
             maxit: int = 100000, key=None, fp64: bool = False) -> int:
@@ -144,7 +144,7 @@ class BatchSolver:
         b64 = b.to(self.device, torch.float64).contiguous()
         x = torch.zeros(n, dtype=torch.float64, device=self.device) if x0 is None else \
             x0.to(self.device, torch.float64).clone()
-        vecs = torch.empty((7, n), dtype=torch.float64 if fp64 else torch.float32, device=self.device)
+        vecs = torch.empty((6, n), dtype=torch.float64 if fp64 else torch.float32, device=self.device)
         self._slots[slot] = _Slot(slot if key is None else key, S, dinv64, b64, x, vecs, float(rtol), int(maxit),
                                   bool(fp64), A)
         self._dirty = True
@@ -192,7 +192,7 @@ class BatchSolver:
             d.val64 = S.val64.data_ptr() if S.val64 is not None else None
             d.fp64 = 1 if sl.fp64 else 0
             d.dinv64, d.b, d.x = sl.dinv64.data_ptr(), sl.b.data_ptr(), sl.x.data_ptr()
-            d.r, d.z, d.p0, d.p1, d.Ap, d.y, d.dinv32 = (v[k].data_ptr() for k in range(7))
+            d.r, d.z, d.p, d.Ap, d.y, d.dinv32 = (v[k].data_ptr() for k in range(6))
             if sl.tiles is None:
                 sl.tiles = (self._tile_bounds(S.n_slices, self.slices_per_tile),
                             self._tile_bounds(S.n, self.rows_per_tile))

@@ -38,14 +38,13 @@ struct BatchCtl {
   int any_update, running;
   int any_acc, running_acc;  // accumulated over the blocks of batch_control
   unsigned int arrived;
-  // tile tickets of the tile kernels (SpMV, update, fold, reliable): each warp
-  // takes the next tile with one atomic; the kernel that follows in stream
-  // order puts the ticket back to 0
-  unsigned int ticket[4];
-  int pad;
+  // tile tickets of the tile kernels (SpMV, update, fold, reliable, p update):
+  // each warp takes the next tile with one atomic; a kernel that follows in
+  // stream order puts the ticket back to 0
+  unsigned int ticket[5];
 };
 
-enum { kTicketSpmv = 0, kTicketUpdate = 1, kTicketFold = 2, kTicketReliable = 3 };
+enum { kTicketSpmv = 0, kTicketUpdate = 1, kTicketFold = 2, kTicketReliable = 3, kTicketP = 4 };
 
 // The next tile for the calling warp (all lanes get the same index).
 __device__ __forceinline__ int next_tile(unsigned int* ticket) {
@@ -78,33 +77,58 @@ template <> struct Vec<double> {
 };
 template <typename T> __device__ __forceinline__ T* vp(void* p) { return static_cast<T*>(p); }
 
-// One slice tile, one warp: Ap, p_new = z + beta p_old, and the lane's p.Ap.
+// One row tile, one warp: p = z + beta p in place (a single
+// gather per entry in the SpMV that follows is cheaper than forming p on the
+// fly from two gathers).
+template <typename T>
+__device__ void p_tile(const fgb_batch_system& A, const fgb_batch_state& S, const fgb_batch_tile& tile) {
+  const T beta = static_cast<T>(S.beta);
+  const T* __restrict__ z = vp<T>(A.z);
+  T* __restrict__ p = vp<T>(A.p);
+  for (int i = tile.begin + (threadIdx.x & 31); i < tile.end; i += 32) p[i] = z[i] + beta * p[i];
+}
+
+// Row tiles (a warp each, by ticket): the p update of every running system.
+__global__ void __launch_bounds__(1024, 1) batch_p_update(const fgb_batch_system* __restrict__ sys,
+                                                          const fgb_batch_state* __restrict__ st,
+                                                          const fgb_batch_tile* __restrict__ tiles,
+                                                          const int32_t* __restrict__ n_tiles, BatchCtl* ctl) {
+  const int nt = *n_tiles;
+  while (true) {
+    const int t = next_tile(&ctl->ticket[kTicketP]);
+    if (t >= nt) break;
+    const fgb_batch_tile tile = tiles[t];
+    const fgb_batch_state& S = st[tile.sys];
+    if (!S.active || S.done || S.need_update) continue;
+    const fgb_batch_system& A = sys[tile.sys];
+    if (A.fp64) p_tile<double>(A, S, tile);
+    else p_tile<float>(A, S, tile);
+  }
+}
+
+// One slice tile, one warp: Ap and the lane's p.Ap (in the vector type, FP64
+// from the warp sum on).
 template <typename T>
 __device__ double spmv_tile(const fgb_batch_system& A, const fgb_batch_state& S, const fgb_batch_tile& tile) {
   const int lane = threadIdx.x & 31;
-  const T beta = static_cast<T>(S.beta);
-  const T* z = vp<T>(A.z);
-  const T* p_old = vp<T>(S.parity ? A.p1 : A.p0);
-  T* p_new = vp<T>(S.parity ? A.p0 : A.p1);
+  const T* p = vp<T>(A.p);
   T* Ap = vp<T>(A.Ap);
-  const GatherP<T> g{z, p_old, beta};
-  double pap = 0.0;
+  const GatherX<T> g{p};
+  T pap = T(0);
   for (int64_t s = tile.begin; s < tile.end; ++s) {
     const int64_t sbase = A.slice_ptr[s];
     const int w = static_cast<int>((A.slice_ptr[s + 1] - sbase) >> 5);
     const T acc = sell_row(A.col, Vec<T>::val(A), sbase, w, lane, g);
     const int32_t row = A.perm[s * kSellC + lane];
     if (row >= 0) {
-      const T pi = z[row] + beta * p_old[row];
-      p_new[row] = pi;
       Ap[row] = acc;
-      pap += static_cast<double>(pi) * static_cast<double>(acc);
+      pap += p[row] * acc;
     }
   }
-  return pap;
+  return static_cast<double>(warp_sum(pap));
 }
 
-// Slice tiles (a warp each, taken by ticket): Ap, p_new and the tile's p.Ap.
+// Slice tiles (a warp each, taken by ticket): Ap and the tile's p.Ap.
 __global__ void __launch_bounds__(1024, 1) batch_spmv_step(const fgb_batch_system* __restrict__ sys,
                                                            const fgb_batch_state* __restrict__ st,
                                                            const fgb_batch_tile* __restrict__ tiles,
@@ -121,16 +145,19 @@ __global__ void __launch_bounds__(1024, 1) batch_spmv_step(const fgb_batch_syste
       const fgb_batch_system& A = sys[tile.sys];
       pap = A.fp64 ? spmv_tile<double>(A, S, tile) : spmv_tile<float>(A, S, tile);
     }
-    pap = warp_sum(pap);
     if ((threadIdx.x & 31) == 0) spart[t] = pap;
   }
 }
 
-// Systems (a block each): alpha = rz / p.Ap.  Also returns the SpMV ticket.
+// Systems (a block each): alpha = rz / p.Ap.  Also returns the p-update and
+// SpMV tickets.
 __global__ void batch_alpha(int32_t n_sys, fgb_batch_state* st, const int32_t* __restrict__ tile_ptr,
                             const double* __restrict__ spart, BatchCtl* ctl) {
   __shared__ double red[32];
-  if (blockIdx.x == 0 && threadIdx.x == 0) ctl->ticket[kTicketSpmv] = 0u;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    ctl->ticket[kTicketSpmv] = 0u;
+    ctl->ticket[kTicketP] = 0u;
+  }
   const int s = blockIdx.x;
   if (s >= n_sys) return;
   fgb_batch_state& S = st[s];
@@ -151,7 +178,7 @@ template <typename T>
 __device__ void update_tile(const fgb_batch_system& A, const fgb_batch_state& S, const fgb_batch_tile& tile,
                             double* rz_out, double* rr_out) {
   const T alpha = static_cast<T>(S.alpha);
-  const T* __restrict__ p = vp<T>(S.parity ? A.p0 : A.p1);  // written by the SpMV step
+  const T* __restrict__ p = vp<T>(A.p);
   const T* __restrict__ Ap = vp<T>(A.Ap);
   const T* __restrict__ dinv = Vec<T>::dinv(A);
   T* __restrict__ y = vp<T>(A.y);
@@ -239,7 +266,6 @@ __global__ void batch_control(int32_t n_sys, fgb_batch_state* st, const int32_t*
             S.rz_prev = S.rz;
             S.beta = rz / S.rz;
             S.rz = rz;
-            S.parity ^= 1;
           }
           any = S.need_update && !S.done;
           running = !S.done;
@@ -339,13 +365,14 @@ __global__ void batch_bnorm(int32_t n_sys, fgb_batch_state* st, const int32_t* _
 // One slice tile, one warp, of a system with an update due (1, 3) or admitted
 // (2): r64 = b - A x in FP64 arithmetic (V: the stored values), r = T(r64),
 // z = Dinv r; the lane's r64.r64 and r.z.  Admission of an FP32 system also
-// builds its FP32 inverse diagonal; admission starts p_old = z.
+// builds its FP32 inverse diagonal; admission starts p = z (with beta = 0 the
+// first p update keeps it).
 template <typename V, typename T>
 __device__ void reliable_tile(const fgb_batch_system& A, const fgb_batch_state& S, const V* __restrict__ val,
                               const fgb_batch_tile& tile, int mode, double* rr_out, double* rz_out) {
   const int lane = threadIdx.x & 31;
   double rr64 = 0.0, rz = 0.0;
-  T* p_old = vp<T>(S.parity ? A.p1 : A.p0);
+  T* p = vp<T>(A.p);
   T* r = vp<T>(A.r);
   T* z = vp<T>(A.z);
   for (int64_t s = tile.begin; s < tile.end; ++s) {
@@ -369,7 +396,7 @@ __device__ void reliable_tile(const fgb_batch_system& A, const fgb_batch_state& 
       const T zi = di * ri;
       r[row] = ri;
       z[row] = zi;
-      if (mode == 2) p_old[row] = zi;
+      if (mode == 2) p[row] = zi;
       rz += static_cast<double>(ri) * static_cast<double>(zi);
     }
   }
@@ -550,6 +577,7 @@ int row_grid(const fgb_batch* b) { return b->max_vt < kBatchRowBlocks ? b->max_v
 
 void launch_iteration(fgb_batch* b, cudaStream_t s, int graph, cudaGraphConditionalHandle h_if,
                       cudaGraphConditionalHandle h_while) {
+  batch_p_update<<<row_grid(b), kBatchRowThreads, 0, s>>>(b->sys, b->st, b->vtiles, b->n_vtiles, b->ctl);
   batch_spmv_step<<<slice_grid(b), b->slice_threads, 0, s>>>(b->sys, b->st, b->stiles, b->n_stiles, b->spart,
                                                               b->ctl);
   batch_alpha<<<b->max_sys, kSysThreads, 0, s>>>(b->max_sys, b->st, b->stile_ptr, b->spart, b->ctl);
@@ -696,7 +724,7 @@ int32_t fgb_batch_set(fgb_batch* b, int32_t n_sys, const fgb_batch_system* syste
     const fgb_batch_system& A = systems[s];
     if (A.n <= 0) continue;  // an empty slot: it must own no tiles
     if (A.n >= (int64_t(1) << 31) || A.n_slices != fgb_sell_slots(A.n) / kSellC || !A.slice_ptr || !A.perm ||
-        !A.col || !A.dinv64 || !A.b || !A.x || !A.r || !A.z || !A.p0 || !A.p1 || !A.Ap || !A.y)
+        !A.col || !A.dinv64 || !A.b || !A.x || !A.r || !A.z || !A.p || !A.Ap || !A.y)
       return FGB_ERR_ARG;
     if (A.fp64 ? !A.val64 : (!A.val32 || !A.dinv32)) return FGB_ERR_ARG;
   }

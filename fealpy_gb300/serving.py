@@ -29,11 +29,11 @@ __all__ = ["SolveServer", "poisson_request_problem", "resident_estimate"]
 def resident_estimate(n: int, nnz: int, fp64: bool) -> int:
     """Device bytes a request keeps resident while admitted: CSR (int64 row
     pointer, int32 columns, values), the SELL copy (about 4% padding), FP64
-    b, x and inverse diagonal, and seven Krylov vectors."""
+    b, x and inverse diagonal, and six Krylov vectors."""
     vb = 8 if fp64 else 4
     csr = (n + 1) * 8 + nnz * (4 + vb)
     sell = int(nnz * 1.05) * (4 + (8 if fp64 else 4)) + n * 4 + (n // 32 + 2) * 8
-    vec = n * 8 * 3 + n * 7 * (8 if fp64 else 4)
+    vec = n * 8 * 3 + n * 6 * (8 if fp64 else 4)
     return csr + sell + vec
 
 

@@ -392,8 +392,7 @@ typedef struct fgb_batch_system {
   double* x;                /* x0 on admission, the solution on retirement */
   void* r;                  /* Krylov vectors, n entries each, owned by    */
   void* z;                  /* the caller: float, or double when fp64      */
-  void* p0;
-  void* p1;
+  void* p;
   void* Ap;
   void* y;
   void* dinv32;             /* float inverse diagonal (unused when fp64)   */
@@ -410,7 +409,7 @@ typedef struct fgb_batch_state {
   int32_t need_update; /* 1: reliable update due, 2: admission pending,   */
                        /* 3: true-residual check on a plateau            */
   int32_t n_updates;
-  int32_t parity;      /* which of p0/p1 holds the current direction      */
+  int32_t reserved;
   int32_t stall;       /* true-residual checks without a 2x improvement   */
   double r_best;       /* best true residual norm so far                  */
   int64_t last_upd;    /* iteration of the last reliable update           */

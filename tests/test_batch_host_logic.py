@@ -45,9 +45,9 @@ def test_tiles_table_layout_and_pointers():
 
 
 def test_struct_sizes_match_the_header():
-    # fgb_batch_system: 2 int64 + 15 pointers + 2 int32; fgb_batch_state: 11 double,
+    # fgb_batch_system: 2 int64 + 14 pointers + 2 int32; fgb_batch_state: 11 double,
     # 2 int64, 6 int32, 1 double, 2 int64
-    assert ctypes.sizeof(_lib.BatchSystem) == 2 * 8 + 15 * 8 + 2 * 4
+    assert ctypes.sizeof(_lib.BatchSystem) == 2 * 8 + 14 * 8 + 2 * 4
     assert ctypes.sizeof(_lib.BatchState) == 11 * 8 + 2 * 8 + 6 * 4 + 8 + 2 * 8
 
 
