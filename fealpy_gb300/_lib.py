@@ -91,7 +91,7 @@ _SIGNATURES = {
     "fgb_sell_fill": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "fgb_sell_spmv": (c_i32, [c_i32, ctypes.c_void_p, c_vp, c_vp, c_vp]),
     "fgb_sell_d16_workspace_bytes": (c_sz, [c_i64]),
-    "fgb_sell_renumber": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_sz, c_vp]),
+    "fgb_sell_renumber": (c_i32, [c_i64, c_vp, c_vp, c_i32, c_vp, c_vp, c_vp, c_vp, c_sz, c_vp]),
     "fgb_csr_permute": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_sz, c_vp]),
     "fgb_sell_d16_indptr": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_vp, c_sz, c_vp]),
     "fgb_sell_fill_d16": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
@@ -186,7 +186,7 @@ KERNELS_PER_CALL = {
     "fgb_pattern_expand_blocks": 2, "fgb_assemble_scalar": 2, "fgb_assemble_elasticity_p1": 2,
     "fgb_dirichlet_count": 1, "fgb_exclusive_scan_i32": 3, "fgb_dirichlet_fill": 1, "fgb_csr_spmv": 1,
     "fgb_csr_diagonal": 1, "fgb_gather_sum": 1, "fgb_sell_plan": 4, "fgb_sell_fill": 1, "fgb_sell_spmv": 1,
-    "fgb_sell_renumber": 7, "fgb_csr_permute": 5, "fgb_sell_d16_indptr": 4, "fgb_sell_fill_d16": 1, "fgb_permute": 1,
+    "fgb_sell_renumber": 1, "fgb_csr_permute": 5, "fgb_sell_d16_indptr": 4, "fgb_sell_fill_d16": 1, "fgb_permute": 1,
 }
 
 _launches = [0]

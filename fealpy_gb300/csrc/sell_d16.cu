@@ -11,9 +11,15 @@
 // diagonal permuted alike; the result is permuted back.
 //
 // Construction (all on the device, deterministic):
-//   renumber     keys = smallest column per row; counting sort by key, each
-//                key group sorted by row (groups are a handful of rows; a
-//                group above 64 rows makes the whole order the identity)
+//   renumber     with the dof blocks of the space (vertex, edge, face, cell
+//                dofs; per component for vector spaces): a stable merge of
+//                the blocks by relative position, key(i) = floor(i_rel *
+//                n_0 / n_b), which puts every edge/face/cell dof next to the
+//                vertex dofs of the same region (FEALPy numbers entities by
+//                their vertices); closed form, no sort.  Without blocks: keys
+//                = smallest column per row; counting sort by key, each key
+//                group sorted by row (a group above 64 rows makes the whole
+//                order the identity)
 //   csr_permute  rows in the new order, columns mapped and sorted (rank sort
 //                by a warp per row, staged in shared memory)
 //   d16_indptr   row lengths with the bridge entries for steps above 65535
@@ -25,6 +31,42 @@
 namespace fgb {
 
 constexpr int kGroupMax = 64;     // largest key group sorted in place
+constexpr int kMaxBlocks = 16;    // dof blocks of the block-merge order
+
+struct DofBlocks {
+  int n;
+  int64_t start[kMaxBlocks + 1];
+};
+
+// Rows of block b (relative index j) whose key is below k: key(j) =
+// floor(j * n0 / nb) < k  <=>  j < ceil(k * nb / n0).
+__device__ __forceinline__ int64_t keys_below(int64_t k, int64_t nb, int64_t n0) {
+  const int64_t c = (k * nb + n0 - 1) / n0;
+  return c < nb ? c : nb;
+}
+
+// Stable merge of the blocks by key: row i (block b, relative index j, key k)
+// goes to j + sum_{b' < b} |{key <= k} in b'| + sum_{b' > b} |{key < k} in b'|.
+__global__ void renumber_blocks(int64_t n, DofBlocks B, int32_t* __restrict__ order, int32_t* __restrict__ inv) {
+  const int64_t n0 = B.start[1] - B.start[0];
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    int b = 0;
+    while (b + 1 < B.n && i >= B.start[b + 1]) ++b;
+    const int64_t nb = B.start[b + 1] - B.start[b];
+    const int64_t j = i - B.start[b];
+    const int64_t k = (j * n0) / nb;
+    int64_t pos = j;
+    for (int q = 0; q < B.n; ++q) {
+      if (q == b) continue;
+      const int64_t nq = B.start[q + 1] - B.start[q];
+      pos += keys_below(q < b ? k + 1 : k, nq, n0);
+    }
+    order[pos] = static_cast<int32_t>(i);
+    inv[i] = static_cast<int32_t>(pos);
+  }
+}
+
 constexpr int kPermWarps = 4;     // warps per block of the row permutation
 constexpr int kPermStage = 1024;  // row entries staged in shared memory per warp
 
@@ -239,12 +281,27 @@ size_t fgb_sell_d16_workspace_bytes(int64_t n) {
          align_up((un + 1) * sizeof(int64_t)) + align_up(sizeof(int32_t)) + scan_workspace_bytes(n);
 }
 
-int32_t fgb_sell_renumber(int64_t n, const int64_t* indptr, const int32_t* indices, int32_t* order, int32_t* inv,
-                          void* workspace, size_t workspace_bytes, void* stream) {
-  if (n <= 0 || !indptr || !indices || !order || !inv) return FGB_ERR_ARG;
+int32_t fgb_sell_renumber(int64_t n, const int64_t* indptr, const int32_t* indices, int32_t n_blocks,
+                          const int64_t* block_sizes_host, int32_t* order, int32_t* inv, void* workspace,
+                          size_t workspace_bytes, void* stream) {
+  if (n <= 0 || !order || !inv || n_blocks < 0 || n_blocks > kMaxBlocks) return FGB_ERR_ARG;
   if (n >= (int64_t(1) << 31)) return FGB_ERR_CAPACITY;
-  if (!workspace || workspace_bytes < fgb_sell_d16_workspace_bytes(n)) return FGB_ERR_WORKSPACE;
   cudaStream_t st = as_stream(stream);
+  if (n_blocks > 0) {
+    if (!block_sizes_host) return FGB_ERR_ARG;
+    DofBlocks B{};
+    B.n = n_blocks;
+    B.start[0] = 0;
+    for (int b = 0; b < n_blocks; ++b) {
+      if (block_sizes_host[b] <= 0) return FGB_ERR_ARG;
+      B.start[b + 1] = B.start[b] + block_sizes_host[b];
+    }
+    if (B.start[n_blocks] != n) return FGB_ERR_ARG;
+    renumber_blocks<<<grid_rows(n), kThreads, 0, st>>>(n, B, order, inv);
+    return launch_status();
+  }
+  if (!indptr || !indices) return FGB_ERR_ARG;
+  if (!workspace || workspace_bytes < fgb_sell_d16_workspace_bytes(n)) return FGB_ERR_WORKSPACE;
   Carver cv(workspace, workspace_bytes);
   int32_t* key = cv.take<int32_t>(n);
   int32_t* cnt = cv.take<int32_t>(n + 1);

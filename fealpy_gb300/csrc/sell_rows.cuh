@@ -145,29 +145,34 @@ __device__ __forceinline__ Pack4DH load_pack_d16(const uint16_t* d16, const doub
   return p;
 }
 
+// Columns of a pack from the column before it: a two-level prefix sum of the
+// four steps, so that the gathers do not wait on a chain of four additions.
+__device__ __forceinline__ int4 pack_cols_d16(uint2 d, int32_t c) {
+  const int32_t d0 = static_cast<int32_t>(d.x & 0xffffu), d1 = static_cast<int32_t>(d.x >> 16);
+  const int32_t d2 = static_cast<int32_t>(d.y & 0xffffu), d3 = static_cast<int32_t>(d.y >> 16);
+  const int32_t c1 = c + (d0 + d1);
+  return make_int4(c + d0, c1, c1 + d2, c1 + (d2 + d3));
+}
+
+__device__ __forceinline__ int32_t pack_total_d16(uint2 d) {
+  return static_cast<int32_t>((d.x & 0xffffu) + (d.x >> 16) + (d.y & 0xffffu) + (d.y >> 16));
+}
+
 template <typename T, typename G>
-__device__ __forceinline__ T pack_dot_d16(const Pack4FH& p, const G& g, int32_t& c, T acc) {
-  c += static_cast<int32_t>(p.d.x & 0xffffu);
-  acc += p.v.x * g(c);
-  c += static_cast<int32_t>(p.d.x >> 16);
-  acc += p.v.y * g(c);
-  c += static_cast<int32_t>(p.d.y & 0xffffu);
-  acc += p.v.z * g(c);
-  c += static_cast<int32_t>(p.d.y >> 16);
-  acc += p.v.w * g(c);
+__device__ __forceinline__ T pack_dot_cols(const Pack4FH& p, int4 cc, const G& g, T acc) {
+  acc += p.v.x * g(cc.x);
+  acc += p.v.y * g(cc.y);
+  acc += p.v.z * g(cc.z);
+  acc += p.v.w * g(cc.w);
   return acc;
 }
 
 template <typename T, typename G>
-__device__ __forceinline__ T pack_dot_d16(const Pack4DH& p, const G& g, int32_t& c, T acc) {
-  c += static_cast<int32_t>(p.d.x & 0xffffu);
-  acc += p.v01.x * g(c);
-  c += static_cast<int32_t>(p.d.x >> 16);
-  acc += p.v01.y * g(c);
-  c += static_cast<int32_t>(p.d.y & 0xffffu);
-  acc += p.v23.x * g(c);
-  c += static_cast<int32_t>(p.d.y >> 16);
-  acc += p.v23.y * g(c);
+__device__ __forceinline__ T pack_dot_cols(const Pack4DH& p, int4 cc, const G& g, T acc) {
+  acc += p.v01.x * g(cc.x);
+  acc += p.v01.y * g(cc.y);
+  acc += p.v23.x * g(cc.z);
+  acc += p.v23.y * g(cc.w);
   return acc;
 }
 
@@ -190,12 +195,19 @@ __device__ __forceinline__ T sell_row_acc_d16(const uint16_t* __restrict__ d16, 
     P a[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) a[u] = load_pack_d16(d16, val, sbase, lane, q + u);
+    // the column before each pack: one addition per pack on the carried chain
+    int32_t base[U];
+    base[0] = c;
 #pragma unroll
-    for (int u = 0; u < U; ++u) acc = pack_dot_d16<T>(a[u], g, c, acc);
+    for (int u = 1; u < U; ++u) base[u] = base[u - 1] + pack_total_d16(a[u - 1].d);
+    c = base[U - 1] + pack_total_d16(a[U - 1].d);
+#pragma unroll
+    for (int u = 0; u < U; ++u) acc = pack_dot_cols<T>(a[u], pack_cols_d16(a[u].d, base[u]), g, acc);
   }
   for (; q < nq; ++q) {
     const P a = load_pack_d16(d16, val, sbase, lane, q);
-    acc = pack_dot_d16<T>(a, g, c, acc);
+    acc = pack_dot_cols<T>(a, pack_cols_d16(a.d, c), g, acc);
+    c += pack_total_d16(a.d);
   }
   return acc;
 }

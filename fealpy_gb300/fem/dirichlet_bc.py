@@ -62,12 +62,16 @@ class DirichletBC:
             self.check_vector(f)
         uh = self._boundary_values(f, uh, gd)
         ptr_, idx, val, f_new = K.dirichlet_apply(A.crow, A.col, A.values, self.is_boundary_dof, f, uh, matrix=True)
-        return CSRTensor(ptr_, idx, val, A.shape), f_new
+        out = CSRTensor(ptr_, idx, val, A.shape)
+        out.dof_blocks = getattr(A, "dof_blocks", None)
+        return out, f_new
 
     def apply_matrix(self, matrix: CSRTensor, *, check=True) -> CSRTensor:
         A = self.check_matrix(matrix) if check else matrix
         ptr_, idx, val, _ = K.dirichlet_apply(A.crow, A.col, A.values, self.is_boundary_dof, None, None, matrix=True)
-        return CSRTensor(ptr_, idx, val, A.shape)
+        out = CSRTensor(ptr_, idx, val, A.shape)
+        out.dof_blocks = getattr(A, "dof_blocks", None)
+        return out
 
     def apply_vector(self, vector, matrix, uh=None, gd=None, *, check=True):
         A = self.check_matrix(matrix) if check else matrix

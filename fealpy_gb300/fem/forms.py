@@ -166,6 +166,7 @@ class BilinearForm(_Form):
             raise NotImplementedError
         _lib.check_status_word("assembly", status)
         M = CSRTensor(indptr, indices, values, (n, n))
+        M.dof_blocks = space.dof_blocks()
         if v32 is not None:
             M._f32 = v32
         self._M = M

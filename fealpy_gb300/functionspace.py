@@ -40,6 +40,11 @@ class LagrangeFESpace:
     def number_of_global_dofs(self) -> int:
         return self.mesh.number_of_global_ipoints(self.p)
 
+    def dof_blocks(self):
+        """Sizes of the contiguous dof ranges (vertex, edge, face and cell
+        dofs) in global dof order."""
+        return self.mesh.ipoint_blocks(self.p)
+
     def cell_to_dof(self, index=_S) -> torch.Tensor:
         if self._c2d is None:
             self._c2d = self.mesh.cell_to_ipoint(self.p).contiguous()
@@ -161,6 +166,15 @@ class TensorFunctionSpace:
 
     def number_of_local_dofs(self, doftype="cell") -> int:
         return self.dof_numel * self.scalar_space.number_of_local_dofs(doftype)
+
+    def dof_blocks(self):
+        """Contiguous dof ranges: the scalar blocks scaled by the number of
+        components (interleaved layout), or repeated per component
+        (component-major layout)."""
+        sb = self.scalar_space.dof_blocks()
+        if self.dof_priority:
+            return sb * self.dof_numel
+        return [self.dof_numel * v for v in sb]
 
     def _expand(self, to_dof: torch.Tensor) -> torch.Tensor:
         n = self.dof_numel

@@ -329,15 +329,18 @@ D16_MAX_GROWTH = 1.25
 
 
 def sell_build(indptr, indices, values64=None, values32=None, want64=True, want32=False,
-               d16: Optional[bool] = None) -> SellMatrix:
+               d16: Optional[bool] = None, blocks: Optional[Sequence[int]] = None) -> SellMatrix:
     """SELL-32 copy of a CSR matrix.  ``d16``: True = delta-coded columns of
     the renumbered matrix, False = 4-byte columns, None = delta-coded when
-    the bridges add at most 25% entries (two host reads for the sizes)."""
+    the bridges add at most 25% entries (two host reads for the sizes).
+    ``blocks``: the dof block sizes of the space (``dof_blocks()``) for the
+    block-merge renumbering; without them the rows are ordered by their
+    smallest column."""
     dev = _dev(indptr)
     n = indptr.numel() - 1
     lib = _lib.lib()
     if d16 is None or d16:
-        S = _sell_build_d16(indptr, indices, values64, values32, want64, want32, force=bool(d16))
+        S = _sell_build_d16(indptr, indices, values64, values32, want64, want32, force=bool(d16), blocks=blocks)
         if S is not None:
             return S
     slots = int(lib.fgb_sell_slots(n))
@@ -356,7 +359,7 @@ def sell_build(indptr, indices, values64=None, values32=None, want64=True, want3
 
 
 def _sell_build_d16(indptr, indices, values64, values32, want64, want32, force=False,
-                    renumber=True) -> Optional[SellMatrix]:
+                    renumber=True, blocks: Optional[Sequence[int]] = None) -> Optional[SellMatrix]:
     """Delta-coded copy of P A P^T (None when not worth it and not forced).
     ``renumber=False`` keeps the matrix's own numbering (columns must be
     ascending in every row; steps above 65535 are bridged)."""
@@ -369,7 +372,14 @@ def _sell_build_d16(indptr, indices, values64, values32, want64, want32, force=F
     if renumber:
         order = torch.empty(n, dtype=torch.int32, device=dev)
         inv = torch.empty(n, dtype=torch.int32, device=dev)
-        call("fgb_sell_renumber", n, ptr(indptr), ptr(indices), ptr(order), ptr(inv), ptr(ws), ws.numel(), s)
+        nb = len(blocks) if blocks else 0
+        if nb and sum(int(v) for v in blocks) != n:
+            raise ValueError("dof blocks do not add up to the matrix size")
+        sizes = (ctypes.c_int64 * max(nb, 1))(*[int(v) for v in (blocks or [])])
+        call("fgb_sell_renumber", n, ptr(indptr), ptr(indices), nb, sizes, ptr(order), ptr(inv), ptr(ws), ws.numel(),
+             s)
+        if not nb:
+            _lib.add_launches(6)  # key pass, 3 scan kernels, placement, group sort
         p_indptr = torch.empty(n + 1, dtype=torch.int64, device=dev)
         p_indices = torch.empty(max(nnz, 1), dtype=torch.int32, device=dev)
         p64 = torch.empty(max(nnz, 1), dtype=torch.float64, device=dev) if want64 else None

@@ -212,6 +212,19 @@ class _SimplexMesh:
         NF = self.number_of_faces()
         return n + NF * (p - 1) * (p - 2) // 2 + NC * (p - 1) * (p - 2) * (p - 3) // 6
 
+    def ipoint_blocks(self, p):
+        """Sizes of the contiguous ranges of the global interpolation-point
+        numbering (vertices, edge interiors, face interiors, cell interiors;
+        empty ranges left out), in the order number_of_global_ipoints counts
+        them."""
+        NN, NE, NC = self.number_of_nodes(), self.number_of_edges(), self.number_of_cells()
+        sizes = [NN, NE * (p - 1)]
+        if self.TD == 2:
+            sizes.append(NC * (p - 1) * (p - 2) // 2)
+        else:
+            sizes += [self.number_of_faces() * (p - 1) * (p - 2) // 2, NC * (p - 1) * (p - 2) * (p - 3) // 6]
+        return [int(v) for v in sizes if v > 0]
+
     def edge_to_ipoint(self, p, index=_S):
         NN = self.number_of_nodes()
         NE = self.number_of_edges()

@@ -68,11 +68,12 @@ def _sell_of(A: CSRTensor, want32: bool, tune: bool = True):
     if S is None or (want32 and S.val32 is None) or (not want32 and S.val64 is None):
         if A.values.dtype == torch.float32 and want32:
             # FP32-assembled operator: the FP32 values are the matrix (no FP64 copy)
-            S = K.sell_build(A.crow, A.col, None, A.values.contiguous(), want64=False, want32=True, d16=SELL_D16)
+            S = K.sell_build(A.crow, A.col, None, A.values.contiguous(), want64=False, want32=True, d16=SELL_D16,
+                             blocks=getattr(A, "dof_blocks", None))
         else:
             v32 = A._f32 if (want32 and A._f32 is not None) else None
             S = K.sell_build(A.crow, A.col, A.values.to(torch.float64).contiguous(), v32, want64=True, want32=want32,
-                             d16=SELL_D16)
+                             d16=SELL_D16, blocks=getattr(A, "dof_blocks", None))
         A._sell = S
         if tune:
             dt = torch.float32 if want32 else torch.float64

@@ -19,6 +19,9 @@ class CSRTensor:
         self._crow = crow
         self._col = col
         self._values = values
+        # sizes of the contiguous dof ranges of the space the matrix was
+        # assembled on (vertex, edge, face, cell dofs), or None
+        self.dof_blocks = None
         if spshape is None:
             spshape = (crow.shape[0] - 1, int(col.max().item()) + 1 if col.numel() else 0)
         self._spshape = tuple(int(s) for s in spshape)

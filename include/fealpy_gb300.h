@@ -323,18 +323,24 @@ int32_t fgb_sell_spmv(int32_t dtype, const fgb_sell* A, const void* x, void* y, 
  * a matrix renumbered so that the steps are small.  No FEALPy counterpart
  * (solver-side layout, as above); the solve is the same Jacobi-PCG on
  * P A P^T with b, x and the inverse diagonal permuted alike.
- *   renumber: order[k] = old index of new row k: rows sorted by (smallest
- *     column, row), which interleaves the node, edge, face and cell dofs of
- *     FEALPy's numbering by location (identity when a group of equal keys
- *     exceeds 64 rows); inv = its inverse.
+ *   renumber: order[k] = old index of new row k, inv = its inverse.  With
+ *     the space's dof blocks (n_blocks > 0 sizes in dof order: vertex, edge,
+ *     face and cell dofs, per component for component-major vector spaces):
+ *     a stable merge of the blocks by relative position, which puts every
+ *     edge/face/cell dof next to the vertex dofs of its region (FEALPy
+ *     numbers entities by their vertices; block sizes of
+ *     fealpy/functionspace/lagrange_fe_space.py number_of_global_dofs).
+ *     Without blocks (n_blocks = 0): rows sorted by (smallest column, row);
+ *     identity when a group of equal keys exceeds 64 rows.
  *   csr_permute: rows order[k] of the CSR with columns inv[col], ascending.
  *   d16_indptr: row pointer of the row lengths including the zero-valued
  *     bridge entries that split steps above 65535 (for fgb_sell_plan).
  *   fill_d16: col0/col16 and values of the plan's slots.
  *   permute: dst[k] = src[order[k]] (scatter = 0) or dst[order[k]] = src[k]. */
 size_t fgb_sell_d16_workspace_bytes(int64_t n);
-int32_t fgb_sell_renumber(int64_t n, const int64_t* indptr, const int32_t* indices, int32_t* order,
-                          int32_t* inv, void* workspace, size_t workspace_bytes, void* stream);
+int32_t fgb_sell_renumber(int64_t n, const int64_t* indptr, const int32_t* indices, int32_t n_blocks,
+                          const int64_t* block_sizes_host, int32_t* order, int32_t* inv,
+                          void* workspace, size_t workspace_bytes, void* stream);
 int32_t fgb_csr_permute(int64_t n, const int64_t* indptr, const int32_t* indices, const double* values64,
                         const float* values32, const int32_t* order, const int32_t* inv,
                         int64_t* new_indptr, int32_t* new_indices, double* new_values64,
