@@ -332,10 +332,10 @@ def run_ours(args):
     # dominant kernel: the fused FP32 PCG SpMV (p = z + beta p_old, Ap = A p, p.Ap)
     nnz = mixed["nnz"]
     # values + columns of the real entries (4-byte columns, or 2-byte steps plus
-    # a first column per row), the slot->row map, z and p_old read once, p_new
-    # and Ap written once (FP32 vectors)
+    # a first column per row), the slot->row map, p read once and Ap written
+    # once (FP32 vectors)
     d16 = mixed["sell_cols"] == "d16"
-    bytes_per_launch = nnz * (4 + 2) + gdof * (4 + 4 + 4 * 4) if d16 else nnz * (4 + 4) + gdof * (4 + 4 * 4)
+    bytes_per_launch = nnz * (4 + 2) + gdof * (4 + 4 + 4 + 4) if d16 else nnz * (4 + 4) + gdof * (4 + 4 + 4)
     achieved = bytes_per_launch / (mixed["kernel_ms_avg"] / 1e3) / 1e9 if mixed["kernel_ms_avg"] > 0 else 0.0
     traffic = None
     tp = os.path.join(ROOT, "profiles", "traffic.json")
@@ -382,7 +382,7 @@ def run_ours(args):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak if peak else None, "traffic": traffic,
                          "kernel": "sell_pcg_spmv<float> (SELL-32" + (", 16-bit column steps" if d16 else "") +
-                                   "; fused p-update + SpMV + p.Ap)",
+                                   "; Ap = A p and p.Ap)",
                          "algorithmic_bytes_per_launch": bytes_per_launch,
                          "avg_launch_ms": mixed["kernel_ms_avg"], "peak_source": peak_kind},
             "clocks": mixed["clocks"],
