@@ -187,7 +187,67 @@ struct SellPcgState {
   double r_best;
   long long last_upd, max_gap;
   int stall, pad;
+  // persistent solver: grid barrier (arrivals, generation) and its error flag
+  unsigned int bar[2];
+  int bar_err, pad2;
 };
+
+// Scalar step of the mixed solver after an FP32 iteration (totals r.z, r.r):
+// the iteration count, the residual estimate, whether a reliable update (1)
+// or a check of the true residual on a plateau (3) is due, and beta.
+__device__ void mixed_iteration_scalars(SellPcgState& S, double trz, double trr, double delta) {
+  S.niter += 1;
+  const double res = sqrt(trr);
+  S.resid = res;
+  S.rr = trr;
+  if (!isfinite(res)) {
+    S.done = FGB_PCG_NONFINITE;
+  } else {
+    // a check of the true residual when the gap since the last update has
+    // grown well past the longest earlier one (FP32 iterations on a plateau)
+    const long long gap = S.niter - S.last_upd;
+    const long long slack = S.max_gap / 2 > 100 ? S.max_gap / 2 : 100;
+    const bool plateau = S.max_gap > 0 ? gap > S.max_gap + slack : gap > 1000;
+    const bool due = (res < delta * S.r_upd) || (res < S.tol) || (S.niter >= S.maxit);
+    S.need_update = due ? 1 : (plateau ? 3 : 0);
+  }
+  S.rz_prev = S.rz;
+  S.beta = trz / S.rz;
+  S.rz = trz;
+}
+
+// Scalar step of a reliable update (totals of the FP64 residual r64.r64 and of
+// the replaced r.z): true-residual test, stall rule, beta from the replaced
+// residual.  first = 1 at the start of the solve.
+__device__ void mixed_reliable_scalars(SellPcgState& S, double trr, double trz, int first) {
+  const double nrm = sqrt(trr);
+  S.true_rel = S.b_norm > 0.0 ? nrm / S.b_norm : 0.0;
+  S.resid = nrm;
+  if (!first) {
+    S.n_updates += 1;
+    const long long gap = S.niter - S.last_upd;
+    if (S.need_update == 1 && gap > S.max_gap) S.max_gap = gap;
+    S.last_upd = S.niter;
+    if (nrm < 0.5 * S.r_best) {
+      S.r_best = nrm;
+      S.stall = 0;
+    } else {
+      S.stall += 1;
+    }
+  } else {
+    S.r_best = nrm;
+    S.last_upd = 0;
+  }
+  if (!isfinite(nrm)) S.done = FGB_PCG_NONFINITE;
+  else if (nrm <= S.tol) S.done = FGB_PCG_RTOL;
+  else if (S.niter >= S.maxit) S.done = FGB_PCG_MAXIT;
+  else if (S.stall >= 1) S.done = FGB_PCG_STAGNATED;  // the caller continues in FP64
+  S.beta = first ? 0.0 : trz / S.rz_prev;
+  S.rz = trz;
+  S.rr = trr;
+  S.r_upd = nrm;
+  S.need_update = 0;
+}
 
 // Last-block-done deterministic reduction of two partials per thread (T =
 // float: FP32 per-thread and per-warp sums, as in the FP32 iterations; T =
@@ -574,23 +634,7 @@ __global__ void __launch_bounds__(1024, 1) sell_mixed_update(int64_t n, const fl
   double trz, trr;
   if (sell_last_block(rz, rr, partials, &st->counter[2], &trz, &trr) &&
       threadIdx.x == 0) {
-    st->niter += 1;
-    const double res = sqrt(trr);
-    st->resid = res;
-    st->rr = trr;
-    if (!isfinite(res)) st->done = FGB_PCG_NONFINITE;
-    else {
-      // a check of the true residual when the gap since the last update has
-      // grown well past the longest earlier one (FP32 iterations on a plateau)
-      const long long gap = st->niter - st->last_upd;
-      const long long slack = st->max_gap / 2 > 100 ? st->max_gap / 2 : 100;
-      const bool plateau = st->max_gap > 0 ? gap > st->max_gap + slack : gap > 1000;
-      const bool due = (res < delta * st->r_upd) || (res < st->tol) || (st->niter >= st->maxit);
-      st->need_update = due ? 1 : (plateau ? 3 : 0);
-    }
-    st->rz_prev = st->rz;
-    st->beta = trz / st->rz;
-    st->rz = trz;
+    mixed_iteration_scalars(*st, trz, trr, delta);
     // graph driver: run the reliable-update node only when it is due
     if (set_if) cudaGraphSetConditional(hif, (st->need_update && !st->done) ? 1u : 0u);
   }
@@ -640,34 +684,270 @@ __global__ void __launch_bounds__(1024, 1) sell_mixed_reliable(SellView A, const
     }
   }
   double trr, trz;
-  if (sell_last_block(rr64, rz, partials, &st->counter[3], &trr, &trz) && threadIdx.x == 0) {
-    const double nrm = sqrt(trr);
-    st->true_rel = st->b_norm > 0.0 ? nrm / st->b_norm : 0.0;
-    st->resid = nrm;
-    if (!first) {
-      st->n_updates += 1;
-      const long long gap = st->niter - st->last_upd;
-      if (st->need_update == 1 && gap > st->max_gap) st->max_gap = gap;
-      st->last_upd = st->niter;
-      if (nrm < 0.5 * st->r_best) {
-        st->r_best = nrm;
-        st->stall = 0;
-      } else {
-        st->stall += 1;
-      }
+  if (sell_last_block(rr64, rz, partials, &st->counter[3], &trr, &trz) && threadIdx.x == 0)
+    mixed_reliable_scalars(*st, trr, trz, first);
+}
+
+// ------------------------------------------------ persistent FP32-refined solver
+// One cooperative launch runs every iteration of the mixed solver: the grid
+// stays resident (two 512-thread blocks per SM) and phases are separated by a
+// software grid barrier instead of kernel boundaries, which removes the launch,
+// ramp-up and tail of three kernels per iteration (the vector kernels are
+// launch-bound: their SMs are busy for less than half of their duration).
+// Per iteration: p = z + beta p (own rows) | barrier | Ap = A p, block partial
+// of p.Ap | barrier | alpha (every block sums the partials in the same order)
+// and y, r, z updates, block partials of r.z, r.r | barrier | beta, the
+// stopping test and whether a reliable update is due (every block computes the
+// same scalars from the same partials; the scalar code is the one of the
+// multi-kernel driver).  A reliable update adds: x += y | barrier | r64 = b -
+// A x in FP64 arithmetic, r, z | barrier | true-residual test.
+// Vectors rewritten by other blocks inside the kernel are read through L2
+// (ld.global.cg): L1 is not coherent across blocks within a launch.
+constexpr int kPersistThreads = 512;
+constexpr long long kBarrierSpins = 20000000;  // >= 64 ns apart: well above a second
+
+struct PersistArgs {
+  SellView A;
+  const float* val32;  // FP32 values (the iterations)
+  const void* valr;    // values of the FP64 residual: double, or the FP32 ones
+  const double* b;
+  double* x;
+  const float* dinv;
+  float *r, *z, *p, *Ap, *y;
+  double* bpart;  // kSellMaxBlocks partials of p.Ap
+  double* vpart;  // 2 * kSellMaxBlocks partials (two values per block)
+  SellPcgState* st;
+  double delta;
+};
+
+// Grid barrier of a cooperative launch (every block resident): arrivals by an
+// atomic counter, release by a generation counter.  A wait longer than
+// kBarrierSpins polls, or any wait once another block has failed, sets the
+// error flag and returns false; the caller then returns, so every block ends.
+__device__ bool grid_barrier(SellPcgState* st) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned int* gen = &st->bar[1];
+    volatile int* err = &st->bar_err;
+    const unsigned int g = *gen;
+    __threadfence();
+    int good = 1;
+    if (atomicAdd(&st->bar[0], 1u) == gridDim.x - 1) {
+      atomicExch(&st->bar[0], 0u);
+      __threadfence();
+      atomicAdd(&st->bar[1], 1u);
     } else {
-      st->r_best = nrm;
-      st->last_upd = 0;
+      long long spins = 0;
+      while (*gen == g) {
+        if (*err || ++spins > kBarrierSpins) {
+          good = 0;
+          atomicExch(&st->bar_err, 1);
+          break;
+        }
+        __nanosleep(64);
+      }
     }
-    if (!isfinite(nrm)) st->done = FGB_PCG_NONFINITE;
-    else if (nrm <= st->tol) st->done = FGB_PCG_RTOL;
-    else if (st->niter >= st->maxit) st->done = FGB_PCG_MAXIT;
-    else if (st->stall >= 1) st->done = FGB_PCG_STAGNATED;  // the caller continues in FP64
-    st->beta = first ? 0.0 : trz / st->rz_prev;
-    st->rz = trz;
-    st->rr = trr;
-    st->r_upd = nrm;
-    st->need_update = 0;
+    __threadfence();
+    ok = good && !*err;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+// Block sums of two per-thread values (T: float or double; warp shuffles in T,
+// the warps' sums added in FP64 in order by warp 0), written by thread 0 to
+// part0[blockIdx.x] and (if part1) part1[blockIdx.x].
+template <typename T>
+__device__ void block_partials2(T v0, T v1, double* part0, double* part1) {
+  __shared__ double2 ws[32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  v0 = warp_sum(v0);
+  v1 = warp_sum(v1);
+  __syncthreads();
+  if (lane == 0) ws[wid] = make_double2(static_cast<double>(v0), static_cast<double>(v1));
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    double2 t = lane < nw ? ws[lane] : make_double2(0.0, 0.0);
+    t.x = warp_sum(t.x);
+    t.y = warp_sum(t.y);
+    if (lane == 0) {
+      part0[blockIdx.x] = t.x;
+      if (part1) part1[blockIdx.x] = t.y;
+    }
+  }
+}
+
+// Sums of the grid's partials (after a barrier), the same in every block:
+// warp 0 loads them through L2 in one unrolled round trip per 320 blocks and
+// adds them in block order; the result is handed to the block in shared memory.
+__device__ double2 grid_totals2(const double* part0, const double* part1, int nb) {
+  __shared__ double2 res;
+  constexpr int kPer = 10;
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    double a = 0.0, b = 0.0;
+    for (int base = 0; base < nb; base += 32 * kPer) {
+      double pa[kPer], pb[kPer];
+#pragma unroll
+      for (int u = 0; u < kPer; ++u) {
+        const int k = base + lane + 32 * u;
+        pa[u] = k < nb ? __ldcg(part0 + k) : 0.0;
+        pb[u] = (part1 && k < nb) ? __ldcg(part1 + k) : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < kPer; ++u) {
+        a += pa[u];
+        b += pb[u];
+      }
+    }
+    a = warp_sum(a);
+    b = warp_sum(b);
+    if (lane == 0) res = make_double2(a, b);
+  }
+  __syncthreads();
+  return res;
+}
+
+template <bool D16, typename V>
+__global__ void __launch_bounds__(kPersistThreads, 2) sell_mixed_persistent(PersistArgs P) {
+  __shared__ SellPcgState S;
+  if (threadIdx.x == 0) S = *P.st;
+  __syncthreads();
+  const SellView& A = P.A;
+  const int64_t n = A.n;
+  const int lane = threadIdx.x & 31;
+  const int64_t tid = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  const int64_t warp0 = tid >> 5, nwarps = stride >> 5;
+  const bool vec = aligned16(P.p, P.Ap) && aligned16(P.y, P.r) && aligned16(P.z, P.dinv);
+  const int64_t n4 = vec ? n >> 2 : 0;
+  float4* P4 = reinterpret_cast<float4*>(P.p);
+  const float4* AP4 = reinterpret_cast<const float4*>(P.Ap);
+  float4* Y4 = reinterpret_cast<float4*>(P.y);
+  float4* R4 = reinterpret_cast<float4*>(P.r);
+  float4* Z4 = reinterpret_cast<float4*>(P.z);
+  const float4* D4 = reinterpret_cast<const float4*>(P.dinv);
+  const long long cap = S.maxit + 16;
+  while (!S.done) {
+    // p = z + beta p
+    {
+      const float beta = static_cast<float>(S.beta);
+      for (int64_t g = tid; g < n4; g += stride) {
+        const float4 zv = __ldcg(Z4 + g);
+        float4 pv = __ldcg(P4 + g);
+        pv.x = zv.x + beta * pv.x;
+        pv.y = zv.y + beta * pv.y;
+        pv.z = zv.z + beta * pv.z;
+        pv.w = zv.w + beta * pv.w;
+        P4[g] = pv;
+      }
+      for (int64_t i = 4 * n4 + tid; i < n; i += stride) P.p[i] = __ldcg(P.z + i) + beta * __ldcg(P.p + i);
+    }
+    if (!grid_barrier(P.st)) return;
+    // Ap = A p and p.Ap
+    {
+      float pap = 0.0f;
+      const GatherCG<float> gp{P.p};
+      for (int64_t s = warp0; s < A.n_slices; s += nwarps) {
+        const float acc = slice_row<D16, float, float>(A, P.val32, s, lane, gp);
+        const int32_t row = A.perm[s * kSellC + lane];
+        if (row >= 0) {
+          P.Ap[row] = acc;
+          pap += __ldcg(P.p + row) * acc;
+        }
+      }
+      block_partials2(pap, 0.0f, P.bpart, nullptr);
+    }
+    if (!grid_barrier(P.st)) return;
+    // alpha; y += alpha p, r -= alpha Ap, z = Dinv r; r.z, r.r
+    {
+      const double pap = grid_totals2(P.bpart, nullptr, gridDim.x).x;
+      const bool ok = pap > 0.0 && isfinite(pap);
+      if (!ok) {
+        if (threadIdx.x == 0) {
+          S.done = isfinite(pap) ? FGB_PCG_BREAKDOWN : FGB_PCG_NONFINITE;
+          S.alpha = 0.0;
+        }
+        __syncthreads();
+        break;
+      }
+      const double alpha = S.rz / pap;
+      const float a32 = static_cast<float>(alpha);
+      float rz = 0.0f, rr = 0.0f;
+      for (int64_t g = tid; g < n4; g += stride) {
+        const float4 pv = __ldcg(P4 + g), av = __ldcg(AP4 + g), dv = __ldg(D4 + g);
+        float4 yv = __ldcg(Y4 + g), rv = __ldcg(R4 + g);
+        yv.x += a32 * pv.x; yv.y += a32 * pv.y; yv.z += a32 * pv.z; yv.w += a32 * pv.w;
+        rv.x -= a32 * av.x; rv.y -= a32 * av.y; rv.z -= a32 * av.z; rv.w -= a32 * av.w;
+        const float4 zv = make_float4(dv.x * rv.x, dv.y * rv.y, dv.z * rv.z, dv.w * rv.w);
+        Y4[g] = yv;
+        R4[g] = rv;
+        Z4[g] = zv;
+        rz += (rv.x * zv.x + rv.y * zv.y) + (rv.z * zv.z + rv.w * zv.w);
+        rr += (rv.x * rv.x + rv.y * rv.y) + (rv.z * rv.z + rv.w * rv.w);
+      }
+      for (int64_t i = 4 * n4 + tid; i < n; i += stride) {
+        P.y[i] += a32 * __ldcg(P.p + i);
+        const float ri = __ldcg(P.r + i) - a32 * __ldcg(P.Ap + i);
+        const float zi = P.dinv[i] * ri;
+        P.r[i] = ri;
+        P.z[i] = zi;
+        rz += ri * zi;
+        rr += ri * ri;
+      }
+      if (threadIdx.x == 0) S.alpha = alpha;
+      block_partials2(rz, rr, P.vpart, P.vpart + kSellMaxBlocks);
+    }
+    if (!grid_barrier(P.st)) return;
+    {
+      const double2 t = grid_totals2(P.vpart, P.vpart + kSellMaxBlocks, gridDim.x);
+      if (threadIdx.x == 0) {
+        mixed_iteration_scalars(S, t.x, t.y, P.delta);
+        if (S.niter >= cap && !S.done) S.done = FGB_PCG_MAXIT;
+      }
+      __syncthreads();
+    }
+    if (S.done || !S.need_update) continue;
+    // reliable update: x += y, y = 0 | r64 = b - A x, r, z | test
+    for (int64_t i = tid; i < n; i += stride) {
+      P.x[i] += static_cast<double>(__ldcg(P.y + i));
+      P.y[i] = 0.0f;
+    }
+    if (!grid_barrier(P.st)) return;
+    {
+      double rr64 = 0.0, rz = 0.0;
+      const GatherCG<double> gx{P.x};
+      const V* valr = static_cast<const V*>(P.valr);
+      for (int64_t s = warp0; s < A.n_slices; s += nwarps) {
+        const double acc = slice_row<D16, V, double>(A, valr, s, lane, gx);
+        const int32_t row = A.perm[s * kSellC + lane];
+        if (row >= 0) {
+          const double r64 = P.b[row] - acc;
+          rr64 += r64 * r64;
+          const float ri = static_cast<float>(r64);
+          const float zi = P.dinv[row] * ri;
+          P.r[row] = ri;
+          P.z[row] = zi;
+          rz += static_cast<double>(ri) * static_cast<double>(zi);
+        }
+      }
+      block_partials2(rr64, rz, P.vpart, P.vpart + kSellMaxBlocks);
+    }
+    if (!grid_barrier(P.st)) return;
+    {
+      const double2 t = grid_totals2(P.vpart, P.vpart + kSellMaxBlocks, gridDim.x);
+      if (threadIdx.x == 0) mixed_reliable_scalars(S, t.x, t.y, 0);
+      __syncthreads();
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    // the barrier words stay as they are in global memory
+    S.bar[0] = 0u;
+    S.bar[1] = *reinterpret_cast<volatile unsigned int*>(&P.st->bar[1]);
+    S.bar_err = *reinterpret_cast<volatile int*>(&P.st->bar_err);
+    *P.st = S;
   }
 }
 
@@ -878,6 +1158,31 @@ void mixed_body(const SellView& A, const float* val32, const double* val64, cons
   if (ctx) ctx->add_if(hif, reliable);
   else reliable(s);
   rec(ev, 4, s);
+}
+
+// Launches the persistent mixed solver as one cooperative kernel (two blocks
+// per SM, as many as stay resident); false when the device cannot run it that
+// way, in which case nothing was launched.
+template <bool D16, typename V>
+bool launch_persistent(const PersistArgs& P, cudaStream_t s) {
+  auto kern = sell_mixed_persistent<D16, V>;
+  int dev = 0, coop = 0, sms = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return false;
+  if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop) return false;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return false;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPersistThreads, 0) != cudaSuccess ||
+      per_sm < 1)
+    return false;
+  const int grid = sms * (per_sm < 2 ? per_sm : 2);
+  if (grid > kSellMaxBlocks) return false;
+  PersistArgs a = P;
+  void* args[] = {&a};
+  if (cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(kern), dim3(grid), dim3(kPersistThreads), args, 0,
+                                  s) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return true;
 }
 
 // Returns FGB_OK after the graph ran to completion.  *launched tells the caller
@@ -1137,6 +1442,24 @@ int32_t fgb_pcg_sell_mixed(const fgb_sell* A, const double* diag_inv64, const do
     ++launches;
     bool graphed = false;
     if (use_graph) {
+      // first choice: every iteration inside one persistent cooperative kernel
+      const PersistArgs pa{v, A->val32, A->val64 ? static_cast<const void*>(A->val64)
+                                                 : static_cast<const void*>(A->val32),
+                           b, x, w.dinv32, w.r, w.z, w.p0, w.Ap, w.y, w.bpart, w.partials, w.st, delta};
+      bool launched = false;
+      with_cols(v, [&](auto d16) {
+        constexpr bool D = decltype(d16)::value;
+        launched = A->val64 ? launch_persistent<D, double>(pa, s) : launch_persistent<D, float>(pa, s);
+      });
+      if (launched) {
+        if ((rc = read_state(w.st, &h, s))) return rc;
+        if (h.bar_err) return FGB_ERR_CUDA;  // a grid barrier gave up (cannot happen with all blocks resident)
+        graphed = true;
+        used_graph = 2;
+        ++launches;
+      }
+    }
+    if (use_graph && !graphed) {
       bool launched = false;
       rc = graph_loop([&](CaptureCtx& c) {
         mixed_body(v, A->val32, A->val64, diag_inv64, b, x, w, delta, 0, nullptr, c.cs, &c);

@@ -218,6 +218,15 @@ struct GatherX {
   __device__ __forceinline__ T operator()(int32_t j) const { return x[j]; }
 };
 
+// Gather through L2 only (ld.global.cg): for vectors that other blocks of the
+// same (persistent) kernel rewrite between phases, where an L1 line filled in
+// an earlier phase would be stale.
+template <typename T>
+struct GatherCG {
+  const T* x;
+  __device__ __forceinline__ T operator()(int32_t j) const { return __ldcg(x + j); }
+};
+
 // p_new[j] = z[j] + beta * p_old[j], formed on the fly for every gathered column
 template <typename T>
 struct GatherP {

@@ -43,7 +43,7 @@ def _info_dict(info, extra=None):
     out = {"residual": info.residual, "niter": int(info.niter), "reason": int(info.reason),
            "launches": int(info.launches), "kernel_ms": float(info.kernel_ms),
            "kernel_launches": int(info.kernel_launches), "other_ms": float(info.other_ms),
-           "extra_ms": float(info.extra_ms), "graph": bool(info.graph)}
+           "extra_ms": float(info.extra_ms), "graph": bool(info.graph), "persistent": int(info.graph) == 2}
     if extra:
         out.update(extra)
     return out

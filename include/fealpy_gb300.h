@@ -75,7 +75,8 @@ typedef struct fgb_pcg_info {
                       /* kernel of those iterations                         */
   double extra_ms;    /* profile != 0: time of the remaining kernels of     */
                       /* those iterations (p update, reliable-update check) */
-  int32_t graph;      /* 1 if the iterations ran as a device-side graph loop */
+  int32_t graph;      /* 1 if the iterations ran as a device-side graph loop, */
+                      /* 2 as one persistent cooperative kernel (mixed)      */
   int32_t reserved;
 } fgb_pcg_info;
 
