@@ -1441,8 +1441,8 @@ int32_t fgb_pcg_sell_mixed(const fgb_sell* A, const double* diag_inv64, const do
     });
     ++launches;
     bool graphed = false;
-    if (use_graph) {
-      // first choice: every iteration inside one persistent cooperative kernel
+    if (use_graph == 2) {
+      // every iteration inside one persistent cooperative kernel
       const PersistArgs pa{v, A->val32, A->val64 ? static_cast<const void*>(A->val64)
                                                  : static_cast<const void*>(A->val32),
                            b, x, w.dinv32, w.r, w.z, w.p0, w.Ap, w.y, w.bpart, w.partials, w.st, delta};

@@ -443,7 +443,7 @@ def pcg_sell_mixed(S: SellMatrix, dinv64, b, x, rtol, delta=0.1, maxit=100000, c
     info = _lib.PcgInfo()
     di, bi, xi = S.to_inner(dinv64), S.to_inner(b), S.to_inner(x)
     call("fgb_pcg_sell_mixed", ctypes.byref(S.desc), ptr(di), ptr(bi), ptr(xi), float(rtol), float(delta),
-         int(maxit), int(check_every), int(bool(graph)), int(bool(profile)), ptr(ws), ws.numel(), ctypes.byref(info),
+         int(maxit), int(check_every), int(graph), int(bool(profile)), ptr(ws), ws.numel(), ctypes.byref(info),
          stream_ptr(dev))
     S.to_outer(xi, out=x)
     _lib.add_launches(info.launches)

@@ -59,6 +59,10 @@ _LAUNCH_CACHE = {}
 # save), None = delta-coded columns of the renumbered matrix where the bridges
 # add at most 25% entries, True = delta-coded always
 SELL_D16: Optional[bool] = False
+# cg_mixed with graph=True runs systems up to this many rows as one persistent
+# cooperative kernel (no launches per iteration), larger ones as the CUDA-graph
+# loop of separate kernels, whose gathers keep their L1 hits
+PERSISTENT_MAX_ROWS = 1 << 18
 
 
 def _sell_of(A: CSRTensor, want32: bool, tune: bool = True):
@@ -156,7 +160,8 @@ def cg_mixed(A: CSRTensor, b: torch.Tensor, x0: Optional[torch.Tensor] = None, M
     x = torch.zeros_like(b) if x0 is None else x0.to(torch.float64).clone()
     if solver_format == "sell":
         S = _sell_of(A, want32=True)
-        info = K.pcg_sell_mixed(S, dinv, b, x, rtol, delta, maxit, check_every, graph and not profile, profile)
+        mode = 0 if (profile or not graph) else (2 if A.shape[0] <= PERSISTENT_MAX_ROWS else 1)
+        info = K.pcg_sell_mixed(S, dinv, b, x, rtol, delta, maxit, check_every, mode, profile)
     elif solver_format == "csr":
         if A.values.dtype != torch.float64:
             raise NotImplementedError("solver_format='csr' cg_mixed needs an FP64 matrix")

@@ -361,7 +361,12 @@ int32_t fgb_permute(int32_t dtype, int64_t n, const int32_t* order, const void* 
  * graph with a device-side while loop (no host polling; profile ignored).
  * fgb_pcg_sell_mixed needs val32; its FP64 residual recomputation uses val64
  * when present, else the FP32 values themselves (an FP32-assembled operator,
- * accumulated in FP64), and then solves that operator to rtol. */
+ * accumulated in FP64), and then solves that operator to rtol.  Its
+ * use_graph = 2 runs all iterations in one persistent cooperative kernel
+ * (grid barriers between phases; falls back to the graph loop where
+ * cooperative launch is unavailable): no launch overhead per iteration, but
+ * its gathers bypass L1 (other blocks rewrite p within the launch), so it
+ * suits small systems. */
 size_t fgb_pcg_sell_workspace_bytes(int64_t n);
 int32_t fgb_pcg_sell_f64(const fgb_sell* A, const double* diag_inv, const double* b, double* x,
                          double atol, double rtol, int64_t maxit, int32_t check_every,
