@@ -59,10 +59,15 @@ _LAUNCH_CACHE = {}
 # save), None = delta-coded columns of the renumbered matrix where the bridges
 # add at most 25% entries, True = delta-coded always
 SELL_D16: Optional[bool] = False
-# cg_mixed with graph=True runs systems up to this many rows as one persistent
-# cooperative kernel (no launches per iteration), larger ones as the CUDA-graph
-# loop of separate kernels, whose gathers keep their L1 hits
-PERSISTENT_MAX_ROWS = 1 << 18
+# cg_mixed with graph=True runs systems of at most this many rows and at most
+# this many nonzeros per row on average as one persistent cooperative kernel
+# (no launches per iteration); the others as the CUDA-graph loop of separate
+# kernels, whose gathers keep their L1 hits.  Measured per solve (graph loop /
+# persistent): P1 triangles 4.2 K rows 4.6 / 4.0 ms, 66 K rows 18.2 / 15.7 ms,
+# 263 K rows 50.4 / 37.3 ms; P2 tetrahedra 118 K rows 6.1 / 6.5 ms, 531 K rows
+# 16.0 / 16.4 ms.
+PERSISTENT_MAX_ROWS = 1 << 19
+PERSISTENT_MAX_ROW_NNZ = 10
 
 
 def _sell_of(A: CSRTensor, want32: bool, tune: bool = True):
@@ -160,7 +165,8 @@ def cg_mixed(A: CSRTensor, b: torch.Tensor, x0: Optional[torch.Tensor] = None, M
     x = torch.zeros_like(b) if x0 is None else x0.to(torch.float64).clone()
     if solver_format == "sell":
         S = _sell_of(A, want32=True)
-        mode = 0 if (profile or not graph) else (2 if A.shape[0] <= PERSISTENT_MAX_ROWS else 1)
+        small = A.shape[0] <= PERSISTENT_MAX_ROWS and A.nnz <= PERSISTENT_MAX_ROW_NNZ * A.shape[0]
+        mode = 0 if (profile or not graph) else (2 if small else 1)
         info = K.pcg_sell_mixed(S, dinv, b, x, rtol, delta, maxit, check_every, mode, profile)
     elif solver_format == "csr":
         if A.values.dtype != torch.float64:
