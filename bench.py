@@ -331,12 +331,22 @@ def run_ours(args):
     value = replica_value(gdof, world, mixed["ms_per_step"])
     # dominant kernel: the fused FP32 PCG SpMV (p = z + beta p_old, Ap = A p, p.Ap)
     nnz = mixed["nnz"]
-    # values + columns of the real entries (4-byte columns, or 2-byte steps plus
-    # a first column per row), the slot->row map, p read once and Ap written
-    # once (FP32 vectors)
+    # SpMV algorithmic bytes B_spmv = nnz (s + 4) + n (8 + 2 s) with s = 4:
+    # value + column per nonzero, a row pointer, x read once and y written once
+    # (the formula of the measurement definition, used verbatim; the SELL copy
+    # reads a 4-byte slot->row map and an 8-byte slice pointer per 32 rows in
+    # place of the row pointer).  With 2-byte column steps: nnz (s + 2) + n (12 + 2 s).
     d16 = mixed["sell_cols"] == "d16"
-    bytes_per_launch = nnz * (4 + 2) + gdof * (4 + 4 + 4 + 4) if d16 else nnz * (4 + 4) + gdof * (4 + 4 + 4)
+    bytes_per_launch = nnz * (4 + 2) + gdof * (12 + 8) if d16 else nnz * (4 + 4) + gdof * (8 + 8)
     achieved = bytes_per_launch / (mixed["kernel_ms_avg"] / 1e3) / 1e9 if mixed["kernel_ms_avg"] > 0 else 0.0
+    # whole FP32 iteration: B_it = B_spmv + 11 n s (the vector traffic of the
+    # update kernels), over the live time per iteration of the timed solve (the
+    # step minus its non-PCG stages as measured in the profiling solve)
+    pre_ms = sum(v for k, v in mixed["stages_ms"].items() if k in STAGES and k != "pcg")
+    it_ms = max(mixed["ms_per_step"] - pre_ms, 1e-9) / max(mixed["niter"], 1)
+    bytes_per_iter = bytes_per_launch + 11 * gdof * 4
+    iter_roof = {"bytes_per_iteration": bytes_per_iter, "us_per_iteration": it_ms * 1e3,
+                 "achieved": bytes_per_iter / (it_ms / 1e3) / 1e9, "unit": "GB/s"}
     traffic = None
     tp = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tp) and n == 64:
@@ -384,7 +394,8 @@ def run_ours(args):
                          "kernel": "sell_pcg_spmv<float> (SELL-32" + (", 16-bit column steps" if d16 else "") +
                                    "; Ap = A p and p.Ap)",
                          "algorithmic_bytes_per_launch": bytes_per_launch,
-                         "avg_launch_ms": mixed["kernel_ms_avg"], "peak_source": peak_kind},
+                         "avg_launch_ms": mixed["kernel_ms_avg"], "peak_source": peak_kind,
+                         "iteration": dict(iter_roof, frac=iter_roof["achieved"] / peak if peak else None)},
             "clocks": mixed["clocks"],
             "cpu_baseline": cpu,
             "serving": serving,
