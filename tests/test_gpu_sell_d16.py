@@ -48,11 +48,24 @@ def _spd(n, extra_cols, seed=0):
     return A
 
 
-def _build(A, dev, d16, want32=True):
+def _build(A, dev, d16, want32=True, blocks=None):
     from fealpy_gb300 import kernels as K
     t = lambda a: torch.as_tensor(a, device=dev)
     return K.sell_build(t(A.indptr.astype(np.int64)), t(A.indices.astype(np.int32)), t(A.data), None, want64=True,
-                        want32=want32, d16=d16)
+                        want32=want32, d16=d16, blocks=blocks)
+
+
+def _merge_order(sizes):
+    """Stable merge of dof blocks by key floor(j * n0 / nb): sort of all rows
+    by (key, block, j), the order the block renumbering computes in closed
+    form."""
+    keys = []
+    start = 0
+    for b, nb in enumerate(sizes):
+        for j in range(nb):
+            keys.append(((j * sizes[0]) // nb, b, j, start + j))
+        start += nb
+    return np.array([k[3] for k in sorted(keys)])
 
 
 def _check_spmv(S, A, dev):
@@ -147,3 +160,20 @@ def test_d16_solvers_match_int32_columns(golden_dir):
     assert rel_err(out[True][0], out[False][0].cpu().numpy()) < 1e-9
     assert rel_err(out[True][2], out[False][2].cpu().numpy()) < 1e-8
     assert rel_err(out[True][0], z["uh"]) < 1e-9
+
+
+def test_d16_block_merge_renumbering(golden_dir):
+    """The renumbering from the space's dof blocks: vertex dofs, then edge
+    (and for P3 triangles cell) dofs merged by relative position."""
+    dev = cuda()
+    import scipy.sparse as sp
+    for name, blocks in (("small_tet_p2.npz", lambda z: [len(z["node"]), len(z["edge"])]),
+                         ("small_tri_p3.npz", lambda z: [len(z["node"]), 2 * len(z["edge"]), len(z["cell"])])):
+        z = np.load(os.path.join(golden_dir, name))
+        n = len(z["crow"]) - 1
+        bl = blocks(z)
+        assert sum(bl) == n
+        A = sp.csr_matrix((z["val"], z["col"], z["crow"]), shape=(n, n))
+        S = _build(A, dev, True, blocks=bl)
+        assert np.array_equal(S.order.cpu().numpy(), _merge_order(bl))
+        _check_spmv(S, A, dev)

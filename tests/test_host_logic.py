@@ -112,3 +112,25 @@ def test_tet_from_box_matches_oracle():
     assert np.array_equal(mesh.edge.numpy(), topo["edge"])
     assert np.array_equal(mesh.face.numpy(), topo["face"])
     assert np.array_equal(mesh.cell_to_ipoint(2).numpy(), O.cell_to_dof(cell, topo, node.shape[0], 2))
+
+
+@pytest.mark.parametrize("kind,p", [("tri", 1), ("tri", 2), ("tri", 3), ("tet", 1), ("tet", 2), ("tet", 3)])
+def test_dof_blocks_partition_the_numbering(kind, p):
+    """dof_blocks(): the contiguous vertex/edge/face/cell ranges of the global
+    dof numbering, in order (the input of the block-merge renumbering of the
+    delta-coded SELL copy); for vector spaces scaled or repeated by component."""
+    mesh = TriangleMesh.from_box([0, 1, 0, 1], 3, 2) if kind == "tri" else \
+        TetrahedronMesh.from_box([0, 1, 0, 1, 0, 1], 2, 2, 1)
+    space = LagrangeFESpace(mesh, p=p)
+    blocks = space.dof_blocks()
+    assert sum(blocks) == space.number_of_global_dofs() and all(b > 0 for b in blocks)
+    assert blocks[0] == mesh.number_of_nodes()
+    c2d = space.cell_to_dof().numpy()
+    starts = np.cumsum([0] + blocks)
+    # the first dofs of a cell (its vertices) lie in the vertex block, the
+    # rest in the later blocks
+    assert np.all(c2d[:, :mesh.cell.shape[1]] < starts[1]) if p == 1 else np.all(c2d.max(axis=1) >= starts[1])
+    gd = mesh.geo_dimension()
+    inter = TensorFunctionSpace(space, (-1, gd)).dof_blocks()
+    major = TensorFunctionSpace(space, (gd, -1)).dof_blocks()
+    assert inter == [gd * b for b in blocks] and major == blocks * gd
