@@ -390,17 +390,15 @@ __device__ bool block_alpha(const double* bpart, int nwp, SellPcgState* st, doub
   return sh_ok != 0;
 }
 
-// kernel A: Ap = A p and per-block partials of p.Ap.  FUSED: p_new = z + beta p_old is
-// formed on the fly for every gathered column (one launch fewer per iteration,
-// but two gathers per entry).  Not FUSED: p has been updated in place by the
-// p-update kernel beforehand.  Both solvers use the unfused form: measured on
-// the P2 64^3 system (57.6 M nonzeros, FP32) the fused SpMV takes 95 us, the
-// plain one 79 us, and the p update a few microseconds; in FP64 the second
-// FMA per entry would also cost FP64 issue slots.
-template <typename T, bool FUSED, bool D16>
+// kernel A: Ap = A p and per-block partials of p.Ap; p has been updated in
+// place by the p-update kernel beforehand.  (Forming p = z + beta p_old on the
+// fly for every gathered column saves that launch but needs two gathers per
+// entry: measured on the P2 64^3 system, 57.6 M nonzeros in FP32, 95 us per
+// SpMV against 79 us, the p update taking a few microseconds; in FP64 the
+// second FMA per entry would also cost FP64 issue slots.)
+template <typename T, bool D16>
 __global__ void __launch_bounds__(1024, 1) sell_pcg_spmv(SellView A, const T* __restrict__ val,
-                                                              const T* __restrict__ z, const T* __restrict__ p_old,
-                                                              T* __restrict__ p_new, T* __restrict__ Ap,
+                                                              const T* __restrict__ p, T* __restrict__ Ap,
                                                               double* bpart, const SellPcgState* st) {
   // per-block combination of the warps' p.Ap without a block barrier at the
   // end: the last warp of the block to arrive adds the warps' slots in order
@@ -409,25 +407,16 @@ __global__ void __launch_bounds__(1024, 1) sell_pcg_spmv(SellView A, const T* __
   if (threadIdx.x == 0) arrivals = 0u;
   __syncthreads();
   if (st->done) return;
-  const T beta = static_cast<T>(st->beta);
   // p.Ap partials in T per thread and warp (FP32 in the FP32 iterations: FP64
   // arithmetic runs at a small fraction of the FP32 rate on this part), FP64
   // from the warp sums on
   T pap = T(0);
   SELL_WARP_LOOP(A) {
-    const T acc = FUSED ? slice_row<D16, T, T>(A, val, s, lane, GatherP<T>{z, p_old, beta})
-                        : slice_row<D16, T, T>(A, val, s, lane, GatherX<T>{p_old});
+    const T acc = slice_row<D16, T, T>(A, val, s, lane, GatherX<T>{p});
     const int32_t row = A.perm[s * kSellC + lane];
     if (row >= 0) {
-      T pi;
-      if (FUSED) {
-        pi = z[row] + beta * p_old[row];
-        p_new[row] = pi;
-      } else {
-        pi = p_old[row];
-      }
       Ap[row] = acc;
-      pap += pi * acc;
+      pap += p[row] * acc;
     }
   }
   pap = warp_sum(pap);
@@ -995,7 +984,6 @@ struct EventPairs {
     for (int k = 0; k < kPer * cap; ++k) cudaEventDestroy(ev[k]);
     delete[] ev;
   }
-  cudaEvent_t at(int k, int j) const { return on ? ev[kPer * k + j] : nullptr; }
   const cudaEvent_t* of(int k) const { return on ? ev + kPer * k : nullptr; }
   // spmv = t2 - t1, update = t3 - t2, extra = (t1 - t0) + (t4 - t3)
   void collect(int64_t executed) {
@@ -1111,8 +1099,7 @@ void f64_body(const SellView& A, const double* val, const double* dinv, double* 
   sell_p_update<<<VEC_LAUNCH(A.n, s)>>>(A.n, w.z, w.p0, w.st);
   rec(ev, 1, s);
   with_cols(A, [&](auto d16) {
-    sell_pcg_spmv<double, false, decltype(d16)::value>
-        <<<SLICE_LAUNCH(A, s)>>>(A, val, w.z, w.p0, nullptr, w.Ap, w.bpart, w.st);
+    sell_pcg_spmv<double, decltype(d16)::value><<<SLICE_LAUNCH(A, s)>>>(A, val, w.p0, w.Ap, w.bpart, w.st);
   });
   rec(ev, 2, s);
   sell_pcg_update_f64<<<VEC_LAUNCH(A.n, s)>>>(A.n, dinv, w.p0, w.Ap, x, w.r, w.z, w.bpart, slice_blocks(A),
@@ -1136,8 +1123,7 @@ void mixed_body(const SellView& A, const float* val32, const double* val64, cons
   sell_p_update_f32<<<VEC_LAUNCH(A.n, s)>>>(A.n, w.z, p, w.st);
   rec(ev, 1, s);
   with_cols(A, [&](auto d16) {
-    sell_pcg_spmv<float, false, decltype(d16)::value>
-        <<<SLICE_LAUNCH(A, s)>>>(A, val32, w.z, p, nullptr, w.Ap, w.bpart, w.st);
+    sell_pcg_spmv<float, decltype(d16)::value><<<SLICE_LAUNCH(A, s)>>>(A, val32, p, w.Ap, w.bpart, w.st);
   });
   rec(ev, 2, s);
   sell_mixed_update<<<VEC_LAUNCH(A.n, s)>>>(A.n, w.dinv32, p, w.Ap, w.y, w.r, w.z, w.bpart, slice_blocks(A),

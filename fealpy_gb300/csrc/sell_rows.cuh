@@ -227,13 +227,4 @@ struct GatherCG {
   __device__ __forceinline__ T operator()(int32_t j) const { return __ldcg(x + j); }
 };
 
-// p_new[j] = z[j] + beta * p_old[j], formed on the fly for every gathered column
-template <typename T>
-struct GatherP {
-  const T* __restrict__ z;
-  const T* __restrict__ p;
-  T beta;
-  __device__ __forceinline__ T operator()(int32_t j) const { return z[j] + beta * p[j]; }
-};
-
 }  // namespace fgb
