@@ -23,7 +23,6 @@
 #include <cmath>
 #include <cstring>
 #include <type_traits>
-#include <utility>
 
 namespace fgb {
 
@@ -93,32 +92,6 @@ inline Launch slice_launch(const SellView& A) {
 // blocks of a slice-kernel launch (one p.Ap partial each)
 inline int slice_blocks(const SellView& A) { return slice_launch(A).blocks; }
 #define VEC_LAUNCH(n, s) vec_launch(n).blocks, vec_launch(n).threads, 0, s
-
-// Programmatic dependent launch: lets the next kernel of the stream be
-// scheduled while this one runs, then waits until the previous kernel has
-// completed and its writes are visible.  Both are no-ops for a launch that
-// carries no programmatic dependency.
-__device__ __forceinline__ void pdl_enter() {
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-  asm volatile("griddepcontrol.wait;" ::: "memory");
-}
-
-// Launch with a programmatic dependency on the previous kernel of the stream
-// (its blocks may be resident and waiting in pdl_enter before that kernel ends).
-template <typename... Exp, typename... Act>
-void launch_pdl(void (*kernel)(Exp...), int grid, int block, cudaStream_t s, Act&&... args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(grid);
-  cfg.blockDim = dim3(block);
-  cfg.dynamicSmemBytes = 0;
-  cfg.stream = s;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  at[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, kernel, std::forward<Act>(args)...);
-}
 
 // both pointers 16-byte aligned (vector kernels take 16-byte accesses then)
 __device__ __forceinline__ bool aligned16(const void* a, const void* b) {
@@ -433,7 +406,6 @@ __global__ void __launch_bounds__(1024, 1) sell_pcg_spmv(SellView A, const T* __
   __shared__ unsigned int arrivals;
   if (threadIdx.x == 0) arrivals = 0u;
   __syncthreads();
-  pdl_enter();
   if (st->done) return;
   // p.Ap partials in T per thread and warp (FP32 in the FP32 iterations: FP64
   // arithmetic runs at a small fraction of the FP32 rate on this part), FP64
@@ -504,7 +476,6 @@ __global__ void __launch_bounds__(1024, 1) sell_p_update(int64_t n, const double
 // thread and trip (16-byte accesses) when both vectors are 16-byte aligned
 __global__ void __launch_bounds__(1024, 1) sell_p_update_f32(int64_t n, const float* __restrict__ z,
                                                                   float* __restrict__ p, const SellPcgState* st) {
-  pdl_enter();
   if (st->done) return;
   const float beta = static_cast<float>(st->beta);
   const int64_t tid = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
@@ -605,7 +576,6 @@ __global__ void __launch_bounds__(1024, 1) sell_mixed_update(int64_t n, const fl
                                                                   const double* bpart, int nwp, double* partials,
                                                                   SellPcgState* st, double delta,
                                                                   cudaGraphConditionalHandle hif, int set_if) {
-  pdl_enter();
   const int64_t tid = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
   const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
   const bool vec = aligned16(p, Ap) && aligned16(y, r) && aligned16(z, dinv);
@@ -1152,28 +1122,12 @@ void mixed_body(const SellView& A, const float* val32, const double* val64, cons
   rec(ev, 0, s);
   sell_p_update_f32<<<VEC_LAUNCH(A.n, s)>>>(A.n, w.z, p, w.st);
   rec(ev, 1, s);
-  // the SpMV and the update carry a programmatic dependency on the kernel
-  // before them (their launch overlaps its tail) unless events are recorded
-  // between them (profiling)
-  const bool pdl = ev == nullptr;
   with_cols(A, [&](auto d16) {
-    auto k = sell_pcg_spmv<float, decltype(d16)::value>;
-    const Launch L = slice_launch(A);
-    if (pdl) launch_pdl(k, L.blocks, L.threads, s, A, val32, static_cast<const float*>(p), w.Ap, w.bpart,
-                        static_cast<const SellPcgState*>(w.st));
-    else k<<<L.blocks, L.threads, 0, s>>>(A, val32, p, w.Ap, w.bpart, w.st);
+    sell_pcg_spmv<float, decltype(d16)::value><<<SLICE_LAUNCH(A, s)>>>(A, val32, p, w.Ap, w.bpart, w.st);
   });
   rec(ev, 2, s);
-  {
-    const Launch L = vec_launch(A.n);
-    if (pdl)
-      launch_pdl(sell_mixed_update, L.blocks, L.threads, s, A.n, static_cast<const float*>(w.dinv32),
-                 static_cast<const float*>(p), static_cast<const float*>(w.Ap), w.y, w.r, w.z,
-                 static_cast<const double*>(w.bpart), slice_blocks(A), w.partials, w.st, delta, hif, ctx ? 1 : 0);
-    else
-      sell_mixed_update<<<L.blocks, L.threads, 0, s>>>(A.n, w.dinv32, p, w.Ap, w.y, w.r, w.z, w.bpart,
-                                                       slice_blocks(A), w.partials, w.st, delta, hif, ctx ? 1 : 0);
-  }
+  sell_mixed_update<<<VEC_LAUNCH(A.n, s)>>>(A.n, w.dinv32, p, w.Ap, w.y, w.r, w.z, w.bpart, slice_blocks(A),
+                                            w.partials, w.st, delta, hif, ctx ? 1 : 0);
   rec(ev, 3, s);
   auto reliable = [&](cudaStream_t rs) {
     sell_mixed_fold<<<VEC_LAUNCH(A.n, rs)>>>(A.n, x, w.y, w.st, 0);
