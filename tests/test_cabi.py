@@ -53,6 +53,20 @@ def test_argument_validation_without_gpu():
     assert lib.fgb_batch_create(4, 16, 16, 100, None, 0, ctypes.byref(h)) == 1
     assert lib.fgb_batch_create(4, 16, 16, 256, None, 0, ctypes.byref(h)) == 2
     assert lib.fgb_batch_destroy(None) == 1
+    # delta-coded SELL copy: sizes, block lists and missing arrays are refused on the host
+    one = ctypes.c_void_p(16)  # a non-null stand-in: nothing is dereferenced on these paths
+    sizes = (ctypes.c_int64 * 3)(4, 4, 4)
+    assert lib.fgb_sell_d16_workspace_bytes(0) == 0 and lib.fgb_sell_d16_workspace_bytes(100) > 0
+    assert lib.fgb_sell_renumber(0, one, one, 0, None, one, one, None, 0, None) == 1
+    assert lib.fgb_sell_renumber(12, one, one, 17, sizes, one, one, None, 0, None) == 1   # too many blocks
+    assert lib.fgb_sell_renumber(13, one, one, 3, sizes, one, one, None, 0, None) == 1    # sizes do not add up
+    assert lib.fgb_sell_renumber(12, one, one, 1, None, one, one, None, 0, None) == 1     # no sizes
+    assert lib.fgb_sell_renumber(12, one, one, 0, None, one, one, None, 0, None) == 2     # min-column order: workspace
+    assert lib.fgb_csr_permute(0, one, one, None, None, one, one, one, one, None, None, None, 0, None) == 1
+    assert lib.fgb_sell_d16_indptr(5, one, one, None, None, 0, None) == 1
+    assert lib.fgb_sell_fill_d16(5, one, one, None, None, one, one, one, None, None, None, None) == 1
+    assert lib.fgb_permute(1, 5, one, one, one, 0, None) == 1                             # src == dst
+    assert lib.fgb_permute(7, 5, one, one, ctypes.c_void_p(32), 0, None) == 1             # bad dtype
 
 
 def test_build_targets_sm103a():
