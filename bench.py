@@ -610,8 +610,10 @@ def run_elasticity(args):
     from fealpy_gb300.fem import BilinearForm, LinearForm, LinearElasticityIntegrator, VectorSourceIntegrator
     from fealpy_gb300.fem import DirichletBC
     from fealpy_gb300.workloads import elasticity_tet_box
+    from fealpy_gb300 import solver as SV
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
+    SV.SELL_TRIPLES = not args.no_triples
     n = args.elast_n
     node_np, cell_np, scale_np = elasticity_tet_box(n)
     mesh = F.TetrahedronMesh(torch.as_tensor(node_np, device=dev), torch.as_tensor(cell_np, device=dev))
@@ -652,7 +654,9 @@ def run_elasticity(args):
         res[mode] = {"ms_per_step": ms, "dof_per_s": gdof / (ms / 1e3), "cg_iters": info["niter"],
                      "true_relres": float(torch.linalg.norm(r) / torch.linalg.norm(F2)),
                      "fp64_iterations": info.get("fp64_iterations", info["niter"] if mode == "fp64" else 0),
-                     "x": x, "nnz": A2.nnz}
+                     "x": x, "nnz": A2.nnz,
+                     "sell": "node triples" if A2._sell.node_triples else ("16-bit steps" if A2._sell.d16 else
+                                                                         "4-byte columns")}
     err = float((res["mixed"]["x"] - res["fp64"]["x"]).abs().max() / res["fp64"]["x"].abs().max())
     for m in res:
         res[m].pop("x")
@@ -770,6 +774,8 @@ def main():
                     help="c2: the P2 tet box (default, the headline line); batched: 256 uneven triangle meshes; "
                          "serving: the request stream; elasticity: P1 vector elasticity on a tet box")
     ap.add_argument("--elast-n", type=int, default=128)
+    ap.add_argument("--no-triples", action="store_true",
+                    help="elasticity: SELL copy with a column per entry instead of one per node triple")
     ap.add_argument("--batch-count", type=int, default=256)
     ap.add_argument("--batch-precision", choices=["mixed", "fp64"], default="mixed",
                     help="iterations of the batched solve: FP32 with FP64 refinement (default) or plain FP64")

@@ -38,26 +38,34 @@ struct SellView {
   int blocks;
   const uint16_t* col16;  // delta-coded columns (then col is unused) or null
   const int32_t* col0;    // first column of every slot's row (delta-coded copies)
+  int node_triples;       // 1: slots are node triples (col = 3c, three values each)
 };
 
-// Row of slot (s, lane): sum over entries of val * g(col), for either column
-// format.  The slice width is a multiple of 4 entries.
-template <bool D16, typename V, typename T, typename G>
+// Storage formats of a SELL copy: 4-byte columns, 16-bit column steps, node
+// triples.
+constexpr int kColsI32 = 0, kColsD16 = 1, kColsB3 = 2;
+
+// Row of slot (s, lane): sum over entries of val * g(col), for each storage
+// format.  The slice width is a multiple of 4 slots.
+template <int FMT, typename V, typename T, typename G>
 __device__ __forceinline__ T slice_row(const SellView& A, const V* __restrict__ val, int64_t s, int lane,
                                        const G& g) {
   const int64_t sbase = A.slice_ptr[s];
   const int w = static_cast<int>((A.slice_ptr[s + 1] - sbase) >> 5);
-  if constexpr (D16)
+  if constexpr (FMT == kColsD16)
     return sell_row_acc_d16<V, T>(A.col16, A.col0[s * kSellC + lane], val, sbase, w, lane, g);
+  else if constexpr (FMT == kColsB3)
+    return sell_row_acc_b3<V, T>(A.col, val, sbase, w, lane, g);
   else
     return sell_row_acc<V, T>(A.col, val, sbase, w, lane, g);
 }
 
-// Launch `f(std::integral_constant<bool, D16>)` for the column format of A.
+// Launch `f(std::integral_constant<int, FMT>)` for the storage format of A.
 template <typename F>
 void with_cols(const SellView& A, F&& f) {
-  if (A.col16) f(std::true_type{});
-  else f(std::false_type{});
+  if (A.node_triples) f(std::integral_constant<int, kColsB3>{});
+  else if (A.col16) f(std::integral_constant<int, kColsD16>{});
+  else f(std::integral_constant<int, kColsI32>{});
 }
 
 // Launch shapes.  Vector kernels: two 512-thread blocks per SM (few blocks
@@ -161,7 +169,7 @@ __global__ void sell_fill_kernel(int64_t n_slices, const int64_t* __restrict__ s
 }
 
 // ------------------------------------------------------------------- SpMV
-template <typename T, bool D16>
+template <typename T, int FMT>
 __global__ void __launch_bounds__(1024, 1) sell_spmv_kernel(SellView A, const T* __restrict__ val,
                                                                  const T* __restrict__ x, T* __restrict__ y) {
   const int lane = threadIdx.x & 31;
@@ -169,7 +177,7 @@ __global__ void __launch_bounds__(1024, 1) sell_spmv_kernel(SellView A, const T*
   const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
   const GatherX<T> g{x};
   for (int64_t s = warp; s < A.n_slices; s += nwarps) {
-    const T acc = slice_row<D16, T, T>(A, val, s, lane, g);
+    const T acc = slice_row<FMT, T, T>(A, val, s, lane, g);
     const int32_t row = A.perm[s * kSellC + lane];
     if (row >= 0) y[row] = acc;
   }
@@ -312,7 +320,7 @@ __device__ bool sell_last_block(T v0, T v1, double* partials, unsigned int* coun
   for (int64_t s = warp0; s < (A).n_slices; s += nwarps)
 
 // r = b - A x ; z = Dinv r ; p = z ; rz, b.b   (T = FP64 state)
-template <typename T, bool D16>
+template <typename T, int FMT>
 __global__ void __launch_bounds__(1024, 1) sell_pcg_init(SellView A, const T* __restrict__ val,
                                                               const T* __restrict__ dinv, const T* __restrict__ b,
                                                               const T* __restrict__ x, T* __restrict__ r,
@@ -320,7 +328,7 @@ __global__ void __launch_bounds__(1024, 1) sell_pcg_init(SellView A, const T* __
                                                               SellPcgState* st) {
   double rz = 0.0, bb = 0.0;
   SELL_WARP_LOOP(A) {
-    const T acc = slice_row<D16, T, T>(A, val, s, lane, GatherX<T>{x});
+    const T acc = slice_row<FMT, T, T>(A, val, s, lane, GatherX<T>{x});
     const int32_t row = A.perm[s * kSellC + lane];
     if (row >= 0) {
       const T bi = b[row];
@@ -396,7 +404,7 @@ __device__ bool block_alpha(const double* bpart, int nwp, SellPcgState* st, doub
 // entry: measured on the P2 64^3 system, 57.6 M nonzeros in FP32, 95 us per
 // SpMV against 79 us, the p update taking a few microseconds; in FP64 the
 // second FMA per entry would also cost FP64 issue slots.)
-template <typename T, bool D16>
+template <typename T, int FMT>
 __global__ void __launch_bounds__(1024, 1) sell_pcg_spmv(SellView A, const T* __restrict__ val,
                                                               const T* __restrict__ p, T* __restrict__ Ap,
                                                               double* bpart, const SellPcgState* st) {
@@ -412,7 +420,7 @@ __global__ void __launch_bounds__(1024, 1) sell_pcg_spmv(SellView A, const T* __
   // from the warp sums on
   T pap = T(0);
   SELL_WARP_LOOP(A) {
-    const T acc = slice_row<D16, T, T>(A, val, s, lane, GatherX<T>{p});
+    const T acc = slice_row<FMT, T, T>(A, val, s, lane, GatherX<T>{p});
     const int32_t row = A.perm[s * kSellC + lane];
     if (row >= 0) {
       Ap[row] = acc;
@@ -646,7 +654,7 @@ __global__ void __launch_bounds__(1024, 1) sell_mixed_fold(int64_t n, double* __
 // FP32-assembled matrix, the operator the solve is for), true residual test,
 // then r = float(r64), z = Dinv r and beta from the replaced residual.  The
 // first call also builds the FP32 inverse diagonal and starts p = z.
-template <typename V, bool D16>
+template <typename V, int FMT>
 __global__ void __launch_bounds__(1024, 1) sell_mixed_reliable(SellView A, const V* __restrict__ val,
                                                                     const double* __restrict__ b,
                                                                     const double* __restrict__ x,
@@ -657,7 +665,7 @@ __global__ void __launch_bounds__(1024, 1) sell_mixed_reliable(SellView A, const
   if (!first && (st->done || !st->need_update)) return;
   double rr64 = 0.0, rz = 0.0;
   SELL_WARP_LOOP(A) {
-    const double acc = slice_row<D16, V, double>(A, val, s, lane, GatherX<double>{x});
+    const double acc = slice_row<FMT, V, double>(A, val, s, lane, GatherX<double>{x});
     const int32_t row = A.perm[s * kSellC + lane];
     if (row >= 0) {
       const double r64 = b[row] - acc;
@@ -799,7 +807,7 @@ __device__ double2 grid_totals2(const double* part0, const double* part1, int nb
   return res;
 }
 
-template <bool D16, typename V>
+template <int FMT, typename V>
 __global__ void __launch_bounds__(kPersistThreads, 2) sell_mixed_persistent(PersistArgs P) {
   __shared__ SellPcgState S;
   if (threadIdx.x == 0) S = *P.st;
@@ -840,7 +848,7 @@ __global__ void __launch_bounds__(kPersistThreads, 2) sell_mixed_persistent(Pers
       float pap = 0.0f;
       const GatherCG<float> gp{P.p};
       for (int64_t s = warp0; s < A.n_slices; s += nwarps) {
-        const float acc = slice_row<D16, float, float>(A, P.val32, s, lane, gp);
+        const float acc = slice_row<FMT, float, float>(A, P.val32, s, lane, gp);
         const int32_t row = A.perm[s * kSellC + lane];
         if (row >= 0) {
           P.Ap[row] = acc;
@@ -910,7 +918,7 @@ __global__ void __launch_bounds__(kPersistThreads, 2) sell_mixed_persistent(Pers
       const GatherCG<double> gx{P.x};
       const V* valr = static_cast<const V*>(P.valr);
       for (int64_t s = warp0; s < A.n_slices; s += nwarps) {
-        const double acc = slice_row<D16, V, double>(A, valr, s, lane, gx);
+        const double acc = slice_row<FMT, V, double>(A, valr, s, lane, gx);
         const int32_t row = A.perm[s * kSellC + lane];
         if (row >= 0) {
           const double r64 = P.b[row] - acc;
@@ -956,7 +964,8 @@ using namespace fgb;
 namespace {
 
 SellView view_of(const fgb_sell* A) {
-  return SellView{A->n, A->n_slices, A->slice_ptr, A->perm, A->col, A->threads, A->blocks, A->col16, A->col0};
+  return SellView{A->n,   A->n_slices, A->slice_ptr, A->perm, A->col,
+                  A->threads, A->blocks, A->col16,  A->col0, A->node_triples};
 }
 
 bool launch_ok(const fgb_sell* A) {
@@ -1132,7 +1141,7 @@ void mixed_body(const SellView& A, const float* val32, const double* val64, cons
   auto reliable = [&](cudaStream_t rs) {
     sell_mixed_fold<<<VEC_LAUNCH(A.n, rs)>>>(A.n, x, w.y, w.st, 0);
     with_cols(A, [&](auto d16) {
-      constexpr bool D = decltype(d16)::value;
+      constexpr int D = decltype(d16)::value;
       if (val64)
         sell_mixed_reliable<double, D><<<SLICE_LAUNCH(A, rs)>>>(A, val64, b, x, dinv64, w.dinv32, w.r, w.z,
                                                                 nullptr, w.partials, w.st, 0);
@@ -1149,9 +1158,9 @@ void mixed_body(const SellView& A, const float* val32, const double* val64, cons
 // Launches the persistent mixed solver as one cooperative kernel (two blocks
 // per SM, as many as stay resident); false when the device cannot run it that
 // way, in which case nothing was launched.
-template <bool D16, typename V>
+template <int FMT, typename V>
 bool launch_persistent(const PersistArgs& P, cudaStream_t s) {
-  auto kern = sell_mixed_persistent<D16, V>;
+  auto kern = sell_mixed_persistent<FMT, V>;
   int dev = 0, coop = 0, sms = 0, per_sm = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return false;
   if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop) return false;
@@ -1417,7 +1426,7 @@ int32_t fgb_pcg_sell_mixed(const fgb_sell* A, const double* diag_inv64, const do
     if ((rc = set_tol(w.st, rtol * h.b_norm, s))) return rc;
     // initial residual in FP64, its FP32 copy, z and p = z
     with_cols(v, [&](auto d16) {
-      constexpr bool D = decltype(d16)::value;
+      constexpr int D = decltype(d16)::value;
       if (A->val64)
         sell_mixed_reliable<double, D><<<SLICE_LAUNCH(v, s)>>>(v, A->val64, b, x, diag_inv64, w.dinv32, w.r, w.z,
                                                                w.p0, w.partials, w.st, 1);
@@ -1434,7 +1443,7 @@ int32_t fgb_pcg_sell_mixed(const fgb_sell* A, const double* diag_inv64, const do
                            b, x, w.dinv32, w.r, w.z, w.p0, w.Ap, w.y, w.bpart, w.partials, w.st, delta};
       bool launched = false;
       with_cols(v, [&](auto d16) {
-        constexpr bool D = decltype(d16)::value;
+        constexpr int D = decltype(d16)::value;
         launched = A->val64 ? launch_persistent<D, double>(pa, s) : launch_persistent<D, float>(pa, s);
       });
       if (launched) {

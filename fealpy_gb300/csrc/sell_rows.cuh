@@ -212,6 +212,101 @@ __device__ __forceinline__ T sell_row_acc_d16(const uint16_t* __restrict__ d16, 
   return acc;
 }
 
+// ------------------------------------------------ node triples (vector problems)
+// For a vector space with three interleaved components (dof = 3 node + comp)
+// every nonzero of a row sits in a run of three consecutive columns 3c..3c+2:
+// one 4-byte column per triple (3c) and the triple's three values, zero where
+// the matrix has no entry.  FP32: 16 bytes per three entries instead of 24.
+// Triple slots follow the same SELL-32x4 layout as scalar entries (four
+// triples per lane and pack); the values of slot k are val[3k..3k+2].
+struct Tri4F {
+  int4 c;
+  float4 a, b, d;  // a.x a.y a.z | a.w b.x b.y | b.z b.w d.x | d.y d.z d.w
+};
+struct Tri4D {
+  int4 c;
+  double2 v0, v1, v2, v3, v4, v5;
+};
+
+__device__ __forceinline__ Tri4F load_triples(const int32_t* col, const float* val, int64_t off) {
+  Tri4F t;
+  t.c = __ldcs(reinterpret_cast<const int4*>(col + off));
+  const float4* v = reinterpret_cast<const float4*>(val + 3 * off);
+  t.a = __ldcs(v);
+  t.b = __ldcs(v + 1);
+  t.d = __ldcs(v + 2);
+  return t;
+}
+
+__device__ __forceinline__ Tri4D load_triples(const int32_t* col, const double* val, int64_t off) {
+  Tri4D t;
+  t.c = __ldcs(reinterpret_cast<const int4*>(col + off));
+  const double2* v = reinterpret_cast<const double2*>(val + 3 * off);
+  t.v0 = __ldcs(v);
+  t.v1 = __ldcs(v + 1);
+  t.v2 = __ldcs(v + 2);
+  t.v3 = __ldcs(v + 3);
+  t.v4 = __ldcs(v + 4);
+  t.v5 = __ldcs(v + 5);
+  return t;
+}
+
+template <typename T, typename G>
+__device__ __forceinline__ T triple_dot(T acc, int32_t c, T a, T b, T d, const G& g) {
+  acc += a * g(c);
+  acc += b * g(c + 1);
+  acc += d * g(c + 2);
+  return acc;
+}
+
+template <typename T, typename G>
+__device__ __forceinline__ T triples_dot(const Tri4F& t, const G& g, T acc) {
+  acc = triple_dot<T>(acc, t.c.x, t.a.x, t.a.y, t.a.z, g);
+  acc = triple_dot<T>(acc, t.c.y, t.a.w, t.b.x, t.b.y, g);
+  acc = triple_dot<T>(acc, t.c.z, t.b.z, t.b.w, t.d.x, g);
+  acc = triple_dot<T>(acc, t.c.w, t.d.y, t.d.z, t.d.w, g);
+  return acc;
+}
+
+template <typename T, typename G>
+__device__ __forceinline__ T triples_dot(const Tri4D& t, const G& g, T acc) {
+  acc = triple_dot<T>(acc, t.c.x, t.v0.x, t.v0.y, t.v1.x, g);
+  acc = triple_dot<T>(acc, t.c.y, t.v1.y, t.v2.x, t.v2.y, g);
+  acc = triple_dot<T>(acc, t.c.z, t.v3.x, t.v3.y, t.v4.x, g);
+  acc = triple_dot<T>(acc, t.c.w, t.v4.y, t.v5.x, t.v5.y, g);
+  return acc;
+}
+
+template <typename T> struct TriplesOf;
+template <> struct TriplesOf<float> { using type = Tri4F; static constexpr int trip = 2; };
+template <> struct TriplesOf<double> { using type = Tri4D; static constexpr int trip = 1; };
+
+// Row of slot `lane` of a node-triple slice (w triples, a multiple of 4):
+// packs of four triples, loaded before their gathers (two packs per trip in
+// FP32, one in FP64).
+template <typename V, typename T, typename G>
+__device__ __forceinline__ T sell_row_acc_b3(const int32_t* __restrict__ col, const V* __restrict__ val,
+                                             int64_t sbase, int w, int lane, const G& g) {
+  using P = typename TriplesOf<V>::type;
+  constexpr int U = TriplesOf<V>::trip;
+  const int nq = w / kSellPack;
+  T acc = T(0);
+  int q = 0;
+  for (; q + U <= nq; q += U) {
+    P t[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+      t[u] = load_triples(col, val, sbase + static_cast<int64_t>(q + u) * (kSellC * kSellPack) + lane * kSellPack);
+#pragma unroll
+    for (int u = 0; u < U; ++u) acc = triples_dot<T>(t[u], g, acc);
+  }
+  for (; q < nq; ++q) {
+    const P t = load_triples(col, val, sbase + static_cast<int64_t>(q) * (kSellC * kSellPack) + lane * kSellPack);
+    acc = triples_dot<T>(t, g, acc);
+  }
+  return acc;
+}
+
 template <typename T>
 struct GatherX {
   const T* __restrict__ x;

@@ -64,6 +64,7 @@ class DirichletBC:
         ptr_, idx, val, f_new = K.dirichlet_apply(A.crow, A.col, A.values, self.is_boundary_dof, f, uh, matrix=True)
         out = CSRTensor(ptr_, idx, val, A.shape)
         out.dof_blocks = getattr(A, "dof_blocks", None)
+        out.node_block = getattr(A, "node_block", 1)
         return out, f_new
 
     def apply_matrix(self, matrix: CSRTensor, *, check=True) -> CSRTensor:
@@ -71,6 +72,7 @@ class DirichletBC:
         ptr_, idx, val, _ = K.dirichlet_apply(A.crow, A.col, A.values, self.is_boundary_dof, None, None, matrix=True)
         out = CSRTensor(ptr_, idx, val, A.shape)
         out.dof_blocks = getattr(A, "dof_blocks", None)
+        out.node_block = getattr(A, "node_block", 1)
         return out
 
     def apply_vector(self, vector, matrix, uh=None, gd=None, *, check=True):

@@ -167,6 +167,10 @@ class BilinearForm(_Form):
         _lib.check_status_word("assembly", status)
         M = CSRTensor(indptr, indices, values, (n, n))
         M.dof_blocks = space.dof_blocks()
+        # three interleaved components: the nonzeros come in runs of three
+        # consecutive columns (node triples)
+        if getattr(space, "dof_priority", True) is False and getattr(space, "dof_numel", 1) == 3:
+            M.node_block = 3
         if v32 is not None:
             M._f32 = v32
         self._M = M

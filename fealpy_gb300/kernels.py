@@ -234,16 +234,17 @@ class SellMatrix:
     and SpMV wrappers below permute vectors into and out of that numbering."""
 
     def __init__(self, n, n_slices, slice_ptr, perm, col, val64, val32, col16=None, col0=None, order=None,
-                 nnz=None):
+                 nnz=None, node_triples=False):
         self.n, self.n_slices = n, n_slices
         self.slice_ptr, self.perm, self.col, self.val64, self.val32 = slice_ptr, perm, col, val64, val32
         self.col16, self.col0, self.order, self.nnz = col16, col0, order, nnz
+        self.node_triples = bool(node_triples)
         self.desc = _lib.SellDesc(n, n_slices, slice_ptr.data_ptr(), perm.data_ptr(),
                                   col.data_ptr() if col is not None else None,
                                   val64.data_ptr() if val64 is not None else None,
                                   val32.data_ptr() if val32 is not None else None, 0, 0,
                                   col16.data_ptr() if col16 is not None else None,
-                                  col0.data_ptr() if col0 is not None else None)
+                                  col0.data_ptr() if col0 is not None else None, 1 if node_triples else 0, 0)
 
     @property
     def d16(self) -> bool:
@@ -255,6 +256,9 @@ class SellMatrix:
 
     @property
     def padded_nnz(self):
+        """Stored entries including padding (three per slot for node triples)."""
+        if self.node_triples:
+            return 3 * self.col.numel()
         return (self.col16 if self.col16 is not None else self.col).numel()
 
     def to_inner(self, v: torch.Tensor) -> torch.Tensor:
@@ -329,16 +333,20 @@ D16_MAX_GROWTH = 1.25
 
 
 def sell_build(indptr, indices, values64=None, values32=None, want64=True, want32=False,
-               d16: Optional[bool] = None, blocks: Optional[Sequence[int]] = None) -> SellMatrix:
+               d16: Optional[bool] = None, blocks: Optional[Sequence[int]] = None,
+               triples: bool = False) -> SellMatrix:
     """SELL-32 copy of a CSR matrix.  ``d16``: True = delta-coded columns of
     the renumbered matrix, False = 4-byte columns, None = delta-coded when
     the bridges add at most 25% entries (two host reads for the sizes).
     ``blocks``: the dof block sizes of the space (``dof_blocks()``) for the
     block-merge renumbering; without them the rows are ordered by their
-    smallest column."""
+    smallest column.  ``triples``: node-triple copy for a vector space with
+    three interleaved components (rows a multiple of 3; ``d16`` ignored)."""
     dev = _dev(indptr)
     n = indptr.numel() - 1
     lib = _lib.lib()
+    if triples:
+        return _sell_build_b3(indptr, indices, values64, values32, want64, want32)
     if d16 is None or d16:
         S = _sell_build_d16(indptr, indices, values64, values32, want64, want32, force=bool(d16), blocks=blocks)
         if S is not None:
@@ -406,6 +414,31 @@ def _sell_build_d16(indptr, indices, values64, values32, want64, want32, force=F
     call("fgb_sell_fill_d16", n, ptr(p_indptr), ptr(p_indices), ptr(p64), ptr(p32), ptr(perm), ptr(slice_ptr),
          ptr(col0), ptr(col16), ptr(v64), ptr(v32), s)
     return SellMatrix(n, n_slices, slice_ptr, perm, None, v64, v32, col16=col16, col0=col0, order=order, nnz=nnz)
+
+
+def _sell_build_b3(indptr, indices, values64, values32, want64, want32) -> SellMatrix:
+    """Node-triple copy: a 4-byte column per run of three consecutive columns."""
+    dev = _dev(indptr)
+    n = indptr.numel() - 1
+    if n % 3:
+        raise ValueError("a node-triple copy needs a multiple of 3 rows")
+    lib = _lib.lib()
+    s = stream_ptr(dev)
+    ws = workspace(max(lib.fgb_sell_d16_workspace_bytes(n), lib.fgb_sell_workspace_bytes(n)), dev)
+    t_indptr = torch.empty(n + 1, dtype=torch.int64, device=dev)
+    call("fgb_sell_b3_indptr", n, ptr(indptr), ptr(indices), ptr(t_indptr), ptr(ws), ws.numel(), s)
+    slots = int(lib.fgb_sell_slots(n))
+    n_slices = slots // 32
+    perm = torch.empty(slots, dtype=torch.int32, device=dev)
+    slice_ptr = torch.empty(n_slices + 1, dtype=torch.int64, device=dev)
+    call("fgb_sell_plan", n, ptr(t_indptr), ptr(perm), ptr(slice_ptr), ptr(ws), ws.numel(), s)
+    total = int(slice_ptr[n_slices].item())
+    col = torch.empty(max(total, 4), dtype=torch.int32, device=dev)
+    v64 = torch.empty(3 * max(total, 4), dtype=torch.float64, device=dev) if want64 else None
+    v32 = torch.empty(3 * max(total, 4), dtype=torch.float32, device=dev) if want32 else None
+    call("fgb_sell_fill_b3", n, ptr(indptr), ptr(indices), ptr(values64), ptr(values32), ptr(perm), ptr(slice_ptr),
+         ptr(col), ptr(v64), ptr(v32), s)
+    return SellMatrix(n, n_slices, slice_ptr, perm, col, v64, v32, nnz=indices.numel(), node_triples=True)
 
 
 def sell_spmv(S: SellMatrix, x, dtype=torch.float64):

@@ -67,7 +67,14 @@ SELL_D16: Optional[bool] = False
 # 263 K rows 50.4 / 37.3 ms; P2 tetrahedra 118 K rows 6.1 / 6.5 ms, 531 K rows
 # 16.0 / 16.4 ms.
 PERSISTENT_MAX_ROWS = 1 << 19
+# node-triple copies (one column per three values) for matrices of vector
+# spaces with three interleaved components
+SELL_TRIPLES = True
 PERSISTENT_MAX_ROW_NNZ = 10
+
+
+def _triples(A: CSRTensor) -> bool:
+    return SELL_TRIPLES and getattr(A, "node_block", 1) == 3 and A.shape[0] % 3 == 0
 
 
 def _sell_of(A: CSRTensor, want32: bool, tune: bool = True):
@@ -78,15 +85,15 @@ def _sell_of(A: CSRTensor, want32: bool, tune: bool = True):
         if A.values.dtype == torch.float32 and want32:
             # FP32-assembled operator: the FP32 values are the matrix (no FP64 copy)
             S = K.sell_build(A.crow, A.col, None, A.values.contiguous(), want64=False, want32=True, d16=SELL_D16,
-                             blocks=getattr(A, "dof_blocks", None))
+                             blocks=getattr(A, "dof_blocks", None), triples=_triples(A))
         else:
             v32 = A._f32 if (want32 and A._f32 is not None) else None
             S = K.sell_build(A.crow, A.col, A.values.to(torch.float64).contiguous(), v32, want64=True, want32=want32,
-                             d16=SELL_D16, blocks=getattr(A, "dof_blocks", None))
+                             d16=SELL_D16, blocks=getattr(A, "dof_blocks", None), triples=_triples(A))
         A._sell = S
         if tune:
             dt = torch.float32 if want32 else torch.float64
-            key = (S.n, S.padded_nnz, dt, S.d16)
+            key = (S.n, S.padded_nnz, dt, S.d16, S.node_triples)
             shape = _LAUNCH_CACHE.get(key)
             if shape is None:
                 times = K.sell_autotune(S, dt)

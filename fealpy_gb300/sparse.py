@@ -22,6 +22,9 @@ class CSRTensor:
         # sizes of the contiguous dof ranges of the space the matrix was
         # assembled on (vertex, edge, face, cell dofs), or None
         self.dof_blocks = None
+        # 3 when the nonzeros come in runs of three consecutive columns (a
+        # vector space with three interleaved components), else 1
+        self.node_block = 1
         if spshape is None:
             spshape = (crow.shape[0] - 1, int(col.max().item()) + 1 if col.numel() else 0)
         self._spshape = tuple(int(s) for s in spshape)

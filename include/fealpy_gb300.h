@@ -305,6 +305,10 @@ typedef struct fgb_sell {
   const uint16_t* col16;    /* delta-coded columns (col unused) or NULL:      */
   const int32_t* col0;      /* column of entry k = col0[slot] + sum of the    */
                             /* steps col16 up to k (fgb_sell_fill_d16)        */
+  int32_t node_triples;     /* 1: every slot is a node triple: col = 3c, and  */
+                            /* three values (columns 3c..3c+2) per slot       */
+                            /* (fgb_sell_fill_b3); 0: one entry per slot      */
+  int32_t reserved;
 } fgb_sell;
 
 /* No FEALPy counterpart: a solver-side layout of CSRTensor (the matrix the
@@ -355,6 +359,23 @@ int32_t fgb_sell_fill_d16(int64_t n, const int64_t* indptr, const int32_t* indic
                           float* val32, void* stream);
 int32_t fgb_permute(int32_t dtype, int64_t n, const int32_t* order, const void* src, void* dst,
                     int32_t scatter, void* stream);
+
+/* Node-triple SELL copy for vector spaces with three interleaved components
+ * (dof = 3 node + comp, FEALPy's TensorFunctionSpace(space, (-1, 3)),
+ * fealpy/functionspace/tensor_space.py): one 4-byte column per run of three
+ * consecutive columns 3c..3c+2 and its three values (zero where the matrix has
+ * no entry), 16 bytes per three FP32 entries instead of 24.  n must be a
+ * multiple of 3 and columns ascending in every row.
+ *   b3_indptr: row pointer of the triple counts (for fgb_sell_plan).
+ *   fill_b3: col (3c per slot) and three values per slot of the plan's slots
+ *     (val64/val32 hold 3 * slice_ptr[n_slices] values). */
+int32_t fgb_sell_b3_indptr(int64_t n, const int64_t* indptr, const int32_t* indices,
+                           int64_t* triple_indptr, void* workspace, size_t workspace_bytes,
+                           void* stream);
+int32_t fgb_sell_fill_b3(int64_t n, const int64_t* indptr, const int32_t* indices,
+                         const double* values64, const float* values32, const int32_t* perm,
+                         const int64_t* slice_ptr, int32_t* col, double* val64, float* val32,
+                         void* stream);
 
 /* Jacobi-PCG on a SELL copy: same iteration, stopping rules and info as
  * fgb_pcg_f64 / fgb_pcg_mixed.  use_graph != 0 runs the iterations as a CUDA

@@ -1,9 +1,12 @@
-"""Delta-coded SELL copy (fealpy_gb300.kernels.sell_build(d16=True)): the
+"""SELL storage formats.  Delta-coded copy (sell_build(d16=True)): the
 locality renumbering is a permutation and deterministic, the renumbered copy
 multiplies like the CSR matrix (FP64 within 1e-14 of scipy; FP32 within
 1e-5), steps above 65535 are bridged, rows above the shared-memory stage and
 key groups above 64 rows take their fallbacks, and the solvers on the
-renumbered copy give the solution in the caller's numbering."""
+renumbered copy give the solution in the caller's numbering.  Node-triple
+copy (sell_build(triples=True), vector spaces with three interleaved
+components): SpMV against scipy, and the solvers against the copy with a
+column per entry."""
 import os
 
 import numpy as np
@@ -177,3 +180,51 @@ def test_d16_block_merge_renumbering(golden_dir):
         S = _build(A, dev, True, blocks=bl)
         assert np.array_equal(S.order.cpu().numpy(), _merge_order(bl))
         _check_spmv(S, A, dev)
+
+
+def test_node_triple_copy_matches_csr(golden_dir):
+    """Node-triple copy of the P1 elasticity matrices (before and after the
+    Dirichlet rows, which leave partial triples): SpMV against scipy."""
+    dev = cuda()
+    import scipy.sparse as sp
+    from fealpy_gb300 import kernels as K
+    z = np.load(os.path.join(golden_dir, "small_elasticity_tet_p1.npz"))
+    for pre in ("", "bc_"):
+        n = len(z[pre + "crow"]) - 1
+        A = sp.csr_matrix((z[pre + "val"], z[pre + "col"], z[pre + "crow"]), shape=(n, n))
+        A.sort_indices()
+        t = lambda a: torch.as_tensor(a, device=dev)
+        S = K.sell_build(t(A.indptr.astype(np.int64)), t(A.indices.astype(np.int32)), t(A.data), None,
+                         want64=True, want32=True, triples=True)
+        assert S.node_triples and S.padded_nnz >= A.nnz and S.order is None
+        _check_spmv(S, A, dev)
+
+
+def test_node_triple_solvers_match_entry_copy(golden_dir):
+    """cg and cg_mixed on the elasticity system with node triples against the
+    copy with a column per entry: iteration counts within 1, solutions within
+    1e-9 (FP64) / 1e-7 (FP32-refined, relres 1e-10)."""
+    dev = cuda()
+    import fealpy_gb300 as F
+    from fealpy_gb300 import solver as SV
+    from fealpy_gb300.sparse import CSRTensor
+    z = np.load(os.path.join(golden_dir, "small_elasticity_tet_p1.npz"))
+    out = {}
+    old = SV.SELL_TRIPLES
+    try:
+        for mode in (False, True):
+            SV.SELL_TRIPLES = mode
+            A = CSRTensor(torch.as_tensor(z["bc_crow"], device=dev), torch.as_tensor(z["bc_col"], device=dev),
+                          torch.as_tensor(z["bc_val"], device=dev), (len(z["bc_crow"]) - 1,) * 2)
+            A.node_block = 3
+            b = torch.as_tensor(z["bc_F"], device=dev)
+            x64, i64 = F.cg(A, b, M=F.JacobiPreconditioner().apply(A), atol=1e-30, rtol=1e-10, returninfo=True)
+            assert A._sell.node_triples == mode
+            xm, im = F.cg_mixed(A, b, rtol=1e-10, returninfo=True)
+            assert im["relres"] <= 1e-10
+            out[mode] = (x64, i64["niter"], xm)
+    finally:
+        SV.SELL_TRIPLES = old
+    assert abs(out[True][1] - out[False][1]) <= 1
+    assert rel_err(out[True][0], out[False][0].cpu().numpy()) < 1e-9
+    assert rel_err(out[True][2], out[False][2].cpu().numpy()) < 1e-7
