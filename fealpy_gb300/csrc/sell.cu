@@ -1182,7 +1182,7 @@ bool launch_persistent(const PersistArgs& P, cudaStream_t s) {
 
 // Returns FGB_OK after the graph ran to completion.  *launched tells the caller
 // whether anything was submitted: when graph construction fails before the
-// launch (a feature missing in the driver), the caller falls back to the
+// launch (a feature missing in the CUDA driver), the caller falls back to the
 // host-polled loop, which runs the same kernels.
 template <typename Body>
 int graph_loop(Body body_two_iters, SellPcgState* st, cudaStream_t s, bool* launched) {
