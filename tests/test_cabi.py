@@ -71,3 +71,22 @@ def test_argument_validation_without_gpu():
 
 def test_build_targets_sm103a():
     assert "arch=compute_103a,code=sm_103a" in " ".join(_build.ARCH_FLAGS)
+
+
+def test_header_compiles_as_c99_and_cxx(tmp_path):
+    """include/fealpy_gb300.h is a plain C header (the boundary a cgo/ctypes/
+    JNI binding includes): it compiles as C99 and as C++17 on its own."""
+    import shutil
+    import subprocess
+    src = tmp_path / "use.c"
+    src.write_text('#include "fealpy_gb300.h"\n'
+                   'int probe(void) { fgb_sell s; fgb_pcg_info i; (void)s; (void)i;\n'
+                   '  return (int)sizeof(fgb_batch_state) + (int)FGB_PCG_STAGNATED; }\n')
+    inc = os.path.join(ROOT, "include")
+    for cc, std in (("gcc", "-std=c99"), ("g++", "-std=c++17")):
+        if shutil.which(cc) is None:
+            pytest.skip(f"{cc} not found")
+        lang = ["-x", "c++"] if cc == "g++" else []
+        res = subprocess.run([cc, std, "-Wall", "-Werror", "-fsyntax-only", "-I", inc] + lang + [str(src)],
+                             capture_output=True, text=True)
+        assert res.returncode == 0, res.stderr
