@@ -632,10 +632,10 @@ def run_elasticity(args):
         lf.add_integrator(VectorSourceIntegrator(source=[0.0, 0.0, -1.0], q=4))
         A2, F2 = bc.apply(A, lf.assembly())
         if mode == "mixed":
-            x, info = F.cg_mixed(A2, F2, rtol=rtol, maxit=200000, returninfo=True)
+            x, info = F.cg_mixed(A2, F2, rtol=rtol, maxit=200000, returninfo=True, graph=not args.no_graph)
         else:
             x, info = F.cg(A2, F2, M=F.JacobiPreconditioner().apply(A2), atol=0.0, rtol=rtol, maxit=200000,
-                           returninfo=True, stop="residual")
+                           returninfo=True, stop="residual", graph=not args.no_graph)
         return x, info, A2, F2
 
     res = {}
