@@ -476,9 +476,17 @@ def batched_setup(torch, F, meshes, dev):
     return probs
 
 
+# precision "auto" of the batched workload: P3 systems above this many dofs
+# iterate in FP64 from the start (their condition numbers are beyond what FP32
+# iterations resolve: with "mixed" exactly these systems stagnate in FP32 and
+# are continued in FP64), all others FP32-refined
+AUTO_FP64_P3_DOFS = 100_000
+
+
 def batched_step(torch, F, probs, dtype, bs_kw, marks=None, fp64=False, graph=True):
     """Assemble every problem (diffusion with the checkerboard coefficient,
-    quadrature p + 3, f = 1, u = 0) and solve all of them in one batch."""
+    quadrature p + 3, f = 1, u = 0) and solve all of them in one batch.
+    ``fp64``: False, True or "auto" (see AUTO_FP64_P3_DOFS)."""
     from fealpy_gb300.fem import BilinearForm, LinearForm, ScalarDiffusionIntegrator, ScalarSourceIntegrator
     from fealpy_gb300.batch import BatchSolver
     bs = BatchSolver(len(probs), **bs_kw)
@@ -491,7 +499,8 @@ def batched_step(torch, F, probs, dtype, bs_kw, marks=None, fp64=False, graph=Tr
         lf = LinearForm(space)
         lf.add_integrator(ScalarSourceIntegrator(1.0, q=p + 3))
         A2, F2 = bc.apply(A, lf.assembly())
-        bs.add(A2, F2, rtol=RTOL, maxit=BATCH_MAXIT, key=k, fp64=fp64)
+        sys64 = (p == 3 and A2.shape[0] > AUTO_FP64_P3_DOFS) if fp64 == "auto" else bool(fp64)
+        bs.add(A2, F2, rtol=RTOL, maxit=BATCH_MAXIT, key=k, fp64=sys64)
         systems.append((A2, F2))
     if marks is not None:
         e = torch.cuda.Event(enable_timing=True)
@@ -554,7 +563,8 @@ def run_batched(args):
     e0.record()
     torch.cuda.nvtx.range_push("timed_batched")
     for _ in range(args.steps):
-        res, systems, bs = batched_step(torch, F, probs, asm_dtype, kw, marks, fp64=args.batch_precision == "fp64",
+        prec = {"mixed": False, "fp64": True, "auto": "auto"}[args.batch_precision]
+        res, systems, bs = batched_step(torch, F, probs, asm_dtype, kw, marks, fp64=prec,
                                         graph=not args.no_graph)
     e1.record()
     torch.cuda.nvtx.range_pop()
@@ -777,8 +787,8 @@ def main():
     ap.add_argument("--no-triples", action="store_true",
                     help="elasticity: SELL copy with a column per entry instead of one per node triple")
     ap.add_argument("--batch-count", type=int, default=256)
-    ap.add_argument("--batch-precision", choices=["mixed", "fp64"], default="mixed",
-                    help="iterations of the batched solve: FP32 with FP64 refinement (default) or plain FP64")
+    ap.add_argument("--batch-precision", choices=["mixed", "fp64", "auto"], default="mixed",
+                    help="iterations of the batched solve: FP32 with FP64 refinement (default), plain FP64, or auto (FP64 for P3 systems above 1e5 dofs)")
     ap.add_argument("--serve-count", type=int, default=200, help="requests per arrival rate")
     ap.add_argument("--serve-rates", default="50,200,1000")
     ap.add_argument("--serve-chunk", type=int, default=64)
