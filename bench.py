@@ -193,6 +193,44 @@ def solve_step(torch, F, space, kappa, bc, mode, profile=False, marks=None, asm_
     return x, info, A2, F2
 
 
+def spmv_roofline(mixed, gdof, n, peak, peak_kind):
+    """`roofline` of the C2 record for the dominant kernel, the FP32 PCG SpMV
+    (Ap = A p and p.Ap), from the profiling solve's mean launch time, plus the
+    whole FP32 iteration over the timed solve."""
+    nnz = mixed["nnz"]
+    # SpMV algorithmic bytes B_spmv = nnz (s + 4) + n (8 + 2 s) with s = 4:
+    # value + column per nonzero, a row pointer, x read once and y written once
+    # (the formula of the measurement definition, used verbatim; the SELL copy
+    # reads a 4-byte slot->row map and an 8-byte slice pointer per 32 rows in
+    # place of the row pointer).  With 2-byte column steps: nnz (s + 2) + n (12 + 2 s).
+    d16 = mixed["sell_cols"] == "d16"
+    bytes_per_launch = nnz * (4 + 2) + gdof * (12 + 8) if d16 else nnz * (4 + 4) + gdof * (8 + 8)
+    achieved = bytes_per_launch / (mixed["kernel_ms_avg"] / 1e3) / 1e9 if mixed["kernel_ms_avg"] > 0 else 0.0
+    # whole FP32 iteration: B_it = B_spmv + 11 n s (the vector traffic of the
+    # update kernels), over the live time per iteration of the timed solve (the
+    # step minus its non-PCG stages as measured in the profiling solve)
+    pre_ms = sum(v for k, v in mixed["stages_ms"].items() if k in STAGES and k != "pcg")
+    it_ms = max(mixed["ms_per_step"] - pre_ms, 1e-9) / max(mixed["niter"], 1)
+    bytes_per_iter = bytes_per_launch + 11 * gdof * 4
+    it_achieved = bytes_per_iter / (it_ms / 1e3) / 1e9
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tp) and n == 64:
+        try:
+            traffic = json.load(open(tp)).get("pcg_spmv_f32_d16_bytes_per_launch_at_n64" if d16 else
+                                              "pcg_spmv_f32_bytes_per_launch_at_n64")
+        except Exception:
+            traffic = None
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak if peak else None, "traffic": traffic,
+            "kernel": "sell_pcg_spmv<float> (SELL-32" + (", 16-bit column steps" if d16 else "") +
+                      "; Ap = A p and p.Ap)",
+            "algorithmic_bytes_per_launch": bytes_per_launch, "avg_launch_ms": mixed["kernel_ms_avg"],
+            "peak_source": peak_kind,
+            "iteration": {"bytes_per_iteration": bytes_per_iter, "us_per_iteration": it_ms * 1e3,
+                          "achieved": it_achieved, "unit": "GB/s", "frac": it_achieved / peak if peak else None}}
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -329,32 +367,7 @@ def run_ours(args):
     mixed = results["mixed"]
     fp64 = results["fp64"]
     value = replica_value(gdof, world, mixed["ms_per_step"])
-    # dominant kernel: the fused FP32 PCG SpMV (p = z + beta p_old, Ap = A p, p.Ap)
-    nnz = mixed["nnz"]
-    # SpMV algorithmic bytes B_spmv = nnz (s + 4) + n (8 + 2 s) with s = 4:
-    # value + column per nonzero, a row pointer, x read once and y written once
-    # (the formula of the measurement definition, used verbatim; the SELL copy
-    # reads a 4-byte slot->row map and an 8-byte slice pointer per 32 rows in
-    # place of the row pointer).  With 2-byte column steps: nnz (s + 2) + n (12 + 2 s).
-    d16 = mixed["sell_cols"] == "d16"
-    bytes_per_launch = nnz * (4 + 2) + gdof * (12 + 8) if d16 else nnz * (4 + 4) + gdof * (8 + 8)
-    achieved = bytes_per_launch / (mixed["kernel_ms_avg"] / 1e3) / 1e9 if mixed["kernel_ms_avg"] > 0 else 0.0
-    # whole FP32 iteration: B_it = B_spmv + 11 n s (the vector traffic of the
-    # update kernels), over the live time per iteration of the timed solve (the
-    # step minus its non-PCG stages as measured in the profiling solve)
-    pre_ms = sum(v for k, v in mixed["stages_ms"].items() if k in STAGES and k != "pcg")
-    it_ms = max(mixed["ms_per_step"] - pre_ms, 1e-9) / max(mixed["niter"], 1)
-    bytes_per_iter = bytes_per_launch + 11 * gdof * 4
-    iter_roof = {"bytes_per_iteration": bytes_per_iter, "us_per_iteration": it_ms * 1e3,
-                 "achieved": bytes_per_iter / (it_ms / 1e3) / 1e9, "unit": "GB/s"}
-    traffic = None
-    tp = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tp) and n == 64:
-        try:
-            traffic = json.load(open(tp)).get("pcg_spmv_f32_d16_bytes_per_launch_at_n64" if d16 else
-                                              "pcg_spmv_f32_bytes_per_launch_at_n64")
-        except Exception:
-            traffic = None
+    roofline = spmv_roofline(mixed, gdof, n, peak, peak_kind)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -372,7 +385,7 @@ def run_ours(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
             "data": "synthetic (seeded jittered tet box, lognormal coefficients)",
             "config": {"workload": f"P2 diffusion+mass TetrahedronMesh box {n}^3 (C2)", "cells": int(cell_np.shape[0]),
-                       "gdof": gdof, "nnz": nnz, "quadrature": Q, "rtol": RTOL,
+                       "gdof": gdof, "nnz": mixed["nnz"], "quadrature": Q, "rtol": RTOL,
                        "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{world}"},
             "fp32_refined": {"ms_per_step": mixed["ms_per_step"], "dof_per_s": value, "cg_iters": mixed["niter"],
                              "reliable_updates": mixed["n_updates"], "true_relres": mixed["relres"],
@@ -389,13 +402,7 @@ def run_ours(args):
             "e2e": {"value": world * gdof * e2e_steps / (e2e_ms / 1e3), "unit": "DOF/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "steps": e2e_steps},
             "gpu_launches": mixed["launches"],
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak if peak else None, "traffic": traffic,
-                         "kernel": "sell_pcg_spmv<float> (SELL-32" + (", 16-bit column steps" if d16 else "") +
-                                   "; Ap = A p and p.Ap)",
-                         "algorithmic_bytes_per_launch": bytes_per_launch,
-                         "avg_launch_ms": mixed["kernel_ms_avg"], "peak_source": peak_kind,
-                         "iteration": dict(iter_roof, frac=iter_roof["achieved"] / peak if peak else None)},
+            "roofline": roofline,
             "clocks": mixed["clocks"],
             "cpu_baseline": cpu,
             "serving": serving,

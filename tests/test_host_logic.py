@@ -134,3 +134,22 @@ def test_dof_blocks_partition_the_numbering(kind, p):
     inter = TensorFunctionSpace(space, (-1, gd)).dof_blocks()
     major = TensorFunctionSpace(space, (gd, -1)).dof_blocks()
     assert inter == [gd * b for b in blocks] and major == blocks * gd
+
+
+def test_bench_roofline_record():
+    """The roofline block of the C2 record (dominant-kernel SpMV and whole
+    iteration) from a profiling-solve summary: formulas and keys."""
+    import importlib
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    bench = importlib.import_module("bench")
+    mixed = {"nnz": 57_611_761, "sell_cols": "i32", "kernel_ms_avg": 0.0841, "ms_per_step": 131.6, "niter": 1127,
+             "stages_ms": {"assembly (pattern + values)": 5.4, "rhs": 1.5, "dirichlet": 1.5,
+                           "solver copy (SELL)": 0.4, "pcg": 143.6, "assembly/pattern": 2.3}}
+    r = bench.spmv_roofline(mixed, 2_146_689, 64, 6685.8, "measured")
+    assert r["algorithmic_bytes_per_launch"] == 57_611_761 * 8 + 2_146_689 * 16
+    assert abs(r["frac"] - r["achieved"] / 6685.8) < 1e-12 and 0.8 < r["frac"] < 0.95
+    it = r["iteration"]
+    assert it["bytes_per_iteration"] == r["algorithmic_bytes_per_launch"] + 11 * 2_146_689 * 4
+    assert abs(it["us_per_iteration"] - (131.6 - 8.8) / 1127 * 1e3) < 1e-6
+    assert r["traffic"] is not None and r["bound"] == "hbm" and r["unit"] == "GB/s"
