@@ -67,6 +67,11 @@ def test_argument_validation_without_gpu():
     assert lib.fgb_sell_fill_d16(5, one, one, None, None, one, one, one, None, None, None, None) == 1
     assert lib.fgb_permute(1, 5, one, one, one, 0, None) == 1                             # src == dst
     assert lib.fgb_permute(7, 5, one, one, ctypes.c_void_p(32), 0, None) == 1             # bad dtype
+    # node-triple copy: rows must come in whole triples
+    assert lib.fgb_sell_b3_indptr(10, one, one, one, one, 1 << 20, None) == 1
+    assert lib.fgb_sell_b3_indptr(9, one, one, one, None, 0, None) == 2
+    assert lib.fgb_sell_fill_b3(10, one, one, one, None, one, one, one, None, None, None) == 1
+    assert lib.fgb_sell_fill_b3(9, one, one, None, None, one, one, one, one, None, None) == 1  # values, no source
 
 
 def test_build_targets_sm103a():
