@@ -442,6 +442,20 @@ def host_replica_rounds(n, rounds, warmup=1):
     PCG iterations)."""
     import multiprocessing
     procs = max(1, min(os.cpu_count() or 1, REF_MAX_PROCS))
+    try:
+        return _replica_rounds(n, rounds, warmup, procs, multiprocessing)
+    except Exception as e:  # no process pool here: one replica in this process
+        print(f"[cpu baseline] process pool unavailable ({e}); one replica in-process", file=sys.stderr)
+        for _ in range(max(warmup, 1)):
+            oracle_step(n)
+        times, gdof, niter = [], 0, 0
+        for _ in range(rounds):
+            gdof, dt, niter = oracle_step(n)
+            times.append(dt)
+        return 1, gdof, times, niter
+
+
+def _replica_rounds(n, rounds, warmup, procs, multiprocessing):
     saved = {k: os.environ.get(k) for k in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS")}
     for k in saved:
         os.environ[k] = "1"  # inherited by the spawned replicas
