@@ -370,7 +370,7 @@ def run_ours(args):
     roofline = spmv_roofline(mixed, gdof, n, peak, peak_kind)
 
     cpu = None
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(CPU_SAMPLE_N, rounds=2)
 
     # a short sample of the serving stream (the full sweep: --workload serving)
