@@ -153,3 +153,30 @@ def test_bench_roofline_record():
     assert it["bytes_per_iteration"] == r["algorithmic_bytes_per_launch"] + 11 * 2_146_689 * 4
     assert abs(it["us_per_iteration"] - (131.6 - 8.8) / 1127 * 1e3) < 1e-6
     assert r["traffic"] is not None and r["bound"] == "hbm" and r["unit"] == "GB/s"
+
+
+def test_no_cpu_fallback():
+    """The product path computes only on the GPU: with CPU tensors every
+    compute entry (assembly, Dirichlet, SpMV, both solvers) raises instead of
+    computing on the host."""
+    import fealpy_gb300 as F
+    from fealpy_gb300.fem import BilinearForm, ScalarDiffusionIntegrator, DirichletBC
+    from fealpy_gb300.sparse import CSRTensor
+    mesh = TriangleMesh.from_box([0, 1, 0, 1], 4, 4)
+    space = LagrangeFESpace(mesh, p=1)
+    bf = BilinearForm(space)
+    bf.add_integrator(ScalarDiffusionIntegrator(coef=1.0, q=3))
+    with pytest.raises((ValueError, RuntimeError)):
+        bf.assembly()
+    n = space.number_of_global_dofs()
+    A = CSRTensor(torch.arange(n + 1, dtype=torch.int64), torch.arange(n, dtype=torch.int32),
+                  torch.ones(n, dtype=torch.float64), (n, n))
+    b = torch.ones(n, dtype=torch.float64)
+    with pytest.raises((ValueError, RuntimeError)):
+        A @ b
+    with pytest.raises((ValueError, RuntimeError)):
+        F.cg(A, b)
+    with pytest.raises((ValueError, RuntimeError)):
+        F.cg_mixed(A, b)
+    with pytest.raises((ValueError, RuntimeError)):
+        DirichletBC(space, gd=0.0).apply(A, b)
