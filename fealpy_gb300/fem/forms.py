@@ -10,11 +10,10 @@ from typing import Optional, Sequence
 
 import torch
 
-from ..functionspace import TensorFunctionSpace
 from ..sparse import CSRTensor
 from .. import _lib
 from .. import kernels as K
-from .integrators import (ElasticityPlan, GroupIntegrator, Integrator, ScalarPlan, VectorSourceIntegrator)
+from .integrators import (ElasticityPlan, GroupIntegrator, Integrator, ScalarPlan)
 
 __all__ = ["BilinearForm", "LinearForm", "symbolic_structure"]
 

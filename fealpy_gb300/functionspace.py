@@ -1,12 +1,10 @@
 """Lagrange and tensor function spaces (``fealpy/functionspace/lagrange_fe_space.py``,
 ``fealpy/functionspace/tensor_space.py``) on the meshes of :mod:`fealpy_gb300.mesh`."""
 from math import prod
-from typing import Callable, Optional, Tuple, Union
+from typing import Callable, Optional, Tuple
 
-import numpy as np
 import torch
 
-from . import simplex as sx
 
 __all__ = ["LagrangeFESpace", "TensorFunctionSpace"]
 

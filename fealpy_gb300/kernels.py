@@ -5,9 +5,8 @@ workspaces through torch's caching allocator, launches on the current stream
 and maps a non-zero status to an exception.  Nothing here computes on the CPU.
 """
 import ctypes
-from typing import List, Optional, Sequence, Tuple
+from typing import Optional, Sequence, Tuple
 
-import numpy as np
 import torch
 
 from . import _lib

@@ -13,7 +13,6 @@ edge ordered from ``edge[:,0]`` to ``edge[:,1]``, then face and cell interior
 points.  Mesh set-up (generation, topology, numbering) is not part of the
 timed assemble/solve path.
 """
-from typing import Optional
 
 import numpy as np
 import torch
