@@ -103,6 +103,8 @@ _SIGNATURES = {
                                  c_vp, c_sz, ctypes.POINTER(PcgInfo), c_vp]),
     "fgb_pcg_sell_mixed": (c_i32, [ctypes.c_void_p, c_vp, c_vp, c_vp, c_dbl, c_dbl, c_i64, c_i32, c_i32, c_i32,
                                    c_vp, c_sz, ctypes.POINTER(PcgInfo), c_vp]),
+    "fgb_pcg_sell_mixed_ex": (c_i32, [ctypes.c_void_p, c_vp, c_vp, c_vp, c_dbl, c_dbl, c_i64, c_i32, c_i32, c_i32,
+                                      c_i64, c_vp, c_sz, ctypes.POINTER(PcgInfo), c_vp]),
     "fgb_batch_bytes": (c_sz, [c_i32, c_i32, c_i32]),
     "fgb_batch_create": (c_i32, [c_i32, c_i32, c_i32, c_i32, c_vp, c_sz, ctypes.POINTER(c_vp)]),
     "fgb_batch_destroy": (c_i32, [c_vp]),

@@ -21,7 +21,6 @@
 
 #include <cmath>
 #include <cstring>
-#include <mutex>
 
 namespace fgb {
 
@@ -511,7 +510,7 @@ int run_pcg_f64(int64_t n, const int64_t* indptr, const int32_t* indices, const 
   h.atol = atol;
   h.maxit = maxit;
   h.norm_rr = norm_rr;
-  cudaMemcpyAsync(pb.st, &h, sizeof(PcgState), cudaMemcpyHostToDevice, s);
+  if (cudaMemcpyAsync(pb.st, &h, sizeof(PcgState), cudaMemcpyHostToDevice, s) != cudaSuccess) return FGB_ERR_CUDA;
   pcg_init_kernel<double, G><<<grid_rows_for(n, G), kPcgThreads, 0, s>>>(n, indptr, indices, values, dinv, b, x, v.r,
                                                                           v.z, v.p0, pb.partials, pb.st);
   ++launches;
@@ -522,8 +521,9 @@ int run_pcg_f64(int64_t n, const int64_t* indptr, const int32_t* indices, const 
     cudaMemsetAsync(x, 0, n * sizeof(double), s);
   } else {
     const double tol = rtol * h.b_norm;
-    cudaMemcpyAsync(reinterpret_cast<char*>(pb.st) + offsetof(PcgState, tol), &tol, sizeof(double),
-                    cudaMemcpyHostToDevice, s);
+    if (cudaMemcpyAsync(reinterpret_cast<char*>(pb.st) + offsetof(PcgState, tol), &tol, sizeof(double),
+                        cudaMemcpyHostToDevice, s) != cudaSuccess)
+      return FGB_ERR_CUDA;
     int64_t it = 0;
     while (true) {
       const int64_t before = h.niter;
@@ -578,7 +578,7 @@ int run_pcg_mixed(int64_t n, const int64_t* indptr, const int32_t* indices, cons
   h.atol = 0.0;
   h.tol = 0.0;
   h.norm_rr = 1;
-  cudaMemcpyAsync(st, &h, sizeof(PcgState), cudaMemcpyHostToDevice, s);
+  if (cudaMemcpyAsync(st, &h, sizeof(PcgState), cudaMemcpyHostToDevice, s) != cudaSuccess) return FGB_ERR_CUDA;
   cudaMemsetAsync(y, 0, n * sizeof(float), s);
   // ||b|| (for tol = rtol ||b||) from the FP64 init kernel, run on the r64 buffer
   // only (r, z and p all alias r64 there, which the kernel tolerates: it writes
@@ -592,8 +592,9 @@ int run_pcg_mixed(int64_t n, const int64_t* indptr, const int32_t* indices, cons
     cudaMemsetAsync(x, 0, n * sizeof(double), s);
   } else {
     const double tol = rtol * h.b_norm;
-    cudaMemcpyAsync(reinterpret_cast<char*>(st) + offsetof(PcgState, tol), &tol, sizeof(double),
-                    cudaMemcpyHostToDevice, s);
+    if (cudaMemcpyAsync(reinterpret_cast<char*>(st) + offsetof(PcgState, tol), &tol, sizeof(double),
+                        cudaMemcpyHostToDevice, s) != cudaSuccess)
+      return FGB_ERR_CUDA;
     // initial residual in FP64, converted to FP32; p = z
     mixed_residual_kernel<G><<<grid_rows, kPcgThreads, 0, s>>>(n, indptr, indices, values64, b, x, y, r64, partials, st, 1);
     mixed_replace_kernel<<<grid_vec, kPcgThreads, 0, s>>>(n, dinv64, r64, r, z, p0, dinv32, partials, st, 0.0, 1);
@@ -738,23 +739,17 @@ constexpr size_t kNoAllocScratchBytes = cx_align(sizeof(PcgState)) + cx_align(2 
 
 __device__ __align__(256) unsigned char g_pcg_noalloc_scratch[kNoAllocScratchBytes];
 
-constexpr int kNoAllocMaxDevices = 64;
-std::mutex g_noalloc_mutex;
-void* g_noalloc_ptr[kNoAllocMaxDevices] = {};
-
-// Device address of the static scratch on the current device, looked up once
-// per device (the lookup may load this library's device code on that device).
+// Device address of the static scratch in the context current on the calling
+// thread.  It is looked up on every call, never cached: the address belongs
+// to the CUDA context that holds this library's module, and a context can be
+// replaced while the process runs (cudaDeviceReset, another context made
+// current on the same device), after which a cached address would point at
+// freed memory.  The first lookup in a context may load this library's device
+// code into it; later ones are a table lookup.
 int noalloc_scratch(void** out) {
-  int dev = -1;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return FGB_ERR_CUDA;
-  if (dev >= kNoAllocMaxDevices) return FGB_ERR_CAPACITY;
-  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (!g_noalloc_ptr[dev]) {
-    void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_pcg_noalloc_scratch) != cudaSuccess || !p) return FGB_ERR_CUDA;
-    g_noalloc_ptr[dev] = p;
-  }
-  *out = g_noalloc_ptr[dev];
+  void* p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_pcg_noalloc_scratch) != cudaSuccess || !p) return FGB_ERR_CUDA;
+  *out = p;
   return FGB_OK;
 }
 

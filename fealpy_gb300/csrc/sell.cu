@@ -715,13 +715,14 @@ struct PersistArgs {
   double* vpart;  // 2 * kSellMaxBlocks partials (two values per block)
   SellPcgState* st;
   double delta;
+  long long bar_limit;  // polls before a grid barrier gives up (kBarrierSpins by default)
 };
 
 // Grid barrier of a cooperative launch (every block resident): arrivals by an
 // atomic counter, release by a generation counter.  A wait longer than
-// kBarrierSpins polls, or any wait once another block has failed, sets the
-// error flag and returns false; the caller then returns, so every block ends.
-__device__ bool grid_barrier(SellPcgState* st) {
+// `limit` polls, or any wait once another block has failed, sets the error
+// flag and returns false; the caller then returns, so every block ends.
+__device__ bool grid_barrier(SellPcgState* st, long long limit) {
   __shared__ int ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -737,7 +738,7 @@ __device__ bool grid_barrier(SellPcgState* st) {
     } else {
       long long spins = 0;
       while (*gen == g) {
-        if (*err || ++spins > kBarrierSpins) {
+        if (*err || ++spins > limit) {
           good = 0;
           atomicExch(&st->bar_err, 1);
           break;
@@ -842,7 +843,7 @@ __global__ void __launch_bounds__(kPersistThreads, 2) sell_mixed_persistent(Pers
       }
       for (int64_t i = 4 * n4 + tid; i < n; i += stride) P.p[i] = __ldcg(P.z + i) + beta * __ldcg(P.p + i);
     }
-    if (!grid_barrier(P.st)) return;
+    if (!grid_barrier(P.st, P.bar_limit)) return;
     // Ap = A p and p.Ap
     {
       float pap = 0.0f;
@@ -857,7 +858,7 @@ __global__ void __launch_bounds__(kPersistThreads, 2) sell_mixed_persistent(Pers
       }
       block_partials2(pap, 0.0f, P.bpart, nullptr);
     }
-    if (!grid_barrier(P.st)) return;
+    if (!grid_barrier(P.st, P.bar_limit)) return;
     // alpha; y += alpha p, r -= alpha Ap, z = Dinv r; r.z, r.r
     {
       const double pap = grid_totals2(P.bpart, nullptr, gridDim.x).x;
@@ -897,7 +898,7 @@ __global__ void __launch_bounds__(kPersistThreads, 2) sell_mixed_persistent(Pers
       if (threadIdx.x == 0) S.alpha = alpha;
       block_partials2(rz, rr, P.vpart, P.vpart + kSellMaxBlocks);
     }
-    if (!grid_barrier(P.st)) return;
+    if (!grid_barrier(P.st, P.bar_limit)) return;
     {
       const double2 t = grid_totals2(P.vpart, P.vpart + kSellMaxBlocks, gridDim.x);
       if (threadIdx.x == 0) {
@@ -912,7 +913,7 @@ __global__ void __launch_bounds__(kPersistThreads, 2) sell_mixed_persistent(Pers
       P.x[i] += static_cast<double>(__ldcg(P.y + i));
       P.y[i] = 0.0f;
     }
-    if (!grid_barrier(P.st)) return;
+    if (!grid_barrier(P.st, P.bar_limit)) return;
     {
       double rr64 = 0.0, rz = 0.0;
       const GatherCG<double> gx{P.x};
@@ -932,7 +933,7 @@ __global__ void __launch_bounds__(kPersistThreads, 2) sell_mixed_persistent(Pers
       }
       block_partials2(rr64, rz, P.vpart, P.vpart + kSellMaxBlocks);
     }
-    if (!grid_barrier(P.st)) return;
+    if (!grid_barrier(P.st, P.bar_limit)) return;
     {
       const double2 t = grid_totals2(P.vpart, P.vpart + kSellMaxBlocks, gridDim.x);
       if (threadIdx.x == 0) mixed_reliable_scalars(S, t.x, t.y, 0);
@@ -1396,6 +1397,14 @@ int32_t fgb_pcg_sell_f64(const fgb_sell* A, const double* diag_inv, const double
 int32_t fgb_pcg_sell_mixed(const fgb_sell* A, const double* diag_inv64, const double* b, double* x, double rtol,
                            double delta, int64_t maxit, int32_t check_every, int32_t use_graph, int32_t profile,
                            void* workspace, size_t workspace_bytes, fgb_pcg_info* info, void* stream) {
+  return fgb_pcg_sell_mixed_ex(A, diag_inv64, b, x, rtol, delta, maxit, check_every, use_graph, profile, 0,
+                               workspace, workspace_bytes, info, stream);
+}
+
+int32_t fgb_pcg_sell_mixed_ex(const fgb_sell* A, const double* diag_inv64, const double* b, double* x, double rtol,
+                              double delta, int64_t maxit, int32_t check_every, int32_t use_graph, int32_t profile,
+                              int64_t barrier_polls, void* workspace, size_t workspace_bytes, fgb_pcg_info* info,
+                              void* stream) {
   if (!A || A->n <= 0 || !A->val32 || !diag_inv64 || !b || !x || maxit <= 0 || !launch_ok(A)) return FGB_ERR_ARG;
   if (!(delta > 0.0 && delta < 1.0)) return FGB_ERR_ARG;
   if (!workspace || workspace_bytes < fgb_pcg_sell_workspace_bytes(A->n)) return FGB_ERR_WORKSPACE;
@@ -1440,7 +1449,8 @@ int32_t fgb_pcg_sell_mixed(const fgb_sell* A, const double* diag_inv64, const do
       // every iteration inside one persistent cooperative kernel
       const PersistArgs pa{v, A->val32, A->val64 ? static_cast<const void*>(A->val64)
                                                  : static_cast<const void*>(A->val32),
-                           b, x, w.dinv32, w.r, w.z, w.p0, w.Ap, w.y, w.bpart, w.partials, w.st, delta};
+                           b, x, w.dinv32, w.r, w.z, w.p0, w.Ap, w.y, w.bpart, w.partials, w.st, delta,
+                           barrier_polls > 0 ? static_cast<long long>(barrier_polls) : kBarrierSpins};
       bool launched = false;
       with_cols(v, [&](auto d16) {
         constexpr int D = decltype(d16)::value;
@@ -1448,7 +1458,9 @@ int32_t fgb_pcg_sell_mixed(const fgb_sell* A, const double* diag_inv64, const do
       });
       if (launched) {
         if ((rc = read_state(w.st, &h, s))) return rc;
-        if (h.bar_err) return FGB_ERR_CUDA;  // a grid barrier gave up (cannot happen with all blocks resident)
+        // a grid barrier gave up: every block has returned; with the default
+        // limit this cannot happen while all blocks are resident
+        if (h.bar_err) return FGB_ERR_CUDA;
         graphed = true;
         used_graph = 2;
         ++launches;

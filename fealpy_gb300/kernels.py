@@ -466,17 +466,20 @@ def pcg_sell_f64(S: SellMatrix, dinv, b, x, atol, rtol, maxit, check_every=16, n
 
 
 def pcg_sell_mixed(S: SellMatrix, dinv64, b, x, rtol, delta=0.1, maxit=100000, check_every=32, graph=True,
-                   profile=False):
+                   profile=False, barrier_polls=0):
     """FP32 Jacobi-PCG with FP64 reliable updates on the SELL copy; dinv64, b
-    and x (updated in place) in the matrix's own numbering."""
+    and x (updated in place) in the matrix's own numbering.  ``graph``: 0
+    host-polled loop, 1 CUDA-graph loop, 2 one persistent cooperative kernel,
+    whose grid barriers wait at most ``barrier_polls`` polls (0: the default
+    limit) before every block returns and the call raises."""
     dev = S.device
     lib = _lib.lib()
     ws = workspace(lib.fgb_pcg_sell_workspace_bytes(S.n), dev)
     info = _lib.PcgInfo()
     di, bi, xi = S.to_inner(dinv64), S.to_inner(b), S.to_inner(x)
-    call("fgb_pcg_sell_mixed", ctypes.byref(S.desc), ptr(di), ptr(bi), ptr(xi), float(rtol), float(delta),
-         int(maxit), int(check_every), int(graph), int(bool(profile)), ptr(ws), ws.numel(), ctypes.byref(info),
-         stream_ptr(dev))
+    call("fgb_pcg_sell_mixed_ex", ctypes.byref(S.desc), ptr(di), ptr(bi), ptr(xi), float(rtol), float(delta),
+         int(maxit), int(check_every), int(graph), int(bool(profile)), int(barrier_polls), ptr(ws), ws.numel(),
+         ctypes.byref(info), stream_ptr(dev))
     S.to_outer(xi, out=x)
     _lib.add_launches(info.launches)
     return info

@@ -16,7 +16,7 @@ arrival time; p50/p99 over all requests and the throughput (requests/s over
 the whole stream) are reported by :meth:`SolveServer.run`.
 """
 import time
-from typing import Callable, Dict, List
+from typing import Callable, Dict, List, Optional
 
 import numpy as np
 import torch
@@ -37,13 +37,15 @@ def resident_estimate(n: int, nnz: int, fp64: bool) -> int:
     return csr + sell + vec
 
 
-def poisson_request_problem(req: dict, device, dtype=torch.float64):
+def poisson_request_problem(req: dict, device, dtype=torch.float64, inputs: Optional[dict] = None):
     """Build the system of one serving request on the device: a jittered
     TriangleMesh box (P1/P2) or TetrahedronMesh box (P1), lognormal(0, 1)
     per-cell coefficient, f = 1, u = 0 on the boundary; or, for kind
     'elast', P1 vector elasticity on a tetrahedral box (lambda = 1, mu = 0.5
     scaled per cell by a lognormal(0, 0.5) factor, clamped at x = 0, body
-    force (0, 0, -1)).  Returns (A, b)."""
+    force (0, 0, -1)).  Returns (A, b).  ``inputs`` (a dict), when given,
+    receives host copies of the mesh and coefficients (for checking a result
+    against another implementation)."""
     from . import TriangleMesh, TetrahedronMesh, LagrangeFESpace
     from .fem import BilinearForm, LinearForm, ScalarDiffusionIntegrator, ScalarSourceIntegrator, DirichletBC
     g = torch.Generator(device="cpu").manual_seed(int(req["seed"]))
@@ -55,6 +57,9 @@ def poisson_request_problem(req: dict, device, dtype=torch.float64):
         scale = torch.exp(0.5 * torch.randn(mesh.number_of_cells(), generator=g, dtype=torch.float64)).to(device)
         ts = TensorFunctionSpace(LagrangeFESpace(mesh, 1), (-1, 3))
         mat = LinearElasticMaterial("m", lame_lambda=1.0, shear_modulus=0.5, cell_scale=scale)
+        if inputs is not None:
+            inputs.update(kind="elast", node=mesh.node.cpu().numpy(), cell=mesh.cell.cpu().numpy(), p=1,
+                          scale=scale.cpu().numpy())
         bf = BilinearForm(ts)
         bf.add_integrator(LinearElasticityIntegrator(mat, q=4))
         lf = LinearForm(ts)
@@ -73,6 +78,9 @@ def poisson_request_problem(req: dict, device, dtype=torch.float64):
     inside = torch.all((node > 1e-12) & (node < 1.0 - 1e-12), dim=1)
     node.add_(d * inside.unsqueeze(1))
     kappa = torch.exp(torch.randn(mesh.number_of_cells(), generator=g, dtype=torch.float64)).to(device)
+    if inputs is not None:
+        inputs.update(kind=req["kind"], node=node.cpu().numpy(), cell=mesh.cell.cpu().numpy(), p=p,
+                      kappa=kappa.cpu().numpy())
     space = LagrangeFESpace(mesh, p=p)
     bf = BilinearForm(space)
     bf.add_integrator(ScalarDiffusionIntegrator(coef=kappa, q=p + 2))

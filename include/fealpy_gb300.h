@@ -259,9 +259,12 @@ int32_t fgb_pcg_f64(int64_t n, const int64_t* indptr, const int32_t* indices, co
  * FGB_ERR_CAPACITY before any device work.  The caller zeroes nothing: each
  * call writes the solver state (with its block-arrival counters, which must
  * start at zero) before the first kernel, and every vector is written before
- * it is read.  The first call on a device looks up the array's device address
- * (and may load this library's device code): make it once per device, with
- * that device current, before any stream capture.  The scratch is shared by
+ * it is read.  Every call looks up the array's device address in the
+ * context current on the calling thread (the address belongs to that
+ * context, so a cudaDeviceReset or a new context between calls is safe); the
+ * first call in a context may load this library's device code into it: make
+ * that first call, with the device current, before any stream capture.
+ * The scratch is shared by
  * all calls on a device, so calls that overlap in time (two host threads, or
  * two streams) race on it: serialise them. */
 #define FGB_PCG_NOALLOC_MAX_ROWS 65536
@@ -398,6 +401,18 @@ int32_t fgb_pcg_sell_mixed(const fgb_sell* A, const double* diag_inv64, const do
                            int32_t check_every, int32_t use_graph, int32_t profile,
                            void* workspace, size_t workspace_bytes, fgb_pcg_info* info_host,
                            void* stream);
+/* fgb_pcg_sell_mixed with the persistent kernel's grid-barrier wait limit:
+ * a block waits at most `barrier_polls` polls (about 64 ns apart) for the
+ * others before it gives up, raises the shared error flag and returns, and
+ * then every block returns and the call reports FGB_ERR_CUDA.  barrier_polls
+ * <= 0 selects the default limit (2e7 polls, over a second), which a
+ * cooperative launch with every block resident never reaches.  Only
+ * use_graph = 2 waits on other blocks. */
+int32_t fgb_pcg_sell_mixed_ex(const fgb_sell* A, const double* diag_inv64, const double* b,
+                              double* x, double rtol, double delta, int64_t maxit,
+                              int32_t check_every, int32_t use_graph, int32_t profile,
+                              int64_t barrier_polls, void* workspace, size_t workspace_bytes,
+                              fgb_pcg_info* info_host, void* stream);
 
 /* ---- batched FP32-refined Jacobi-PCG over many systems ------------------ */
 

@@ -430,8 +430,10 @@ def jacobi_cg(crow, col, val, b, atol=1e-12, rtol=1e-8, maxit=10000, use_jacobi=
 
 # ------------------------------------------------------------------ pipelines
 def poisson_pipeline(node, cell, p, kappa=None, rho=None, q=None, f_at_q=None, gd_dofs=None, rtol=1e-10,
-                     maxit=100000):
+                     maxit=100000, f_vec=None):
     """Full reference pipeline: assembly (diffusion [+ mass]) -> RHS -> BC -> Jacobi-PCG.
+    ``f_vec``: a right-hand-side vector given per dof (instead of the source
+    integral of ``f_at_q``, default f = 1).
     Returns a dict of every intermediate (used by the parity tests and the CPU baseline)."""
     topo = construct(cell)
     NN = node.shape[0]
@@ -443,13 +445,47 @@ def poisson_pipeline(node, cell, p, kappa=None, rho=None, q=None, f_at_q=None, g
     crow, col, val = coalesce_to_csr(c2d, K, n)
     TD = cell.shape[1] - 1
     bcs, _ = _rule(TD, p, q)
-    fq = np.ones((cell.shape[0], bcs.shape[0])) if f_at_q is None else f_at_q(bc_to_point(node, cell, bcs))
-    F = source_vector(node, cell, c2d, p, n, fq, q)
+    if f_vec is not None:
+        F = np.asarray(f_vec, dtype=np.float64).copy()
+    else:
+        fq = np.ones((cell.shape[0], bcs.shape[0])) if f_at_q is None else f_at_q(bc_to_point(node, cell, bcs))
+        F = source_vector(node, cell, c2d, p, n, fq, q)
     is_bd = boundary_dof_flag(cell, topo, c2d, p, n)
     uh = np.zeros(n)
     if gd_dofs is not None:
         uh[is_bd] = gd_dofs[is_bd]
     (bcrow, bcol, bval), Fb = dirichlet_apply(crow, col, val, is_bd, F, uh)
+    x, info = jacobi_cg(bcrow, bcol, bval, Fb, atol=1e-30, rtol=rtol, maxit=maxit)
+    return {"c2d": c2d, "n": n, "crow": crow, "col": col, "val": val, "F": F, "is_bd": is_bd,
+            "bc_crow": bcrow, "bc_col": bcol, "bc_val": bval, "bc_F": Fb, "x": x, "info": info}
+
+
+def elasticity_pipeline(node, cell, lam, mu, q=4, force=(0.0, 0.0, -1.0), clamp=None, rtol=1e-10, maxit=100000):
+    """P1 vector elasticity on tetrahedra, interleaved dofs (3 node + comp):
+    LinearElasticityIntegrator local matrices (elasticity_local), coalesce to
+    CSR, a constant body force through VectorSourceIntegrator
+    (fealpy/fem/vector_source_integrator.py; the cell vector is
+    sum_q w_q |T| phi_i f_d), Dirichlet u = 0 on the boundary nodes where
+    ``clamp(node)`` holds (TensorFunctionSpace.is_boundary_dof, method 'interp',
+    fealpy/functionspace/tensor_space.py:156-185: boundary-face dofs filtered
+    at their interpolation points, the nodes for P1), Jacobi-PCG."""
+    NN = node.shape[0]
+    n = 3 * NN
+    topo = construct(cell)
+    c2d = vector_elasticity_dofs(cell)
+    KK = elasticity_local(node, cell, lam, mu, q)
+    crow, col, val = coalesce_to_csr(c2d, KK, n)
+    bcs, ws = _rule(3, 1, q)
+    cm = simplex_measure(cell, node)
+    phi = simplex_shape_function(bcs, 1)
+    loc = np.einsum("c, q, qi, d -> cid", cm, ws, phi, np.asarray(force, dtype=np.float64), optimize=True)
+    F = np.zeros(n)
+    np.add.at(F, c2d, loc.reshape(cell.shape[0], -1))
+    node_bd = boundary_dof_flag(cell, topo, cell, 1, NN)
+    if clamp is not None:
+        node_bd &= np.asarray(clamp(node), dtype=bool)
+    is_bd = np.repeat(node_bd, 3)
+    (bcrow, bcol, bval), Fb = dirichlet_apply(crow, col, val, is_bd, F, np.zeros(n))
     x, info = jacobi_cg(bcrow, bcol, bval, Fb, atol=1e-30, rtol=rtol, maxit=maxit)
     return {"c2d": c2d, "n": n, "crow": crow, "col": col, "val": val, "F": F, "is_bd": is_bd,
             "bc_crow": bcrow, "bc_col": bcol, "bc_val": bval, "bc_F": Fb, "x": x, "info": info}

@@ -3,7 +3,8 @@ FEALPy (numpy backend, unmodified) through its public API.
 
 Run in an environment where the reference checkout is importable:
 
-    python tests/golden/make_golden.py /path/to/fealpy-checkout
+    python tests/golden/make_golden.py /path/to/fealpy-checkout            # small cases, C1
+    python tests/golden/make_golden.py --configs /path/to/fealpy-checkout  # mid-size config laws
 
 The fixtures hold only inputs and outputs of the reference (meshes, dof maps,
 local matrices, CSR matrices, vectors, iteration counts, quadrature tables and
@@ -205,5 +206,140 @@ def main(ref_root):
     print("done")
 
 
+def config_cases(ref_root):
+    """Mid-size cases of the benchmark configurations' laws, run through the
+    reference (numpy backend) with the same seeded generators as the GPU
+    workloads (``fealpy_gb300.workloads``):
+
+    * ``cfg_c2_tet_p2_8``: P2 diffusion + mass on the 8^3 tetrahedral box,
+      interior nodes jittered by U(+-0.2h), lognormal(0, 1) per-cell diffusion,
+      reaction 1, f = 1, u = 0, q = 4 (4,913 dofs, 3,375 interior);
+    * ``cfg_c3_tri_p3_32``: P3 diffusion on the 32x32 triangle box, jitter
+      U(+-0.15h), a 4x4 checkerboard coefficient log-uniform in [0.1, 10],
+      q = p + 3, f = 1, u = 0 (9,409 dofs);
+    * ``cfg_c5_elasticity_8``: P1 vector elasticity on the 8^3 tetrahedral box,
+      lambda = 1, mu = 0.5 scaled per cell by lognormal(0, 0.5), clamped at
+      x = 0, body force (0, 0, -1), q = 4 (2,187 dofs).
+
+    Each fixture holds the inputs and the reference's pre- and post-Dirichlet
+    CSR (canonical order), right-hand sides, Jacobi-PCG solution (rtol 1e-10)
+    and iteration count."""
+    sys.path.insert(0, HERE)
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    import refshim
+    refshim.install(ref_root)
+    from fealpy.backend import backend_manager as bm
+    bm.set_backend("numpy")
+    from fealpy.mesh import TriangleMesh, TetrahedronMesh
+    from fealpy.functionspace import LagrangeFESpace, TensorFunctionSpace
+    from fealpy.fem import (BilinearForm, LinearForm, ScalarDiffusionIntegrator, ScalarMassIntegrator,
+                            LinearElasticityIntegrator, ScalarSourceIntegrator, VectorSourceIntegrator, DirichletBC)
+    from fealpy.solver import cg
+    from fealpy.material import LinearElasticMaterial
+    from fealpy.sparse import CSRTensor
+    from fealpy.decorator import cartesian
+    from fealpy_gb300 import workloads as W
+
+    def jacobi(A):
+        d = A.diags()
+        return CSRTensor(d.crow, d.col, 1.0 / d.values, A.shape)
+
+    @cartesian
+    def zero(p):
+        return np.zeros(p.shape[:-1], dtype=np.float64)
+
+    def scalar_case(name, mesh, p, q, integrators, extra):
+        space = LagrangeFESpace(mesh, p=p)
+        bf = BilinearForm(space)
+        bf.add_integrator(*integrators)
+        A = bf.assembly()
+        lf = LinearForm(space)
+        lf.add_integrator(ScalarSourceIntegrator(1.0, q=q))
+        F = lf.assembly()
+        bc = DirichletBC(space, gd=zero)
+        A2, F2 = bc.apply(A, F.copy())
+        uh, info = cg(A2, F2, M=jacobi(A2), atol=1e-30, rtol=1e-10, returninfo=True)
+        c0, c1, c2 = canonical(A.crow, A.col, A.values)
+        p0, p1, p2 = canonical(A2.crow, A2.col, A2.values)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), node=mesh.node, cell=mesh.cell, p=np.int64(p),
+                            q=np.int64(q), cell2dof=space.cell_to_dof(), crow=c0, col=c1, val=c2, F=F,
+                            is_bd=bc.is_boundary_dof, bc_crow=p0, bc_col=p1, bc_val=p2, bc_F=F2, uh=uh,
+                            niter=np.int64(info["niter"]), **extra)
+        print(name, space.number_of_global_dofs(), A.nnz, A2.nnz, info["niter"])
+
+    # C2 law: the bench generator at 8^3
+    node, cell, kappa = W.diffusion_mass_tet_box(8)
+    mesh = TetrahedronMesh(node, cell)
+    scalar_case("cfg_c2_tet_p2_8", mesh, 2, 4,
+                [ScalarDiffusionIntegrator(coef=kappa, q=4), ScalarMassIntegrator(coef=1.0, q=4)],
+                {"kappa": kappa})
+
+    # C3 law: a P3 mesh of the batched generator's law at nx = 32
+    rng = np.random.default_rng(32)
+    values = np.exp(rng.uniform(np.log(0.1), np.log(10.0), size=16))
+    node, cell = W.tri_box_arrays(32, 32)
+    node = W.jitter_interior(node, 1.0 / 32, 0.15, seed=int(rng.integers(0, 2 ** 31 - 1)))
+    kappa = W.checkerboard_cells(node, cell, values)
+    mesh = TriangleMesh(node, cell)
+    scalar_case("cfg_c3_tri_p3_32", mesh, 3, 6, [ScalarDiffusionIntegrator(coef=kappa, q=6)], {"kappa": kappa})
+
+    # C5 law: the elasticity generator at 8^3
+    node, cell, scale = W.elasticity_tet_box(8)
+    mesh = TetrahedronMesh(node, cell)
+
+    class ScaledMaterial(LinearElasticMaterial):
+        def __init__(self, s, **kw):
+            super().__init__(**kw)
+            self._s = s
+
+        def elastic_matrix(self, bcs=None):
+            return self._s[:, None, None, None] * super().elastic_matrix(bcs)
+
+    mat = ScaledMaterial(scale, name="m", lame_lambda=1.0, shear_modulus=0.5)
+    ts = TensorFunctionSpace(LagrangeFESpace(mesh, p=1), (-1, 3))
+    bf = BilinearForm(ts)
+    bf.add_integrator(LinearElasticityIntegrator(mat, q=4))
+    A = bf.assembly()
+
+    @cartesian
+    def body_force(p):
+        out = np.zeros(p.shape[:-1] + (3,), dtype=np.float64)
+        out[..., 2] = -1.0
+        return out
+
+    @cartesian
+    def clamp(p):
+        return np.abs(p[..., 0]) < 1e-12
+
+    @cartesian
+    def zero_disp(p):
+        return np.zeros(p.shape[:-1] + (3,), dtype=np.float64)
+
+    lf = LinearForm(ts)
+    lf.add_integrator(VectorSourceIntegrator(source=body_force, q=4))
+    F = lf.assembly()
+    bc = DirichletBC(ts, gd=zero_disp, threshold=clamp)
+    A2, F2 = bc.apply(A, F)
+    uh, info = cg(A2, F2, M=jacobi(A2), atol=1e-30, rtol=1e-10, returninfo=True)
+    c0, c1, c2 = canonical(A.crow, A.col, A.values)
+    p0, p1, p2 = canonical(A2.crow, A2.col, A2.values)
+    np.savez_compressed(os.path.join(HERE, "cfg_c5_elasticity_8.npz"), node=mesh.node, cell=mesh.cell, scale=scale,
+                        cell2dof=ts.cell_to_dof(), crow=c0, col=c1, val=c2, F=F, is_bd=bc.is_boundary_dof,
+                        bc_crow=p0, bc_col=p1, bc_val=p2, bc_F=F2, uh=uh, niter=np.int64(info["niter"]))
+    print("cfg_c5_elasticity_8", ts.number_of_global_dofs(), A.nnz, A2.nnz, info["niter"])
+
+
+def _reference_root(argv):
+    root = argv[0] if argv else os.environ.get("FEALPY_REFERENCE")
+    if not root:
+        raise SystemExit("usage: make_golden.py [--configs] /path/to/fealpy-checkout "
+                         "(or set FEALPY_REFERENCE)")
+    return root
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("FEALPY_REFERENCE", "/root/reference"))
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    if "--configs" in sys.argv[1:]:
+        config_cases(_reference_root(args))
+    else:
+        main(_reference_root(args))

@@ -1,7 +1,8 @@
 """Batched FP32-refined PCG (fealpy_gb300.batch): every system of a batch
 reaches the true relative residual 1e-10, agrees with the single-system FP64
-solve, and gives the same bits alone and inside any mix, whether it joins
+solve and with the CPU oracle's pipeline on the same inputs, and gives the same bits alone and inside any mix, whether it joins
 at the start or while others are in flight (continuous batching)."""
+import numpy as np
 import pytest
 import torch
 
@@ -16,7 +17,10 @@ def cuda():
     return torch.device("cuda", 0)
 
 
-def _poisson(F, mesh, p, seed, dtype=torch.float64):
+def _poisson(F, mesh, p, seed, dtype=torch.float64, inputs=None):
+    """Diffusion (lognormal kappa) + mass, quadrature p + 2, a random nodal
+    right-hand side, u = 0 on the boundary.  ``inputs`` (a list) receives the
+    host copies of the mesh, kappa and f for the oracle."""
     from fealpy_gb300.fem import BilinearForm, ScalarDiffusionIntegrator, ScalarMassIntegrator, DirichletBC
     g = torch.Generator(device="cpu").manual_seed(seed)
     NC = mesh.number_of_cells()
@@ -27,18 +31,29 @@ def _poisson(F, mesh, p, seed, dtype=torch.float64):
     A = bf.assembly(dtype=dtype)
     n = space.number_of_global_dofs()
     f = torch.rand(n, generator=g, dtype=torch.float64).to(mesh.node.device)
+    if inputs is not None:
+        inputs.append({"node": mesh.node.cpu().numpy(), "cell": mesh.cell.cpu().numpy(), "p": p,
+                       "kappa": kappa.cpu().numpy(), "f": f.cpu().numpy()})
     return DirichletBC(space, gd=0.0).apply(A, f)
 
 
-def _systems(dev):
+def _systems(dev, inputs=None):
     import fealpy_gb300 as F
     out = []
     for k, (nx, p) in enumerate([(8, 1), (20, 2), (13, 3), (40, 1), (6, 2)]):
         m = F.TriangleMesh.from_box([0, 1, 0, 1], nx, nx, device=dev)
-        out.append(_poisson(F, m, p, k))
+        out.append(_poisson(F, m, p, k, inputs=inputs))
     m = F.TetrahedronMesh.from_box([0, 1, 0, 1, 0, 1], 6, 5, 4, device=dev)
-    out.append(_poisson(F, m, 1, 9))
+    out.append(_poisson(F, m, 1, 9, inputs=inputs))
     return out
+
+
+def _oracle_solution(d):
+    """The CPU oracle's pipeline (reference algorithm) on the same inputs."""
+    from oracle import fem_oracle as O
+    out = O.poisson_pipeline(d["node"], d["cell"], d["p"], kappa=d["kappa"], rho=1.0, q=d["p"] + 2,
+                             f_vec=d["f"], rtol=1e-12)
+    return out["x"]
 
 
 def _residual(A, b, x):
@@ -52,7 +67,8 @@ def test_batch_converges_and_matches_fp64():
     dev = cuda()
     import fealpy_gb300 as F
     from fealpy_gb300.batch import BatchSolver
-    systems = _systems(dev)
+    inputs = []
+    systems = _systems(dev, inputs)
     bs = BatchSolver(8, slices_per_tile=4, rows_per_tile=512)
     for k, (A, b) in enumerate(systems):
         bs.add(A, b, rtol=RTOL, key=k)
@@ -67,6 +83,10 @@ def test_batch_converges_and_matches_fp64():
         x64 = F.cg(A, b, M=F.JacobiPreconditioner().apply(A), atol=1e-30, rtol=1e-13)
         err = float((r.x - x64).abs().max() / x64.abs().max())
         assert err < 1e-8, (k, err)
+        # against the CPU oracle's assembly + Dirichlet + PCG of the same inputs
+        xo = _oracle_solution(inputs[k])
+        erro = float(np.max(np.abs(r.x.cpu().numpy() - xo)) / np.max(np.abs(xo)))
+        assert erro < 1e-8, (k, erro)
 
 
 def test_batch_solo_equals_mix_and_late_admission():

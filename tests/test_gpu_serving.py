@@ -1,7 +1,7 @@
 """Serving loop (fealpy_gb300.serving): requests arriving over time are
 admitted into the running batch as slots and memory free up, every result
-meets the 1e-10 true residual, and each result is the same (bit for bit)
-alone and in the mix."""
+meets the 1e-10 true residual, matches the CPU oracle's solution of the same
+request, and is the same (bit for bit) alone and in the mix."""
 import numpy as np
 import pytest
 import torch
@@ -35,12 +35,23 @@ def test_serving_mix_equals_solo_and_converges():
     assert out["n"] == len(reqs) and out["p99_s"] >= out["p50_s"] > 0
     assert out["max_relres"] <= 1e-10 * 1.0001
     assert srv.resident == 0 and srv.peak_resident > 0
+    from oracle import fem_oracle as O
     for i, r in enumerate(reqs):
-        A, b = poisson_request_problem(r, dev)
+        inp = {}
+        A, b = poisson_request_problem(r, dev, inputs=inp)
         bs = BatchSolver(1, max_slice_tiles=1 << 17, max_row_tiles=1 << 17, device=dev)
         bs.add(A, b, rtol=1e-10, maxit=100000, key=0)
         solo = bs.solve_all()[0]
         assert np.array_equal(solo.x.cpu().numpy(), out["solutions"][i]), i
+        # against the CPU oracle's pipeline (reference algorithm) on the same inputs
+        if inp["kind"] == "elast":
+            ref = O.elasticity_pipeline(inp["node"], inp["cell"], 1.0 * inp["scale"], 0.5 * inp["scale"], q=4,
+                                        clamp=lambda x: np.abs(x[..., 0]) < 1e-12, rtol=1e-12)
+        else:
+            ref = O.poisson_pipeline(inp["node"], inp["cell"], inp["p"], kappa=inp["kappa"], q=inp["p"] + 2,
+                                     rtol=1e-12)
+        err = np.max(np.abs(out["solutions"][i] - ref["x"])) / np.max(np.abs(ref["x"]))
+        assert err < 1e-8, (i, inp["kind"], err)
 
 
 def test_serving_memory_budget_limits_admission():

@@ -129,3 +129,43 @@ def test_elasticity_case(golden_dir):
     x, info = O.jacobi_cg(bcrow, bcol, bval, F, atol=1e-30, rtol=1e-10)
     assert abs(info["niter"] - int(z["niter"])) <= 1
     assert rel_err(x, z["uh"]) < 1e-8
+
+
+@pytest.mark.parametrize("name", ["cfg_c2_tet_p2_8", "cfg_c3_tri_p3_32"])
+def test_config_law_scalar_cases(golden_dir, name):
+    """Mid-size cases of the C2 (P2 tet 8^3, diffusion + mass) and C3 (P3
+    triangles 32x32, checkerboard coefficient) laws: the oracle's full
+    pipeline against the reference's outputs."""
+    z = load(golden_dir, name + ".npz")
+    node, cell, p, q = z["node"], z["cell"], int(z["p"]), int(z["q"])
+    rho = 1.0 if cell.shape[1] == 4 else None
+    out = O.poisson_pipeline(node, cell, p, kappa=z["kappa"], rho=rho, q=q, rtol=1e-10)
+    assert np.array_equal(out["c2d"], z["cell2dof"])
+    assert np.array_equal(out["crow"], z["crow"]) and np.array_equal(out["col"], z["col"])
+    assert rel_err(out["val"], z["val"]) < RTOL
+    assert rel_err(out["F"], z["F"]) < RTOL
+    assert np.array_equal(out["is_bd"], z["is_bd"])
+    assert np.array_equal(out["bc_crow"], z["bc_crow"]) and np.array_equal(out["bc_col"], z["bc_col"])
+    assert rel_err(out["bc_val"], z["bc_val"]) < RTOL
+    assert rel_err(out["bc_F"], z["bc_F"]) < RTOL
+    assert abs(out["info"]["niter"] - int(z["niter"])) <= 1
+    assert rel_err(out["x"], z["uh"]) < 1e-9
+
+
+def test_config_law_elasticity_case(golden_dir):
+    """Mid-size case of the C5 law (P1 elasticity 8^3, per-cell scaled
+    material, x = 0 clamp, body force -z): the oracle's pipeline against the
+    reference's outputs."""
+    z = load(golden_dir, "cfg_c5_elasticity_8.npz")
+    node, cell, s = z["node"], z["cell"], z["scale"]
+    out = O.elasticity_pipeline(node, cell, 1.0 * s, 0.5 * s, q=4, clamp=lambda x: np.abs(x[..., 0]) < 1e-12)
+    assert np.array_equal(out["c2d"], z["cell2dof"])
+    assert np.array_equal(out["crow"], z["crow"]) and np.array_equal(out["col"], z["col"])
+    assert rel_err(out["val"], z["val"]) < RTOL
+    assert rel_err(out["F"], z["F"]) < RTOL
+    assert np.array_equal(out["is_bd"], z["is_bd"])
+    assert np.array_equal(out["bc_crow"], z["bc_crow"]) and np.array_equal(out["bc_col"], z["bc_col"])
+    assert rel_err(out["bc_val"], z["bc_val"]) < RTOL
+    assert rel_err(out["bc_F"], z["bc_F"]) < RTOL
+    assert abs(out["info"]["niter"] - int(z["niter"])) <= 1
+    assert rel_err(out["x"], z["uh"]) < 1e-9

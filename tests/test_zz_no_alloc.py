@@ -2,8 +2,9 @@
 array of the library) against fgb_pcg_f64 with a caller workspace, called
 through the C ABI on the C1 system (P1 Poisson on a 64x64 triangle box after
 Dirichlet elimination, 4,225 rows).  Two no-allocation calls in a row must
-both match the workspace solve; a size above the fixed limit is refused
-before any device work.  This file is named to be collected last so that it
+both match the workspace solve, and the second must leave the device's free
+memory unchanged; a size above the fixed limit is refused before any device
+work.  This file is named to be collected last so that it
 also runs after every other GPU test in the same process."""
 import ctypes
 import os
@@ -56,10 +57,17 @@ def test_noalloc_matches_workspace_entry_point(golden_dir):
     for call in range(2):
         x = torch.zeros(n, dtype=torch.float64, device=b.device)
         info = _lib.PcgInfo()
+        torch.cuda.synchronize()
+        free_before = torch.cuda.mem_get_info(b.device)[0]
         rc = lib.fgb_pcg_f64_noalloc(n, _p(crow), _p(col), _p(val), _p(dinv), _p(b), _p(x), *args[:2], args[2],
                                      args[3], args[4], args[5], ctypes.byref(info), stream)
         torch.cuda.synchronize()
+        free_after = torch.cuda.mem_get_info(b.device)[0]
         assert rc == 0, (call, lib.fgb_status_string(rc))
+        if call == 1:
+            # the defining property: a call allocates no device memory (the
+            # first call is exempt: it may load the library's device code)
+            assert free_after == free_before, (free_before, free_after)
         assert info.reason == info_ws.reason and abs(info.niter - info_ws.niter) <= 1, (call, info.niter)
         err = float((x - x_ws).abs().max() / x_ws.abs().max())
         assert err <= TOL, (call, err)
