@@ -203,8 +203,17 @@ def spmv_roofline(mixed, gdof, n, peak, peak_kind):
     # (the formula of the measurement definition, used verbatim; the SELL copy
     # reads a 4-byte slot->row map and an 8-byte slice pointer per 32 rows in
     # place of the row pointer).  With 2-byte column steps: nnz (s + 2) + n (12 + 2 s).
-    d16 = mixed["sell_cols"] == "d16"
-    bytes_per_launch = nnz * (4 + 2) + gdof * (12 + 8) if d16 else nnz * (4 + 4) + gdof * (8 + 8)
+    # 15-bit steps: E (s + 2) + n (8 + 2 s), E = nonzeros + long-step entries
+    # (a 2-byte code and a value each; per row a first column and a slot map
+    # entry replace the row pointer)
+    cols = mixed["sell_cols"]
+    d16 = cols == "d16"
+    if cols == "d15":
+        bytes_per_launch = mixed["stored_entries"] * (4 + 2) + gdof * (8 + 8)
+    elif d16:
+        bytes_per_launch = nnz * (4 + 2) + gdof * (12 + 8)
+    else:
+        bytes_per_launch = nnz * (4 + 4) + gdof * (8 + 8)
     achieved = bytes_per_launch / (mixed["kernel_ms_avg"] / 1e3) / 1e9 if mixed["kernel_ms_avg"] > 0 else 0.0
     # whole FP32 iteration: B_it = B_spmv + 11 n s (the vector traffic of the
     # update kernels), over the live time per iteration of the timed solve (the
@@ -223,9 +232,10 @@ def spmv_roofline(mixed, gdof, n, peak, peak_kind):
             traffic = None
     return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak if peak else None, "traffic": traffic,
-            "kernel": "sell_pcg_spmv<float> (SELL-32" + (", 16-bit column steps" if d16 else "") +
-                      "; Ap = A p and p.Ap)",
+            "kernel": "sell_pcg_spmv<float> (SELL-32" + {"d16": ", 16-bit column steps", "d15": ", 15-bit column "
+                      "steps"}.get(cols, "") + "; Ap = A p and p.Ap)",
             "algorithmic_bytes_per_launch": bytes_per_launch, "avg_launch_ms": mixed["kernel_ms_avg"],
+            "bytes_with_4_byte_columns": nnz * (4 + 4) + gdof * (8 + 8),
             "peak_source": peak_kind,
             "iteration": {"bytes_per_iteration": bytes_per_iter, "us_per_iteration": it_ms * 1e3,
                           "achieved": it_achieved, "unit": "GB/s", "frac": it_achieved / peak if peak else None}}
@@ -247,7 +257,8 @@ def run_ours(args):
     dev = torch.device("cuda", local)
 
     from fealpy_gb300 import solver as SV
-    SV.SELL_D16 = {"auto": None, "i32": False, "d16": True}[args.sell_cols]
+    SV.SELL_D16 = {"auto": None, "i32": False, "d16": True, "d15": False}[args.sell_cols]
+    SV.SELL_D15 = args.sell_cols == "d15"
     n = args.n
     node_np, cell_np, kappa_np = diffusion_mass_tet_box(n)
     mesh, space, kappa, bc = build_problem(torch, F, node_np, cell_np, kappa_np, dev)
@@ -313,8 +324,9 @@ def run_ours(args):
                          "extra_ms_avg": pinfo["extra_ms"] / max(kl, 1), "stages_ms": stages,
                          "clocks": clocks, "nnz": A2.nnz, "n": gdof,
                          "sell_launch": list(A2._sell.launch) if getattr(A2, "_sell", None) is not None else None,
-                         "sell_cols": ("d16" if A2._sell.d16 else "i32") if getattr(A2, "_sell", None) is not None
-                         else None}
+                         "sell_cols": A2._sell.cols if getattr(A2, "_sell", None) is not None else None,
+                         "stored_entries": A2._sell.stored_entries() if getattr(A2, "_sell", None) is not None
+                         else A2.nnz}
 
     if set(modes) != {"fp64", "mixed"} or args.no_e2e:
         # profiling run: report the per-mode timings on stderr only
@@ -392,7 +404,8 @@ def run_ours(args):
                              "max_rel_err_vs_fp64": err, "stages_ms": mixed["stages_ms"],
                              "spmv_us": mixed["kernel_ms_avg"] * 1e3, "update_us": mixed["other_ms_avg"] * 1e3,
                              "other_kernels_us": mixed["extra_ms_avg"] * 1e3,
-                             "sell_launch_threads_blocks": mixed["sell_launch"], "sell_columns": mixed["sell_cols"]},
+                             "sell_launch_threads_blocks": mixed["sell_launch"], "sell_columns": mixed["sell_cols"],
+                             "sell_stored_entries": mixed["stored_entries"]},
             "fp64": {"ms_per_step": fp64["ms_per_step"], "dof_per_s": world * gdof / (fp64["ms_per_step"] / 1e3),
                      "cg_iters": fp64["niter"], "true_relres": fp64["relres"], "stages_ms": fp64["stages_ms"],
                      "spmv_us": fp64["kernel_ms_avg"] * 1e3, "update_us": fp64["other_ms_avg"] * 1e3,
@@ -850,8 +863,10 @@ def main():
     ap.add_argument("--serve-chunk", type=int, default=64)
     ap.add_argument("--serve-sample", type=int, default=32, help="requests of the serving sample in the default run")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving sample of the default run")
-    ap.add_argument("--sell-cols", choices=["auto", "i32", "d16"], default="i32",
-                    help="column format of the solvers' SELL copies (auto: 16-bit steps where they fit)")
+    ap.add_argument("--sell-cols", choices=["auto", "i32", "d16", "d15"], default="d15",
+                    help="column format of the FP32-refined solver's SELL copy: d15 = 15-bit steps in FEALPy's "
+                         "numbering (default), i32 = 4-byte columns, d16 = 16-bit steps of a renumbered matrix, "
+                         "auto = d16 where its bridges fit; the FP64 solver's copy has 4-byte columns")
     args = ap.parse_args()
     if args.workload == "batched" and args.impl == "ours":
         run_batched(args)

@@ -95,6 +95,8 @@ _SIGNATURES = {
     "fgb_csr_permute": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_sz, c_vp]),
     "fgb_sell_d16_indptr": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_vp, c_sz, c_vp]),
     "fgb_sell_fill_d16": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "fgb_sell_d15_indptr": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_sz, c_vp]),
+    "fgb_sell_fill_d15": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "fgb_permute": (c_i32, [c_i32, c_i64, c_vp, c_vp, c_vp, c_i32, c_vp]),
     "fgb_sell_b3_indptr": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_vp, c_sz, c_vp]),
     "fgb_sell_fill_b3": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
@@ -140,7 +142,7 @@ class SellDesc(ctypes.Structure):
     """``fgb_sell`` (include/fealpy_gb300.h)."""
     _fields_ = [("n", c_i64), ("n_slices", c_i64), ("slice_ptr", c_vp), ("perm", c_vp), ("col", c_vp),
                 ("val64", c_vp), ("val32", c_vp), ("threads", c_i32), ("blocks", c_i32), ("col16", c_vp),
-                ("col0", c_vp), ("node_triples", c_i32), ("reserved", c_i32)]
+                ("col0", c_vp), ("node_triples", c_i32), ("col_long", c_i32)]
 
 
 def library_path() -> str:
@@ -190,7 +192,8 @@ KERNELS_PER_CALL = {
     "fgb_pattern_expand_blocks": 2, "fgb_assemble_scalar": 2, "fgb_assemble_elasticity_p1": 2,
     "fgb_dirichlet_count": 1, "fgb_exclusive_scan_i32": 3, "fgb_dirichlet_fill": 1, "fgb_csr_spmv": 1,
     "fgb_csr_diagonal": 1, "fgb_gather_sum": 1, "fgb_sell_plan": 4, "fgb_sell_fill": 1, "fgb_sell_spmv": 1,
-    "fgb_sell_renumber": 1, "fgb_csr_permute": 5, "fgb_sell_d16_indptr": 4, "fgb_sell_fill_d16": 1, "fgb_permute": 1,
+    "fgb_sell_renumber": 1, "fgb_csr_permute": 5, "fgb_sell_d16_indptr": 4, "fgb_sell_fill_d16": 1,
+    "fgb_sell_d15_indptr": 4, "fgb_sell_fill_d15": 1, "fgb_permute": 1,
     "fgb_sell_b3_indptr": 4, "fgb_sell_fill_b3": 1,
 }
 

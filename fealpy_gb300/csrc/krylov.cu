@@ -651,7 +651,7 @@ const char* fgb_status_string(int32_t status) {
   }
 }
 
-int32_t fgb_abi_version(void) { return 1; }
+int32_t fgb_abi_version(void) { return 2; }
 
 int32_t fgb_csr_spmv(int32_t dtype, int64_t n_row, const int64_t* indptr, const int32_t* indices, const void* values,
                      const void* x, void* y, int32_t lanes_per_row, void* stream) {

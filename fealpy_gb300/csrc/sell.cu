@@ -39,11 +39,13 @@ struct SellView {
   const uint16_t* col16;  // delta-coded columns (then col is unused) or null
   const int32_t* col0;    // first column of every slot's row (delta-coded copies)
   int node_triples;       // 1: slots are node triples (col = 3c, three values each)
+  int d15;                // 1: col16 holds 15-bit steps and long steps (own numbering)
 };
 
-// Storage formats of a SELL copy: 4-byte columns, 16-bit column steps, node
-// triples.
-constexpr int kColsI32 = 0, kColsD16 = 1, kColsB3 = 2;
+// Storage formats of a SELL copy: 4-byte columns, 16-bit column steps
+// (renumbered matrix), node triples, 15-bit steps with long steps (own
+// numbering).
+constexpr int kColsI32 = 0, kColsD16 = 1, kColsB3 = 2, kColsD15 = 3;
 
 // Row of slot (s, lane): sum over entries of val * g(col), for each storage
 // format.  The slice width is a multiple of 4 slots.
@@ -54,6 +56,8 @@ __device__ __forceinline__ T slice_row(const SellView& A, const V* __restrict__ 
   const int w = static_cast<int>((A.slice_ptr[s + 1] - sbase) >> 5);
   if constexpr (FMT == kColsD16)
     return sell_row_acc_d16<V, T>(A.col16, A.col0[s * kSellC + lane], val, sbase, w, lane, g);
+  else if constexpr (FMT == kColsD15)
+    return sell_row_acc_d15<V, T>(A.col16, A.col0[s * kSellC + lane], val, sbase, w, lane, g);
   else if constexpr (FMT == kColsB3)
     return sell_row_acc_b3<V, T>(A.col, val, sbase, w, lane, g);
   else
@@ -64,6 +68,7 @@ __device__ __forceinline__ T slice_row(const SellView& A, const V* __restrict__ 
 template <typename F>
 void with_cols(const SellView& A, F&& f) {
   if (A.node_triples) f(std::integral_constant<int, kColsB3>{});
+  else if (A.col16 && A.d15) f(std::integral_constant<int, kColsD15>{});
   else if (A.col16) f(std::integral_constant<int, kColsD16>{});
   else f(std::integral_constant<int, kColsI32>{});
 }
@@ -965,13 +970,15 @@ using namespace fgb;
 namespace {
 
 SellView view_of(const fgb_sell* A) {
-  return SellView{A->n,   A->n_slices, A->slice_ptr, A->perm, A->col,
-                  A->threads, A->blocks, A->col16,  A->col0, A->node_triples};
+  return SellView{A->n,   A->n_slices, A->slice_ptr, A->perm, A->col,       A->threads,
+                  A->blocks, A->col16,   A->col0,      A->node_triples, A->col_long};
 }
 
+// launch shape in range, and the column arrays the storage format reads present
 bool launch_ok(const fgb_sell* A) {
-  return A->threads >= 0 && A->threads <= 1024 && A->threads % 32 == 0 && A->blocks >= 0 &&
-         A->blocks <= kSellMaxBlocks;
+  const bool cols = A->col16 ? (A->col0 != nullptr && !A->node_triples) : (A->col != nullptr && !A->col_long);
+  return cols && A->slice_ptr && A->perm && A->threads >= 0 && A->threads <= 1024 && A->threads % 32 == 0 &&
+         A->blocks >= 0 && A->blocks <= kSellMaxBlocks;
 }
 
 // CUDA events before the SpMV, after the SpMV and after the rest of each

@@ -250,6 +250,83 @@ __global__ void sell_fill_d16_kernel(int64_t n_slices, const int64_t* __restrict
   }
 }
 
+// entries of a row in the 15-bit copy: its entries plus one long-step entry
+// per 2^30 - 1 of every step above 32767 (columns ascending)
+__device__ __forceinline__ int d15_long_entries(int64_t step) {
+  int m = 0;
+  while (step > 32767) {
+    const int64_t h = (step >> 15) < 0x7fff ? (step >> 15) : 0x7fff;
+    step -= h << 15;
+    ++m;
+  }
+  return m;
+}
+
+__global__ void d15_lengths(int64_t n, const int64_t* __restrict__ indptr, const int32_t* __restrict__ indices,
+                            int32_t* __restrict__ len, int32_t* __restrict__ status) {
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int64_t a = indptr[i], b = indptr[i + 1];
+    int64_t m = b - a;
+    for (int64_t e = a + 1; e < b; ++e) {
+      const int64_t step = static_cast<int64_t>(indices[e]) - indices[e - 1];
+      if (step <= 0) set_status(status, FGB_ERR_ARG);  // columns must ascend strictly
+      else if (step > 32767) m += d15_long_entries(step);
+    }
+    len[i] = static_cast<int32_t>(m);
+  }
+}
+
+// Lane per slot: the slot's first column, then per entry a 15-bit step (or
+// long steps before a far entry), padding with code 0 and value 0 up to the
+// slice width.
+__global__ void sell_fill_d15_kernel(int64_t n_slices, const int64_t* __restrict__ slice_ptr,
+                                     const int32_t* __restrict__ perm, const int64_t* __restrict__ indptr,
+                                     const int32_t* __restrict__ indices, const double* __restrict__ v64,
+                                     const float* __restrict__ v32, int32_t* __restrict__ col0,
+                                     uint16_t* __restrict__ col16, double* __restrict__ s64,
+                                     float* __restrict__ s32) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
+  const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+  for (int64_t s = warp; s < n_slices; s += nwarps) {
+    const int64_t base = slice_ptr[s];
+    const int w = static_cast<int>((slice_ptr[s + 1] - base) / kSellC);
+    const int32_t row = perm[s * kSellC + lane];
+    int64_t rs = 0;
+    int len = 0;
+    if (row >= 0) {
+      rs = indptr[row];
+      len = static_cast<int>(indptr[row + 1] - rs);
+    }
+    int64_t c = len > 0 ? indices[rs] : (row >= 0 ? row : 0);
+    col0[s * kSellC + lane] = static_cast<int32_t>(c);
+    int k = 0;
+    auto put = [&](uint32_t code, double a, float b) {
+      if (k >= w) return;  // cannot happen: the plan's width covers the row with its long steps
+      const int64_t pos = base + sell_pos(lane, k);
+      col16[pos] = static_cast<uint16_t>(code);
+      if (s64) s64[pos] = a;
+      if (s32) s32[pos] = b;
+      ++k;
+    };
+    for (int e = 0; e < len; ++e) {
+      const int64_t col = indices[rs + e];
+      int64_t step = col - c;
+      while (step > 32767) {
+        const int64_t h = (step >> 15) < 0x7fff ? (step >> 15) : 0x7fff;
+        put(0x8000u | static_cast<uint32_t>(h), 0.0, 0.0f);
+        step -= h << 15;
+      }
+      const double a = s64 ? (v64 ? v64[rs + e] : static_cast<double>(v32[rs + e])) : 0.0;
+      const float b = s32 ? (v32 ? v32[rs + e] : static_cast<float>(v64[rs + e])) : 0.0f;
+      put(static_cast<uint32_t>(step), a, b);
+      c = col;
+    }
+    while (k < w) put(0u, 0.0, 0.0f);
+  }
+}
+
 template <typename T>
 __global__ void permute_kernel(int64_t n, const int32_t* __restrict__ order, const T* __restrict__ src,
                                T* __restrict__ dst, int scatter) {
@@ -364,6 +441,31 @@ int32_t fgb_sell_fill_d16(int64_t n, const int64_t* indptr, const int32_t* indic
   if ((val64 || val32) && !values64 && !values32) return FGB_ERR_ARG;
   const int64_t slices = fgb_sell_slots(n) / kSellC;
   sell_fill_d16_kernel<<<grid_for(slices * 32, 256, kNumSMs * 16), 256, 0, as_stream(stream)>>>(
+      slices, slice_ptr, perm, indptr, indices, values64, values32, col0, col16, val64, val32);
+  return launch_status();
+}
+
+int32_t fgb_sell_d15_indptr(int64_t n, const int64_t* indptr, const int32_t* indices, int64_t* entry_indptr,
+                            int32_t* status, void* workspace, size_t workspace_bytes, void* stream) {
+  if (n <= 0 || !indptr || !indices || !entry_indptr || !status) return FGB_ERR_ARG;
+  if (!workspace || workspace_bytes < fgb_sell_d16_workspace_bytes(n)) return FGB_ERR_WORKSPACE;
+  cudaStream_t st = as_stream(stream);
+  Carver cv(workspace, workspace_bytes);
+  int32_t* len = cv.take<int32_t>(n);
+  void* scan_ws = cv.base + cv.off;
+  const size_t scan_bytes = workspace_bytes - cv.off;
+  if (!cv.ok) return FGB_ERR_WORKSPACE;
+  d15_lengths<<<grid_rows(n), kThreads, 0, st>>>(n, indptr, indices, len, status);
+  return exclusive_scan_i32_to_i64(len, n, entry_indptr, scan_ws, scan_bytes, st);
+}
+
+int32_t fgb_sell_fill_d15(int64_t n, const int64_t* indptr, const int32_t* indices, const double* values64,
+                          const float* values32, const int32_t* perm, const int64_t* slice_ptr, int32_t* col0,
+                          uint16_t* col16, double* val64, float* val32, void* stream) {
+  if (n <= 0 || !indptr || !indices || !perm || !slice_ptr || !col0 || !col16) return FGB_ERR_ARG;
+  if ((val64 || val32) && !values64 && !values32) return FGB_ERR_ARG;
+  const int64_t slices = fgb_sell_slots(n) / kSellC;
+  sell_fill_d15_kernel<<<grid_for(slices * 32, 256, kNumSMs * 16), 256, 0, as_stream(stream)>>>(
       slices, slice_ptr, perm, indptr, indices, values64, values32, col0, col16, val64, val32);
   return launch_status();
 }

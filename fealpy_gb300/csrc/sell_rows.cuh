@@ -212,6 +212,83 @@ __device__ __forceinline__ T sell_row_acc_d16(const uint16_t* __restrict__ d16, 
   return acc;
 }
 
+// ------------------------------------------------ 15-bit column steps
+// Columns of a row ascending, in the matrix's own numbering (no renumbering):
+// the slot's first column c0, then one 16-bit code per entry.  A code below
+// 0x8000 is a step: the entry's column is the previous column plus the code.
+// A code 0x8000 | h is a long step: a zero-valued entry that gathers the
+// previous column again (already in cache) and moves the running column on by
+// h * 32768, so that the next step lands on a column far away (FEALPy's
+// numbering puts all vertex dofs before all edge dofs: one long step per row
+// for P2).  Padding entries have code 0 and value 0.  6 bytes per FP32 entry
+// instead of 8, with the gather locality of the original numbering.
+// Advance of one code and the offset its gather takes from the column before
+// it: a step t moves by t and gathers the new column; a long step moves by
+// t * 32768 and gathers the old one.
+__device__ __forceinline__ void d15_code(uint32_t code, int32_t& inc, int32_t& own) {
+  const int32_t t = static_cast<int32_t>(code & 0x7fffu);
+  const bool lng = (code & 0x8000u) != 0u;
+  inc = lng ? (t << 15) : t;
+  own = lng ? 0 : t;
+}
+
+// Columns of a pack from the column before it (base) and the pack's total
+// advance, by prefix sums inside the pack: every pack of a trip is decoded
+// independently of the others, and only the four totals chain.
+__device__ __forceinline__ int4 pack_cols_d15(uint2 d, int32_t base, int32_t& total) {
+  int32_t i0, i1, i2, i3, o0, o1, o2, o3;
+  d15_code(d.x & 0xffffu, i0, o0);
+  d15_code(d.x >> 16, i1, o1);
+  d15_code(d.y & 0xffffu, i2, o2);
+  d15_code(d.y >> 16, i3, o3);
+  const int32_t s01 = i0 + i1;
+  total = s01 + (i2 + i3);
+  return make_int4(base + o0, base + (i0 + o1), base + (s01 + o2), base + (s01 + (i2 + o3)));
+}
+
+// Packs per trip of the 15-bit kernel: a pack carries 24 bytes per FP32
+// entry quad instead of 32, so more packs are kept in flight per warp.
+template <typename T> struct PacksPerTripD15 { static constexpr int value = 2; };
+template <> struct PacksPerTripD15<float> { static constexpr int value = 6; };
+
+// As sell_row_acc, with 15-bit steps and long steps starting from c0.
+template <typename V, typename T, typename G>
+__device__ __forceinline__ T sell_row_acc_d15(const uint16_t* __restrict__ d16, int32_t c0,
+                                              const V* __restrict__ val, int64_t sbase, int w, int lane,
+                                              const G& g) {
+  using P = typename PackD16Of<V>::type;
+  constexpr int U = PacksPerTripD15<V>::value;
+  const int nq = w / kSellPack;
+  T acc = T(0);
+  int32_t c = c0;
+  int q = 0;
+  for (; q + U <= nq; q += U) {
+    P a[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) a[u] = load_pack_d16(d16, val, sbase, lane, q + u);
+    int4 cc[U];
+    int32_t tot[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) cc[u] = pack_cols_d15(a[u].d, 0, tot[u]);
+    int32_t base = c;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int4 k = make_int4(cc[u].x + base, cc[u].y + base, cc[u].z + base, cc[u].w + base);
+      acc = pack_dot_cols<T>(a[u], k, g, acc);
+      base += tot[u];
+    }
+    c = base;
+  }
+  for (; q < nq; ++q) {
+    const P a = load_pack_d16(d16, val, sbase, lane, q);
+    int32_t tot;
+    const int4 k = pack_cols_d15(a.d, c, tot);
+    acc = pack_dot_cols<T>(a, k, g, acc);
+    c += tot;
+  }
+  return acc;
+}
+
 // ------------------------------------------------ node triples (vector problems)
 // For a vector space with three interleaved components (dof = 3 node + comp)
 // every nonzero of a row sits in a run of three consecutive columns 3c..3c+2:

@@ -233,21 +233,42 @@ class SellMatrix:
     and SpMV wrappers below permute vectors into and out of that numbering."""
 
     def __init__(self, n, n_slices, slice_ptr, perm, col, val64, val32, col16=None, col0=None, order=None,
-                 nnz=None, node_triples=False):
+                 nnz=None, node_triples=False, d15=False):
         self.n, self.n_slices = n, n_slices
         self.slice_ptr, self.perm, self.col, self.val64, self.val32 = slice_ptr, perm, col, val64, val32
         self.col16, self.col0, self.order, self.nnz = col16, col0, order, nnz
         self.node_triples = bool(node_triples)
+        self._d15 = bool(d15)
         self.desc = _lib.SellDesc(n, n_slices, slice_ptr.data_ptr(), perm.data_ptr(),
                                   col.data_ptr() if col is not None else None,
                                   val64.data_ptr() if val64 is not None else None,
                                   val32.data_ptr() if val32 is not None else None, 0, 0,
                                   col16.data_ptr() if col16 is not None else None,
-                                  col0.data_ptr() if col0 is not None else None, 1 if node_triples else 0, 0)
+                                  col0.data_ptr() if col0 is not None else None, 1 if node_triples else 0,
+                                  1 if d15 else 0)
 
     @property
     def d16(self) -> bool:
-        return self.col16 is not None
+        """16-bit steps of a renumbered matrix."""
+        return self.col16 is not None and not self._d15
+
+    @property
+    def d15(self) -> bool:
+        """15-bit steps with long steps, in the matrix's own numbering."""
+        return self._d15
+
+    def stored_entries(self) -> int:
+        """Entries of the copy without padding: the nonzeros, plus the
+        long-step entries of a 15-bit copy (one host read)."""
+        ep = getattr(self, "entry_indptr", None)
+        return int(ep[-1].item()) if ep is not None else int(self.nnz or 0)
+
+    @property
+    def cols(self) -> str:
+        """Column storage: 'i32', 'd16', 'd15' or 'triples'."""
+        if self.node_triples:
+            return "triples"
+        return "d15" if self._d15 else ("d16" if self.col16 is not None else "i32")
 
     @property
     def device(self):
@@ -333,19 +354,23 @@ D16_MAX_GROWTH = 1.25
 
 def sell_build(indptr, indices, values64=None, values32=None, want64=True, want32=False,
                d16: Optional[bool] = None, blocks: Optional[Sequence[int]] = None,
-               triples: bool = False) -> SellMatrix:
-    """SELL-32 copy of a CSR matrix.  ``d16``: True = delta-coded columns of
-    the renumbered matrix, False = 4-byte columns, None = delta-coded when
-    the bridges add at most 25% entries (two host reads for the sizes).
-    ``blocks``: the dof block sizes of the space (``dof_blocks()``) for the
-    block-merge renumbering; without them the rows are ordered by their
-    smallest column.  ``triples``: node-triple copy for a vector space with
-    three interleaved components (rows a multiple of 3; ``d16`` ignored)."""
+               triples: bool = False, d15: bool = False) -> SellMatrix:
+    """SELL-32 copy of a CSR matrix.  ``d15``: 15-bit column steps with long
+    steps in the matrix's own numbering (columns must ascend in every row;
+    ``d16`` ignored).  ``d16``: True = delta-coded columns of the renumbered
+    matrix, False = 4-byte columns, None = delta-coded when the bridges add
+    at most 25% entries (two host reads for the sizes).  ``blocks``: the dof
+    block sizes of the space (``dof_blocks()``) for the block-merge
+    renumbering; without them the rows are ordered by their smallest column.
+    ``triples``: node-triple copy for a vector space with three interleaved
+    components (rows a multiple of 3; ``d16`` and ``d15`` ignored)."""
     dev = _dev(indptr)
     n = indptr.numel() - 1
     lib = _lib.lib()
     if triples:
         return _sell_build_b3(indptr, indices, values64, values32, want64, want32)
+    if d15:
+        return _sell_build_d15(indptr, indices, values64, values32, want64, want32)
     if d16 is None or d16:
         S = _sell_build_d16(indptr, indices, values64, values32, want64, want32, force=bool(d16), blocks=blocks)
         if S is not None:
@@ -413,6 +438,37 @@ def _sell_build_d16(indptr, indices, values64, values32, want64, want32, force=F
     call("fgb_sell_fill_d16", n, ptr(p_indptr), ptr(p_indices), ptr(p64), ptr(p32), ptr(perm), ptr(slice_ptr),
          ptr(col0), ptr(col16), ptr(v64), ptr(v32), s)
     return SellMatrix(n, n_slices, slice_ptr, perm, None, v64, v32, col16=col16, col0=col0, order=order, nnz=nnz)
+
+
+def _sell_build_d15(indptr, indices, values64, values32, want64, want32) -> SellMatrix:
+    """15-bit column copy in the matrix's own numbering."""
+    dev = _dev(indptr)
+    n = indptr.numel() - 1
+    nnz = indices.numel()
+    lib = _lib.lib()
+    s = stream_ptr(dev)
+    ws = workspace(max(lib.fgb_sell_d16_workspace_bytes(n), lib.fgb_sell_workspace_bytes(n)), dev)
+    st = status_word(dev)
+    e_indptr = torch.empty(n + 1, dtype=torch.int64, device=dev)
+    call("fgb_sell_d15_indptr", n, ptr(indptr), ptr(indices), ptr(e_indptr), ptr(st), ptr(ws), ws.numel(), s)
+    slots = int(lib.fgb_sell_slots(n))
+    n_slices = slots // 32
+    perm = torch.empty(slots, dtype=torch.int32, device=dev)
+    slice_ptr = torch.empty(n_slices + 1, dtype=torch.int64, device=dev)
+    call("fgb_sell_plan", n, ptr(e_indptr), ptr(perm), ptr(slice_ptr), ptr(ws), ws.numel(), s)
+    # one host read for the status of the length pass and the copy's size
+    code, total = (int(v) for v in torch.stack([st.to(torch.int64)[0], slice_ptr[n_slices]]).cpu())
+    if code:
+        raise _lib.FgbError("sell_build(d15): columns must ascend strictly in every row", code)
+    col0 = torch.empty(slots, dtype=torch.int32, device=dev)
+    col16 = torch.empty(max(total, 4), dtype=torch.int16, device=dev)
+    v64 = torch.empty(max(total, 1), dtype=torch.float64, device=dev) if want64 else None
+    v32 = torch.empty(max(total, 1), dtype=torch.float32, device=dev) if want32 else None
+    call("fgb_sell_fill_d15", n, ptr(indptr), ptr(indices), ptr(values64), ptr(values32), ptr(perm), ptr(slice_ptr),
+         ptr(col0), ptr(col16), ptr(v64), ptr(v32), s)
+    S = SellMatrix(n, n_slices, slice_ptr, perm, None, v64, v32, col16=col16, col0=col0, nnz=nnz, d15=True)
+    S.entry_indptr = e_indptr  # entries per row with the long steps (``stored_entries``)
+    return S
 
 
 def _sell_build_b3(indptr, indices, values64, values32, want64, want32) -> SellMatrix:

@@ -59,6 +59,11 @@ _LAUNCH_CACHE = {}
 # save), None = delta-coded columns of the renumbered matrix where the bridges
 # add at most 25% entries, True = delta-coded always
 SELL_D16: Optional[bool] = False
+# FP32 copies (cg_mixed) with 15-bit column steps in the matrix's own
+# numbering: 6 bytes per FP32 nonzero instead of 8, the gather locality of
+# FEALPy's numbering unchanged.  The FP64 solver's copy keeps 4-byte columns
+# (its SpMV is limited by the FP64 multiply-add rate, not by the bytes).
+SELL_D15 = True
 # cg_mixed with graph=True runs systems of at most this many rows and at most
 # this many nonzeros per row on average as one persistent cooperative kernel
 # (no launches per iteration); the others as the CUDA-graph loop of separate
@@ -82,18 +87,19 @@ def _sell_of(A: CSRTensor, want32: bool, tune: bool = True):
     launch shape from the autotuner cache."""
     S = getattr(A, "_sell", None)
     if S is None or (want32 and S.val32 is None) or (not want32 and S.val64 is None):
+        d15 = SELL_D15 and want32
         if A.values.dtype == torch.float32 and want32:
             # FP32-assembled operator: the FP32 values are the matrix (no FP64 copy)
             S = K.sell_build(A.crow, A.col, None, A.values.contiguous(), want64=False, want32=True, d16=SELL_D16,
-                             blocks=getattr(A, "dof_blocks", None), triples=_triples(A))
+                             blocks=getattr(A, "dof_blocks", None), triples=_triples(A), d15=d15)
         else:
             v32 = A._f32 if (want32 and A._f32 is not None) else None
             S = K.sell_build(A.crow, A.col, A.values.to(torch.float64).contiguous(), v32, want64=True, want32=want32,
-                             d16=SELL_D16, blocks=getattr(A, "dof_blocks", None), triples=_triples(A))
+                             d16=SELL_D16, blocks=getattr(A, "dof_blocks", None), triples=_triples(A), d15=d15)
         A._sell = S
         if tune:
             dt = torch.float32 if want32 else torch.float64
-            key = (S.n, S.padded_nnz, dt, S.d16, S.node_triples)
+            key = (S.n, S.padded_nnz, dt, S.cols)
             shape = _LAUNCH_CACHE.get(key)
             if shape is None:
                 times = K.sell_autotune(S, dt)

@@ -311,7 +311,8 @@ typedef struct fgb_sell {
   int32_t node_triples;     /* 1: every slot is a node triple: col = 3c, and  */
                             /* three values (columns 3c..3c+2) per slot       */
                             /* (fgb_sell_fill_b3); 0: one entry per slot      */
-  int32_t reserved;
+  int32_t col_long;         /* 1: col16 holds 15-bit steps and long steps     */
+                            /* (fgb_sell_fill_d15); 0: 16-bit steps           */
 } fgb_sell;
 
 /* No FEALPy counterpart: a solver-side layout of CSRTensor (the matrix the
@@ -360,6 +361,26 @@ int32_t fgb_sell_fill_d16(int64_t n, const int64_t* indptr, const int32_t* indic
                           const double* values64, const float* values32, const int32_t* perm,
                           const int64_t* slice_ptr, int32_t* col0, uint16_t* col16, double* val64,
                           float* val32, void* stream);
+
+/* The 15-bit column copy of a matrix in its own numbering (no renumbering;
+ * columns must ascend strictly in every row).  Per slot the first column
+ * (col0), per entry a 16-bit code: below 0x8000 a step from the previous
+ * column; 0x8000 | h a zero-valued long-step entry that gathers the previous
+ * column again and moves the running column on by h * 32768 (so any gap fits
+ * with one or two such entries).  6 bytes per FP32 entry instead of 8, and
+ * the solvers' vectors stay in the matrix's numbering.  The descriptor sets
+ * col16, col0 and col_long = 1 (col = NULL).  d15_indptr: entries per row
+ * with the long steps, scanned (a row whose columns do not ascend sets
+ * FGB_ERR_ARG in *status); fgb_sell_plan on it gives perm and slice_ptr, and
+ * fill_d15 writes col0, col16 and the values.  No FEALPy counterpart (storage
+ * of the solver's copy). */
+int32_t fgb_sell_d15_indptr(int64_t n, const int64_t* indptr, const int32_t* indices,
+                            int64_t* entry_indptr, int32_t* status, void* workspace,
+                            size_t workspace_bytes, void* stream);
+int32_t fgb_sell_fill_d15(int64_t n, const int64_t* indptr, const int32_t* indices,
+                          const double* values64, const float* values32, const int32_t* perm,
+                          const int64_t* slice_ptr, int32_t* col0, uint16_t* col16,
+                          double* val64, float* val32, void* stream);
 int32_t fgb_permute(int32_t dtype, int64_t n, const int32_t* order, const void* src, void* dst,
                     int32_t scatter, void* stream);
 

@@ -30,7 +30,7 @@ def test_binding_covers_header():
 
 def test_host_only_entry_points():
     lib = _lib.lib()
-    assert lib.fgb_abi_version() == 1
+    assert lib.fgb_abi_version() == 2
     assert lib.fgb_status_string(0) == b"ok"
     assert b"pattern" in lib.fgb_status_string(4)
     assert lib.fgb_pcg_workspace_bytes(1000) >= 5 * 8 * 1000

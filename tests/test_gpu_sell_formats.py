@@ -6,7 +6,10 @@ key groups above 64 rows take their fallbacks, and the solvers on the
 renumbered copy give the solution in the caller's numbering.  Node-triple
 copy (sell_build(triples=True), vector spaces with three interleaved
 components): SpMV against scipy, and the solvers against the copy with a
-column per entry."""
+column per entry.  15-bit copy (sell_build(d15=True), the matrix's own
+numbering): SpMV against scipy on FEALPy matrices and on gaps that need long
+steps, empty rows, an FP32-only copy, refusal of unsorted rows, and the
+FP32-refined solver against the 4-byte copy."""
 import os
 
 import numpy as np
@@ -228,3 +231,100 @@ def test_node_triple_solvers_match_entry_copy(golden_dir):
     assert abs(out[True][1] - out[False][1]) <= 1
     assert rel_err(out[True][0], out[False][0].cpu().numpy()) < 1e-9
     assert rel_err(out[True][2], out[False][2].cpu().numpy()) < 1e-7
+
+
+# ------------------------------------------------------------- 15-bit steps
+def _build_d15(A, dev, want64=True, want32=True):
+    from fealpy_gb300 import kernels as K
+    t = lambda a: torch.as_tensor(a, device=dev)
+    return K.sell_build(t(A.indptr.astype(np.int64)), t(A.indices.astype(np.int32)),
+                        t(A.data) if want64 else None, None if want64 else t(A.data.astype(np.float32)),
+                        want64=want64, want32=want32, d15=True)
+
+
+def _long_entries(A):
+    """Long-step entries the 15-bit copy needs: one per step above 32767 (the
+    steps here are below 2^30, which one long step covers)."""
+    row = np.repeat(np.arange(A.shape[0]), np.diff(A.indptr))
+    same = row[1:] == row[:-1]
+    st = np.diff(A.indices.astype(np.int64))[same]
+    assert st.max(initial=0) < (1 << 30)
+    return int(np.count_nonzero(st > 32767))
+
+
+def test_d15_golden_and_config_matrices_match_csr(golden_dir):
+    """15-bit copies (own numbering) of FEALPy matrices: P2/P3 triangles, P1
+    Poisson, and the P2 tetrahedral C2-law matrix whose vertex rows step from
+    the vertex block into the edge block (one long step per such row)."""
+    dev = cuda()
+    import scipy.sparse as sp
+    for name in ("small_tet_p2.npz", "small_tri_p3.npz", "c1_poisson_tri_p1_64.npz", "cfg_c2_tet_p2_8.npz"):
+        z = np.load(os.path.join(golden_dir, name))
+        n = len(z["crow"]) - 1
+        for pre in ("", "bc_"):
+            A = sp.csr_matrix((z[pre + "val"], z[pre + "col"], z[pre + "crow"]), shape=(n, n))
+            S = _build_d15(A, dev)
+            assert S.d15 and not S.d16 and S.order is None and S.cols == "d15"
+            assert S.stored_entries() == A.nnz + _long_entries(A)
+            S2 = _build_d15(A, dev)
+            assert torch.equal(S.col16, S2.col16) and torch.equal(S.val32, S2.val32)
+            _check_spmv(S, A, dev)
+
+
+def test_d15_long_steps_empty_rows_and_fp32_operator():
+    """Gaps of exactly 32767 and 32768, multiples of 32768, gaps of millions
+    (one long-step entry each), empty rows, and an FP32-only copy."""
+    dev = cuda()
+    import scipy.sparse as sp
+    n = 1_500_000
+    A = _spd(n, [32767, 32768, 3 * 32768, 1_234_567]).tocoo()
+    empty = np.array([5, 77, n - 3])  # empty rows (and columns), as the solvers may meet
+    keep = ~(np.isin(A.row, empty) | np.isin(A.col, empty))
+    A = sp.csr_matrix((A.data[keep], (A.row[keep], A.col[keep])), shape=(n, n))
+    A.sort_indices()
+    assert np.all(np.diff(A.indptr)[empty] == 0)
+    S = _build_d15(A, dev)
+    assert S.stored_entries() == A.nnz + _long_entries(A) and _long_entries(A) > 0
+    _check_spmv(S, A, dev)
+    from fealpy_gb300 import kernels as K
+    S32 = _build_d15(A, dev, want64=False)
+    assert S32.val64 is None and S32.val32 is not None
+    x = np.random.default_rng(6).normal(size=n)
+    y = K.sell_spmv(S32, torch.as_tensor(x, device=dev, dtype=torch.float32), torch.float32)
+    assert rel_err(y, A.astype(np.float32).astype(np.float64) @ x) < 1e-5
+    # a row whose columns do not ascend is refused
+    t = lambda a: torch.as_tensor(a, device=dev)
+    bad_ptr = t(np.array([0, 2, 3], dtype=np.int64))
+    bad_col = t(np.array([1, 0, 1], dtype=np.int32))
+    with pytest.raises(RuntimeError):
+        K.sell_build(bad_ptr, bad_col, t(np.ones(3)), None, want64=True, want32=True, d15=True)
+
+
+def test_d15_solvers_match_the_four_byte_copy(golden_dir):
+    """cg_mixed on the 15-bit copy (the default for FP32 copies) against the
+    same solve on the 4-byte copy: every row's product is the same sum in the
+    same order (a long-step entry adds an exact zero), but the rows sit in
+    other slots (their lengths differ), so the dot products add their terms
+    in another order: the same iterations within 2, solutions within 1e-9,
+    and the reference's solution."""
+    dev = cuda()
+    import fealpy_gb300 as F
+    from fealpy_gb300 import solver as SV
+    for name in ("c1_poisson_tri_p1_64.npz", "cfg_c2_tet_p2_8.npz"):
+        z = np.load(os.path.join(golden_dir, name))
+        out = {}
+        for d15 in (True, False):
+            A = F.CSRTensor(torch.as_tensor(z["bc_crow"], device=dev), torch.as_tensor(z["bc_col"], device=dev),
+                            torch.as_tensor(z["bc_val"], device=dev), (len(z["bc_crow"]) - 1,) * 2)
+            b = torch.as_tensor(z["bc_F" if "bc_F" in z else "F"], device=dev)
+            saved = SV.SELL_D15
+            SV.SELL_D15 = d15
+            try:
+                x, info = F.cg_mixed(A, b, rtol=1e-10, returninfo=True, graph=False)
+                assert A._sell.d15 == d15
+            finally:
+                SV.SELL_D15 = saved
+            assert info["relres"] <= 1e-10 and rel_err(x, z["uh"]) < 1e-8, (name, d15, info)
+            out[d15] = (x, info["niter"])
+        assert abs(out[True][1] - out[False][1]) <= 2, (name, out[True][1], out[False][1])
+        assert rel_err(out[True][0], out[False][0].cpu().numpy()) < 1e-9, name
