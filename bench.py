@@ -35,6 +35,9 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 METRIC = "DOF/s assemble+PCG to 1e-10 rel res, FP32-refined vs FP64 on GB300; serve p50/p99"
+# the C2 record's value: FP32 iterations with FP64 reliable updates on the
+# FP64-assembled operator (the 1e-10 residual is against that operator)
+HEADLINE = "mixed64"
 RTOL = 1e-10
 Q = 4
 CPU_SAMPLE_N = 24
@@ -173,6 +176,9 @@ def solve_step(torch, F, space, kappa, bc, mode, profile=False, marks=None, asm_
     bf.add_integrator(ScalarDiffusionIntegrator(coef=kappa, q=Q), ScalarMassIntegrator(coef=1.0, q=Q))
     # FP32-refined: FP32 cell-local assembly (factors from the FP64 Jacobian,
     # determinant and inverse of every cell), FP32 inner CG, FP64 refinement
+    # "mixed": FP32 cell-local assembly (the FP32 values are the operator);
+    # "mixed64": FP64 assembly, FP32 iterations on its rounded copy, FP64
+    # residuals with the FP64 values; "fp64": FP64 throughout
     A = bf.assembly(marks=asm_marks, dtype=torch.float32 if mode == "mixed" else torch.float64)
     mark()
     lf = LinearForm(space)
@@ -181,9 +187,9 @@ def solve_step(torch, F, space, kappa, bc, mode, profile=False, marks=None, asm_
     mark()
     A2, F2 = bc.apply(A, Fv)
     mark()
-    _sell_of(A2, want32=(mode == "mixed"))
+    _sell_of(A2, want32=(mode != "fp64"))
     mark()
-    if mode == "mixed":
+    if mode != "fp64":
         x, info = F.cg_mixed(A2, F2, rtol=RTOL, maxit=MAXIT, returninfo=True, profile=profile, graph=graph)
     else:
         M = F.JacobiPreconditioner().apply(A2)
@@ -280,7 +286,7 @@ def run_ours(args):
             solve_step(torch, F, space, kappa, bc, mode, graph=not args.no_graph)
         barrier()
         sampler = ClockSampler(getattr(torch.cuda.get_device_properties(dev), "uuid", None) and
-                               str(torch.cuda.get_device_properties(dev).uuid)) if mode == "mixed" else None
+                               str(torch.cuda.get_device_properties(dev).uuid)) if mode == HEADLINE else None
         if sampler:
             sampler.start()
             time.sleep(0.3)
@@ -326,9 +332,9 @@ def run_ours(args):
                          "sell_launch": list(A2._sell.launch) if getattr(A2, "_sell", None) is not None else None,
                          "sell_cols": A2._sell.cols if getattr(A2, "_sell", None) is not None else None,
                          "stored_entries": A2._sell.stored_entries() if getattr(A2, "_sell", None) is not None
-                         else A2.nnz}
+                         else A2.nnz, "A2": A2, "F2": F2}
 
-    if set(modes) != {"fp64", "mixed"} or args.no_e2e:
+    if not {"fp64", "mixed", HEADLINE} <= set(modes) or args.no_e2e:
         # profiling run: report the per-mode timings on stderr only
         for m, r in results.items():
             print(f"[profile run] {m}: {r['ms_per_step']:.3f} ms/step, {r['niter']} iterations, "
@@ -339,8 +345,16 @@ def run_ours(args):
             dist.destroy_process_group()
         return
     x64 = results["fp64"]["x"]
-    xm = results["mixed"]["x"]
-    err = float(torch.max(torch.abs(xm - x64)) / torch.max(torch.abs(x64)))
+    A64op, F64op = results["fp64"]["A2"], results["fp64"]["F2"]
+    # each FP32-refined solution against the FP64-assembled operator and the
+    # FP64 solution
+    for m in ("mixed", "mixed64"):
+        if m in results:
+            xm = results[m]["x"]
+            results[m]["err_vs_fp64"] = float(torch.max(torch.abs(xm - x64)) / torch.max(torch.abs(x64)))
+            results[m]["relres_vs_fp64_operator"] = float(torch.linalg.norm(F64op - A64op @ xm) /
+                                                         torch.linalg.norm(F64op))
+    err = results[HEADLINE]["err_vs_fp64"]
 
     # e2e: from pinned host arrays through the public API, solution back to host
     node_h = torch.as_tensor(node_np).pin_memory()
@@ -356,7 +370,7 @@ def run_ours(args):
         sp_ = F.LagrangeFESpace(m, p=2)
         from fealpy_gb300.fem import DirichletBC
         bc_ = DirichletBC(sp_, gd=0.0)
-        x, info, _, _ = solve_step(torch, F, sp_, kp, bc_, "mixed")
+        x, info, _, _ = solve_step(torch, F, sp_, kp, bc_, HEADLINE)
         x_h.copy_(x, non_blocking=True)
         torch.cuda.synchronize(dev)
 
@@ -376,7 +390,8 @@ def run_ours(args):
     d2h = gdof * 8
 
     peak, peak_kind = read_peaks()
-    mixed = results["mixed"]
+    mixed = results[HEADLINE]
+    m32 = results["mixed"]
     fp64 = results["fp64"]
     value = replica_value(gdof, world, mixed["ms_per_step"])
     roofline = spmv_roofline(mixed, gdof, n, peak, peak_kind)
@@ -385,10 +400,22 @@ def run_ours(args):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(CPU_SAMPLE_N, rounds=2)
 
-    # a short sample of the serving stream (the full sweep: --workload serving)
-    serving = None
-    if rank == 0 and world == 1 and not args.no_serving:
-        serving = serving_sample(torch, dev, args.serve_sample)
+    # the other configurations, one step each, on rank 0 of a single-GPU run:
+    # C5 elasticity 128^3, C3 batched meshes, C4 serving at two arrival rates
+    extras = {}
+    if rank == 0 and world == 1 and not args.no_extras:
+        ex_args = argparse.Namespace(**vars(args))
+        ex_args.steps, ex_args.warmup = 1, 1
+        jobs = [("elasticity", lambda: elasticity_record(ex_args)), ("batched", lambda: batched_record(ex_args))]
+        if not args.no_serving:
+            jobs.append(("serving", lambda: serving_record(ex_args, [100.0, 1000.0], args.serve_count)))
+        for key, fn in jobs:
+            t0 = time.perf_counter()
+            try:
+                extras[key] = fn()
+            except Exception as e:  # recorded, so that one configuration cannot void the record
+                extras[key] = {"error": f"{type(e).__name__}: {e}"}
+            extras[key]["wall_s"] = time.perf_counter() - t0
 
     if rank == 0:
         line = {
@@ -399,13 +426,26 @@ def run_ours(args):
             "config": {"workload": f"P2 diffusion+mass TetrahedronMesh box {n}^3 (C2)", "cells": int(cell_np.shape[0]),
                        "gdof": gdof, "nnz": mixed["nnz"], "quadrature": Q, "rtol": RTOL,
                        "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{world}"},
-            "fp32_refined": {"ms_per_step": mixed["ms_per_step"], "dof_per_s": value, "cg_iters": mixed["niter"],
-                             "reliable_updates": mixed["n_updates"], "true_relres": mixed["relres"],
-                             "max_rel_err_vs_fp64": err, "stages_ms": mixed["stages_ms"],
-                             "spmv_us": mixed["kernel_ms_avg"] * 1e3, "update_us": mixed["other_ms_avg"] * 1e3,
-                             "other_kernels_us": mixed["extra_ms_avg"] * 1e3,
-                             "sell_launch_threads_blocks": mixed["sell_launch"], "sell_columns": mixed["sell_cols"],
-                             "sell_stored_entries": mixed["stored_entries"]},
+            "headline": "fp32_refined_fp64_operator: FP64 cell-local assembly, FP32 inner CG on its FP32 copy, "
+                        "FP64 reliable updates with the FP64 values; the variant whose 1e-10 relative residual is "
+                        "against the FP64-assembled operator",
+            "fp32_refined_fp64_operator": {
+                "ms_per_step": mixed["ms_per_step"], "dof_per_s": value, "cg_iters": mixed["niter"],
+                "reliable_updates": mixed["n_updates"], "true_relres_vs_fp64_operator": mixed["relres"],
+                "max_rel_err_vs_fp64": mixed["err_vs_fp64"], "stages_ms": mixed["stages_ms"],
+                "spmv_us": mixed["kernel_ms_avg"] * 1e3, "update_us": mixed["other_ms_avg"] * 1e3,
+                "other_kernels_us": mixed["extra_ms_avg"] * 1e3, "sell_launch_threads_blocks": mixed["sell_launch"],
+                "sell_columns": mixed["sell_cols"], "sell_stored_entries": mixed["stored_entries"]},
+            "fp32_refined": {"operator": "FP32-assembled (FP32 cell-local assembly from the FP64 geometry)",
+                             "ms_per_step": m32["ms_per_step"], "dof_per_s": world * gdof / (m32["ms_per_step"] / 1e3),
+                             "cg_iters": m32["niter"], "reliable_updates": m32["n_updates"],
+                             "true_relres": m32["relres"], "true_relres_vs_fp64_operator": m32["relres_vs_fp64_operator"],
+                             "max_rel_err_vs_fp64": m32["err_vs_fp64"], "stages_ms": m32["stages_ms"],
+                             "spmv_us": m32["kernel_ms_avg"] * 1e3, "update_us": m32["other_ms_avg"] * 1e3,
+                             "other_kernels_us": m32["extra_ms_avg"] * 1e3,
+                             "sell_launch_threads_blocks": m32["sell_launch"], "sell_columns": m32["sell_cols"],
+                             "sell_stored_entries": m32["stored_entries"],
+                             "speedup_vs_fp64": fp64["ms_per_step"] / m32["ms_per_step"]},
             "fp64": {"ms_per_step": fp64["ms_per_step"], "dof_per_s": world * gdof / (fp64["ms_per_step"] / 1e3),
                      "cg_iters": fp64["niter"], "true_relres": fp64["relres"], "stages_ms": fp64["stages_ms"],
                      "spmv_us": fp64["kernel_ms_avg"] * 1e3, "update_us": fp64["other_ms_avg"] * 1e3,
@@ -418,8 +458,8 @@ def run_ours(args):
             "roofline": roofline,
             "clocks": mixed["clocks"],
             "cpu_baseline": cpu,
-            "serving": serving,
         }
+        line.update(extras)
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.barrier()
@@ -506,25 +546,93 @@ def cpu_baseline(n, rounds=2):
             "seconds_per_round": t}
 
 
+# the reference arm: at most this much host time on timed steps (a full
+# assemble + Dirichlet + PCG solve of the 64^3 system per step)
+REF_TIME_BUDGET_S = 150.0
+
+
+def _mem_available_gb():
+    try:
+        with open("/proc/meminfo") as fh:
+            for ln in fh:
+                if ln.startswith("MemAvailable:"):
+                    return int(ln.split()[1]) / 1e6
+    except Exception:
+        pass
+    return None
+
+
 def run_reference(args):
+    """The reference algorithm (the oracle port of FEALPy's numpy path) on the
+    same configuration as our arm: P2 diffusion + mass on the n^3 tet box,
+    full assembly + right-hand side + Dirichlet + Jacobi-PCG to 1e-10 per
+    step, split over the host's cores (processes over row ranges, threads
+    over row blocks in the CG products; results bit-identical to the
+    sequential oracle).  One untimed warm-up step (worker set-up: mesh,
+    topology, dof numbering, as excluded from our arm's value), then as many
+    timed steps as fit in REF_TIME_BUDGET_S, at least one."""
+    import multiprocessing
+    import resource
+    from oracle import parallel_port as PP
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    n = CPU_SAMPLE_N
-    procs, gdof, times, niter = host_replica_rounds(n, args.steps, args.warmup)
+    n = args.n
+    cores = PP.host_cores()
+    avail = _mem_available_gb()
+    # about 3 GB per worker at 64^3 (set-up + one row range), scaled by size
+    per_worker = 3.0 * (n / 64.0) ** 3
+    procs = cores if avail is None else max(1, min(cores, int((avail - 20.0 * (n / 64.0) ** 3) / per_worker)))
+    saved = {k: os.environ.get(k) for k in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS")}
+    for k in saved:
+        os.environ[k] = "1"
+    ctx = multiprocessing.get_context("spawn")
+    gdof = (2 * n + 1) ** 3
+    times, stages, niter = [], [], 0
+    try:
+        with ctx.Pool(procs) as pool:
+            t_w = time.perf_counter()
+            PP.assemble(pool, "c2", n, gdof, 4 * procs)  # warm-up: builds the set-up in every worker
+            warm_s = time.perf_counter() - t_w
+            want = max(1, args.steps)
+            while len(times) < want:
+                t0 = time.perf_counter()
+                out = PP.assemble(pool, "c2", n, gdof, 4 * procs)
+                t1 = time.perf_counter()
+                A = PP.BlockOperator(out["blocks"], out["bounds"], cores)
+                try:
+                    x, info = PP.jacobi_cg(A, out["b"], atol=1e-30, rtol=RTOL)
+                finally:
+                    A.close()
+                t2 = time.perf_counter()
+                times.append(t2 - t0)
+                niter = info["niter"]
+                stages.append({"assembly_rhs_dirichlet_s": t1 - t0, "pcg_s": t2 - t1,
+                               "worker_setup_in_step_s": out["setup_s"]})
+                if sum(times) + times[-1] > REF_TIME_BUDGET_S:
+                    break
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+    rss = max(resource.getrusage(resource.RUSAGE_SELF).ru_maxrss, resource.getrusage(resource.RUSAGE_CHILDREN).ru_maxrss)
     tot = sum(times)
-    value = procs * gdof * len(times) / tot
-    line = {"metric": METRIC, "value": value, "unit": "DOF/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": tot / len(times) * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded jittered tet box)",
-            "impl": "reference",
-            "config": {"workload": f"P2 diffusion+mass TetrahedronMesh box (C2 family), bounded host sample {n}^3",
-                       "gdof": gdof, "quadrature": Q, "rtol": RTOL},
-            "cpu_baseline": {"value": value, "unit": "DOF/s", "cores": procs, "kind": "port",
-                             "sample": f"per step {procs} concurrent single-threaded replicas (spawned processes, one "
-                                       f"BLAS thread each) of the {n}^3 P2 tet box ({gdof} dofs, {niter} PCG "
-                                       f"iterations): whole-host throughput of the reference numpy path"},
+    value = gdof * len(times) / tot
+    sample = (f"full C2 step at {n}^3 ({gdof} dofs): assembly + right-hand side + Dirichlet + Jacobi-PCG to "
+              f"{RTOL:g} ({niter} iterations) per step; {procs} processes over row ranges, {cores} threads in "
+              f"the CG products; {len(times)} timed step(s) after 1 untimed warm-up ({warm_s:.1f} s, includes "
+              f"the workers' mesh/topology/dof set-up)")
+    line = {"metric": METRIC, "value": value, "unit": "DOF/s", "n_gpus": world, "steps": len(times),
+            "warmup": 1, "requested_steps": args.steps, "requested_warmup": args.warmup,
+            "ms_per_step": tot / len(times) * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded jittered tet box, lognormal coefficients)", "impl": "reference",
+            "config": {"workload": f"P2 diffusion+mass TetrahedronMesh box {n}^3 (C2)", "gdof": gdof, "quadrature": Q,
+                       "rtol": RTOL, "same_config": True},
+            "stages": stages, "peak_rss_gb": rss / 1e6, "host_cores": cores, "mem_available_gb": avail,
+            "cpu_baseline": {"value": value, "unit": "DOF/s", "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "DOF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -600,6 +708,10 @@ def cpu_sample_batched(meshes, budget_s=15.0, max_dofs=80000):
 
 
 def run_batched(args):
+    print(json.dumps(batched_record(args)), flush=True)
+
+
+def batched_record(args):
     import torch
     import fealpy_gb300 as F
     from fealpy_gb300.workloads import batched_tri_meshes
@@ -673,13 +785,17 @@ def run_batched(args):
             "max_true_relres": max(rel), "iters_max": max(iters), "iters_mean": sum(iters) / len(iters),
             "max_rel_err_vs_fp64_sample": max(err), "gpu_launches": (_lib.launch_count() - l0) // args.steps,
             "cpu_baseline": None if args.no_cpu_baseline else cpu_sample_batched(meshes)}
-    print(json.dumps(line), flush=True)
+    return line
 
 
 # ---------------------------------------------------------------------------
 # serving workload: Poisson arrivals, continuous batching under a memory budget
 # ---------------------------------------------------------------------------
 def run_elasticity(args):
+    print(json.dumps(elasticity_record(args)), flush=True)
+
+
+def elasticity_record(args):
     """P1 vector linear elasticity on an n^3 tetrahedral box (default 128^3:
     12,582,912 cells, 6,440,067 dofs): lambda = 1, mu = 0.5 scaled per cell by
     exp(N(0, 0.5)), clamped at x = 0, body force (0, 0, -1), q = 4, rtol 1e-8;
@@ -733,10 +849,31 @@ def run_elasticity(args):
         res[mode] = {"ms_per_step": ms, "dof_per_s": gdof / (ms / 1e3), "cg_iters": info["niter"],
                      "true_relres": float(torch.linalg.norm(r) / torch.linalg.norm(F2)),
                      "fp64_iterations": info.get("fp64_iterations", info["niter"] if mode == "fp64" else 0),
-                     "x": x, "nnz": A2.nnz,
-                     "sell": "node triples" if A2._sell.node_triples else ("16-bit steps" if A2._sell.d16 else
-                                                                         "4-byte columns")}
+                     "x": x, "nnz": A2.nnz, "A2": A2, "F2": F2,
+                     "sell": A2._sell.cols}
     err = float((res["mixed"]["x"] - res["fp64"]["x"]).abs().max() / res["fp64"]["x"].abs().max())
+    # roofline of the dominant kernel, the FP32 SpMV of the FP32-refined
+    # iterations, from one more (host-polled) solve with CUDA events around
+    # every SpMV.  Algorithmic bytes: node-triple copy T (4 + 3 s) + n (8 + 2 s)
+    # (a column and three values per triple slot, T = stored triples; a slot
+    # map entry and a slice pointer share per row, x read once, y written
+    # once); 4-byte columns: nnz (4 + s) + n (8 + 2 s)
+    A2 = res["mixed"].pop("A2")
+    F2 = res["mixed"].pop("F2")
+    res["fp64"].pop("A2", None)
+    res["fp64"].pop("F2", None)
+    _, pinfo = F.cg_mixed(A2, F2, rtol=rtol, maxit=200000, returninfo=True, profile=True)
+    S = A2._sell
+    peak, peak_kind = read_peaks()
+    if S.node_triples:
+        b = S.stored_entries() * (4 + 3 * 4) + gdof * (8 + 8)
+    else:
+        b = S.stored_entries() * (4 + 2 if S.d15 else 4 + 4) + gdof * (8 + 8)
+    avg = pinfo["kernel_ms"] / max(pinfo["kernel_launches"], 1)
+    ach = b / (avg / 1e3) / 1e9 if avg > 0 else 0.0
+    roof = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak, "traffic": None,
+            "kernel": f"sell_pcg_spmv<float> ({S.cols}; Ap = A p and p.Ap)", "algorithmic_bytes_per_launch": b,
+            "avg_launch_ms": avg, "peak_source": peak_kind}
     for m in res:
         res[m].pop("x")
     line = {"metric": "DOF/s assemble+PCG to 1e-8 rel res, P1 vector elasticity (C5)",
@@ -747,26 +884,9 @@ def run_elasticity(args):
             "config": {"workload": f"LinearElasticityIntegrator P1 TetrahedronMesh box {n}^3 (C5)",
                        "cells": int(cell_np.shape[0]), "gdof": gdof, "rtol": rtol, "quadrature": 4},
             "fp32_refined": res["mixed"], "fp64": res["fp64"], "max_rel_err_vs_fp64": err,
-            "speedup_fp32_refined_vs_fp64": res["fp64"]["ms_per_step"] / res["mixed"]["ms_per_step"]}
-    print(json.dumps(line), flush=True)
-
-
-def serving_sample(torch, dev, count, rate=200.0):
-    """p50/p99 latency and throughput of a short request stream, FP32-refined
-    and plain FP64 (continuous batching, 150 GB budget, 256 slots)."""
-    from fealpy_gb300.serving import SolveServer, poisson_request_problem
-    from fealpy_gb300.workloads import serving_requests
-    reqs = serving_requests(count, rate=rate, seed=3)
-    out = {"requests": count, "arrival_rate_rps": rate, "workload": "C4 stream (70% tri P1/P2, 30% tet P1, "
-                                                                    "1e3-2e6 dofs)"}
-    SolveServer(max_slots=8, device=dev).run(serving_requests(4, rate=1e6, seed=99, dof_range=(1e3, 1e4)))
-    for prec in ("mixed", "fp64"):
-        srv = SolveServer(hbm_budget=150e9, max_slots=256, chunk=64, fp64=(prec == "fp64"), device=dev)
-        r = srv.run(reqs, poisson_request_problem)
-        out[prec] = {"p50_ms": r["p50_s"] * 1e3, "p99_ms": r["p99_s"] * 1e3, "throughput_rps": r["throughput_rps"],
-                     "dofs_per_s": r["dofs_per_s"], "max_relres": r["max_relres"],
-                     "fp64_continuations": r["fp64_continuations"]}
-    return out
+            "speedup_fp32_refined_vs_fp64": res["fp64"]["ms_per_step"] / res["mixed"]["ms_per_step"],
+            "roofline": roof}
+    return line
 
 
 def cpu_sample_serving(reqs, budget_s=15.0, max_dofs=60000):
@@ -799,6 +919,11 @@ def cpu_sample_serving(reqs, budget_s=15.0, max_dofs=60000):
 
 
 def run_serving(args):
+    print(json.dumps(serving_record(args, [float(r) for r in args.serve_rates.split(",")], args.serve_count)),
+          flush=True)
+
+
+def serving_record(args, rates, count):
     import torch
     from fealpy_gb300.serving import SolveServer, poisson_request_problem
     from fealpy_gb300.workloads import serving_requests
@@ -808,8 +933,8 @@ def run_serving(args):
     warm = serving_requests(8, rate=1e6, seed=99, dof_range=(1e3, 2e4))
     SolveServer(max_slots=8, device=dev).run(warm)
     rows = []
-    for rate in [float(r) for r in args.serve_rates.split(",")]:
-        reqs = serving_requests(args.serve_count, rate=rate, seed=3)
+    for rate in rates:
+        reqs = serving_requests(count, rate=rate, seed=3)
         for prec in ("mixed", "fp64"):
             torch.cuda.synchronize()
             srv = SolveServer(hbm_budget=150e9, max_slots=256, chunk=args.serve_chunk, fp64=(prec == "fp64"),
@@ -827,12 +952,12 @@ def run_serving(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64 / f64",
             "data": "synthetic request stream (seeded Poisson arrivals, jittered meshes, lognormal coefficients)",
             "config": {"workload": "70% tri P1/P2, 30% tet P1, 1e3-2e6 dofs log-uniform (C4)",
-                       "requests_per_rate": args.serve_count, "hbm_budget_gb": 150, "slots": 256,
+                       "requests_per_rate": count, "hbm_budget_gb": 150, "slots": 256,
                        "chunk_iterations": args.serve_chunk},
             "sweep": rows,
             "cpu_baseline": None if args.no_cpu_baseline else cpu_sample_serving(
-                serving_requests(args.serve_count, rate=50.0, seed=3))}
-    print(json.dumps(line), flush=True)
+                serving_requests(count, rate=50.0, seed=3))}
+    return line
 
 
 def main():
@@ -843,7 +968,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=64)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--modes", default="fp64,mixed",
+    ap.add_argument("--modes", default="fp64,mixed,mixed64",
                     help="solver modes to time (a single-mode run is for profiling and prints no JSON line)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--no-graph", action="store_true",
@@ -861,8 +986,9 @@ def main():
     ap.add_argument("--serve-count", type=int, default=200, help="requests per arrival rate")
     ap.add_argument("--serve-rates", default="50,200,1000")
     ap.add_argument("--serve-chunk", type=int, default=64)
-    ap.add_argument("--serve-sample", type=int, default=32, help="requests of the serving sample in the default run")
-    ap.add_argument("--no-serving", action="store_true", help="skip the serving sample of the default run")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving sweep of the default run")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the C5, C3 and C4 records of the default run (only the C2 line)")
     ap.add_argument("--sell-cols", choices=["auto", "i32", "d16", "d15"], default="d15",
                     help="column format of the FP32-refined solver's SELL copy: d15 = 15-bit steps in FEALPy's "
                          "numbering (default), i32 = 4-byte columns, d16 = 16-bit steps of a renumbered matrix, "

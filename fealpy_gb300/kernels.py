@@ -258,8 +258,9 @@ class SellMatrix:
         return self._d15
 
     def stored_entries(self) -> int:
-        """Entries of the copy without padding: the nonzeros, plus the
-        long-step entries of a 15-bit copy (one host read)."""
+        """Slots of the copy without padding: the nonzeros, plus the long-step
+        entries of a 15-bit copy; triple slots of a node-triple copy (one
+        host read)."""
         ep = getattr(self, "entry_indptr", None)
         return int(ep[-1].item()) if ep is not None else int(self.nnz or 0)
 
@@ -493,7 +494,9 @@ def _sell_build_b3(indptr, indices, values64, values32, want64, want32) -> SellM
     v32 = torch.empty(3 * max(total, 4), dtype=torch.float32, device=dev) if want32 else None
     call("fgb_sell_fill_b3", n, ptr(indptr), ptr(indices), ptr(values64), ptr(values32), ptr(perm), ptr(slice_ptr),
          ptr(col), ptr(v64), ptr(v32), s)
-    return SellMatrix(n, n_slices, slice_ptr, perm, col, v64, v32, nnz=indices.numel(), node_triples=True)
+    S = SellMatrix(n, n_slices, slice_ptr, perm, col, v64, v32, nnz=indices.numel(), node_triples=True)
+    S.entry_indptr = t_indptr  # triples per row (``stored_entries`` counts triple slots)
+    return S
 
 
 def sell_spmv(S: SellMatrix, x, dtype=torch.float64):
