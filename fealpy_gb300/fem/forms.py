@@ -70,6 +70,7 @@ class _Form:
                 I.set_region(region)
         else:
             I = GroupIntegrator(*I, region=region)
+        self._mf_cache = None  # matrix-free data belongs to the former integrators
         group = f"_group_{self._cursor}" if group is None else group
         self._cursor += 1
         if group in self.integrators:
@@ -176,12 +177,52 @@ class BilinearForm(_Form):
         return M
 
     def __matmul__(self, u):
-        if self._M is None:
-            self.assembly()
-        return self._M @ u
+        """``A @ u``; without an assembled matrix the product is formed matrix
+        free, as FEALPy does (``fealpy/fem/bilinear_form.py:126-158``): a
+        kernel forms every cell's K_c u_c from the cell factors and the
+        tables, and the dof adjacency adds them per dof in cell order.  No
+        global matrix is built (``_M`` stays None).  ``u`` may carry a batch
+        on the first dimension."""
+        if self._M is not None:
+            return self._M @ u
+        if not isinstance(u, torch.Tensor):
+            raise TypeError("u must be a torch tensor")
+        if u.ndim >= 2:
+            return torch.stack([self._matfree(v) for v in u.reshape(-1, u.shape[-1])]).reshape(
+                u.shape[:-1] + (self.shape[0],))
+        return self._matfree(u)
+
+    def _matfree(self, u):
+        plan = self._plan()
+        if not isinstance(plan, ScalarPlan):
+            raise NotImplementedError("matrix-free products are provided for scalar integrators")
+        space = self.space
+        dtype = u.dtype if u.dtype in (torch.float32, torch.float64) else torch.float64
+        key = ("matfree", dtype)
+        cache = getattr(self, "_mf_cache", None)
+        if cache is None or cache[0] != key:
+            status = _lib.status_word(space.device)
+            fac = K.cell_factors(space.mesh, plan.channels, plan.coef_matrix(), dtype, status)
+            _lib.check_status_word("matrix-free factors", status)
+            n = space.number_of_global_dofs()
+            akey = ("adjacency", n)
+            if akey not in space._cache:
+                st = _lib.status_word(space.device)
+                adj_ptr, adj, _ = K.build_adjacency(space.cell_to_dof(), n, st)
+                _lib.check_status_word("adjacency", st)
+                space._cache[akey] = (adj_ptr, adj)
+            cache = (key, fac, plan.tables, space._cache[akey])
+            self._mf_cache = cache
+        _, fac, tables, (adj_ptr, adj) = cache
+        yc = K.cell_apply(space.cell_to_dof(), tables, fac, u.to(device=space.device, dtype=dtype))
+        return K.gather_sum(adj_ptr, adj, yc)
 
     def mult(self, x, out=None):
-        return self @ x
+        y = self @ x
+        if out is not None:
+            out.copy_(y)
+            return out
+        return y
 
 
 class LinearForm(_Form):

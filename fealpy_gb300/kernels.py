@@ -223,6 +223,25 @@ def gather_sum(adj_ptr, adj, local: torch.Tensor, out: Optional[torch.Tensor] = 
     return y
 
 
+def cell_apply(c2d, tables: "np.ndarray", factors: torch.Tensor, x: torch.Tensor) -> torch.Tensor:
+    """(NC, ldof) cell products K_c x_c (``fgb_cell_apply``) in the factors'
+    dtype; ``tables`` is the (nt, ldof, ldof) FP64 table array on the host."""
+    import numpy as np
+    dev = _dev(c2d)
+    NC, ldof = c2d.shape
+    nt = factors.shape[1]
+    dt = factors.dtype
+    tab_host = np.ascontiguousarray(tables, dtype=np.float64)
+    if tab_host.shape != (nt, ldof, ldof):
+        raise ValueError(f"tables must be ({nt}, {ldof}, {ldof})")
+    tab_dev = None if ldof in (3, 4, 6, 10) else torch.as_tensor(tab_host, dtype=dt, device=dev)
+    y = torch.empty((NC, ldof), dtype=dt, device=dev)
+    call("fgb_cell_apply", dtype_code(dt), NC, ldof, ptr(c2d.contiguous()), nt,
+         tab_host.ctypes.data_as(ctypes.c_void_p), ptr(tab_dev), ptr(factors.contiguous()),
+         ptr(x.to(dt).contiguous()), ptr(y), stream_ptr(dev))
+    return y
+
+
 class SellMatrix:
     """Device SELL-32 copy of a CSR matrix (tensors kept alive here) and the
     ``fgb_sell`` descriptor pointing at them.

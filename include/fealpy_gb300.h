@@ -201,6 +201,19 @@ int32_t fgb_assemble_elasticity_p1(int32_t dtype, int32_t gd, int64_t n_node,
 int32_t fgb_gather_sum(int32_t dtype, int64_t n, const int64_t* adj_ptr, const int32_t* adj,
                        const void* local, void* out, void* stream);
 
+/* Matrix-free y_cell = K_c x_c for every cell, K_c = sum_t factors[c][t] *
+ * tables[t] (the factorisation of fgb_assemble_scalar), the cell-local half
+ * of BilinearForm.__matmul__ without a global matrix
+ * (fealpy/fem/bilinear_form.py:126-158: gather u at the cell dofs, einsum with
+ * the cell-local matrices); fgb_gather_sum over the dof adjacency then adds
+ * the cells' results per dof (the index_add, deterministic).  ycell:
+ * (n_cell, ldof) in the factor dtype.  tables_host (n_table*ldof*ldof FP64,
+ * host memory) is used for ldof in {3, 4, 6, 10} (the tables go into the
+ * kernel's parameter space); otherwise `tables` (device, the factor dtype). */
+int32_t fgb_cell_apply(int32_t dtype, int64_t n_cell, int32_t ldof, const int32_t* cell2dof,
+                       int32_t n_table, const double* tables_host, const void* tables,
+                       const void* factors, const void* x, void* ycell, void* stream);
+
 /* ---- Dirichlet boundary conditions ------------------------------------- */
 
 /* DirichletBC.apply (fealpy/fem/dirichlet_bc.py:101-229): given is_bd (uint8,
