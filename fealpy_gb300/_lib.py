@@ -74,6 +74,13 @@ _SIGNATURES = {
                                            c_vp, c_vp, c_vp, c_sz, c_vp]),
     "fgb_dirichlet_count": (c_i32, [c_i32, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "fgb_dirichlet_fill": (c_i32, [c_i32, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "fgb_topology_workspace_bytes": (c_sz, [c_i64, c_i64]),
+    "fgb_topology_count": (c_i32, [c_i64, c_i32, c_vp, c_i64, c_i32, c_i32, c_vp, ctypes.POINTER(c_i64), c_vp, c_vp,
+                                   c_sz, c_vp]),
+    "fgb_topology_fill": (c_i32, [c_i64, c_i32, c_vp, c_i64, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_sz,
+                                  c_vp]),
+    "fgb_cell_to_ipoint": (c_i32, [c_i64, c_i32, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_i64, c_i64, c_vp, c_vp, c_vp,
+                                   c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "fgb_cell_apply": (c_i32, [c_i32, c_i64, c_i32, c_vp, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "fgb_csr_spmv": (c_i32, [c_i32, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_i32, c_vp]),
     "fgb_csr_diagonal": (c_i32, [c_i32, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
@@ -192,7 +199,8 @@ KERNELS_PER_CALL = {
     "fgb_cell_factors": 1, "fgb_adjacency_build": 6, "fgb_pattern_count": 5, "fgb_pattern_fill": 2, "fgb_pattern_build": 5, "fgb_pattern_compact": 2,
     "fgb_pattern_expand_blocks": 2, "fgb_assemble_scalar": 2, "fgb_assemble_elasticity_p1": 2,
     "fgb_dirichlet_count": 1, "fgb_exclusive_scan_i32": 3, "fgb_dirichlet_fill": 1, "fgb_csr_spmv": 1,
-    "fgb_csr_diagonal": 1, "fgb_gather_sum": 1, "fgb_cell_apply": 1, "fgb_sell_plan": 4, "fgb_sell_fill": 1, "fgb_sell_spmv": 1,
+    "fgb_csr_diagonal": 1, "fgb_gather_sum": 1, "fgb_cell_apply": 1,
+    "fgb_topology_count": 8, "fgb_topology_fill": 2, "fgb_cell_to_ipoint": 1, "fgb_sell_plan": 4, "fgb_sell_fill": 1, "fgb_sell_spmv": 1,
     "fgb_sell_renumber": 1, "fgb_csr_permute": 5, "fgb_sell_d16_indptr": 4, "fgb_sell_fill_d16": 1,
     "fgb_sell_d15_indptr": 4, "fgb_sell_fill_d15": 1, "fgb_permute": 1,
     "fgb_sell_b3_indptr": 4, "fgb_sell_fill_b3": 1,

@@ -223,6 +223,73 @@ def gather_sum(adj_ptr, adj, local: torch.Tensor, out: Optional[torch.Tensor] = 
     return y
 
 
+def mesh_entities(cell: torch.Tensor, n_node: int, local, want_entity2cell: bool):
+    """(entity (NE, k), entity2cell (NE, 4) or None, cell2entity (NC, nfc)),
+    int32, of the local entities ``local`` (nfc x k vertex indices) of every
+    cell (``fgb_topology_count`` + ``fgb_topology_fill``)."""
+    import numpy as np
+    dev = _dev(cell)
+    cell = cell.to(torch.int32).contiguous()
+    NC, nv = cell.shape
+    loc = np.ascontiguousarray(local, dtype=np.int32)
+    nfc, k = loc.shape
+    lib = _lib.lib()
+    ws = workspace(lib.fgb_topology_workspace_bytes(n_node, NC * nfc), dev)
+    st = status_word(dev)
+    lp = loc.ctypes.data_as(ctypes.c_void_p)
+    ne = ctypes.c_int64(0)
+    s = stream_ptr(dev)
+    call("fgb_topology_count", NC, nv, ptr(cell), int(n_node), k, nfc, lp, ctypes.byref(ne), ptr(st), ptr(ws),
+         ws.numel(), s)
+    check_status_word("mesh topology (cell vertex indices)", st)
+    NE = int(ne.value)
+    entity = torch.empty((NE, k), dtype=torch.int32, device=dev)
+    e2c = torch.empty((NE, 4), dtype=torch.int32, device=dev) if want_entity2cell else None
+    c2e = torch.empty((NC, nfc), dtype=torch.int32, device=dev)
+    call("fgb_topology_fill", NC, nv, ptr(cell), int(n_node), k, nfc, lp, ptr(entity), ptr(e2c), ptr(c2e), ptr(st),
+         ptr(ws), ws.numel(), s)
+    check_status_word("mesh topology", st)
+    return entity, e2c, c2e
+
+
+def cell_to_ipoint(mesh, p: int) -> torch.Tensor:
+    """(NC, ldof) int32 interpolation-point numbering of a mesh on the device
+    (``fgb_cell_to_ipoint``): the per-point table is built here from the
+    multi-index matrix, the numbering by one thread per (cell, point)."""
+    import numpy as np
+    from . import simplex as sx
+    TD = mesh.TD
+    mi = sx.multi_index_matrix(p, TD)
+    ldof = mi.shape[0]
+    local_edge = [(1, 2), (2, 0), (0, 1)] if TD == 2 else list(mesh.localEdge)
+    edge_id = {tuple(sorted(e)): q for q, e in enumerate(local_edge)}
+    tab = {name: np.zeros(ldof, dtype=np.int32) for name in ("kind", "a", "b", "le", "ma", "mb", "rank")}
+    interior = 0
+    for q in range(ldof):
+        support = np.nonzero(mi[q] > 0)[0]
+        if len(support) == 1:
+            tab["kind"][q], tab["a"][q] = 0, support[0]
+        elif len(support) == 2:
+            a, b = int(support[0]), int(support[1])
+            tab["kind"][q], tab["a"][q], tab["b"][q] = 1, a, b
+            tab["le"][q], tab["ma"][q], tab["mb"][q] = edge_id[(a, b)], mi[q, a], mi[q, b]
+        elif TD == 2:
+            tab["kind"][q], tab["rank"][q] = 2, interior
+            interior += 1
+        else:
+            # P3 tetrahedron: the point of the face opposite the vertex whose entry is 0
+            tab["kind"][q], tab["le"][q] = 3, int(np.nonzero(mi[q] == 0)[0][0])
+    dev = _dev(mesh.cell)
+    NC = mesh.number_of_cells()
+    out = torch.empty((NC, ldof), dtype=torch.int32, device=dev)
+    hp = [tab[k].ctypes.data_as(ctypes.c_void_p) for k in ("kind", "a", "b", "le", "ma", "mb", "rank")]
+    c2f = mesh.cell2face if TD == 3 else None
+    call("fgb_cell_to_ipoint", NC, TD, p, ldof, ptr(mesh.cell), ptr(mesh.cell2edge.contiguous()),
+         ptr(mesh.edge.contiguous()), ptr(c2f.contiguous() if c2f is not None else None), mesh.number_of_nodes(),
+         mesh.number_of_edges(), *hp, ptr(out), stream_ptr(dev))
+    return out
+
+
 def cell_apply(c2d, tables: "np.ndarray", factors: torch.Tensor, x: torch.Tensor) -> torch.Tensor:
     """(NC, ldof) cell products K_c x_c (``fgb_cell_apply``) in the factors'
     dtype; ``tables`` is the (nt, ldof, ldof) FP64 table array on the host."""

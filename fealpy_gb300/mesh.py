@@ -10,8 +10,11 @@ first local index, last local index]``.  Interpolation-point (dof) numbering
 follows ``cell_to_ipoint`` (``fealpy/mesh/triangle_mesh.py:218-270``,
 ``fealpy/mesh/tetrahedron_mesh.py:388-441``): vertices, then ``p-1`` points per
 edge ordered from ``edge[:,0]`` to ``edge[:,1]``, then face and cell interior
-points.  Mesh set-up (generation, topology, numbering) is not part of the
-timed assemble/solve path.
+points.  On a CUDA device the topology and the numbering are built by the
+library's kernels (``fgb_topology_*``, ``fgb_cell_to_ipoint``); meshes held in
+host memory use the same construction written with torch sorts (host-side
+checks).  Mesh set-up is not part of the timed assemble/solve path; the
+end-to-end bench leg includes it.
 """
 
 import numpy as np
@@ -85,6 +88,23 @@ class _SimplexMesh:
 
     # -- topology ---------------------------------------------------------
     def construct(self):
+        if self.device.type == "cuda":
+            # device kernels (fgb_topology_*): per-vertex grouping of the
+            # local entities, ranked sorted tuples, first/last occurrences
+            from .kernels import mesh_entities
+            NN = self.number_of_nodes()
+            self.face, self.face2cell, self.cell2face = mesh_entities(
+                self.cell, NN, np.asarray(self.localFace, dtype=np.int32), True)
+            if self.TD == 3:
+                self.edge, _, self.cell2edge = mesh_entities(self.cell, NN, np.asarray(self.localEdge,
+                                                                                      dtype=np.int32), False)
+            else:
+                self.edge = self.face
+                self.cell2edge = self.cell2face
+                self.edge2cell = self.face2cell
+            return
+        # meshes held in host memory (host-side checks): the same construction
+        # with torch sorts
         NC = self.cell.shape[0]
         lf = torch.tensor(self.localFace, dtype=torch.int64, device=self.device)
         total_face = self.cell[:, lf].reshape(-1, lf.shape[1])
@@ -238,6 +258,9 @@ class _SimplexMesh:
         TD = self.TD
         if TD == 3 and p > 3:
             raise NotImplementedError("tetrahedron dofs are provided up to p = 3")
+        if self.device.type == "cuda":
+            from .kernels import cell_to_ipoint
+            return cell_to_ipoint(self, p)[index]
         mi = sx.multi_index_matrix(p, TD)
         NC = self.number_of_cells()
         NN = self.number_of_nodes()

@@ -97,6 +97,43 @@ size_t fgb_scan_workspace_bytes(int64_t n);
 int32_t fgb_exclusive_scan_i32(const int32_t* in, int64_t n, int64_t* out, void* workspace,
                                size_t workspace_bytes, void* stream);
 
+/* ---- mesh topology and dof numbering ------------------------------------ */
+
+/* Unique sub-entities (edges, or faces) of a simplex mesh as MeshDS.construct
+ * builds them (fealpy/mesh/mesh_data_structure.py:428-464, flocc in
+ * fealpy/mesh/utils.py:81-110): the distinct sorted vertex tuples of the
+ * cells' local entities local_host (nfc x k, host memory), numbered in
+ * lexicographic order, each stored in the orientation of its first
+ * occurrence (cell order, then local index); entity2cell (optional, ne x 4)
+ * = [first cell, last cell, first local index, last local index];
+ * cell2entity (n_cell x nfc).  count groups the occurrences by smallest
+ * vertex, ranks the distinct tuples and writes their number to
+ * *n_entity_host (it synchronises the stream); fill then writes the arrays,
+ * with the same workspace (fgb_topology_workspace_bytes(n_node,
+ * n_cell * nfc)), which carries the grouping from count to fill. */
+size_t fgb_topology_workspace_bytes(int64_t n_node, int64_t n_occ);
+int32_t fgb_topology_count(int64_t n_cell, int32_t nv, const int32_t* cell, int64_t n_node, int32_t k,
+                           int32_t nfc, const int32_t* local_host, int64_t* n_entity_host,
+                           int32_t* status, void* workspace, size_t workspace_bytes, void* stream);
+int32_t fgb_topology_fill(int64_t n_cell, int32_t nv, const int32_t* cell, int64_t n_node, int32_t k,
+                          int32_t nfc, const int32_t* local_host, int32_t* entity, int32_t* entity2cell,
+                          int32_t* cell2entity, int32_t* status, void* workspace,
+                          size_t workspace_bytes, void* stream);
+
+/* cell_to_ipoint (fealpy/mesh/triangle_mesh.py:218-270,
+ * fealpy/mesh/tetrahedron_mesh.py:388-441): per local point k (host tables,
+ * ldof entries): kind 0 vertex a; kind 1 edge point between local vertices
+ * a < b on local edge le, with multi-index entries ma, mb (numbered from the
+ * global edge's first vertex); kind 2 the rank-th interior point of a
+ * triangle; kind 3 the interior point of local face le of a P3
+ * tetrahedron.  Writes cell2ipoint (n_cell x ldof, int32). */
+int32_t fgb_cell_to_ipoint(int64_t n_cell, int32_t td, int32_t p, int32_t ldof, const int32_t* cell,
+                           const int32_t* cell2edge, const int32_t* edge, const int32_t* cell2face,
+                           int64_t n_node, int64_t n_edge, const int32_t* kind_host,
+                           const int32_t* a_host, const int32_t* b_host, const int32_t* le_host,
+                           const int32_t* ma_host, const int32_t* mb_host, const int32_t* rank_host,
+                           int32_t* cell2ipoint, void* stream);
+
 /* ---- symbolic assembly ------------------------------------------------- */
 
 /* dof -> (cell, local index) adjacency, sorted by cell then local index:
