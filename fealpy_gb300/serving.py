@@ -9,13 +9,16 @@ allows (every admitted request keeps its CSR, SELL copy and Krylov vectors
 resident until it finishes), runs the batch for a chunk of iterations,
 returns the finished solutions to the host, and repeats.  Requests that
 arrive while others are iterating join at the next chunk boundary, so their
-work overlaps on the device with the work already in flight.
+work overlaps on the device with the work already in flight; their systems
+are built ahead by a builder thread on a second CUDA stream while the batch
+iterates, and results go back to the host by asynchronous copies.
 
 Latency of a request = the moment its solution is on the host minus its
 arrival time; p50/p99 over all requests and the throughput (requests/s over
 the whole stream) are reported by :meth:`SolveServer.run`.
 """
 import time
+from concurrent.futures import Future, ThreadPoolExecutor
 from typing import Callable, Dict, List, Optional
 
 import numpy as np
@@ -122,10 +125,18 @@ class SolveServer:
         return True
 
     def run(self, requests: List[dict], build: Callable = poisson_request_problem, *, time_scale: float = 1.0,
-            keep_solutions: bool = False) -> dict:
+            keep_solutions: bool = False, prefetch: int = 16) -> dict:
         """Serve ``requests`` (dicts with arrival time ``t`` in seconds) in
-        real time.  ``build(req, device)`` makes the system of a request when
-        it is admitted.  Returns latencies (s), p50/p99, throughput and, with
+        real time.  ``build(req, device)`` makes the system of a request.
+
+        Requests are built ahead of admission (up to ``prefetch`` queued ones)
+        by a builder thread on its own CUDA stream while the batch iterates on
+        the main stream, so that mesh set-up, assembly and boundary conditions
+        overlap with the running solves; a built system is admitted after the
+        main stream waits on its build event.  Finished solutions are copied
+        to pinned host memory asynchronously, and a completion thread records
+        the moment each copy lands (latency = that moment minus the arrival).
+        Returns latencies (s), p50/p99, throughput and, with
         ``keep_solutions``, every solution on the host."""
         order = sorted(range(len(requests)), key=lambda i: requests[i]["t"])
         queue: List[int] = []
@@ -133,39 +144,81 @@ class SolveServer:
         lat: Dict[int, float] = {}
         info: Dict[int, dict] = {}
         sols: Dict[int, np.ndarray] = {}
-        pending_sys: Dict[int, tuple] = {}
+        futures: Dict[int, Future] = {}
+        # high priority: the batch's tile kernels fill every SM, so the build
+        # kernels are scheduled first whenever blocks retire between them
+        build_stream = torch.cuda.Stream(self.device, priority=-1)
+        main_stream = torch.cuda.current_stream(self.device)
+
+        def build_async(req):
+            with torch.cuda.stream(build_stream):
+                A, b = build(req, self.device)
+                ev = torch.cuda.Event()
+                ev.record(build_stream)
+            return A, b, ev
+
+        def complete(key, x_dev, x_host, ev, arrival):
+            ev.synchronize()  # the copy has landed: the request ends here
+            lat[key] = time.perf_counter() - t0 - arrival
+            if keep_solutions:
+                sols[key] = x_host.numpy()
+            del x_dev
+
+        builder = ThreadPoolExecutor(1)
+        finisher = ThreadPoolExecutor(1)
+        done_jobs = []
         t0 = time.perf_counter()
-        while len(lat) < len(requests):
-            now = time.perf_counter() - t0
-            while nxt < len(order) and requests[order[nxt]]["t"] * time_scale <= now:
-                queue.append(order[nxt])
-                nxt += 1
-            # admission: FIFO while a slot and the memory budget allow
-            while queue and self.batch.free_slots() > 0:
-                i = queue[0]
-                if i not in pending_sys:
-                    pending_sys[i] = build(requests[i], self.device)
-                A, b = pending_sys[i]
-                if not self.admit(i, A, b):
-                    if self.batch.active() == 0:
-                        raise RuntimeError(f"request {i} does not fit in the memory budget")
-                    break
-                queue.pop(0)
-                del pending_sys[i]
-            if self.batch.active() == 0:
-                if nxt < len(order):
-                    wait = requests[order[nxt]]["t"] * time_scale - (time.perf_counter() - t0)
-                    if wait > 0:
-                        time.sleep(wait)
-                continue
-            for r in self.batch.step(max_iterations=self.chunk):
-                x = r.x.cpu()  # the result on the host ends the request
-                done = time.perf_counter() - t0
-                lat[r.key] = done - requests[r.key]["t"] * time_scale
-                info[r.key] = r.info()
-                if keep_solutions:
-                    sols[r.key] = x.numpy()
-                self.resident -= self._bytes.pop(r.key)
+        try:
+            finished = 0
+            while finished < len(requests):
+                now = time.perf_counter() - t0
+                while nxt < len(order) and requests[order[nxt]]["t"] * time_scale <= now:
+                    queue.append(order[nxt])
+                    nxt += 1
+                for i in queue[:max(prefetch, 1)]:
+                    if i not in futures:
+                        futures[i] = builder.submit(build_async, requests[i])
+                # admission: FIFO while a slot and the memory budget allow; a
+                # request still being built is waited for while the batch runs
+                # below half its slots, otherwise it blocks the ones behind it
+                # until the next chunk boundary
+                while queue and self.batch.free_slots() > 0:
+                    i = queue[0]
+                    fut = futures[i]
+                    if not fut.done() and 2 * self.batch.active() >= self.max_slots:
+                        break
+                    A, b, ev = fut.result()
+                    main_stream.wait_event(ev)
+                    if not self.admit(i, A, b):
+                        if self.batch.active() == 0:
+                            raise RuntimeError(f"request {i} does not fit in the memory budget")
+                        break
+                    queue.pop(0)
+                    del futures[i]
+                    for j in queue[:max(prefetch, 1)]:
+                        if j not in futures:
+                            futures[j] = builder.submit(build_async, requests[j])
+                if self.batch.active() == 0:
+                    if nxt < len(order):
+                        wait = requests[order[nxt]]["t"] * time_scale - (time.perf_counter() - t0)
+                        if wait > 0:
+                            time.sleep(wait)
+                    continue
+                for r in self.batch.step(max_iterations=self.chunk):
+                    x_host = torch.empty(r.x.shape, dtype=r.x.dtype, pin_memory=True)
+                    x_host.copy_(r.x, non_blocking=True)
+                    ev = torch.cuda.Event()
+                    ev.record(main_stream)
+                    info[r.key] = r.info()
+                    self.resident -= self._bytes.pop(r.key)
+                    done_jobs.append(finisher.submit(complete, r.key, r.x, x_host, ev,
+                                                     requests[r.key]["t"] * time_scale))
+                    finished += 1
+            for j in done_jobs:
+                j.result()
+        finally:
+            builder.shutdown(wait=True)
+            finisher.shutdown(wait=True)
         makespan = time.perf_counter() - t0
         v = np.array([lat[i] for i in range(len(requests))])
         out = {"n": len(requests), "p50_s": float(np.percentile(v, 50)), "p99_s": float(np.percentile(v, 99)),
