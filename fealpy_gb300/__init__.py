@@ -3,7 +3,8 @@
 The public modules mirror FEALPy's: ``mesh`` (TriangleMesh, TetrahedronMesh),
 ``functionspace`` (LagrangeFESpace, TensorFunctionSpace), ``fem``
 (BilinearForm, LinearForm, integrators, DirichletBC), ``sparse`` (CSRTensor),
-``solver`` (cg, cg_mixed, JacobiPreconditioner) and ``material``.  Assembly,
+``solver`` (cg, cg_mixed, JacobiPreconditioner), ``amg`` (GAMGSolver,
+AMGPreconditioner: the multigrid for cg's M slot) and ``material``.  Assembly,
 boundary conditions, SpMV and CG run as hand-written sm_103a kernels reached
 through the C ABI of ``fealpy_gb300/_lib/libfealpy_gb300.so``.
 """
@@ -11,10 +12,11 @@ from .mesh import TriangleMesh, TetrahedronMesh
 from .functionspace import LagrangeFESpace, TensorFunctionSpace
 from .sparse import CSRTensor
 from .solver import cg, cg_mixed, JacobiPreconditioner
+from .amg import GAMGSolver, AMGPreconditioner
 from .material import LinearElasticMaterial
 from . import fem
 
 __version__ = "0.1.0"
 
 __all__ = ["TriangleMesh", "TetrahedronMesh", "LagrangeFESpace", "TensorFunctionSpace", "CSRTensor", "cg",
-           "cg_mixed", "JacobiPreconditioner", "LinearElasticMaterial", "fem"]
+           "cg_mixed", "JacobiPreconditioner", "GAMGSolver", "AMGPreconditioner", "LinearElasticMaterial", "fem"]

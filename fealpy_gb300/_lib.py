@@ -45,6 +45,12 @@ PCG_REASONS = {0: "running", 1: "atol", 2: "rtol", 3: "maxit", 4: "zero rhs", 5:
                7: "stagnated"}
 
 
+class AmgLevel(ctypes.Structure):
+    """``fgb_amg_level`` (include/fealpy_gb300.h)."""
+    _fields_ = [("n", c_i64), ("nnz", c_i64), ("indptr", c_vp), ("indices", c_vp), ("values", c_vp), ("dinv", c_vp),
+                ("lmax", c_dbl), ("agg", c_vp), ("n_coarse", c_i64), ("member_ptr", c_vp), ("members", c_vp)]
+
+
 class PcgInfo(ctypes.Structure):
     _fields_ = [("niter", c_i64), ("residual", c_dbl), ("b_norm", c_dbl), ("true_relres", c_dbl),
                 ("reason", c_i32), ("n_updates", c_i32), ("launches", c_i64), ("kernel_ms", c_dbl),
@@ -74,6 +80,18 @@ _SIGNATURES = {
                                            c_vp, c_vp, c_vp, c_sz, c_vp]),
     "fgb_dirichlet_count": (c_i32, [c_i32, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "fgb_dirichlet_fill": (c_i32, [c_i32, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "fgb_amg_setup_workspace_bytes": (c_sz, [c_i64]),
+    "fgb_amg_aggregate": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_dbl, c_vp, ctypes.POINTER(c_i64), c_vp,
+                                  ctypes.POINTER(c_dbl), c_vp, c_vp, c_sz, c_vp]),
+    "fgb_amg_coarse_workspace_bytes": (c_sz, [c_i64, c_i64]),
+    "fgb_amg_coarse_count": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, ctypes.POINTER(c_i64),
+                                     c_vp, c_vp, c_sz, c_vp]),
+    "fgb_amg_coarse_fill": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp,
+                                    c_sz, c_vp]),
+    "fgb_amg_workspace_bytes": (c_sz, [c_vp, c_i32]),
+    "fgb_amg_vcycle": (c_i32, [c_vp, c_i32, c_i32, c_i32, c_dbl, c_vp, c_vp, c_vp, c_sz, c_vp]),
+    "fgb_pcg_amg": (c_i32, [c_vp, c_i32, c_i32, c_i32, c_dbl, c_vp, c_vp, c_dbl, c_dbl, c_i64, c_i32,
+                            ctypes.POINTER(PcgInfo), c_vp, c_sz, c_vp]),
     "fgb_topology_workspace_bytes": (c_sz, [c_i64, c_i64]),
     "fgb_topology_count": (c_i32, [c_i64, c_i32, c_vp, c_i64, c_i32, c_i32, c_vp, ctypes.POINTER(c_i64), c_vp, c_vp,
                                    c_sz, c_vp]),

@@ -1,0 +1,199 @@
+"""Aggregation algebraic multigrid for the ``M`` slot of ``cg``, with the
+interface of FEALPy's ``GAMGSolver`` (``fealpy/solver/gamg_solver.py:14-256``:
+``GAMGSolver(theta, csize, ..., isolver, maxit, rtol, atol).setup(A)`` then
+``solve(b)``; the hierarchy also applies as a preconditioner, ``M @ r``).
+
+FEALPy builds a Ruge-Stuben hierarchy and smooths with Gauss-Seidel sweeps,
+both sequential algorithms.  The GB300 hierarchy is built and applied by the
+library's kernels (``csrc/amg.cu``): distance-2 maximal-independent-set
+aggregation, Galerkin coarse matrices of the aggregate indicator (summed in a
+fixed order: the hierarchy and every V-cycle are deterministic), Chebyshev
+smoothing with the diagonal, coarse corrections scaled by ``omega``, and a
+Chebyshev solve on the coarsest level.  Each V-cycle is a fixed symmetric
+linear map, so it is a valid CG preconditioner; ``cg(A, b, M=amg)`` runs the
+whole PCG loop in the library (``fgb_pcg_amg``).
+"""
+import ctypes
+from typing import List, Optional
+
+import torch
+
+from . import _lib
+from . import kernels as K
+from .sparse import CSRTensor
+from ._lib import call, ptr, stream_ptr, workspace, status_word, check_status_word
+
+__all__ = ["GAMGSolver", "AMGPreconditioner"]
+
+
+class _Level:
+    def __init__(self, indptr, indices, values):
+        self.indptr, self.indices, self.values = indptr, indices, values
+        self.n = indptr.numel() - 1
+        self.nnz = indices.numel()
+        self.dinv = None
+        self.lmax = 0.0
+        self.agg = self.member_ptr = self.members = None
+        self.n_coarse = 0
+
+
+class GAMGSolver:
+    """Algebraic multigrid (see the module docstring).
+
+    Parameters as FEALPy's GAMGSolver where they apply: ``theta`` (strength
+    threshold of the aggregation graph; 0 takes every nonzero coupling, which
+    suits Lagrange matrices of degree 2 and 3 whose couplings change sign),
+    ``csize`` (coarsest size), ``ptype`` ('V'), ``sstep`` (Chebyshev degree of
+    each smoothing), ``isolver`` ('CG': PCG with the V-cycle, 'MG': V-cycle
+    iterations), ``maxit``, ``rtol``, ``atol``.  GB300 additions: ``omega``
+    (coarse-correction scale, plain aggregation needs > 1), ``cdeg`` (degree
+    of the coarsest Chebyshev solve), ``max_levels``."""
+
+    def __init__(self, theta: float = 0.0, csize: int = 300, ctype: str = "A", itype: str = "T", ptype: str = "V",
+                 sstep: int = 3, isolver: str = "CG", maxit: int = 200, csolver: str = "chebyshev",
+                 rtol: float = 1e-8, atol: float = 1e-8, omega: float = 1.7, cdeg: int = 16, max_levels: int = 10):
+        if ptype != "V":
+            raise NotImplementedError("the GB300 multigrid provides V-cycles")
+        if isolver not in ("CG", "MG"):
+            raise ValueError("isolver must be 'CG' or 'MG'")
+        self.theta, self.csize, self.ptype, self.sstep = float(theta), int(csize), ptype, int(sstep)
+        self.isolver, self.maxit, self.rtol, self.atol = isolver, int(maxit), float(rtol), float(atol)
+        self.omega, self.cdeg, self.max_levels = float(omega), int(cdeg), int(max_levels)
+        self.levels: List[_Level] = []
+        self._desc = None
+        self.A = None
+
+    # ------------------------------------------------------------ set-up
+    def setup(self, A: CSRTensor, P=None, R=None, mesh=None, space=None, cdegree=None):
+        """Build the hierarchy of ``A`` (FP64 CSR on the device)."""
+        if P is not None or R is not None or mesh is not None or space is not None:
+            raise NotImplementedError("the GB300 multigrid builds its own (algebraic) hierarchy")
+        if not isinstance(A, CSRTensor):
+            raise TypeError("A must be a CSRTensor")
+        dev = A.values.device
+        if dev.type != "cuda":
+            raise ValueError("GAMGSolver runs on the GPU only")
+        self.A = A
+        lib = _lib.lib()
+        s = stream_ptr(dev)
+        st = status_word(dev)
+        lev = _Level(A.crow.contiguous(), A.col.to(torch.int32).contiguous(),
+                     A.values.to(torch.float64).contiguous())
+        self.levels = []
+        while True:
+            n = lev.n
+            ws = workspace(lib.fgb_amg_setup_workspace_bytes(n), dev)
+            lev.agg = torch.empty(n, dtype=torch.int32, device=dev)
+            lev.dinv = torch.empty(n, dtype=torch.float64, device=dev)
+            nagg = ctypes.c_int64(0)
+            lmax = ctypes.c_double(0.0)
+            call("fgb_amg_aggregate", n, ptr(lev.indptr), ptr(lev.indices), ptr(lev.values), self.theta, ptr(lev.agg),
+                 ctypes.byref(nagg), ptr(lev.dinv), ctypes.byref(lmax), ptr(st), ptr(ws), ws.numel(), s)
+            check_status_word("multigrid set-up (the matrix needs a positive diagonal)", st)
+            lev.lmax = float(lmax.value)
+            nc = int(nagg.value)
+            self.levels.append(lev)
+            last = (n <= self.csize or len(self.levels) >= self.max_levels or nc == 0 or nc > 0.8 * n)
+            if last:
+                lev.agg = None
+                break
+            lev.n_coarse = nc
+            lev.member_ptr = torch.empty(nc + 1, dtype=torch.int64, device=dev)
+            lev.members = torch.empty(max(n, 1), dtype=torch.int32, device=dev)
+            cptr = torch.empty(nc + 1, dtype=torch.int64, device=dev)
+            cws = workspace(lib.fgb_amg_coarse_workspace_bytes(n, nc), dev)
+            nnz = ctypes.c_int64(0)
+            call("fgb_amg_coarse_count", n, ptr(lev.indptr), ptr(lev.indices), ptr(lev.values), ptr(lev.agg), nc,
+                 ptr(lev.member_ptr), ptr(lev.members), ptr(cptr), ctypes.byref(nnz), ptr(st), ptr(cws), cws.numel(),
+                 s)
+            ccol = torch.empty(max(int(nnz.value), 1), dtype=torch.int32, device=dev)
+            cval = torch.empty(max(int(nnz.value), 1), dtype=torch.float64, device=dev)
+            call("fgb_amg_coarse_fill", n, ptr(lev.indptr), ptr(lev.indices), ptr(lev.values), ptr(lev.agg), nc,
+                 ptr(lev.member_ptr), ptr(lev.members), ptr(cptr), ptr(ccol), ptr(cval), ptr(st), ptr(cws),
+                 cws.numel(), s)
+            check_status_word("multigrid coarse matrix (aggregate rows above the candidate capacity)", st)
+            lev = _Level(cptr, ccol[: int(nnz.value)], cval[: int(nnz.value)])
+        self._desc = (_lib.AmgLevel * len(self.levels))()
+        for k, L in enumerate(self.levels):
+            d = self._desc[k]
+            d.n, d.nnz = L.n, L.nnz
+            d.indptr, d.indices, d.values, d.dinv = (L.indptr.data_ptr(), L.indices.data_ptr(), L.values.data_ptr(),
+                                                    L.dinv.data_ptr())
+            d.lmax = L.lmax
+            if L.agg is not None:
+                d.agg, d.n_coarse = L.agg.data_ptr(), L.n_coarse
+                d.member_ptr, d.members = L.member_ptr.data_ptr(), L.members.data_ptr()
+        return self
+
+    def _ws(self):
+        dev = self.levels[0].values.device
+        nb = _lib.lib().fgb_amg_workspace_bytes(self._desc, len(self.levels))
+        if nb == 0:
+            raise RuntimeError("multigrid hierarchy is inconsistent")
+        return workspace(nb, dev)
+
+    def info(self):
+        """Rows, nonzeros and Chebyshev bound of every level."""
+        return [{"n": L.n, "nnz": L.nnz, "lmax": L.lmax} for L in self.levels]
+
+    # ------------------------------------------------------------ apply
+    def vcycle(self, r: torch.Tensor) -> torch.Tensor:
+        """One V-cycle applied to r (x = 0 start)."""
+        if self._desc is None:
+            raise RuntimeError("call setup(A) first")
+        dev = self.levels[0].values.device
+        r = r.to(device=dev, dtype=torch.float64).contiguous()
+        x = torch.empty_like(r)
+        ws = self._ws()
+        call("fgb_amg_vcycle", self._desc, len(self.levels), self.sstep, self.cdeg, self.omega, ptr(r), ptr(x),
+             ptr(ws), ws.numel(), stream_ptr(dev))
+        _lib.add_launches(6 * len(self.levels) * self.sstep)
+        return x
+
+    __matmul__ = vcycle
+
+    def pcg(self, b: torch.Tensor, x0: Optional[torch.Tensor] = None, atol: float = 1e-12, rtol: float = 1e-8,
+            maxit: int = 10000, norm: int = 0):
+        """CG preconditioned by the V-cycle (FEALPy's recurrence; norm 0 stops
+        on sqrt(r.z), 1 on ||r||); returns (x, info)."""
+        dev = self.levels[0].values.device
+        b = b.to(device=dev, dtype=torch.float64).contiguous()
+        x = torch.zeros_like(b) if x0 is None else x0.to(device=dev, dtype=torch.float64).clone()
+        ws = self._ws()
+        info = _lib.PcgInfo()
+        call("fgb_pcg_amg", self._desc, len(self.levels), self.sstep, self.cdeg, self.omega, ptr(b), ptr(x),
+             float(atol), float(rtol), int(maxit), int(norm), ctypes.byref(info), ptr(ws), ws.numel(), stream_ptr(dev))
+        _lib.add_launches(info.launches)
+        return x, info
+
+    def solve(self, b: torch.Tensor):
+        """Solve A x = b: PCG with the V-cycle ('CG') or V-cycle iterations
+        x += V(b - A x) ('MG'); returns (x, info) with FEALPy's keys."""
+        if self.isolver == "CG":
+            x, info = self.pcg(b, atol=self.atol, rtol=self.rtol, maxit=self.maxit, norm=1)
+            return x, {"residual": info.residual, "niter": int(info.niter)}
+        A = self.A
+        dev = self.levels[0].values.device
+        b = b.to(device=dev, dtype=torch.float64)
+        x = torch.zeros_like(b)
+        bn = float(torch.linalg.norm(b))
+        res, it = bn, 0
+        while it < self.maxit:
+            r = b - K.csr_spmv(A.crow, A.col, A.values, x)
+            res = float(torch.linalg.norm(r))
+            if res < self.atol or res < self.rtol * bn:
+                break
+            x += self.vcycle(r)
+            it += 1
+        return x, {"residual": res, "niter": it}
+
+
+class AMGPreconditioner:
+    """``AMGPreconditioner(**kw).apply(A)`` builds the hierarchy and returns
+    it for ``cg(A, b, M=...)`` (the shape of ``JacobiPreconditioner``)."""
+
+    def __init__(self, **kw):
+        self.kw = kw
+
+    def apply(self, A: CSRTensor) -> GAMGSolver:
+        return GAMGSolver(**self.kw).setup(A)

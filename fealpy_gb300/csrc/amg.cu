@@ -1,0 +1,958 @@
+// Aggregation algebraic multigrid: hierarchy set-up and the V-cycle
+// preconditioned CG, for the `M` slot of fealpy/solver/cg.py (FEALPy's
+// GAMGSolver, fealpy/solver/gamg_solver.py:14-256, fills it with a
+// Ruge-Stuben hierarchy and Gauss-Seidel smoothing; both are sequential
+// algorithms, so the GPU version uses their data-parallel counterparts).
+//
+// Set-up of one level (integer work, deterministic):
+//   aggregation  a distance-2 maximal independent set of the matrix graph
+//                (off-diagonal entries with |a_ij| > theta sqrt(|a_ii a_jj|)):
+//                every node carries a key (state, hash priority, index); two
+//                neighbourhood-max sweeps find the nodes whose key is the
+//                largest within distance 2, which become roots; nodes with a
+//                root within distance 2 drop out; repeat until every node is
+//                decided.  Roots are numbered in index order; the other nodes
+//                join the aggregate of their strongest-keyed assigned
+//                neighbour, in two sweeps.  Rows without off-diagonal entries
+//                (Dirichlet rows) join no aggregate.
+//   coarse matrix  A_c = P^T A P with P the aggregate indicator: the members
+//                of every aggregate (counting sort, each list sorted), and per
+//                coarse row the entries of the member rows mapped to their
+//                aggregates, sorted by (coarse column, position) in shared
+//                memory and summed in that order (count pass, scan, fill pass).
+//   bounds       per row 1/a_ii and the Gershgorin bound of D^-1 A (max over
+//                rows of sum_j |a_ij| / |a_ii|), for the Chebyshev smoother.
+// Apply (V-cycle on r, from x = 0): Chebyshev smoothing of degree `deg` with
+// D^-1 on [lmax/10, lmax]; the residual restricted by aggregate sums; the
+// coarse correction prolonged and scaled by `omega` (over-correction, which
+// plain aggregation needs); the same smoothing after; on the coarsest level
+// a Chebyshev solve of degree `cdeg` on [lmax/20, lmax].  Every step is a
+// fixed linear map, symmetric in A, so the V-cycle is a valid CG
+// preconditioner.
+
+#include "fgb_common.cuh"
+
+#include <climits>
+#include <cmath>
+#include <vector>
+
+namespace fgb {
+
+constexpr int kAmgThreads = 256;
+
+__device__ __forceinline__ uint32_t amg_hash(uint32_t x) {
+  x ^= x >> 16;
+  x *= 0x7feb352dU;
+  x ^= x >> 15;
+  x *= 0x846ca68bU;
+  x ^= x >> 16;
+  return x & 0x7fffffffU;
+}
+
+// key = rank (2 root, 1 undecided, 0 out) | 31-bit priority | 31-bit index
+__device__ __forceinline__ unsigned long long amg_key(int rank, int64_t i) {
+  return (static_cast<unsigned long long>(rank) << 62) |
+         (static_cast<unsigned long long>(amg_hash(static_cast<uint32_t>(i))) << 31) |
+         static_cast<unsigned long long>(i);
+}
+
+__device__ __forceinline__ bool amg_strong(double aij, double dii, double djj, double theta) {
+  return aij != 0.0 && fabs(aij) > theta * sqrt(fabs(dii * djj));
+}
+
+template <typename T>
+__global__ void amg_diag_kernel(int64_t n, const int64_t* __restrict__ indptr, const int32_t* __restrict__ indices,
+                                const T* __restrict__ values, double* __restrict__ diag, int32_t* __restrict__ has_off,
+                                unsigned long long* __restrict__ bound_bits, int32_t* status) {
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    double d = 0.0, s = 0.0;
+    int off = 0;
+    for (int64_t e = indptr[i]; e < indptr[i + 1]; ++e) {
+      const double a = static_cast<double>(values[e]);
+      const int32_t j = indices[e];
+      if (j == i) d += a;
+      else if (a != 0.0) off = 1;
+      s += fabs(a);
+    }
+    diag[i] = d;
+    has_off[i] = off;
+    if (!(d > 0.0) || !isfinite(d)) {
+      set_status(status, FGB_ERR_BREAKDOWN);  // an SPD matrix has a positive diagonal
+      continue;
+    }
+    const double b = s / d;
+    atomicMax(bound_bits, static_cast<unsigned long long>(__double_as_longlong(b)));  // positive doubles order as ints
+  }
+}
+
+// state: 1 undecided, 2 root, 0 out, -1 isolated (no strong off-diagonal)
+__global__ void amg_init_state(int64_t n, const int64_t* __restrict__ indptr, const int32_t* __restrict__ indices,
+                               const double* __restrict__ values, const double* __restrict__ diag, double theta,
+                               int32_t* __restrict__ state) {
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    int strong = 0;
+    for (int64_t e = indptr[i]; e < indptr[i + 1] && !strong; ++e) {
+      const int32_t j = indices[e];
+      if (j < 0 || j >= n) continue;
+      if (j != i && amg_strong(values[e], diag[i], diag[j], theta)) strong = 1;
+    }
+    state[i] = strong ? 1 : -1;
+  }
+}
+
+__global__ void amg_keys(int64_t n, const int32_t* __restrict__ state, unsigned long long* __restrict__ key) {
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int s = state[i];
+    key[i] = s < 0 ? 0ull : amg_key(s == 2 ? 2 : (s == 1 ? 1 : 0), i);
+  }
+}
+
+// out[i] = max of src over i and its strong neighbours
+__global__ void amg_nbmax(int64_t n, const int64_t* __restrict__ indptr, const int32_t* __restrict__ indices,
+                          const double* __restrict__ values, const double* __restrict__ diag, double theta,
+                          const int32_t* __restrict__ state, const unsigned long long* __restrict__ src,
+                          unsigned long long* __restrict__ out) {
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    unsigned long long m = src[i];
+    if (state[i] >= 0) {
+      for (int64_t e = indptr[i]; e < indptr[i + 1]; ++e) {
+        const int32_t j = indices[e];
+        if (j < 0 || j >= n) continue;
+        if (j != i && amg_strong(values[e], diag[i], diag[j], theta)) {
+          const unsigned long long v = src[j];
+          m = v > m ? v : m;
+        }
+      }
+    }
+    out[i] = m;
+  }
+}
+
+__global__ void amg_mis_update(int64_t n, const unsigned long long* __restrict__ key,
+                               const unsigned long long* __restrict__ m2, int32_t* __restrict__ state,
+                               int32_t* __restrict__ undecided) {
+  int local = 0;
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    if (state[i] != 1) continue;
+    if (m2[i] == key[i]) state[i] = 2;
+    else if ((m2[i] >> 62) == 2ull) state[i] = 0;
+    else ++local;
+  }
+  if (local) atomicAdd(undecided, local);
+}
+
+__global__ void amg_root_flags(int64_t n, const int32_t* __restrict__ state, int32_t* __restrict__ flag) {
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    flag[i] = state[i] == 2 ? 1 : 0;
+}
+
+__global__ void amg_root_ids(int64_t n, const int32_t* __restrict__ state, const int64_t* __restrict__ off,
+                             int32_t* __restrict__ agg) {
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    agg[i] = state[i] == 2 ? static_cast<int32_t>(off[i]) : -1;
+}
+
+// One assignment sweep: an unassigned node with strong neighbours takes the
+// aggregate of the assigned strong neighbour with the largest (priority,
+// index); reads agg_in, writes agg_out (so the sweep does not depend on the
+// order of the threads); counts the nodes still unassigned.
+__global__ void amg_assign(int64_t n, const int64_t* __restrict__ indptr, const int32_t* __restrict__ indices,
+                           const double* __restrict__ values, const double* __restrict__ diag, double theta,
+                           const int32_t* __restrict__ state, const int32_t* __restrict__ agg_in,
+                           int32_t* __restrict__ agg_out, int32_t* __restrict__ left) {
+  int local = 0;
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    int32_t a = agg_in[i];
+    if (a < 0 && state[i] >= 0) {
+      unsigned long long best = 0ull;
+      int32_t pick = -1;
+      for (int64_t e = indptr[i]; e < indptr[i + 1]; ++e) {
+        const int32_t j = indices[e];
+        if (j < 0 || j >= n || j == i || agg_in[j] < 0 || !amg_strong(values[e], diag[i], diag[j], theta)) continue;
+        const unsigned long long k = amg_key(0, j);
+        if (pick < 0 || k > best) {
+          best = k;
+          pick = agg_in[j];
+        }
+      }
+      a = pick;
+      if (a < 0) ++local;
+    }
+    agg_out[i] = a;
+  }
+  if (local) atomicAdd(left, local);
+}
+
+// ------------------------------------------------------------ coarse matrix
+__global__ void amg_member_count(int64_t n, const int32_t* __restrict__ agg, int32_t* __restrict__ cnt) {
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    if (agg[i] >= 0) atomicAdd(cnt + agg[i], 1);
+}
+
+__global__ void amg_member_fill(int64_t n, const int32_t* __restrict__ agg, const int64_t* __restrict__ mptr,
+                                int32_t* __restrict__ cursor, int32_t* __restrict__ members) {
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    if (agg[i] >= 0) members[mptr[agg[i]] + atomicAdd(cursor + agg[i], 1)] = static_cast<int32_t>(i);
+}
+
+// each member list in ascending row order (insertion sort by one thread;
+// aggregates hold tens of rows)
+__global__ void amg_member_sort(int64_t nc, const int64_t* __restrict__ mptr, int32_t* __restrict__ members) {
+  for (int64_t c = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; c < nc;
+       c += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int64_t a = mptr[c], b = mptr[c + 1];
+    for (int64_t k = a + 1; k < b; ++k) {
+      const int32_t v = members[k];
+      int64_t u = k - 1;
+      while (u >= a && members[u] > v) {
+        members[u + 1] = members[u];
+        --u;
+      }
+      members[u + 1] = v;
+    }
+  }
+}
+
+constexpr int kCoarseThreads = 256;
+constexpr int kCoarseCap = 2048;      // candidates per coarse row, first pass (shared memory)
+constexpr int kCoarseBigCap = 8192;  // second pass (dynamic shared memory, 128 KB)
+
+// Coarse row I: candidates (J << 32 | position, value) of the member rows in
+// order, sorted in shared memory, summed per J in position order.  mode 0:
+// the number of distinct J to cnt[I]; mode 1: columns and values at
+// cptr[I].  Returns false when the candidates exceed cap (nothing written).
+__device__ bool amg_coarse_row(int64_t n, int64_t I, int mode, const int64_t* __restrict__ indptr,
+                               const int32_t* __restrict__ indices, const double* __restrict__ values,
+                               const int32_t* __restrict__ agg, const int64_t* __restrict__ mptr,
+                               const int32_t* __restrict__ members, int32_t* __restrict__ cnt,
+                               const int64_t* __restrict__ cptr, int32_t* __restrict__ ccol,
+                               double* __restrict__ cval, unsigned long long* kbuf, double* vbuf, int cap,
+                               int* sh_m, int* sh_u) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  // candidate count: sum of the member rows' lengths
+  if (tid == 0) {
+    int64_t m = 0;
+    for (int64_t k = mptr[I]; k < mptr[I + 1]; ++k) {
+      const int32_t r = members[k];
+      m += indptr[r + 1] - indptr[r];
+    }
+    *sh_m = m > cap ? -1 : static_cast<int>(m);
+  }
+  __syncthreads();
+  const int m = *sh_m;
+  if (m < 0) return false;
+  int np2 = 1;
+  while (np2 < m) np2 <<= 1;
+  // fill: walk member rows in order; positions are the running entry index
+  if (tid == 0) *sh_u = 0;
+  for (int64_t k = mptr[I]; k < mptr[I + 1]; ++k) {
+    const int32_t r = members[k];
+    const int64_t a = indptr[r];
+    const int len = static_cast<int>(indptr[r + 1] - a);
+    __syncthreads();
+    const int base = *sh_u;
+    for (int t = tid; t < len; t += nt) {
+      const int32_t j = indices[a + t];
+      const int32_t J = (j >= 0 && j < n) ? agg[j] : -1;
+      const int pos = base + t;
+      kbuf[pos] = J >= 0 ? ((static_cast<unsigned long long>(static_cast<uint32_t>(J)) << 32) | static_cast<uint32_t>(pos))
+                         : ULLONG_MAX;
+      vbuf[pos] = values[a + t];
+    }
+    __syncthreads();
+    if (tid == 0) *sh_u = base + len;
+  }
+  __syncthreads();
+  for (int t = m + tid; t < np2; t += nt) {
+    kbuf[t] = ULLONG_MAX;
+    vbuf[t] = 0.0;
+  }
+  __syncthreads();
+  for (int kk = 2; kk <= np2; kk <<= 1) {
+    for (int j = kk >> 1; j > 0; j >>= 1) {
+      for (int t = tid; t < np2; t += nt) {
+        const int u = t ^ j;
+        if (u > t) {
+          const unsigned long long a = kbuf[t], b = kbuf[u];
+          const bool up = (t & kk) == 0;
+          if ((a > b) == up) {
+            kbuf[t] = b;
+            kbuf[u] = a;
+            const double va = vbuf[t];
+            vbuf[t] = vbuf[u];
+            vbuf[u] = va;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  // distinct coarse columns (entries with J < 0 sorted last as ULLONG_MAX)
+  if (tid == 0) {
+    int u = 0;
+    const int64_t out0 = mode == 1 ? cptr[I] : 0;
+    int t = 0;
+    while (t < m && kbuf[t] != ULLONG_MAX) {
+      const uint32_t J = static_cast<uint32_t>(kbuf[t] >> 32);
+      double s = 0.0;
+      while (t < m && kbuf[t] != ULLONG_MAX && static_cast<uint32_t>(kbuf[t] >> 32) == J) {
+        s += vbuf[t];
+        ++t;
+      }
+      if (mode == 1) {
+        ccol[out0 + u] = static_cast<int32_t>(J);
+        cval[out0 + u] = s;
+      }
+      ++u;
+    }
+    if (mode == 0) cnt[I] = u;
+  }
+  __syncthreads();
+  return true;
+}
+
+__global__ void __launch_bounds__(kCoarseThreads) amg_coarse_rows(int64_t n, int64_t nc, int mode,
+                                                                 const int64_t* __restrict__ indptr,
+                                                                 const int32_t* __restrict__ indices,
+                                                                 const double* __restrict__ values,
+                                                                 const int32_t* __restrict__ agg,
+                                                                 const int64_t* __restrict__ mptr,
+                                                                 const int32_t* __restrict__ members,
+                                                                 int32_t* __restrict__ cnt,
+                                                                 const int64_t* __restrict__ cptr,
+                                                                 int32_t* __restrict__ ccol, double* __restrict__ cval,
+                                                                 int32_t* __restrict__ ovf, int32_t* __restrict__ ovf_len) {
+  __shared__ unsigned long long kbuf[kCoarseCap];
+  __shared__ double vbuf[kCoarseCap];
+  __shared__ int sh_m, sh_u;
+  for (int64_t I = blockIdx.x; I < nc; I += gridDim.x) {
+    const bool ok = amg_coarse_row(n, I, mode, indptr, indices, values, agg, mptr, members, cnt, cptr, ccol, cval, kbuf,
+                                   vbuf, kCoarseCap, &sh_m, &sh_u);
+    if (!ok && threadIdx.x == 0) ovf[atomicAdd(ovf_len, 1)] = static_cast<int32_t>(I);
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kCoarseThreads) amg_coarse_rows_big(int64_t n, int mode,
+                                                                     const int64_t* __restrict__ indptr,
+                                                                     const int32_t* __restrict__ indices,
+                                                                     const double* __restrict__ values,
+                                                                     const int32_t* __restrict__ agg,
+                                                                     const int64_t* __restrict__ mptr,
+                                                                     const int32_t* __restrict__ members,
+                                                                     int32_t* __restrict__ cnt,
+                                                                     const int64_t* __restrict__ cptr,
+                                                                     int32_t* __restrict__ ccol,
+                                                                     double* __restrict__ cval,
+                                                                     const int32_t* __restrict__ ovf,
+                                                                     const int32_t* __restrict__ ovf_len,
+                                                                     int32_t* status) {
+  extern __shared__ __align__(16) unsigned char dsm[];
+  unsigned long long* kbuf = reinterpret_cast<unsigned long long*>(dsm);
+  double* vbuf = reinterpret_cast<double*>(dsm + static_cast<size_t>(kCoarseBigCap) * 8);
+  __shared__ int sh_m, sh_u;
+  const int n_ovf = *ovf_len;
+  for (int r = blockIdx.x; r < n_ovf; r += gridDim.x) {
+    const bool ok = amg_coarse_row(n, ovf[r], mode, indptr, indices, values, agg, mptr, members, cnt, cptr, ccol, cval,
+                                   kbuf, vbuf, kCoarseBigCap, &sh_m, &sh_u);
+    if (!ok && threadIdx.x == 0) set_status(status, FGB_ERR_CAPACITY);
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------ apply kernels
+// Rows with G lanes each (G in {4, 8, 16, 32}); y = A x fused with a
+// per-row epilogue.
+// (A x)_i by the G lanes of row i; every lane of the warp calls it (rows past
+// n pass active = false and contribute nothing), so the full-warp shuffles
+// always have all 32 lanes present.
+template <int G>
+__device__ __forceinline__ double csr_row_dot(int64_t i, bool active, const int64_t* __restrict__ indptr,
+                                              const int32_t* __restrict__ indices, const double* __restrict__ values,
+                                              const double* __restrict__ x, int sub) {
+  double acc = 0.0;
+  if (active)
+    for (int64_t e = indptr[i] + sub; e < indptr[i + 1]; e += G) acc += values[e] * x[indices[e]];
+#pragma unroll
+  for (int o = G >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, G);
+  return acc;
+}
+
+// Rows in groups of 32 / G per warp; the trip count is the same for every
+// lane of a warp (the bound is tested on the warp's first row).
+#define AMG_ROW_LOOP(n, G)                                                                                   \
+  const int sub = threadIdx.x & ((G) - 1);                                                                   \
+  const int64_t wfirst = ((blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5) * (32 / (G));  \
+  const int64_t wstep = ((static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5) * (32 / (G));                  \
+  for (int64_t wr = wfirst, i = wfirst + (threadIdx.x & 31) / (G); wr < (n); wr += wstep, i += wstep)
+
+// Chebyshev step: d = c1 d + c2 Dinv (r - A x_in); x_out = x_in + d
+template <int G>
+__global__ void amg_cheb_step(int64_t n, const int64_t* __restrict__ indptr, const int32_t* __restrict__ indices,
+                              const double* __restrict__ values, const double* __restrict__ dinv,
+                              const double* __restrict__ r, const double* __restrict__ x_in,
+                              double* __restrict__ x_out, double* __restrict__ d, double c1, double c2) {
+  AMG_ROW_LOOP(n, G) {
+    const bool active = i < n;
+    const double ax = csr_row_dot<G>(i, active, indptr, indices, values, x_in, sub);
+    if (active && sub == 0) {
+      const double di = (c1 != 0.0 ? c1 * d[i] : 0.0) + c2 * dinv[i] * (r[i] - ax);
+      d[i] = di;
+      x_out[i] = x_in[i] + di;
+    }
+  }
+}
+
+// first Chebyshev step from x = 0: d = c2 Dinv r, x = d
+__global__ void amg_invert(int64_t n, const double* __restrict__ diag, double* __restrict__ dinv) {
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    dinv[i] = 1.0 / diag[i];
+}
+
+__global__ void amg_cheb_first(int64_t n, const double* __restrict__ dinv, const double* __restrict__ r,
+                               double* __restrict__ x, double* __restrict__ d, double c2) {
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const double di = c2 * dinv[i] * r[i];
+    d[i] = di;
+    x[i] = di;
+  }
+}
+
+// res = r - A x
+template <int G>
+__global__ void amg_residual(int64_t n, const int64_t* __restrict__ indptr, const int32_t* __restrict__ indices,
+                             const double* __restrict__ values, const double* __restrict__ r,
+                             const double* __restrict__ x, double* __restrict__ res) {
+  AMG_ROW_LOOP(n, G) {
+    const bool active = i < n;
+    const double ax = csr_row_dot<G>(i, active, indptr, indices, values, x, sub);
+    if (active && sub == 0) res[i] = r[i] - ax;
+  }
+}
+
+// rc[I] = sum of res over the members of aggregate I, in row order
+__global__ void amg_restrict(int64_t nc, const int64_t* __restrict__ mptr, const int32_t* __restrict__ members,
+                             const double* __restrict__ res, double* __restrict__ rc) {
+  for (int64_t I = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; I < nc;
+       I += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    double s = 0.0;
+    for (int64_t k = mptr[I]; k < mptr[I + 1]; ++k) s += res[members[k]];
+    rc[I] = s;
+  }
+}
+
+// x[i] += omega * ec[agg[i]]
+__global__ void amg_prolong(int64_t n, const int32_t* __restrict__ agg, const double* __restrict__ ec, double omega,
+                            double* __restrict__ x) {
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int32_t a = agg[i];
+    if (a >= 0) x[i] += omega * ec[a];
+  }
+}
+
+// ------------------------------------------------------------ PCG kernels
+constexpr int kDotBlocks = 2 * kNumSMs;
+constexpr int kMaxGrid = kNumSMs * 16;  // grids of every kernel here (grid_for caps)
+
+// Deterministic two-value reduction: per-block sums in a fixed order, the last
+// block adds the blocks' sums in block order into out[0..1].
+__device__ void amg_reduce2(double a, double b, double* partials, unsigned int* counter, double* out) {
+  __shared__ double sa[32], sb[32];
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  a = warp_sum(a);
+  b = warp_sum(b);
+  if (lane == 0) {
+    sa[wid] = a;
+    sb[wid] = b;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double ta = 0.0, tb = 0.0;
+    for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) {
+      ta += sa[w];
+      tb += sb[w];
+    }
+    partials[blockIdx.x] = ta;
+    partials[gridDim.x + blockIdx.x] = tb;
+    __threadfence();
+    last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (last && threadIdx.x == 0) {
+    __threadfence();
+    double ta = 0.0, tb = 0.0;
+    for (unsigned int k = 0; k < gridDim.x; ++k) {
+      ta += __ldcg(partials + k);
+      tb += __ldcg(partials + gridDim.x + k);
+    }
+    out[0] = ta;
+    out[1] = tb;
+    *counter = 0u;
+  }
+}
+
+// Ap = A p; out = (p.Ap, 0)
+template <int G>
+__global__ void amg_pcg_spmv(int64_t n, const int64_t* __restrict__ indptr, const int32_t* __restrict__ indices,
+                             const double* __restrict__ values, const double* __restrict__ p, double* __restrict__ Ap,
+                             double* partials, unsigned int* counter, double* out) {
+  double pap = 0.0;
+  AMG_ROW_LOOP(n, G) {
+    const bool active = i < n;
+    const double ax = csr_row_dot<G>(i, active, indptr, indices, values, p, sub);
+    if (active && sub == 0) {
+      Ap[i] = ax;
+      pap += p[i] * ax;
+    }
+  }
+  amg_reduce2(pap, 0.0, partials, counter, out);
+}
+
+// x += alpha p, r -= alpha Ap; out = (r.r, 0)
+__global__ void amg_pcg_update(int64_t n, double alpha, const double* __restrict__ p, const double* __restrict__ Ap,
+                               double* __restrict__ x, double* __restrict__ r, double* partials, unsigned int* counter,
+                               double* out) {
+  double rr = 0.0;
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    x[i] += alpha * p[i];
+    const double ri = r[i] - alpha * Ap[i];
+    r[i] = ri;
+    rr += ri * ri;
+  }
+  amg_reduce2(rr, 0.0, partials, counter, out);
+}
+
+// out = (a.b, a.a)
+__global__ void amg_dot2(int64_t n, const double* __restrict__ a, const double* __restrict__ b, double* partials,
+                         unsigned int* counter, double* out) {
+  double ab = 0.0, aa = 0.0;
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    ab += a[i] * b[i];
+    aa += a[i] * a[i];
+  }
+  amg_reduce2(ab, aa, partials, counter, out);
+}
+
+// p = z + beta p
+__global__ void amg_pupdate(int64_t n, double beta, const double* __restrict__ z, double* __restrict__ p) {
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    p[i] = z[i] + beta * p[i];
+}
+
+inline int amg_lanes(int64_t n, int64_t nnz) {
+  const double avg = n > 0 ? static_cast<double>(nnz) / n : 0.0;
+  return avg <= 6 ? 4 : (avg <= 14 ? 8 : (avg <= 40 ? 16 : 32));
+}
+
+inline int rows_grid(int64_t n, int G) { return grid_for(n * G, kAmgThreads, kNumSMs * 16); }
+inline int vec_grid(int64_t n) { return grid_for(n, kAmgThreads, kNumSMs * 16); }
+
+#define AMG_DISPATCH_G(G, KERNEL, ...)                                                                 \
+  switch (G) {                                                                                         \
+    case 4: KERNEL<4><<<rows_grid(n, 4), kAmgThreads, 0, st>>>(__VA_ARGS__); break;                   \
+    case 8: KERNEL<8><<<rows_grid(n, 8), kAmgThreads, 0, st>>>(__VA_ARGS__); break;                   \
+    case 16: KERNEL<16><<<rows_grid(n, 16), kAmgThreads, 0, st>>>(__VA_ARGS__); break;                \
+    default: KERNEL<32><<<rows_grid(n, 32), kAmgThreads, 0, st>>>(__VA_ARGS__); break;                \
+  }
+
+}  // namespace fgb
+
+using namespace fgb;
+
+namespace {
+
+// scratch vectors of one level in the V-cycle workspace
+struct LevelVecs {
+  double *r, *x, *x2, *d, *res;
+};
+
+size_t level_vec_bytes(int64_t n) { return 5 * align_up(static_cast<size_t>(n) * sizeof(double)); }
+
+LevelVecs carve_level(Carver& cv, int64_t n) {
+  LevelVecs v;
+  v.r = cv.take<double>(n);
+  v.x = cv.take<double>(n);
+  v.x2 = cv.take<double>(n);
+  v.d = cv.take<double>(n);
+  v.res = cv.take<double>(n);
+  return v;
+}
+
+// Chebyshev polynomial in D^-1 A of degree deg on [lmax * lo, lmax], applied
+// to r from x = 0 (x0 == nullptr) or as a correction of x0; the result ends
+// in *xout (one of the two buffers).
+void cheb(const fgb_amg_level& L, const double* r, double* xa, double* xb, double* d, int deg, double lo,
+          bool from_zero, double** xout, cudaStream_t st) {
+  const int64_t n = L.n;
+  const double lmax = L.lmax, lmin = L.lmax * lo;
+  const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin), sigma = theta / delta;
+  const int G = amg_lanes(n, L.nnz);
+  double rho = 1.0 / sigma;
+  double* cur = xa;
+  double* nxt = xb;
+  int k = 0;
+  if (from_zero) {
+    amg_cheb_first<<<vec_grid(n), kAmgThreads, 0, st>>>(n, L.dinv, r, cur, d, 1.0 / theta);
+    k = 1;
+  } else {
+    // first correction of a given x: d = Dinv (r - A x) / theta
+    AMG_DISPATCH_G(G, amg_cheb_step, n, L.indptr, L.indices, L.values, L.dinv, r, cur, nxt, d, 0.0, 1.0 / theta);
+    double* t = cur;
+    cur = nxt;
+    nxt = t;
+    k = 1;
+  }
+  for (; k < deg; ++k) {
+    const double rho1 = 1.0 / (2.0 * sigma - rho);
+    AMG_DISPATCH_G(G, amg_cheb_step, n, L.indptr, L.indices, L.values, L.dinv, r, cur, nxt, d, rho1 * rho,
+                   2.0 * rho1 / delta);
+    double* t = cur;
+    cur = nxt;
+    nxt = t;
+    rho = rho1;
+  }
+  *xout = cur;
+}
+
+int vcycle(const fgb_amg_level* levels, int nl, const double* r0, double* x_out, int deg, int cdeg, double omega,
+           LevelVecs* V, cudaStream_t st) {
+  // down: smoothing from zero, residual, restriction
+  std::vector<double*> xs(nl);
+  const double* rin = r0;
+  for (int l = 0; l < nl; ++l) {
+    const fgb_amg_level& L = levels[l];
+    const int64_t n = L.n;
+    if (l == nl - 1) {
+      double* xo = nullptr;
+      cheb(L, rin, V[l].x, V[l].x2, V[l].d, cdeg, 0.05, true, &xo, st);
+      xs[l] = xo;
+      break;
+    }
+    double* xo = nullptr;
+    cheb(L, rin, V[l].x, V[l].x2, V[l].d, deg, 0.1, true, &xo, st);
+    xs[l] = xo;
+    const int G = amg_lanes(n, L.nnz);
+    AMG_DISPATCH_G(G, amg_residual, n, L.indptr, L.indices, L.values, rin, xo, V[l].res);
+    amg_restrict<<<vec_grid(L.n_coarse), kAmgThreads, 0, st>>>(L.n_coarse, L.member_ptr, L.members, V[l].res,
+                                                               V[l + 1].r);
+    rin = V[l + 1].r;
+  }
+  // up: prolongation with over-correction, smoothing of the corrected x
+  for (int l = nl - 2; l >= 0; --l) {
+    const fgb_amg_level& L = levels[l];
+    const double* rl = l == 0 ? r0 : V[l].r;
+    amg_prolong<<<vec_grid(L.n), kAmgThreads, 0, st>>>(L.n, L.agg, xs[l + 1], omega, xs[l]);
+    double* other = xs[l] == V[l].x ? V[l].x2 : V[l].x;
+    double* xo = nullptr;
+    cheb(L, rl, xs[l], other, V[l].d, deg, 0.1, false, &xo, st);
+    xs[l] = xo;
+  }
+  return cudaMemcpyAsync(x_out, xs[0], levels[0].n * sizeof(double), cudaMemcpyDeviceToDevice, st) == cudaSuccess
+             ? launch_status()
+             : FGB_ERR_CUDA;
+}
+
+size_t vcycle_bytes(const fgb_amg_level* levels, int nl) {
+  size_t b = 0;
+  for (int l = 0; l < nl; ++l) b += level_vec_bytes(levels[l].n);
+  return b;
+}
+
+bool levels_ok(const fgb_amg_level* levels, int nl) {
+  if (!levels || nl < 1 || nl > FGB_AMG_MAX_LEVELS) return false;
+  for (int l = 0; l < nl; ++l) {
+    const fgb_amg_level& L = levels[l];
+    if (L.n <= 0 || !L.indptr || !L.indices || !L.values || !L.dinv || !(L.lmax > 0.0)) return false;
+    if (l < nl - 1 && (!L.agg || !L.member_ptr || !L.members || L.n_coarse != levels[l + 1].n)) return false;
+  }
+  return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t fgb_amg_setup_workspace_bytes(int64_t n) {
+  const size_t un = static_cast<size_t>(n);
+  return align_up(un * 8) * 4 + align_up((un + 1) * 4) * 3 + align_up(8) + align_up(8) + align_up((un + 1) * 8) +
+         scan_workspace_bytes(n + 1);
+}
+
+int32_t fgb_amg_aggregate(int64_t n, const int64_t* indptr, const int32_t* indices, const double* values,
+                          double theta, int32_t* agg, int64_t* n_agg_host, double* dinv, double* lmax_host,
+                          int32_t* status, void* workspace, size_t workspace_bytes, void* stream) {
+  if (n <= 0 || !indptr || !indices || !values || !agg || !n_agg_host || !dinv || !lmax_host || !status ||
+      !(theta >= 0.0))
+    return FGB_ERR_ARG;
+  if (n >= (int64_t(1) << 31)) return FGB_ERR_CAPACITY;
+  if (!workspace || workspace_bytes < fgb_amg_setup_workspace_bytes(n)) return FGB_ERR_WORKSPACE;
+  cudaStream_t st = as_stream(stream);
+  Carver cv(workspace, workspace_bytes);
+  double* diag = cv.take<double>(n);
+  unsigned long long* key = cv.take<unsigned long long>(n);
+  unsigned long long* m1 = cv.take<unsigned long long>(n);
+  unsigned long long* m2 = cv.take<unsigned long long>(n);
+  int32_t* state = cv.take<int32_t>(n + 1);
+  int32_t* flag = cv.take<int32_t>(n + 1);
+  int32_t* agg2 = cv.take<int32_t>(n + 1);
+  unsigned long long* bound = cv.take<unsigned long long>(1);
+  int32_t* counter = cv.take<int32_t>(2);
+  int64_t* off = cv.take<int64_t>(n + 1);
+  void* scan_ws = cv.base + cv.off;
+  const size_t scan_bytes = workspace_bytes - cv.off;
+  if (!cv.ok) return FGB_ERR_WORKSPACE;
+  const int g = vec_grid(n);
+  if (cudaMemsetAsync(bound, 0, sizeof(unsigned long long), st) != cudaSuccess) return FGB_ERR_CUDA;
+  amg_diag_kernel<double><<<g, kAmgThreads, 0, st>>>(n, indptr, indices, values, diag, flag, bound, status);
+  amg_invert<<<g, kAmgThreads, 0, st>>>(n, diag, dinv);
+  amg_init_state<<<g, kAmgThreads, 0, st>>>(n, indptr, indices, values, diag, theta, state);
+  // distance-2 maximal independent set (each round decides at least the
+  // undecided node of largest key; 64 rounds bound the loop)
+  int32_t und = 1;
+  for (int round = 0; round < 64 && und > 0; ++round) {
+    amg_keys<<<g, kAmgThreads, 0, st>>>(n, state, key);
+    amg_nbmax<<<g, kAmgThreads, 0, st>>>(n, indptr, indices, values, diag, theta, state, key, m1);
+    amg_nbmax<<<g, kAmgThreads, 0, st>>>(n, indptr, indices, values, diag, theta, state, m1, m2);
+    if (cudaMemsetAsync(counter, 0, sizeof(int32_t), st) != cudaSuccess) return FGB_ERR_CUDA;
+    amg_mis_update<<<g, kAmgThreads, 0, st>>>(n, key, m2, state, counter);
+    if (cudaMemcpyAsync(&und, counter, sizeof(int32_t), cudaMemcpyDeviceToHost, st) != cudaSuccess) return FGB_ERR_CUDA;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return FGB_ERR_CUDA;
+  }
+  if (und > 0) return FGB_ERR_CAPACITY;
+  // roots numbered in index order
+  amg_root_flags<<<g, kAmgThreads, 0, st>>>(n, state, flag);
+  int rc = exclusive_scan_i32_to_i64(flag, n, off, scan_ws, scan_bytes, st);
+  if (rc) return rc;
+  int64_t nroot = 0;
+  if (cudaMemcpyAsync(&nroot, off + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st) != cudaSuccess) return FGB_ERR_CUDA;
+  amg_root_ids<<<g, kAmgThreads, 0, st>>>(n, state, off, agg);
+  // assignment sweeps (ping-pong between agg and agg2) until every node with
+  // strong neighbours belongs to an aggregate
+  int32_t left = 1;
+  int32_t* cur = agg;
+  int32_t* nxt = agg2;
+  for (int sweep = 0; sweep < 8 && left > 0; ++sweep) {
+    if (cudaMemsetAsync(counter, 0, sizeof(int32_t), st) != cudaSuccess) return FGB_ERR_CUDA;
+    amg_assign<<<g, kAmgThreads, 0, st>>>(n, indptr, indices, values, diag, theta, state, cur, nxt, counter);
+    if (cudaMemcpyAsync(&left, counter, sizeof(int32_t), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+      return FGB_ERR_CUDA;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return FGB_ERR_CUDA;
+    int32_t* t = cur;
+    cur = nxt;
+    nxt = t;
+  }
+  if (left > 0) return FGB_ERR_CAPACITY;
+  if (cur != agg && cudaMemcpyAsync(agg, cur, n * sizeof(int32_t), cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+    return FGB_ERR_CUDA;
+  unsigned long long bbits = 0;
+  if (cudaMemcpyAsync(&bbits, bound, sizeof(bbits), cudaMemcpyDeviceToHost, st) != cudaSuccess) return FGB_ERR_CUDA;
+  if (cudaStreamSynchronize(st) != cudaSuccess) return FGB_ERR_CUDA;
+  *n_agg_host = nroot;
+  double b = 0.0;
+  memcpy(&b, &bbits, sizeof(b));
+  *lmax_host = b;
+  return launch_status();
+}
+
+size_t fgb_amg_coarse_workspace_bytes(int64_t n, int64_t n_coarse) {
+  const size_t c = static_cast<size_t>(n_coarse) + 1;
+  return align_up(c * 4) * 3 + align_up(sizeof(int32_t)) + scan_workspace_bytes(n_coarse + 1) +
+         align_up(static_cast<size_t>(n) * 0 + 8);
+}
+
+int32_t fgb_amg_coarse_count(int64_t n, const int64_t* indptr, const int32_t* indices, const double* values,
+                             const int32_t* agg, int64_t n_coarse, int64_t* member_ptr, int32_t* members,
+                             int64_t* coarse_indptr, int64_t* nnz_host, int32_t* status, void* workspace,
+                             size_t workspace_bytes, void* stream) {
+  if (n <= 0 || n_coarse <= 0 || !indptr || !indices || !values || !agg || !member_ptr || !members ||
+      !coarse_indptr || !nnz_host || !status)
+    return FGB_ERR_ARG;
+  if (!workspace || workspace_bytes < fgb_amg_coarse_workspace_bytes(n, n_coarse)) return FGB_ERR_WORKSPACE;
+  cudaStream_t st = as_stream(stream);
+  Carver cv(workspace, workspace_bytes);
+  int32_t* cnt = cv.take<int32_t>(n_coarse + 1);
+  int32_t* ovf = cv.take<int32_t>(n_coarse + 1);
+  int32_t* rowcnt = cv.take<int32_t>(n_coarse + 1);
+  int32_t* ovf_len = cv.take<int32_t>(1);
+  void* scan_ws = cv.base + cv.off;
+  const size_t scan_bytes = workspace_bytes - cv.off;
+  if (!cv.ok) return FGB_ERR_WORKSPACE;
+  if (cudaMemsetAsync(cnt, 0, (n_coarse + 1) * sizeof(int32_t), st) != cudaSuccess) return FGB_ERR_CUDA;
+  amg_member_count<<<vec_grid(n), kAmgThreads, 0, st>>>(n, agg, cnt);
+  int rc = exclusive_scan_i32_to_i64(cnt, n_coarse, member_ptr, scan_ws, scan_bytes, st);
+  if (rc) return rc;
+  if (cudaMemsetAsync(cnt, 0, (n_coarse + 1) * sizeof(int32_t), st) != cudaSuccess) return FGB_ERR_CUDA;
+  amg_member_fill<<<vec_grid(n), kAmgThreads, 0, st>>>(n, agg, member_ptr, cnt, members);
+  amg_member_sort<<<vec_grid(n_coarse), kAmgThreads, 0, st>>>(n_coarse, member_ptr, members);
+  if (cudaMemsetAsync(ovf_len, 0, sizeof(int32_t), st) != cudaSuccess) return FGB_ERR_CUDA;
+  amg_coarse_rows<<<grid_for(n_coarse, 1, kNumSMs * 8), kCoarseThreads, 0, st>>>(
+      n, n_coarse, 0, indptr, indices, values, agg, member_ptr, members, rowcnt, nullptr, nullptr, nullptr, ovf,
+      ovf_len);
+  const size_t big = static_cast<size_t>(kCoarseBigCap) * 16;
+  cudaFuncSetAttribute(amg_coarse_rows_big, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(big));
+  amg_coarse_rows_big<<<kNumSMs, kCoarseThreads, big, st>>>(n, 0, indptr, indices, values, agg, member_ptr, members,
+                                                             rowcnt, nullptr, nullptr, nullptr, ovf, ovf_len, status);
+  rc = exclusive_scan_i32_to_i64(rowcnt, n_coarse, coarse_indptr, scan_ws, scan_bytes, st);
+  if (rc) return rc;
+  if (cudaMemcpyAsync(nnz_host, coarse_indptr + n_coarse, sizeof(int64_t), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+    return FGB_ERR_CUDA;
+  if (cudaStreamSynchronize(st) != cudaSuccess) return FGB_ERR_CUDA;
+  return launch_status();
+}
+
+int32_t fgb_amg_coarse_fill(int64_t n, const int64_t* indptr, const int32_t* indices, const double* values,
+                            const int32_t* agg, int64_t n_coarse, const int64_t* member_ptr, const int32_t* members,
+                            const int64_t* coarse_indptr, int32_t* coarse_indices, double* coarse_values,
+                            int32_t* status, void* workspace, size_t workspace_bytes, void* stream) {
+  if (n <= 0 || n_coarse <= 0 || !indptr || !indices || !values || !agg || !member_ptr || !members ||
+      !coarse_indptr || !coarse_indices || !coarse_values || !status)
+    return FGB_ERR_ARG;
+  if (!workspace || workspace_bytes < fgb_amg_coarse_workspace_bytes(n, n_coarse)) return FGB_ERR_WORKSPACE;
+  cudaStream_t st = as_stream(stream);
+  Carver cv(workspace, workspace_bytes);
+  int32_t* cnt = cv.take<int32_t>(n_coarse + 1);
+  int32_t* ovf = cv.take<int32_t>(n_coarse + 1);
+  int32_t* rowcnt = cv.take<int32_t>(n_coarse + 1);
+  int32_t* ovf_len = cv.take<int32_t>(1);
+  if (!cv.ok) return FGB_ERR_WORKSPACE;
+  (void)cnt;
+  if (cudaMemsetAsync(ovf_len, 0, sizeof(int32_t), st) != cudaSuccess) return FGB_ERR_CUDA;
+  amg_coarse_rows<<<grid_for(n_coarse, 1, kNumSMs * 8), kCoarseThreads, 0, st>>>(
+      n, n_coarse, 1, indptr, indices, values, agg, member_ptr, members, rowcnt, coarse_indptr, coarse_indices,
+      coarse_values, ovf, ovf_len);
+  const size_t big = static_cast<size_t>(kCoarseBigCap) * 16;
+  cudaFuncSetAttribute(amg_coarse_rows_big, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(big));
+  amg_coarse_rows_big<<<kNumSMs, kCoarseThreads, big, st>>>(n, 1, indptr, indices, values, agg, member_ptr, members,
+                                                             rowcnt, coarse_indptr, coarse_indices, coarse_values, ovf,
+                                                             ovf_len, status);
+  return launch_status();
+}
+
+size_t fgb_amg_workspace_bytes(const fgb_amg_level* levels, int32_t n_levels) {
+  if (!levels_ok(levels, n_levels)) return 0;
+  const int64_t n = levels[0].n;
+  return vcycle_bytes(levels, n_levels) + 4 * align_up(static_cast<size_t>(n) * sizeof(double)) +
+         align_up(2 * kMaxGrid * sizeof(double)) + align_up(8 * sizeof(double)) + align_up(4 * sizeof(unsigned int));
+}
+
+int32_t fgb_amg_vcycle(const fgb_amg_level* levels, int32_t n_levels, int32_t deg, int32_t cdeg, double omega,
+                       const double* r, double* x, void* workspace, size_t workspace_bytes, void* stream) {
+  if (!levels_ok(levels, n_levels) || !r || !x || deg < 1 || cdeg < 1 || !(omega > 0.0)) return FGB_ERR_ARG;
+  if (!workspace || workspace_bytes < fgb_amg_workspace_bytes(levels, n_levels)) return FGB_ERR_WORKSPACE;
+  Carver cv(workspace, workspace_bytes);
+  LevelVecs V[FGB_AMG_MAX_LEVELS];
+  for (int l = 0; l < n_levels; ++l) V[l] = carve_level(cv, levels[l].n);
+  if (!cv.ok) return FGB_ERR_WORKSPACE;
+  return vcycle(levels, n_levels, r, x, deg, cdeg, omega, V, as_stream(stream));
+}
+
+int32_t fgb_pcg_amg(const fgb_amg_level* levels, int32_t n_levels, int32_t deg, int32_t cdeg, double omega,
+                    const double* b, double* x, double atol, double rtol, int64_t maxit, int32_t norm,
+                    fgb_pcg_info* info, void* workspace, size_t workspace_bytes, void* stream) {
+  if (!levels_ok(levels, n_levels) || !b || !x || deg < 1 || cdeg < 1 || !(omega > 0.0) || maxit <= 0)
+    return FGB_ERR_ARG;
+  if (!workspace || workspace_bytes < fgb_amg_workspace_bytes(levels, n_levels)) return FGB_ERR_WORKSPACE;
+  cudaStream_t st = as_stream(stream);
+  Carver cv(workspace, workspace_bytes);
+  LevelVecs V[FGB_AMG_MAX_LEVELS];
+  for (int l = 0; l < n_levels; ++l) V[l] = carve_level(cv, levels[l].n);
+  const fgb_amg_level& L = levels[0];
+  const int64_t n = L.n;
+  double* r = cv.take<double>(n);
+  double* z = cv.take<double>(n);
+  double* p = cv.take<double>(n);
+  double* Ap = cv.take<double>(n);
+  double* partials = cv.take<double>(2 * kMaxGrid);
+  double* out = cv.take<double>(8);
+  unsigned int* counter = cv.take<unsigned int>(4);
+  if (!cv.ok) return FGB_ERR_WORKSPACE;
+  if (cudaMemsetAsync(counter, 0, 4 * sizeof(unsigned int), st) != cudaSuccess) return FGB_ERR_CUDA;
+  const int G = amg_lanes(n, L.nnz);
+  double h[8];
+  auto read = [&](int k) -> int {
+    if (cudaMemcpyAsync(h, out, 8 * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess) return FGB_ERR_CUDA;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return FGB_ERR_CUDA;
+    (void)k;
+    return FGB_OK;
+  };
+  int64_t launches = 0, niter = 0;
+  int reason = FGB_PCG_RUNNING;
+  double resid = 0.0;
+  // ||b||, r = b - A x, z = M r, rz
+  amg_dot2<<<kDotBlocks, kAmgThreads, 0, st>>>(n, b, b, partials, counter, out);
+  int rc = read(0);
+  if (rc) return rc;
+  const double bnorm = sqrt(h[0]);
+  if (bnorm < 1e-15) {
+    if (cudaMemsetAsync(x, 0, n * sizeof(double), st) != cudaSuccess) return FGB_ERR_CUDA;
+    reason = FGB_PCG_ZERO_RHS;
+  } else {
+    AMG_DISPATCH_G(G, amg_residual, n, L.indptr, L.indices, L.values, b, x, r);
+    if ((rc = vcycle(levels, n_levels, r, z, deg, cdeg, omega, V, st))) return rc;
+    if (cudaMemcpyAsync(p, z, n * sizeof(double), cudaMemcpyDeviceToDevice, st) != cudaSuccess) return FGB_ERR_CUDA;
+    amg_dot2<<<kDotBlocks, kAmgThreads, 0, st>>>(n, r, z, partials, counter, out);
+    if ((rc = read(0))) return rc;
+    double rz = h[0];
+    const double tol = rtol * bnorm;
+    while (true) {
+      AMG_DISPATCH_G(G, amg_pcg_spmv, n, L.indptr, L.indices, L.values, p, Ap, partials, counter, out);
+      if ((rc = read(0))) return rc;
+      const double pap = h[0];
+      if (!(pap > 0.0) || !std::isfinite(pap)) {
+        reason = std::isfinite(pap) ? FGB_PCG_BREAKDOWN : FGB_PCG_NONFINITE;
+        break;
+      }
+      const double alpha = rz / pap;
+      amg_pcg_update<<<kDotBlocks, kAmgThreads, 0, st>>>(n, alpha, p, Ap, x, r, partials, counter, out + 2);
+      if ((rc = vcycle(levels, n_levels, r, z, deg, cdeg, omega, V, st))) return rc;
+      amg_dot2<<<kDotBlocks, kAmgThreads, 0, st>>>(n, r, z, partials, counter, out + 4);
+      if ((rc = read(0))) return rc;
+      const double rr = h[2], rz_new = h[4];
+      ++niter;
+      resid = norm ? sqrt(rr) : sqrt(fabs(rz_new));
+      if (!std::isfinite(resid)) {
+        reason = FGB_PCG_NONFINITE;
+        break;
+      }
+      if (resid < atol) { reason = FGB_PCG_ATOL; break; }
+      if (resid < tol) { reason = FGB_PCG_RTOL; break; }
+      if (niter >= maxit) { reason = FGB_PCG_MAXIT; break; }
+      const double beta = rz_new / rz;
+      amg_pupdate<<<vec_grid(n), kAmgThreads, 0, st>>>(n, beta, z, p);
+      rz = rz_new;
+      launches += 4;
+    }
+  }
+  if (cudaStreamSynchronize(st) != cudaSuccess) return FGB_ERR_CUDA;
+  if (info) {
+    memset(info, 0, sizeof(*info));
+    info->niter = niter;
+    info->residual = resid;
+    info->b_norm = bnorm;
+    info->true_relres = -1.0;
+    info->reason = reason;
+    info->launches = launches;
+  }
+  if (reason == FGB_PCG_BREAKDOWN) return FGB_ERR_BREAKDOWN;
+  if (reason == FGB_PCG_NONFINITE) return FGB_ERR_NONFINITE;
+  return launch_status();
+}
+
+}  // extern "C"

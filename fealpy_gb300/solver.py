@@ -36,7 +36,8 @@ def _diag_inv_of(M):
         return None
     if isinstance(M, CSRTensor) and M.is_diagonal():
         return M.values.contiguous()
-    raise NotImplementedError("cg on the GB300 path takes M=None or a diagonal CSRTensor (Jacobi)")
+    raise NotImplementedError("cg on the GB300 path takes M=None, a diagonal CSRTensor (Jacobi) or a GAMGSolver "
+                              "hierarchy")
 
 
 def _info_dict(info, extra=None):
@@ -134,6 +135,14 @@ def cg(A, b: torch.Tensor, x0: Optional[torch.Tensor] = None, M=None, *, batch_f
         raise NotImplementedError("multi-right-hand-side cg is not provided on the GB300 path")
     if stop not in ("preconditioned", "residual"):
         raise ValueError("stop must be 'preconditioned' or 'residual'")
+    from .amg import GAMGSolver
+    if isinstance(M, GAMGSolver):
+        # multigrid preconditioner: the whole PCG loop in the library
+        x, info = M.pcg(b, x0=x0, atol=atol, rtol=rtol, maxit=maxit if maxit is not None else 2 ** 62,
+                        norm=0 if stop == "preconditioned" else 1)
+        out = {"residual": info.residual, "niter": int(info.niter), "reason": int(info.reason),
+               "launches": int(info.launches), "graph": False, "persistent": False, "amg_levels": len(M.levels)}
+        return (x, out) if returninfo else x
     dinv = _diag_inv_of(M)
     b = b.to(dtype=torch.float64).contiguous()
     x = torch.zeros_like(b) if x0 is None else x0.to(torch.float64).clone()

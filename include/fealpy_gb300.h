@@ -485,6 +485,69 @@ int32_t fgb_pcg_sell_mixed_ex(const fgb_sell* A, const double* diag_inv64, const
                               int64_t barrier_polls, void* workspace, size_t workspace_bytes,
                               fgb_pcg_info* info_host, void* stream);
 
+/* ---- aggregation AMG preconditioner -------------------------------------- */
+
+/* The `M` slot of fealpy/solver/cg.py filled with a multigrid V-cycle, the
+ * role of FEALPy's GAMGSolver (fealpy/solver/gamg_solver.py:14-256, a
+ * Ruge-Stuben hierarchy with Gauss-Seidel smoothing).  Here, with data-
+ * parallel counterparts: aggregation by a distance-2 maximal independent set
+ * of the graph of entries |a_ij| > theta sqrt(|a_ii a_jj|) (rows without such
+ * entries, e.g. Dirichlet rows, join no aggregate), Galerkin coarse matrices
+ * P^T A P for the aggregate indicator P, Chebyshev smoothing with D^-1 and
+ * the Gershgorin bound lmax of D^-1 A, coarse corrections scaled by omega,
+ * a Chebyshev solve on the coarsest level.  FP64.  No FEALPy counterpart for
+ * the individual kernels.
+ *
+ * One level (caller-owned arrays; agg, member_ptr, members and n_coarse for
+ * every level but the coarsest). */
+#define FGB_AMG_MAX_LEVELS 16
+typedef struct fgb_amg_level {
+  int64_t n, nnz;
+  const int64_t* indptr;    /* CSR of the level's matrix                      */
+  const int32_t* indices;
+  const double* values;
+  const double* dinv;       /* 1 / a_ii                                       */
+  double lmax;              /* Gershgorin bound of D^-1 A                     */
+  const int32_t* agg;       /* aggregate of every row, -1: none               */
+  int64_t n_coarse;         /* aggregates = rows of the next level            */
+  const int64_t* member_ptr; /* n_coarse + 1: rows of each aggregate,         */
+  const int32_t* members;    /* ascending                                     */
+} fgb_amg_level;
+
+/* Aggregates of a level: agg (n), their number, dinv (n) and lmax. */
+size_t fgb_amg_setup_workspace_bytes(int64_t n);
+int32_t fgb_amg_aggregate(int64_t n, const int64_t* indptr, const int32_t* indices,
+                          const double* values, double theta, int32_t* agg, int64_t* n_agg_host,
+                          double* dinv, double* lmax_host, int32_t* status, void* workspace,
+                          size_t workspace_bytes, void* stream);
+/* The next level: member lists and the coarse row pointer (count, which
+ * returns its nnz on the host), then its columns and values (fill, same
+ * workspace).  Columns ascending; every coarse value is the sum of its fine
+ * entries taken member row by member row, in CSR order. */
+size_t fgb_amg_coarse_workspace_bytes(int64_t n, int64_t n_coarse);
+int32_t fgb_amg_coarse_count(int64_t n, const int64_t* indptr, const int32_t* indices,
+                             const double* values, const int32_t* agg, int64_t n_coarse,
+                             int64_t* member_ptr, int32_t* members, int64_t* coarse_indptr,
+                             int64_t* nnz_host, int32_t* status, void* workspace,
+                             size_t workspace_bytes, void* stream);
+int32_t fgb_amg_coarse_fill(int64_t n, const int64_t* indptr, const int32_t* indices,
+                            const double* values, const int32_t* agg, int64_t n_coarse,
+                            const int64_t* member_ptr, const int32_t* members,
+                            const int64_t* coarse_indptr, int32_t* coarse_indices,
+                            double* coarse_values, int32_t* status, void* workspace,
+                            size_t workspace_bytes, void* stream);
+/* x = V-cycle(r) (x = 0 start; deg: smoothing degree, cdeg: degree of the
+ * coarsest solve) and PCG with it (FEALPy's recurrence and stopping rule;
+ * norm 0: sqrt(r.z), 1: ||r||; info->true_relres = -1). */
+size_t fgb_amg_workspace_bytes(const fgb_amg_level* levels, int32_t n_levels);
+int32_t fgb_amg_vcycle(const fgb_amg_level* levels, int32_t n_levels, int32_t deg, int32_t cdeg,
+                       double omega, const double* r, double* x, void* workspace,
+                       size_t workspace_bytes, void* stream);
+int32_t fgb_pcg_amg(const fgb_amg_level* levels, int32_t n_levels, int32_t deg, int32_t cdeg,
+                    double omega, const double* b, double* x, double atol, double rtol, int64_t maxit,
+                    int32_t norm, fgb_pcg_info* info_host, void* workspace, size_t workspace_bytes,
+                    void* stream);
+
 /* ---- batched FP32-refined Jacobi-PCG over many systems ------------------ */
 
 /* No FEALPy counterpart: FEALPy solves one system per fealpy/solver/cg.py
