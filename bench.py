@@ -187,9 +187,15 @@ def solve_step(torch, F, space, kappa, bc, mode, profile=False, marks=None, asm_
     mark()
     A2, F2 = bc.apply(A, Fv)
     mark()
-    _sell_of(A2, want32=(mode != "fp64"))
+    if mode != "amg":
+        _sell_of(A2, want32=(mode != "fp64"))
     mark()
-    if mode != "fp64":
+    if mode == "amg":
+        # FP64 PCG preconditioned by the aggregation AMG V-cycle (set-up inside the step)
+        M = F.GAMGSolver().setup(A2)
+        x, info = F.cg(A2, F2, M=M, atol=0.0, rtol=RTOL, maxit=MAXIT, returninfo=True, stop="residual")
+        info["amg_levels_n"] = [L.n for L in M.levels]
+    elif mode != "fp64":
         x, info = F.cg_mixed(A2, F2, rtol=RTOL, maxit=MAXIT, returninfo=True, profile=profile, graph=graph)
     else:
         M = F.JacobiPreconditioner().apply(A2)
@@ -321,13 +327,14 @@ def run_ours(args):
         stages = {name: marks[k].elapsed_time(marks[k + 1]) for k, name in enumerate(STAGES)}
         for k in range(1, len(amarks)):
             stages["assembly/" + amarks[k][0]] = amarks[k - 1][1].elapsed_time(amarks[k][1])
-        kms = pinfo["kernel_ms"]
-        kl = pinfo["kernel_launches"]
+        kms = pinfo.get("kernel_ms", 0.0)
+        kl = pinfo.get("kernel_launches", 0)
         results[mode] = {"ms": ms, "ms_per_step": ms / args.steps, "x": x, "relres": relres,
                          "niter": infos[-1]["niter"], "n_updates": infos[-1].get("n_updates", 0),
                          "kernel_ms_avg": kms / max(kl, 1), "kernel_launches": kl, "launches": launches,
-                         "other_ms_avg": pinfo["other_ms"] / max(kl, 1),
-                         "extra_ms_avg": pinfo["extra_ms"] / max(kl, 1), "stages_ms": stages,
+                         "other_ms_avg": pinfo.get("other_ms", 0.0) / max(kl, 1),
+                         "extra_ms_avg": pinfo.get("extra_ms", 0.0) / max(kl, 1), "stages_ms": stages,
+                         "amg_levels": infos[-1].get("amg_levels_n"),
                          "clocks": clocks, "nnz": A2.nnz, "n": gdof,
                          "sell_launch": list(A2._sell.launch) if getattr(A2, "_sell", None) is not None else None,
                          "sell_cols": A2._sell.cols if getattr(A2, "_sell", None) is not None else None,
@@ -452,6 +459,13 @@ def run_ours(args):
                      "other_kernels_us": fp64["extra_ms_avg"] * 1e3,
                      "sell_launch_threads_blocks": fp64["sell_launch"], "sell_columns": fp64["sell_cols"]},
             "speedup_fp32_refined_vs_fp64": fp64["ms_per_step"] / mixed["ms_per_step"],
+            "fp64_amg": None if "amg" not in results else {
+                "preconditioner": "aggregation AMG V-cycle (GAMGSolver; set-up inside the step), FP64",
+                "ms_per_step": results["amg"]["ms_per_step"],
+                "dof_per_s": world * gdof / (results["amg"]["ms_per_step"] / 1e3),
+                "cg_iters": results["amg"]["niter"], "true_relres": results["amg"]["relres"],
+                "levels_rows": results["amg"]["amg_levels"], "stages_ms": results["amg"]["stages_ms"],
+                "speedup_vs_fp64_jacobi": fp64["ms_per_step"] / results["amg"]["ms_per_step"]},
             "e2e": {"value": world * gdof * e2e_steps / (e2e_ms / 1e3), "unit": "DOF/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "steps": e2e_steps},
             "gpu_launches": mixed["launches"],
@@ -968,7 +982,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=64)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--modes", default="fp64,mixed,mixed64",
+    ap.add_argument("--modes", default="fp64,mixed,mixed64,amg",
                     help="solver modes to time (a single-mode run is for profiling and prints no JSON line)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--no-graph", action="store_true",

@@ -48,7 +48,8 @@ PCG_REASONS = {0: "running", 1: "atol", 2: "rtol", 3: "maxit", 4: "zero rhs", 5:
 class AmgLevel(ctypes.Structure):
     """``fgb_amg_level`` (include/fealpy_gb300.h)."""
     _fields_ = [("n", c_i64), ("nnz", c_i64), ("indptr", c_vp), ("indices", c_vp), ("values", c_vp), ("dinv", c_vp),
-                ("lmax", c_dbl), ("agg", c_vp), ("n_coarse", c_i64), ("member_ptr", c_vp), ("members", c_vp)]
+                ("lmax", c_dbl), ("agg", c_vp), ("n_coarse", c_i64), ("member_ptr", c_vp), ("members", c_vp),
+                ("values32", c_vp), ("dinv32", c_vp)]
 
 
 class PcgInfo(ctypes.Structure):

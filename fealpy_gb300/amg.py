@@ -5,8 +5,8 @@ interface of FEALPy's ``GAMGSolver`` (``fealpy/solver/gamg_solver.py:14-256``:
 
 FEALPy builds a Ruge-Stuben hierarchy and smooths with Gauss-Seidel sweeps,
 both sequential algorithms.  The GB300 hierarchy is built and applied by the
-library's kernels (``csrc/amg.cu``): distance-2 maximal-independent-set
-aggregation, Galerkin coarse matrices of the aggregate indicator (summed in a
+library's kernels (``csrc/amg.cu``): maximal-independent-set aggregation
+(a root and its neighbours), Galerkin coarse matrices of the aggregate indicator (summed in a
 fixed order: the hierarchy and every V-cycle are deterministic), Chebyshev
 smoothing with the diagonal, coarse corrections scaled by ``omega``, and a
 Chebyshev solve on the coarsest level.  Each V-cycle is a fixed symmetric
@@ -33,7 +33,7 @@ class _Level:
         self.nnz = indices.numel()
         self.dinv = None
         self.lmax = 0.0
-        self.agg = self.member_ptr = self.members = None
+        self.agg = self.member_ptr = self.members = self.values32 = self.dinv32 = None
         self.n_coarse = 0
 
 
@@ -47,11 +47,14 @@ class GAMGSolver:
     each smoothing), ``isolver`` ('CG': PCG with the V-cycle, 'MG': V-cycle
     iterations), ``maxit``, ``rtol``, ``atol``.  GB300 additions: ``omega``
     (coarse-correction scale, plain aggregation needs > 1), ``cdeg`` (degree
-    of the coarsest Chebyshev solve), ``max_levels``."""
+    of the coarsest Chebyshev solve), ``max_levels``, ``vcycle_f32`` (the
+    V-cycle runs in FP32 on FP32 copies of the level matrices; the PCG
+    operator and its vectors stay FP64)."""
 
     def __init__(self, theta: float = 0.0, csize: int = 300, ctype: str = "A", itype: str = "T", ptype: str = "V",
                  sstep: int = 3, isolver: str = "CG", maxit: int = 200, csolver: str = "chebyshev",
-                 rtol: float = 1e-8, atol: float = 1e-8, omega: float = 1.7, cdeg: int = 16, max_levels: int = 10):
+                 rtol: float = 1e-8, atol: float = 1e-8, omega: float = 1.7, cdeg: int = 16, max_levels: int = 10,
+                 vcycle_f32: bool = True):
         if ptype != "V":
             raise NotImplementedError("the GB300 multigrid provides V-cycles")
         if isolver not in ("CG", "MG"):
@@ -59,6 +62,7 @@ class GAMGSolver:
         self.theta, self.csize, self.ptype, self.sstep = float(theta), int(csize), ptype, int(sstep)
         self.isolver, self.maxit, self.rtol, self.atol = isolver, int(maxit), float(rtol), float(atol)
         self.omega, self.cdeg, self.max_levels = float(omega), int(cdeg), int(max_levels)
+        self.vcycle_f32 = bool(vcycle_f32)
         self.levels: List[_Level] = []
         self._desc = None
         self.A = None
@@ -93,7 +97,9 @@ class GAMGSolver:
             lev.lmax = float(lmax.value)
             nc = int(nagg.value)
             self.levels.append(lev)
-            last = (n <= self.csize or len(self.levels) >= self.max_levels or nc == 0 or nc > 0.8 * n)
+            # a level that shrinks by less than half adds sweeps and no
+            # convergence: the current one is then the coarsest
+            last = (n <= self.csize or len(self.levels) >= self.max_levels or nc == 0 or nc > 0.5 * n)
             if last:
                 lev.agg = None
                 break
@@ -113,6 +119,9 @@ class GAMGSolver:
                  cws.numel(), s)
             check_status_word("multigrid coarse matrix (aggregate rows above the candidate capacity)", st)
             lev = _Level(cptr, ccol[: int(nnz.value)], cval[: int(nnz.value)])
+        for L in self.levels:
+            L.values32 = L.values.to(torch.float32) if self.vcycle_f32 else None
+            L.dinv32 = L.dinv.to(torch.float32) if self.vcycle_f32 else None
         self._desc = (_lib.AmgLevel * len(self.levels))()
         for k, L in enumerate(self.levels):
             d = self._desc[k]
@@ -120,6 +129,8 @@ class GAMGSolver:
             d.indptr, d.indices, d.values, d.dinv = (L.indptr.data_ptr(), L.indices.data_ptr(), L.values.data_ptr(),
                                                     L.dinv.data_ptr())
             d.lmax = L.lmax
+            d.values32 = L.values32.data_ptr() if L.values32 is not None else None
+            d.dinv32 = L.dinv32.data_ptr() if L.dinv32 is not None else None
             if L.agg is not None:
                 d.agg, d.n_coarse = L.agg.data_ptr(), L.n_coarse
                 d.member_ptr, d.members = L.member_ptr.data_ptr(), L.members.data_ptr()

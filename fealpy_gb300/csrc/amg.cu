@@ -5,16 +5,20 @@
 // algorithms, so the GPU version uses their data-parallel counterparts).
 //
 // Set-up of one level (integer work, deterministic):
-//   aggregation  a distance-2 maximal independent set of the matrix graph
-//                (off-diagonal entries with |a_ij| > theta sqrt(|a_ii a_jj|)):
-//                every node carries a key (state, hash priority, index); two
-//                neighbourhood-max sweeps find the nodes whose key is the
-//                largest within distance 2, which become roots; nodes with a
-//                root within distance 2 drop out; repeat until every node is
-//                decided.  Roots are numbered in index order; the other nodes
-//                join the aggregate of their strongest-keyed assigned
-//                neighbour, in two sweeps.  Rows without off-diagonal entries
-//                (Dirichlet rows) join no aggregate.
+//   aggregation  a maximal independent set of the matrix graph (off-diagonal
+//                entries with |a_ij| > theta sqrt(|a_ii a_jj|)): every node
+//                carries a key (state, hash priority, index); a
+//                neighbourhood-max sweep finds the undecided nodes whose key
+//                is the largest among their neighbours, which become roots;
+//                their neighbours drop out; repeat until every node is
+//                decided.  Roots are numbered in index order; every other
+//                node joins the aggregate of its largest-keyed assigned
+//                neighbour (one sweep reaches all of them: each dropped node
+//                has a root neighbour).  Rows without off-diagonal entries
+//                (Dirichlet rows) join no aggregate.  Distance-1 independence
+//                keeps aggregates at a root and its neighbours, about a dozen
+//                rows for Lagrange matrices of degree 2; a distance-2 set makes
+//                aggregates of about fifty and more PCG iterations.
 //   coarse matrix  A_c = P^T A P with P the aggregate indicator: the members
 //                of every aggregate (counting sort, each list sorted), and per
 //                coarse row the entries of the member rows mapped to their
@@ -28,12 +32,16 @@
 // plain aggregation needs); the same smoothing after; on the coarsest level
 // a Chebyshev solve of degree `cdeg` on [lmax/20, lmax].  Every step is a
 // fixed linear map, symmetric in A, so the V-cycle is a valid CG
-// preconditioner.
+// preconditioner.  The V-cycle reads the FP32 copy of a level's values when
+// the level carries one (half the value bytes of the dominant sweeps; the
+// rounded matrix is still symmetric, so the V-cycle stays a symmetric map);
+// vectors and the PCG operator stay FP64.
 
 #include "fgb_common.cuh"
 
 #include <climits>
 #include <cmath>
+#include <type_traits>
 #include <vector>
 
 namespace fgb {
@@ -56,49 +64,84 @@ __device__ __forceinline__ unsigned long long amg_key(int rank, int64_t i) {
          static_cast<unsigned long long>(i);
 }
 
-__device__ __forceinline__ bool amg_strong(double aij, double dii, double djj, double theta) {
-  return aij != 0.0 && fabs(aij) > theta * sqrt(fabs(dii * djj));
+// Strong coupling of entry (i, j): with theta = 0 every nonzero (no diagonal
+// read); otherwise |a_ij| > theta sqrt(|a_ii a_jj|).
+__device__ __forceinline__ bool amg_strong_at(double aij, double dii, const double* __restrict__ diag, int32_t j,
+                                              double theta) {
+  if (aij == 0.0) return false;
+  if (theta == 0.0) return true;
+  return fabs(aij) > theta * sqrt(fabs(dii * diag[j]));
 }
 
-template <typename T>
+// Rows in groups of 32 / G per warp (G lanes per row, G in {4, 8, 16, 32});
+// the trip count is the same for every lane of a warp (the bound is tested
+// on the warp's first row), so full-warp shuffles always have all 32 lanes
+// present; rows past n take part with active = false.
+#define AMG_ROW_LOOP(n, G)                                                                                   \
+  const int sub = threadIdx.x & ((G) - 1);                                                                   \
+  const int64_t wfirst = ((blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5) * (32 / (G));  \
+  const int64_t wstep = ((static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5) * (32 / (G));                  \
+  for (int64_t wr = wfirst, i = wfirst + (threadIdx.x & 31) / (G); wr < (n); wr += wstep, i += wstep)
+
+template <int G, typename T>
+__device__ __forceinline__ T group_max(T v) {
+#pragma unroll
+  for (int o = G >> 1; o > 0; o >>= 1) {
+    const T u = __shfl_xor_sync(0xffffffffu, v, o, G);
+    v = u > v ? u : v;
+  }
+  return v;
+}
+
+// diag and the Gershgorin bound of D^-1 A (G lanes per row)
+template <int G>
 __global__ void amg_diag_kernel(int64_t n, const int64_t* __restrict__ indptr, const int32_t* __restrict__ indices,
-                                const T* __restrict__ values, double* __restrict__ diag, int32_t* __restrict__ has_off,
+                                const double* __restrict__ values, double* __restrict__ diag,
                                 unsigned long long* __restrict__ bound_bits, int32_t* status) {
-  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
-       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+  AMG_ROW_LOOP(n, G) {
+    const bool active = i < n;
     double d = 0.0, s = 0.0;
-    int off = 0;
-    for (int64_t e = indptr[i]; e < indptr[i + 1]; ++e) {
-      const double a = static_cast<double>(values[e]);
-      const int32_t j = indices[e];
-      if (j == i) d += a;
-      else if (a != 0.0) off = 1;
-      s += fabs(a);
+    if (active)
+      for (int64_t e = indptr[i] + sub; e < indptr[i + 1]; e += G) {
+        const double a = values[e];
+        if (indices[e] == i) d += a;
+        s += fabs(a);
+      }
+#pragma unroll
+    for (int o = G >> 1; o > 0; o >>= 1) {
+      d += __shfl_xor_sync(0xffffffffu, d, o, G);
+      s += __shfl_xor_sync(0xffffffffu, s, o, G);
     }
-    diag[i] = d;
-    has_off[i] = off;
-    if (!(d > 0.0) || !isfinite(d)) {
-      set_status(status, FGB_ERR_BREAKDOWN);  // an SPD matrix has a positive diagonal
-      continue;
+    if (active && sub == 0) {
+      diag[i] = d;
+      if (!(d > 0.0) || !isfinite(d)) {
+        set_status(status, FGB_ERR_BREAKDOWN);  // an SPD matrix has a positive diagonal
+      } else {
+        const double b = s / d;
+        atomicMax(bound_bits, static_cast<unsigned long long>(__double_as_longlong(b)));  // positive doubles order as ints
+      }
     }
-    const double b = s / d;
-    atomicMax(bound_bits, static_cast<unsigned long long>(__double_as_longlong(b)));  // positive doubles order as ints
   }
 }
 
 // state: 1 undecided, 2 root, 0 out, -1 isolated (no strong off-diagonal)
+template <int G>
 __global__ void amg_init_state(int64_t n, const int64_t* __restrict__ indptr, const int32_t* __restrict__ indices,
                                const double* __restrict__ values, const double* __restrict__ diag, double theta,
                                int32_t* __restrict__ state) {
-  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
-       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+  AMG_ROW_LOOP(n, G) {
+    const bool active = i < n;
     int strong = 0;
-    for (int64_t e = indptr[i]; e < indptr[i + 1] && !strong; ++e) {
-      const int32_t j = indices[e];
-      if (j < 0 || j >= n) continue;
-      if (j != i && amg_strong(values[e], diag[i], diag[j], theta)) strong = 1;
+    if (active) {
+      const double di = diag[i];
+      for (int64_t e = indptr[i] + sub; e < indptr[i + 1]; e += G) {
+        const int32_t j = indices[e];
+        if (j < 0 || j >= n || j == i) continue;
+        if (amg_strong_at(values[e], di, diag, j, theta)) strong = 1;
+      }
     }
-    state[i] = strong ? 1 : -1;
+    strong = group_max<G>(strong);
+    if (active && sub == 0) state[i] = strong ? 1 : -1;
   }
 }
 
@@ -110,38 +153,38 @@ __global__ void amg_keys(int64_t n, const int32_t* __restrict__ state, unsigned 
   }
 }
 
-// out[i] = max of src over i and its strong neighbours
-__global__ void amg_nbmax(int64_t n, const int64_t* __restrict__ indptr, const int32_t* __restrict__ indices,
-                          const double* __restrict__ values, const double* __restrict__ diag, double theta,
-                          const int32_t* __restrict__ state, const unsigned long long* __restrict__ src,
-                          unsigned long long* __restrict__ out) {
-  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
-       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-    unsigned long long m = src[i];
-    if (state[i] >= 0) {
-      for (int64_t e = indptr[i]; e < indptr[i + 1]; ++e) {
+// One maximal-independent-set round: m = max of key over the strong
+// neighbours of i; an undecided node whose own key exceeds it becomes a root,
+// one that sees a root drops out; counts the nodes still undecided.  Reads
+// only the keys of the round (written by amg_keys before), so the result does
+// not depend on the order of the threads.
+template <int G>
+__global__ void amg_mis_round(int64_t n, const int64_t* __restrict__ indptr, const int32_t* __restrict__ indices,
+                              const double* __restrict__ values, const double* __restrict__ diag, double theta,
+                              const unsigned long long* __restrict__ key, int32_t* __restrict__ state,
+                              int32_t* __restrict__ undecided) {
+  int local = 0;
+  AMG_ROW_LOOP(n, G) {
+    const bool active = i < n && state[i] == 1;  // uniform within the row's lanes
+    unsigned long long m = 0ull;
+    if (active) {
+      const double di = diag[i];
+      for (int64_t e = indptr[i] + sub; e < indptr[i + 1]; e += G) {
         const int32_t j = indices[e];
-        if (j < 0 || j >= n) continue;
-        if (j != i && amg_strong(values[e], diag[i], diag[j], theta)) {
-          const unsigned long long v = src[j];
+        if (j < 0 || j >= n || j == i) continue;
+        if (amg_strong_at(values[e], di, diag, j, theta)) {
+          const unsigned long long v = key[j];
           m = v > m ? v : m;
         }
       }
     }
-    out[i] = m;
-  }
-}
-
-__global__ void amg_mis_update(int64_t n, const unsigned long long* __restrict__ key,
-                               const unsigned long long* __restrict__ m2, int32_t* __restrict__ state,
-                               int32_t* __restrict__ undecided) {
-  int local = 0;
-  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
-       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-    if (state[i] != 1) continue;
-    if (m2[i] == key[i]) state[i] = 2;
-    else if ((m2[i] >> 62) == 2ull) state[i] = 0;
-    else ++local;
+    m = group_max<G>(m);
+    if (active && sub == 0) {
+      const unsigned long long k = key[i];
+      if (k > m) state[i] = 2;
+      else if ((m >> 62) == 2ull) state[i] = 0;
+      else ++local;
+    }
   }
   if (local) atomicAdd(undecided, local);
 }
@@ -163,30 +206,36 @@ __global__ void amg_root_ids(int64_t n, const int32_t* __restrict__ state, const
 // aggregate of the assigned strong neighbour with the largest (priority,
 // index); reads agg_in, writes agg_out (so the sweep does not depend on the
 // order of the threads); counts the nodes still unassigned.
+template <int G>
 __global__ void amg_assign(int64_t n, const int64_t* __restrict__ indptr, const int32_t* __restrict__ indices,
                            const double* __restrict__ values, const double* __restrict__ diag, double theta,
                            const int32_t* __restrict__ state, const int32_t* __restrict__ agg_in,
                            int32_t* __restrict__ agg_out, int32_t* __restrict__ left) {
   int local = 0;
-  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
-       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-    int32_t a = agg_in[i];
-    if (a < 0 && state[i] >= 0) {
-      unsigned long long best = 0ull;
-      int32_t pick = -1;
-      for (int64_t e = indptr[i]; e < indptr[i + 1]; ++e) {
+  AMG_ROW_LOOP(n, G) {
+    const bool active = i < n;
+    const int32_t a0 = active ? agg_in[i] : 0;
+    const bool need = active && a0 < 0 && state[i] >= 0;  // uniform within the row's lanes
+    // best assigned neighbour as amg_key(1, j): nonzero when found
+    unsigned long long best = 0ull;
+    if (need) {
+      const double di = diag[i];
+      for (int64_t e = indptr[i] + sub; e < indptr[i + 1]; e += G) {
         const int32_t j = indices[e];
-        if (j < 0 || j >= n || j == i || agg_in[j] < 0 || !amg_strong(values[e], diag[i], diag[j], theta)) continue;
-        const unsigned long long k = amg_key(0, j);
-        if (pick < 0 || k > best) {
-          best = k;
-          pick = agg_in[j];
-        }
+        if (j < 0 || j >= n || j == i || agg_in[j] < 0 || !amg_strong_at(values[e], di, diag, j, theta)) continue;
+        const unsigned long long k = amg_key(1, j);
+        best = k > best ? k : best;
       }
-      a = pick;
-      if (a < 0) ++local;
     }
-    agg_out[i] = a;
+    best = group_max<G>(best);
+    if (active && sub == 0) {
+      int32_t a = a0;
+      if (need) {
+        a = best ? agg_in[static_cast<int32_t>(best & 0x7fffffffull)] : -1;
+        if (a < 0) ++local;
+      }
+      agg_out[i] = a;
+    }
   }
   if (local) atomicAdd(left, local);
 }
@@ -297,26 +346,46 @@ __device__ bool amg_coarse_row(int64_t n, int64_t I, int mode, const int64_t* __
       __syncthreads();
     }
   }
-  // distinct coarse columns (entries with J < 0 sorted last as ULLONG_MAX)
-  if (tid == 0) {
-    int u = 0;
-    const int64_t out0 = mode == 1 ? cptr[I] : 0;
-    int t = 0;
-    while (t < m && kbuf[t] != ULLONG_MAX) {
-      const uint32_t J = static_cast<uint32_t>(kbuf[t] >> 32);
+  // distinct coarse columns (entries with J < 0 sorted last as ULLONG_MAX):
+  // thread tid owns the sorted positions [tid * chunk, (tid + 1) * chunk),
+  // counts the run heads there, takes its output offset from a block scan of
+  // the counts, and sums each of its runs serially in position order (a run
+  // may extend past the chunk), which is the order of a serial merge.
+  const int chunk = (m + nt - 1) / nt;
+  const int t0 = min(m, tid * chunk), t1 = min(m, t0 + chunk);
+  auto head = [&](int t) -> bool {
+    const unsigned long long k = kbuf[t];
+    return k != ULLONG_MAX && (t == 0 || (kbuf[t - 1] >> 32) != (k >> 32));
+  };
+  int heads = 0;
+  for (int t = t0; t < t1; ++t) heads += head(t) ? 1 : 0;
+  // exclusive block scan of heads (warp scans, then the warp totals)
+  const int lane = tid & 31, wid = tid >> 5;
+  int incl = heads;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int u = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += u;
+  }
+  int* wsum = sh_u + 1;  // nt / 32 ints after sh_u
+  if (lane == 31) wsum[wid] = incl;
+  __syncthreads();
+  int base = 0;
+  for (int w = 0; w < wid; ++w) base += wsum[w];
+  int u = base + incl - heads;
+  if (mode == 1) {
+    const int64_t out0 = cptr[I];
+    for (int t = t0; t < t1; ++t) {
+      if (!head(t)) continue;
+      const unsigned long long J = kbuf[t] >> 32;
       double s = 0.0;
-      while (t < m && kbuf[t] != ULLONG_MAX && static_cast<uint32_t>(kbuf[t] >> 32) == J) {
-        s += vbuf[t];
-        ++t;
-      }
-      if (mode == 1) {
-        ccol[out0 + u] = static_cast<int32_t>(J);
-        cval[out0 + u] = s;
-      }
+      for (int q = t; q < m && kbuf[q] != ULLONG_MAX && (kbuf[q] >> 32) == J; ++q) s += vbuf[q];
+      ccol[out0 + u] = static_cast<int32_t>(J);
+      cval[out0 + u] = s;
       ++u;
     }
-    if (mode == 0) cnt[I] = u;
   }
+  if (mode == 0 && tid == nt - 1) cnt[I] = base + incl;
   __syncthreads();
   return true;
 }
@@ -334,10 +403,10 @@ __global__ void __launch_bounds__(kCoarseThreads) amg_coarse_rows(int64_t n, int
                                                                  int32_t* __restrict__ ovf, int32_t* __restrict__ ovf_len) {
   __shared__ unsigned long long kbuf[kCoarseCap];
   __shared__ double vbuf[kCoarseCap];
-  __shared__ int sh_m, sh_u;
+  __shared__ int sh[2 + kCoarseThreads / 32];  // candidate count, fill offset, warp totals
   for (int64_t I = blockIdx.x; I < nc; I += gridDim.x) {
     const bool ok = amg_coarse_row(n, I, mode, indptr, indices, values, agg, mptr, members, cnt, cptr, ccol, cval, kbuf,
-                                   vbuf, kCoarseCap, &sh_m, &sh_u);
+                                   vbuf, kCoarseCap, sh, sh + 1);
     if (!ok && threadIdx.x == 0) ovf[atomicAdd(ovf_len, 1)] = static_cast<int32_t>(I);
     __syncthreads();
   }
@@ -360,11 +429,11 @@ __global__ void __launch_bounds__(kCoarseThreads) amg_coarse_rows_big(int64_t n,
   extern __shared__ __align__(16) unsigned char dsm[];
   unsigned long long* kbuf = reinterpret_cast<unsigned long long*>(dsm);
   double* vbuf = reinterpret_cast<double*>(dsm + static_cast<size_t>(kCoarseBigCap) * 8);
-  __shared__ int sh_m, sh_u;
+  __shared__ int sh[2 + kCoarseThreads / 32];
   const int n_ovf = *ovf_len;
   for (int r = blockIdx.x; r < n_ovf; r += gridDim.x) {
     const bool ok = amg_coarse_row(n, ovf[r], mode, indptr, indices, values, agg, mptr, members, cnt, cptr, ccol, cval,
-                                   kbuf, vbuf, kCoarseBigCap, &sh_m, &sh_u);
+                                   kbuf, vbuf, kCoarseBigCap, sh, sh + 1);
     if (!ok && threadIdx.x == 0) set_status(status, FGB_ERR_CAPACITY);
     __syncthreads();
   }
@@ -372,90 +441,96 @@ __global__ void __launch_bounds__(kCoarseThreads) amg_coarse_rows_big(int64_t n,
 
 // ------------------------------------------------------------ apply kernels
 // Rows with G lanes each (G in {4, 8, 16, 32}); y = A x fused with a
-// per-row epilogue.
+// per-row epilogue.  V: type of the matrix values, T: type of the vectors and
+// of the arithmetic (float for the FP32 V-cycle: GB300's FP64 pipe is narrow
+// enough that FP64 products bound a sweep's time well above its bytes).
 // (A x)_i by the G lanes of row i; every lane of the warp calls it (rows past
 // n pass active = false and contribute nothing), so the full-warp shuffles
 // always have all 32 lanes present.
-template <int G>
-__device__ __forceinline__ double csr_row_dot(int64_t i, bool active, const int64_t* __restrict__ indptr,
-                                              const int32_t* __restrict__ indices, const double* __restrict__ values,
-                                              const double* __restrict__ x, int sub) {
-  double acc = 0.0;
-  if (active)
-    for (int64_t e = indptr[i] + sub; e < indptr[i + 1]; e += G) acc += values[e] * x[indices[e]];
+template <int G, typename V, typename T>
+__device__ __forceinline__ T csr_row_dot(int64_t i, bool active, const int64_t* __restrict__ indptr,
+                                         const int32_t* __restrict__ indices, const V* __restrict__ values,
+                                         const T* __restrict__ x, int sub) {
+  T acc = T(0);
+  if (active) {
+    const int64_t e1 = indptr[i + 1];
+#pragma unroll 4
+    for (int64_t e = indptr[i] + sub; e < e1; e += G) acc += static_cast<T>(values[e]) * x[indices[e]];
+  }
 #pragma unroll
   for (int o = G >> 1; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, G);
   return acc;
 }
 
-// Rows in groups of 32 / G per warp; the trip count is the same for every
-// lane of a warp (the bound is tested on the warp's first row).
-#define AMG_ROW_LOOP(n, G)                                                                                   \
-  const int sub = threadIdx.x & ((G) - 1);                                                                   \
-  const int64_t wfirst = ((blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5) * (32 / (G));  \
-  const int64_t wstep = ((static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5) * (32 / (G));                  \
-  for (int64_t wr = wfirst, i = wfirst + (threadIdx.x & 31) / (G); wr < (n); wr += wstep, i += wstep)
-
 // Chebyshev step: d = c1 d + c2 Dinv (r - A x_in); x_out = x_in + d
-template <int G>
+template <int G, typename V, typename T>
 __global__ void amg_cheb_step(int64_t n, const int64_t* __restrict__ indptr, const int32_t* __restrict__ indices,
-                              const double* __restrict__ values, const double* __restrict__ dinv,
-                              const double* __restrict__ r, const double* __restrict__ x_in,
-                              double* __restrict__ x_out, double* __restrict__ d, double c1, double c2) {
+                              const V* __restrict__ values, const T* __restrict__ dinv, const T* __restrict__ r,
+                              const T* __restrict__ x_in, T* __restrict__ x_out, T* __restrict__ d, T c1, T c2) {
   AMG_ROW_LOOP(n, G) {
     const bool active = i < n;
-    const double ax = csr_row_dot<G>(i, active, indptr, indices, values, x_in, sub);
+    const T ax = csr_row_dot<G, V, T>(i, active, indptr, indices, values, x_in, sub);
     if (active && sub == 0) {
-      const double di = (c1 != 0.0 ? c1 * d[i] : 0.0) + c2 * dinv[i] * (r[i] - ax);
+      const T di = (c1 != T(0) ? c1 * d[i] : T(0)) + c2 * dinv[i] * (r[i] - ax);
       d[i] = di;
       x_out[i] = x_in[i] + di;
     }
   }
 }
 
-// first Chebyshev step from x = 0: d = c2 Dinv r, x = d
 __global__ void amg_invert(int64_t n, const double* __restrict__ diag, double* __restrict__ dinv) {
   for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
        i += static_cast<int64_t>(gridDim.x) * blockDim.x)
     dinv[i] = 1.0 / diag[i];
 }
 
-__global__ void amg_cheb_first(int64_t n, const double* __restrict__ dinv, const double* __restrict__ r,
-                               double* __restrict__ x, double* __restrict__ d, double c2) {
+template <typename A, typename B>
+__global__ void amg_convert(int64_t n, const A* __restrict__ a, B* __restrict__ b) {
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    b[i] = static_cast<B>(a[i]);
+}
+
+// first Chebyshev step from x = 0: d = c2 Dinv r, x = d
+template <typename T>
+__global__ void amg_cheb_first(int64_t n, const T* __restrict__ dinv, const T* __restrict__ r, T* __restrict__ x,
+                               T* __restrict__ d, T c2) {
   for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
        i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-    const double di = c2 * dinv[i] * r[i];
+    const T di = c2 * dinv[i] * r[i];
     d[i] = di;
     x[i] = di;
   }
 }
 
 // res = r - A x
-template <int G>
+template <int G, typename V, typename T>
 __global__ void amg_residual(int64_t n, const int64_t* __restrict__ indptr, const int32_t* __restrict__ indices,
-                             const double* __restrict__ values, const double* __restrict__ r,
-                             const double* __restrict__ x, double* __restrict__ res) {
+                             const V* __restrict__ values, const T* __restrict__ r, const T* __restrict__ x,
+                             T* __restrict__ res) {
   AMG_ROW_LOOP(n, G) {
     const bool active = i < n;
-    const double ax = csr_row_dot<G>(i, active, indptr, indices, values, x, sub);
+    const T ax = csr_row_dot<G, V, T>(i, active, indptr, indices, values, x, sub);
     if (active && sub == 0) res[i] = r[i] - ax;
   }
 }
 
 // rc[I] = sum of res over the members of aggregate I, in row order
+template <typename T>
 __global__ void amg_restrict(int64_t nc, const int64_t* __restrict__ mptr, const int32_t* __restrict__ members,
-                             const double* __restrict__ res, double* __restrict__ rc) {
+                             const T* __restrict__ res, T* __restrict__ rc) {
   for (int64_t I = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; I < nc;
        I += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-    double s = 0.0;
+    T s = T(0);
     for (int64_t k = mptr[I]; k < mptr[I + 1]; ++k) s += res[members[k]];
     rc[I] = s;
   }
 }
 
 // x[i] += omega * ec[agg[i]]
-__global__ void amg_prolong(int64_t n, const int32_t* __restrict__ agg, const double* __restrict__ ec, double omega,
-                            double* __restrict__ x) {
+template <typename T>
+__global__ void amg_prolong(int64_t n, const int32_t* __restrict__ agg, const T* __restrict__ ec, T omega,
+                            T* __restrict__ x) {
   for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
        i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
     const int32_t a = agg[i];
@@ -492,28 +567,44 @@ __device__ void amg_reduce2(double a, double b, double* partials, unsigned int* 
     last = atomicAdd(counter, 1u) == gridDim.x - 1;
   }
   __syncthreads();
-  if (last && threadIdx.x == 0) {
-    __threadfence();
-    double ta = 0.0, tb = 0.0;
-    for (unsigned int k = 0; k < gridDim.x; ++k) {
-      ta += __ldcg(partials + k);
-      tb += __ldcg(partials + gridDim.x + k);
+  if (!last) return;  // uniform within the block
+  // last block: thread t sums the partials t, t + blockDim.x, ... in order,
+  // then the block's sums combine as above (a fixed order for a fixed grid)
+  __threadfence();
+  double ta = 0.0, tb = 0.0;
+  for (unsigned int k = threadIdx.x; k < gridDim.x; k += blockDim.x) {
+    ta += __ldcg(partials + k);
+    tb += __ldcg(partials + gridDim.x + k);
+  }
+  ta = warp_sum(ta);
+  tb = warp_sum(tb);
+  __syncthreads();  // the first combine's reads of sa, sb are done
+  if (lane == 0) {
+    sa[wid] = ta;
+    sb[wid] = tb;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double fa = 0.0, fb = 0.0;
+    for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) {
+      fa += sa[w];
+      fb += sb[w];
     }
-    out[0] = ta;
-    out[1] = tb;
+    out[0] = fa;
+    out[1] = fb;
     *counter = 0u;
   }
 }
 
 // Ap = A p; out = (p.Ap, 0)
-template <int G>
+template <int G, typename V>
 __global__ void amg_pcg_spmv(int64_t n, const int64_t* __restrict__ indptr, const int32_t* __restrict__ indices,
-                             const double* __restrict__ values, const double* __restrict__ p, double* __restrict__ Ap,
+                             const V* __restrict__ values, const double* __restrict__ p, double* __restrict__ Ap,
                              double* partials, unsigned int* counter, double* out) {
   double pap = 0.0;
   AMG_ROW_LOOP(n, G) {
     const bool active = i < n;
-    const double ax = csr_row_dot<G>(i, active, indptr, indices, values, p, sub);
+    const double ax = csr_row_dot<G, V, double>(i, active, indptr, indices, values, p, sub);
     if (active && sub == 0) {
       Ap[i] = ax;
       pap += p[i] * ax;
@@ -549,22 +640,81 @@ __global__ void amg_dot2(int64_t n, const double* __restrict__ a, const double* 
   amg_reduce2(ab, aa, partials, counter, out);
 }
 
-// p = z + beta p
-__global__ void amg_pupdate(int64_t n, double beta, const double* __restrict__ z, double* __restrict__ p) {
+// Device state of the PCG loop (the loop runs as a CUDA-graph while node:
+// alpha, beta and the stopping test are computed on the device).
+struct AmgPcgState {
+  double rz, beta, tol, atol, resid;
+  double red[6];  // reduction outputs: [0] p.Ap, [2] r.r, [4] r.z
+  long long niter, maxit, trips, trip_cap;
+  int done, norm;
+};
+
+// x += alpha p, r -= alpha Ap with alpha = rz / p.Ap; a non-positive or
+// non-finite p.Ap ends the solve and leaves x and r as they are; r.r to red[2]
+__global__ void amg_pcg_update_dev(int64_t n, AmgPcgState* s, const double* __restrict__ p,
+                                   const double* __restrict__ Ap, double* __restrict__ x, double* __restrict__ r,
+                                   double* partials, unsigned int* counter) {
+  const double pap = s->red[0];
+  const bool bad = !(pap > 0.0) || !isfinite(pap);
+  double rr = 0.0;
+  if (!bad) {
+    const double alpha = s->rz / pap;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+      x[i] += alpha * p[i];
+      const double ri = r[i] - alpha * Ap[i];
+      r[i] = ri;
+      rr += ri * ri;
+    }
+  } else if (blockIdx.x == 0 && threadIdx.x == 0) {
+    s->done = isfinite(pap) ? FGB_PCG_BREAKDOWN : FGB_PCG_NONFINITE;
+  }
+  amg_reduce2(rr, 0.0, partials, counter, s->red + 2);
+}
+
+// End of an iteration (one thread): FEALPy's stopping rule on the residual
+// (norm 0: sqrt(r.z), 1: ||r||), then beta = rz_new / rz; clears the while
+// condition when the solve ends, and in any case after trip_cap iterations.
+__global__ void amg_pcg_ctl(AmgPcgState* s, cudaGraphConditionalHandle handle) {
+  if (!s->done) {
+    const double rr = s->red[2], rzn = s->red[4];
+    s->niter += 1;
+    const double resid = s->norm ? sqrt(rr) : sqrt(fabs(rzn));
+    s->resid = resid;
+    if (!isfinite(resid)) s->done = FGB_PCG_NONFINITE;
+    else if (resid < s->atol) s->done = FGB_PCG_ATOL;
+    else if (resid < s->tol) s->done = FGB_PCG_RTOL;
+    else if (s->niter >= s->maxit) s->done = FGB_PCG_MAXIT;
+    else {
+      s->beta = rzn / s->rz;
+      s->rz = rzn;
+    }
+  }
+  s->trips += 1;
+  if (!s->done && s->trips >= s->trip_cap) s->done = FGB_PCG_MAXIT;
+  if (s->done) cudaGraphSetConditional(handle, 0);
+}
+
+// p = z + beta p (nothing once the solve has ended)
+__global__ void amg_pupdate_dev(int64_t n, const AmgPcgState* s, const double* __restrict__ z,
+                                double* __restrict__ p) {
+  if (s->done) return;
+  const double beta = s->beta;
   for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
        i += static_cast<int64_t>(gridDim.x) * blockDim.x)
     p[i] = z[i] + beta * p[i];
 }
 
+// lanes per row: rows of up to about two entries per lane per pass
 inline int amg_lanes(int64_t n, int64_t nnz) {
   const double avg = n > 0 ? static_cast<double>(nnz) / n : 0.0;
-  return avg <= 6 ? 4 : (avg <= 14 ? 8 : (avg <= 40 ? 16 : 32));
+  return avg <= 10 ? 4 : (avg <= 48 ? 8 : (avg <= 96 ? 16 : 32));
 }
 
 inline int rows_grid(int64_t n, int G) { return grid_for(n * G, kAmgThreads, kNumSMs * 16); }
 inline int vec_grid(int64_t n) { return grid_for(n, kAmgThreads, kNumSMs * 16); }
 
-#define AMG_DISPATCH_G(G, KERNEL, ...)                                                                 \
+#define AMG_DISPATCH_ROWS(G, KERNEL, ...)                                                              \
   switch (G) {                                                                                         \
     case 4: KERNEL<4><<<rows_grid(n, 4), kAmgThreads, 0, st>>>(__VA_ARGS__); break;                   \
     case 8: KERNEL<8><<<rows_grid(n, 8), kAmgThreads, 0, st>>>(__VA_ARGS__); break;                   \
@@ -572,58 +722,98 @@ inline int vec_grid(int64_t n) { return grid_for(n, kAmgThreads, kNumSMs * 16); 
     default: KERNEL<32><<<rows_grid(n, 32), kAmgThreads, 0, st>>>(__VA_ARGS__); break;                \
   }
 
+// f(std::integral_constant<int, G>) for the lanes count G of a level
+template <typename F>
+void with_lanes(int G, F&& f) {
+  switch (G) {
+    case 4: f(std::integral_constant<int, 4>{}); break;
+    case 8: f(std::integral_constant<int, 8>{}); break;
+    case 16: f(std::integral_constant<int, 16>{}); break;
+    default: f(std::integral_constant<int, 32>{}); break;
+  }
+}
+
 }  // namespace fgb
 
 using namespace fgb;
 
 namespace {
 
-// scratch vectors of one level in the V-cycle workspace
+// scratch vectors of one level in the V-cycle workspace (T: the V-cycle's
+// arithmetic type)
+template <typename T>
 struct LevelVecs {
-  double *r, *x, *x2, *d, *res;
+  T *r, *x, *x2, *d, *res;
 };
 
 size_t level_vec_bytes(int64_t n) { return 5 * align_up(static_cast<size_t>(n) * sizeof(double)); }
 
-LevelVecs carve_level(Carver& cv, int64_t n) {
-  LevelVecs v;
-  v.r = cv.take<double>(n);
-  v.x = cv.take<double>(n);
-  v.x2 = cv.take<double>(n);
-  v.d = cv.take<double>(n);
-  v.res = cv.take<double>(n);
+template <typename T>
+LevelVecs<T> carve_level(Carver& cv, int64_t n) {
+  LevelVecs<T> v;
+  v.r = cv.take<T>(n);
+  v.x = cv.take<T>(n);
+  v.x2 = cv.take<T>(n);
+  v.d = cv.take<T>(n);
+  v.res = cv.take<T>(n);
   return v;
 }
 
+// a level's values and 1 / a_ii in the V-cycle's type
+template <typename T>
+const T* level_values(const fgb_amg_level& L) {
+  if constexpr (std::is_same<T, float>::value) return L.values32;
+  else return L.values;
+}
+template <typename T>
+const T* level_dinv(const fgb_amg_level& L) {
+  if constexpr (std::is_same<T, float>::value) return L.dinv32;
+  else return L.dinv;
+}
+
+template <typename T>
+void cheb_sweep(const fgb_amg_level& L, const T* r, const T* x_in, T* x_out, T* d, double c1, double c2,
+                cudaStream_t st) {
+  const int64_t n = L.n;
+  const T* vals = level_values<T>(L);
+  const T* dinv = level_dinv<T>(L);
+  with_lanes(amg_lanes(n, L.nnz), [&](auto g) {
+    constexpr int GG = decltype(g)::value;
+    amg_cheb_step<GG, T, T><<<rows_grid(n, GG), kAmgThreads, 0, st>>>(n, L.indptr, L.indices, vals, dinv, r, x_in,
+                                                                       x_out, d, static_cast<T>(c1),
+                                                                       static_cast<T>(c2));
+  });
+}
+
 // Chebyshev polynomial in D^-1 A of degree deg on [lmax * lo, lmax], applied
-// to r from x = 0 (x0 == nullptr) or as a correction of x0; the result ends
-// in *xout (one of the two buffers).
-void cheb(const fgb_amg_level& L, const double* r, double* xa, double* xb, double* d, int deg, double lo,
-          bool from_zero, double** xout, cudaStream_t st) {
+// to r from x = 0 (from_zero) or as a correction of the x in xa; the result
+// ends in *xout (one of the two buffers).
+template <typename T>
+void cheb(const fgb_amg_level& L, const T* r, T* xa, T* xb, T* d, int deg, double lo, bool from_zero, T** xout,
+          cudaStream_t st) {
   const int64_t n = L.n;
   const double lmax = L.lmax, lmin = L.lmax * lo;
   const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin), sigma = theta / delta;
-  const int G = amg_lanes(n, L.nnz);
   double rho = 1.0 / sigma;
-  double* cur = xa;
-  double* nxt = xb;
+  T* cur = xa;
+  T* nxt = xb;
   int k = 0;
   if (from_zero) {
-    amg_cheb_first<<<vec_grid(n), kAmgThreads, 0, st>>>(n, L.dinv, r, cur, d, 1.0 / theta);
+    amg_cheb_first<T><<<vec_grid(n), kAmgThreads, 0, st>>>(n, level_dinv<T>(L), r, cur, d,
+                                                            static_cast<T>(1.0 / theta));
     k = 1;
   } else {
     // first correction of a given x: d = Dinv (r - A x) / theta
-    AMG_DISPATCH_G(G, amg_cheb_step, n, L.indptr, L.indices, L.values, L.dinv, r, cur, nxt, d, 0.0, 1.0 / theta);
-    double* t = cur;
+    cheb_sweep<T>(L, r, cur, nxt, d, 0.0, 1.0 / theta, st);
+    T* t = cur;
     cur = nxt;
     nxt = t;
     k = 1;
   }
   for (; k < deg; ++k) {
     const double rho1 = 1.0 / (2.0 * sigma - rho);
-    AMG_DISPATCH_G(G, amg_cheb_step, n, L.indptr, L.indices, L.values, L.dinv, r, cur, nxt, d, rho1 * rho,
-                   2.0 * rho1 / delta);
-    double* t = cur;
+    cheb_sweep<T>(L, r, cur, nxt, d, rho1 * rho, 2.0 * rho1 / delta, st);
+    T* t = cur;
     cur = nxt;
     nxt = t;
     rho = rho1;
@@ -631,42 +821,60 @@ void cheb(const fgb_amg_level& L, const double* r, double* xa, double* xb, doubl
   *xout = cur;
 }
 
+template <typename T>
 int vcycle(const fgb_amg_level* levels, int nl, const double* r0, double* x_out, int deg, int cdeg, double omega,
-           LevelVecs* V, cudaStream_t st) {
+           LevelVecs<T>* V, cudaStream_t st) {
+  const int64_t n0 = levels[0].n;
+  const T* r_top;
+  if constexpr (std::is_same<T, float>::value) {
+    amg_convert<double, float><<<vec_grid(n0), kAmgThreads, 0, st>>>(n0, r0, V[0].r);
+    r_top = V[0].r;
+  } else {
+    r_top = r0;
+  }
   // down: smoothing from zero, residual, restriction
-  std::vector<double*> xs(nl);
-  const double* rin = r0;
+  T* xs[FGB_AMG_MAX_LEVELS];
+  const T* rin = r_top;
   for (int l = 0; l < nl; ++l) {
     const fgb_amg_level& L = levels[l];
     const int64_t n = L.n;
     if (l == nl - 1) {
-      double* xo = nullptr;
-      cheb(L, rin, V[l].x, V[l].x2, V[l].d, cdeg, 0.05, true, &xo, st);
+      T* xo = nullptr;
+      cheb<T>(L, rin, V[l].x, V[l].x2, V[l].d, cdeg, 0.05, true, &xo, st);
       xs[l] = xo;
       break;
     }
-    double* xo = nullptr;
-    cheb(L, rin, V[l].x, V[l].x2, V[l].d, deg, 0.1, true, &xo, st);
+    T* xo = nullptr;
+    cheb<T>(L, rin, V[l].x, V[l].x2, V[l].d, deg, 0.1, true, &xo, st);
     xs[l] = xo;
-    const int G = amg_lanes(n, L.nnz);
-    AMG_DISPATCH_G(G, amg_residual, n, L.indptr, L.indices, L.values, rin, xo, V[l].res);
-    amg_restrict<<<vec_grid(L.n_coarse), kAmgThreads, 0, st>>>(L.n_coarse, L.member_ptr, L.members, V[l].res,
-                                                               V[l + 1].r);
+    const T* vals = level_values<T>(L);
+    with_lanes(amg_lanes(n, L.nnz), [&](auto g) {
+      constexpr int GG = decltype(g)::value;
+      amg_residual<GG, T, T><<<rows_grid(n, GG), kAmgThreads, 0, st>>>(n, L.indptr, L.indices, vals, rin, xo,
+                                                                        V[l].res);
+    });
+    amg_restrict<T><<<vec_grid(L.n_coarse), kAmgThreads, 0, st>>>(L.n_coarse, L.member_ptr, L.members, V[l].res,
+                                                                  V[l + 1].r);
     rin = V[l + 1].r;
   }
   // up: prolongation with over-correction, smoothing of the corrected x
   for (int l = nl - 2; l >= 0; --l) {
     const fgb_amg_level& L = levels[l];
-    const double* rl = l == 0 ? r0 : V[l].r;
-    amg_prolong<<<vec_grid(L.n), kAmgThreads, 0, st>>>(L.n, L.agg, xs[l + 1], omega, xs[l]);
-    double* other = xs[l] == V[l].x ? V[l].x2 : V[l].x;
-    double* xo = nullptr;
-    cheb(L, rl, xs[l], other, V[l].d, deg, 0.1, false, &xo, st);
+    const T* rl = l == 0 ? r_top : V[l].r;
+    amg_prolong<T><<<vec_grid(L.n), kAmgThreads, 0, st>>>(L.n, L.agg, xs[l + 1], static_cast<T>(omega), xs[l]);
+    T* other = xs[l] == V[l].x ? V[l].x2 : V[l].x;
+    T* xo = nullptr;
+    cheb<T>(L, rl, xs[l], other, V[l].d, deg, 0.1, false, &xo, st);
     xs[l] = xo;
   }
-  return cudaMemcpyAsync(x_out, xs[0], levels[0].n * sizeof(double), cudaMemcpyDeviceToDevice, st) == cudaSuccess
-             ? launch_status()
-             : FGB_ERR_CUDA;
+  if constexpr (std::is_same<T, float>::value) {
+    amg_convert<float, double><<<vec_grid(n0), kAmgThreads, 0, st>>>(n0, xs[0], x_out);
+    return launch_status();
+  } else {
+    return cudaMemcpyAsync(x_out, xs[0], n0 * sizeof(double), cudaMemcpyDeviceToDevice, st) == cudaSuccess
+               ? launch_status()
+               : FGB_ERR_CUDA;
+  }
 }
 
 size_t vcycle_bytes(const fgb_amg_level* levels, int nl) {
@@ -675,15 +883,39 @@ size_t vcycle_bytes(const fgb_amg_level* levels, int nl) {
   return b;
 }
 
-bool levels_ok(const fgb_amg_level* levels, int nl) {
-  if (!levels || nl < 1 || nl > FGB_AMG_MAX_LEVELS) return false;
+// -1: inconsistent levels; 0: FP64 V-cycle; 1: FP32 V-cycle (every level
+// carries values32 and dinv32)
+int levels_mode(const fgb_amg_level* levels, int nl) {
+  if (!levels || nl < 1 || nl > FGB_AMG_MAX_LEVELS) return -1;
+  int n32 = 0;
   for (int l = 0; l < nl; ++l) {
     const fgb_amg_level& L = levels[l];
-    if (L.n <= 0 || !L.indptr || !L.indices || !L.values || !L.dinv || !(L.lmax > 0.0)) return false;
-    if (l < nl - 1 && (!L.agg || !L.member_ptr || !L.members || L.n_coarse != levels[l + 1].n)) return false;
+    if (L.n <= 0 || !L.indptr || !L.indices || !L.values || !L.dinv || !(L.lmax > 0.0)) return -1;
+    if (l < nl - 1 && (!L.agg || !L.member_ptr || !L.members || L.n_coarse != levels[l + 1].n)) return -1;
+    if ((L.values32 == nullptr) != (L.dinv32 == nullptr)) return -1;
+    n32 += L.values32 ? 1 : 0;
   }
-  return true;
+  if (n32 != 0 && n32 != nl) return -1;
+  return n32 ? 1 : 0;
 }
+
+// the V-cycle's scratch in either type
+struct VcycleScratch {
+  int mode = 0;
+  LevelVecs<float> f[FGB_AMG_MAX_LEVELS];
+  LevelVecs<double> d[FGB_AMG_MAX_LEVELS];
+  void carve(Carver& cv, const fgb_amg_level* levels, int nl) {
+    for (int l = 0; l < nl; ++l) {
+      if (mode) f[l] = carve_level<float>(cv, levels[l].n);
+      else d[l] = carve_level<double>(cv, levels[l].n);
+    }
+  }
+  int run(const fgb_amg_level* levels, int nl, const double* r, double* x, int deg, int cdeg, double omega,
+          cudaStream_t st) {
+    return mode ? vcycle<float>(levels, nl, r, x, deg, cdeg, omega, f, st)
+                : vcycle<double>(levels, nl, r, x, deg, cdeg, omega, d, st);
+  }
+};
 
 }  // namespace
 
@@ -691,7 +923,7 @@ extern "C" {
 
 size_t fgb_amg_setup_workspace_bytes(int64_t n) {
   const size_t un = static_cast<size_t>(n);
-  return align_up(un * 8) * 4 + align_up((un + 1) * 4) * 3 + align_up(8) + align_up(8) + align_up((un + 1) * 8) +
+  return align_up(un * 8) * 2 + align_up((un + 1) * 4) * 3 + align_up(8) + align_up(8) + align_up((un + 1) * 8) +
          scan_workspace_bytes(n + 1);
 }
 
@@ -707,8 +939,6 @@ int32_t fgb_amg_aggregate(int64_t n, const int64_t* indptr, const int32_t* indic
   Carver cv(workspace, workspace_bytes);
   double* diag = cv.take<double>(n);
   unsigned long long* key = cv.take<unsigned long long>(n);
-  unsigned long long* m1 = cv.take<unsigned long long>(n);
-  unsigned long long* m2 = cv.take<unsigned long long>(n);
   int32_t* state = cv.take<int32_t>(n + 1);
   int32_t* flag = cv.take<int32_t>(n + 1);
   int32_t* agg2 = cv.take<int32_t>(n + 1);
@@ -718,20 +948,24 @@ int32_t fgb_amg_aggregate(int64_t n, const int64_t* indptr, const int32_t* indic
   void* scan_ws = cv.base + cv.off;
   const size_t scan_bytes = workspace_bytes - cv.off;
   if (!cv.ok) return FGB_ERR_WORKSPACE;
+  int64_t nnz = 0;
+  if (cudaMemcpyAsync(&nnz, indptr + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return FGB_ERR_CUDA;
+  if (nnz < 0) return FGB_ERR_ARG;
+  const int G = amg_lanes(n, nnz);
   const int g = vec_grid(n);
   if (cudaMemsetAsync(bound, 0, sizeof(unsigned long long), st) != cudaSuccess) return FGB_ERR_CUDA;
-  amg_diag_kernel<double><<<g, kAmgThreads, 0, st>>>(n, indptr, indices, values, diag, flag, bound, status);
+  AMG_DISPATCH_ROWS(G, amg_diag_kernel, n, indptr, indices, values, diag, bound, status);
   amg_invert<<<g, kAmgThreads, 0, st>>>(n, diag, dinv);
-  amg_init_state<<<g, kAmgThreads, 0, st>>>(n, indptr, indices, values, diag, theta, state);
-  // distance-2 maximal independent set (each round decides at least the
-  // undecided node of largest key; 64 rounds bound the loop)
+  AMG_DISPATCH_ROWS(G, amg_init_state, n, indptr, indices, values, diag, theta, state);
+  // maximal independent set (each round decides at least the undecided node
+  // of largest key; 64 rounds bound the loop)
   int32_t und = 1;
   for (int round = 0; round < 64 && und > 0; ++round) {
     amg_keys<<<g, kAmgThreads, 0, st>>>(n, state, key);
-    amg_nbmax<<<g, kAmgThreads, 0, st>>>(n, indptr, indices, values, diag, theta, state, key, m1);
-    amg_nbmax<<<g, kAmgThreads, 0, st>>>(n, indptr, indices, values, diag, theta, state, m1, m2);
     if (cudaMemsetAsync(counter, 0, sizeof(int32_t), st) != cudaSuccess) return FGB_ERR_CUDA;
-    amg_mis_update<<<g, kAmgThreads, 0, st>>>(n, key, m2, state, counter);
+    AMG_DISPATCH_ROWS(G, amg_mis_round, n, indptr, indices, values, diag, theta, key, state, counter);
     if (cudaMemcpyAsync(&und, counter, sizeof(int32_t), cudaMemcpyDeviceToHost, st) != cudaSuccess) return FGB_ERR_CUDA;
     if (cudaStreamSynchronize(st) != cudaSuccess) return FGB_ERR_CUDA;
   }
@@ -750,7 +984,7 @@ int32_t fgb_amg_aggregate(int64_t n, const int64_t* indptr, const int32_t* indic
   int32_t* nxt = agg2;
   for (int sweep = 0; sweep < 8 && left > 0; ++sweep) {
     if (cudaMemsetAsync(counter, 0, sizeof(int32_t), st) != cudaSuccess) return FGB_ERR_CUDA;
-    amg_assign<<<g, kAmgThreads, 0, st>>>(n, indptr, indices, values, diag, theta, state, cur, nxt, counter);
+    AMG_DISPATCH_ROWS(G, amg_assign, n, indptr, indices, values, diag, theta, state, cur, nxt, counter);
     if (cudaMemcpyAsync(&left, counter, sizeof(int32_t), cudaMemcpyDeviceToHost, st) != cudaSuccess)
       return FGB_ERR_CUDA;
     if (cudaStreamSynchronize(st) != cudaSuccess) return FGB_ERR_CUDA;
@@ -846,33 +1080,36 @@ int32_t fgb_amg_coarse_fill(int64_t n, const int64_t* indptr, const int32_t* ind
 }
 
 size_t fgb_amg_workspace_bytes(const fgb_amg_level* levels, int32_t n_levels) {
-  if (!levels_ok(levels, n_levels)) return 0;
+  if (levels_mode(levels, n_levels) < 0) return 0;
   const int64_t n = levels[0].n;
   return vcycle_bytes(levels, n_levels) + 4 * align_up(static_cast<size_t>(n) * sizeof(double)) +
-         align_up(2 * kMaxGrid * sizeof(double)) + align_up(8 * sizeof(double)) + align_up(4 * sizeof(unsigned int));
+         align_up(2 * kMaxGrid * sizeof(double)) + align_up(sizeof(AmgPcgState)) + align_up(4 * sizeof(unsigned int));
 }
 
 int32_t fgb_amg_vcycle(const fgb_amg_level* levels, int32_t n_levels, int32_t deg, int32_t cdeg, double omega,
                        const double* r, double* x, void* workspace, size_t workspace_bytes, void* stream) {
-  if (!levels_ok(levels, n_levels) || !r || !x || deg < 1 || cdeg < 1 || !(omega > 0.0)) return FGB_ERR_ARG;
+  const int mode = levels_mode(levels, n_levels);
+  if (mode < 0 || !r || !x || deg < 1 || cdeg < 1 || !(omega > 0.0)) return FGB_ERR_ARG;
   if (!workspace || workspace_bytes < fgb_amg_workspace_bytes(levels, n_levels)) return FGB_ERR_WORKSPACE;
   Carver cv(workspace, workspace_bytes);
-  LevelVecs V[FGB_AMG_MAX_LEVELS];
-  for (int l = 0; l < n_levels; ++l) V[l] = carve_level(cv, levels[l].n);
+  VcycleScratch V;
+  V.mode = mode;
+  V.carve(cv, levels, n_levels);
   if (!cv.ok) return FGB_ERR_WORKSPACE;
-  return vcycle(levels, n_levels, r, x, deg, cdeg, omega, V, as_stream(stream));
+  return V.run(levels, n_levels, r, x, deg, cdeg, omega, as_stream(stream));
 }
 
 int32_t fgb_pcg_amg(const fgb_amg_level* levels, int32_t n_levels, int32_t deg, int32_t cdeg, double omega,
                     const double* b, double* x, double atol, double rtol, int64_t maxit, int32_t norm,
                     fgb_pcg_info* info, void* workspace, size_t workspace_bytes, void* stream) {
-  if (!levels_ok(levels, n_levels) || !b || !x || deg < 1 || cdeg < 1 || !(omega > 0.0) || maxit <= 0)
-    return FGB_ERR_ARG;
+  const int mode = levels_mode(levels, n_levels);
+  if (mode < 0 || !b || !x || deg < 1 || cdeg < 1 || !(omega > 0.0) || maxit <= 0) return FGB_ERR_ARG;
   if (!workspace || workspace_bytes < fgb_amg_workspace_bytes(levels, n_levels)) return FGB_ERR_WORKSPACE;
   cudaStream_t st = as_stream(stream);
   Carver cv(workspace, workspace_bytes);
-  LevelVecs V[FGB_AMG_MAX_LEVELS];
-  for (int l = 0; l < n_levels; ++l) V[l] = carve_level(cv, levels[l].n);
+  VcycleScratch V;
+  V.mode = mode;
+  V.carve(cv, levels, n_levels);
   const fgb_amg_level& L = levels[0];
   const int64_t n = L.n;
   double* r = cv.take<double>(n);
@@ -880,75 +1117,112 @@ int32_t fgb_pcg_amg(const fgb_amg_level* levels, int32_t n_levels, int32_t deg, 
   double* p = cv.take<double>(n);
   double* Ap = cv.take<double>(n);
   double* partials = cv.take<double>(2 * kMaxGrid);
-  double* out = cv.take<double>(8);
+  AmgPcgState* s = cv.take<AmgPcgState>(1);
   unsigned int* counter = cv.take<unsigned int>(4);
   if (!cv.ok) return FGB_ERR_WORKSPACE;
   if (cudaMemsetAsync(counter, 0, 4 * sizeof(unsigned int), st) != cudaSuccess) return FGB_ERR_CUDA;
   const int G = amg_lanes(n, L.nnz);
-  double h[8];
-  auto read = [&](int k) -> int {
-    if (cudaMemcpyAsync(h, out, 8 * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess) return FGB_ERR_CUDA;
-    if (cudaStreamSynchronize(st) != cudaSuccess) return FGB_ERR_CUDA;
-    (void)k;
-    return FGB_OK;
+  AmgPcgState h = {};
+  auto read = [&]() -> int {
+    if (cudaMemcpyAsync(&h, s, sizeof(h), cudaMemcpyDeviceToHost, st) != cudaSuccess) return FGB_ERR_CUDA;
+    return cudaStreamSynchronize(st) == cudaSuccess ? FGB_OK : FGB_ERR_CUDA;
   };
-  int64_t launches = 0, niter = 0;
+  // kernels of one iteration: SpMV, update, the V-cycle, r.z, control, p
+  int per_vcycle = mode ? 2 : 0;
+  for (int l = 0; l < n_levels; ++l) per_vcycle += l == n_levels - 1 ? cdeg : 2 * deg + 3;
+  const int64_t per_iter = 5 + per_vcycle;
+  int64_t launches = 0;
   int reason = FGB_PCG_RUNNING;
-  double resid = 0.0;
-  // ||b||, r = b - A x, z = M r, rz
-  amg_dot2<<<kDotBlocks, kAmgThreads, 0, st>>>(n, b, b, partials, counter, out);
-  int rc = read(0);
+  // ||b||, r = b - A x, z = M r, rz (host-synchronous, once)
+  amg_dot2<<<kDotBlocks, kAmgThreads, 0, st>>>(n, b, b, partials, counter, s->red);
+  int rc = read();
   if (rc) return rc;
-  const double bnorm = sqrt(h[0]);
+  const double bnorm = sqrt(h.red[0]);
   if (bnorm < 1e-15) {
     if (cudaMemsetAsync(x, 0, n * sizeof(double), st) != cudaSuccess) return FGB_ERR_CUDA;
     reason = FGB_PCG_ZERO_RHS;
+    h.niter = 0;
+    h.resid = 0.0;
   } else {
-    AMG_DISPATCH_G(G, amg_residual, n, L.indptr, L.indices, L.values, b, x, r);
-    if ((rc = vcycle(levels, n_levels, r, z, deg, cdeg, omega, V, st))) return rc;
+    with_lanes(G, [&](auto g) {
+      constexpr int GG = decltype(g)::value;
+      amg_residual<GG, double, double><<<rows_grid(n, GG), kAmgThreads, 0, st>>>(n, L.indptr, L.indices, L.values, b,
+                                                                                  x, r);
+    });
+    if ((rc = V.run(levels, n_levels, r, z, deg, cdeg, omega, st))) return rc;
     if (cudaMemcpyAsync(p, z, n * sizeof(double), cudaMemcpyDeviceToDevice, st) != cudaSuccess) return FGB_ERR_CUDA;
-    amg_dot2<<<kDotBlocks, kAmgThreads, 0, st>>>(n, r, z, partials, counter, out);
-    if ((rc = read(0))) return rc;
-    double rz = h[0];
-    const double tol = rtol * bnorm;
-    while (true) {
-      AMG_DISPATCH_G(G, amg_pcg_spmv, n, L.indptr, L.indices, L.values, p, Ap, partials, counter, out);
-      if ((rc = read(0))) return rc;
-      const double pap = h[0];
-      if (!(pap > 0.0) || !std::isfinite(pap)) {
-        reason = std::isfinite(pap) ? FGB_PCG_BREAKDOWN : FGB_PCG_NONFINITE;
+    amg_dot2<<<kDotBlocks, kAmgThreads, 0, st>>>(n, r, z, partials, counter, s->red + 4);
+    if ((rc = read())) return rc;
+    launches += 3 + per_vcycle;
+    AmgPcgState init = {};
+    init.rz = h.red[4];
+    init.tol = rtol * bnorm;
+    init.atol = atol;
+    init.maxit = maxit;
+    init.trip_cap = maxit + 1;
+    init.norm = norm;
+    if (cudaMemcpyAsync(s, &init, sizeof(init), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      return FGB_ERR_CUDA;
+    // while (!done) { iteration } as one graph launch
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaStream_t cs = nullptr;
+    rc = FGB_OK;
+    do {
+      if (cudaGraphCreate(&g, 0) != cudaSuccess) { g = nullptr; rc = FGB_ERR_CUDA; break; }
+      cudaGraphConditionalHandle hw;
+      if (cudaGraphConditionalHandleCreate(&hw, g, 1, cudaGraphCondAssignDefault) != cudaSuccess) { rc = FGB_ERR_CUDA; break; }
+      cudaGraphNodeParams wp = {};
+      wp.type = cudaGraphNodeTypeConditional;
+      wp.conditional.handle = hw;
+      wp.conditional.type = cudaGraphCondTypeWhile;
+      wp.conditional.size = 1;
+      cudaGraphNode_t wnode;
+      if (cudaGraphAddNode(&wnode, g, nullptr, nullptr, 0, &wp) != cudaSuccess) { rc = FGB_ERR_CUDA; break; }
+      if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) { cs = nullptr; rc = FGB_ERR_CUDA; break; }
+      if (cudaStreamBeginCaptureToGraph(cs, wp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                        cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+        rc = FGB_ERR_CUDA;
         break;
       }
-      const double alpha = rz / pap;
-      amg_pcg_update<<<kDotBlocks, kAmgThreads, 0, st>>>(n, alpha, p, Ap, x, r, partials, counter, out + 2);
-      if ((rc = vcycle(levels, n_levels, r, z, deg, cdeg, omega, V, st))) return rc;
-      amg_dot2<<<kDotBlocks, kAmgThreads, 0, st>>>(n, r, z, partials, counter, out + 4);
-      if ((rc = read(0))) return rc;
-      const double rr = h[2], rz_new = h[4];
-      ++niter;
-      resid = norm ? sqrt(rr) : sqrt(fabs(rz_new));
-      if (!std::isfinite(resid)) {
-        reason = FGB_PCG_NONFINITE;
-        break;
-      }
-      if (resid < atol) { reason = FGB_PCG_ATOL; break; }
-      if (resid < tol) { reason = FGB_PCG_RTOL; break; }
-      if (niter >= maxit) { reason = FGB_PCG_MAXIT; break; }
-      const double beta = rz_new / rz;
-      amg_pupdate<<<vec_grid(n), kAmgThreads, 0, st>>>(n, beta, z, p);
-      rz = rz_new;
-      launches += 4;
+      with_lanes(G, [&](auto gl) {
+        constexpr int GG = decltype(gl)::value;
+        amg_pcg_spmv<GG, double><<<rows_grid(n, GG), kAmgThreads, 0, cs>>>(n, L.indptr, L.indices, L.values, p, Ap,
+                                                                            partials, counter, s->red);
+      });
+      amg_pcg_update_dev<<<kDotBlocks, kAmgThreads, 0, cs>>>(n, s, p, Ap, x, r, partials, counter);
+      const int vrc = V.run(levels, n_levels, r, z, deg, cdeg, omega, cs);
+      amg_dot2<<<kDotBlocks, kAmgThreads, 0, cs>>>(n, r, z, partials, counter, s->red + 4);
+      amg_pcg_ctl<<<1, 1, 0, cs>>>(s, hw);
+      amg_pupdate_dev<<<vec_grid(n), kAmgThreads, 0, cs>>>(n, s, z, p);
+      cudaGraph_t captured = nullptr;
+      const bool ended = cudaStreamEndCapture(cs, &captured) == cudaSuccess;
+      if (vrc || !ended) { rc = vrc ? vrc : FGB_ERR_CUDA; break; }
+      if (cudaGraphInstantiate(&exec, g, 0) != cudaSuccess) { exec = nullptr; rc = FGB_ERR_CUDA; break; }
+      if (cudaGraphLaunch(exec, st) != cudaSuccess) { rc = FGB_ERR_CUDA; break; }
+      rc = read();
+    } while (false);
+    if (exec) cudaGraphExecDestroy(exec);
+    if (g) cudaGraphDestroy(g);
+    if (cs) cudaStreamDestroy(cs);
+    if (rc) {
+      cudaGetLastError();
+      return rc;
     }
+    reason = h.done;
+    launches += per_iter * h.trips;
   }
   if (cudaStreamSynchronize(st) != cudaSuccess) return FGB_ERR_CUDA;
   if (info) {
     memset(info, 0, sizeof(*info));
-    info->niter = niter;
-    info->residual = resid;
+    info->niter = h.niter;
+    info->residual = h.resid;
     info->b_norm = bnorm;
     info->true_relres = -1.0;
     info->reason = reason;
     info->launches = launches;
+    info->graph = reason == FGB_PCG_ZERO_RHS ? 0 : 1;
   }
   if (reason == FGB_PCG_BREAKDOWN) return FGB_ERR_BREAKDOWN;
   if (reason == FGB_PCG_NONFINITE) return FGB_ERR_NONFINITE;

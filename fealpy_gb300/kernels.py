@@ -110,8 +110,12 @@ def assemble_scalar(adj_ptr, adj, c2d, tables: torch.Tensor, factors: torch.Tens
     ws = workspace(lib.fgb_assemble_workspace_bytes(n_dof), dev)
     own = status is None
     st = status_word(dev) if own else status
+    # converted inputs bound to names: two temporaries in one argument list
+    # could share a freed block before the launch
+    tab_d = tables.to(dev, dtype).contiguous()
+    fac_d = factors.contiguous()
     call("fgb_assemble_scalar", dtype_code(dtype), n_dof, ptr(adj_ptr), ptr(adj), ptr(c2d), ldof, nt,
-         ptr(tables.to(dev, dtype).contiguous()), ptr(factors.contiguous()), ptr(indptr), ptr(indices), ptr(values),
+         ptr(tab_d), ptr(fac_d), ptr(indptr), ptr(indices), ptr(values),
          ptr(v32), ptr(st), ptr(ws), ws.numel(), stream_ptr(dev))
     if own:
         check_status_word("fgb_assemble_scalar", st)
@@ -129,8 +133,9 @@ def assemble_elasticity_p1(gd, adj_ptr, adj, cell, factors, node_indptr, node_in
     ws = workspace(lib.fgb_assemble_workspace_bytes(n_node), dev)
     own = status is None
     st = status_word(dev) if own else status
+    fac_d = factors.contiguous()
     call("fgb_assemble_elasticity_p1", dtype_code(dtype), gd, n_node, ptr(adj_ptr), ptr(adj), ptr(cell),
-         ptr(factors.contiguous()), ptr(node_indptr), ptr(node_indices), ptr(indptr), ptr(values), ptr(v32), ptr(st),
+         ptr(fac_d), ptr(node_indptr), ptr(node_indices), ptr(indptr), ptr(values), ptr(v32), ptr(st),
          ptr(ws), ws.numel(), stream_ptr(dev))
     if own:
         check_status_word("fgb_assemble_elasticity_p1", st)
@@ -284,8 +289,10 @@ def cell_to_ipoint(mesh, p: int) -> torch.Tensor:
     out = torch.empty((NC, ldof), dtype=torch.int32, device=dev)
     hp = [tab[k].ctypes.data_as(ctypes.c_void_p) for k in ("kind", "a", "b", "le", "ma", "mb", "rank")]
     c2f = mesh.cell2face if TD == 3 else None
-    call("fgb_cell_to_ipoint", NC, TD, p, ldof, ptr(mesh.cell), ptr(mesh.cell2edge.contiguous()),
-         ptr(mesh.edge.contiguous()), ptr(c2f.contiguous() if c2f is not None else None), mesh.number_of_nodes(),
+    c2e_d, edge_d = mesh.cell2edge.contiguous(), mesh.edge.contiguous()
+    c2f_d = c2f.contiguous() if c2f is not None else None
+    call("fgb_cell_to_ipoint", NC, TD, p, ldof, ptr(mesh.cell), ptr(c2e_d),
+         ptr(edge_d), ptr(c2f_d), mesh.number_of_nodes(),
          mesh.number_of_edges(), *hp, ptr(out), stream_ptr(dev))
     return out
 
@@ -303,9 +310,10 @@ def cell_apply(c2d, tables: "np.ndarray", factors: torch.Tensor, x: torch.Tensor
         raise ValueError(f"tables must be ({nt}, {ldof}, {ldof})")
     tab_dev = None if ldof in (3, 4, 6, 10) else torch.as_tensor(tab_host, dtype=dt, device=dev)
     y = torch.empty((NC, ldof), dtype=dt, device=dev)
-    call("fgb_cell_apply", dtype_code(dt), NC, ldof, ptr(c2d.contiguous()), nt,
-         tab_host.ctypes.data_as(ctypes.c_void_p), ptr(tab_dev), ptr(factors.contiguous()),
-         ptr(x.to(dt).contiguous()), ptr(y), stream_ptr(dev))
+    c2d_d, fac_d, x_d = c2d.contiguous(), factors.contiguous(), x.to(dt).contiguous()
+    call("fgb_cell_apply", dtype_code(dt), NC, ldof, ptr(c2d_d), nt,
+         tab_host.ctypes.data_as(ctypes.c_void_p), ptr(tab_dev), ptr(fac_d),
+         ptr(x_d), ptr(y), stream_ptr(dev))
     return y
 
 
@@ -385,7 +393,8 @@ class SellMatrix:
                 return out
             return v
         res = out if out is not None else torch.empty_like(v)
-        call("fgb_permute", dtype_code(v.dtype), self.n, ptr(self.order), ptr(v.contiguous()), ptr(res), 1,
+        v_d = v.contiguous()
+        call("fgb_permute", dtype_code(v.dtype), self.n, ptr(self.order), ptr(v_d), ptr(res), 1,
              stream_ptr(v.device))
         return res
 

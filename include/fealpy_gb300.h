@@ -490,12 +490,15 @@ int32_t fgb_pcg_sell_mixed_ex(const fgb_sell* A, const double* diag_inv64, const
 /* The `M` slot of fealpy/solver/cg.py filled with a multigrid V-cycle, the
  * role of FEALPy's GAMGSolver (fealpy/solver/gamg_solver.py:14-256, a
  * Ruge-Stuben hierarchy with Gauss-Seidel smoothing).  Here, with data-
- * parallel counterparts: aggregation by a distance-2 maximal independent set
- * of the graph of entries |a_ij| > theta sqrt(|a_ii a_jj|) (rows without such
- * entries, e.g. Dirichlet rows, join no aggregate), Galerkin coarse matrices
+ * parallel counterparts: aggregation by a maximal independent set of the
+ * graph of entries |a_ij| > theta sqrt(|a_ii a_jj|) (a root and its
+ * neighbours; rows without such entries, e.g. Dirichlet rows, join no
+ * aggregate), Galerkin coarse matrices
  * P^T A P for the aggregate indicator P, Chebyshev smoothing with D^-1 and
  * the Gershgorin bound lmax of D^-1 A, coarse corrections scaled by omega,
- * a Chebyshev solve on the coarsest level.  FP64.  No FEALPy counterpart for
+ * a Chebyshev solve on the coarsest level.  PCG in FP64; the V-cycle in FP32
+ * when the levels carry FP32 copies (values32, dinv32), else FP64.  No
+ * FEALPy counterpart for
  * the individual kernels.
  *
  * One level (caller-owned arrays; agg, member_ptr, members and n_coarse for
@@ -512,6 +515,9 @@ typedef struct fgb_amg_level {
   int64_t n_coarse;         /* aggregates = rows of the next level            */
   const int64_t* member_ptr; /* n_coarse + 1: rows of each aggregate,         */
   const int32_t* members;    /* ascending                                     */
+  const float* values32;     /* optional FP32 copies of values and dinv, set  */
+  const float* dinv32;       /* on every level or on none: with them the      */
+                             /* V-cycle runs in FP32 (vectors and arithmetic) */
 } fgb_amg_level;
 
 /* Aggregates of a level: agg (n), their number, dinv (n) and lmax. */

@@ -32,6 +32,88 @@ def _fixture_system(golden_dir, name, dev):
     return A, torch.as_tensor(z["bc_F"], device=dev), z
 
 
+def _hash31(i):
+    """The aggregation's node priority (a 32-bit integer mix), restated."""
+    m = np.uint64(0xffffffff)
+    x = i.astype(np.uint64)
+    x ^= x >> np.uint64(16)
+    x = (x * np.uint64(0x7feb352d)) & m
+    x ^= x >> np.uint64(15)
+    x = (x * np.uint64(0x846ca68b)) & m
+    x ^= x >> np.uint64(16)
+    return x & np.uint64(0x7fffffff)
+
+
+def _mis_aggregates(A, theta=0.0):
+    """numpy restatement of the set-up's aggregation: maximal independent set
+    by rounds of (rank, priority, index) keys over the strong graph, roots
+    numbered in index order, every other node joining its largest-keyed
+    assigned neighbour (sweeps until none is left)."""
+    import scipy.sparse as sp
+    n = A.shape[0]
+    d = A.diagonal()
+    C = A.tocoo()
+    off = (C.row != C.col) & (C.data != 0)
+    if theta > 0:
+        off &= np.abs(C.data) > theta * np.sqrt(np.abs(d[C.row] * d[C.col]))
+    S = sp.csr_matrix((np.ones(off.sum()), (C.row[off], C.col[off])), shape=(n, n))
+    rows = np.repeat(np.arange(n), np.diff(S.indptr))
+    idx = np.arange(n).astype(np.uint64)
+    pr = _hash31(np.arange(n))
+    state = np.where(np.diff(S.indptr) == 0, -1, 1)
+    U = np.uint64
+    while (state == 1).any():
+        rank = np.where(state == 2, 2, np.where(state == 1, 1, 0)).astype(U)
+        key = np.where(state < 0, U(0), (rank << U(62)) | (pr << U(31)) | idx)
+        m = np.zeros(n, dtype=U)
+        np.maximum.at(m, rows, key[S.indices])
+        und = state == 1
+        root = und & (key > m)
+        out = und & ((m >> U(62)) == 2) & ~root
+        state[root] = 2
+        state[out] = 0
+    agg = np.full(n, -1, dtype=np.int64)
+    roots = np.nonzero(state == 2)[0]
+    agg[roots] = np.arange(len(roots))
+    while True:
+        cand = (agg[S.indices] >= 0)
+        kk = np.where(cand, ((U(1) << U(62)) | (pr[S.indices] << U(31)) | idx[S.indices]), U(0))
+        best = np.zeros(n, dtype=U)
+        np.maximum.at(best, rows, kk)
+        need = (agg < 0) & (state >= 0) & (best > 0)
+        if not need.any():
+            break
+        agg[need] = agg[(best[need] & U(0x7fffffff)).astype(np.int64)]
+    return agg, len(roots)
+
+
+def test_amg_hierarchy_matches_restatement(golden_dir):
+    """The aggregates equal the numpy restatement bit for bit, and the coarse
+    matrix equals P^T A P (scipy) to rounding."""
+    dev = cuda()
+    import scipy.sparse as sp
+    import fealpy_gb300 as F
+    A, b, z = _fixture_system(golden_dir, "cfg_c2_tet_p2_8.npz", dev)
+    Ah = sp.csr_matrix((z["bc_val"], z["bc_col"], z["bc_crow"]))
+    M = F.GAMGSolver().setup(A)
+    L0 = M.levels[0]
+    agg_ref, nc_ref = _mis_aggregates(Ah)
+    assert L0.n_coarse == nc_ref
+    assert np.array_equal(L0.agg.cpu().numpy(), agg_ref)
+    sizes = np.bincount(agg_ref[agg_ref >= 0])
+    assert 4 <= sizes.mean() <= 30, sizes.mean()
+    m = agg_ref >= 0
+    P = sp.csr_matrix((np.ones(m.sum()), (np.nonzero(m)[0], agg_ref[m])), shape=(Ah.shape[0], nc_ref))
+    Ac = (P.T @ Ah @ P).tocsr()
+    Ac.sort_indices()
+    L1 = M.levels[1]
+    got = sp.csr_matrix((L1.values.cpu().numpy(), L1.indices.cpu().numpy(), L1.indptr.cpu().numpy()),
+                        shape=(nc_ref, nc_ref))
+    assert np.array_equal(got.indptr, Ac.indptr) and np.array_equal(got.indices, Ac.indices)
+    assert np.max(np.abs(got.data - Ac.data)) <= 1e-12 * np.max(np.abs(Ac.data))
+    assert torch.equal(L0.values32, L0.values.to(torch.float32))
+
+
 def test_amg_pcg_c2_law_against_reference(golden_dir):
     dev = cuda()
     import fealpy_gb300 as F
