@@ -49,7 +49,7 @@ class AmgLevel(ctypes.Structure):
     """``fgb_amg_level`` (include/fealpy_gb300.h)."""
     _fields_ = [("n", c_i64), ("nnz", c_i64), ("indptr", c_vp), ("indices", c_vp), ("values", c_vp), ("dinv", c_vp),
                 ("lmax", c_dbl), ("agg", c_vp), ("n_coarse", c_i64), ("member_ptr", c_vp), ("members", c_vp),
-                ("values32", c_vp), ("dinv32", c_vp)]
+                ("values32", c_vp), ("dinv32", c_vp), ("sell", c_vp)]
 
 
 class PcgInfo(ctypes.Structure):

@@ -33,8 +33,29 @@ class _Level:
         self.nnz = indices.numel()
         self.dinv = None
         self.lmax = 0.0
-        self.agg = self.member_ptr = self.members = self.values32 = self.dinv32 = None
+        self.agg = self.member_ptr = self.members = self.values32 = self.dinv32 = self.sell = None
         self.n_coarse = 0
+
+
+def _level_sell(L: "_Level", with64: bool = False):
+    """SELL-32 copy of a level with FP32 values for its smoothing sweeps
+    (and FP64 values for PCG's operator when ``with64``): 15-bit column steps
+    where every row's columns ascend, else 4-byte columns; the solver's
+    autotuned launch shape."""
+    from . import solver as _solver
+    v64 = L.values if with64 else None
+    try:
+        S = K.sell_build(L.indptr, L.indices, v64, L.values32, want64=with64, want32=True, d15=True)
+    except _lib.FgbError:
+        S = K.sell_build(L.indptr, L.indices, v64, L.values32, want64=with64, want32=True, d16=False)
+    key = (S.n, S.padded_nnz, torch.float32, S.cols)
+    shape = _solver._LAUNCH_CACHE.get(key)
+    if shape is None:
+        times = K.sell_autotune(S, torch.float32)
+        shape = min(times, key=times.get)
+        _solver._LAUNCH_CACHE[key] = shape
+    S.set_launch(*shape)
+    return S
 
 
 class GAMGSolver:
@@ -49,12 +70,14 @@ class GAMGSolver:
     (coarse-correction scale, plain aggregation needs > 1), ``cdeg`` (degree
     of the coarsest Chebyshev solve), ``max_levels``, ``vcycle_f32`` (the
     V-cycle runs in FP32 on FP32 copies of the level matrices; the PCG
-    operator and its vectors stay FP64)."""
+    operator and its vectors stay FP64), ``sell_min_rows`` (levels of at
+    least this many rows smooth on a SELL-32 copy, 15-bit column steps where
+    the columns ascend, instead of the CSR arrays)."""
 
     def __init__(self, theta: float = 0.0, csize: int = 300, ctype: str = "A", itype: str = "T", ptype: str = "V",
                  sstep: int = 3, isolver: str = "CG", maxit: int = 200, csolver: str = "chebyshev",
                  rtol: float = 1e-8, atol: float = 1e-8, omega: float = 1.7, cdeg: int = 16, max_levels: int = 10,
-                 vcycle_f32: bool = True):
+                 vcycle_f32: bool = True, sell_min_rows: int = 1 << 16):
         if ptype != "V":
             raise NotImplementedError("the GB300 multigrid provides V-cycles")
         if isolver not in ("CG", "MG"):
@@ -63,6 +86,7 @@ class GAMGSolver:
         self.isolver, self.maxit, self.rtol, self.atol = isolver, int(maxit), float(rtol), float(atol)
         self.omega, self.cdeg, self.max_levels = float(omega), int(cdeg), int(max_levels)
         self.vcycle_f32 = bool(vcycle_f32)
+        self.sell_min_rows = int(sell_min_rows)
         self.levels: List[_Level] = []
         self._desc = None
         self.A = None
@@ -119,9 +143,12 @@ class GAMGSolver:
                  cws.numel(), s)
             check_status_word("multigrid coarse matrix (aggregate rows above the candidate capacity)", st)
             lev = _Level(cptr, ccol[: int(nnz.value)], cval[: int(nnz.value)])
-        for L in self.levels:
+        for k, L in enumerate(self.levels):
             L.values32 = L.values.to(torch.float32) if self.vcycle_f32 else None
             L.dinv32 = L.dinv.to(torch.float32) if self.vcycle_f32 else None
+            if self.vcycle_f32 and L.n >= self.sell_min_rows:
+                # the finest copy also carries the FP64 values: PCG's operator
+                L.sell = _level_sell(L, with64=(k == 0))
         self._desc = (_lib.AmgLevel * len(self.levels))()
         for k, L in enumerate(self.levels):
             d = self._desc[k]
@@ -131,6 +158,7 @@ class GAMGSolver:
             d.lmax = L.lmax
             d.values32 = L.values32.data_ptr() if L.values32 is not None else None
             d.dinv32 = L.dinv32.data_ptr() if L.dinv32 is not None else None
+            d.sell = ctypes.addressof(L.sell.desc) if L.sell is not None else None
             if L.agg is not None:
                 d.agg, d.n_coarse = L.agg.data_ptr(), L.n_coarse
                 d.member_ptr, d.members = L.member_ptr.data_ptr(), L.members.data_ptr()

@@ -22,8 +22,11 @@
 //   coarse matrix  A_c = P^T A P with P the aggregate indicator: the members
 //                of every aggregate (counting sort, each list sorted), and per
 //                coarse row the entries of the member rows mapped to their
-//                aggregates, sorted by (coarse column, position) in shared
-//                memory and summed in that order (count pass, scan, fill pass).
+//                aggregates and summed per coarse column in a fixed order: by
+//                one warp through a shared-memory hash table (rows of up to
+//                192 coarse columns), else by a block that sorts the entries
+//                by (coarse column, position) in shared memory (count pass,
+//                scan, fill pass).
 //   bounds       per row 1/a_ii and the Gershgorin bound of D^-1 A (max over
 //                rows of sum_j |a_ij| / |a_ii|), for the Chebyshev smoother.
 // Apply (V-cycle on r, from x = 0): Chebyshev smoothing of degree `deg` with
@@ -98,6 +101,7 @@ template <int G>
 __global__ void amg_diag_kernel(int64_t n, const int64_t* __restrict__ indptr, const int32_t* __restrict__ indices,
                                 const double* __restrict__ values, double* __restrict__ diag,
                                 unsigned long long* __restrict__ bound_bits, int32_t* status) {
+  unsigned long long bmax = 0ull;
   AMG_ROW_LOOP(n, G) {
     const bool active = i < n;
     double d = 0.0, s = 0.0;
@@ -117,11 +121,14 @@ __global__ void amg_diag_kernel(int64_t n, const int64_t* __restrict__ indptr, c
       if (!(d > 0.0) || !isfinite(d)) {
         set_status(status, FGB_ERR_BREAKDOWN);  // an SPD matrix has a positive diagonal
       } else {
-        const double b = s / d;
-        atomicMax(bound_bits, static_cast<unsigned long long>(__double_as_longlong(b)));  // positive doubles order as ints
+        const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(s / d));
+        bmax = b > bmax ? b : bmax;  // positive doubles order as integers
       }
     }
   }
+  // one atomic per warp
+  bmax = group_max<32>(bmax);
+  if ((threadIdx.x & 31) == 0 && bmax) atomicMax(bound_bits, bmax);
 }
 
 // state: 1 undecided, 2 root, 0 out, -1 isolated (no strong off-diagonal)
@@ -390,7 +397,108 @@ __device__ bool amg_coarse_row(int64_t n, int64_t I, int mode, const int64_t* __
   return true;
 }
 
-__global__ void __launch_bounds__(kCoarseThreads) amg_coarse_rows(int64_t n, int64_t nc, int mode,
+constexpr int kWarpRowWarps = 8;   // warps per block of the warp path
+constexpr int kHashSlots = 256;    // coarse columns per warp (open addressing)
+constexpr int kHashMax = 192;      // distinct coarse columns the warp path takes
+
+// Coarse row I by one warp (the common case): the member rows' entries,
+// member by member in CSR order, 32 at a time; lanes with the same coarse
+// column J (the aggregate of the entry's column) sum their values in lane
+// order, and the lowest of them adds that sum to J's slot of a shared-memory
+// hash table (chunks in order, so every J's sum is taken in a fixed order).
+// mode 0: the number of distinct J to cnt[I]; mode 1: columns ascending and
+// values at cptr[I].  A row with more than kHashMax distinct J goes to the
+// overflow list (block path).
+__global__ void __launch_bounds__(kWarpRowWarps * 32) amg_coarse_rows_warp(
+    int64_t n, int64_t nc, int mode, const int64_t* __restrict__ indptr, const int32_t* __restrict__ indices,
+    const double* __restrict__ values, const int32_t* __restrict__ agg, const int64_t* __restrict__ mptr,
+    const int32_t* __restrict__ members, int32_t* __restrict__ cnt, const int64_t* __restrict__ cptr,
+    int32_t* __restrict__ ccol, double* __restrict__ cval, int32_t* __restrict__ ovf, int32_t* __restrict__ ovf_len) {
+  __shared__ int32_t hkey[kWarpRowWarps][kHashSlots];
+  __shared__ double hval[kWarpRowWarps][kHashSlots];
+  __shared__ double stage[kWarpRowWarps][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int32_t* K = hkey[w];
+  double* V = hval[w];
+  double* S = stage[w];
+  const int64_t gw = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
+  const int64_t nw = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+  for (int64_t I = gw; I < nc; I += nw) {
+    for (int t = lane; t < kHashSlots; t += 32) {
+      K[t] = -1;
+      V[t] = 0.0;
+    }
+    __syncwarp();
+    bool over = false;  // warp-uniform
+    int distinct = 0;   // warp-uniform
+    const int64_t m0 = mptr[I], m1 = mptr[I + 1];
+    for (int64_t k = m0; k < m1 && !over; ++k) {
+      const int32_t row = members[k];
+      const int64_t a = indptr[row], b = indptr[row + 1];
+      for (int64_t e0 = a; e0 < b && !over; e0 += 32) {
+        const int64_t e = e0 + lane;
+        int32_t J = -1;
+        double v = 0.0;
+        if (e < b) {
+          const int32_t j = indices[e];
+          if (j >= 0 && j < n) J = agg[j];
+          v = values[e];
+        }
+        S[lane] = v;
+        __syncwarp();
+        const unsigned grp = __match_any_sync(0xffffffffu, J);
+        int claimed = 0, fail = 0;
+        if (J >= 0 && __ffs(grp) - 1 == lane) {
+          double sum = 0.0;
+          for (unsigned m = grp; m; m &= m - 1) sum += S[__ffs(m) - 1];
+          unsigned h = (static_cast<unsigned>(J) * 2654435761u) >> 24;
+          int probes = 0;
+          while (true) {
+            const int32_t old = atomicCAS(&K[h], -1, J);
+            if (old == -1) {
+              claimed = 1;
+              break;
+            }
+            if (old == J) break;
+            h = (h + 1) & (kHashSlots - 1);
+            if (++probes >= kHashSlots) {
+              fail = 1;
+              break;
+            }
+          }
+          if (!fail) V[h] += sum;
+        }
+        distinct += __popc(__ballot_sync(0xffffffffu, claimed));
+        over = __any_sync(0xffffffffu, fail) || distinct > kHashMax;
+        __syncwarp();
+      }
+    }
+    if (over) {
+      if (lane == 0) ovf[atomicAdd(ovf_len, 1)] = static_cast<int32_t>(I);
+    } else if (mode == 0) {
+      if (lane == 0) cnt[I] = distinct;
+    } else {
+      // ascending J: each occupied slot's rank among the occupied keys
+      const int64_t out0 = cptr[I];
+      for (int t = lane; t < kHashSlots; t += 32) {
+        const int32_t J = K[t];
+        if (J < 0) continue;
+        int rank = 0;
+        for (int u = 0; u < kHashSlots; ++u) {
+          const int32_t q = K[u];
+          rank += (q >= 0 && q < J) ? 1 : 0;
+        }
+        ccol[out0 + rank] = J;
+        cval[out0 + rank] = V[t];
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// Coarse rows of a list (the warp path's overflow) by a block each; rows
+// above kCoarseCap candidates go on to the next list.
+__global__ void __launch_bounds__(kCoarseThreads) amg_coarse_rows(int64_t n, int mode,
                                                                  const int64_t* __restrict__ indptr,
                                                                  const int32_t* __restrict__ indices,
                                                                  const double* __restrict__ values,
@@ -400,14 +508,18 @@ __global__ void __launch_bounds__(kCoarseThreads) amg_coarse_rows(int64_t n, int
                                                                  int32_t* __restrict__ cnt,
                                                                  const int64_t* __restrict__ cptr,
                                                                  int32_t* __restrict__ ccol, double* __restrict__ cval,
+                                                                 const int32_t* __restrict__ rows,
+                                                                 const int32_t* __restrict__ rows_len,
                                                                  int32_t* __restrict__ ovf, int32_t* __restrict__ ovf_len) {
   __shared__ unsigned long long kbuf[kCoarseCap];
   __shared__ double vbuf[kCoarseCap];
   __shared__ int sh[2 + kCoarseThreads / 32];  // candidate count, fill offset, warp totals
-  for (int64_t I = blockIdx.x; I < nc; I += gridDim.x) {
+  const int nr = *rows_len;
+  for (int r = blockIdx.x; r < nr; r += gridDim.x) {
+    const int32_t I = rows[r];
     const bool ok = amg_coarse_row(n, I, mode, indptr, indices, values, agg, mptr, members, cnt, cptr, ccol, cval, kbuf,
                                    vbuf, kCoarseCap, sh, sh + 1);
-    if (!ok && threadIdx.x == 0) ovf[atomicAdd(ovf_len, 1)] = static_cast<int32_t>(I);
+    if (!ok && threadIdx.x == 0) ovf[atomicAdd(ovf_len, 1)] = I;
     __syncthreads();
   }
 }
@@ -541,6 +653,7 @@ __global__ void amg_prolong(int64_t n, const int32_t* __restrict__ agg, const T*
 // ------------------------------------------------------------ PCG kernels
 constexpr int kDotBlocks = 2 * kNumSMs;
 constexpr int kMaxGrid = kNumSMs * 16;  // grids of every kernel here (grid_for caps)
+static_assert(2 * kMaxGrid >= kNumSMs * 8, "the partials buffer holds a SELL launch's block partials");
 
 // Deterministic two-value reduction: per-block sums in a fixed order, the last
 // block adds the blocks' sums in block order into out[0..1].
@@ -733,6 +846,28 @@ void with_lanes(int G, F&& f) {
   }
 }
 
+// smoother sweep of a level's SELL copy, and Ap = A p with per-block p.Ap
+// partials on its FP64 values (sell.cu)
+int sell_smooth_f32(const fgb_sell* A, const float* dinv, const float* r, const float* x_in, float* x_out, float* d,
+                    float c1, float c2, int mode, cudaStream_t st);
+int sell_spmv_pap_f64(const fgb_sell* A, const double* p, double* Ap, double* bpart, int* n_part, cudaStream_t st);
+
+// out[0] = sum of part[0..nb) in a fixed order (one block), out[1] = 0
+__global__ void amg_sum_partials(const double* __restrict__ part, int nb, double* __restrict__ out) {
+  __shared__ double ws[32];
+  double t = 0.0;
+  for (int k = threadIdx.x; k < nb; k += blockDim.x) t += part[k];
+  t = warp_sum(t);
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = t;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0;
+    for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) a += ws[w];
+    out[0] = a;
+    out[1] = 0.0;
+  }
+}
+
 }  // namespace fgb
 
 using namespace fgb;
@@ -774,6 +909,12 @@ const T* level_dinv(const fgb_amg_level& L) {
 template <typename T>
 void cheb_sweep(const fgb_amg_level& L, const T* r, const T* x_in, T* x_out, T* d, double c1, double c2,
                 cudaStream_t st) {
+  if constexpr (std::is_same<T, float>::value) {
+    if (L.sell) {
+      sell_smooth_f32(L.sell, L.dinv32, r, x_in, x_out, d, static_cast<float>(c1), static_cast<float>(c2), 0, st);
+      return;
+    }
+  }
   const int64_t n = L.n;
   const T* vals = level_values<T>(L);
   const T* dinv = level_dinv<T>(L);
@@ -848,11 +989,19 @@ int vcycle(const fgb_amg_level* levels, int nl, const double* r0, double* x_out,
     cheb<T>(L, rin, V[l].x, V[l].x2, V[l].d, deg, 0.1, true, &xo, st);
     xs[l] = xo;
     const T* vals = level_values<T>(L);
-    with_lanes(amg_lanes(n, L.nnz), [&](auto g) {
-      constexpr int GG = decltype(g)::value;
-      amg_residual<GG, T, T><<<rows_grid(n, GG), kAmgThreads, 0, st>>>(n, L.indptr, L.indices, vals, rin, xo,
-                                                                        V[l].res);
-    });
+    bool done = false;
+    if constexpr (std::is_same<T, float>::value) {
+      if (L.sell) {
+        sell_smooth_f32(L.sell, nullptr, rin, xo, V[l].res, nullptr, 0.0f, 0.0f, 1, st);
+        done = true;
+      }
+    }
+    if (!done)
+      with_lanes(amg_lanes(n, L.nnz), [&](auto g) {
+        constexpr int GG = decltype(g)::value;
+        amg_residual<GG, T, T><<<rows_grid(n, GG), kAmgThreads, 0, st>>>(n, L.indptr, L.indices, vals, rin, xo,
+                                                                          V[l].res);
+      });
     amg_restrict<T><<<vec_grid(L.n_coarse), kAmgThreads, 0, st>>>(L.n_coarse, L.member_ptr, L.members, V[l].res,
                                                                   V[l + 1].r);
     rin = V[l + 1].r;
@@ -893,6 +1042,7 @@ int levels_mode(const fgb_amg_level* levels, int nl) {
     if (L.n <= 0 || !L.indptr || !L.indices || !L.values || !L.dinv || !(L.lmax > 0.0)) return -1;
     if (l < nl - 1 && (!L.agg || !L.member_ptr || !L.members || L.n_coarse != levels[l + 1].n)) return -1;
     if ((L.values32 == nullptr) != (L.dinv32 == nullptr)) return -1;
+    if (L.sell && (!L.values32 || L.sell->n != L.n || !L.sell->val32)) return -1;
     n32 += L.values32 ? 1 : 0;
   }
   if (n32 != 0 && n32 != nl) return -1;
@@ -1007,9 +1157,30 @@ int32_t fgb_amg_aggregate(int64_t n, const int64_t* indptr, const int32_t* indic
 
 size_t fgb_amg_coarse_workspace_bytes(int64_t n, int64_t n_coarse) {
   const size_t c = static_cast<size_t>(n_coarse) + 1;
-  return align_up(c * 4) * 3 + align_up(sizeof(int32_t)) + scan_workspace_bytes(n_coarse + 1) +
-         align_up(static_cast<size_t>(n) * 0 + 8);
+  (void)n;
+  return align_up(c * 4) * 4 + align_up(4 * sizeof(int32_t)) + scan_workspace_bytes(n_coarse + 1);
 }
+
+namespace {
+
+// Rows of the next level, count (mode 0, to rowcnt) or fill (mode 1): the
+// warp path, its overflow by blocks, theirs by blocks with 128 KB of shared
+// memory (above that: capacity error).
+void coarse_rows(int64_t n, int mode, const int64_t* indptr, const int32_t* indices, const double* values,
+                 const int32_t* agg, int64_t n_coarse, const int64_t* member_ptr, const int32_t* members,
+                 int32_t* rowcnt, const int64_t* cptr, int32_t* ccol, double* cval, int32_t* ovf, int32_t* ovf2,
+                 int32_t* lens, int32_t* status, cudaStream_t st) {
+  amg_coarse_rows_warp<<<grid_for(n_coarse * 32, kWarpRowWarps * 32, kNumSMs * 16), kWarpRowWarps * 32, 0, st>>>(
+      n, n_coarse, mode, indptr, indices, values, agg, member_ptr, members, rowcnt, cptr, ccol, cval, ovf, lens);
+  amg_coarse_rows<<<kNumSMs * 2, kCoarseThreads, 0, st>>>(n, mode, indptr, indices, values, agg, member_ptr, members,
+                                                          rowcnt, cptr, ccol, cval, ovf, lens, ovf2, lens + 1);
+  const size_t big = static_cast<size_t>(kCoarseBigCap) * 16;
+  cudaFuncSetAttribute(amg_coarse_rows_big, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(big));
+  amg_coarse_rows_big<<<kNumSMs, kCoarseThreads, big, st>>>(n, mode, indptr, indices, values, agg, member_ptr,
+                                                             members, rowcnt, cptr, ccol, cval, ovf2, lens + 1, status);
+}
+
+}  // namespace
 
 int32_t fgb_amg_coarse_count(int64_t n, const int64_t* indptr, const int32_t* indices, const double* values,
                              const int32_t* agg, int64_t n_coarse, int64_t* member_ptr, int32_t* members,
@@ -1018,13 +1189,15 @@ int32_t fgb_amg_coarse_count(int64_t n, const int64_t* indptr, const int32_t* in
   if (n <= 0 || n_coarse <= 0 || !indptr || !indices || !values || !agg || !member_ptr || !members ||
       !coarse_indptr || !nnz_host || !status)
     return FGB_ERR_ARG;
+  if (n_coarse >= (int64_t(1) << 31)) return FGB_ERR_CAPACITY;
   if (!workspace || workspace_bytes < fgb_amg_coarse_workspace_bytes(n, n_coarse)) return FGB_ERR_WORKSPACE;
   cudaStream_t st = as_stream(stream);
   Carver cv(workspace, workspace_bytes);
   int32_t* cnt = cv.take<int32_t>(n_coarse + 1);
   int32_t* ovf = cv.take<int32_t>(n_coarse + 1);
+  int32_t* ovf2 = cv.take<int32_t>(n_coarse + 1);
   int32_t* rowcnt = cv.take<int32_t>(n_coarse + 1);
-  int32_t* ovf_len = cv.take<int32_t>(1);
+  int32_t* lens = cv.take<int32_t>(4);
   void* scan_ws = cv.base + cv.off;
   const size_t scan_bytes = workspace_bytes - cv.off;
   if (!cv.ok) return FGB_ERR_WORKSPACE;
@@ -1035,14 +1208,9 @@ int32_t fgb_amg_coarse_count(int64_t n, const int64_t* indptr, const int32_t* in
   if (cudaMemsetAsync(cnt, 0, (n_coarse + 1) * sizeof(int32_t), st) != cudaSuccess) return FGB_ERR_CUDA;
   amg_member_fill<<<vec_grid(n), kAmgThreads, 0, st>>>(n, agg, member_ptr, cnt, members);
   amg_member_sort<<<vec_grid(n_coarse), kAmgThreads, 0, st>>>(n_coarse, member_ptr, members);
-  if (cudaMemsetAsync(ovf_len, 0, sizeof(int32_t), st) != cudaSuccess) return FGB_ERR_CUDA;
-  amg_coarse_rows<<<grid_for(n_coarse, 1, kNumSMs * 8), kCoarseThreads, 0, st>>>(
-      n, n_coarse, 0, indptr, indices, values, agg, member_ptr, members, rowcnt, nullptr, nullptr, nullptr, ovf,
-      ovf_len);
-  const size_t big = static_cast<size_t>(kCoarseBigCap) * 16;
-  cudaFuncSetAttribute(amg_coarse_rows_big, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(big));
-  amg_coarse_rows_big<<<kNumSMs, kCoarseThreads, big, st>>>(n, 0, indptr, indices, values, agg, member_ptr, members,
-                                                             rowcnt, nullptr, nullptr, nullptr, ovf, ovf_len, status);
+  if (cudaMemsetAsync(lens, 0, 4 * sizeof(int32_t), st) != cudaSuccess) return FGB_ERR_CUDA;
+  coarse_rows(n, 0, indptr, indices, values, agg, n_coarse, member_ptr, members, rowcnt, nullptr, nullptr, nullptr,
+              ovf, ovf2, lens, status, st);
   rc = exclusive_scan_i32_to_i64(rowcnt, n_coarse, coarse_indptr, scan_ws, scan_bytes, st);
   if (rc) return rc;
   if (cudaMemcpyAsync(nnz_host, coarse_indptr + n_coarse, sizeof(int64_t), cudaMemcpyDeviceToHost, st) != cudaSuccess)
@@ -1058,24 +1226,20 @@ int32_t fgb_amg_coarse_fill(int64_t n, const int64_t* indptr, const int32_t* ind
   if (n <= 0 || n_coarse <= 0 || !indptr || !indices || !values || !agg || !member_ptr || !members ||
       !coarse_indptr || !coarse_indices || !coarse_values || !status)
     return FGB_ERR_ARG;
+  if (n_coarse >= (int64_t(1) << 31)) return FGB_ERR_CAPACITY;
   if (!workspace || workspace_bytes < fgb_amg_coarse_workspace_bytes(n, n_coarse)) return FGB_ERR_WORKSPACE;
   cudaStream_t st = as_stream(stream);
   Carver cv(workspace, workspace_bytes);
   int32_t* cnt = cv.take<int32_t>(n_coarse + 1);
   int32_t* ovf = cv.take<int32_t>(n_coarse + 1);
+  int32_t* ovf2 = cv.take<int32_t>(n_coarse + 1);
   int32_t* rowcnt = cv.take<int32_t>(n_coarse + 1);
-  int32_t* ovf_len = cv.take<int32_t>(1);
+  int32_t* lens = cv.take<int32_t>(4);
   if (!cv.ok) return FGB_ERR_WORKSPACE;
   (void)cnt;
-  if (cudaMemsetAsync(ovf_len, 0, sizeof(int32_t), st) != cudaSuccess) return FGB_ERR_CUDA;
-  amg_coarse_rows<<<grid_for(n_coarse, 1, kNumSMs * 8), kCoarseThreads, 0, st>>>(
-      n, n_coarse, 1, indptr, indices, values, agg, member_ptr, members, rowcnt, coarse_indptr, coarse_indices,
-      coarse_values, ovf, ovf_len);
-  const size_t big = static_cast<size_t>(kCoarseBigCap) * 16;
-  cudaFuncSetAttribute(amg_coarse_rows_big, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(big));
-  amg_coarse_rows_big<<<kNumSMs, kCoarseThreads, big, st>>>(n, 1, indptr, indices, values, agg, member_ptr, members,
-                                                             rowcnt, coarse_indptr, coarse_indices, coarse_values, ovf,
-                                                             ovf_len, status);
+  if (cudaMemsetAsync(lens, 0, 4 * sizeof(int32_t), st) != cudaSuccess) return FGB_ERR_CUDA;
+  coarse_rows(n, 1, indptr, indices, values, agg, n_coarse, member_ptr, members, rowcnt, coarse_indptr, coarse_indices,
+              coarse_values, ovf, ovf2, lens, status, st);
   return launch_status();
 }
 
@@ -1186,11 +1350,22 @@ int32_t fgb_pcg_amg(const fgb_amg_level* levels, int32_t n_levels, int32_t deg, 
         rc = FGB_ERR_CUDA;
         break;
       }
-      with_lanes(G, [&](auto gl) {
-        constexpr int GG = decltype(gl)::value;
-        amg_pcg_spmv<GG, double><<<rows_grid(n, GG), kAmgThreads, 0, cs>>>(n, L.indptr, L.indices, L.values, p, Ap,
-                                                                            partials, counter, s->red);
-      });
+      if (L.sell && L.sell->val64) {
+        // the operator on the level's SELL copy: Ap and block partials of p.Ap
+        int nb = 0;
+        if ((rc = sell_spmv_pap_f64(L.sell, p, Ap, partials, &nb, cs)) != FGB_OK) {
+          cudaGraph_t dummy = nullptr;
+          cudaStreamEndCapture(cs, &dummy);
+          break;
+        }
+        amg_sum_partials<<<1, 256, 0, cs>>>(partials, nb, s->red);
+      } else {
+        with_lanes(G, [&](auto gl) {
+          constexpr int GG = decltype(gl)::value;
+          amg_pcg_spmv<GG, double><<<rows_grid(n, GG), kAmgThreads, 0, cs>>>(n, L.indptr, L.indices, L.values, p,
+                                                                              Ap, partials, counter, s->red);
+        });
+      }
       amg_pcg_update_dev<<<kDotBlocks, kAmgThreads, 0, cs>>>(n, s, p, Ap, x, r, partials, counter);
       const int vrc = V.run(levels, n_levels, r, z, deg, cdeg, omega, cs);
       amg_dot2<<<kDotBlocks, kAmgThreads, 0, cs>>>(n, r, z, partials, counter, s->red + 4);

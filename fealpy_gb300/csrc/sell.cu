@@ -188,6 +188,72 @@ __global__ void __launch_bounds__(1024, 1) sell_spmv_kernel(SellView A, const T*
   }
 }
 
+// Smoother sweep of an FP32 copy (a multigrid level matrix): mode 0, a
+// Chebyshev step d = c1 d + c2 dinv (r - A x_in), x_out = x_in + d (d is not
+// read when c1 = 0); mode 1, the residual x_out = r - A x_in.
+template <int FMT>
+__global__ void __launch_bounds__(1024, 1) sell_smooth_kernel(SellView A, const float* __restrict__ val,
+                                                               const float* __restrict__ dinv,
+                                                               const float* __restrict__ r,
+                                                               const float* __restrict__ x_in,
+                                                               float* __restrict__ x_out, float* __restrict__ d,
+                                                               float c1, float c2, int mode) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
+  const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+  const GatherX<float> g{x_in};
+  for (int64_t s = warp; s < A.n_slices; s += nwarps) {
+    const float acc = slice_row<FMT, float, float>(A, val, s, lane, g);
+    const int32_t row = A.perm[s * kSellC + lane];
+    if (row < 0) continue;
+    const float res = r[row] - acc;
+    if (mode) {
+      x_out[row] = res;
+    } else {
+      const float di = (c1 != 0.0f ? c1 * d[row] : 0.0f) + c2 * dinv[row] * res;
+      d[row] = di;
+      x_out[row] = x_in[row] + di;
+    }
+  }
+}
+
+// Ap = A p (FP64 values) with per-block p.Ap partials in bpart (warps'
+// sums combined in warp order by the block's last warp).
+template <int FMT>
+__global__ void __launch_bounds__(1024, 1) sell_spmv_pap_kernel(SellView A, const double* __restrict__ val,
+                                                                 const double* __restrict__ p,
+                                                                 double* __restrict__ Ap, double* bpart) {
+  __shared__ double wslot[32];
+  __shared__ unsigned int arrivals;
+  if (threadIdx.x == 0) arrivals = 0u;
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
+  const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+  double pap = 0.0;
+  for (int64_t s = warp; s < A.n_slices; s += nwarps) {
+    const double acc = slice_row<FMT, double, double>(A, val, s, lane, GatherX<double>{p});
+    const int32_t row = A.perm[s * kSellC + lane];
+    if (row >= 0) {
+      Ap[row] = acc;
+      pap += p[row] * acc;
+    }
+  }
+  pap = warp_sum(pap);
+  if (lane == 0) {
+    const unsigned int nw = blockDim.x >> 5;
+    wslot[threadIdx.x >> 5] = pap;
+    __threadfence_block();
+    if (atomicAdd(&arrivals, 1u) == nw - 1) {
+      __threadfence_block();
+      const volatile double* ws = wslot;
+      double t = 0.0;
+      for (unsigned int k = 0; k < nw; ++k) t += ws[k];
+      bpart[blockIdx.x] = t;
+    }
+  }
+}
+
 // ------------------------------------------------------------ PCG kernels
 struct SellPcgState {
   double rz, rz_prev, rr, alpha, beta, b_norm, tol, atol, resid, r_upd, true_rel;
@@ -1258,6 +1324,36 @@ int finish(int done) {
 }
 
 }  // namespace
+
+namespace fgb {
+
+// Smoother sweep on the FP32 values of a SELL copy (used by the multigrid
+// V-cycle for its large levels); the shape of the copy's launch.
+int sell_smooth_f32(const fgb_sell* A, const float* dinv, const float* r, const float* x_in, float* x_out, float* d,
+                    float c1, float c2, int mode, cudaStream_t st) {
+  if (!A || !A->val32 || !launch_ok(A) || !r || !x_in || !x_out || (mode == 0 && (!dinv || !d))) return FGB_ERR_ARG;
+  const SellView V = view_of(A);
+  with_cols(V, [&](auto f) {
+    constexpr int FMT = decltype(f)::value;
+    sell_smooth_kernel<FMT><<<SLICE_LAUNCH(V, st)>>>(V, A->val32, dinv, r, x_in, x_out, d, c1, c2, mode);
+  });
+  return FGB_OK;
+}
+
+// Ap = A p on the FP64 values of a SELL copy; per-block p.Ap partials in
+// bpart (at least kSellMaxBlocks doubles), their number in *n_part.
+int sell_spmv_pap_f64(const fgb_sell* A, const double* p, double* Ap, double* bpart, int* n_part, cudaStream_t st) {
+  if (!A || !A->val64 || !launch_ok(A) || !p || !Ap || !bpart || !n_part) return FGB_ERR_ARG;
+  const SellView V = view_of(A);
+  *n_part = slice_blocks(V);
+  with_cols(V, [&](auto f) {
+    constexpr int FMT = decltype(f)::value;
+    sell_spmv_pap_kernel<FMT><<<SLICE_LAUNCH(V, st)>>>(V, A->val64, p, Ap, bpart);
+  });
+  return FGB_OK;
+}
+
+}  // namespace fgb
 
 extern "C" {
 

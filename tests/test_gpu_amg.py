@@ -157,6 +157,14 @@ def test_amg_bench_workload_24_against_oracle():
     x, info = F.cg(A2, F2, M=M, atol=0.0, rtol=1e-10, returninfo=True, stop="residual")
     assert info["reason"] == 2 and info["niter"] < 120, info
     assert rel(x, ref["x"]) < 1e-8
+    # level 0 (117649 rows) smooths on its SELL copy; the CSR sweeps give the
+    # same V-cycle to FP32 rounding, and an FP64 V-cycle to FP32 accuracy
+    assert M.levels[0].sell is not None
+    z_sell = M.vcycle(F2)
+    z_csr = F.GAMGSolver(sell_min_rows=1 << 40).setup(A2).vcycle(F2)
+    z_64 = F.GAMGSolver(vcycle_f32=False).setup(A2).vcycle(F2)
+    assert rel(z_sell, z_csr.cpu().numpy()) < 1e-4
+    assert rel(z_sell, z_64.cpu().numpy()) < 1e-4
     # the reference's solver interface: setup + solve, CG and MG
     xs, inf = F.GAMGSolver(rtol=1e-10, atol=1e-30, maxit=500).setup(A2).solve(F2)
     assert inf["niter"] > 0 and rel(xs, ref["x"]) < 1e-8
