@@ -187,15 +187,16 @@ def solve_step(torch, F, space, kappa, bc, mode, profile=False, marks=None, asm_
     mark()
     A2, F2 = bc.apply(A, Fv)
     mark()
-    if mode != "amg":
+    if not mode.startswith("amg"):
         _sell_of(A2, want32=(mode != "fp64"))
     mark()
-    if mode == "amg":
-        # FP64 PCG preconditioned by the aggregation AMG V-cycle (set-up inside the step)
+    if mode.startswith("amg"):
+        # FP64 PCG preconditioned by the aggregation AMG V-cycle (set-up inside
+        # the step): V-cycle in FP32 ("amg") or FP64 ("amg64")
         s0 = torch.cuda.Event(enable_timing=True)
         s1 = torch.cuda.Event(enable_timing=True)
         s0.record()
-        M = F.GAMGSolver().setup(A2)
+        M = F.GAMGSolver(vcycle_f32=(mode == "amg")).setup(A2)
         s1.record()
         x, info = F.cg(A2, F2, M=M, atol=0.0, rtol=RTOL, maxit=MAXIT, returninfo=True, stop="residual")
         info["amg_levels_n"] = [L.n for L in M.levels]
@@ -210,6 +211,26 @@ def solve_step(torch, F, space, kappa, bc, mode, profile=False, marks=None, asm_
                        profile=profile, graph=graph)
     mark()
     return x, info, A2, F2
+
+
+def amg_record(results, fp64, mixed, world, gdof):
+    """C2 with the aggregation AMG V-cycle in cg's M slot (GAMGSolver: MIS
+    aggregation, Galerkin coarse levels, Chebyshev smoothing; set-up inside the
+    step; PCG and its operator FP64): the V-cycle in FP32 and in FP64."""
+    out = {}
+    for key, mode in (("fp32_vcycle", "amg"), ("fp64_vcycle", "amg64")):
+        r = results.get(mode)
+        if r is None:
+            continue
+        out[key] = {"ms_per_step": r["ms_per_step"], "dof_per_s": world * gdof / (r["ms_per_step"] / 1e3),
+                    "cg_iters": r["niter"], "true_relres": r["relres"],
+                    "max_rel_err_vs_fp64_jacobi": float((r["x"] - fp64["x"]).abs().max() / fp64["x"].abs().max()),
+                    "levels_rows": r["amg_levels"], "setup_ms": r["amg_setup_ms"], "stages_ms": r["stages_ms"],
+                    "speedup_vs_fp64_jacobi": fp64["ms_per_step"] / r["ms_per_step"],
+                    "speedup_vs_fp32_refined_jacobi": mixed["ms_per_step"] / r["ms_per_step"]}
+    if "fp32_vcycle" in out and "fp64_vcycle" in out:
+        out["speedup_fp32_vcycle_vs_fp64_vcycle"] = results["amg64"]["ms_per_step"] / results["amg"]["ms_per_step"]
+    return out or None
 
 
 def spmv_roofline(mixed, gdof, n, peak, peak_kind):
@@ -467,18 +488,7 @@ def run_ours(args):
                      "other_kernels_us": fp64["extra_ms_avg"] * 1e3,
                      "sell_launch_threads_blocks": fp64["sell_launch"], "sell_columns": fp64["sell_cols"]},
             "speedup_fp32_refined_vs_fp64": fp64["ms_per_step"] / mixed["ms_per_step"],
-            "fp64_amg": None if "amg" not in results else {
-                "preconditioner": ("aggregation AMG V-cycle (GAMGSolver: MIS aggregation, Galerkin coarse levels, "
-                                   "Chebyshev smoothing; set-up inside the step); PCG and its operator FP64, "
-                                   "V-cycle FP32 on SELL copies of the large levels"),
-                "ms_per_step": results["amg"]["ms_per_step"],
-                "dof_per_s": world * gdof / (results["amg"]["ms_per_step"] / 1e3),
-                "cg_iters": results["amg"]["niter"], "true_relres": results["amg"]["relres"],
-                "max_rel_err_vs_fp64": float((results["amg"]["x"] - fp64["x"]).abs().max() / fp64["x"].abs().max()),
-                "levels_rows": results["amg"]["amg_levels"], "setup_ms": results["amg"]["amg_setup_ms"],
-                "stages_ms": results["amg"]["stages_ms"],
-                "speedup_vs_fp64_jacobi": fp64["ms_per_step"] / results["amg"]["ms_per_step"],
-                "speedup_vs_fp32_refined_jacobi": mixed["ms_per_step"] / results["amg"]["ms_per_step"]},
+            "amg": amg_record(results, fp64, mixed, world, gdof),
             "e2e": {"value": world * gdof * e2e_steps / (e2e_ms / 1e3), "unit": "DOF/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "steps": e2e_steps},
             "gpu_launches": mixed["launches"],
@@ -995,7 +1005,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=64)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--modes", default="fp64,mixed,mixed64,amg",
+    ap.add_argument("--modes", default="fp64,mixed,mixed64,amg,amg64",
                     help="solver modes to time (a single-mode run is for profiling and prints no JSON line)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--no-graph", action="store_true",

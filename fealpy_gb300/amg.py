@@ -37,21 +37,23 @@ class _Level:
         self.n_coarse = 0
 
 
-def _level_sell(L: "_Level", with64: bool = False):
-    """SELL-32 copy of a level with FP32 values for its smoothing sweeps
-    (and FP64 values for PCG's operator when ``with64``): 15-bit column steps
-    where every row's columns ascend, else 4-byte columns; the solver's
+def _level_sell(L: "_Level", with32: bool = True, with64: bool = False):
+    """SELL-32 copy of a level with FP32 values for an FP32 V-cycle's sweeps
+    and FP64 values for an FP64 V-cycle or PCG's operator: 15-bit column
+    steps where every row's columns ascend, else 4-byte columns; the solver's
     autotuned launch shape."""
     from . import solver as _solver
     v64 = L.values if with64 else None
+    v32 = L.values32 if with32 else None
     try:
-        S = K.sell_build(L.indptr, L.indices, v64, L.values32, want64=with64, want32=True, d15=True)
+        S = K.sell_build(L.indptr, L.indices, v64, v32, want64=with64, want32=with32, d15=True)
     except _lib.FgbError:
-        S = K.sell_build(L.indptr, L.indices, v64, L.values32, want64=with64, want32=True, d16=False)
-    key = (S.n, S.padded_nnz, torch.float32, S.cols)
+        S = K.sell_build(L.indptr, L.indices, v64, v32, want64=with64, want32=with32, d16=False)
+    dt = torch.float32 if with32 else torch.float64
+    key = (S.n, S.padded_nnz, dt, S.cols)
     shape = _solver._LAUNCH_CACHE.get(key)
     if shape is None:
-        times = K.sell_autotune(S, torch.float32)
+        times = K.sell_autotune(S, dt)
         shape = min(times, key=times.get)
         _solver._LAUNCH_CACHE[key] = shape
     S.set_launch(*shape)
@@ -72,7 +74,7 @@ class GAMGSolver:
     V-cycle runs in FP32 on FP32 copies of the level matrices; the PCG
     operator and its vectors stay FP64), ``sell_min_rows`` (levels of at
     least this many rows smooth on a SELL-32 copy, 15-bit column steps where
-    the columns ascend, instead of the CSR arrays)."""
+    the columns ascend, instead of the CSR arrays; in either precision)."""
 
     def __init__(self, theta: float = 0.0, csize: int = 300, ctype: str = "A", itype: str = "T", ptype: str = "V",
                  sstep: int = 3, isolver: str = "CG", maxit: int = 200, csolver: str = "chebyshev",
@@ -146,9 +148,10 @@ class GAMGSolver:
         for k, L in enumerate(self.levels):
             L.values32 = L.values.to(torch.float32) if self.vcycle_f32 else None
             L.dinv32 = L.dinv.to(torch.float32) if self.vcycle_f32 else None
-            if self.vcycle_f32 and L.n >= self.sell_min_rows:
-                # the finest copy also carries the FP64 values: PCG's operator
-                L.sell = _level_sell(L, with64=(k == 0))
+            if L.n >= self.sell_min_rows:
+                # values of the V-cycle's type; the finest copy also carries
+                # the FP64 values for PCG's operator
+                L.sell = _level_sell(L, with32=self.vcycle_f32, with64=(k == 0 or not self.vcycle_f32))
         self._desc = (_lib.AmgLevel * len(self.levels))()
         for k, L in enumerate(self.levels):
             d = self._desc[k]

@@ -850,7 +850,24 @@ void with_lanes(int G, F&& f) {
 // partials on its FP64 values (sell.cu)
 int sell_smooth_f32(const fgb_sell* A, const float* dinv, const float* r, const float* x_in, float* x_out, float* d,
                     float c1, float c2, int mode, cudaStream_t st);
+int sell_smooth_f64(const fgb_sell* A, const double* dinv, const double* r, const double* x_in, double* x_out,
+                    double* d, double c1, double c2, int mode, cudaStream_t st);
 int sell_spmv_pap_f64(const fgb_sell* A, const double* p, double* Ap, double* bpart, int* n_part, cudaStream_t st);
+
+// the level's SELL sweep in the V-cycle's type (false: the level has no copy
+// with values of that type)
+inline bool sell_sweep(const fgb_amg_level& L, const float* dinv, const float* r, const float* x_in, float* x_out,
+                       float* d, double c1, double c2, int mode, cudaStream_t st) {
+  if (!L.sell || !L.sell->val32) return false;
+  sell_smooth_f32(L.sell, dinv, r, x_in, x_out, d, static_cast<float>(c1), static_cast<float>(c2), mode, st);
+  return true;
+}
+inline bool sell_sweep(const fgb_amg_level& L, const double* dinv, const double* r, const double* x_in,
+                       double* x_out, double* d, double c1, double c2, int mode, cudaStream_t st) {
+  if (!L.sell || !L.sell->val64) return false;
+  sell_smooth_f64(L.sell, dinv, r, x_in, x_out, d, c1, c2, mode, st);
+  return true;
+}
 
 // out[0] = sum of part[0..nb) in a fixed order (one block), out[1] = 0
 __global__ void amg_sum_partials(const double* __restrict__ part, int nb, double* __restrict__ out) {
@@ -909,12 +926,7 @@ const T* level_dinv(const fgb_amg_level& L) {
 template <typename T>
 void cheb_sweep(const fgb_amg_level& L, const T* r, const T* x_in, T* x_out, T* d, double c1, double c2,
                 cudaStream_t st) {
-  if constexpr (std::is_same<T, float>::value) {
-    if (L.sell) {
-      sell_smooth_f32(L.sell, L.dinv32, r, x_in, x_out, d, static_cast<float>(c1), static_cast<float>(c2), 0, st);
-      return;
-    }
-  }
+  if (sell_sweep(L, level_dinv<T>(L), r, x_in, x_out, d, c1, c2, 0, st)) return;
   const int64_t n = L.n;
   const T* vals = level_values<T>(L);
   const T* dinv = level_dinv<T>(L);
@@ -989,14 +1001,7 @@ int vcycle(const fgb_amg_level* levels, int nl, const double* r0, double* x_out,
     cheb<T>(L, rin, V[l].x, V[l].x2, V[l].d, deg, 0.1, true, &xo, st);
     xs[l] = xo;
     const T* vals = level_values<T>(L);
-    bool done = false;
-    if constexpr (std::is_same<T, float>::value) {
-      if (L.sell) {
-        sell_smooth_f32(L.sell, nullptr, rin, xo, V[l].res, nullptr, 0.0f, 0.0f, 1, st);
-        done = true;
-      }
-    }
-    if (!done)
+    if (!sell_sweep(L, static_cast<const T*>(nullptr), rin, xo, V[l].res, static_cast<T*>(nullptr), 0.0, 0.0, 1, st))
       with_lanes(amg_lanes(n, L.nnz), [&](auto g) {
         constexpr int GG = decltype(g)::value;
         amg_residual<GG, T, T><<<rows_grid(n, GG), kAmgThreads, 0, st>>>(n, L.indptr, L.indices, vals, rin, xo,
@@ -1042,7 +1047,7 @@ int levels_mode(const fgb_amg_level* levels, int nl) {
     if (L.n <= 0 || !L.indptr || !L.indices || !L.values || !L.dinv || !(L.lmax > 0.0)) return -1;
     if (l < nl - 1 && (!L.agg || !L.member_ptr || !L.members || L.n_coarse != levels[l + 1].n)) return -1;
     if ((L.values32 == nullptr) != (L.dinv32 == nullptr)) return -1;
-    if (L.sell && (!L.values32 || L.sell->n != L.n || !L.sell->val32)) return -1;
+    if (L.sell && L.sell->n != L.n) return -1;
     n32 += L.values32 ? 1 : 0;
   }
   if (n32 != 0 && n32 != nl) return -1;

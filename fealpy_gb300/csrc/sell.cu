@@ -191,26 +191,24 @@ __global__ void __launch_bounds__(1024, 1) sell_spmv_kernel(SellView A, const T*
 // Smoother sweep of an FP32 copy (a multigrid level matrix): mode 0, a
 // Chebyshev step d = c1 d + c2 dinv (r - A x_in), x_out = x_in + d (d is not
 // read when c1 = 0); mode 1, the residual x_out = r - A x_in.
-template <int FMT>
-__global__ void __launch_bounds__(1024, 1) sell_smooth_kernel(SellView A, const float* __restrict__ val,
-                                                               const float* __restrict__ dinv,
-                                                               const float* __restrict__ r,
-                                                               const float* __restrict__ x_in,
-                                                               float* __restrict__ x_out, float* __restrict__ d,
-                                                               float c1, float c2, int mode) {
+template <int FMT, typename T>
+__global__ void __launch_bounds__(1024, 1) sell_smooth_kernel(SellView A, const T* __restrict__ val,
+                                                               const T* __restrict__ dinv, const T* __restrict__ r,
+                                                               const T* __restrict__ x_in, T* __restrict__ x_out,
+                                                               T* __restrict__ d, T c1, T c2, int mode) {
   const int lane = threadIdx.x & 31;
   const int64_t warp = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
   const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
-  const GatherX<float> g{x_in};
+  const GatherX<T> g{x_in};
   for (int64_t s = warp; s < A.n_slices; s += nwarps) {
-    const float acc = slice_row<FMT, float, float>(A, val, s, lane, g);
+    const T acc = slice_row<FMT, T, T>(A, val, s, lane, g);
     const int32_t row = A.perm[s * kSellC + lane];
     if (row < 0) continue;
-    const float res = r[row] - acc;
+    const T res = r[row] - acc;
     if (mode) {
       x_out[row] = res;
     } else {
-      const float di = (c1 != 0.0f ? c1 * d[row] : 0.0f) + c2 * dinv[row] * res;
+      const T di = (c1 != T(0) ? c1 * d[row] : T(0)) + c2 * dinv[row] * res;
       d[row] = di;
       x_out[row] = x_in[row] + di;
     }
@@ -1327,15 +1325,26 @@ int finish(int done) {
 
 namespace fgb {
 
-// Smoother sweep on the FP32 values of a SELL copy (used by the multigrid
-// V-cycle for its large levels); the shape of the copy's launch.
+// Smoother sweep on the FP32 (FP64) values of a SELL copy (used by the
+// multigrid V-cycle for its large levels); the shape of the copy's launch.
 int sell_smooth_f32(const fgb_sell* A, const float* dinv, const float* r, const float* x_in, float* x_out, float* d,
                     float c1, float c2, int mode, cudaStream_t st) {
   if (!A || !A->val32 || !launch_ok(A) || !r || !x_in || !x_out || (mode == 0 && (!dinv || !d))) return FGB_ERR_ARG;
   const SellView V = view_of(A);
   with_cols(V, [&](auto f) {
     constexpr int FMT = decltype(f)::value;
-    sell_smooth_kernel<FMT><<<SLICE_LAUNCH(V, st)>>>(V, A->val32, dinv, r, x_in, x_out, d, c1, c2, mode);
+    sell_smooth_kernel<FMT, float><<<SLICE_LAUNCH(V, st)>>>(V, A->val32, dinv, r, x_in, x_out, d, c1, c2, mode);
+  });
+  return FGB_OK;
+}
+
+int sell_smooth_f64(const fgb_sell* A, const double* dinv, const double* r, const double* x_in, double* x_out,
+                    double* d, double c1, double c2, int mode, cudaStream_t st) {
+  if (!A || !A->val64 || !launch_ok(A) || !r || !x_in || !x_out || (mode == 0 && (!dinv || !d))) return FGB_ERR_ARG;
+  const SellView V = view_of(A);
+  with_cols(V, [&](auto f) {
+    constexpr int FMT = decltype(f)::value;
+    sell_smooth_kernel<FMT, double><<<SLICE_LAUNCH(V, st)>>>(V, A->val64, dinv, r, x_in, x_out, d, c1, c2, mode);
   });
   return FGB_OK;
 }

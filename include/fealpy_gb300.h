@@ -518,9 +518,11 @@ typedef struct fgb_amg_level {
   const float* values32;     /* optional FP32 copies of values and dinv, set  */
   const float* dinv32;       /* on every level or on none: with them the      */
                              /* V-cycle runs in FP32 (vectors and arithmetic) */
-  const struct fgb_sell* sell; /* optional SELL copy of the level with FP32    */
-                             /* values (FP32 V-cycle only): its smoothing and */
-                             /* residual sweeps run on the copy               */
+  const struct fgb_sell* sell; /* optional SELL copy of the level: its         */
+                             /* smoothing and residual sweeps run on the copy */
+                             /* when it holds values of the V-cycle's type;   */
+                             /* on level 0 PCG's operator product runs on its */
+                             /* FP64 values when present                      */
 } fgb_amg_level;
 
 /* Aggregates of a level: agg (n), their number, dinv (n) and lmax. */
