@@ -233,6 +233,27 @@ def amg_record(results, fp64, mixed, world, gdof):
     return out or None
 
 
+def assembly_roofline(rec, NN, NC, ldof, gdof, peak):
+    """HBM fractions of the numeric assembly (factor + values kernels) and of
+    the symbolic phase (adjacency + pattern) of a C2 record, from its stage
+    times (FP64 assembly: s = 8):
+    B_asm = NC ldof 4 (cell2dof) + NN 3 8 (vertex coordinates) + NC 8 (cell
+    coefficient) + nnz 8 (values); B_pattern = nnz 4 + (n + 1) 8."""
+    st = rec["stages_ms"]
+    nnz = rec["nnz"]
+    b_asm = NC * ldof * 4 + NN * 3 * 8 + NC * 8 + nnz * 8
+    b_pat = nnz * 4 + (gdof + 1) * 8
+    t_asm = st.get("assembly/factors", 0.0) + st.get("assembly/values", 0.0)
+    t_pat = st.get("assembly/adjacency", 0.0) + st.get("assembly/pattern", 0.0)
+    out = {}
+    for key, b, t, what in (("assembly", b_asm, t_asm, "cell_factors_kernel + assemble_scalar_kernel<double, 10>"),
+                            ("pattern", b_pat, t_pat, "adjacency build + pattern passes")):
+        ach = b / (t / 1e3) / 1e9 if t > 0 else 0.0
+        out[key] = {"kernels": what, "algorithmic_bytes": b, "ms": t, "achieved": ach, "unit": "GB/s",
+                    "frac": ach / peak if peak else None}
+    return out
+
+
 def spmv_roofline(mixed, gdof, n, peak, peak_kind):
     """`roofline` of the C2 record for the dominant kernel, the FP32 PCG SpMV
     (Ap = A p and p.Ap), from the profiling solve's mean launch time, plus the
@@ -431,6 +452,8 @@ def run_ours(args):
     fp64 = results["fp64"]
     value = replica_value(gdof, world, mixed["ms_per_step"])
     roofline = spmv_roofline(mixed, gdof, n, peak, peak_kind)
+    roofline.update(assembly_roofline(mixed, node_np.shape[0], cell_np.shape[0], space.number_of_local_dofs(),
+                                      gdof, peak))
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

@@ -120,7 +120,7 @@ __device__ bool assemble_scalar_row(int64_t i, const int64_t* __restrict__ adj_p
                                     const T* __restrict__ factors, const int64_t* __restrict__ indptr,
                                     const int32_t* __restrict__ indices, T* __restrict__ values,
                                     float* __restrict__ values32, int32_t* cols, T* acc, int cap, int ncopy,
-                                    int32_t* status) {
+                                    int accumulate, int32_t* status) {
   const int ldof = LDOF > 0 ? LDOF : ldof_rt;
   const int lane = threadIdx.x & 31;
   const int64_t base = indptr[i];
@@ -153,6 +153,7 @@ __device__ bool assemble_scalar_row(int64_t i, const int64_t* __restrict__ adj_p
   for (int t = lane; t < L; t += 32) {
     T v = acc[t];
     for (int gg = 1; gg < ncopy; ++gg) v += acc[gg * cap + t];
+    if (accumulate) v = values[base + t] + v;  // a later pass of split factor channels
     values[base + t] = v;
     if (values32) values32[base + t] = static_cast<float>(v);
   }
@@ -168,7 +169,8 @@ __global__ void assemble_scalar_kernel(int64_t n_rows, const int32_t* __restrict
                                        int nt, const T* __restrict__ tables, const T* __restrict__ factors,
                                        const int64_t* __restrict__ indptr, const int32_t* __restrict__ indices,
                                        T* __restrict__ values, float* __restrict__ values32, int cap, int ncopy,
-                                       int32_t* __restrict__ ovf, int32_t* __restrict__ ovf_len, int32_t* status) {
+                                       int accumulate, int32_t* __restrict__ ovf, int32_t* __restrict__ ovf_len,
+                                       int32_t* status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* tab = reinterpret_cast<T*>(smem_raw);
   const int ntab = nt * ldof * ldof;
@@ -185,7 +187,7 @@ __global__ void assemble_scalar_kernel(int64_t n_rows, const int32_t* __restrict
   for (int64_t r = warp; r < n; r += nwarps) {
     const int64_t i = row_list ? row_list[r] : r;
     bool done = assemble_scalar_row<T, LDOF>(i, adj_ptr, adj, c2d, ldof, nt, tab, factors, indptr, indices, values,
-                                             values32, cols, acc, cap, ncopy, status);
+                                             values32, cols, acc, cap, ncopy, accumulate, status);
     if (!done && lane == 0) {
       if (ovf) { int slot = atomicAdd(ovf_len, 1); ovf[slot] = static_cast<int32_t>(i); }
       else set_status(status, FGB_ERR_CAPACITY);
@@ -329,7 +331,8 @@ constexpr size_t kMaxDynSmem = 200 * 1024;
 template <typename T>
 int launch_scalar(int64_t n_dof, const int64_t* adj_ptr, const int32_t* adj, const int32_t* c2d, int ldof, int nt,
                   const T* tables, const T* factors, const int64_t* indptr, const int32_t* indices, T* values,
-                  float* values32, int32_t* status, int32_t* ovf, int32_t* ovf_len, cudaStream_t st) {
+                  float* values32, int accumulate, int32_t* status, int32_t* ovf, int32_t* ovf_len,
+                  cudaStream_t st) {
   const size_t tab_bytes = align_up(static_cast<size_t>(nt) * ldof * ldof * sizeof(T), 16);
   const int ncopy = 32 / ldof;
   const size_t per_warp1 = align_up(static_cast<size_t>(ncopy) * kAsmCap * sizeof(T) + kAsmCap * 4, 16);
@@ -349,9 +352,10 @@ int launch_scalar(int64_t n_dof, const int64_t* adj_ptr, const int32_t* adj, con
   cudaMemsetAsync(ovf_len, 0, sizeof(int32_t), st);
   const int grid1 = grid_for(n_dof, kAsmWarps, kNumSMs * 16);
   kern<<<grid1, kAsmWarps * 32, smem1, st>>>(n_dof, nullptr, nullptr, adj_ptr, adj, c2d, ldof, nt, tables, factors,
-                                             indptr, indices, values, values32, kAsmCap, ncopy, ovf, ovf_len, status);
+                                             indptr, indices, values, values32, kAsmCap, ncopy, accumulate, ovf,
+                                             ovf_len, status);
   kern<<<kNumSMs, 32, smem2, st>>>(n_dof, ovf, ovf_len, adj_ptr, adj, c2d, ldof, nt, tables, factors, indptr, indices,
-                                   values, values32, kAsmBigCap, 1, nullptr, nullptr, status);
+                                   values, values32, kAsmBigCap, 1, accumulate, nullptr, nullptr, status);
   return launch_status();
 }
 
@@ -449,6 +453,15 @@ int32_t fgb_assemble_scalar(int32_t dtype, int64_t n_dof, const int64_t* adj_ptr
                             const void* factors, const int64_t* indptr, const int32_t* indices, void* values,
                             float* values_f32, int32_t* status, void* workspace, size_t workspace_bytes,
                             void* stream) {
+  return fgb_assemble_scalar_acc(dtype, n_dof, adj_ptr, adj, cell2dof, ldof, n_table, tables, factors, indptr, indices,
+                                 values, values_f32, 0, status, workspace, workspace_bytes, stream);
+}
+
+int32_t fgb_assemble_scalar_acc(int32_t dtype, int64_t n_dof, const int64_t* adj_ptr, const int32_t* adj,
+                                const int32_t* cell2dof, int32_t ldof, int32_t n_table, const void* tables,
+                                const void* factors, const int64_t* indptr, const int32_t* indices, void* values,
+                                float* values_f32, int32_t accumulate, int32_t* status, void* workspace,
+                                size_t workspace_bytes, void* stream) {
   if (n_dof <= 0 || ldof <= 0 || ldof > 32 || n_table <= 0 || !adj_ptr || !adj || !cell2dof || !tables ||
       !factors || !indptr || !indices || !values)
     return FGB_ERR_ARG;
@@ -460,11 +473,11 @@ int32_t fgb_assemble_scalar(int32_t dtype, int64_t n_dof, const int64_t* adj_ptr
   if (dtype == FGB_F64)
     return launch_scalar<double>(n_dof, adj_ptr, adj, cell2dof, ldof, n_table, static_cast<const double*>(tables),
                                  static_cast<const double*>(factors), indptr, indices, static_cast<double*>(values),
-                                 values_f32, status, ovf, ovf_len, st);
+                                 values_f32, accumulate ? 1 : 0, status, ovf, ovf_len, st);
   if (dtype == FGB_F32)
     return launch_scalar<float>(n_dof, adj_ptr, adj, cell2dof, ldof, n_table, static_cast<const float*>(tables),
                                 static_cast<const float*>(factors), indptr, indices, static_cast<float*>(values),
-                                values_f32, status, ovf, ovf_len, st);
+                                values_f32, accumulate ? 1 : 0, status, ovf, ovf_len, st);
   return FGB_ERR_ARG;
 }
 

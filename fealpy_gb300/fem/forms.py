@@ -142,11 +142,20 @@ class BilinearForm(_Form):
             n = space.number_of_global_dofs()
             adj_ptr, adj, indptr, indices = self._symbolic(space, c2d, n, marks)
             mesh = space.mesh
-            fac = K.cell_factors(mesh, plan.channels, plan.coef_matrix(), dtype, status)
-            _mark(marks, "factors")
-            tab = torch.as_tensor(plan.tables, dtype=dtype, device=space.device)
-            values, v32 = K.assemble_scalar(adj_ptr, adj, c2d, tab, fac, indptr, indices,
-                                            values_f32=emit_f32 and dtype == torch.float64, status=status)
+            coef = plan.coef_matrix()
+            passes = plan.passes()
+            values = v32 = None
+            for k, (chans, tabs) in enumerate(passes):
+                # more channels than one factor launch holds (coefficients per
+                # quadrature point): passes that add into the values
+                fac = K.cell_factors(mesh, chans, coef, dtype, status)
+                if k == 0:
+                    _mark(marks, "factors")
+                tab = torch.as_tensor(tabs, dtype=dtype, device=space.device)
+                last = k == len(passes) - 1
+                values, v32 = K.assemble_scalar(adj_ptr, adj, c2d, tab, fac, indptr, indices,
+                                                values_f32=emit_f32 and dtype == torch.float64 and last,
+                                                status=status, accumulate_into=values)
             _mark(marks, "values")
         elif isinstance(plan, ElasticityPlan):
             ss = space.scalar_space
@@ -202,7 +211,8 @@ class BilinearForm(_Form):
         cache = getattr(self, "_mf_cache", None)
         if cache is None or cache[0] != key:
             status = _lib.status_word(space.device)
-            fac = K.cell_factors(space.mesh, plan.channels, plan.coef_matrix(), dtype, status)
+            coef = plan.coef_matrix()
+            fac = [(K.cell_factors(space.mesh, chans, coef, dtype, status), tabs) for chans, tabs in plan.passes()]
             _lib.check_status_word("matrix-free factors", status)
             n = space.number_of_global_dofs()
             akey = ("adjacency", n)
@@ -211,10 +221,14 @@ class BilinearForm(_Form):
                 adj_ptr, adj, _ = K.build_adjacency(space.cell_to_dof(), n, st)
                 _lib.check_status_word("adjacency", st)
                 space._cache[akey] = (adj_ptr, adj)
-            cache = (key, fac, plan.tables, space._cache[akey])
+            cache = (key, fac, space._cache[akey])
             self._mf_cache = cache
-        _, fac, tables, (adj_ptr, adj) = cache
-        yc = K.cell_apply(space.cell_to_dof(), tables, fac, u.to(device=space.device, dtype=dtype))
+        _, fac, (adj_ptr, adj) = cache
+        ud = u.to(device=space.device, dtype=dtype)
+        yc = None
+        for f, tables in fac:
+            y = K.cell_apply(space.cell_to_dof(), tables, f, ud)
+            yc = y if yc is None else yc + y
         return K.gather_sum(adj_ptr, adj, yc)
 
     def mult(self, x, out=None):

@@ -49,6 +49,13 @@ class ScalarPlan:
     def coef_matrix(self):
         return torch.stack(self.coefs, 0) if self.coefs else None
 
+    def passes(self, limit: int = _lib.FGB_MAX_CHANNELS):
+        """The channels in passes of at most ``limit`` (the factor kernel's
+        capacity): [(channels, tables)]; coefficient rows keep indexing
+        :meth:`coef_matrix`."""
+        n = len(self.channels)
+        return [(self.channels[a:a + limit], self.tables[a:a + limit]) for a in range(0, n, limit)]
+
 
 class ElasticityPlan:
     """P1 elasticity: factor channels = grad(lambda_{1..GD}) then |T| D00, |T| D_lambda, |T| D_mu."""
@@ -62,27 +69,32 @@ class ElasticityPlan:
         return torch.stack(self.coefs, 0) if self.coefs else None
 
 
-def _cell_coefficient(coef, space, q: int) -> Tuple[float, Optional[torch.Tensor]]:
-    """(scale, per-cell array or None) from a FEALPy CoefLike.  Coefficients must
-    be constant on each cell; a callable is evaluated at the quadrature points
-    and accepted when its values agree across each cell's points."""
+def _cell_coefficient(coef, space, q: int) -> Tuple[float, Optional[torch.Tensor], Optional[torch.Tensor]]:
+    """(scale, per-cell array or None, per-point array or None) from a FEALPy
+    CoefLike (``fealpy/utils/utils.py:21-53``): a number, an (NC,) array, an
+    (NC, NQ) array of values at the quadrature points of rule ``q``, or a
+    callable evaluated there.  Values that agree across each cell's points
+    become a per-cell array; otherwise the (NC, NQ) array is returned."""
     mesh = space.mesh
     NC = mesh.number_of_cells()
     if coef is None:
-        return 1.0, None
+        return 1.0, None, None
     if isinstance(coef, (int, float)):
-        return float(coef), None
+        return float(coef), None, None
     if isinstance(coef, torch.Tensor):
         if coef.numel() == 1:
-            return float(coef.reshape(-1)[0].item()), None
+            return float(coef.reshape(-1)[0].item()), None, None
         if coef.ndim == 1 and coef.shape[0] == NC:
-            return 1.0, coef.to(device=mesh.device, dtype=torch.float64)
+            return 1.0, coef.to(device=mesh.device, dtype=torch.float64), None
         if coef.ndim == 2 and coef.shape[0] == NC:
             val = coef.to(device=mesh.device, dtype=torch.float64)
+            NQ = mesh.quadrature_formula(q).number_of_quadrature_points()
+            if val.shape[1] == NQ and not bool(torch.all(val == val[:, :1])):
+                return 1.0, None, val.contiguous()
             if bool(torch.all(val == val[:, :1])):
-                return 1.0, val[:, 0].contiguous()
-        raise NotImplementedError("coefficients must be constant per cell: scalar, (NC,) or (NC, NQ) with equal "
-                                  "values along the quadrature axis")
+                return 1.0, val[:, 0].contiguous(), None
+            raise ValueError(f"an (NC, NQ) coefficient needs NQ = {NQ} values per cell for quadrature order {q}")
+        raise ValueError("coefficients are a number, (NC,) or (NC, NQ)")
     if isinstance(coef, np.ndarray):
         return _cell_coefficient(torch.as_tensor(coef, device=mesh.device), space, q)
     if callable(coef):
@@ -151,12 +163,12 @@ class _OperatorIntegrator(Integrator):
         """Local matrices (NC, ldof, ldof), FP64 (a convenience; the CSR path
         never materialises them)."""
         plan = self.plan(space)
-        if isinstance(plan, ElasticityPlan):
-            raise NotImplementedError("local elasticity matrices are only formed inside the CSR kernel")
         mesh = space.mesh
-        f = K.cell_factors(mesh, plan.channels, plan.coef_matrix(), torch.float64)
-        tab = torch.as_tensor(plan.tables, dtype=torch.float64, device=mesh.device)
-        out = torch.einsum("ct,tij->cij", f, tab)
+        coef = plan.coef_matrix()
+        out = None
+        for chans, tabs in plan.passes():
+            f = K.cell_factors(mesh, chans, coef, torch.float64)
+            out = K.local_matrices(f, torch.as_tensor(tabs, dtype=torch.float64, device=mesh.device), out)
         return out if indices is None else out[indices]
 
 
@@ -179,10 +191,17 @@ class ScalarDiffusionIntegrator(_OperatorIntegrator):
         mesh = space.mesh
         TD = mesh.TD
         q = space.p + 3 if self.q is None else self.q
-        scale, arr = _cell_coefficient(self.coef, space, q)
+        scale, arr, arrq = _cell_coefficient(self.coef, space, q)
+        pairs = sx.metric_pairs(TD)
+        if arrq is not None:
+            # a coefficient per quadrature point: one channel per (point,
+            # metric entry) with that point's table
+            coefs = [arrq[:, iq].contiguous() for iq in range(arrq.shape[1])]
+            ch = [(_lib.FGB_CH_METRIC + k * 3 + l, iq, 1.0) for iq in range(arrq.shape[1]) for k, l in pairs]
+            return ScalarPlan(ch, coefs, sx.diffusion_tables_q(TD, space.p, q))
         coefs = [arr] if arr is not None else []
         ci = 0 if arr is not None else -1
-        ch = [(_lib.FGB_CH_METRIC + k * 3 + l, ci, scale) for k, l in sx.metric_pairs(TD)]
+        ch = [(_lib.FGB_CH_METRIC + k * 3 + l, ci, scale) for k, l in pairs]
         return ScalarPlan(ch, coefs, sx.diffusion_tables(TD, space.p, q))
 
 
@@ -203,7 +222,11 @@ class ScalarMassIntegrator(_OperatorIntegrator):
         self._check_region()
         mesh = space.mesh
         q = space.p + 3 if self.q is None else self.q
-        scale, arr = _cell_coefficient(self.coef, space, q)
+        scale, arr, arrq = _cell_coefficient(self.coef, space, q)
+        if arrq is not None:
+            coefs = [arrq[:, iq].contiguous() for iq in range(arrq.shape[1])]
+            ch = [(_lib.FGB_CH_MEASURE, iq, 1.0) for iq in range(arrq.shape[1])]
+            return ScalarPlan(ch, coefs, sx.mass_tables_q(mesh.TD, space.p, q))
         coefs = [arr] if arr is not None else []
         ch = [(_lib.FGB_CH_MEASURE, 0 if arr is not None else -1, scale)]
         return ScalarPlan(ch, coefs, sx.mass_table(mesh.TD, space.p, q))
@@ -221,7 +244,14 @@ class LinearElasticityIntegrator(_OperatorIntegrator):
         self.q = q
         self.index = index
 
-    def plan(self, space) -> ElasticityPlan:
+    def assembly(self, space, /, indices=None):
+        """Local matrices ((NC, (GD+1) GD, (GD+1) GD), FP64) in the space's
+        local dof order (interleaved or component-major)."""
+        out = K.local_elasticity_p1(space.scalar_space.mesh, self.plan(space, local=True),
+                                    priority=bool(space.dof_priority))
+        return out if indices is None else out[indices]
+
+    def plan(self, space, local: bool = False) -> ElasticityPlan:
         self._check_region()
         if not isinstance(space, TensorFunctionSpace):
             raise TypeError("LinearElasticityIntegrator needs a TensorFunctionSpace")
@@ -230,7 +260,7 @@ class LinearElasticityIntegrator(_OperatorIntegrator):
         gd = mesh.GD
         if ss.p != 1:
             raise NotImplementedError("the GB300 elasticity kernel covers P1 spaces")
-        if space.dof_priority:
+        if space.dof_priority and not local:
             raise NotImplementedError("the GB300 elasticity kernel covers the interleaved layout (shape=(-1, GD))")
         q = ss.p + 3 if self.q is None else self.q
         _, ws = mesh.quadrature_formula(q).get_quadrature_points_and_weights()

@@ -96,7 +96,10 @@ def expand_blocks(n_node: int, bs: int, dof_priority: bool, indptr, indices):
 
 
 def assemble_scalar(adj_ptr, adj, c2d, tables: torch.Tensor, factors: torch.Tensor, indptr, indices,
-                    values_f32: bool = False, status: Optional[torch.Tensor] = None):
+                    values_f32: bool = False, status: Optional[torch.Tensor] = None,
+                    accumulate_into: Optional[torch.Tensor] = None):
+    """CSR values of sum_t factors[:, t] * tables[t] over the pattern; with
+    ``accumulate_into`` (values of an earlier pass) this pass is added to them."""
     dev = _dev(c2d)
     n_dof = adj_ptr.numel() - 1
     ldof = c2d.shape[1]
@@ -104,7 +107,12 @@ def assemble_scalar(adj_ptr, adj, c2d, tables: torch.Tensor, factors: torch.Tens
     nt = tables.shape[0]
     if tables.shape[1:] != (ldof, ldof) or factors.shape[1] != nt:
         raise ValueError("table/factor shapes do not match")
-    values = torch.empty(indices.numel(), dtype=dtype, device=dev)
+    if accumulate_into is not None:
+        if accumulate_into.dtype != dtype or accumulate_into.numel() != indices.numel():
+            raise ValueError("accumulate_into must hold the pattern's values in the factor dtype")
+        values = accumulate_into
+    else:
+        values = torch.empty(indices.numel(), dtype=dtype, device=dev)
     v32 = torch.empty(indices.numel(), dtype=torch.float32, device=dev) if values_f32 else None
     lib = _lib.lib()
     ws = workspace(lib.fgb_assemble_workspace_bytes(n_dof), dev)
@@ -114,12 +122,43 @@ def assemble_scalar(adj_ptr, adj, c2d, tables: torch.Tensor, factors: torch.Tens
     # could share a freed block before the launch
     tab_d = tables.to(dev, dtype).contiguous()
     fac_d = factors.contiguous()
-    call("fgb_assemble_scalar", dtype_code(dtype), n_dof, ptr(adj_ptr), ptr(adj), ptr(c2d), ldof, nt,
+    call("fgb_assemble_scalar_acc", dtype_code(dtype), n_dof, ptr(adj_ptr), ptr(adj), ptr(c2d), ldof, nt,
          ptr(tab_d), ptr(fac_d), ptr(indptr), ptr(indices), ptr(values),
-         ptr(v32), ptr(st), ptr(ws), ws.numel(), stream_ptr(dev))
+         ptr(v32), 1 if accumulate_into is not None else 0, ptr(st), ptr(ws), ws.numel(), stream_ptr(dev))
     if own:
         check_status_word("fgb_assemble_scalar", st)
     return values, v32
+
+
+def local_matrices(factors: torch.Tensor, tables: torch.Tensor, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+    """(NC, ldof, ldof) local matrices sum_t factors[:, t] * tables[t]; with
+    ``out`` (an earlier pass) this pass is added to it."""
+    dev = factors.device
+    NC, nt = factors.shape
+    ldof = tables.shape[1]
+    if tables.shape != (nt, ldof, ldof):
+        raise ValueError("table/factor shapes do not match")
+    acc = out is not None
+    if out is None:
+        out = torch.empty((NC, ldof, ldof), dtype=factors.dtype, device=dev)
+    tab_d = tables.to(dev, factors.dtype).contiguous()
+    fac_d = factors.contiguous()
+    call("fgb_local_matrices", dtype_code(factors.dtype), NC, ldof, nt, ptr(tab_d), ptr(fac_d), ptr(out),
+         1 if acc else 0, stream_ptr(dev))
+    return out
+
+
+def local_elasticity_p1(mesh, plan, priority: bool = False) -> torch.Tensor:
+    """(NC, (GD+1) GD, (GD+1) GD) P1 elasticity local matrices from the
+    plan's factor channels; ``priority``: component-major local order."""
+    dev = _dev(mesh.node)
+    gd = plan.gd
+    f = cell_factors(mesh, plan.channels, plan.coef_matrix(), torch.float64)
+    ld = (gd + 1) * gd
+    out = torch.empty((f.shape[0], ld, ld), dtype=torch.float64, device=dev)
+    call("fgb_local_elasticity_p1", dtype_code(torch.float64), gd, f.shape[0], ptr(f), 1 if priority else 0,
+         ptr(out), stream_ptr(dev))
+    return out
 
 
 def assemble_elasticity_p1(gd, adj_ptr, adj, cell, factors, node_indptr, node_indices, indptr, nnz,

@@ -101,6 +101,39 @@ def _diffusion_tables(TD: int, p: int, q: int):
     return 0.5 * (T + T.transpose(0, 2, 1))   # exactly symmetric tables -> symmetric local matrices
 
 
+@lru_cache(maxsize=None)
+def _diffusion_tables_q(TD: int, p: int, q: int):
+    bcs, ws = simplex_quadrature(TD, q)
+    R = grad_shape_function(bcs, p)
+    Rr = R[:, :, 1:] - R[:, :, :1]
+    S = np.einsum("q,qik,qjl->qklij", ws, Rr, Rr)    # (NQ, TD, TD, ldof, ldof)
+    tabs = []
+    for iq in range(S.shape[0]):
+        for k, l in metric_pairs(TD):
+            tabs.append(S[iq, k, k] if k == l else S[iq, k, l] + S[iq, l, k])
+    T = np.stack(tabs, axis=0)
+    return 0.5 * (T + T.transpose(0, 2, 1))
+
+
+def diffusion_tables_q(TD: int, p: int, q: int) -> np.ndarray:
+    """Per-quadrature-point tables (NQ * n_metric, ldof, ldof), point-major:
+    with a coefficient c_q given per point the diffusion local matrix is
+    ``sum_q sum_t c_q G_t * T_{q,t}`` (``G_t`` as in :func:`diffusion_tables`)."""
+    return _diffusion_tables_q(TD, p, q).copy()
+
+
+@lru_cache(maxsize=None)
+def _mass_tables_q(TD: int, p: int, q: int):
+    bcs, ws = simplex_quadrature(TD, q)
+    phi = shape_function(bcs, p)
+    return np.einsum("q,qi,qj->qij", ws, phi, phi)
+
+
+def mass_tables_q(TD: int, p: int, q: int) -> np.ndarray:
+    """Per-quadrature-point mass tables (NQ, ldof, ldof): ``w_q phi_i phi_j``."""
+    return _mass_tables_q(TD, p, q).copy()
+
+
 def diffusion_tables(TD: int, p: int, q: int) -> np.ndarray:
     """Tables (n_metric, ldof, ldof) such that the diffusion local matrix is
     ``sum_t G_t * T_t`` with ``G_t = |T| kappa grad(l_{k+1}).grad(l_{l+1})``

@@ -215,6 +215,16 @@ int32_t fgb_assemble_scalar(int32_t dtype, int64_t n_dof, const int64_t* adj_ptr
                             const int64_t* indptr, const int32_t* indices, void* values,
                             float* values_f32, int32_t* status, void* workspace,
                             size_t workspace_bytes, void* stream);
+/* The same with accumulate != 0: values += this pass (values_f32, when given,
+ * receives the FP32 rounding of the sum).  For local matrices with more than
+ * FGB_MAX_CHANNELS factor channels (coefficients given per quadrature point,
+ * fealpy/utils/utils.py:21-53): the channels are split into passes. */
+int32_t fgb_assemble_scalar_acc(int32_t dtype, int64_t n_dof, const int64_t* adj_ptr,
+                                const int32_t* adj, const int32_t* cell2dof, int32_t ldof,
+                                int32_t n_table, const void* tables, const void* factors,
+                                const int64_t* indptr, const int32_t* indices, void* values,
+                                float* values_f32, int32_t accumulate, int32_t* status,
+                                void* workspace, size_t workspace_bytes, void* stream);
 
 /* P1 linear elasticity, interleaved vector dofs (LinearElasticityIntegrator
  * default variant, fealpy/fem/linear_elasticity_integrator.py:60-181, the
@@ -237,6 +247,20 @@ int32_t fgb_assemble_elasticity_p1(int32_t dtype, int32_t gd, int64_t n_node,
  * LinearForm._scalar_assembly (fealpy/fem/linear_form.py:36-86). */
 int32_t fgb_gather_sum(int32_t dtype, int64_t n, const int64_t* adj_ptr, const int32_t* adj,
                        const void* local, void* out, void* stream);
+
+/* Cell-local matrices for callers that want them (Integrator.assembly(space),
+ * fealpy/fem/scalar_diffusion_integrator.py, scalar_mass_integrator.py):
+ * out (n_cell, ldof, ldof) = sum_t factors[c][t] * tables[t] (device tables,
+ * the factor dtype); accumulate != 0 adds to out (passes of split channels).
+ * P1 elasticity (fealpy/fem/linear_elasticity_integrator.py:61-181): out
+ * (n_cell, (gd+1) gd, (gd+1) gd) from the factor channels of
+ * fgb_assemble_elasticity_p1; priority 0: local index vertex * gd + component
+ * (interleaved), 1: component * (gd + 1) + vertex. */
+int32_t fgb_local_matrices(int32_t dtype, int64_t n_cell, int32_t ldof, int32_t n_table,
+                           const void* tables, const void* factors, void* out, int32_t accumulate,
+                           void* stream);
+int32_t fgb_local_elasticity_p1(int32_t dtype, int32_t gd, int64_t n_cell, const void* factors,
+                                int32_t priority, void* out, void* stream);
 
 /* Matrix-free y_cell = K_c x_c for every cell, K_c = sum_t factors[c][t] *
  * tables[t] (the factorisation of fgb_assemble_scalar), the cell-local half

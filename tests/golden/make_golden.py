@@ -5,6 +5,7 @@ Run in an environment where the reference checkout is importable:
 
     python tests/golden/make_golden.py /path/to/fealpy-checkout            # small cases, C1
     python tests/golden/make_golden.py --configs /path/to/fealpy-checkout  # mid-size config laws
+    python tests/golden/make_golden.py --coef /path/to/fealpy-checkout     # (NC, NQ) coefficients
 
 The fixtures hold only inputs and outputs of the reference (meshes, dof maps,
 local matrices, CSR matrices, vectors, iteration counts, quadrature tables and
@@ -329,6 +330,58 @@ def config_cases(ref_root):
     print("cfg_c5_elasticity_8", ts.number_of_global_dofs(), A.nnz, A2.nnz, info["niter"])
 
 
+def coef_cases(ref_root):
+    """Coefficients that vary inside a cell (``fealpy/utils/utils.py:21-53``
+    hands (NC, NQ) values to ``bilinear_integral``): per seeded jittered mesh,
+    a diffusion coefficient given as a cartesian function (1 + x^2 + y z or
+    1 + x^2 + y in 2-D) and a mass coefficient given as an (NC, NQ) array
+    (uniform in [0.5, 2]), on P2 triangles (4x3 box) and P2 tetrahedra (2^3
+    box), q = 4.  Each fixture ``coefq_<tag>`` holds the inputs, the
+    reference's local matrices of both integrators and its CSR of their sum
+    (canonical order)."""
+    sys.path.insert(0, HERE)
+    import refshim
+    refshim.install(ref_root)
+    from fealpy.backend import backend_manager as bm
+    bm.set_backend("numpy")
+    from fealpy.mesh import TriangleMesh, TetrahedronMesh
+    from fealpy.functionspace import LagrangeFESpace
+    from fealpy.fem import BilinearForm, ScalarDiffusionIntegrator, ScalarMassIntegrator
+    from fealpy.decorator import cartesian
+
+    @cartesian
+    def kappa2(p):
+        return 1.0 + p[..., 0] ** 2 + p[..., 1]
+
+    @cartesian
+    def kappa3(p):
+        return 1.0 + p[..., 0] ** 2 + p[..., 1] * p[..., 2]
+
+    rng = np.random.default_rng(20261204)
+    for tag, kind, dims, p, q in (("tri_p2", "tri", (4, 3), 2, 4), ("tet_p2", "tet", (2, 2, 2), 2, 4)):
+        if kind == "tri":
+            m0 = TriangleMesh.from_box([0, 1, 0, 1], *dims)
+            node = jitter(m0.node, m0.boundary_node_flag(), 1.0 / max(dims), 0.15, rng)
+            mesh, kappa = TriangleMesh(node, m0.cell), kappa2
+        else:
+            m0 = TetrahedronMesh.from_box([0, 1, 0, 1, 0, 1], *dims)
+            node = jitter(m0.node, m0.boundary_node_flag(), 1.0 / max(dims), 0.2, rng)
+            mesh, kappa = TetrahedronMesh(node, m0.cell), kappa3
+        space = LagrangeFESpace(mesh, p=p)
+        NC = mesh.number_of_cells()
+        NQ = mesh.quadrature_formula(q).number_of_quadrature_points()
+        rho = rng.uniform(0.5, 2.0, size=(NC, NQ))
+        Kd = ScalarDiffusionIntegrator(coef=kappa, q=q).assembly(space)
+        Km = ScalarMassIntegrator(coef=rho, q=q).assembly(space)
+        bf = BilinearForm(space)
+        bf.add_integrator(ScalarDiffusionIntegrator(coef=kappa, q=q), ScalarMassIntegrator(coef=rho, q=q))
+        A = bf.assembly()
+        c0, c1, c2 = canonical(A.crow, A.col, A.values)
+        np.savez_compressed(os.path.join(HERE, f"coefq_{tag}.npz"), node=mesh.node, cell=mesh.cell, p=np.int64(p),
+                            q=np.int64(q), rho=rho, K_diff=Kd, K_mass=Km, crow=c0, col=c1, val=c2)
+        print("coefq", tag, NC, NQ, A.nnz)
+
+
 def _reference_root(argv):
     root = argv[0] if argv else os.environ.get("FEALPY_REFERENCE")
     if not root:
@@ -341,5 +394,7 @@ if __name__ == "__main__":
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
     if "--configs" in sys.argv[1:]:
         config_cases(_reference_root(args))
+    elif "--coef" in sys.argv[1:]:
+        coef_cases(_reference_root(args))
     else:
         main(_reference_root(args))
