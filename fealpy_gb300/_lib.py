@@ -77,6 +77,9 @@ _SIGNATURES = {
     "fgb_assemble_workspace_bytes": (c_sz, [c_i64]),
     "fgb_assemble_scalar": (c_i32, [c_i32, c_i64, c_vp, c_vp, c_vp, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp,
                                     c_vp, c_vp, c_vp, c_sz, c_vp]),
+    "fgb_pcg_multi_workspace_bytes": (c_sz, [c_i64, c_i32]),
+    "fgb_pcg_multi_f64": (c_i32, [c_i64, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_dbl, c_dbl, c_i64, c_vp, c_vp,
+                                  c_sz, c_vp]),
     "fgb_local_matrices": (c_i32, [c_i32, c_i64, c_i32, c_i32, c_vp, c_vp, c_vp, c_i32, c_vp]),
     "fgb_local_elasticity_p1": (c_i32, [c_i32, c_i32, c_i64, c_vp, c_i32, c_vp, c_vp]),
     "fgb_assemble_scalar_acc": (c_i32, [c_i32, c_i64, c_vp, c_vp, c_vp, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp,

@@ -130,6 +130,26 @@ def assemble_scalar(adj_ptr, adj, c2d, tables: torch.Tensor, factors: torch.Tens
     return values, v32
 
 
+def pcg_multi(indptr, indices, values, dinv, B: torch.Tensor, X: torch.Tensor, atol: float, rtol: float,
+              maxit: int):
+    """Jacobi-PCG (``dinv`` None: plain CG) on every column of B (n, k),
+    FEALPy's multi-right-hand-side recurrence; X (n, k) in/out."""
+    dev = B.device
+    n, k = B.shape
+    lib = _lib.lib()
+    nb = lib.fgb_pcg_multi_workspace_bytes(n, k)
+    if nb == 0:
+        raise ValueError(f"between 1 and 64 right-hand sides are supported, got {k}")
+    ws = workspace(nb, dev)
+    info = _lib.PcgInfo()
+    vals = values.to(torch.float64).contiguous()
+    b_d = B.to(torch.float64).contiguous()
+    call("fgb_pcg_multi_f64", n, k, ptr(indptr), ptr(indices), ptr(vals), ptr(dinv), ptr(b_d), ptr(X), float(atol),
+         float(rtol), int(maxit), ctypes.byref(info), ptr(ws), ws.numel(), stream_ptr(dev))
+    _lib.add_launches(info.launches)
+    return info
+
+
 def local_matrices(factors: torch.Tensor, tables: torch.Tensor, out: Optional[torch.Tensor] = None) -> torch.Tensor:
     """(NC, ldof, ldof) local matrices sum_t factors[:, t] * tables[t]; with
     ``out`` (an earlier pass) this pass is added to it."""

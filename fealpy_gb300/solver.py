@@ -131,11 +131,25 @@ def cg(A, b: torch.Tensor, x0: Optional[torch.Tensor] = None, M=None, *, batch_f
         raise ValueError("x0 and b must have the same shape")
     if not isinstance(A, CSRTensor):
         raise NotImplementedError("cg on the GB300 path takes a CSRTensor matrix")
-    if b.ndim == 2:
-        raise NotImplementedError("multi-right-hand-side cg is not provided on the GB300 path")
     if stop not in ("preconditioned", "residual"):
         raise ValueError("stop must be 'preconditioned' or 'residual'")
     from .amg import GAMGSolver
+    if b.ndim == 2:
+        # (n, batch) right-hand sides (or (batch, n) with batch_first):
+        # FEALPy's joint recurrence, fealpy/solver/cg.py:60-123
+        if isinstance(M, GAMGSolver):
+            raise NotImplementedError("several right-hand sides take M=None or a Jacobi preconditioner")
+        if stop != "preconditioned":
+            raise ValueError("several right-hand sides stop on sqrt(sum r.z) as FEALPy does")
+        dinv = _diag_inv_of(M)
+        B = (b.transpose(0, 1) if batch_first else b).to(torch.float64).contiguous()
+        X = torch.zeros_like(B) if x0 is None else (x0.transpose(0, 1) if batch_first else x0).to(
+            torch.float64).contiguous().clone()
+        info = K.pcg_multi(A.crow, A.col, A.values, dinv, B, X, atol, rtol,
+                           maxit if maxit is not None else 2 ** 62)
+        x = X.transpose(0, 1) if batch_first else X
+        out = _info_dict(info)
+        return (x, out) if returninfo else x
     if isinstance(M, GAMGSolver):
         # multigrid preconditioner: the whole PCG loop in the library
         x, info = M.pcg(b, x0=x0, atol=atol, rtol=rtol, maxit=maxit if maxit is not None else 2 ** 62,

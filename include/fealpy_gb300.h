@@ -348,6 +348,18 @@ int32_t fgb_pcg_f64_noalloc(int64_t n, const int64_t* indptr, const int32_t* ind
                             int32_t check_every, int32_t lanes_per_row, int32_t norm,
                             fgb_pcg_info* info_host, void* stream);
 
+/* Several right-hand sides of one matrix, the (n, batch) path of
+ * fealpy/solver/cg.py:60-123: B and X row-major (n, k), 1 <= k <= 64; every
+ * column runs its own recurrence (alpha, beta per column), all take the same
+ * iterations, and the solve stops when sqrt(sum_c r_c . z_c) < atol or
+ * < rtol * ||B||_F (diag_inv NULL: no preconditioner).  A zero B gives
+ * X = 0.  The iterations run as one CUDA-graph launch. */
+size_t fgb_pcg_multi_workspace_bytes(int64_t n, int32_t k);
+int32_t fgb_pcg_multi_f64(int64_t n, int32_t k, const int64_t* indptr, const int32_t* indices,
+                          const double* values, const double* diag_inv, const double* B, double* X,
+                          double atol, double rtol, int64_t maxit, fgb_pcg_info* info_host,
+                          void* workspace, size_t workspace_bytes, void* stream);
+
 /* Mixed precision: Jacobi-PCG iterations in FP32 on values32 (FP32 SpMV,
  * dots and updates) with FP64 reliable updates: whenever the FP32 residual
  * has dropped by `delta` since the last update (or looks converged), the

@@ -380,6 +380,21 @@ def coef_cases(ref_root):
         np.savez_compressed(os.path.join(HERE, f"coefq_{tag}.npz"), node=mesh.node, cell=mesh.cell, p=np.int64(p),
                             q=np.int64(q), rho=rho, K_diff=Kd, K_mass=Km, crow=c0, col=c1, val=c2)
         print("coefq", tag, NC, NQ, A.nnz)
+        if tag == "tet_p2":
+            # several right-hand sides of the last matrix (fealpy/solver/cg.py:60-123),
+            # with and without the Jacobi preconditioner
+            from fealpy.solver import cg
+            from fealpy.sparse import CSRTensor
+            Bm = rng.normal(size=(A.shape[0], 3))
+            d = A.diags()
+            Mj = CSRTensor(d.crow, d.col, 1.0 / d.values, A.shape)
+            xj, ij = cg(A, Bm.copy(), M=Mj, atol=1e-30, rtol=1e-10, returninfo=True)
+            xp, ip = cg(A, Bm.copy(), atol=1e-30, rtol=1e-10, returninfo=True)
+            np.savez_compressed(os.path.join(HERE, "cg_multi_rhs.npz"), crow=c0, col=c1, val=c2, B=Bm,
+                                x_jacobi=xj, niter_jacobi=np.int64(ij["niter"]),
+                                residual_jacobi=np.float64(ij["residual"]), x_plain=xp,
+                                niter_plain=np.int64(ip["niter"]), residual_plain=np.float64(ip["residual"]))
+            print("cg multi rhs", ij["niter"], ip["niter"])
 
 
 def _reference_root(argv):
