@@ -113,13 +113,13 @@ class BilinearForm(_Form):
                 raise NotImplementedError("only several scalar integrators can share one form")
         return out
 
-    def _symbolic(self, space, c2d, n, marks=None):
+    def _symbolic(self, space, c2d, n, marks=None, sub: bool = False):
         key = ("symbolic", n)
         cache = getattr(space, "_cache", {})
-        if self.reuse_pattern and key in cache:
+        if self.reuse_pattern and not sub and key in cache:
             return cache[key]
         out = symbolic_structure(c2d, n, marks=marks)
-        if self.reuse_pattern:
+        if self.reuse_pattern and not sub:
             cache[key] = out
         return out
 
@@ -139,8 +139,13 @@ class BilinearForm(_Form):
         _mark(marks, "start")
         if isinstance(plan, ScalarPlan):
             c2d = space.cell_to_dof()
+            sub = plan.cells is not None
+            if sub:
+                # integration over a sub-region: the pattern of its cells only
+                # (FEALPy scatters the region's local matrices alone)
+                c2d = c2d[plan.cells].contiguous()
             n = space.number_of_global_dofs()
-            adj_ptr, adj, indptr, indices = self._symbolic(space, c2d, n, marks)
+            adj_ptr, adj, indptr, indices = self._symbolic(space, c2d, n, marks, sub)
             mesh = space.mesh
             coef = plan.coef_matrix()
             passes = plan.passes()
@@ -148,7 +153,7 @@ class BilinearForm(_Form):
             for k, (chans, tabs) in enumerate(passes):
                 # more channels than one factor launch holds (coefficients per
                 # quadrature point): passes that add into the values
-                fac = K.cell_factors(mesh, chans, coef, dtype, status)
+                fac = K.cell_factors(mesh, chans, coef, dtype, status, cells=plan.cells)
                 if k == 0:
                     _mark(marks, "factors")
                 tab = torch.as_tensor(tabs, dtype=dtype, device=space.device)
@@ -160,12 +165,12 @@ class BilinearForm(_Form):
         elif isinstance(plan, ElasticityPlan):
             ss = space.scalar_space
             mesh = ss.mesh
-            cell = mesh.cell
+            cell = mesh.cell if plan.cells is None else mesh.cell[plan.cells].contiguous()
             NN = mesh.number_of_nodes()
-            adj_ptr, adj, nptr, nidx = self._symbolic(ss, cell, NN, marks)
+            adj_ptr, adj, nptr, nidx = self._symbolic(ss, cell, NN, marks, plan.cells is not None)
             indptr, indices = K.expand_blocks(NN, plan.gd, space.dof_priority, nptr, nidx)
             n = space.number_of_global_dofs()
-            fac = K.cell_factors(mesh, plan.channels, plan.coef_matrix(), dtype, status)
+            fac = K.cell_factors(mesh, plan.channels, plan.coef_matrix(), dtype, status, cells=plan.cells)
             _mark(marks, "factors")
             values, v32 = K.assemble_elasticity_p1(plan.gd, adj_ptr, adj, cell, fac, nptr, nidx, indptr,
                                                    indices.numel(), values_f32=emit_f32 and dtype == torch.float64,
@@ -212,22 +217,31 @@ class BilinearForm(_Form):
         if cache is None or cache[0] != key:
             status = _lib.status_word(space.device)
             coef = plan.coef_matrix()
-            fac = [(K.cell_factors(space.mesh, chans, coef, dtype, status), tabs) for chans, tabs in plan.passes()]
+            fac = [(K.cell_factors(space.mesh, chans, coef, dtype, status, cells=plan.cells), tabs)
+                   for chans, tabs in plan.passes()]
             _lib.check_status_word("matrix-free factors", status)
             n = space.number_of_global_dofs()
+            c2d = space.cell_to_dof() if plan.cells is None else space.cell_to_dof()[plan.cells].contiguous()
             akey = ("adjacency", n)
-            if akey not in space._cache:
+            if plan.cells is not None:
                 st = _lib.status_word(space.device)
-                adj_ptr, adj, _ = K.build_adjacency(space.cell_to_dof(), n, st)
+                adj_ptr, adj, _ = K.build_adjacency(c2d, n, st)
                 _lib.check_status_word("adjacency", st)
-                space._cache[akey] = (adj_ptr, adj)
-            cache = (key, fac, space._cache[akey])
+                adjacency = (adj_ptr, adj)
+            else:
+                if akey not in space._cache:
+                    st = _lib.status_word(space.device)
+                    adj_ptr, adj, _ = K.build_adjacency(c2d, n, st)
+                    _lib.check_status_word("adjacency", st)
+                    space._cache[akey] = (adj_ptr, adj)
+                adjacency = space._cache[akey]
+            cache = (key, fac, c2d, adjacency)
             self._mf_cache = cache
-        _, fac, (adj_ptr, adj) = cache
+        _, fac, c2d, (adj_ptr, adj) = cache
         ud = u.to(device=space.device, dtype=dtype)
         yc = None
         for f, tables in fac:
-            y = K.cell_apply(space.cell_to_dof(), tables, f, ud)
+            y = K.cell_apply(c2d, tables, f, ud)
             yc = y if yc is None else yc + y
         return K.gather_sum(adj_ptr, adj, yc)
 
@@ -249,23 +263,41 @@ class LinearForm(_Form):
 
     def assembly(self, *, format="dense") -> torch.Tensor:
         space = self.space
-        local = None
+        mesh = space.scalar_space.mesh if hasattr(space, "scalar_space") else space.mesh
+        # local vectors grouped by the cells they integrate over (all cells,
+        # or a sub-region): one dof gather per group
+        groups = []
         for it in self.integrators.values():
             ints = it.ints if isinstance(it, GroupIntegrator) else [it]
             for i in ints:
                 v = i.assembly(space)
-                local = v if local is None else local + v
-        if local is None:
+                cells = i.cell_selection(mesh)
+                for g in groups:
+                    if (g[0] is None and cells is None) or (g[0] is not None and cells is not None and
+                                                           g[0].shape == cells.shape and torch.equal(g[0], cells)):
+                        g[1] = g[1] + v
+                        break
+                else:
+                    groups.append([cells, v])
+        if not groups:
             raise RuntimeError("no integrator added to the form")
-        c2d = space.cell_to_dof()
         n = space.number_of_global_dofs()
-        key = ("adjacency", n)
-        cache = space._cache
-        if key not in cache:
-            st = _lib.status_word(space.device)
-            adj_ptr, adj, _ = K.build_adjacency(c2d, n, st)
-            _lib.check_status_word("adjacency", st)
-            cache[key] = (adj_ptr, adj)
-        adj_ptr, adj = cache[key]
-        self._V = K.gather_sum(adj_ptr, adj, local.to(torch.float64).contiguous())
+        out = None
+        for cells, local in groups:
+            if cells is None:
+                key = ("adjacency", n)
+                cache = space._cache
+                if key not in cache:
+                    st = _lib.status_word(space.device)
+                    adj_ptr, adj, _ = K.build_adjacency(space.cell_to_dof(), n, st)
+                    _lib.check_status_word("adjacency", st)
+                    cache[key] = (adj_ptr, adj)
+                adj_ptr, adj = cache[key]
+            else:
+                st = _lib.status_word(space.device)
+                adj_ptr, adj, _ = K.build_adjacency(space.cell_to_dof()[cells].contiguous(), n, st)
+                _lib.check_status_word("adjacency", st)
+            vec = K.gather_sum(adj_ptr, adj, local.to(torch.float64).contiguous())
+            out = vec if out is None else out + vec
+        self._V = out
         return self._V

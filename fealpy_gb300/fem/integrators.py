@@ -36,15 +36,20 @@ def _is_full(index) -> bool:
 class ScalarPlan:
     """Local matrix = sum_t factor_t(c) * tables[t]; channel t = (kind, coef_row, scale)."""
 
-    def __init__(self, channels: List[Tuple[int, int, float]], coefs: List[torch.Tensor], tables: np.ndarray):
+    def __init__(self, channels: List[Tuple[int, int, float]], coefs: List[torch.Tensor], tables: np.ndarray,
+                 cells: Optional[torch.Tensor] = None):
         self.channels = channels
         self.coefs = coefs
         self.tables = tables
+        self.cells = cells  # sub-region (int64 cell indices) or None
 
     def __add__(self, other: "ScalarPlan") -> "ScalarPlan":
+        if not _same_cells(self.cells, other.cells):
+            raise NotImplementedError("integrators of one form integrate over the same cells on the GB300 path")
         off = len(self.coefs)
         ch = list(self.channels) + [(k, (c + off) if c >= 0 else -1, s) for k, c, s in other.channels]
-        return ScalarPlan(ch, self.coefs + other.coefs, np.concatenate([self.tables, other.tables], axis=0))
+        return ScalarPlan(ch, self.coefs + other.coefs, np.concatenate([self.tables, other.tables], axis=0),
+                          self.cells)
 
     def coef_matrix(self):
         return torch.stack(self.coefs, 0) if self.coefs else None
@@ -57,26 +62,36 @@ class ScalarPlan:
         return [(self.channels[a:a + limit], self.tables[a:a + limit]) for a in range(0, n, limit)]
 
 
+def _same_cells(a: Optional[torch.Tensor], b: Optional[torch.Tensor]) -> bool:
+    if a is None or b is None:
+        return a is None and b is None
+    return a is b or (a.shape == b.shape and bool(torch.equal(a, b)))
+
+
 class ElasticityPlan:
     """P1 elasticity: factor channels = grad(lambda_{1..GD}) then |T| D00, |T| D_lambda, |T| D_mu."""
 
-    def __init__(self, gd: int, channels, coefs):
+    def __init__(self, gd: int, channels, coefs, cells: Optional[torch.Tensor] = None):
         self.gd = gd
         self.channels = channels
         self.coefs = coefs
+        self.cells = cells
 
     def coef_matrix(self):
         return torch.stack(self.coefs, 0) if self.coefs else None
 
 
-def _cell_coefficient(coef, space, q: int) -> Tuple[float, Optional[torch.Tensor], Optional[torch.Tensor]]:
+def _cell_coefficient(coef, space, q: int, cells: Optional[torch.Tensor] = None
+                      ) -> Tuple[float, Optional[torch.Tensor], Optional[torch.Tensor]]:
     """(scale, per-cell array or None, per-point array or None) from a FEALPy
     CoefLike (``fealpy/utils/utils.py:21-53``): a number, an (NC,) array, an
     (NC, NQ) array of values at the quadrature points of rule ``q``, or a
     callable evaluated there.  Values that agree across each cell's points
-    become a per-cell array; otherwise the (NC, NQ) array is returned."""
+    become a per-cell array; otherwise the (NC, NQ) array is returned.  With
+    ``cells`` (a sub-region) NC counts the selected cells and callables are
+    evaluated on them."""
     mesh = space.mesh
-    NC = mesh.number_of_cells()
+    NC = mesh.number_of_cells() if cells is None else int(cells.numel())
     if coef is None:
         return 1.0, None, None
     if isinstance(coef, (int, float)):
@@ -96,14 +111,15 @@ def _cell_coefficient(coef, space, q: int) -> Tuple[float, Optional[torch.Tensor
             raise ValueError(f"an (NC, NQ) coefficient needs NQ = {NQ} values per cell for quadrature order {q}")
         raise ValueError("coefficients are a number, (NC,) or (NC, NQ)")
     if isinstance(coef, np.ndarray):
-        return _cell_coefficient(torch.as_tensor(coef, device=mesh.device), space, q)
+        return _cell_coefficient(torch.as_tensor(coef, device=mesh.device), space, q, cells)
     if callable(coef):
         bcs, _ = mesh.quadrature_formula(q).get_quadrature_points_and_weights()
+        index = _S if cells is None else cells
         if getattr(coef, "coordtype", "barycentric") == "cartesian":
-            val = coef(mesh.bc_to_point(bcs))
+            val = coef(mesh.bc_to_point(bcs, index=index))
         else:
-            val = coef(torch.as_tensor(bcs, device=mesh.device), index=_S)
-        return _cell_coefficient(torch.as_tensor(val, device=mesh.device), space, q)
+            val = coef(torch.as_tensor(bcs, device=mesh.device), index=index)
+        return _cell_coefficient(torch.as_tensor(val, device=mesh.device), space, q, cells)
     raise TypeError(f"coef should be int, float, TensorLike or callable, but got {type(coef)}")
 
 
@@ -134,8 +150,35 @@ class Integrator:
         return self._region
 
     def _check_region(self):
-        if self._region is not None or not _is_full(getattr(self, "index", None)):
-            raise NotImplementedError("integration over a sub-region of cells is not provided on the GB300 path")
+        """Kept for callers of the former interface: sub-regions are supported."""
+        return None
+
+    def cell_selection(self, mesh) -> Optional[torch.Tensor]:
+        """The cells integrated over as an int64 index tensor on the mesh's
+        device, or None for all cells: ``region`` (index or boolean tensor, or
+        a callable of the mesh; ``fealpy/fem/integrator.py:141-162``) or, for
+        the integrators that take it, ``index`` (``scalar_mass_integrator.py``,
+        ``linear_elasticity_integrator.py``)."""
+        sel = self._region
+        if sel is None:
+            idx = getattr(self, "index", None)
+            if _is_full(idx):
+                return None
+            sel = idx
+        if callable(sel) and not isinstance(sel, (torch.Tensor, np.ndarray)):
+            sel = sel(mesh)
+        NC = mesh.number_of_cells()
+        if isinstance(sel, slice):
+            return torch.arange(NC, device=mesh.device)[sel]
+        t = torch.as_tensor(sel, device=mesh.device)
+        if t.dtype == torch.bool:
+            if t.numel() != NC:
+                raise ValueError("a boolean region has one entry per cell")
+            return torch.nonzero(t).reshape(-1)
+        t = t.reshape(-1).to(torch.int64)
+        if t.numel() and (int(t.min()) < 0 or int(t.max()) >= NC):
+            raise IndexError("region cell index out of range")
+        return t
 
     def __add__(self, other):
         if isinstance(other, Integrator):
@@ -149,6 +192,9 @@ class Integrator:
 
     def to_global_dof(self, space, /, indices=None):
         c2d = space.cell_to_dof()
+        sel = self.cell_selection(space.mesh)
+        if sel is not None:
+            c2d = c2d[sel]
         return c2d if indices is None else c2d[indices]
 
     def __repr__(self):
@@ -167,7 +213,7 @@ class _OperatorIntegrator(Integrator):
         coef = plan.coef_matrix()
         out = None
         for chans, tabs in plan.passes():
-            f = K.cell_factors(mesh, chans, coef, torch.float64)
+            f = K.cell_factors(mesh, chans, coef, torch.float64, cells=plan.cells)
             out = K.local_matrices(f, torch.as_tensor(tabs, dtype=torch.float64, device=mesh.device), out)
         return out if indices is None else out[indices]
 
@@ -191,18 +237,19 @@ class ScalarDiffusionIntegrator(_OperatorIntegrator):
         mesh = space.mesh
         TD = mesh.TD
         q = space.p + 3 if self.q is None else self.q
-        scale, arr, arrq = _cell_coefficient(self.coef, space, q)
+        cells = self.cell_selection(mesh)
+        scale, arr, arrq = _cell_coefficient(self.coef, space, q, cells)
         pairs = sx.metric_pairs(TD)
         if arrq is not None:
             # a coefficient per quadrature point: one channel per (point,
             # metric entry) with that point's table
             coefs = [arrq[:, iq].contiguous() for iq in range(arrq.shape[1])]
             ch = [(_lib.FGB_CH_METRIC + k * 3 + l, iq, 1.0) for iq in range(arrq.shape[1]) for k, l in pairs]
-            return ScalarPlan(ch, coefs, sx.diffusion_tables_q(TD, space.p, q))
+            return ScalarPlan(ch, coefs, sx.diffusion_tables_q(TD, space.p, q), cells)
         coefs = [arr] if arr is not None else []
         ci = 0 if arr is not None else -1
         ch = [(_lib.FGB_CH_METRIC + k * 3 + l, ci, scale) for k, l in pairs]
-        return ScalarPlan(ch, coefs, sx.diffusion_tables(TD, space.p, q))
+        return ScalarPlan(ch, coefs, sx.diffusion_tables(TD, space.p, q), cells)
 
 
 class ScalarMassIntegrator(_OperatorIntegrator):
@@ -222,14 +269,15 @@ class ScalarMassIntegrator(_OperatorIntegrator):
         self._check_region()
         mesh = space.mesh
         q = space.p + 3 if self.q is None else self.q
-        scale, arr, arrq = _cell_coefficient(self.coef, space, q)
+        cells = self.cell_selection(mesh)
+        scale, arr, arrq = _cell_coefficient(self.coef, space, q, cells)
         if arrq is not None:
             coefs = [arrq[:, iq].contiguous() for iq in range(arrq.shape[1])]
             ch = [(_lib.FGB_CH_MEASURE, iq, 1.0) for iq in range(arrq.shape[1])]
-            return ScalarPlan(ch, coefs, sx.mass_tables_q(mesh.TD, space.p, q))
+            return ScalarPlan(ch, coefs, sx.mass_tables_q(mesh.TD, space.p, q), cells)
         coefs = [arr] if arr is not None else []
         ch = [(_lib.FGB_CH_MEASURE, 0 if arr is not None else -1, scale)]
-        return ScalarPlan(ch, coefs, sx.mass_table(mesh.TD, space.p, q))
+        return ScalarPlan(ch, coefs, sx.mass_table(mesh.TD, space.p, q), cells)
 
 
 class LinearElasticityIntegrator(_OperatorIntegrator):
@@ -273,15 +321,18 @@ class LinearElasticityIntegrator(_OperatorIntegrator):
             d00 = 2.0 * dmu + d01
         else:
             d00, d01, dmu = D[:, 0, 0, 0], D[:, 0, 0, 1], D[:, 0, 2, 2]
+        cells = self.cell_selection(mesh)
         chans = [(_lib.FGB_CH_GRAD + k * 3 + a, -1, 1.0) for k in range(gd) for a in range(gd)]
         coefs = []
         for v in (d00, d01, dmu):
             if v.numel() == 1:
                 chans.append((_lib.FGB_CH_MEASURE, -1, float(v.item()) * wsum))
             else:
+                if cells is not None and v.numel() == mesh.number_of_cells():
+                    v = v[cells]  # per-cell material of the whole mesh, restricted to the region
                 chans.append((_lib.FGB_CH_MEASURE, len(coefs), wsum))
                 coefs.append(v.contiguous())
-        return ElasticityPlan(gd, chans, coefs)
+        return ElasticityPlan(gd, chans, coefs, cells)
 
 
 class GroupIntegrator(Integrator):
@@ -347,16 +398,18 @@ class GroupIntegrator(Integrator):
 # ---------------------------------------------------------------------------
 # source integrators (right-hand sides)
 # ---------------------------------------------------------------------------
-def _source_values(source, mesh, bcs):
-    """Source values at quadrature points: (NC, NQ) or broadcastable."""
+def _source_values(source, mesh, bcs, index=_S):
+    """Source values at quadrature points: (NC, NQ) or broadcastable (NC: the
+    cells of ``index``)."""
     if isinstance(source, (int, float)):
         return float(source)
     if isinstance(source, torch.Tensor):
         return source.to(device=mesh.device, dtype=torch.float64)
     if callable(source):
         if getattr(source, "coordtype", "barycentric") == "cartesian":
-            return torch.as_tensor(source(mesh.bc_to_point(bcs)), dtype=torch.float64, device=mesh.device)
-        return torch.as_tensor(source(torch.as_tensor(bcs, device=mesh.device), index=_S), dtype=torch.float64,
+            return torch.as_tensor(source(mesh.bc_to_point(bcs, index=index)), dtype=torch.float64,
+                                   device=mesh.device)
+        return torch.as_tensor(source(torch.as_tensor(bcs, device=mesh.device), index=index), dtype=torch.float64,
                                device=mesh.device)
     raise TypeError(f"source should be int, float, TensorLike or callable, but got {type(source)}")
 
@@ -375,13 +428,15 @@ class ScalarSourceIntegrator(Integrator):
         mesh = space.mesh
         q = space.p + 3 if self.q is None else self.q
         bcs, ws = mesh.quadrature_formula(q).get_quadrature_points_and_weights()
-        cm = mesh.entity_measure("cell")
+        cells = self.cell_selection(mesh)
+        index = _S if cells is None else cells
+        cm = mesh.entity_measure("cell", index=index)
         phi = torch.as_tensor(sx.shape_function(bcs, space.p), device=mesh.device)       # (NQ, ldof)
         w = torch.as_tensor(ws, device=mesh.device)
-        f = _source_values(self.source, mesh, bcs)
+        f = _source_values(self.source, mesh, bcs, index)
         if isinstance(f, float):
             return torch.einsum("c,q,qi->ci", cm, w, phi) * f
-        if f.ndim == 1 and f.shape[0] == mesh.number_of_cells():
+        if f.ndim == 1 and f.shape[0] == cm.shape[0]:
             f = f[:, None].expand(-1, len(ws))
         return torch.einsum("c,q,qi,cq->ci", cm, w, phi, f)
 
@@ -402,15 +457,17 @@ class VectorSourceIntegrator(Integrator):
         gd = space.dof_numel
         q = ss.p + 3 if self.q is None else self.q
         bcs, ws = mesh.quadrature_formula(q).get_quadrature_points_and_weights()
-        cm = mesh.entity_measure("cell")
+        cells = self.cell_selection(mesh)
+        index = _S if cells is None else cells
+        cm = mesh.entity_measure("cell", index=index)
         phi = torch.as_tensor(sx.shape_function(bcs, ss.p), device=mesh.device)
         w = torch.as_tensor(ws, device=mesh.device)
         f = self.source
         if callable(f):
-            f = _source_values(f, mesh, bcs)                      # (NC, NQ, gd)
+            f = _source_values(f, mesh, bcs, index)               # (NC, NQ, gd)
         else:
             f = torch.as_tensor(f, dtype=torch.float64, device=mesh.device).reshape(1, 1, gd)
-            f = f.expand(mesh.number_of_cells(), len(ws), gd)
+            f = f.expand(cm.shape[0], len(ws), gd)
         loc = torch.einsum("c,q,qi,cqd->cid", cm, w, phi, f)       # (NC, ldof, gd)
         if space.dof_priority:
             loc = loc.transpose(1, 2)

@@ -24,11 +24,14 @@ def _dev(mesh_or_tensor):
 
 
 def cell_factors(mesh, channels: Sequence[Tuple[int, int, float]], coef: Optional[torch.Tensor],
-                 out_dtype=torch.float64, status: Optional[torch.Tensor] = None) -> torch.Tensor:
+                 out_dtype=torch.float64, status: Optional[torch.Tensor] = None,
+                 cells: Optional[torch.Tensor] = None) -> torch.Tensor:
     """(NC, nch) factor channels, see ``fgb_cell_factors``.  ``channels`` is a
-    list of ``(kind, coef_row or -1, scale)``; ``coef`` is (n_coef, NC) float64."""
+    list of ``(kind, coef_row or -1, scale)``; ``coef`` is (n_coef, NC) float64.
+    ``cells``: the factors of these cells only (a sub-region; NC = its size)."""
     dev = _dev(mesh.node)
-    NC = mesh.number_of_cells()
+    cell_arr = mesh.cell if cells is None else mesh.cell[cells].contiguous()
+    NC = cell_arr.shape[0]
     nch = len(channels)
     if nch == 0 or nch > _lib.FGB_MAX_CHANNELS:
         raise ValueError(f"between 1 and {_lib.FGB_MAX_CHANNELS} factor channels are supported, got {nch}")
@@ -42,7 +45,7 @@ def cell_factors(mesh, channels: Sequence[Tuple[int, int, float]], coef: Optiona
         coef = coef.to(device=dev, dtype=torch.float64).contiguous()
     own = status is None
     st = status_word(dev) if own else status
-    call("fgb_cell_factors", mesh.TD, NC, ptr(mesh.node), ptr(mesh.cell), nch, kinds, coefs, scales, ptr(coef),
+    call("fgb_cell_factors", mesh.TD, NC, ptr(mesh.node), ptr(cell_arr), nch, kinds, coefs, scales, ptr(coef),
          dtype_code(out_dtype), ptr(out), ptr(st), stream_ptr(dev))
     if own:
         check_status_word("fgb_cell_factors", st)
@@ -170,10 +173,11 @@ def local_matrices(factors: torch.Tensor, tables: torch.Tensor, out: Optional[to
 
 def local_elasticity_p1(mesh, plan, priority: bool = False) -> torch.Tensor:
     """(NC, (GD+1) GD, (GD+1) GD) P1 elasticity local matrices from the
-    plan's factor channels; ``priority``: component-major local order."""
+    plan's factor channels (its cells); ``priority``: component-major local
+    order."""
     dev = _dev(mesh.node)
     gd = plan.gd
-    f = cell_factors(mesh, plan.channels, plan.coef_matrix(), torch.float64)
+    f = cell_factors(mesh, plan.channels, plan.coef_matrix(), torch.float64, cells=plan.cells)
     ld = (gd + 1) * gd
     out = torch.empty((f.shape[0], ld, ld), dtype=torch.float64, device=dev)
     call("fgb_local_elasticity_p1", dtype_code(torch.float64), gd, f.shape[0], ptr(f), 1 if priority else 0,

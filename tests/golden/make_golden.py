@@ -396,6 +396,26 @@ def coef_cases(ref_root):
                                 niter_plain=np.int64(ip["niter"]), residual_plain=np.float64(ip["residual"]))
             print("cg multi rhs", ij["niter"], ip["niter"])
 
+    # integration over a sub-region (fealpy/fem/integrator.py:141-162): the
+    # cells whose centroid has x < 0.55 (region= for diffusion, index= for
+    # mass) on P2 triangles.  (A ScalarSourceIntegrator with region= and a
+    # LinearElasticityIntegrator with index= do not run in the reference: the
+    # former's to_global_dof ignores the region, the latter sizes its local
+    # matrices by all cells.)
+
+    m0 = TriangleMesh.from_box([0, 1, 0, 1], 5, 4)
+    mesh = TriangleMesh(jitter(m0.node, m0.boundary_node_flag(), 0.2, 0.15, rng), m0.cell)
+    reg = np.nonzero(mesh.entity_barycenter("cell")[:, 0] < 0.55)[0]
+    space = LagrangeFESpace(mesh, p=2)
+    bf = BilinearForm(space)
+    bf.add_integrator(ScalarDiffusionIntegrator(coef=kappa2, q=4, region=reg),
+                      ScalarMassIntegrator(coef=2.0, q=4, index=reg))
+    A = bf.assembly()
+    c0, c1, c2 = canonical(A.crow, A.col, A.values)
+    np.savez_compressed(os.path.join(HERE, "region_cases.npz"), node=mesh.node, cell=mesh.cell, region=reg,
+                        crow=c0, col=c1, val=c2)
+    print("region", len(reg), mesh.number_of_cells(), A.nnz)
+
 
 def _reference_root(argv):
     root = argv[0] if argv else os.environ.get("FEALPY_REFERENCE")
