@@ -50,13 +50,13 @@ def _level_sell(L: "_Level", with32: bool = True, with64: bool = False):
     except _lib.FgbError:
         S = K.sell_build(L.indptr, L.indices, v64, v32, want64=with64, want32=with32, d16=False)
     dt = torch.float32 if with32 else torch.float64
-    key = (S.n, S.padded_nnz, dt, S.cols)
-    shape = _solver._LAUNCH_CACHE.get(key)
-    if shape is None:
-        times = K.sell_autotune(S, dt)
-        shape = min(times, key=times.get)
-        _solver._LAUNCH_CACHE[key] = shape
-    S.set_launch(*shape)
+    # the solver's autotuned launch shape when this size was tuned before (the
+    # same matrix solved by cg), else the kernels' default shape: a hierarchy
+    # is built per system, and timing candidate shapes for every new size
+    # would cost more than it saves
+    shape = _solver._LAUNCH_CACHE.get((S.n, S.padded_nnz, dt, S.cols))
+    if shape is not None:
+        S.set_launch(*shape)
     return S
 
 

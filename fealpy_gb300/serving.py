@@ -26,7 +26,7 @@ import torch
 
 from .batch import BatchSolver
 
-__all__ = ["SolveServer", "poisson_request_problem", "resident_estimate"]
+__all__ = ["SolveServer", "poisson_request_problem", "resident_estimate", "multigrid_solve"]
 
 
 def resident_estimate(n: int, nnz: int, fp64: bool) -> int:
@@ -92,20 +92,63 @@ def poisson_request_problem(req: dict, device, dtype=torch.float64, inputs: Opti
     return DirichletBC(space, gd=0.0).apply(bf.assembly(dtype=dtype), lf.assembly())
 
 
+def multigrid_solve(A, b, rtol: float = 1e-10, maxit: int = 100000, fp64: bool = False):
+    """The multigrid lane's solve of one system on the current stream: the
+    AMG hierarchy (FP32 V-cycle, FP64 with ``fp64``), PCG on the iterated
+    residual, restarted from the iterate on the true residual b - A x while
+    that is above ``rtol`` and still halves (the iterated residual drifts
+    below the true one on ill-conditioned systems).  Returns (x, iterations,
+    stop reason, true relative residual)."""
+    from .amg import GAMGSolver
+    from .solver import cg
+    M = GAMGSolver(vcycle_f32=not fp64).setup(A)
+    bnorm = float(torch.linalg.norm(b))
+    x, niter, reason, relres = None, 0, 0, float("inf")
+    for _ in range(4):
+        x, inf = cg(A, b, x0=x, M=M, atol=0.0, rtol=rtol, maxit=maxit, returninfo=True, stop="residual")
+        niter += int(inf["niter"])
+        reason = int(inf["reason"])
+        r_new = float(torch.linalg.norm(b - A @ x)) / bnorm if bnorm > 0 else 0.0
+        improved = r_new < 0.5 * relres
+        relres = min(relres, r_new)
+        if r_new <= rtol or not improved:
+            break
+    return x, niter, reason, relres
+
+
 class SolveServer:
     """Continuous-batching solve server.
 
     ``fp64``: plain FP64 PCG for every request (else FP32 iterations with FP64
     refinement, FP64 continuation where FP32 stalls).  ``hbm_budget`` bounds
     the resident bytes of admitted requests; ``max_slots`` the batch size;
-    ``chunk`` the iterations run between admissions."""
+    ``chunk`` the iterations run between admissions; ``build_workers``
+    threads build queued requests ahead, each on its own high-priority
+    stream (measured on the C4 stream with the multigrid lane: 1 builder
+    20-26 req/s, 2: 37, 4: 40-47, 6: 49).
+
+    ``amg_min_dofs``: requests of at least this many dofs go to a multigrid
+    lane: PCG with the aggregation AMG V-cycle (``GAMGSolver``; FP32 V-cycle,
+    or FP64 with ``fp64``), on worker threads with their own CUDA streams,
+    beside the batch.  Jacobi needs iterations that grow with the
+    mesh size (thousands for the largest requests), the multigrid about sixty;
+    the batch keeps the many small requests.  ``amg_workers`` lane requests
+    run at once, each on its worker's stream.  A lane result is the same alone
+    and in any mix (its hierarchy and iterations depend only on its system)."""
 
     def __init__(self, *, hbm_budget: float = 150e9, max_slots: int = 256, chunk: int = 64, fp64: bool = False,
-                 rtol: float = 1e-10, maxit: int = 100000, device=None, **batch_kw):
+                 rtol: float = 1e-10, maxit: int = 100000, device=None, amg_min_dofs: Optional[int] = None,
+                 amg_workers: int = 4, build_workers: int = 6, **batch_kw):
         self.device = torch.device(device) if device is not None else torch.device("cuda",
                                                                                    torch.cuda.current_device())
         self.hbm_budget, self.max_slots, self.chunk = float(hbm_budget), int(max_slots), int(chunk)
         self.fp64, self.rtol, self.maxit = bool(fp64), float(rtol), int(maxit)
+        # requests of at least this many dofs (the request's "dofs") are solved
+        # by the multigrid lane instead of the batch; None: every request in
+        # the batch
+        self.amg_min_dofs = None if amg_min_dofs is None else int(amg_min_dofs)
+        self.amg_workers = max(int(amg_workers), 1)
+        self.build_workers = max(int(build_workers), 1)
         kw = dict(max_slice_tiles=1 << 18, max_row_tiles=1 << 18)
         kw.update(batch_kw)
         self.batch = BatchSolver(self.max_slots, device=self.device, **kw)
@@ -146,11 +189,16 @@ class SolveServer:
         sols: Dict[int, np.ndarray] = {}
         futures: Dict[int, Future] = {}
         # high priority: the batch's tile kernels fill every SM, so the build
-        # kernels are scheduled first whenever blocks retire between them
-        build_stream = torch.cuda.Stream(self.device, priority=-1)
+        # kernels are scheduled first whenever blocks retire between them;
+        # one stream per builder thread
+        import threading
+        build_local = threading.local()
         main_stream = torch.cuda.current_stream(self.device)
 
         def build_async(req):
+            build_stream = getattr(build_local, "stream", None)
+            if build_stream is None:
+                build_stream = build_local.stream = torch.cuda.Stream(self.device, priority=-1)
             with torch.cuda.stream(build_stream):
                 A, b = build(req, self.device)
                 ev = torch.cuda.Event()
@@ -164,13 +212,48 @@ class SolveServer:
                 sols[key] = x_host.numpy()
             del x_dev
 
-        builder = ThreadPoolExecutor(1)
+        lane_local = threading.local()
+        lane_done = [0]
+        lane_lock = threading.Lock()
+
+        def amg_job(key, A, b, ev, arrival):
+            """One request through the multigrid lane: hierarchy, PCG, true
+            residual, asynchronous copy; the request ends when the copy lands.
+            Each lane worker thread has its own CUDA stream."""
+            amg_stream = getattr(lane_local, "stream", None)
+            if amg_stream is None:
+                amg_stream = lane_local.stream = torch.cuda.Stream(self.device)
+            with torch.cuda.stream(amg_stream):
+                amg_stream.wait_event(ev)
+                x, niter, reason, relres = multigrid_solve(A, b, self.rtol, self.maxit, self.fp64)
+                x_host = torch.empty(x.shape, dtype=x.dtype, pin_memory=True)
+                x_host.copy_(x, non_blocking=True)
+                done = torch.cuda.Event()
+                done.record(amg_stream)
+            done.synchronize()
+            lat[key] = time.perf_counter() - t0 - arrival
+            info[key] = {"relres": relres, "niter": niter, "lane": "amg", "reason": reason}
+            if keep_solutions:
+                sols[key] = x_host.numpy()
+            with lane_lock:
+                lane_done[0] += 1
+
+        def to_lane(i):
+            return self.amg_min_dofs is not None and requests[i].get("dofs", 0) >= self.amg_min_dofs
+
+        builder = ThreadPoolExecutor(self.build_workers)
         finisher = ThreadPoolExecutor(1)
+        lane = ThreadPoolExecutor(self.amg_workers)
         done_jobs = []
+        lane_jobs = []
         t0 = time.perf_counter()
         try:
             finished = 0
-            while finished < len(requests):
+            pending_lane: List[Future] = []
+            while finished + lane_done[0] < len(requests):
+                for j in [j for j in pending_lane if j.done()]:
+                    j.result()  # a failure in the lane surfaces here
+                    pending_lane.remove(j)
                 now = time.perf_counter() - t0
                 while nxt < len(order) and requests[order[nxt]]["t"] * time_scale <= now:
                     queue.append(order[nxt])
@@ -181,10 +264,25 @@ class SolveServer:
                 # admission: FIFO while a slot and the memory budget allow; a
                 # request still being built is waited for while the batch runs
                 # below half its slots, otherwise it blocks the ones behind it
-                # until the next chunk boundary
-                while queue and self.batch.free_slots() > 0:
+                # until the next chunk boundary.  Requests of the multigrid
+                # lane leave the queue as soon as they are built.
+                while queue:
                     i = queue[0]
                     fut = futures[i]
+                    if to_lane(i):
+                        if not fut.done():
+                            break
+                        A, b, ev = fut.result()
+                        lane_jobs.append(lane.submit(amg_job, i, A, b, ev, requests[i]["t"] * time_scale))
+                        pending_lane.append(lane_jobs[-1])
+                        queue.pop(0)
+                        del futures[i]
+                        for j in queue[:max(prefetch, 1)]:
+                            if j not in futures:
+                                futures[j] = builder.submit(build_async, requests[j])
+                        continue
+                    if self.batch.free_slots() <= 0:
+                        break
                     if not fut.done() and 2 * self.batch.active() >= self.max_slots:
                         break
                     A, b, ev = fut.result()
@@ -199,10 +297,12 @@ class SolveServer:
                         if j not in futures:
                             futures[j] = builder.submit(build_async, requests[j])
                 if self.batch.active() == 0:
-                    if nxt < len(order):
+                    if nxt < len(order) and not queue:
                         wait = requests[order[nxt]]["t"] * time_scale - (time.perf_counter() - t0)
                         if wait > 0:
-                            time.sleep(wait)
+                            time.sleep(min(wait, 0.002) if pending_lane else wait)
+                    else:
+                        time.sleep(0.0005)  # builds or lane jobs in flight
                     continue
                 for r in self.batch.step(max_iterations=self.chunk):
                     x_host = torch.empty(r.x.shape, dtype=r.x.dtype, pin_memory=True)
@@ -216,15 +316,19 @@ class SolveServer:
                     finished += 1
             for j in done_jobs:
                 j.result()
+            for j in lane_jobs:
+                j.result()
         finally:
             builder.shutdown(wait=True)
             finisher.shutdown(wait=True)
+            lane.shutdown(wait=True)
         makespan = time.perf_counter() - t0
         v = np.array([lat[i] for i in range(len(requests))])
         out = {"n": len(requests), "p50_s": float(np.percentile(v, 50)), "p99_s": float(np.percentile(v, 99)),
                "mean_s": float(v.mean()), "throughput_rps": len(requests) / makespan, "makespan_s": makespan,
                "dofs_per_s": float(sum(req.get("dofs", 0) for req in requests) / makespan),
                "peak_resident_bytes": int(self.peak_resident), "fp64_continuations": self.batch.fallbacks,
+               "amg_lane_requests": len(lane_jobs),
                "max_relres": max(d["relres"] for d in info.values()), "latencies_s": v.tolist(), "info": info}
         if keep_solutions:
             out["solutions"] = sols

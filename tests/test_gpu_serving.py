@@ -64,3 +64,34 @@ def test_serving_memory_budget_limits_admission():
     out = srv.run(reqs)
     assert out["n"] == len(reqs) and out["max_relres"] <= 1e-10 * 1.0001
     assert srv.peak_resident <= 1.2 * big
+
+
+def test_serving_multigrid_lane_mix_equals_solo():
+    """Requests above the lane threshold are solved by multigrid PCG beside the
+    batch: every result meets 1e-10, a lane result equals the same request
+    solved alone through the lane's path bit for bit, and matches the oracle."""
+    dev = cuda()
+    from fealpy_gb300.serving import SolveServer, poisson_request_problem, multigrid_solve
+    from oracle import fem_oracle as O
+    reqs = _stream()
+    thr = sorted(r["dofs"] for r in reqs)[len(reqs) // 2]  # about half the requests in the lane
+    srv = SolveServer(max_slots=6, chunk=16, device=dev, amg_min_dofs=thr)
+    out = srv.run(reqs, keep_solutions=True)
+    lane = [i for i, r in enumerate(reqs) if r["dofs"] >= thr]
+    assert out["amg_lane_requests"] == len(lane) > 0
+    assert out["max_relres"] <= 1e-10 * 1.0001
+    for i in lane:
+        assert out["info"][i]["lane"] == "amg" and out["info"][i]["niter"] < 200
+        inp = {}
+        A, b = poisson_request_problem(reqs[i], dev, inputs=inp)
+        x, niter, _, relres = multigrid_solve(A, b, 1e-10, 100000)
+        assert np.array_equal(x.cpu().numpy(), out["solutions"][i]), i
+        assert niter == out["info"][i]["niter"] and relres == out["info"][i]["relres"]
+        if inp["kind"] == "elast":
+            ref = O.elasticity_pipeline(inp["node"], inp["cell"], 1.0 * inp["scale"], 0.5 * inp["scale"], q=4,
+                                        clamp=lambda x: np.abs(x[..., 0]) < 1e-12, rtol=1e-12)
+        else:
+            ref = O.poisson_pipeline(inp["node"], inp["cell"], inp["p"], kappa=inp["kappa"], q=inp["p"] + 2,
+                                     rtol=1e-12)
+        err = np.max(np.abs(out["solutions"][i] - ref["x"])) / np.max(np.abs(ref["x"]))
+        assert err < 1e-8, (i, inp["kind"], err)
