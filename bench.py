@@ -733,16 +733,22 @@ def batched_setup(torch, F, meshes, dev):
 # iterations resolve: with "mixed" exactly these systems stagnate in FP32 and
 # are continued in FP64), all others FP32-refined
 AUTO_FP64_P3_DOFS = 100_000
+# batched workload, multigrid-lane variant: systems of at least this many dofs
+# are solved by multigrid PCG beside the batch
+BATCH_LANE_MIN_DOFS = 100_000
 
 
-def batched_step(torch, F, probs, dtype, bs_kw, marks=None, fp64=False, graph=True):
+def batched_step(torch, F, probs, dtype, bs_kw, marks=None, fp64=False, graph=True, lane_min_dofs=None):
     """Assemble every problem (diffusion with the checkerboard coefficient,
     quadrature p + 3, f = 1, u = 0) and solve all of them in one batch.
-    ``fp64``: False, True or "auto" (see AUTO_FP64_P3_DOFS)."""
+    ``fp64``: False, True or "auto" (see AUTO_FP64_P3_DOFS).  With
+    ``lane_min_dofs``, systems of at least that many dofs are solved by
+    multigrid PCG on worker streams beside the batch instead."""
     from fealpy_gb300.fem import BilinearForm, LinearForm, ScalarDiffusionIntegrator, ScalarSourceIntegrator
-    from fealpy_gb300.batch import BatchSolver
+    from fealpy_gb300.batch import BatchSolver, solve_with_multigrid_lane
     bs = BatchSolver(len(probs), **bs_kw)
     systems = []
+    lane = []
     for k, (space, kappa, bc, p) in enumerate(probs):
         space._cache.clear()
         bf = BilinearForm(space)
@@ -751,14 +757,20 @@ def batched_step(torch, F, probs, dtype, bs_kw, marks=None, fp64=False, graph=Tr
         lf = LinearForm(space)
         lf.add_integrator(ScalarSourceIntegrator(1.0, q=p + 3))
         A2, F2 = bc.apply(A, lf.assembly())
+        systems.append((A2, F2))
+        if lane_min_dofs is not None and A2.shape[0] >= lane_min_dofs:
+            lane.append((k, A2, F2, RTOL, BATCH_MAXIT))
+            continue
         sys64 = (p == 3 and A2.shape[0] > AUTO_FP64_P3_DOFS) if fp64 == "auto" else bool(fp64)
         bs.add(A2, F2, rtol=RTOL, maxit=BATCH_MAXIT, key=k, fp64=sys64)
-        systems.append((A2, F2))
     if marks is not None:
         e = torch.cuda.Event(enable_timing=True)
         e.record()
         marks.append(e)
-    res = bs.solve_all(graph=graph)
+    if lane:
+        res = solve_with_multigrid_lane(bs, lane, graph=graph)
+    else:
+        res = bs.solve_all(graph=graph)
     return res, systems, bs
 
 
@@ -860,6 +872,28 @@ def batched_record(args):
             "max_true_relres": max(rel), "iters_max": max(iters), "iters_mean": sum(iters) / len(iters),
             "max_rel_err_vs_fp64_sample": max(err), "gpu_launches": (_lib.launch_count() - l0) // args.steps,
             "cpu_baseline": None if args.no_cpu_baseline else cpu_sample_batched(meshes)}
+    # variant: the large systems by multigrid PCG beside the batch (the
+    # configuration asks for one launch for all 256; this shows what the
+    # Jacobi iterations of the largest P3 systems cost)
+    prec = {"mixed": False, "fp64": True, "auto": "auto"}[args.batch_precision]
+    batched_step(torch, F, probs, asm_dtype, kw, fp64=prec, lane_min_dofs=BATCH_LANE_MIN_DOFS)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(args.steps):
+        res_l, systems_l, _ = batched_step(torch, F, probs, asm_dtype, kw, fp64=prec,
+                                           lane_min_dofs=BATCH_LANE_MIN_DOFS, graph=not args.no_graph)
+    e1.record()
+    torch.cuda.synchronize()
+    ms_l = e0.elapsed_time(e1) / args.steps
+    rel_l = []
+    for k, (A2, F2) in enumerate(systems_l):
+        Ad = F.CSRTensor(A2.crow, A2.col, A2.values.to(torch.float64), A2.shape)
+        bd = F2.to(torch.float64)
+        rel_l.append(float(torch.linalg.norm(bd - Ad @ res_l[k].x) / torch.linalg.norm(bd)))
+    n_lane = sum(1 for (A2, _) in systems_l if A2.shape[0] >= BATCH_LANE_MIN_DOFS)
+    line["multigrid_lane"] = {"lane_min_dofs": BATCH_LANE_MIN_DOFS, "lane_systems": n_lane,
+                              "ms_per_step": ms_l, "dof_per_s": gdof / (ms_l / 1e3),
+                              "max_true_relres": max(rel_l), "speedup_vs_one_batch": ms / ms_l}
     return line
 
 

@@ -23,7 +23,7 @@ from . import kernels as K
 from .sparse import CSRTensor
 from ._lib import call, ptr, stream_ptr, workspace, status_word, check_status_word
 
-__all__ = ["GAMGSolver", "AMGPreconditioner"]
+__all__ = ["GAMGSolver", "AMGPreconditioner", "multigrid_solve"]
 
 
 class _Level:
@@ -239,3 +239,29 @@ class AMGPreconditioner:
 
     def apply(self, A: CSRTensor) -> GAMGSolver:
         return GAMGSolver(**self.kw).setup(A)
+
+
+def multigrid_solve(A, b, rtol: float = 1e-10, maxit: int = 100000, fp64: bool = False):
+    """One system by multigrid PCG on the current stream (the multigrid lane
+    of the serving loop and of the batched solve): the AMG hierarchy (FP32
+    V-cycle, FP64 with ``fp64``), PCG on the iterated residual, restarted
+    from the iterate on the true residual b - A x while that is above
+    ``rtol`` and still halves (the iterated residual drifts below the true
+    one on ill-conditioned systems).  Returns (x with the smallest true
+    residual, iterations, stop reason, its true relative residual)."""
+    from .solver import cg
+    M = GAMGSolver(vcycle_f32=not fp64).setup(A)
+    bnorm = float(torch.linalg.norm(b))
+    x, niter, reason = None, 0, 0
+    best_x, best_r = None, float("inf")
+    for _ in range(4):
+        x, inf = cg(A, b, x0=x, M=M, atol=0.0, rtol=rtol, maxit=maxit, returninfo=True, stop="residual")
+        niter += int(inf["niter"])
+        reason = int(inf["reason"])
+        r_new = float(torch.linalg.norm(b - A @ x)) / bnorm if bnorm > 0 else 0.0
+        improved = r_new < 0.5 * best_r
+        if r_new < best_r:
+            best_x, best_r = x, r_new
+        if r_new <= rtol or not improved:
+            break
+    return best_x, niter, reason, best_r

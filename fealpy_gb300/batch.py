@@ -24,7 +24,7 @@ from . import kernels as K
 from ._lib import call, ptr, stream_ptr
 from .sparse import CSRTensor
 
-__all__ = ["BatchSolver", "BatchResult"]
+__all__ = ["BatchSolver", "BatchResult", "solve_with_multigrid_lane"]
 
 
 class BatchResult:
@@ -308,3 +308,38 @@ def autotune(systems, candidates=((4, 256), (8, 256), (16, 256), (8, 512), (16, 
         times[(spt, thr)] = bs.spmv_time_us()
         del bs
     return times
+
+
+def solve_with_multigrid_lane(batch: BatchSolver, lane_systems, *, workers: int = 4, fp64: bool = False,
+                              graph: bool = True) -> Dict[object, BatchResult]:
+    """Solve the systems already added to ``batch`` and, at the same time, the
+    ``lane_systems`` ([(key, A, b, rtol, maxit)]) by multigrid PCG
+    (:func:`fealpy_gb300.amg.multigrid_solve`) on ``workers`` threads, each
+    with its own CUDA stream.  Large systems, whose Jacobi iterations would
+    set the batch's makespan, go to the lane.  Returns every result by key
+    (lane results: ``reason`` from PCG, ``n_updates`` 0).  Call with the
+    current stream idle of other work on the lane systems' data."""
+    import threading
+    from concurrent.futures import ThreadPoolExecutor
+    from .amg import multigrid_solve
+    local = threading.local()
+    ready = torch.cuda.Event()
+    ready.record(torch.cuda.current_stream(batch.device))
+
+    def job(key, A, b, rtol, maxit):
+        st = getattr(local, "stream", None)
+        if st is None:
+            st = local.stream = torch.cuda.Stream(batch.device)
+        with torch.cuda.stream(st):
+            st.wait_event(ready)
+            x, niter, reason, relres = multigrid_solve(A, b, rtol, maxit, fp64)
+            st.synchronize()
+        return BatchResult(key, x, niter, relres, reason, 0)
+
+    with ThreadPoolExecutor(max(int(workers), 1)) as pool:
+        futs = [pool.submit(job, *s) for s in lane_systems]
+        out = batch.solve_all(graph=graph) if batch.active() else {}
+        for f in futs:
+            r = f.result()
+            out[r.key] = r
+    return out

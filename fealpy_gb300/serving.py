@@ -24,6 +24,7 @@ from typing import Callable, Dict, List, Optional
 import numpy as np
 import torch
 
+from .amg import multigrid_solve
 from .batch import BatchSolver
 
 __all__ = ["SolveServer", "poisson_request_problem", "resident_estimate", "multigrid_solve"]
@@ -90,30 +91,6 @@ def poisson_request_problem(req: dict, device, dtype=torch.float64, inputs: Opti
     lf = LinearForm(space)
     lf.add_integrator(ScalarSourceIntegrator(1.0, q=p + 2))
     return DirichletBC(space, gd=0.0).apply(bf.assembly(dtype=dtype), lf.assembly())
-
-
-def multigrid_solve(A, b, rtol: float = 1e-10, maxit: int = 100000, fp64: bool = False):
-    """The multigrid lane's solve of one system on the current stream: the
-    AMG hierarchy (FP32 V-cycle, FP64 with ``fp64``), PCG on the iterated
-    residual, restarted from the iterate on the true residual b - A x while
-    that is above ``rtol`` and still halves (the iterated residual drifts
-    below the true one on ill-conditioned systems).  Returns (x, iterations,
-    stop reason, true relative residual)."""
-    from .amg import GAMGSolver
-    from .solver import cg
-    M = GAMGSolver(vcycle_f32=not fp64).setup(A)
-    bnorm = float(torch.linalg.norm(b))
-    x, niter, reason, relres = None, 0, 0, float("inf")
-    for _ in range(4):
-        x, inf = cg(A, b, x0=x, M=M, atol=0.0, rtol=rtol, maxit=maxit, returninfo=True, stop="residual")
-        niter += int(inf["niter"])
-        reason = int(inf["reason"])
-        r_new = float(torch.linalg.norm(b - A @ x)) / bnorm if bnorm > 0 else 0.0
-        improved = r_new < 0.5 * relres
-        relres = min(relres, r_new)
-        if r_new <= rtol or not improved:
-            break
-    return x, niter, reason, relres
 
 
 class SolveServer:

@@ -190,3 +190,34 @@ def test_cg_mixed_continues_in_fp64_after_stagnation():
     x, info = F.cg_mixed(L, lb, rtol=RTOL, maxit=200000, returninfo=True)
     assert info["fp64_iterations"] > 0, info
     assert info["reason"] in (2, 7) and _residual(L, lb, x) <= 2 * RTOL, info
+
+
+def test_batch_with_multigrid_lane():
+    """The two largest systems by multigrid PCG beside the batch: every result
+    at 1e-10 against the oracle's solution; a lane result equals the same
+    system's multigrid solve alone (bit for bit)."""
+    dev = cuda()
+    from fealpy_gb300.batch import BatchSolver, solve_with_multigrid_lane
+    from fealpy_gb300.amg import multigrid_solve
+    inputs = []
+    systems = _systems(dev, inputs)
+    big = sorted(range(len(systems)), key=lambda k: systems[k][0].shape[0])[-2:]
+    bs = BatchSolver(8, slices_per_tile=4, rows_per_tile=512)
+    lane = []
+    for k, (A, b) in enumerate(systems):
+        if k in big:
+            lane.append((k, A, b, RTOL, 100000))
+        else:
+            bs.add(A, b, rtol=RTOL, key=k)
+    res = solve_with_multigrid_lane(bs, lane, workers=2)
+    assert sorted(res) == list(range(len(systems)))
+    for k, (A, b) in enumerate(systems):
+        rel = _residual(A, b, res[k].x)
+        assert rel <= RTOL * 1.0001, (k, rel)
+        xo = _oracle_solution(inputs[k])
+        erro = float(np.max(np.abs(res[k].x.cpu().numpy() - xo)) / np.max(np.abs(xo)))
+        assert erro < 1e-8, (k, erro)
+    for k in big:
+        A, b = systems[k]
+        x, niter, _, _ = multigrid_solve(A, b, RTOL, 100000)
+        assert torch.equal(x, res[k].x) and niter == res[k].niter
