@@ -937,13 +937,17 @@ def elasticity_record(args):
         A2, F2 = bc.apply(A, lf.assembly())
         if mode == "mixed":
             x, info = F.cg_mixed(A2, F2, rtol=rtol, maxit=200000, returninfo=True, graph=not args.no_graph)
+        elif mode == "amg":
+            from fealpy_gb300.amg import multigrid_solve
+            x, niter, reason, relres = multigrid_solve(A2, F2, rtol, 200000)
+            info = {"niter": niter, "reason": reason, "fp64_iterations": 0}
         else:
             x, info = F.cg(A2, F2, M=F.JacobiPreconditioner().apply(A2), atol=0.0, rtol=rtol, maxit=200000,
                            returninfo=True, stop="residual", graph=not args.no_graph)
         return x, info, A2, F2
 
     res = {}
-    for mode in ("mixed", "fp64"):
+    for mode in ("mixed", "fp64", "amg"):
         for _ in range(args.warmup):
             step(mode)
         torch.cuda.synchronize()
@@ -959,7 +963,7 @@ def elasticity_record(args):
                      "true_relres": float(torch.linalg.norm(r) / torch.linalg.norm(F2)),
                      "fp64_iterations": info.get("fp64_iterations", info["niter"] if mode == "fp64" else 0),
                      "x": x, "nnz": A2.nnz, "A2": A2, "F2": F2,
-                     "sell": A2._sell.cols}
+                     "sell": A2._sell.cols if getattr(A2, "_sell", None) is not None else None}
     err = float((res["mixed"]["x"] - res["fp64"]["x"]).abs().max() / res["fp64"]["x"].abs().max())
     # roofline of the dominant kernel, the FP32 SpMV of the FP32-refined
     # iterations, from one more (host-polled) solve with CUDA events around
@@ -969,8 +973,10 @@ def elasticity_record(args):
     # once); 4-byte columns: nnz (4 + s) + n (8 + 2 s)
     A2 = res["mixed"].pop("A2")
     F2 = res["mixed"].pop("F2")
-    res["fp64"].pop("A2", None)
-    res["fp64"].pop("F2", None)
+    for m in ("fp64", "amg"):
+        res[m].pop("A2", None)
+        res[m].pop("F2", None)
+    err_amg = float((res["amg"]["x"] - res["fp64"]["x"]).abs().max() / res["fp64"]["x"].abs().max())
     _, pinfo = F.cg_mixed(A2, F2, rtol=rtol, maxit=200000, returninfo=True, profile=True)
     S = A2._sell
     peak, peak_kind = read_peaks()
@@ -993,6 +999,9 @@ def elasticity_record(args):
             "config": {"workload": f"LinearElasticityIntegrator P1 TetrahedronMesh box {n}^3 (C5)",
                        "cells": int(cell_np.shape[0]), "gdof": gdof, "rtol": rtol, "quadrature": 4},
             "fp32_refined": res["mixed"], "fp64": res["fp64"], "max_rel_err_vs_fp64": err,
+            "multigrid": dict(res["amg"], preconditioner="aggregation AMG V-cycle (FP32), FP64 PCG",
+                              max_rel_err_vs_fp64=err_amg,
+                              speedup_vs_fp32_refined=res["mixed"]["ms_per_step"] / res["amg"]["ms_per_step"]),
             "speedup_fp32_refined_vs_fp64": res["fp64"]["ms_per_step"] / res["mixed"]["ms_per_step"],
             "roofline": roof}
     return line

@@ -74,12 +74,14 @@ class GAMGSolver:
     V-cycle runs in FP32 on FP32 copies of the level matrices; the PCG
     operator and its vectors stay FP64), ``sell_min_rows`` (levels of at
     least this many rows smooth on a SELL-32 copy, 15-bit column steps where
-    the columns ascend, instead of the CSR arrays; in either precision)."""
+    the columns ascend, instead of the CSR arrays; in either precision),
+    ``block_size`` (aggregate whole nodes of a vector space with that many
+    interleaved components, as elasticity matrices need)."""
 
     def __init__(self, theta: float = 0.0, csize: int = 300, ctype: str = "A", itype: str = "T", ptype: str = "V",
                  sstep: int = 3, isolver: str = "CG", maxit: int = 200, csolver: str = "chebyshev",
                  rtol: float = 1e-8, atol: float = 1e-8, omega: float = 1.7, cdeg: int = 16, max_levels: int = 10,
-                 vcycle_f32: bool = True, sell_min_rows: int = 1 << 16):
+                 vcycle_f32: bool = True, sell_min_rows: int = 1 << 16, block_size: int = 1):
         if ptype != "V":
             raise NotImplementedError("the GB300 multigrid provides V-cycles")
         if isolver not in ("CG", "MG"):
@@ -89,11 +91,63 @@ class GAMGSolver:
         self.omega, self.cdeg, self.max_levels = float(omega), int(cdeg), int(max_levels)
         self.vcycle_f32 = bool(vcycle_f32)
         self.sell_min_rows = int(sell_min_rows)
+        self.block_size = max(int(block_size), 1)
         self.levels: List[_Level] = []
         self._desc = None
         self.A = None
 
     # ------------------------------------------------------------ set-up
+    def _aggregate(self, lev: "_Level", dev, st, s):
+        """(agg, number of aggregates, 1/a_ii, Chebyshev bound) of a level."""
+        lib = _lib.lib()
+        n = lev.n
+        ws = workspace(lib.fgb_amg_setup_workspace_bytes(n), dev)
+        agg = torch.empty(n, dtype=torch.int32, device=dev)
+        dinv = torch.empty(n, dtype=torch.float64, device=dev)
+        nagg = ctypes.c_int64(0)
+        lmax = ctypes.c_double(0.0)
+        call("fgb_amg_aggregate", n, ptr(lev.indptr), ptr(lev.indices), ptr(lev.values), self.theta, ptr(agg),
+             ctypes.byref(nagg), ptr(dinv), ctypes.byref(lmax), ptr(st), ptr(ws), ws.numel(), s)
+        check_status_word("multigrid set-up (the matrix needs a positive diagonal)", st)
+        return agg, int(nagg.value), dinv, float(lmax.value)
+
+    def _coarse(self, indptr, indices, values, agg, nc, dev, st, s):
+        """P^T A P for the aggregate indicator of ``agg``: (member_ptr, members,
+        coarse indptr, indices, values)."""
+        lib = _lib.lib()
+        n = indptr.numel() - 1
+        member_ptr = torch.empty(nc + 1, dtype=torch.int64, device=dev)
+        members = torch.empty(max(n, 1), dtype=torch.int32, device=dev)
+        cptr = torch.empty(nc + 1, dtype=torch.int64, device=dev)
+        cws = workspace(lib.fgb_amg_coarse_workspace_bytes(n, nc), dev)
+        nnz = ctypes.c_int64(0)
+        call("fgb_amg_coarse_count", n, ptr(indptr), ptr(indices), ptr(values), ptr(agg), nc, ptr(member_ptr),
+             ptr(members), ptr(cptr), ctypes.byref(nnz), ptr(st), ptr(cws), cws.numel(), s)
+        ccol = torch.empty(max(int(nnz.value), 1), dtype=torch.int32, device=dev)
+        cval = torch.empty(max(int(nnz.value), 1), dtype=torch.float64, device=dev)
+        call("fgb_amg_coarse_fill", n, ptr(indptr), ptr(indices), ptr(values), ptr(agg), nc, ptr(member_ptr),
+             ptr(members), ptr(cptr), ptr(ccol), ptr(cval), ptr(st), ptr(cws), cws.numel(), s)
+        check_status_word("multigrid coarse matrix (aggregate rows above the candidate capacity)", st)
+        return member_ptr, members, cptr, ccol[: int(nnz.value)], cval[: int(nnz.value)]
+
+    def _block_aggregate(self, lev: "_Level", dev, st, s):
+        """Aggregates of whole nodes for a matrix of ``block_size`` interleaved
+        components (dof = block_size * node + component): the node graph is
+        P_b^T |A| P_b (P_b groups each node's dofs), its aggregates expand to
+        one coarse dof per (aggregate, component), so every level keeps the
+        interleaved layout."""
+        b = self.block_size
+        n = lev.n
+        _, _, dinv, lmax = self._aggregate(lev, dev, st, s)  # 1/a_ii and the bound of the dof matrix
+        dof = torch.arange(n, device=dev, dtype=torch.int32)
+        node = dof // b
+        absval = lev.values.abs()
+        _, _, nptr, ncol, nval = self._coarse(lev.indptr, lev.indices, absval, node, n // b, dev, st, s)
+        agg_n, nagg, _, _ = self._aggregate(_Level(nptr, ncol, nval), dev, st, s)
+        an = agg_n[node.long()]
+        agg = torch.where(an >= 0, an * b + dof % b, an).to(torch.int32).contiguous()
+        return agg, nagg * b, dinv, lmax
+
     def setup(self, A: CSRTensor, P=None, R=None, mesh=None, space=None, cdegree=None):
         """Build the hierarchy of ``A`` (FP64 CSR on the device)."""
         if P is not None or R is not None or mesh is not None or space is not None:
@@ -104,7 +158,6 @@ class GAMGSolver:
         if dev.type != "cuda":
             raise ValueError("GAMGSolver runs on the GPU only")
         self.A = A
-        lib = _lib.lib()
         s = stream_ptr(dev)
         st = status_word(dev)
         lev = _Level(A.crow.contiguous(), A.col.to(torch.int32).contiguous(),
@@ -112,16 +165,10 @@ class GAMGSolver:
         self.levels = []
         while True:
             n = lev.n
-            ws = workspace(lib.fgb_amg_setup_workspace_bytes(n), dev)
-            lev.agg = torch.empty(n, dtype=torch.int32, device=dev)
-            lev.dinv = torch.empty(n, dtype=torch.float64, device=dev)
-            nagg = ctypes.c_int64(0)
-            lmax = ctypes.c_double(0.0)
-            call("fgb_amg_aggregate", n, ptr(lev.indptr), ptr(lev.indices), ptr(lev.values), self.theta, ptr(lev.agg),
-                 ctypes.byref(nagg), ptr(lev.dinv), ctypes.byref(lmax), ptr(st), ptr(ws), ws.numel(), s)
-            check_status_word("multigrid set-up (the matrix needs a positive diagonal)", st)
-            lev.lmax = float(lmax.value)
-            nc = int(nagg.value)
+            if self.block_size > 1 and n % self.block_size == 0:
+                lev.agg, nc, lev.dinv, lev.lmax = self._block_aggregate(lev, dev, st, s)
+            else:
+                lev.agg, nc, lev.dinv, lev.lmax = self._aggregate(lev, dev, st, s)
             self.levels.append(lev)
             # a level that shrinks by less than half adds sweeps and no
             # convergence: the current one is then the coarsest
@@ -130,21 +177,9 @@ class GAMGSolver:
                 lev.agg = None
                 break
             lev.n_coarse = nc
-            lev.member_ptr = torch.empty(nc + 1, dtype=torch.int64, device=dev)
-            lev.members = torch.empty(max(n, 1), dtype=torch.int32, device=dev)
-            cptr = torch.empty(nc + 1, dtype=torch.int64, device=dev)
-            cws = workspace(lib.fgb_amg_coarse_workspace_bytes(n, nc), dev)
-            nnz = ctypes.c_int64(0)
-            call("fgb_amg_coarse_count", n, ptr(lev.indptr), ptr(lev.indices), ptr(lev.values), ptr(lev.agg), nc,
-                 ptr(lev.member_ptr), ptr(lev.members), ptr(cptr), ctypes.byref(nnz), ptr(st), ptr(cws), cws.numel(),
-                 s)
-            ccol = torch.empty(max(int(nnz.value), 1), dtype=torch.int32, device=dev)
-            cval = torch.empty(max(int(nnz.value), 1), dtype=torch.float64, device=dev)
-            call("fgb_amg_coarse_fill", n, ptr(lev.indptr), ptr(lev.indices), ptr(lev.values), ptr(lev.agg), nc,
-                 ptr(lev.member_ptr), ptr(lev.members), ptr(cptr), ptr(ccol), ptr(cval), ptr(st), ptr(cws),
-                 cws.numel(), s)
-            check_status_word("multigrid coarse matrix (aggregate rows above the candidate capacity)", st)
-            lev = _Level(cptr, ccol[: int(nnz.value)], cval[: int(nnz.value)])
+            lev.member_ptr, lev.members, cptr, ccol, cval = self._coarse(lev.indptr, lev.indices, lev.values,
+                                                                         lev.agg, nc, dev, st, s)
+            lev = _Level(cptr, ccol, cval)
         for k, L in enumerate(self.levels):
             L.values32 = L.values.to(torch.float32) if self.vcycle_f32 else None
             L.dinv32 = L.dinv.to(torch.float32) if self.vcycle_f32 else None
@@ -241,16 +276,20 @@ class AMGPreconditioner:
         return GAMGSolver(**self.kw).setup(A)
 
 
-def multigrid_solve(A, b, rtol: float = 1e-10, maxit: int = 100000, fp64: bool = False):
+def multigrid_solve(A, b, rtol: float = 1e-10, maxit: int = 100000, fp64: bool = False, block_size: int = 0):
     """One system by multigrid PCG on the current stream (the multigrid lane
     of the serving loop and of the batched solve): the AMG hierarchy (FP32
     V-cycle, FP64 with ``fp64``), PCG on the iterated residual, restarted
     from the iterate on the true residual b - A x while that is above
     ``rtol`` and still halves (the iterated residual drifts below the true
-    one on ill-conditioned systems).  Returns (x with the smallest true
-    residual, iterations, stop reason, its true relative residual)."""
+    one on ill-conditioned systems).  ``block_size`` 0: node blocks of 3
+    when the matrix is marked as three interleaved components, else none.
+    Returns (x with the smallest true residual, iterations, stop reason, its
+    true relative residual)."""
     from .solver import cg
-    M = GAMGSolver(vcycle_f32=not fp64).setup(A)
+    if block_size == 0:
+        block_size = 3 if getattr(A, "node_block", 1) == 3 else 1
+    M = GAMGSolver(vcycle_f32=not fp64, block_size=block_size).setup(A)
     bnorm = float(torch.linalg.norm(b))
     x, niter, reason = None, 0, 0
     best_x, best_r = None, float("inf")

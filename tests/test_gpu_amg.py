@@ -179,3 +179,12 @@ def test_amg_elasticity_c5_law(golden_dir):
     x, info = F.cg(A, b, M=F.AMGPreconditioner().apply(A), atol=1e-30, rtol=1e-10, returninfo=True)
     assert info["reason"] == 2 and info["niter"] < int(z["niter"]), (info["niter"], int(z["niter"]))
     assert rel(x, z["uh"]) < 1e-8
+    # aggregates of whole nodes (three interleaved components): every level
+    # keeps the interleaved layout, and the solve reaches the same solution
+    M3 = F.GAMGSolver(block_size=3).setup(A)
+    for L in M3.levels[:-1]:
+        agg = L.agg.cpu().numpy().reshape(-1, 3)
+        ok = agg[:, 0] >= 0
+        assert np.array_equal(agg[ok], (agg[ok, :1] // 3) * 3 + np.arange(3)) and np.all(agg[~ok] == -1)
+    x3, info3 = F.cg(A, b, M=M3, atol=1e-30, rtol=1e-10, returninfo=True)
+    assert info3["reason"] == 2 and rel(x3, z["uh"]) < 1e-8
