@@ -900,6 +900,51 @@ def batched_record(args):
 # ---------------------------------------------------------------------------
 # serving workload: Poisson arrivals, continuous batching under a memory budget
 # ---------------------------------------------------------------------------
+def run_amg(args):
+    """The multigrid on the C2 system at ``--n``: one set-up in the NVTX range
+    "setup" (after a warm-up one), three V-cycles in the range "vcycles" (for a
+    profiler's launch list: the PCG loop runs inside a conditional graph whose
+    kernel nodes a profiler does not list), then set-up, V-cycle and PCG times
+    by CUDA events.  Prints one JSON line."""
+    import torch
+    import fealpy_gb300 as F
+    from fealpy_gb300.workloads import diffusion_mass_tet_box
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    node_np, cell_np, kappa_np = diffusion_mass_tet_box(args.n)
+    mesh, space, kappa, bc = build_problem(torch, F, node_np, cell_np, kappa_np, dev)
+    _, _, A2, F2 = solve_step(torch, F, space, kappa, bc, "fp64")
+    F.GAMGSolver().setup(A2)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push("setup")
+    M = F.GAMGSolver().setup(A2)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
+    M.vcycle(F2)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push("vcycles")
+    for _ in range(3):
+        M.vcycle(F2)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
+    ev[0].record()
+    M = F.GAMGSolver().setup(A2)
+    ev[1].record()
+    ev[2].record()
+    for _ in range(10):
+        M.vcycle(F2)
+    ev[3].record()
+    ev[4].record()
+    x, info = F.cg(A2, F2, M=M, atol=0.0, rtol=RTOL, maxit=MAXIT, returninfo=True, stop="residual")
+    ev[5].record()
+    torch.cuda.synchronize()
+    print(json.dumps({"workload": f"multigrid on the P2 diffusion+mass tet box {args.n}^3", "rows": A2.shape[0],
+                      "levels_rows": [L.n for L in M.levels], "setup_ms": ev[0].elapsed_time(ev[1]),
+                      "vcycle_ms": ev[2].elapsed_time(ev[3]) / 10, "pcg_ms": ev[4].elapsed_time(ev[5]),
+                      "pcg_iters": info["niter"]}), flush=True)
+
+
 def run_elasticity(args):
     print(json.dumps(elasticity_record(args)), flush=True)
 
@@ -1104,7 +1149,7 @@ def main():
     ap.add_argument("--no-graph", action="store_true",
                     help="host-polled solver loop instead of the CUDA-graph loop (profiling runs: a profiler "
                          "cannot capture kernels inside a graph that has conditional nodes)")
-    ap.add_argument("--workload", choices=["c2", "batched", "serving", "elasticity"], default="c2",
+    ap.add_argument("--workload", choices=["c2", "batched", "serving", "elasticity", "amg"], default="c2",
                     help="c2: the P2 tet box (default, the headline line); batched: 256 uneven triangle meshes; "
                          "serving: the request stream; elasticity: P1 vector elasticity on a tet box")
     ap.add_argument("--elast-n", type=int, default=128)
@@ -1132,6 +1177,9 @@ def main():
         return
     if args.workload == "elasticity" and args.impl == "ours":
         run_elasticity(args)
+        return
+    if args.workload == "amg" and args.impl == "ours":
+        run_amg(args)
         return
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
