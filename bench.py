@@ -738,7 +738,23 @@ AUTO_FP64_P3_DOFS = 100_000
 BATCH_LANE_MIN_DOFS = 100_000
 
 
-def batched_step(torch, F, probs, dtype, bs_kw, marks=None, fp64=False, graph=True, lane_min_dofs=None):
+def batched_assembler(probs):
+    """The batched assembly of the problems (forms built once: diffusion with
+    the checkerboard coefficient, quadrature p + 3, f = 1, u = 0)."""
+    from fealpy_gb300.fem import BilinearForm, LinearForm, ScalarDiffusionIntegrator, ScalarSourceIntegrator
+    from fealpy_gb300.fem.batch_assembly import BatchAssembler
+    systems = []
+    for space, kappa, bc, p in probs:
+        bf = BilinearForm(space)
+        bf.add_integrator(ScalarDiffusionIntegrator(coef=kappa, q=p + 3))
+        lf = LinearForm(space)
+        lf.add_integrator(ScalarSourceIntegrator(1.0, q=p + 3))
+        systems.append((bf, lf, bc))
+    return BatchAssembler(systems)
+
+
+def batched_step(torch, F, probs, dtype, bs_kw, marks=None, fp64=False, graph=True, lane_min_dofs=None,
+                 assembler=None, stats=None):
     """Assemble every problem (diffusion with the checkerboard coefficient,
     quadrature p + 3, f = 1, u = 0) and solve all of them in one batch.
     ``fp64``: False, True or "auto" (see AUTO_FP64_P3_DOFS).  With
@@ -749,14 +765,29 @@ def batched_step(torch, F, probs, dtype, bs_kw, marks=None, fp64=False, graph=Tr
     bs = BatchSolver(len(probs), **bs_kw)
     systems = []
     lane = []
+    if assembler is not None:
+        # every mesh of a degree assembled together: a few launches per degree
+        from fealpy_gb300 import _lib as L
+        l0 = L.launch_count()
+        ea, eb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ea.record()
+        built = assembler.assemble(dtype)
+        eb.record()
+        if stats is not None:
+            eb.synchronize()
+            stats["assembly_launches"] = L.launch_count() - l0
+            stats["assembly_ms"] = ea.elapsed_time(eb)
+    else:
+        built = []
+        for k, (space, kappa, bc, p) in enumerate(probs):
+            space._cache.clear()
+            bf = BilinearForm(space)
+            bf.add_integrator(ScalarDiffusionIntegrator(coef=kappa, q=p + 3))
+            lf = LinearForm(space)
+            lf.add_integrator(ScalarSourceIntegrator(1.0, q=p + 3))
+            built.append(bc.apply(bf.assembly(dtype=dtype), lf.assembly()))
     for k, (space, kappa, bc, p) in enumerate(probs):
-        space._cache.clear()
-        bf = BilinearForm(space)
-        bf.add_integrator(ScalarDiffusionIntegrator(coef=kappa, q=p + 3))
-        A = bf.assembly(dtype=dtype)
-        lf = LinearForm(space)
-        lf.add_integrator(ScalarSourceIntegrator(1.0, q=p + 3))
-        A2, F2 = bc.apply(A, lf.assembly())
+        A2, F2 = built[k]
         systems.append((A2, F2))
         if lane_min_dofs is not None and A2.shape[0] >= lane_min_dofs:
             lane.append((k, A2, F2, RTOL, BATCH_MAXIT))
@@ -813,27 +844,29 @@ def batched_record(args):
     asm_dtype = torch.float64
     meshes = batched_tri_meshes(args.batch_count)
     probs = batched_setup(torch, F, meshes, dev)
+    asm = batched_assembler(probs)
     gdof = sum(pr[0].number_of_global_dofs() for pr in probs)
     # tile capacity for the finest candidate split (4 slices of 32 rows per
     # tile) plus one partial tile per system
     kw = dict(max_slice_tiles=gdof // 128 + 2 * len(probs) + 1024, max_row_tiles=1 << 18)
     # autotune the slice tiling on the first step's systems
-    res, systems, _ = batched_step(torch, F, probs, asm_dtype, kw)
+    res, systems, _ = batched_step(torch, F, probs, asm_dtype, kw, assembler=asm)
     times = autotune(systems[:64], device=dev, **kw)
     spt, thr = min(times, key=times.get)
     kw.update(slices_per_tile=spt, slice_threads=thr)
     for _ in range(max(args.warmup - 1, 0)):
-        batched_step(torch, F, probs, asm_dtype, kw)
+        batched_step(torch, F, probs, asm_dtype, kw, assembler=asm)
     torch.cuda.synchronize()
     l0 = _lib.launch_count()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     marks = []
+    asm_stats = {}
     e0.record()
     torch.cuda.nvtx.range_push("timed_batched")
     for _ in range(args.steps):
         prec = {"mixed": False, "fp64": True, "auto": "auto"}[args.batch_precision]
         res, systems, bs = batched_step(torch, F, probs, asm_dtype, kw, marks, fp64=prec,
-                                        graph=not args.no_graph)
+                                        graph=not args.no_graph, assembler=asm, stats=asm_stats)
     e1.record()
     torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize()
@@ -867,6 +900,9 @@ def batched_record(args):
                        "gdof": gdof, "rtol": RTOL, "autotune_us": {f"{a}x{b}": t for (a, b), t in times.items()},
                        "slices_per_tile": spt, "slice_threads": thr},
             "solve_ms": solve_ms, "assembly_ms": ms - solve_ms, "graph": bs.used_graph,
+            "batched_assembly": {"ms": asm_stats.get("assembly_ms"), "launches": asm_stats.get("assembly_launches"),
+                                 "what": "pattern, factors, values, right-hand side, Dirichlet and split of all "
+                                         "256 systems, grouped by degree (fem.batch_assembly.BatchAssembler)"},
             "fp64_continuations": bs.fallbacks,
             "fp64_iterations": sum(getattr(res[k], "fp64_iterations", 0) for k in res),
             "max_true_relres": max(rel), "iters_max": max(iters), "iters_mean": sum(iters) / len(iters),
@@ -876,12 +912,13 @@ def batched_record(args):
     # configuration asks for one launch for all 256; this shows what the
     # Jacobi iterations of the largest P3 systems cost)
     prec = {"mixed": False, "fp64": True, "auto": "auto"}[args.batch_precision]
-    batched_step(torch, F, probs, asm_dtype, kw, fp64=prec, lane_min_dofs=BATCH_LANE_MIN_DOFS)
+    batched_step(torch, F, probs, asm_dtype, kw, fp64=prec, lane_min_dofs=BATCH_LANE_MIN_DOFS, assembler=asm)
     torch.cuda.synchronize()
     e0.record()
     for _ in range(args.steps):
         res_l, systems_l, _ = batched_step(torch, F, probs, asm_dtype, kw, fp64=prec,
-                                           lane_min_dofs=BATCH_LANE_MIN_DOFS, graph=not args.no_graph)
+                                           lane_min_dofs=BATCH_LANE_MIN_DOFS, graph=not args.no_graph,
+                                           assembler=asm)
     e1.record()
     torch.cuda.synchronize()
     ms_l = e0.elapsed_time(e1) / args.steps

@@ -275,6 +275,17 @@ int32_t fgb_cell_apply(int32_t dtype, int64_t n_cell, int32_t ldof, const int32_
                        int32_t n_table, const double* tables_host, const void* tables,
                        const void* factors, const void* x, void* ycell, void* stream);
 
+/* Split of a block-diagonal CSR of many systems assembled together (system s
+ * owns rows and columns [row_off[s], row_off[s+1]), n_rows = row_off[n_sys]):
+ * columns rebased in place to each system's numbering (a column outside its
+ * system's range sets FGB_ERR_PATTERN in *status), and per system a row
+ * pointer starting at 0 in indptr_out (n_rows + n_sys entries, system s at
+ * offset row_off[s] + s).  Each system's entries stay a contiguous range of
+ * the union's indices and values. */
+int32_t fgb_csr_split_blocks(int32_t n_sys, const int64_t* row_off, const int64_t* indptr,
+                             int32_t* indices, int64_t* indptr_out, int64_t n_rows, int32_t* status,
+                             void* stream);
+
 /* ---- Dirichlet boundary conditions ------------------------------------- */
 
 /* DirichletBC.apply (fealpy/fem/dirichlet_bc.py:101-229): given is_bd (uint8,
