@@ -107,8 +107,10 @@ class BatchAssembler:
         space0 = self.systems[members[0]][0].space
         q = sig[-1]
         bcs, ws = mesh0.quadrature_formula(q).get_quadrature_points_and_weights()
-        g.phi = torch.as_tensor(sx.shape_function(bcs, space0.p), device=dev)
-        g.w = torch.as_tensor(ws, device=dev)
+        wphi = ws[:, None] * sx.shape_function(bcs, space0.p)
+        g.wphi = torch.as_tensor(wphi, dtype=torch.float64, device=dev).contiguous()
+        g.sv = torch.as_tensor(wphi.sum(axis=0), dtype=torch.float64, device=dev)
+        g.ldof = space0.number_of_local_dofs()
         g.cell_count = [self.systems[k][0].space.mesh.number_of_cells() for k in members]
         return g
 
@@ -158,12 +160,12 @@ class BatchAssembler:
             tab = torch.as_tensor(tabs_all[a:a + _lib.FGB_MAX_CHANNELS], dtype=dtype, device=dev)
             values, _ = K.assemble_scalar(adj_ptr, adj, g.c2d, tab, fac_mat[:, a:a + _lib.FGB_MAX_CHANNELS].contiguous(),
                                           indptr, indices, status=status, accumulate_into=values)
-        # right-hand side: (|T| sum_q w_q phi_i) * f per cell, the source
-        # integrator's own contraction, gathered per dof
+        # right-hand side: |T| (sum_q w_q phi_i) f per (cell, local dof),
+        # formed and summed per dof as the single-system LinearForm does (the
+        # source of every member as a per-cell value: the same products)
         fcell = torch.repeat_interleave(torch.as_tensor(srcs, dtype=torch.float64, device=dev),
                                         torch.as_tensor(g.cell_count, device=dev))
-        local = torch.einsum("c,q,qi->ci", cm, g.w, g.phi) * fcell[:, None]
-        F = K.gather_sum(adj_ptr, adj, local.contiguous())
+        F = K.source_gather(adj_ptr, adj, g.ldof, cm.contiguous(), 1, 0.0, fcell, g.wphi, g.sv)
         _lib.check_status_word("batched assembly", status)
         uh = torch.zeros(g.n, dtype=values.dtype, device=dev)
         bptr, bidx, bval, bF = K.dirichlet_apply(indptr, indices, values, g.is_bd, F.to(values.dtype), uh)

@@ -13,7 +13,7 @@ import torch
 from ..sparse import CSRTensor
 from .. import _lib
 from .. import kernels as K
-from .integrators import (ElasticityPlan, GroupIntegrator, Integrator, ScalarPlan)
+from .integrators import (ElasticityPlan, GroupIntegrator, Integrator, ScalarPlan, ScalarSourceIntegrator)
 
 __all__ = ["BilinearForm", "LinearForm", "symbolic_structure"]
 
@@ -254,7 +254,8 @@ class BilinearForm(_Form):
 
 
 class LinearForm(_Form):
-    """Right-hand-side vector: cell vectors from the source integrators, summed
+    """Right-hand-side vector: scalar sources formed and summed per dof in one
+    kernel (``fgb_source_gather``); other integrators' cell vectors summed
     into dofs by the deterministic adjacency gather."""
 
     def __init__(self, *space, batch_size: int = 0):
@@ -264,40 +265,58 @@ class LinearForm(_Form):
     def assembly(self, *, format="dense") -> torch.Tensor:
         space = self.space
         mesh = space.scalar_space.mesh if hasattr(space, "scalar_space") else space.mesh
-        # local vectors grouped by the cells they integrate over (all cells,
-        # or a sub-region): one dof gather per group
-        groups = []
+        n = space.number_of_global_dofs()
+        out = None
+        # scalar sources: formed and gathered per dof in one kernel each
+        # (fgb_source_gather), no cell-vector array
+        rest = []
         for it in self.integrators.values():
             ints = it.ints if isinstance(it, GroupIntegrator) else [it]
             for i in ints:
-                v = i.assembly(space)
-                cells = i.cell_selection(mesh)
-                for g in groups:
-                    if (g[0] is None and cells is None) or (g[0] is not None and cells is not None and
-                                                           g[0].shape == cells.shape and torch.equal(g[0], cells)):
-                        g[1] = g[1] + v
-                        break
+                if isinstance(i, ScalarSourceIntegrator) and not hasattr(space, "scalar_space"):
+                    cells, cm, mode, fs, f, wphi, sv = i.source_data(space)
+                    adj_ptr, adj = self._adjacency(space, cells)
+                    out = K.source_gather(adj_ptr, adj, space.number_of_local_dofs(), cm, mode, fs, f, wphi, sv,
+                                          out=out)
                 else:
-                    groups.append([cells, v])
-        if not groups:
-            raise RuntimeError("no integrator added to the form")
-        n = space.number_of_global_dofs()
-        out = None
-        for cells, local in groups:
-            if cells is None:
-                key = ("adjacency", n)
-                cache = space._cache
-                if key not in cache:
-                    st = _lib.status_word(space.device)
-                    adj_ptr, adj, _ = K.build_adjacency(space.cell_to_dof(), n, st)
-                    _lib.check_status_word("adjacency", st)
-                    cache[key] = (adj_ptr, adj)
-                adj_ptr, adj = cache[key]
+                    rest.append(i)
+        # other integrators: cell vectors grouped by the cells they integrate
+        # over (all cells, or a sub-region), one dof gather per group
+        groups = []
+        for i in rest:
+            v = i.assembly(space)
+            cells = i.cell_selection(mesh)
+            for g in groups:
+                if (g[0] is None and cells is None) or (g[0] is not None and cells is not None and
+                                                       g[0].shape == cells.shape and torch.equal(g[0], cells)):
+                    g[1] = g[1] + v
+                    break
             else:
-                st = _lib.status_word(space.device)
-                adj_ptr, adj, _ = K.build_adjacency(space.cell_to_dof()[cells].contiguous(), n, st)
-                _lib.check_status_word("adjacency", st)
+                groups.append([cells, v])
+        if not groups and out is None:
+            raise RuntimeError("no integrator added to the form")
+        for cells, local in groups:
+            adj_ptr, adj = self._adjacency(space, cells)
             vec = K.gather_sum(adj_ptr, adj, local.to(torch.float64).contiguous())
             out = vec if out is None else out + vec
         self._V = out
         return self._V
+
+    @staticmethod
+    def _adjacency(space, cells):
+        """dof -> (cell, local) adjacency of all cells (cached on the space)
+        or of a sub-region."""
+        n = space.number_of_global_dofs()
+        if cells is None:
+            key = ("adjacency", n)
+            cache = space._cache
+            if key not in cache:
+                st = _lib.status_word(space.device)
+                adj_ptr, adj, _ = K.build_adjacency(space.cell_to_dof(), n, st)
+                _lib.check_status_word("adjacency", st)
+                cache[key] = (adj_ptr, adj)
+            return cache[key]
+        st = _lib.status_word(space.device)
+        adj_ptr, adj, _ = K.build_adjacency(space.cell_to_dof()[cells].contiguous(), n, st)
+        _lib.check_status_word("adjacency", st)
+        return adj_ptr, adj

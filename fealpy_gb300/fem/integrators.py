@@ -423,22 +423,35 @@ class ScalarSourceIntegrator(Integrator):
         self.q = q
         self.set_region(region)
 
-    def assembly(self, space, /, indices=None) -> torch.Tensor:
-        self._check_region()
+    def source_data(self, space):
+        """(cells or None, signed measures, mode, number, values, w phi table,
+        its column sums) of this source for ``fgb_source_local/gather``:
+        mode 0 a number, 1 one value per cell, 2 one per quadrature point."""
         mesh = space.mesh
         q = space.p + 3 if self.q is None else self.q
         bcs, ws = mesh.quadrature_formula(q).get_quadrature_points_and_weights()
         cells = self.cell_selection(mesh)
         index = _S if cells is None else cells
         cm = mesh.entity_measure("cell", index=index)
-        phi = torch.as_tensor(sx.shape_function(bcs, space.p), device=mesh.device)       # (NQ, ldof)
-        w = torch.as_tensor(ws, device=mesh.device)
+        wphi_np = ws[:, None] * sx.shape_function(bcs, space.p)                       # (NQ, ldof)
+        wphi = torch.as_tensor(wphi_np, dtype=torch.float64, device=mesh.device).contiguous()
+        sv = torch.as_tensor(wphi_np.sum(axis=0), dtype=torch.float64, device=mesh.device)
         f = _source_values(self.source, mesh, bcs, index)
+        NC = cm.shape[0]
         if isinstance(f, float):
-            return torch.einsum("c,q,qi->ci", cm, w, phi) * f
-        if f.ndim == 1 and f.shape[0] == cm.shape[0]:
-            f = f[:, None].expand(-1, len(ws))
-        return torch.einsum("c,q,qi,cq->ci", cm, w, phi, f)
+            return cells, cm, 0, f, None, wphi, sv
+        if f.numel() == 1:
+            return cells, cm, 0, float(f.reshape(-1)[0].item()), None, wphi, sv
+        if f.ndim == 1 and f.shape[0] == NC:
+            return cells, cm, 1, 0.0, f, wphi, sv
+        f = torch.broadcast_to(f, (NC, len(ws))).contiguous()
+        return cells, cm, 2, 0.0, f, wphi, sv
+
+    def assembly(self, space, /, indices=None) -> torch.Tensor:
+        """Cell vectors (NC, ldof) of the source (``fgb_source_local``)."""
+        _, cm, mode, fs, f, wphi, sv = self.source_data(space)
+        out = K.source_local(cm, mode, fs, f, wphi, sv, space.number_of_local_dofs())
+        return out if indices is None else out[indices]
 
 
 class VectorSourceIntegrator(Integrator):

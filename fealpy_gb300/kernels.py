@@ -133,6 +133,34 @@ def assemble_scalar(adj_ptr, adj, c2d, tables: torch.Tensor, factors: torch.Tens
     return values, v32
 
 
+def source_local(cm, mode: int, f_scalar: float, f, wphi, sv, ldof: int) -> torch.Tensor:
+    """(NC, ldof) cell vectors of a scalar source (see ``fgb_source_local``)."""
+    dev = cm.device
+    NC = cm.numel()
+    out = torch.empty((NC, ldof), dtype=torch.float64, device=dev)
+    cm_d = cm.to(torch.float64).contiguous()
+    f_d = f.to(device=dev, dtype=torch.float64).contiguous() if f is not None else None
+    call("fgb_source_local", NC, ldof, wphi.shape[0], ptr(cm_d), mode, float(f_scalar), ptr(f_d), ptr(wphi), ptr(sv),
+         ptr(out), stream_ptr(dev))
+    return out
+
+
+def source_gather(adj_ptr, adj, ldof: int, cm, mode: int, f_scalar: float, f, wphi, sv,
+                  out: Optional[torch.Tensor] = None) -> torch.Tensor:
+    """Global vector of a scalar source over the dof adjacency; adds to ``out``
+    when given (see ``fgb_source_gather``)."""
+    dev = cm.device
+    n = adj_ptr.numel() - 1
+    acc = out is not None
+    if out is None:
+        out = torch.empty(n, dtype=torch.float64, device=dev)
+    cm_d = cm.to(torch.float64).contiguous()
+    f_d = f.to(device=dev, dtype=torch.float64).contiguous() if f is not None else None
+    call("fgb_source_gather", n, ptr(adj_ptr), ptr(adj), ldof, wphi.shape[0], ptr(cm_d), mode, float(f_scalar),
+         ptr(f_d), ptr(wphi), ptr(sv), ptr(out), 1 if acc else 0, stream_ptr(dev))
+    return out
+
+
 def pcg_multi(indptr, indices, values, dinv, B: torch.Tensor, X: torch.Tensor, atol: float, rtol: float,
               maxit: int):
     """Jacobi-PCG (``dinv`` None: plain CG) on every column of B (n, k),

@@ -275,6 +275,22 @@ int32_t fgb_cell_apply(int32_t dtype, int64_t n_cell, int32_t ldof, const int32_
                        int32_t n_table, const double* tables_host, const void* tables,
                        const void* factors, const void* x, void* ycell, void* stream);
 
+/* Scalar source right-hand sides (ScalarSourceIntegrator, fealpy/fem/
+ * scalar_source_integrator.py:51-58; LinearForm's scatter, fealpy/fem/
+ * linear_form.py:36-86): b_c[i] = cm[c] sum_q w_q phi_i(q) f(c, q), the
+ * source as one number (mode 0, f_scalar), one value per cell (mode 1, f
+ * (NC)) or per quadrature point (mode 2, f (NC, NQ)); wphi (NQ x ldof) =
+ * w_q phi_i(q), sv (ldof) its column sums (device).  local: the cell vectors
+ * (NC x ldof); gather: the global vector over the dof adjacency in adjacency
+ * order (accumulate != 0 adds to out). */
+int32_t fgb_source_local(int64_t n_cell, int32_t ldof, int32_t nq, const double* cm, int32_t mode,
+                         double f_scalar, const double* f, const double* wphi, const double* sv,
+                         double* out, void* stream);
+int32_t fgb_source_gather(int64_t n_dof, const int64_t* adj_ptr, const int32_t* adj, int32_t ldof,
+                          int32_t nq, const double* cm, int32_t mode, double f_scalar, const double* f,
+                          const double* wphi, const double* sv, double* out, int32_t accumulate,
+                          void* stream);
+
 /* Split of a block-diagonal CSR of many systems assembled together (system s
  * owns rows and columns [row_off[s], row_off[s+1]), n_rows = row_off[n_sys]):
  * columns rebased in place to each system's numbering (a column outside its
