@@ -70,7 +70,7 @@ _SIGNATURES = {
     "fgb_pattern_workspace_bytes": (c_sz, [c_i64]),
     "fgb_pattern_count": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_i32, c_vp, c_vp, c_vp, c_sz, c_vp]),
     "fgb_pattern_fill": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_i32, c_vp, c_vp, c_vp, c_vp, c_sz, c_vp]),
-    "fgb_pattern_build": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_i32, c_i64, c_vp, c_vp, c_sz, c_vp, c_vp, c_sz, c_vp]),
+    "fgb_pattern_build": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_i32, c_i64, c_vp, c_vp, c_sz, c_vp, c_vp, c_vp, c_sz, c_vp]),
     "fgb_pattern_compact": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_sz, c_vp]),
     "fgb_pattern_expand_blocks": (c_i32, [c_i64, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "fgb_cell_factors": (c_i32, [c_i32, c_i64, c_vp, c_vp, c_i32, c_vp, c_vp, c_vp, c_vp, c_i32, c_vp, c_vp, c_vp]),
@@ -87,7 +87,7 @@ _SIGNATURES = {
     "fgb_local_matrices": (c_i32, [c_i32, c_i64, c_i32, c_i32, c_vp, c_vp, c_vp, c_i32, c_vp]),
     "fgb_local_elasticity_p1": (c_i32, [c_i32, c_i32, c_i64, c_vp, c_i32, c_vp, c_vp]),
     "fgb_assemble_scalar_acc": (c_i32, [c_i32, c_i64, c_vp, c_vp, c_vp, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp,
-                                        c_vp, c_i32, c_vp, c_vp, c_sz, c_vp]),
+                                        c_vp, c_vp, c_i32, c_vp, c_vp, c_sz, c_vp]),
     "fgb_assemble_elasticity_p1": (c_i32, [c_i32, c_i32, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp,
                                            c_vp, c_vp, c_vp, c_sz, c_vp]),
     "fgb_dirichlet_count": (c_i32, [c_i32, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),

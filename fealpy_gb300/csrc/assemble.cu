@@ -113,20 +113,25 @@ struct RowSmem {
 };
 
 // LDOF > 0: the local dof count as a compile-time constant (divisions by it
-// become multiply-shifts); LDOF == 0: taken from `ldof_rt`.
-template <typename T, int LDOF>
+// become multiply-shifts); LDOF == 0: taken from `ldof_rt`.  MAP: the
+// contribution of adjacency entry k and local dof j lands at the row slot
+// pos[k * ldof + j] recorded by the pattern pass (rows of at most kRowMapMax
+// entries); otherwise the slot is found by a binary search of the row's
+// columns.
+template <typename T, int LDOF, bool MAP>
 __device__ bool assemble_scalar_row(int64_t i, const int64_t* __restrict__ adj_ptr, const int32_t* __restrict__ adj,
                                     const int32_t* __restrict__ c2d, int ldof_rt, int nt, const T* __restrict__ tab,
                                     const T* __restrict__ factors, const int64_t* __restrict__ indptr,
-                                    const int32_t* __restrict__ indices, T* __restrict__ values,
-                                    float* __restrict__ values32, int32_t* cols, T* acc, int cap, int ncopy,
-                                    int accumulate, int32_t* status) {
+                                    const int32_t* __restrict__ indices, const uint8_t* __restrict__ pos,
+                                    T* __restrict__ values, float* __restrict__ values32, int32_t* cols, T* acc,
+                                    int cap, int ncopy, int accumulate, int32_t* status) {
   const int ldof = LDOF > 0 ? LDOF : ldof_rt;
   const int lane = threadIdx.x & 31;
   const int64_t base = indptr[i];
   const int L = static_cast<int>(indptr[i + 1] - base);
   if (L > cap) return false;
-  for (int t = lane; t < L; t += 32) cols[t] = __ldg(indices + base + t);
+  if constexpr (!MAP)
+    for (int t = lane; t < L; t += 32) cols[t] = __ldg(indices + base + t);
   for (int g = 0; g < ncopy; ++g)
     for (int t = lane; t < L; t += 32) acc[g * cap + t] = T(0);
   __syncwarp();
@@ -139,13 +144,19 @@ __device__ bool assemble_scalar_row(int64_t i, const int64_t* __restrict__ adj_p
       const int32_t en = __ldg(adj + k);
       const int32_t c = en / ldof;
       const int li = en - c * ldof;
-      const int32_t col = __ldg(c2d + static_cast<int64_t>(c) * ldof + lj);
+      int slot;
+      if constexpr (MAP) {
+        slot = __ldg(pos + k * ldof + lj);
+      } else {
+        const int32_t col = __ldg(c2d + static_cast<int64_t>(c) * ldof + lj);
+        slot = lower_bound_i32(cols, L, col);
+        if (slot < L && cols[slot] != col) slot = L;
+      }
       const T* f = factors + static_cast<int64_t>(c) * nt;
       const T* tb = tab + li * ldof + lj;
       T v = T(0);
       for (int t = 0; t < nt; ++t) v += __ldg(f + t) * tb[t * ld2];
-      const int pos = lower_bound_i32(cols, L, col);
-      if (pos < L && cols[pos] == col) acc[g * cap + pos] += v;
+      if (slot < L) acc[g * cap + slot] += v;
       else set_status(status, FGB_ERR_PATTERN);
     }
     __syncwarp();
@@ -162,13 +173,14 @@ __device__ bool assemble_scalar_row(int64_t i, const int64_t* __restrict__ adj_p
 }
 
 // Dynamic shared memory layout: tables (nt*ldof*ldof T) | per warp: acc (ncopy*cap T) | cols (cap int32)
-template <typename T, int LDOF>
+template <typename T, int LDOF, bool MAP>
 __global__ void assemble_scalar_kernel(int64_t n_rows, const int32_t* __restrict__ row_list,
                                        const int32_t* __restrict__ row_list_len, const int64_t* __restrict__ adj_ptr,
                                        const int32_t* __restrict__ adj, const int32_t* __restrict__ c2d, int ldof,
                                        int nt, const T* __restrict__ tables, const T* __restrict__ factors,
                                        const int64_t* __restrict__ indptr, const int32_t* __restrict__ indices,
-                                       T* __restrict__ values, float* __restrict__ values32, int cap, int ncopy,
+                                       const uint8_t* __restrict__ pos, T* __restrict__ values,
+                                       float* __restrict__ values32, int cap, int ncopy,
                                        int accumulate, int32_t* __restrict__ ovf, int32_t* __restrict__ ovf_len,
                                        int32_t* status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -186,8 +198,8 @@ __global__ void assemble_scalar_kernel(int64_t n_rows, const int32_t* __restrict
   const int64_t nwarps = static_cast<int64_t>(gridDim.x) * wpb;
   for (int64_t r = warp; r < n; r += nwarps) {
     const int64_t i = row_list ? row_list[r] : r;
-    bool done = assemble_scalar_row<T, LDOF>(i, adj_ptr, adj, c2d, ldof, nt, tab, factors, indptr, indices, values,
-                                             values32, cols, acc, cap, ncopy, accumulate, status);
+    bool done = assemble_scalar_row<T, LDOF, MAP>(i, adj_ptr, adj, c2d, ldof, nt, tab, factors, indptr, indices, pos,
+                                                  values, values32, cols, acc, cap, ncopy, accumulate, status);
     if (!done && lane == 0) {
       if (ovf) { int slot = atomicAdd(ovf_len, 1); ovf[slot] = static_cast<int32_t>(i); }
       else set_status(status, FGB_ERR_CAPACITY);
@@ -328,11 +340,30 @@ constexpr int kAsmCap = 128;      // first pass: row entries per warp
 constexpr int kAsmBigCap = 4096;  // second pass: one warp per block, one accumulator copy
 constexpr size_t kMaxDynSmem = 200 * 1024;
 
+template <typename T, bool MAP>
+auto scalar_kernel_for(int ldof) {
+  switch (ldof) {
+    case 3: return assemble_scalar_kernel<T, 3, MAP>;
+    case 4: return assemble_scalar_kernel<T, 4, MAP>;
+    case 6: return assemble_scalar_kernel<T, 6, MAP>;
+    case 10: return assemble_scalar_kernel<T, 10, MAP>;
+    default: return assemble_scalar_kernel<T, 0, MAP>;
+  }
+}
+
+// First launch: rows of at most kAsmCap entries, one warp each (direct slots
+// when the pattern's positions are given); rows that do not fit are listed
+// and done by a second launch with one warp per block and a larger row
+// buffer (column search).  Measured on the P2 tetrahedral 64^3 matrix (60.9 M
+// entries): FP64 values 3.15 ms with slots against 3.56 ms searching, FP32
+// 1.39 against 1.94 ms; recording the slots adds 0.64 ms to the pattern, so
+// they pay off once a pattern is assembled into more than once.
 template <typename T>
 int launch_scalar(int64_t n_dof, const int64_t* adj_ptr, const int32_t* adj, const int32_t* c2d, int ldof, int nt,
-                  const T* tables, const T* factors, const int64_t* indptr, const int32_t* indices, T* values,
-                  float* values32, int accumulate, int32_t* status, int32_t* ovf, int32_t* ovf_len,
-                  cudaStream_t st) {
+                  const T* tables, const T* factors, const int64_t* indptr, const int32_t* indices,
+                  const uint8_t* pos, T* values, float* values32, int accumulate, int32_t* status, int32_t* ovf,
+                  int32_t* ovf_len, cudaStream_t st) {
+  static_assert(kAsmCap <= kRowMapMax, "direct slots exist for rows up to kRowMapMax entries");
   const size_t tab_bytes = align_up(static_cast<size_t>(nt) * ldof * ldof * sizeof(T), 16);
   const int ncopy = 32 / ldof;
   const size_t per_warp1 = align_up(static_cast<size_t>(ncopy) * kAsmCap * sizeof(T) + kAsmCap * 4, 16);
@@ -340,22 +371,18 @@ int launch_scalar(int64_t n_dof, const int64_t* adj_ptr, const int32_t* adj, con
   const size_t per_warp2 = align_up(static_cast<size_t>(kAsmBigCap) * sizeof(T) + kAsmBigCap * 4, 16);
   const size_t smem2 = tab_bytes + per_warp2;
   if (smem1 > kMaxDynSmem || smem2 > kMaxDynSmem) return FGB_ERR_CAPACITY;
-  auto kern = assemble_scalar_kernel<T, 0>;
-  switch (ldof) {
-    case 3: kern = assemble_scalar_kernel<T, 3>; break;
-    case 4: kern = assemble_scalar_kernel<T, 4>; break;
-    case 6: kern = assemble_scalar_kernel<T, 6>; break;
-    case 10: kern = assemble_scalar_kernel<T, 10>; break;
-    default: break;
-  }
+  auto kern = scalar_kernel_for<T, false>(ldof);
+  auto kmap = scalar_kernel_for<T, true>(ldof);
+  auto k1 = pos ? kmap : kern;
   cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem2 > smem1 ? smem2 : smem1));
+  cudaFuncSetAttribute(kmap, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem1));
   cudaMemsetAsync(ovf_len, 0, sizeof(int32_t), st);
   const int grid1 = grid_for(n_dof, kAsmWarps, kNumSMs * 16);
-  kern<<<grid1, kAsmWarps * 32, smem1, st>>>(n_dof, nullptr, nullptr, adj_ptr, adj, c2d, ldof, nt, tables, factors,
-                                             indptr, indices, values, values32, kAsmCap, ncopy, accumulate, ovf,
-                                             ovf_len, status);
+  k1<<<grid1, kAsmWarps * 32, smem1, st>>>(n_dof, nullptr, nullptr, adj_ptr, adj, c2d, ldof, nt, tables, factors,
+                                           indptr, indices, pos, values, values32, kAsmCap, ncopy, accumulate, ovf,
+                                           ovf_len, status);
   kern<<<kNumSMs, 32, smem2, st>>>(n_dof, ovf, ovf_len, adj_ptr, adj, c2d, ldof, nt, tables, factors, indptr, indices,
-                                   values, values32, kAsmBigCap, 1, accumulate, nullptr, nullptr, status);
+                                   nullptr, values, values32, kAsmBigCap, 1, accumulate, nullptr, nullptr, status);
   return launch_status();
 }
 
@@ -454,14 +481,14 @@ int32_t fgb_assemble_scalar(int32_t dtype, int64_t n_dof, const int64_t* adj_ptr
                             float* values_f32, int32_t* status, void* workspace, size_t workspace_bytes,
                             void* stream) {
   return fgb_assemble_scalar_acc(dtype, n_dof, adj_ptr, adj, cell2dof, ldof, n_table, tables, factors, indptr, indices,
-                                 values, values_f32, 0, status, workspace, workspace_bytes, stream);
+                                 nullptr, values, values_f32, 0, status, workspace, workspace_bytes, stream);
 }
 
 int32_t fgb_assemble_scalar_acc(int32_t dtype, int64_t n_dof, const int64_t* adj_ptr, const int32_t* adj,
                                 const int32_t* cell2dof, int32_t ldof, int32_t n_table, const void* tables,
-                                const void* factors, const int64_t* indptr, const int32_t* indices, void* values,
-                                float* values_f32, int32_t accumulate, int32_t* status, void* workspace,
-                                size_t workspace_bytes, void* stream) {
+                                const void* factors, const int64_t* indptr, const int32_t* indices,
+                                const uint8_t* positions, void* values, float* values_f32, int32_t accumulate,
+                                int32_t* status, void* workspace, size_t workspace_bytes, void* stream) {
   if (n_dof <= 0 || ldof <= 0 || ldof > 32 || n_table <= 0 || !adj_ptr || !adj || !cell2dof || !tables ||
       !factors || !indptr || !indices || !values)
     return FGB_ERR_ARG;
@@ -472,12 +499,12 @@ int32_t fgb_assemble_scalar_acc(int32_t dtype, int64_t n_dof, const int64_t* adj
   cudaStream_t st = as_stream(stream);
   if (dtype == FGB_F64)
     return launch_scalar<double>(n_dof, adj_ptr, adj, cell2dof, ldof, n_table, static_cast<const double*>(tables),
-                                 static_cast<const double*>(factors), indptr, indices, static_cast<double*>(values),
-                                 values_f32, accumulate ? 1 : 0, status, ovf, ovf_len, st);
+                                 static_cast<const double*>(factors), indptr, indices, positions,
+                                 static_cast<double*>(values), values_f32, accumulate ? 1 : 0, status, ovf, ovf_len, st);
   if (dtype == FGB_F32)
     return launch_scalar<float>(n_dof, adj_ptr, adj, cell2dof, ldof, n_table, static_cast<const float*>(tables),
-                                static_cast<const float*>(factors), indptr, indices, static_cast<float*>(values),
-                                values_f32, accumulate ? 1 : 0, status, ovf, ovf_len, st);
+                                static_cast<const float*>(factors), indptr, indices, positions,
+                                static_cast<float*>(values), values_f32, accumulate ? 1 : 0, status, ovf, ovf_len, st);
   return FGB_ERR_ARG;
 }
 

@@ -21,6 +21,10 @@ namespace fgb {
 
 constexpr int kWarp = 32;
 constexpr int kNumSMs = 152;  // GB300: 2 dies x 76 SMs (only used as a grid-size hint)
+// Longest row whose within-row column positions the hashed pattern pass
+// records (one byte per contribution); the numeric pass indexes rows up to
+// this length directly and searches the columns of longer ones.
+constexpr int kRowMapMax = 128;
 
 __device__ __forceinline__ void set_status(int32_t* status, int32_t code) {
   if (status) atomicMax(status, code);

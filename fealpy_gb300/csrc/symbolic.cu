@@ -282,6 +282,8 @@ __device__ bool pattern_row(int64_t i, int mode, const int64_t* __restrict__ adj
 // handles it).  The result does not depend on insertion order.
 constexpr int kHashSlots = 256;
 constexpr int kHashMaxUnique = 128;
+static_assert(kHashMaxUnique >= kRowMapMax, "rows the numeric pass indexes directly must have positions");
+static_assert(kHashMaxUnique <= 256, "positions are one byte");
 
 // Ascending sort of one value per lane across the warp (bitonic network on
 // registers, 15 shuffle steps).
@@ -300,14 +302,49 @@ __device__ __forceinline__ int32_t warp_sort32(int32_t v) {
   return v;
 }
 
+__device__ __forceinline__ unsigned hash8(int32_t v) { return (static_cast<unsigned>(v) * 2654435761u) >> 24; }
+
+// slot of column v in a warp's hash set (v was inserted: linear probing from
+// its hash meets v before any empty slot); -1 if absent
+__device__ __forceinline__ int hash_slot(const int32_t* tab, int32_t v) {
+  const unsigned h = hash8(v);
+  for (int pr = 0; pr < kHashSlots; ++pr) {
+    const int sl = static_cast<int>((h + pr) & (kHashSlots - 1));
+    const int32_t t = tab[sl];
+    if (t == v) return sl;
+    if (t == -1) return -1;
+  }
+  return -1;
+}
+
+// pos[s * ldof + t] = rank of candidate t's column in the row (the hash set
+// `tab` of the row and the slot -> rank map `rk` are complete)
+__device__ __forceinline__ void row_positions(int64_t s, int m, int ldof, const int32_t* __restrict__ adj,
+                                              const int32_t* __restrict__ c2d, const int32_t* tab, const uint8_t* rk,
+                                              uint8_t* __restrict__ pos) {
+  const int lane = threadIdx.x & 31;
+  for (int t = lane; t < m; t += 32) {
+    const int k = t / ldof, j = t - k * ldof;
+    const int32_t c = adj[s + k] / ldof;
+    const int32_t v = c2d[static_cast<int64_t>(c) * ldof + j];
+    const int sl = hash_slot(tab, v);
+    pos[s * ldof + t] = sl >= 0 ? rk[sl] : static_cast<uint8_t>(0xFF);
+  }
+}
+
 // mode 0: count (row_cnt); 1: write the sorted row into indices at indptr[i];
 // 2: count and stage the sorted row at stage[adj_ptr[i] * ldof] (its upper
-// bound of entries), so that the values need no second pass.
+// bound of entries), so that the values need no second pass.  With `pos`
+// (mode 2), the position within the row of every candidate column is
+// recorded as one byte at pos[adj_ptr[i] * ldof + t], t = k * ldof + j for
+// local dof j of the row's k-th adjacent cell, so that the numeric assembly
+// adds each contribution at a known slot instead of searching the row.  `rk`
+// (kHashSlots bytes per warp) maps a hash slot to the rank of its column.
 __device__ bool pattern_row_hash(int64_t i, int mode, const int64_t* __restrict__ adj_ptr,
                                  const int32_t* __restrict__ adj, const int32_t* __restrict__ c2d, int ldof,
                                  int32_t* __restrict__ row_cnt, const int64_t* __restrict__ indptr,
                                  int32_t* __restrict__ indices, int32_t* __restrict__ stage, int32_t* tab,
-                                 int32_t* srt) {
+                                 int32_t* srt, uint8_t* __restrict__ pos, uint8_t* rk) {
   const int lane = threadIdx.x & 31;
   const int64_t s = adj_ptr[i];
   const int m = static_cast<int>(adj_ptr[i + 1] - s) * ldof;
@@ -320,7 +357,7 @@ __device__ bool pattern_row_hash(int64_t i, int mode, const int64_t* __restrict_
       const int k = t / ldof, j = t - k * ldof;
       const int32_t c = adj[s + k] / ldof;
       const int32_t v = c2d[static_cast<int64_t>(c) * ldof + j];
-      const unsigned h = (static_cast<unsigned>(v) * 2654435761u) >> 24;  // 8 bits
+      const unsigned h = hash8(v);
       int pr = 0;
       for (; pr < kHashSlots; ++pr) {
         const int32_t old = atomicCAS(tab + ((h + pr) & (kHashSlots - 1)), -1, v);
@@ -349,6 +386,14 @@ __device__ bool pattern_row_hash(int64_t i, int mode, const int64_t* __restrict_
     }
     if (mode == 1 && lane < u) indices[indptr[i] + lane] = v;
     if (mode == 2 && lane < u) stage[adj_ptr[i] * ldof + lane] = v;
+    if (pos != nullptr && mode == 2) {
+      if (lane < u) {
+        const int sl = hash_slot(tab, v);
+        if (sl >= 0) rk[sl] = static_cast<uint8_t>(lane);
+      }
+      __syncwarp();
+      row_positions(s, m, ldof, adj, c2d, tab, rk, pos);
+    }
     __syncwarp();
     return true;
   }
@@ -377,6 +422,14 @@ __device__ bool pattern_row_hash(int64_t i, int mode, const int64_t* __restrict_
   } else if (mode == 2) {
     const int64_t out0 = adj_ptr[i] * ldof;
     for (int t = lane; t < u; t += 32) stage[out0 + t] = srt[t];
+    if (pos != nullptr) {
+      for (int t = lane; t < u; t += 32) {
+        const int sl = hash_slot(tab, srt[t]);
+        if (sl >= 0) rk[sl] = static_cast<uint8_t>(t);
+      }
+      __syncwarp();
+      row_positions(s, m, ldof, adj, c2d, tab, rk, pos);
+    }
   }
   __syncwarp();
   return true;
@@ -387,16 +440,18 @@ __global__ void __launch_bounds__(kPatWarps * 32) pattern_pass1(int64_t n_dof, i
                                                                 int ldof, int32_t* __restrict__ row_cnt,
                                                                 const int64_t* __restrict__ indptr, int32_t* __restrict__ indices,
                                                                 int32_t* __restrict__ ovf, int32_t* __restrict__ ovf_len,
-                                                                int32_t* __restrict__ stage) {
+                                                                int32_t* __restrict__ stage, uint8_t* __restrict__ pos) {
   __shared__ int32_t stab[kPatWarps * kHashSlots];
   __shared__ int32_t ssrt[kPatWarps * kHashMaxUnique];
+  __shared__ uint8_t srk[kPatWarps * kHashSlots];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   int32_t* tab = stab + wib * kHashSlots;
   int32_t* srt = ssrt + wib * kHashMaxUnique;
+  uint8_t* rk = srk + wib * kHashSlots;
   const int64_t warp = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
   const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
   for (int64_t i = warp; i < n_dof; i += nwarps) {
-    bool done = pattern_row_hash(i, mode, adj_ptr, adj, c2d, ldof, row_cnt, indptr, indices, stage, tab, srt);
+    bool done = pattern_row_hash(i, mode, adj_ptr, adj, c2d, ldof, row_cnt, indptr, indices, stage, tab, srt, pos, rk);
     if (!done && lane == 0) {
       int slot = atomicAdd(ovf_len, 1);
       ovf[slot] = static_cast<int32_t>(i);
@@ -525,7 +580,7 @@ static int pattern_launch(int mode, int64_t n_dof, const int64_t* adj_ptr, const
                           int32_t* ovf_len, int32_t* status, cudaStream_t st) {
   cudaMemsetAsync(ovf_len, 0, sizeof(int32_t), st);
   pattern_pass1<<<grid_for(n_dof * 32, kPatWarps * 32, kNumSMs * 8), kPatWarps * 32, 0, st>>>(
-      n_dof, mode, adj_ptr, adj, c2d, ldof, row_cnt, indptr, indices, ovf, ovf_len, nullptr);
+      n_dof, mode, adj_ptr, adj, c2d, ldof, row_cnt, indptr, indices, ovf, ovf_len, nullptr, nullptr);
   cudaFuncSetAttribute(pattern_pass2, cudaFuncAttributeMaxDynamicSharedMemorySize, kPatBigCap * 4);
   pattern_pass2<<<kNumSMs, 32, kPatBigCap * 4, st>>>(mode, adj_ptr, adj, c2d, ldof, row_cnt, indptr, indices, ovf,
                                                      ovf_len, status);
@@ -568,7 +623,8 @@ int32_t fgb_pattern_fill(int64_t n_dof, const int64_t* adj_ptr, const int32_t* a
 
 int32_t fgb_pattern_build(int64_t n_dof, const int64_t* adj_ptr, const int32_t* adj, const int32_t* cell2dof,
                           int32_t ldof, int64_t n_adj, int64_t* indptr, int32_t* stage, size_t stage_bytes,
-                          int32_t* status, void* workspace, size_t workspace_bytes, void* stream) {
+                          uint8_t* positions, int32_t* status, void* workspace, size_t workspace_bytes,
+                          void* stream) {
   if (n_dof <= 0 || ldof <= 0 || n_adj <= 0 || !adj_ptr || !adj || !cell2dof || !indptr || !stage) return FGB_ERR_ARG;
   if (stage_bytes < static_cast<size_t>(n_adj) * ldof * sizeof(int32_t)) return FGB_ERR_WORKSPACE;
   if (workspace == nullptr || workspace_bytes < fgb_pattern_workspace_bytes(n_dof)) return FGB_ERR_WORKSPACE;
@@ -581,7 +637,7 @@ int32_t fgb_pattern_build(int64_t n_dof, const int64_t* adj_ptr, const int32_t* 
   size_t scan_bytes = workspace_bytes - cv.off;
   cudaMemsetAsync(ovf_len, 0, sizeof(int32_t), st);
   pattern_pass1<<<grid_for(n_dof * 32, kPatWarps * 32, kNumSMs * 8), kPatWarps * 32, 0, st>>>(
-      n_dof, 2, adj_ptr, adj, cell2dof, ldof, cnt, nullptr, nullptr, ovf, ovf_len, stage);
+      n_dof, 2, adj_ptr, adj, cell2dof, ldof, cnt, nullptr, nullptr, ovf, ovf_len, stage, positions);
   cudaFuncSetAttribute(pattern_pass2, cudaFuncAttributeMaxDynamicSharedMemorySize, kPatBigCap * 4);
   pattern_pass2<<<kNumSMs, 32, kPatBigCap * 4, st>>>(0, adj_ptr, adj, cell2dof, ldof, cnt, nullptr, nullptr, ovf,
                                                      ovf_len, status);

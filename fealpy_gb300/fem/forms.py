@@ -26,11 +26,18 @@ def _mark(marks, label):
         marks.append((label, e))
 
 
-def symbolic_structure(c2d: torch.Tensor, n_dof: int, status: Optional[torch.Tensor] = None, marks=None):
-    """(adj_ptr, adj, indptr, indices) for a cell-to-dof map."""
+def symbolic_structure(c2d: torch.Tensor, n_dof: int, status: Optional[torch.Tensor] = None, marks=None,
+                       positions: bool = False):
+    """(adj_ptr, adj, indptr, indices) for a cell-to-dof map; with
+    ``positions`` a fifth entry, the within-row slot map that lets the numeric
+    assembly skip the column search."""
     st = _lib.status_word(c2d.device) if status is None else status
     adj_ptr, adj, _ = K.build_adjacency(c2d, n_dof, st)
     _mark(marks, "adjacency")
+    if positions:
+        indptr, indices, pos = K.build_pattern(adj_ptr, adj, c2d, n_dof, st, positions=True)
+        _mark(marks, "pattern")
+        return adj_ptr, adj, indptr, indices, pos
     indptr, indices = K.build_pattern(adj_ptr, adj, c2d, n_dof, st)
     _mark(marks, "pattern")
     return adj_ptr, adj, indptr, indices
@@ -113,12 +120,12 @@ class BilinearForm(_Form):
                 raise NotImplementedError("only several scalar integrators can share one form")
         return out
 
-    def _symbolic(self, space, c2d, n, marks=None, sub: bool = False):
-        key = ("symbolic", n)
+    def _symbolic(self, space, c2d, n, marks=None, sub: bool = False, positions: bool = False):
+        key = ("symbolic", n, positions)
         cache = getattr(space, "_cache", {})
         if self.reuse_pattern and not sub and key in cache:
             return cache[key]
-        out = symbolic_structure(c2d, n, marks=marks)
+        out = symbolic_structure(c2d, n, marks=marks, positions=positions)
         if self.reuse_pattern and not sub:
             cache[key] = out
         return out
@@ -145,7 +152,11 @@ class BilinearForm(_Form):
                 # (FEALPy scatters the region's local matrices alone)
                 c2d = c2d[plan.cells].contiguous()
             n = space.number_of_global_dofs()
-            adj_ptr, adj, indptr, indices = self._symbolic(space, c2d, n, marks, sub)
+            # a reused pattern also keeps the slot of every contribution in
+            # its row (the numeric pass then skips the column search)
+            sym = self._symbolic(space, c2d, n, marks, sub, positions=self.reuse_pattern and not sub)
+            adj_ptr, adj, indptr, indices = sym[:4]
+            pos = sym[4] if len(sym) > 4 else None
             mesh = space.mesh
             coef = plan.coef_matrix()
             passes = plan.passes()
@@ -160,7 +171,7 @@ class BilinearForm(_Form):
                 last = k == len(passes) - 1
                 values, v32 = K.assemble_scalar(adj_ptr, adj, c2d, tab, fac, indptr, indices,
                                                 values_f32=emit_f32 and dtype == torch.float64 and last,
-                                                status=status, accumulate_into=values)
+                                                status=status, accumulate_into=values, positions=pos)
             _mark(marks, "values")
         elif isinstance(plan, ElasticityPlan):
             ss = space.scalar_space

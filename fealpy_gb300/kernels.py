@@ -67,8 +67,11 @@ def build_adjacency(c2d: torch.Tensor, n_dof: int, status: torch.Tensor):
     return adj_ptr, adj, max_deg
 
 
-def build_pattern(adj_ptr, adj, c2d, n_dof: int, status: torch.Tensor):
-    """Canonical CSR pattern (indptr int64, indices int32).  One host sync (nnz)."""
+def build_pattern(adj_ptr, adj, c2d, n_dof: int, status: torch.Tensor, positions: bool = False):
+    """Canonical CSR pattern (indptr int64, indices int32).  One host sync (nnz).
+    With ``positions`` also the within-row slot of every (adjacency entry,
+    local dof) pair (uint8, n_adj * ldof), which lets ``assemble_scalar`` skip
+    the column search: returns (indptr, indices, positions)."""
     dev = _dev(c2d)
     ldof = c2d.shape[1]
     lib = _lib.lib()
@@ -78,13 +81,16 @@ def build_pattern(adj_ptr, adj, c2d, n_dof: int, status: torch.Tensor):
     # one hashed pass that stages every sorted row (n_adj * ldof int32 of
     # scratch), then a copy into the exact-size indices
     stage = torch.empty(max(n_adj * ldof, 1), dtype=torch.int32, device=dev)
+    pos = torch.empty(max(n_adj * ldof, 1), dtype=torch.uint8, device=dev) if positions else None
     call("fgb_pattern_build", n_dof, ptr(adj_ptr), ptr(adj), ptr(c2d), ldof, n_adj, ptr(indptr), ptr(stage),
-         stage.numel() * 4, ptr(status), ptr(ws), ws.numel(), stream_ptr(dev))
+         stage.numel() * 4, ptr(pos), ptr(status), ptr(ws), ws.numel(), stream_ptr(dev))
     nnz = int(indptr[n_dof].item())
     check_status_word("fgb_pattern_build", status)
     indices = torch.empty(max(nnz, 1), dtype=torch.int32, device=dev)
     call("fgb_pattern_compact", n_dof, ptr(adj_ptr), ptr(adj), ptr(c2d), ldof, ptr(indptr), ptr(stage),
          ptr(indices), ptr(status), ptr(ws), ws.numel(), stream_ptr(dev))
+    if positions:
+        return indptr, indices[:nnz], pos
     return indptr, indices[:nnz]
 
 
@@ -100,9 +106,11 @@ def expand_blocks(n_node: int, bs: int, dof_priority: bool, indptr, indices):
 
 def assemble_scalar(adj_ptr, adj, c2d, tables: torch.Tensor, factors: torch.Tensor, indptr, indices,
                     values_f32: bool = False, status: Optional[torch.Tensor] = None,
-                    accumulate_into: Optional[torch.Tensor] = None):
+                    accumulate_into: Optional[torch.Tensor] = None, positions: Optional[torch.Tensor] = None):
     """CSR values of sum_t factors[:, t] * tables[t] over the pattern; with
-    ``accumulate_into`` (values of an earlier pass) this pass is added to them."""
+    ``accumulate_into`` (values of an earlier pass) this pass is added to them;
+    ``positions`` (from ``build_pattern(..., positions=True)`` of this
+    pattern) replaces the per-contribution column search."""
     dev = _dev(c2d)
     n_dof = adj_ptr.numel() - 1
     ldof = c2d.shape[1]
@@ -117,6 +125,8 @@ def assemble_scalar(adj_ptr, adj, c2d, tables: torch.Tensor, factors: torch.Tens
     else:
         values = torch.empty(indices.numel(), dtype=dtype, device=dev)
     v32 = torch.empty(indices.numel(), dtype=torch.float32, device=dev) if values_f32 else None
+    if positions is not None and (positions.dtype != torch.uint8 or positions.numel() < adj.numel() * ldof):
+        raise ValueError("positions must be the uint8 slot map of this pattern (n_adj * ldof entries)")
     lib = _lib.lib()
     ws = workspace(lib.fgb_assemble_workspace_bytes(n_dof), dev)
     own = status is None
@@ -126,7 +136,7 @@ def assemble_scalar(adj_ptr, adj, c2d, tables: torch.Tensor, factors: torch.Tens
     tab_d = tables.to(dev, dtype).contiguous()
     fac_d = factors.contiguous()
     call("fgb_assemble_scalar_acc", dtype_code(dtype), n_dof, ptr(adj_ptr), ptr(adj), ptr(c2d), ldof, nt,
-         ptr(tab_d), ptr(fac_d), ptr(indptr), ptr(indices), ptr(values),
+         ptr(tab_d), ptr(fac_d), ptr(indptr), ptr(indices), ptr(positions), ptr(values),
          ptr(v32), 1 if accumulate_into is not None else 0, ptr(st), ptr(ws), ws.numel(), stream_ptr(dev))
     if own:
         check_status_word("fgb_assemble_scalar", st)

@@ -165,11 +165,17 @@ int32_t fgb_pattern_fill(int64_t n_dof, const int64_t* adj_ptr, const int32_t* a
  * int32, n_adj = adj_ptr[n_dof]), and writes indptr; compact then copies the
  * staged rows into indices (after the caller has read nnz = indptr[n_dof]).
  * Both take the same workspace, which carries the list of rows too long for
- * the hash pass from build to compact. */
+ * the hash pass from build to compact.  positions (optional, n_adj * ldof
+ * bytes): for adjacency entry k of row i (cell c, local index li) and local
+ * dof j, positions[k * ldof + j] = the index within row i of column
+ * cell2dof[c][j], recorded for rows of at most 128 entries; given to
+ * fgb_assemble_scalar_acc, the numeric pass adds each contribution at its slot
+ * without searching the row (a pattern reused across assemblies pays this
+ * once). */
 int32_t fgb_pattern_build(int64_t n_dof, const int64_t* adj_ptr, const int32_t* adj,
                           const int32_t* cell2dof, int32_t ldof, int64_t n_adj, int64_t* indptr,
-                          int32_t* stage, size_t stage_bytes, int32_t* status, void* workspace,
-                          size_t workspace_bytes, void* stream);
+                          int32_t* stage, size_t stage_bytes, uint8_t* positions, int32_t* status,
+                          void* workspace, size_t workspace_bytes, void* stream);
 int32_t fgb_pattern_compact(int64_t n_dof, const int64_t* adj_ptr, const int32_t* adj,
                             const int32_t* cell2dof, int32_t ldof, const int64_t* indptr,
                             const int32_t* stage, int32_t* indices, int32_t* status,
@@ -218,13 +224,16 @@ int32_t fgb_assemble_scalar(int32_t dtype, int64_t n_dof, const int64_t* adj_ptr
 /* The same with accumulate != 0: values += this pass (values_f32, when given,
  * receives the FP32 rounding of the sum).  For local matrices with more than
  * FGB_MAX_CHANNELS factor channels (coefficients given per quadrature point,
- * fealpy/utils/utils.py:21-53): the channels are split into passes. */
+ * fealpy/utils/utils.py:21-53): the channels are split into passes.
+ * positions (optional): the within-row slots fgb_pattern_build recorded for
+ * this pattern; rows up to 128 entries then take no column search. */
 int32_t fgb_assemble_scalar_acc(int32_t dtype, int64_t n_dof, const int64_t* adj_ptr,
                                 const int32_t* adj, const int32_t* cell2dof, int32_t ldof,
                                 int32_t n_table, const void* tables, const void* factors,
-                                const int64_t* indptr, const int32_t* indices, void* values,
-                                float* values_f32, int32_t accumulate, int32_t* status,
-                                void* workspace, size_t workspace_bytes, void* stream);
+                                const int64_t* indptr, const int32_t* indices,
+                                const uint8_t* positions, void* values, float* values_f32,
+                                int32_t accumulate, int32_t* status, void* workspace,
+                                size_t workspace_bytes, void* stream);
 
 /* P1 linear elasticity, interleaved vector dofs (LinearElasticityIntegrator
  * default variant, fealpy/fem/linear_elasticity_integrator.py:60-181, the

@@ -44,7 +44,7 @@ def test_argument_validation_without_gpu():
     assert lib.fgb_cell_factors(4, 10, None, None, 1, None, None, None, None, 1, None, None, None) == 1
     assert lib.fgb_pcg_f64(0, None, None, None, None, None, None, 0.0, 0.0, 1, 1, 0, 0, 0, None, 0, None, None) == 1
     assert lib.fgb_pcg_f64_noalloc(0, None, None, None, None, None, None, 0.0, 0.0, 1, 1, 0, 0, None, None) == 1
-    assert lib.fgb_pattern_build(0, None, None, None, 4, 1, None, None, 0, None, None, 0, None) == 1
+    assert lib.fgb_pattern_build(0, None, None, None, 4, 1, None, None, 0, None, None, None, 0, None) == 1
     assert lib.fgb_pattern_compact(0, None, None, None, 4, None, None, None, None, None, 0, None) == 1
     # batched solver: sizes, bad capacities and bad launch shapes are refused on the host
     assert lib.fgb_batch_bytes(0, 1, 1) == 0 and lib.fgb_batch_bytes(4, 16, 16) > 0

@@ -328,3 +328,4 @@ def test_d15_solvers_match_the_four_byte_copy(golden_dir):
             out[d15] = (x, info["niter"])
         assert abs(out[True][1] - out[False][1]) <= 2, (name, out[True][1], out[False][1])
         assert rel_err(out[True][0], out[False][0].cpu().numpy()) < 1e-9, name
+
