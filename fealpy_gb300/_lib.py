@@ -141,6 +141,7 @@ _SIGNATURES = {
     "fgb_pcg_sell_workspace_bytes": (c_sz, [c_i64]),
     "fgb_pcg_sell_f64": (c_i32, [ctypes.c_void_p, c_vp, c_vp, c_vp, c_dbl, c_dbl, c_i64, c_i32, c_i32, c_i32, c_i32,
                                  c_vp, c_sz, ctypes.POINTER(PcgInfo), c_vp]),
+    "fgb_sell_set_pipeline": (None, [c_i32]),
     "fgb_pcg_sell_mixed": (c_i32, [ctypes.c_void_p, c_vp, c_vp, c_vp, c_dbl, c_dbl, c_i64, c_i32, c_i32, c_i32,
                                    c_vp, c_sz, ctypes.POINTER(PcgInfo), c_vp]),
     "fgb_pcg_sell_mixed_ex": (c_i32, [ctypes.c_void_p, c_vp, c_vp, c_vp, c_dbl, c_dbl, c_i64, c_i32, c_i32, c_i32,

@@ -511,6 +511,194 @@ __global__ void __launch_bounds__(1024, 1) sell_pcg_spmv(SellView A, const T* __
   }
 }
 
+// ------------------------------------------------ pipelined FP32 SpMV (15-bit steps)
+// A warp of the one-trip-at-a-time SpMV alternates between waiting for a
+// trip's matrix packs and waiting for that trip's gathers; while it gathers,
+// none of its matrix loads are in flight, and with the bytes in flight per SM
+// capped by the register file, HBM sees each SM's loads only part of the
+// time.  This kernel keeps one trip (four packs) in registers and issues the
+// next trip's loads, from the same slice or the first trip of the warp's next
+// slice (whose bounds, slot map and first columns are loaded one slice
+// ahead), before it decodes and gathers the current one.  Every row is summed
+// in the same order as slice_row.  Launched as one wave of three 256-thread
+// blocks per SM (measured on the P2 64^3 system, 59.7 M stored entries:
+// 71.8 us per SpMV against 78-80 us; two-pack trips at four blocks per SM
+// 72.0 us, six-pack trips at two blocks 83.5 us, variants held to fewer
+// registers spill and run at 84-123 us).
+constexpr int kPipeU = 4;
+constexpr int kPipeThreads = 256;
+constexpr int kPipeBlocksPerSM = 3;
+
+struct PipeMeta {
+  int64_t lo;
+  int nq;  // packs per row
+  int32_t row, c0;
+};
+
+__device__ __forceinline__ PipeMeta pipe_meta(const SellView& A, int64_t s, int lane) {
+  PipeMeta m{0, 0, -1, 0};
+  if (s < A.n_slices) {
+    const int64_t lo = A.slice_ptr[s], hi = A.slice_ptr[s + 1];
+    m.lo = lo;
+    m.nq = static_cast<int>((hi - lo) >> 7);  // entries / (32 rows x 4 per pack)
+    m.row = A.perm[s * kSellC + lane];
+    m.c0 = A.col0[s * kSellC + lane];
+  }
+  return m;
+}
+
+__device__ __forceinline__ void pipe_load(const uint16_t* __restrict__ d16, const float* __restrict__ val,
+                                          int64_t sbase, int q0, int nq, int lane, Pack4FH (&a)[kPipeU]) {
+#pragma unroll
+  for (int u = 0; u < kPipeU; ++u) {
+    if (q0 + u < nq) a[u] = load_pack_d16(d16, val, sbase, lane, q0 + u);
+    else a[u] = Pack4FH{};
+  }
+}
+
+// Row epilogues: the PCG product (Ap and the p.Ap partial), a plain product,
+// and a smoother sweep (as sell_smooth_kernel).
+struct PipePcg {
+  static constexpr bool kPap = true;
+  const float* __restrict__ p;
+  float* __restrict__ Ap;
+  __device__ __forceinline__ void row(int32_t r, float acc, float& pap) const {
+    Ap[r] = acc;
+    pap += p[r] * acc;
+  }
+};
+struct PipePlain {
+  static constexpr bool kPap = false;
+  float* __restrict__ y;
+  __device__ __forceinline__ void row(int32_t r, float acc, float&) const { y[r] = acc; }
+};
+struct PipeSmooth {
+  static constexpr bool kPap = false;
+  const float* __restrict__ dinv;
+  const float* __restrict__ rhs;
+  const float* __restrict__ x_in;
+  float* __restrict__ x_out;
+  float* __restrict__ d;
+  float c1, c2;
+  int mode;
+  __device__ __forceinline__ void row(int32_t r, float acc, float&) const {
+    const float res = rhs[r] - acc;
+    if (mode) {
+      x_out[r] = res;
+    } else {
+      const float di = (c1 != 0.0f ? c1 * d[r] : 0.0f) + c2 * dinv[r] * res;
+      d[r] = di;
+      x_out[r] = x_in[r] + di;
+    }
+  }
+};
+
+// x: the gathered vector; bpart/st only for the PCG epilogue (st->done ends
+// the launch at once, as in sell_pcg_spmv)
+template <typename Epi>
+__global__ void __launch_bounds__(kPipeThreads, kPipeBlocksPerSM) sell_d15_pipe(SellView A,
+                                                                              const float* __restrict__ val,
+                                                                              const float* __restrict__ x, Epi epi,
+                                                                              double* bpart,
+                                                                              const SellPcgState* st) {
+  __shared__ double wslot[32];
+  __shared__ unsigned int arrivals;
+  if constexpr (Epi::kPap) {
+    if (threadIdx.x == 0) arrivals = 0u;
+    __syncthreads();
+    if (st->done) return;
+  }
+  const int lane = threadIdx.x & 31;
+  const int64_t warp0 = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
+  const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+  const GatherX<float> g{x};
+  float pap = 0.0f;
+  int64_t s = warp0;
+  PipeMeta cur = pipe_meta(A, s, lane);
+  PipeMeta nxt = pipe_meta(A, s + nwarps, lane);
+  Pack4FH a[kPipeU];
+  pipe_load(A.col16, val, cur.lo, 0, cur.nq, lane, a);
+  int q = 0;
+  float acc = 0.0f;
+  int32_t c = cur.c0;
+  while (s < A.n_slices) {
+    const bool same = q + kPipeU < cur.nq;
+    Pack4FH b[kPipeU];
+    if (same) pipe_load(A.col16, val, cur.lo, q + kPipeU, cur.nq, lane, b);
+    else pipe_load(A.col16, val, nxt.lo, 0, nxt.nq, lane, b);  // nq = 0 past the last slice: no loads
+    int4 cc[kPipeU];
+    int32_t tot[kPipeU];
+#pragma unroll
+    for (int u = 0; u < kPipeU; ++u) cc[u] = pack_cols_d15(a[u].d, 0, tot[u]);
+    int32_t base = c;
+#pragma unroll
+    for (int u = 0; u < kPipeU; ++u) {
+      const int4 k = make_int4(cc[u].x + base, cc[u].y + base, cc[u].z + base, cc[u].w + base);
+      if (q + u < cur.nq) acc = pack_dot_cols<float>(a[u], k, g, acc);
+      base += tot[u];
+    }
+    c = base;
+    if (same) {
+      q += kPipeU;
+    } else {
+      if (cur.row >= 0) epi.row(cur.row, acc, pap);
+      s += nwarps;
+      q = 0;
+      acc = 0.0f;
+      cur = nxt;
+      c = cur.c0;
+      nxt = pipe_meta(A, s + nwarps, lane);
+    }
+#pragma unroll
+    for (int u = 0; u < kPipeU; ++u) a[u] = b[u];
+  }
+  if constexpr (Epi::kPap) {
+    pap = warp_sum(pap);
+    if (lane == 0) {
+      const unsigned int nw = blockDim.x >> 5;
+      wslot[threadIdx.x >> 5] = static_cast<double>(pap);
+      __threadfence_block();
+      if (atomicAdd(&arrivals, 1u) == nw - 1) {
+        __threadfence_block();
+        const volatile double* ws = wslot;
+        double t = 0.0;
+        for (unsigned int k = 0; k < nw; ++k) t += ws[k];
+        bpart[blockIdx.x] = t;
+      }
+    }
+  }
+}
+
+// the pipelined kernel serves FP32 products of 15-bit-step copies unless the
+// process-wide switch (fgb_sell_set_pipeline) selects the one-trip kernels
+int g_sell_pipe = 1;
+
+inline bool use_pipe(const SellView& A) { return g_sell_pipe && A.col16 && A.d15 && !A.node_triples; }
+
+// blocks of one wave (the PCG epilogue writes one p.Ap partial per block)
+template <typename Epi>
+int pipe_grid() {
+  static int grid = 0;
+  if (grid == 0) {
+    int dev = 0, sms = kNumSMs, per_sm = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sell_d15_pipe<Epi>, kPipeThreads, 0) != cudaSuccess ||
+        per_sm < 1)
+      per_sm = 1;
+    const int gr = per_sm * sms;
+    grid = gr < kSellMaxBlocks ? gr : kSellMaxBlocks;
+  }
+  return grid;
+}
+
+template <typename Epi>
+int pipe_launch(const SellView& A, const float* val, const float* x, const Epi& epi, double* bpart,
+                const SellPcgState* st, cudaStream_t s) {
+  const int grid = pipe_grid<Epi>();
+  sell_d15_pipe<Epi><<<grid, kPipeThreads, 0, s>>>(A, val, x, epi, bpart, st);
+  return grid;
+}
+
 // ||b|| (mixed solver set-up); marks a zero right-hand side
 __global__ void __launch_bounds__(1024, 1) sell_bnorm(int64_t n, const double* __restrict__ b, double* partials,
                                                            SellPcgState* st) {
@@ -1203,11 +1391,16 @@ void mixed_body(const SellView& A, const float* val32, const double* val64, cons
   rec(ev, 0, s);
   sell_p_update_f32<<<VEC_LAUNCH(A.n, s)>>>(A.n, w.z, p, w.st);
   rec(ev, 1, s);
-  with_cols(A, [&](auto d16) {
-    sell_pcg_spmv<float, decltype(d16)::value><<<SLICE_LAUNCH(A, s)>>>(A, val32, p, w.Ap, w.bpart, w.st);
-  });
+  int nwp = slice_blocks(A);
+  if (use_pipe(A)) {
+    nwp = pipe_launch(A, val32, p, PipePcg{p, w.Ap}, w.bpart, w.st, s);
+  } else {
+    with_cols(A, [&](auto d16) {
+      sell_pcg_spmv<float, decltype(d16)::value><<<SLICE_LAUNCH(A, s)>>>(A, val32, p, w.Ap, w.bpart, w.st);
+    });
+  }
   rec(ev, 2, s);
-  sell_mixed_update<<<VEC_LAUNCH(A.n, s)>>>(A.n, w.dinv32, p, w.Ap, w.y, w.r, w.z, w.bpart, slice_blocks(A),
+  sell_mixed_update<<<VEC_LAUNCH(A.n, s)>>>(A.n, w.dinv32, p, w.Ap, w.y, w.r, w.z, w.bpart, nwp,
                                             w.partials, w.st, delta, hif, ctx ? 1 : 0);
   rec(ev, 3, s);
   auto reliable = [&](cudaStream_t rs) {
@@ -1331,6 +1524,10 @@ int sell_smooth_f32(const fgb_sell* A, const float* dinv, const float* r, const 
                     float c1, float c2, int mode, cudaStream_t st) {
   if (!A || !A->val32 || !launch_ok(A) || !r || !x_in || !x_out || (mode == 0 && (!dinv || !d))) return FGB_ERR_ARG;
   const SellView V = view_of(A);
+  if (use_pipe(V)) {
+    pipe_launch(V, A->val32, x_in, PipeSmooth{dinv, r, x_in, x_out, d, c1, c2, mode}, nullptr, nullptr, st);
+    return FGB_OK;
+  }
   with_cols(V, [&](auto f) {
     constexpr int FMT = decltype(f)::value;
     sell_smooth_kernel<FMT, float><<<SLICE_LAUNCH(V, st)>>>(V, A->val32, dinv, r, x_in, x_out, d, c1, c2, mode);
@@ -1414,10 +1611,14 @@ int32_t fgb_sell_spmv(int32_t dtype, const fgb_sell* A, const void* x, void* y, 
     });
   } else if (dtype == FGB_F32) {
     if (!A->val32) return FGB_ERR_ARG;
-    with_cols(v, [&](auto d16) {
-      sell_spmv_kernel<float, decltype(d16)::value>
-          <<<SLICE_LAUNCH(v, st)>>>(v, A->val32, static_cast<const float*>(x), static_cast<float*>(y));
-    });
+    if (use_pipe(v)) {
+      pipe_launch(v, A->val32, static_cast<const float*>(x), PipePlain{static_cast<float*>(y)}, nullptr, nullptr, st);
+    } else {
+      with_cols(v, [&](auto d16) {
+        sell_spmv_kernel<float, decltype(d16)::value>
+            <<<SLICE_LAUNCH(v, st)>>>(v, A->val32, static_cast<const float*>(x), static_cast<float*>(y));
+      });
+    }
   } else {
     return FGB_ERR_ARG;
   }
@@ -1505,6 +1706,8 @@ int32_t fgb_pcg_sell_f64(const fgb_sell* A, const double* diag_inv, const double
   }
   return finish(h.done);
 }
+
+void fgb_sell_set_pipeline(int32_t enable) { g_sell_pipe = enable ? 1 : 0; }
 
 int32_t fgb_pcg_sell_mixed(const fgb_sell* A, const double* diag_inv64, const double* b, double* x, double rtol,
                            double delta, int64_t maxit, int32_t check_every, int32_t use_graph, int32_t profile,

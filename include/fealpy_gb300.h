@@ -539,6 +539,12 @@ int32_t fgb_pcg_sell_f64(const fgb_sell* A, const double* diag_inv, const double
                          double atol, double rtol, int64_t maxit, int32_t check_every,
                          int32_t norm, int32_t use_graph, int32_t profile, void* workspace,
                          size_t workspace_bytes, fgb_pcg_info* info_host, void* stream);
+/* Process-wide switch for the FP32 products on 15-bit-step copies
+ * (fgb_pcg_sell_mixed's SpMV, fgb_sell_spmv, the multigrid smoother): 1
+ * (default) runs the pipelined kernel, which loads a warp's next trip of
+ * packs before it gathers the current one; 0 runs the one-trip kernels.
+ * Every row is the same sum in the same order either way. */
+void fgb_sell_set_pipeline(int32_t enable);
 int32_t fgb_pcg_sell_mixed(const fgb_sell* A, const double* diag_inv64, const double* b,
                            double* x, double rtol, double delta, int64_t maxit,
                            int32_t check_every, int32_t use_graph, int32_t profile,

@@ -329,3 +329,57 @@ def test_d15_solvers_match_the_four_byte_copy(golden_dir):
         assert abs(out[True][1] - out[False][1]) <= 2, (name, out[True][1], out[False][1])
         assert rel_err(out[True][0], out[False][0].cpu().numpy()) < 1e-9, name
 
+
+def test_d15_pipelined_kernels_match_one_trip_kernels(golden_dir):
+    """FP32 products of 15-bit copies run in the pipelined kernel (a warp
+    loads its next trip of packs before it gathers the current one) unless
+    switched off: its products equal the one-trip kernel's bit for bit (every
+    row is the same sum in the same order), on the C2-law matrix and on a
+    matrix with long steps, rows wider than a trip and empty rows; the
+    FP32-refined solves agree (the p.Ap partials are grouped by the blocks of
+    another launch shape: iterations within 2, solutions within 1e-9)."""
+    dev = cuda()
+    import scipy.sparse as sp
+    import fealpy_gb300 as F
+    from fealpy_gb300 import _lib, kernels as K
+    from fealpy_gb300 import solver as SV
+    z = np.load(os.path.join(golden_dir, "cfg_c2_tet_p2_8.npz"))
+    n0 = len(z["bc_crow"]) - 1
+    c2 = sp.csr_matrix((z["bc_val"], z["bc_col"], z["bc_crow"]), shape=(n0, n0))
+    wide = _spd(200_000, list(range(2, 30)) + [40_000, 1_000_000 % 200_000 + 7], seed=4).tocoo()
+    empty = np.array([3, 64, 199_990])
+    keep = ~(np.isin(wide.row, empty) | np.isin(wide.col, empty))
+    wide = sp.csr_matrix((wide.data[keep], (wide.row[keep], wide.col[keep])), shape=wide.shape)
+    wide.sort_indices()
+    lib = _lib.lib()
+    try:
+        for name, A_np in (("c2", c2), ("wide", wide)):
+            S = _build_d15(A_np, dev)
+            xs = torch.as_tensor(np.random.default_rng(2).normal(size=A_np.shape[0]), device=dev,
+                                 dtype=torch.float32)
+            lib.fgb_sell_set_pipeline(1)
+            y1 = K.sell_spmv(S, xs, torch.float32)
+            lib.fgb_sell_set_pipeline(0)
+            y0 = K.sell_spmv(S, xs, torch.float32)
+            assert torch.equal(y1, y0), name
+            if name == "wide":
+                continue
+            b = torch.as_tensor(z["bc_F"] if "bc_F" in z else z["F"], device=dev)
+            out = {}
+            for pipe in (1, 0):
+                lib.fgb_sell_set_pipeline(pipe)
+                A = F.CSRTensor(torch.as_tensor(z["bc_crow"], device=dev), torch.as_tensor(z["bc_col"], device=dev),
+                                torch.as_tensor(z["bc_val"], device=dev), (n0, n0))
+                saved = SV.SELL_D15
+                SV.SELL_D15 = True
+                try:
+                    x, info = F.cg_mixed(A, b, rtol=1e-10, returninfo=True, graph=False)
+                finally:
+                    SV.SELL_D15 = saved
+                assert info["relres"] <= 1e-10 and rel_err(x, z["uh"]) < 1e-8, (pipe, info)
+                out[pipe] = (x, info["niter"])
+            assert abs(out[1][1] - out[0][1]) <= 2
+            assert rel_err(out[1][0], out[0][0].cpu().numpy()) < 1e-9
+    finally:
+        lib.fgb_sell_set_pipeline(1)
+
