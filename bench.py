@@ -309,8 +309,10 @@ def spmv_roofline(mixed, gdof, n, peak, peak_kind):
             traffic = None
     return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak if peak else None, "traffic": traffic,
-            "kernel": "sell_pcg_spmv<float> (SELL-32" + {"d16": ", 16-bit column steps", "d15": ", 15-bit column "
-                      "steps"}.get(cols, "") + "; Ap = A p and p.Ap)",
+            "kernel": ("sell_d15_pipe<PipePcg> (SELL-32, 15-bit column steps, next trip loaded before the "
+                       "current one is gathered; Ap = A p and p.Ap)" if cols == "d15" else
+                       "sell_pcg_spmv<float> (SELL-32" + {"d16": ", 16-bit column steps"}.get(cols, "") +
+                       "; Ap = A p and p.Ap)"),
             "algorithmic_bytes_per_launch": bytes_per_launch, "avg_launch_ms": mixed["kernel_ms_avg"],
             "bytes_with_4_byte_columns": nnz * (4 + 4) + gdof * (8 + 8),
             "peak_source": peak_kind,
