@@ -80,7 +80,7 @@ class GAMGSolver:
 
     def __init__(self, theta: float = 0.0, csize: int = 300, ctype: str = "A", itype: str = "T", ptype: str = "V",
                  sstep: int = 3, isolver: str = "CG", maxit: int = 200, csolver: str = "chebyshev",
-                 rtol: float = 1e-8, atol: float = 1e-8, omega: float = 1.7, cdeg: int = 8, max_levels: int = 10,
+                 rtol: float = 1e-8, atol: float = 1e-8, omega: float = 1.7, cdeg: int = 16, max_levels: int = 10,
                  vcycle_f32: bool = True, sell_min_rows: int = 1 << 16, block_size: int = 1):
         if ptype != "V":
             raise NotImplementedError("the GB300 multigrid provides V-cycles")

@@ -691,10 +691,16 @@ int pipe_grid() {
   return grid;
 }
 
+// One wave at most, and at least two slices per warp: a small matrix (a
+// multigrid level, a system solved beside others on its own stream) leaves
+// the rest of the GPU to concurrent work.
 template <typename Epi>
 int pipe_launch(const SellView& A, const float* val, const float* x, const Epi& epi, double* bpart,
                 const SellPcgState* st, cudaStream_t s) {
-  const int grid = pipe_grid<Epi>();
+  constexpr int64_t kSlicesPerBlock = 2 * (kPipeThreads / 32);
+  const int64_t want = (A.n_slices + kSlicesPerBlock - 1) / kSlicesPerBlock;
+  const int wave = pipe_grid<Epi>();
+  const int grid = static_cast<int>(want < 1 ? 1 : (want < wave ? want : wave));
   sell_d15_pipe<Epi><<<grid, kPipeThreads, 0, s>>>(A, val, x, epi, bpart, st);
   return grid;
 }

@@ -304,9 +304,11 @@ def test_d15_solvers_match_the_four_byte_copy(golden_dir):
     """cg_mixed on the 15-bit copy (the default for FP32 copies) against the
     same solve on the 4-byte copy: every row's product is the same sum in the
     same order (a long-step entry adds an exact zero), but the rows sit in
-    other slots (their lengths differ), so the dot products add their terms
-    in another order: the same iterations within 2, solutions within 1e-9,
-    and the reference's solution."""
+    other slots (their lengths differ) and the kernels' launch shapes group
+    the p.Ap partials differently, so the FP32 dot products round
+    differently: FP32 iteration counts of these small systems move by a few
+    percent with such rounding, so the counts agree within 10% (and 2),
+    solutions within 1e-9, and both meet the reference's solution."""
     dev = cuda()
     import fealpy_gb300 as F
     from fealpy_gb300 import solver as SV
@@ -326,7 +328,7 @@ def test_d15_solvers_match_the_four_byte_copy(golden_dir):
                 SV.SELL_D15 = saved
             assert info["relres"] <= 1e-10 and rel_err(x, z["uh"]) < 1e-8, (name, d15, info)
             out[d15] = (x, info["niter"])
-        assert abs(out[True][1] - out[False][1]) <= 2, (name, out[True][1], out[False][1])
+        assert abs(out[True][1] - out[False][1]) <= max(2, out[False][1] // 10), (name, out[True][1], out[False][1])
         assert rel_err(out[True][0], out[False][0].cpu().numpy()) < 1e-9, name
 
 
@@ -337,7 +339,7 @@ def test_d15_pipelined_kernels_match_one_trip_kernels(golden_dir):
     row is the same sum in the same order), on the C2-law matrix and on a
     matrix with long steps, rows wider than a trip and empty rows; the
     FP32-refined solves agree (the p.Ap partials are grouped by the blocks of
-    another launch shape: iterations within 2, solutions within 1e-9)."""
+    another launch shape: iterations within 10%, solutions within 1e-9)."""
     dev = cuda()
     import scipy.sparse as sp
     import fealpy_gb300 as F
@@ -378,7 +380,7 @@ def test_d15_pipelined_kernels_match_one_trip_kernels(golden_dir):
                     SV.SELL_D15 = saved
                 assert info["relres"] <= 1e-10 and rel_err(x, z["uh"]) < 1e-8, (pipe, info)
                 out[pipe] = (x, info["niter"])
-            assert abs(out[1][1] - out[0][1]) <= 2
+            assert abs(out[1][1] - out[0][1]) <= max(2, out[0][1] // 10)
             assert rel_err(out[1][0], out[0][0].cpu().numpy()) < 1e-9
     finally:
         lib.fgb_sell_set_pipeline(1)
