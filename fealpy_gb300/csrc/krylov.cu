@@ -634,6 +634,64 @@ int run_pcg_mixed(int64_t n, const int64_t* indptr, const int32_t* indices, cons
 
 }  // namespace
 
+namespace fgb {
+
+constexpr int kResBlocks = 2 * kNumSMs;
+constexpr int kResThreads = 512;
+
+// per block: sum of r_i^2 over its rows (a warp per row, rows strided over
+// the grid's warps) and of b_i^2, in double2 partials [2 * block]
+__global__ void __launch_bounds__(kResThreads) residual_partials(int64_t n, const int64_t* __restrict__ indptr,
+                                                               const int32_t* __restrict__ indices,
+                                                               const double* __restrict__ values,
+                                                               const double* __restrict__ b,
+                                                               const double* __restrict__ x, double* part) {
+  __shared__ double2 ws[kResThreads / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int64_t warp = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
+  const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+  double rr = 0.0, bb = 0.0;
+  for (int64_t i = warp; i < n; i += nwarps) {
+    double acc = 0.0;
+    for (int64_t k = indptr[i] + lane; k < indptr[i + 1]; k += 32) acc += values[k] * x[indices[k]];
+    acc = warp_sum(acc);
+    if (lane == 0) {
+      const double ri = b[i] - acc;
+      rr += ri * ri;
+      bb += b[i] * b[i];
+    }
+  }
+  if (lane == 0) ws[wid] = make_double2(rr, bb);
+  __syncthreads();
+  if (wid == 0) {
+    double2 t = lane < kResThreads / 32 ? ws[lane] : make_double2(0.0, 0.0);
+    t.x = warp_sum(t.x);
+    t.y = warp_sum(t.y);
+    if (lane == 0) {
+      part[2 * blockIdx.x] = t.x;
+      part[2 * blockIdx.x + 1] = t.y;
+    }
+  }
+}
+
+// one warp: the partials in block order -> out2[0] = ||r||^2, out2[1] = ||b||^2
+__global__ void residual_total(const double* __restrict__ part, double* out2) {
+  const int lane = threadIdx.x;
+  double a = 0.0, c = 0.0;
+  for (int k = lane; k < kResBlocks; k += 32) {
+    a += part[2 * k];
+    c += part[2 * k + 1];
+  }
+  a = warp_sum(a);
+  c = warp_sum(c);
+  if (lane == 0) {
+    out2[0] = a;
+    out2[1] = c;
+  }
+}
+
+}  // namespace fgb
+
 extern "C" {
 
 const char* fgb_status_string(int32_t status) {
@@ -673,6 +731,25 @@ int32_t fgb_csr_spmv(int32_t dtype, int64_t n_row, const int64_t* indptr, const 
     return spmv_dispatch<float>(n_row, indptr, indices, static_cast<const float*>(values),
                                 static_cast<const float*>(x), static_cast<float*>(y), lanes, as_stream(stream));
   return FGB_ERR_ARG;
+}
+
+// two partial sums (r.r, b.b) per block of residual_partials
+size_t fgb_residual_norm_workspace_bytes(void) { return align_up(2 * kResBlocks * sizeof(double)); }
+
+// ||b - A x||^2 and ||b||^2 (FP64 values, vectors and sums): a warp per row
+// forms r_i = b_i - (A x)_i, every block writes its partial sums, one block
+// adds the partials in block order (deterministic).  The true residual of
+// the restart loops of cg_mixed's FP64 continuation and of multigrid_solve.
+int32_t fgb_residual_norm(int64_t n, const int64_t* indptr, const int32_t* indices, const double* values,
+                          const double* b, const double* x, double* out2, void* workspace, size_t workspace_bytes,
+                          void* stream) {
+  if (n <= 0 || !indptr || !indices || !values || !b || !x || !out2) return FGB_ERR_ARG;
+  if (!workspace || workspace_bytes < fgb_residual_norm_workspace_bytes()) return FGB_ERR_WORKSPACE;
+  cudaStream_t st = as_stream(stream);
+  double* part = static_cast<double*>(workspace);
+  residual_partials<<<kResBlocks, kResThreads, 0, st>>>(n, indptr, indices, values, b, x, part);
+  residual_total<<<1, 32, 0, st>>>(part, out2);
+  return launch_status();
 }
 
 int32_t fgb_csr_diagonal(int32_t dtype, int64_t n, const int64_t* indptr, const int32_t* indices, const void* values,

@@ -464,6 +464,11 @@ class VectorSourceIntegrator(Integrator):
         self.set_region(region)
 
     def assembly(self, space, /, indices=None) -> torch.Tensor:
+        """Cell vectors (NC, ldof * GD): per component the scalar source
+        kernel (``fgb_source_local``; a constant component as a number, a
+        callable's values per quadrature point, a (NC, GD) tensor per cell),
+        laid out as the space numbers its components (interleaved or
+        component-major), as ``fealpy/fem/vector_source_integrator.py`` does."""
         self._check_region()
         ss = space.scalar_space
         mesh = ss.mesh
@@ -473,15 +478,30 @@ class VectorSourceIntegrator(Integrator):
         cells = self.cell_selection(mesh)
         index = _S if cells is None else cells
         cm = mesh.entity_measure("cell", index=index)
-        phi = torch.as_tensor(sx.shape_function(bcs, ss.p), device=mesh.device)
-        w = torch.as_tensor(ws, device=mesh.device)
+        NC = cm.shape[0]
+        wphi_np = ws[:, None] * sx.shape_function(bcs, ss.p)                       # (NQ, ldof)
+        wphi = torch.as_tensor(wphi_np, dtype=torch.float64, device=mesh.device).contiguous()
+        sv = torch.as_tensor(wphi_np.sum(axis=0), dtype=torch.float64, device=mesh.device)
+        ldof = ss.number_of_local_dofs()
         f = self.source
+        comps = []
         if callable(f):
-            f = _source_values(f, mesh, bcs, index)               # (NC, NQ, gd)
+            fq = torch.broadcast_to(_source_values(f, mesh, bcs, index), (NC, len(ws), gd))
+            for d in range(gd):
+                comps.append(K.source_local(cm, 2, 0.0, fq[..., d].contiguous(), wphi, sv, ldof))
         else:
-            f = torch.as_tensor(f, dtype=torch.float64, device=mesh.device).reshape(1, 1, gd)
-            f = f.expand(cm.shape[0], len(ws), gd)
-        loc = torch.einsum("c,q,qi,cqd->cid", cm, w, phi, f)       # (NC, ldof, gd)
+            ft = torch.as_tensor(f, dtype=torch.float64)
+            if ft.ndim == 2 and ft.shape == (NC, gd):
+                ft = ft.to(mesh.device)
+                for d in range(gd):
+                    comps.append(K.source_local(cm, 1, 0.0, ft[:, d].contiguous(), wphi, sv, ldof))
+            else:
+                fv = ft.reshape(-1).cpu().tolist()
+                if len(fv) != gd:
+                    raise ValueError(f"a constant vector source needs {gd} components")
+                for d in range(gd):
+                    comps.append(K.source_local(cm, 0, float(fv[d]), None, wphi, sv, ldof))
+        loc = torch.stack(comps, dim=-1)                                           # (NC, ldof, gd)
         if space.dof_priority:
             loc = loc.transpose(1, 2)
-        return loc.reshape(loc.shape[0], -1)
+        return loc.reshape(NC, -1)

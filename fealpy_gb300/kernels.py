@@ -282,6 +282,23 @@ def csr_spmv(indptr, indices, values, x, lanes: int = 0, out: Optional[torch.Ten
     return y
 
 
+def residual_norm(indptr, indices, values, b, x):
+    """(||b - A x||, ||b||) of an FP64 CSR matrix, formed on the device in one
+    pass (``fgb_residual_norm``); one host read of the two sums."""
+    dev = _dev(indptr)
+    n = indptr.numel() - 1
+    vals = values.to(torch.float64).contiguous()
+    bd = b.to(dev, torch.float64).contiguous()
+    xd = x.to(dev, torch.float64).contiguous()
+    out = torch.empty(2, dtype=torch.float64, device=dev)
+    lib = _lib.lib()
+    ws = workspace(lib.fgb_residual_norm_workspace_bytes(), dev)
+    call("fgb_residual_norm", n, ptr(indptr), ptr(indices), ptr(vals), ptr(bd), ptr(xd), ptr(out), ptr(ws),
+         ws.numel(), stream_ptr(dev))
+    rr, bb = out.cpu().tolist()
+    return rr ** 0.5, bb ** 0.5
+
+
 def csr_diagonal(indptr, indices, values):
     dev = _dev(indptr)
     n = indptr.numel() - 1

@@ -219,8 +219,7 @@ def cg_mixed(A: CSRTensor, b: torch.Tensor, x0: Optional[torch.Tensor] = None, M
         dinv64 = dinv if dinv is not None else A.diagonal_inverse().to(torch.float64)
         M64 = CSRTensor(torch.arange(A.shape[0] + 1, device=x.device), torch.arange(A.shape[0], device=x.device,
                         dtype=torch.int32), dinv64, A.shape)
-        Ad = CSRTensor(A.crow, A.col, A.values.to(torch.float64), A.shape)
-        bn = float(torch.linalg.norm(b))
+        vals64 = A.values.to(torch.float64)
         left, its, rel, reason = max(maxit - int(info.niter), 1), 0, float(info.true_relres), 3
         # FP64 PCG restarted from the current iterate until the true residual
         # (formed in FP64) meets rtol; each restart re-forms r = b - A x, so the
@@ -230,7 +229,8 @@ def cg_mixed(A: CSRTensor, b: torch.Tensor, x0: Optional[torch.Tensor] = None, M
                         graph=graph)
             its += i64["niter"]
             left -= i64["niter"]
-            new = float(torch.linalg.norm(b - Ad @ x)) / bn
+            res, bn = K.residual_norm(A.crow, A.col, vals64, b, x)
+            new = res / bn if bn > 0 else 0.0
             if new <= rtol:
                 rel, reason = new, 2
                 break

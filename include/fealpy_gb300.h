@@ -336,6 +336,16 @@ int32_t fgb_csr_spmv(int32_t dtype, int64_t n_row, const int64_t* indptr, const 
                      const void* values, const void* x, void* y, int32_t lanes_per_row,
                      void* stream);
 
+/* out2[0] = ||b - A x||^2, out2[1] = ||b||^2 (FP64 CSR, device scalars,
+ * deterministic): the true residual of FEALPy's stopping test
+ * (fealpy/solver/cg.py:99-113) as the restart loops of the FP32-refined
+ * solver's FP64 continuation and of the multigrid solve form it.  workspace:
+ * fgb_residual_norm_workspace_bytes() bytes of device memory. */
+size_t fgb_residual_norm_workspace_bytes(void);
+int32_t fgb_residual_norm(int64_t n, const int64_t* indptr, const int32_t* indices,
+                          const double* values, const double* b, const double* x, double* out2,
+                          void* workspace, size_t workspace_bytes, void* stream);
+
 /* diag(A) and 1/diag(A) (CSRTensor.diags + JacobiPreconditioner.apply,
  * fealpy/sparse/csr_tensor.py:467-475, fealpy/solver/iterative_solver_manger.py:
  * 273-280).  A missing diagonal yields 0 and 1/0 = inf, as in FEALPy. */

@@ -425,3 +425,22 @@ def test_elasticity_fp32_assembly_and_refined_solve(golden_dir):
     rel = float(torch.linalg.norm(f.double() - Bd @ x) / torch.linalg.norm(f.double()))
     assert info["reason"] == 2 and rel <= 1e-10 * 1.0001, (info, rel)
     assert rel_err(x, z["uh"]) < 1e-4
+
+
+def test_residual_norm_kernel_matches_numpy(golden_dir):
+    """fgb_residual_norm (the true residual of the restart loops): ||b - A x||
+    and ||b|| against numpy on a FEALPy matrix, deterministic across calls."""
+    dev = cuda()
+    import scipy.sparse as sp
+    from fealpy_gb300 import kernels as K
+    z = load(golden_dir, "cfg_c2_tet_p2_8.npz")
+    n = len(z["bc_crow"]) - 1
+    A = sp.csr_matrix((z["bc_val"], z["bc_col"], z["bc_crow"]), shape=(n, n))
+    rng = np.random.default_rng(11)
+    x, b = rng.normal(size=n), rng.normal(size=n)
+    t = lambda a: torch.as_tensor(a, device=dev)
+    r1, b1 = K.residual_norm(t(z["bc_crow"]), t(z["bc_col"]), t(z["bc_val"]), t(b), t(x))
+    r2, b2 = K.residual_norm(t(z["bc_crow"]), t(z["bc_col"]), t(z["bc_val"]), t(b), t(x))
+    assert (r1, b1) == (r2, b2)
+    assert abs(r1 - np.linalg.norm(b - A @ x)) <= 1e-12 * np.linalg.norm(b - A @ x)
+    assert abs(b1 - np.linalg.norm(b)) <= 1e-13 * np.linalg.norm(b)
