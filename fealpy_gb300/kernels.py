@@ -322,7 +322,7 @@ def pcg_f64(indptr, indices, values, dinv, b, x, atol, rtol, maxit, check_every=
     return info
 
 
-def pcg_mixed(indptr, indices, values64, values32, dinv64, b, x, rtol, delta=0.1, maxit=100000, check_every=32,
+def pcg_mixed(indptr, indices, values64, values32, dinv64, b, x, rtol, delta=0.2, maxit=100000, check_every=32,
               lanes=0, profile=False):
     dev = _dev(indptr)
     n = indptr.numel() - 1
@@ -737,7 +737,7 @@ def pcg_sell_f64(S: SellMatrix, dinv, b, x, atol, rtol, maxit, check_every=16, n
     return info
 
 
-def pcg_sell_mixed(S: SellMatrix, dinv64, b, x, rtol, delta=0.1, maxit=100000, check_every=32, graph=True,
+def pcg_sell_mixed(S: SellMatrix, dinv64, b, x, rtol, delta=0.2, maxit=100000, check_every=32, graph=True,
                    profile=False, barrier_polls=0):
     """FP32 Jacobi-PCG with FP64 reliable updates on the SELL copy; dinv64, b
     and x (updated in place) in the matrix's own numbering.  ``graph``: 0

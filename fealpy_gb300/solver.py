@@ -179,7 +179,7 @@ def cg(A, b: torch.Tensor, x0: Optional[torch.Tensor] = None, M=None, *, batch_f
 
 
 def cg_mixed(A: CSRTensor, b: torch.Tensor, x0: Optional[torch.Tensor] = None, M=None, *, rtol: float = 1e-10,
-             delta: float = 0.1, maxit: int = 100000, returninfo: bool = False, check_every: int = 32,
+             delta: float = 0.2, maxit: int = 100000, returninfo: bool = False, check_every: int = 32,
              lanes_per_row: int = 0, profile: bool = False, solver_format: str = "sell", graph: bool = True):
     """FP32 Jacobi-PCG iterations with FP64 reliable updates; stops on the true
     relative residual computed in FP64 arithmetic.  ``M`` must be None (Jacobi
