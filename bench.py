@@ -255,14 +255,14 @@ def assembly_roofline(rec, NN, NC, ldof, gdof, peak, n_channel=7):
     t_asm = st.get("assembly/factors", 0.0) + t_val
     t_pat = st.get("assembly/adjacency", 0.0) + st.get("assembly/pattern", 0.0)
     out = {}
-    for key, b, t, what in (("assembly", b_asm, t_asm, "cell_factors_kernel + assemble_scalar_kernel<double, 10>"),
+    for key, b, t, what in (("assembly", b_asm, t_asm, "cell_factors_kernel + assemble_scalar_kernel<double, 10, 0>"),
                             ("pattern", b_pat, t_pat, "adjacency build + pattern passes")):
         ach = b / (t / 1e3) / 1e9 if t > 0 else 0.0
         out[key] = {"kernels": what, "bound": "hbm", "algorithmic_bytes": b, "ms": t, "achieved": ach,
                     "unit": "GB/s", "frac": ach / peak if peak else None}
     flops = 2.0 * NC * ldof * ldof * n_channel
     tf = flops / (t_val / 1e3) / 1e12 if t_val > 0 else 0.0
-    out["assembly_fp64"] = {"kernels": "assemble_scalar_kernel<double, 10>", "bound": "fp64",
+    out["assembly_fp64"] = {"kernels": "assemble_scalar_kernel<double, 10, 0>", "bound": "fp64",
                             "algorithmic_flops": flops, "ms": t_val, "achieved": tf, "unit": "TFLOP/s",
                             "peak": FP64_PEAK_TFLOPS, "frac": tf / FP64_PEAK_TFLOPS,
                             "peak_source": "nominal FP64 rate of the part"}
