@@ -2,7 +2,7 @@
 Jacobi-PCG) split over the host's cores, for timing the reference algorithm
 on the full-size bench workload.
 
-TEST AND BASELINE INFRASTRUCTURE ONLY: used by ``bench.py --impl reference``
+TEST INFRASTRUCTURE AND CPU TIMING ONLY: used by ``bench.py --impl reference``
 (the reference arm) and by ``tests/``; the product never imports it.
 
 The work is split by row ranges of the global matrix.  A process takes a range
