@@ -678,16 +678,17 @@ inline bool use_pipe(const SellView& A) { return g_sell_pipe && A.col16 && A.d15
 // blocks of one wave (the PCG epilogue writes one p.Ap partial per block)
 template <typename Epi>
 int pipe_grid() {
-  static int grid = 0;
-  if (grid == 0) {
+  // computed once per process (thread-safe static initialisation: the
+  // serving loop and the multigrid lanes call the solvers from several threads)
+  static const int grid = [] {
     int dev = 0, sms = kNumSMs, per_sm = 0;
     if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sell_d15_pipe<Epi>, kPipeThreads, 0) != cudaSuccess ||
         per_sm < 1)
       per_sm = 1;
     const int gr = per_sm * sms;
-    grid = gr < kSellMaxBlocks ? gr : kSellMaxBlocks;
-  }
+    return gr < kSellMaxBlocks ? gr : kSellMaxBlocks;
+  }();
   return grid;
 }
 
