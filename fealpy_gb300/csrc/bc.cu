@@ -20,10 +20,14 @@ __global__ void dirichlet_count_kernel(int64_t n, const int64_t* __restrict__ in
   const int lane = threadIdx.x & 31;
   const int64_t warp = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
   const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+  // u_bd = NULL: all boundary values zero (homogeneous data), so A uh = 0
+  // and the values need not be read (f_out = f off the boundary, the same
+  // bits as subtracting the zero product)
+  const bool prod = f_out && u_bd;
   for (int64_t i = warp; i < n; i += nwarps) {
     if (is_bd[i]) {
       if (lane == 0) {
-        if (f_out) f_out[i] = u_bd[i];
+        if (f_out) f_out[i] = u_bd ? u_bd[i] : T(0);
         row_nnz[i] = 1;
       }
       continue;
@@ -35,11 +39,11 @@ __global__ void dirichlet_count_kernel(int64_t n, const int64_t* __restrict__ in
     int cnt = 0;
     for (int64_t k = s + lane; k < e; k += 32) {
       const int32_t j = indices[k];
-      if (f_out) acc += values[k] * u_bd[j];
+      if (prod) acc += values[k] * u_bd[j];
       if (!is_bd[j]) ++cnt;
     }
     cnt = warp_sum(cnt);
-    if (f_out) acc = warp_sum(acc);
+    if (prod) acc = warp_sum(acc);
     if (lane == 0) {
       row_nnz[i] = cnt;
       if (f_out) f_out[i] = f[i] - acc;
@@ -95,7 +99,7 @@ int32_t fgb_dirichlet_count(int32_t dtype, int64_t n, const int64_t* indptr, con
                             const void* values, const uint8_t* is_bd, const void* f, const void* u_bd, void* f_out,
                             int32_t* row_nnz, void* stream) {
   if (n <= 0 || !indptr || !indices || !is_bd || !row_nnz) return FGB_ERR_ARG;
-  if (f_out && (!values || !f || !u_bd)) return FGB_ERR_ARG;
+  if (f_out && (!f || (u_bd && !values))) return FGB_ERR_ARG;
   cudaStream_t st = as_stream(stream);
   const int grid = grid_for(n * 32, 256, kNumSMs * 16);
   if (dtype == FGB_F64)

@@ -167,8 +167,8 @@ class BatchAssembler:
                                         torch.as_tensor(g.cell_count, device=dev))
         F = K.source_gather(adj_ptr, adj, g.ldof, cm.contiguous(), 1, 0.0, fcell, g.wphi, g.sv)
         _lib.check_status_word("batched assembly", status)
-        uh = torch.zeros(g.n, dtype=values.dtype, device=dev)
-        bptr, bidx, bval, bF = K.dirichlet_apply(indptr, indices, values, g.is_bd, F.to(values.dtype), uh)
+        # homogeneous boundary data: no u_h (the elimination skips A u_h)
+        bptr, bidx, bval, bF = K.dirichlet_apply(indptr, indices, values, g.is_bd, F.to(values.dtype), None)
         # split into the systems' own CSRs
         nsys = len(g.members)
         iptr_out = torch.empty(g.n + nsys, dtype=torch.int64, device=dev)

@@ -48,9 +48,14 @@ class DirichletBC:
         return vector
 
     def _boundary_values(self, f, uh, gd):
+        """u_h with the boundary values interpolated; None for homogeneous data
+        (``gd`` the number 0 and no ``uh``), which lets the elimination skip
+        the product A u_h (it is zero)."""
         gd = self.gd if gd is None else gd
         if gd is None:
             raise RuntimeError("The boundary condition is None.")
+        if uh is None and isinstance(gd, (int, float)) and float(gd) == 0.0:
+            return None
         if uh is None:
             uh = torch.zeros_like(f)
         uh, _ = self.space.boundary_interpolate(gd=gd, uh=uh, threshold=self.threshold, method=self.method)

@@ -245,7 +245,8 @@ def assemble_elasticity_p1(gd, adj_ptr, adj, cell, factors, node_indptr, node_in
 
 def dirichlet_apply(indptr, indices, values, is_bd: torch.Tensor, f: Optional[torch.Tensor],
                     uh: Optional[torch.Tensor], matrix: bool = True):
-    """Returns (new_indptr, new_indices, new_values, f_new); entries not asked for are None."""
+    """Returns (new_indptr, new_indices, new_values, f_new); entries not asked for are None.
+    ``uh`` None with ``f`` given: all boundary values zero."""
     dev = _dev(indptr)
     n = indptr.numel() - 1
     dt = values.dtype
@@ -255,7 +256,8 @@ def dirichlet_apply(indptr, indices, values, is_bd: torch.Tensor, f: Optional[to
     if f is not None:
         f_out = torch.empty(n, dtype=dt, device=dev)
         f = f.to(dev, dt).contiguous()
-        uh = uh.to(dev, dt).contiguous()
+        # uh None: homogeneous boundary data (the kernel skips A uh)
+        uh = uh.to(dev, dt).contiguous() if uh is not None else None
     call("fgb_dirichlet_count", dtype_code(dt), n, ptr(indptr), ptr(indices), ptr(values), ptr(isb), ptr(f), ptr(uh),
          ptr(f_out), ptr(row_nnz), stream_ptr(dev))
     if not matrix:

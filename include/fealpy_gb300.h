@@ -314,7 +314,8 @@ int32_t fgb_csr_split_blocks(int32_t n_sys, const int64_t* row_off, const int64_
 /* ---- Dirichlet boundary conditions ------------------------------------- */
 
 /* DirichletBC.apply (fealpy/fem/dirichlet_bc.py:101-229): given is_bd (uint8,
- * n), the boundary values u_bd (n, zero off the boundary) and f:
+ * n), the boundary values u_bd (n, zero off the boundary; NULL when they are
+ * all zero, which skips the product A u_bd) and f:
  *   count: f_out = f - A u_bd off the boundary, f_out[bd] = u_bd[bd];
  *          row_nnz (n, int32) = kept entries per row (1 on boundary rows);
  *   fill:  new_indices/new_values of the eliminated matrix (boundary rows and
