@@ -128,6 +128,10 @@ class BilinearForm(_Form):
         out = symbolic_structure(c2d, n, marks=marks, positions=positions)
         if self.reuse_pattern and not sub:
             cache[key] = out
+        if not sub and hasattr(space, "_cache"):
+            # the dof adjacency depends on the dof map alone: the right-hand
+            # side of the same space gathers over it (LinearForm._adjacency)
+            space._cache[("adjacency", n)] = (out[0], out[1])
         return out
 
     def assembly(self, *, format="csr", dtype=torch.float64, emit_f32: bool = False, marks=None) -> CSRTensor:
