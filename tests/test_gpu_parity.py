@@ -197,6 +197,13 @@ def test_high_valence_rows_take_the_wide_path():
     crow, col, val = O.coalesce_to_csr(c2d, O.diffusion_local(node, cell, 2, 4), n)
     assert same(A.crow, crow) and same(A.col, col)
     assert rel_err(A.values, val) < VAL_TOL
+    # a form that reuses its pattern (slot map for rows up to 128 entries, the
+    # column search for the wide row): the same values, bit for bit, twice
+    rf = BilinearForm(space, reuse_pattern=True)
+    rf.add_integrator(ScalarDiffusionIntegrator(q=4))
+    for _ in range(2):
+        R = rf.assembly()
+        assert torch.equal(R.col, A.col) and torch.equal(R.values, A.values)
 
 
 def test_mixed_precision_reaches_fp64_accuracy():
