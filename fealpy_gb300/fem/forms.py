@@ -134,16 +134,17 @@ class BilinearForm(_Form):
             space._cache[("adjacency", n)] = (out[0], out[1])
         return out
 
-    def assembly(self, *, format="csr", dtype=torch.float64, emit_f32: bool = False, marks=None) -> CSRTensor:
-        """Assemble the global matrix.  ``dtype`` float64 (default) or float32
+    def assembly(self, *, format="csr", dtype=torch.float64, emit_f32: bool = False, marks=None):
+        """Assemble the global matrix, a CSRTensor (``format="csr"``) or its
+        coalesced COOTensor (``format="coo"``; FEALPy
+        ``fealpy/fem/bilinear_form.py:83-104``: the kernels emit CSR, the COO
+        form is its row expansion).  ``dtype`` float64 (default) or float32
         selects the arithmetic of the factor and assembly kernels;
         ``emit_f32`` also stores a float copy of float64 values on the result
         (used by the mixed-precision solver).  ``marks`` (a list) receives
         labelled CUDA events after each sub-stage (instrumentation)."""
         if format not in ("csr", "coo"):
             raise ValueError(f"Unsupported format {format}.")
-        if format == "coo":
-            raise NotImplementedError("the GB300 path emits CSR")
         space = self.space
         plan = self._plan()
         status = _lib.status_word(space.device)
@@ -203,7 +204,7 @@ class BilinearForm(_Form):
         if v32 is not None:
             M._f32 = v32
         self._M = M
-        return M
+        return M.tocoo() if format == "coo" else M
 
     def __matmul__(self, u):
         """``A @ u``; without an assembled matrix the product is formed matrix

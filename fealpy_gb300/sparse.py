@@ -6,7 +6,7 @@ import torch
 
 from . import kernels as K
 
-__all__ = ["CSRTensor", "spdiags"]
+__all__ = ["CSRTensor", "COOTensor", "spdiags"]
 
 
 class CSRTensor:
@@ -109,6 +109,14 @@ class CSRTensor:
     def tocsr(self, copy=False):
         return self.copy() if copy else self
 
+    def tocoo(self, *, copy=False) -> "COOTensor":
+        """Coordinate form of the same entries in the same order
+        (``fealpy/sparse/csr_tensor.py:149-155``); a canonical CSR gives a
+        coalesced COO."""
+        indices = torch.stack([self.row, self._col.long()], dim=0)
+        values = self._values.clone() if (copy and self._values is not None) else self._values
+        return COOTensor(indices, values, self._spshape, is_coalesced=True)
+
     def copy(self):
         return CSRTensor(self._crow.clone(), self._col.clone(),
                          None if self._values is None else self._values.clone(), self._spshape)
@@ -174,6 +182,129 @@ class CSRTensor:
 
     __mul__ = mul
     __rmul__ = mul
+
+
+class COOTensor:
+    """Coordinate sparse matrix with FEALPy's ``COOTensor`` interface
+    (``fealpy/sparse/coo_tensor.py:14-213``): ``indices`` (2, nnz) int64 rows
+    and columns, ``values`` (nnz,) or None.  Products go through the CSR form
+    (``tocsr``) and its SpMV kernel."""
+
+    def __init__(self, indices: torch.Tensor, values: Optional[torch.Tensor],
+                 spshape: Optional[Tuple[int, int]] = None, *, is_coalesced: Optional[bool] = None):
+        if not isinstance(indices, torch.Tensor):
+            raise TypeError(f"indices must be a Tensor, but got {type(indices)}")
+        if indices.ndim != 2 or indices.shape[0] != 2:
+            raise ValueError("indices must be shaped (2, nnz)")
+        if values is not None:
+            if not isinstance(values, torch.Tensor):
+                raise TypeError(f"values must be a Tensor or None, but got {type(values)}")
+            if values.ndim != 1 or values.shape[0] != indices.shape[1]:
+                raise ValueError("values must be shaped (nnz,) like the indices")
+        self._indices = indices
+        self._values = values
+        self.is_coalesced = is_coalesced
+        if spshape is None:
+            spshape = tuple(int(v) + 1 for v in indices.max(dim=1).values.tolist()) if indices.numel() else (0, 0)
+        if len(spshape) != 2:
+            raise ValueError("a COO matrix has two sparse dimensions")
+        self._spshape = tuple(int(s) for s in spshape)
+
+    @property
+    def indices(self):
+        return self._indices
+
+    @property
+    def values(self):
+        return self._values
+
+    data = values
+
+    @property
+    def row(self):
+        return self._indices[0]
+
+    @property
+    def col(self):
+        return self._indices[1]
+
+    @property
+    def nnz(self):
+        return self._indices.shape[1]
+
+    @property
+    def shape(self):
+        return self._spshape
+
+    sparse_shape = shape
+
+    @property
+    def dtype(self):
+        return None if self._values is None else self._values.dtype
+
+    @property
+    def itype(self):
+        return self._indices.dtype
+
+    @property
+    def device(self):
+        return self._indices.device
+
+    def __repr__(self):
+        return f"COOTensor(shape={self.shape}, nnz={self.nnz}, dtype={self.dtype}, device={self.device})"
+
+    def coalesce(self) -> "COOTensor":
+        """Entries sorted by (row, column) with duplicates summed
+        (``fealpy/sparse/coo_tensor.py:184-213``); a matrix without values
+        gets the multiplicity of each position."""
+        if self.is_coalesced or self.nnz == 0:
+            return self
+        key = self._indices[0] * self._spshape[1] + self._indices[1]
+        uniq, inv = torch.unique(key, sorted=True, return_inverse=True)
+        indices = torch.stack([uniq // self._spshape[1], uniq % self._spshape[1]], dim=0)
+        src = self._values if self._values is not None else torch.ones(self.nnz, dtype=torch.int64,
+                                                                       device=self.device)
+        values = torch.zeros(uniq.numel(), dtype=src.dtype, device=self.device).index_add_(0, inv, src)
+        return COOTensor(indices, values, self._spshape, is_coalesced=True)
+
+    def tocoo(self, *, copy=False):
+        return self.copy() if copy else self
+
+    def tocsr(self, *, copy=False) -> CSRTensor:
+        """CSR form of the coalesced entries (``fealpy/sparse/coo_tensor.py:137``)."""
+        c = self.coalesce()
+        counts = torch.bincount(c.row, minlength=self._spshape[0])
+        crow = torch.zeros(self._spshape[0] + 1, dtype=torch.int64, device=self.device)
+        torch.cumsum(counts, 0, out=crow[1:])
+        values = c.values if c.values is not None else torch.ones(c.nnz, dtype=torch.float64, device=self.device)
+        if copy and c is self:
+            values = values.clone()
+        return CSRTensor(crow, c.col.to(torch.int32), values, self._spshape)
+
+    def to_dense(self):
+        values = self._values if self._values is not None else torch.ones(self.nnz, dtype=torch.float64,
+                                                                           device=self.device)
+        out = torch.zeros(self._spshape[0] * self._spshape[1], dtype=values.dtype, device=self.device)
+        out.index_add_(0, self._indices[0] * self._spshape[1] + self._indices[1], values)
+        return out.reshape(self._spshape)
+
+    def copy(self):
+        return COOTensor(self._indices.clone(), None if self._values is None else self._values.clone(),
+                         self._spshape, is_coalesced=self.is_coalesced)
+
+    def astype(self, dtype=None, *, copy=True):
+        values = torch.ones(self.nnz, dtype=dtype, device=self.device) if self._values is None \
+            else self._values.to(dtype)
+        return COOTensor(self._indices, values, self._spshape, is_coalesced=self.is_coalesced)
+
+    def device_put(self, device=None):
+        return COOTensor(self._indices.to(device), None if self._values is None else self._values.to(device),
+                         self._spshape, is_coalesced=self.is_coalesced)
+
+    def matmul(self, other):
+        return self.tocsr().matmul(other)
+
+    __matmul__ = matmul
 
 
 def spdiags(data: torch.Tensor, diags: int, M: int, N: int, format="csr") -> CSRTensor:

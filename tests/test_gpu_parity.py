@@ -60,6 +60,12 @@ def test_c1_poisson_full_path(golden_dir):
     A = bf.assembly()
     assert same(A.crow, z["crow"]) and same(A.col, z["col"])
     assert rel_err(A.values, z["val"]) < VAL_TOL
+    # format="coo": the coalesced coordinate form of the same matrix
+    Ac = bf.assembly(format="coo")
+    assert isinstance(Ac, F.COOTensor) and Ac.is_coalesced and Ac.shape == A.shape
+    assert torch.equal(Ac.row, A.row) and torch.equal(Ac.col, A.col.long())
+    assert torch.equal(Ac.values, A.values)
+    assert torch.equal(Ac.tocsr().crow, A.crow)
     lf = LinearForm(space)
     lf.add_integrator(ScalarSourceIntegrator(source, q=3))
     Fv = lf.assembly()

@@ -180,3 +180,39 @@ def test_no_cpu_fallback():
         F.cg_mixed(A, b)
     with pytest.raises((ValueError, RuntimeError)):
         DirichletBC(space, gd=0.0).apply(A, b)
+
+
+def test_coo_tensor_conversions():
+    """COOTensor (``fealpy/sparse/coo_tensor.py``): coalescing sorts by
+    (row, column) and sums duplicates; tocsr/tocoo round trip; to_dense adds
+    repeated entries.  Pure index bookkeeping on CPU tensors, compared with
+    scipy."""
+    from scipy.sparse import coo_matrix
+    from fealpy_gb300.sparse import COOTensor, CSRTensor
+    g = torch.Generator().manual_seed(5)
+    n, m, nnz = 13, 9, 60
+    rows = torch.randint(0, n, (nnz,), generator=g)
+    cols = torch.randint(0, m, (nnz,), generator=g)
+    vals = torch.rand(nnz, generator=g, dtype=torch.float64)
+    A = COOTensor(torch.stack([rows, cols]), vals, (n, m))
+    S = coo_matrix((vals.numpy(), (rows.numpy(), cols.numpy())), shape=(n, m)).tocsr()
+    S.sum_duplicates()
+    C = A.tocsr()
+    assert isinstance(C, CSRTensor) and C.shape == (n, m)
+    assert np.array_equal(C.crow.numpy(), S.indptr)
+    assert np.array_equal(C.col.numpy(), S.indices)
+    assert np.allclose(C.values.numpy(), S.data, rtol=0, atol=1e-15)
+    assert np.allclose(A.to_dense().numpy(), S.toarray(), rtol=0, atol=1e-15)
+    B = C.tocoo()
+    assert B.is_coalesced and B.nnz == S.nnz
+    assert torch.equal(B.row, C.row) and torch.equal(B.col, C.col.long())
+    assert B.tocsr().crow.equal(C.crow)
+    # no values: coalescing counts each position's multiplicity
+    P = COOTensor(torch.stack([rows, cols]), None, (n, m)).coalesce()
+    ones = coo_matrix((np.ones(nnz), (rows.numpy(), cols.numpy())), shape=(n, m)).tocsr()
+    ones.sum_duplicates()
+    assert np.array_equal(P.values.numpy(), ones.data.astype(np.int64))
+    # shape inferred from the largest index, as FEALPy does
+    assert COOTensor(torch.tensor([[0, 4], [2, 1]]), None).shape == (5, 3)
+    with pytest.raises(ValueError):
+        COOTensor(torch.zeros(3, 2, dtype=torch.int64), None)
