@@ -253,15 +253,18 @@ class COOTensor:
     def __repr__(self):
         return f"COOTensor(shape={self.shape}, nnz={self.nnz}, dtype={self.dtype}, device={self.device})"
 
-    def coalesce(self) -> "COOTensor":
+    def coalesce(self, accumulate: bool = True) -> "COOTensor":
         """Entries sorted by (row, column) with duplicates summed
         (``fealpy/sparse/coo_tensor.py:184-213``); a matrix without values
-        gets the multiplicity of each position."""
+        gets the multiplicity of each position (``accumulate``) or stays
+        without values."""
         if self.is_coalesced or self.nnz == 0:
             return self
         key = self._indices[0] * self._spshape[1] + self._indices[1]
         uniq, inv = torch.unique(key, sorted=True, return_inverse=True)
         indices = torch.stack([uniq // self._spshape[1], uniq % self._spshape[1]], dim=0)
+        if self._values is None and not accumulate:
+            return COOTensor(indices, None, self._spshape, is_coalesced=True)
         src = self._values if self._values is not None else torch.ones(self.nnz, dtype=torch.int64,
                                                                        device=self.device)
         values = torch.zeros(uniq.numel(), dtype=src.dtype, device=self.device).index_add_(0, inv, src)

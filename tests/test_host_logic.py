@@ -216,3 +216,23 @@ def test_coo_tensor_conversions():
     assert COOTensor(torch.tensor([[0, 4], [2, 1]]), None).shape == (5, 3)
     with pytest.raises(ValueError):
         COOTensor(torch.zeros(3, 2, dtype=torch.int64), None)
+
+
+def test_coo_coalesce_reference_known_answers():
+    """The reference's own coalesce cases (``test/sparse/test_coo_tensor.py:29-90``):
+    duplicates summed in (row, column) order; without values the multiplicity
+    (accumulate) or no values at all."""
+    from fealpy_gb300.sparse import COOTensor
+    idx = torch.tensor([[0, 0, 1, 2, 0, 1], [1, 2, 0, 0, 2, 0]])
+    c = COOTensor(idx, torch.tensor([1, 2, 3, 4, 5, 6], dtype=torch.float64), torch.tensor([3, 3]),
+                  is_coalesced=False).coalesce()
+    assert c.is_coalesced
+    assert torch.equal(c.indices, torch.tensor([[0, 0, 1, 2], [1, 2, 0, 0]]))
+    assert torch.equal(c.values, torch.tensor([1, 7, 9, 4], dtype=torch.float64))
+    c = COOTensor(torch.tensor([[0, 0, 1, 2, 0], [1, 2, 0, 0, 2]]), None, (3, 3), is_coalesced=False)
+    a = c.coalesce(accumulate=True)
+    assert torch.equal(a.indices, torch.tensor([[0, 0, 1, 2], [1, 2, 0, 0]]))
+    assert torch.equal(a.values, torch.tensor([1, 2, 1, 1]))
+    b = COOTensor(torch.tensor([[0, 0, 1, 2], [1, 2, 0, 0]]), None, (3, 3),
+                  is_coalesced=False).coalesce(accumulate=False)
+    assert b.is_coalesced and b.values is None
