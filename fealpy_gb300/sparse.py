@@ -175,13 +175,144 @@ class CSRTensor:
 
     __neg__ = neg
 
-    def mul(self, scalar):
-        if isinstance(scalar, (int, float)):
-            return CSRTensor(self._crow, self._col, self._values * scalar, self._spshape)
-        raise NotImplementedError("only scalar scaling is provided")
+    # FEALPy's element-wise arithmetic and sparse utilities
+    # (``fealpy/sparse/csr_tensor.py:218-420``, operators
+    # ``fealpy/sparse/sparse_tensor.py:131-216``) ------------------------------
+    @property
+    def nonzero_slice(self):
+        return self.row, self._col.long()
+
+    def _vals(self):
+        return self._values if self._values is not None else torch.ones(self.nnz, dtype=torch.float64,
+                                                                         device=self.device)
+
+    def _same_pattern(self, other: "CSRTensor") -> bool:
+        if self._crow is other._crow and self._col is other._col:
+            return True
+        return (self.nnz == other.nnz and torch.equal(self._crow, other._crow)
+                and torch.equal(self._col, other._col))
+
+    def add(self, other, alpha=1):
+        """``self + alpha * other``: a CSRTensor for a CSRTensor (the union of
+        the two patterns, duplicates summed; two matrices of one pattern, such
+        as two forms assembled on one space, add their values) or a number
+        (added to the stored entries); a dense tensor for a dense tensor."""
+        if isinstance(other, CSRTensor):
+            if tuple(self.shape) != tuple(other.shape):
+                raise ValueError(f"shapes {self.shape} and {other.shape} do not match")
+            if self._same_pattern(other):
+                return CSRTensor(self._crow, self._col, self._vals() + alpha * other._vals(), self._spshape)
+            indices = torch.cat([torch.stack(self.nonzero_slice), torch.stack(other.nonzero_slice)], dim=1)
+            values = torch.cat([self._vals(), alpha * other._vals()])
+            return COOTensor(indices, values, self._spshape).tocsr()
+        if isinstance(other, torch.Tensor):
+            if tuple(other.shape) != tuple(self.shape):
+                raise ValueError(f"shapes {self.shape} and {tuple(other.shape)} do not match")
+            out = other * alpha
+            out = out.to(torch.promote_types(out.dtype, self._vals().dtype)).clone()
+            out.index_put_(self.nonzero_slice, self._vals().to(out.dtype), accumulate=True)
+            return out
+        if isinstance(other, (int, float)):
+            return CSRTensor(self._crow.clone(), self._col.clone(), self._vals() + alpha * other, self._spshape)
+        raise TypeError(f"Unsupported type {type(other).__name__} in addition")
+
+    def __add__(self, other):
+        return self.add(other)
+
+    __radd__ = __add__
+
+    def __sub__(self, other):
+        return self.add(other, alpha=-1)
+
+    def __rsub__(self, other):
+        return self.neg().add(other)
+
+    def mul(self, other):
+        """Element-wise product with a number or a dense tensor (the stored
+        entries only)."""
+        if isinstance(other, (int, float)):
+            if self._values is None:
+                raise ValueError("Cannot multiply CSRTensor without value with scalar")
+            return CSRTensor(self._crow, self._col, self._values * other, self._spshape)
+        if isinstance(other, torch.Tensor):
+            if tuple(other.shape) != tuple(self.shape):
+                raise ValueError(f"shapes {self.shape} and {tuple(other.shape)} do not match")
+            vals = other[self.nonzero_slice]
+            if self._values is not None:
+                vals = self._values * vals
+            return CSRTensor(self._crow, self._col, vals, self._spshape)
+        if isinstance(other, CSRTensor):
+            raise NotImplementedError("element-wise products of two sparse matrices are not provided")
+        raise TypeError(f"Unsupported type {type(other).__name__} in multiplication")
 
     __mul__ = mul
     __rmul__ = mul
+
+    def div(self, other):
+        """Element-wise quotient by a number or a dense tensor (a vector of
+        length rows or columns broadcasts along that axis)."""
+        if self._values is None:
+            raise ValueError("Cannot divide CSRTensor without value")
+        if isinstance(other, (int, float)):
+            return CSRTensor(self._crow, self._col, self._values / other, self._spshape)
+        if isinstance(other, torch.Tensor):
+            if other.ndim == 1:
+                if other.shape[0] == self._spshape[0]:
+                    return CSRTensor(self._crow, self._col, self._values / other[self.row], self._spshape)
+                if other.shape[0] == self._spshape[1]:
+                    return CSRTensor(self._crow, self._col, self._values / other[self._col.long()], self._spshape)
+            if tuple(other.shape) != tuple(self.shape):
+                raise ValueError(f"shapes {self.shape} and {tuple(other.shape)} do not match")
+            return CSRTensor(self._crow, self._col, self._values / other[self.nonzero_slice], self._spshape)
+        raise TypeError(f"Unsupported type {type(other).__name__} in division")
+
+    __truediv__ = div
+
+    def pow(self, other):
+        if self._values is None:
+            raise ValueError("Cannot power CSRTensor without value with tensor")
+        if isinstance(other, (int, float)):
+            return CSRTensor(self._crow, self._col, self._values ** other, self._spshape)
+        if isinstance(other, torch.Tensor):
+            if tuple(other.shape) != tuple(self.shape):
+                raise ValueError(f"shapes {self.shape} and {tuple(other.shape)} do not match")
+            return CSRTensor(self._crow, self._col, self._values ** other[self.nonzero_slice], self._spshape)
+        raise TypeError(f"Unsupported type {type(other).__name__} in power")
+
+    __pow__ = pow
+
+    def partial(self, index) -> "CSRTensor":
+        """The stored entries selected by a boolean mask (or an index) over
+        the nonzeros, rows kept."""
+        sel = torch.zeros(self.nnz, dtype=torch.bool, device=self.device)
+        sel[index] = True
+        cum = torch.zeros(self.nnz + 1, dtype=torch.int64, device=self.device)
+        torch.cumsum(sel, 0, out=cum[1:])
+        crow = cum[self._crow]
+        values = None if self._values is None else self._values[sel]
+        return CSRTensor(crow, self._col[sel], values, self._spshape)
+
+    def tril(self, k: int = 0) -> "CSRTensor":
+        return self.partial(self.row + k >= self._col.long())
+
+    def triu(self, k: int = 0) -> "CSRTensor":
+        return self.partial(self._col.long() - k >= self.row)
+
+    def sum(self, axis=0):
+        """Row sums (axis 0, the product with a vector of ones, as FEALPy
+        forms it) or column sums (axis 1)."""
+        if axis == 0:
+            return self @ torch.ones(self._spshape[1], dtype=self._vals().dtype, device=self.device)
+        if axis == 1:
+            out = torch.zeros(self._spshape[1], dtype=self._vals().dtype, device=self.device)
+            return out.index_add_(0, self._col.long(), self._vals())
+        raise ValueError("axis must be 0 or 1")
+
+    @property
+    def T(self) -> "CSRTensor":
+        """The transpose (through the coordinate form, as FEALPy forms it)."""
+        row, col = self.nonzero_slice
+        return COOTensor(torch.stack([col, row]), self._values, (self._spshape[1], self._spshape[0])).tocsr()
 
 
 class COOTensor:

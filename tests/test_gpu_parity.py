@@ -457,3 +457,35 @@ def test_residual_norm_kernel_matches_numpy(golden_dir):
     assert (r1, b1) == (r2, b2)
     assert abs(r1 - np.linalg.norm(b - A @ x)) <= 1e-12 * np.linalg.norm(b - A @ x)
     assert abs(b1 - np.linalg.norm(b)) <= 1e-13 * np.linalg.norm(b)
+
+
+def test_forms_assembled_apart_add_to_the_grouped_form(golden_dir):
+    """K + M of two forms assembled on one space (one pattern: the values add)
+    equals the reference's grouped diffusion+mass matrix; the row sums
+    (``sum(axis=0)``, the GPU product with ones) and the transpose of the
+    symmetric matrix agree as well."""
+    dev = cuda()
+    import fealpy_gb300 as F
+    from fealpy_gb300.fem import BilinearForm, ScalarDiffusionIntegrator, ScalarMassIntegrator
+    z = load(golden_dir, "small_tet_p2.npz")
+    mesh = F.TetrahedronMesh(torch.as_tensor(z["node"], device=dev),
+                             torch.as_tensor(z["cell"], dtype=torch.int32, device=dev))
+    q = None if int(z["q"]) < 0 else int(z["q"])
+    space = F.LagrangeFESpace(mesh, int(z["p"]))
+    kappa = torch.as_tensor(z["kappa"], device=dev)
+    bk, bm_ = BilinearForm(space), BilinearForm(space)
+    bk.add_integrator(ScalarDiffusionIntegrator(coef=kappa, q=q))
+    bm_.add_integrator(ScalarMassIntegrator(coef=1.0, q=q))
+    K, M = bk.assembly(), bm_.assembly()
+    S = K + M
+    assert same(S.crow, z["crow"]) and same(S.col, z["col"])
+    assert rel_err(S.values, z["val"]) < VAL_TOL
+    n = S.shape[1]
+    ref = np.zeros(n)
+    np.add.at(ref, np.repeat(np.arange(n), np.diff(z["crow"])), z["val"])
+    ones = torch.ones(n, dtype=torch.float64, device=dev)
+    assert torch.equal(S.sum(axis=0), S @ ones)
+    assert rel_err(S.sum(axis=0), ref) < VAL_TOL
+    T = S.T
+    assert same(T.crow, z["crow"]) and same(T.col, z["col"])
+    assert rel_err(T.values, z["val"]) < VAL_TOL

@@ -236,3 +236,49 @@ def test_coo_coalesce_reference_known_answers():
     b = COOTensor(torch.tensor([[0, 0, 1, 2], [1, 2, 0, 0]]), None, (3, 3),
                   is_coalesced=False).coalesce(accumulate=False)
     assert b.is_coalesced and b.values is None
+
+
+def test_csr_arithmetic_matches_scipy():
+    """CSRTensor arithmetic of FEALPy's interface (``fealpy/sparse/csr_tensor.py:218-420``):
+    sums of two patterns (union, duplicates added) and of one pattern
+    (values added), scalar and dense operands, transpose, triangles, column
+    sums, selection.  Index bookkeeping on CPU tensors, compared with scipy."""
+    import scipy.sparse as sps
+    from fealpy_gb300.sparse import CSRTensor
+    a = sps.random(40, 30, density=0.15, random_state=3, format="csr")
+    b = sps.random(40, 30, density=0.15, random_state=4, format="csr")
+    a.sort_indices(); b.sort_indices()
+    A, B = CSRTensor.from_scipy(a, device="cpu"), CSRTensor.from_scipy(b, device="cpu")
+
+    def same(M, ref, exact_pattern=True):
+        ref = sps.csr_matrix(ref)
+        ref.sum_duplicates()
+        ref.sort_indices()
+        assert isinstance(M, CSRTensor) and tuple(M.shape) == ref.shape
+        assert np.allclose(M.to_dense().numpy(), ref.toarray(), rtol=0, atol=1e-14)
+        if exact_pattern:
+            assert np.array_equal(M.crow.numpy(), ref.indptr) and np.array_equal(M.col.numpy(), ref.indices)
+
+    same(A + B, a + b)
+    same(A - B, a - b)
+    same(A.add(B, alpha=2.5), a + 2.5 * b)
+    C = A + A                       # one pattern: values added, the pattern shared
+    assert C.crow is A.crow and C.col is A.col
+    same(C, 2 * a)
+    same(A * 3.0, 3.0 * a)
+    same(A / 4.0, a / 4.0)
+    same(A ** 2, a.power(2))
+    D = torch.rand(40, 30, dtype=torch.float64, generator=torch.Generator().manual_seed(1))
+    assert np.allclose((A + D).numpy(), a.toarray() + D.numpy(), rtol=0, atol=1e-14)
+    same(A.mul(D), a.multiply(D.numpy()))
+    rs = torch.arange(1, 41, dtype=torch.float64)
+    same(A.div(rs), sps.diags(1.0 / rs.numpy()) @ a)
+    same(A.T, a.T)
+    same(A.tril(), sps.tril(a)); same(A.triu(1), sps.triu(a, 1))
+    assert np.allclose(A.sum(axis=1).numpy(), np.asarray(a.sum(axis=0)).ravel(), rtol=0, atol=1e-14)
+    mask = A.values > 0.5
+    same(A.partial(mask), sps.csr_matrix((a.data * (a.data > 0.5), a.indices, a.indptr), shape=a.shape),
+         exact_pattern=False)
+    assert A.partial(mask).nnz == int(mask.sum())
+    with pytest.raises(ValueError):
+        A + CSRTensor.from_scipy(sps.random(30, 30, density=0.1, format="csr"), device="cpu")
