@@ -13,7 +13,7 @@ from typing import Optional
 
 import torch
 
-from .sparse import CSRTensor
+from .sparse import CSRTensor, COOTensor
 from . import kernels as K
 
 __all__ = ["cg", "cg_mixed", "JacobiPreconditioner"]
@@ -111,6 +111,58 @@ def _sell_of(A: CSRTensor, want32: bool, tune: bool = True):
     return S
 
 
+def _cg_operator(A, b, x0, M, atol, rtol, maxit, batch_first):
+    """FEALPy's recurrence and stopping rule (``fealpy/solver/cg.py:76-123``)
+    for an operator that is not a stored matrix: anything with ``@`` (``cg``
+    takes ``SupportsMatmul``, ``fealpy/solver/cg.py:10-17``), such as a
+    BilinearForm before assembly, whose product is the matrix-free kernel
+    pair.  The products are the operator's own; the vector updates and dot
+    products run on the device, and the stopping test reads one scalar per
+    iteration.  ``M`` is None, a diagonal CSRTensor (Jacobi: an element-wise
+    product) or any operator with ``@``."""
+    if b.ndim != 1:
+        raise NotImplementedError("an operator without a stored matrix takes one right-hand side")
+    info = {"residual": 0.0, "niter": 0}
+    b = b.to(torch.float64)
+    b_norm = float(torch.linalg.norm(b))
+    if b_norm < 1e-15:
+        return torch.zeros_like(b), info
+    if M is None:
+        prec = lambda v: v
+    elif isinstance(M, CSRTensor) and M.is_diagonal():
+        dinv = M.values.to(torch.float64)
+        prec = lambda v: dinv * v
+    elif hasattr(M, "__matmul__"):
+        prec = lambda v: M @ v
+    else:
+        raise TypeError(f"M must support matrix products, got {type(M).__name__}")
+    x = torch.zeros_like(b) if x0 is None else x0.to(torch.float64).clone()
+    r = b - A @ x
+    z = prec(r)
+    p = z
+    rz = torch.dot(r, z)
+    n_iter = 0
+    while True:
+        Ap = A @ p
+        alpha = rz / torch.dot(p, Ap)
+        x = x + alpha * p
+        r = r - alpha * Ap
+        z = prec(r)
+        rz_new = torch.dot(r, z)
+        res = float(torch.sqrt(rz_new))
+        n_iter += 1
+        info["residual"] = res
+        info["niter"] = n_iter
+        if res < atol or res < rtol * b_norm:
+            break
+        if maxit is not None and n_iter >= maxit:
+            logger.info(f"CG: failed, stopped by maxit ({maxit}).")
+            break
+        p = z + (rz_new / rz) * p
+        rz = rz_new
+    return x, info
+
+
 def cg(A, b: torch.Tensor, x0: Optional[torch.Tensor] = None, M=None, *, batch_first: bool = False,
        atol: float = 1e-12, rtol: float = 1e-8, maxit: Optional[int] = 10000, returninfo: bool = False,
        check_every: int = 16, lanes_per_row: int = 0, stop: str = "preconditioned", profile: bool = False,
@@ -129,8 +181,13 @@ def cg(A, b: torch.Tensor, x0: Optional[torch.Tensor] = None, M=None, *, batch_f
         raise ValueError("b must be a 1D or 2D dense tensor")
     if x0 is not None and x0.shape != b.shape:
         raise ValueError("x0 and b must have the same shape")
+    if isinstance(A, COOTensor):
+        A = A.tocsr()
     if not isinstance(A, CSRTensor):
-        raise NotImplementedError("cg on the GB300 path takes a CSRTensor matrix")
+        if not hasattr(A, "__matmul__"):
+            raise TypeError(f"A must support matrix products, got {type(A).__name__}")
+        x, info = _cg_operator(A, b, x0, M, atol, rtol, maxit, batch_first)
+        return (x, info) if returninfo else x
     if stop not in ("preconditioned", "residual"):
         raise ValueError("stop must be 'preconditioned' or 'residual'")
     from .amg import GAMGSolver

@@ -95,3 +95,42 @@ def test_matfree_c3_law_p3_triangles(golden_dir):
     x = np.random.default_rng(1).normal(size=space.number_of_global_dofs())
     y = bf @ torch.as_tensor(x, device=dev)
     assert rel(y, _fixture_product(z, x)) < 1e-12
+
+
+def test_cg_on_the_unassembled_form(golden_dir):
+    """``cg`` takes any operator with ``@`` (fealpy/solver/cg.py:10-17): the
+    C2-law form before assembly (diffusion + mass, no boundary condition: SPD)
+    solved matrix free with Jacobi, against a direct solve of the reference's
+    assembled matrix, and against cg on the assembled CSR (same recurrence:
+    the same iteration count within one)."""
+    dev = cuda()
+    import scipy.sparse as sps
+    from scipy.sparse.linalg import spsolve
+    import fealpy_gb300 as F
+    from fealpy_gb300.fem import BilinearForm, ScalarDiffusionIntegrator, ScalarMassIntegrator
+    z = np.load(os.path.join(golden_dir, "cfg_c2_tet_p2_8.npz"))
+    mesh = F.TetrahedronMesh(torch.as_tensor(z["node"], device=dev),
+                             torch.as_tensor(z["cell"], dtype=torch.int32, device=dev))
+    space = F.LagrangeFESpace(mesh, 2)
+    kappa = torch.as_tensor(z["kappa"], device=dev)
+    ints = lambda: (ScalarDiffusionIntegrator(coef=kappa, q=4), ScalarMassIntegrator(coef=1.0, q=4))
+    bf = BilinearForm(space)
+    bf.add_integrator(*ints())
+    n = space.number_of_global_dofs()
+    b = np.random.default_rng(2).normal(size=n)
+    A_ref = sps.csr_matrix((z["val"], z["col"], z["crow"]), shape=(n, n))
+    u_ref = spsolve(A_ref.tocsc(), b)
+    ba = BilinearForm(space)
+    ba.add_integrator(*ints())
+    A = ba.assembly()
+    M = F.JacobiPreconditioner().apply(A)
+    bt = torch.as_tensor(b, device=dev)
+    u, info = F.cg(bf, bt, M=M, atol=1e-30, rtol=1e-11, returninfo=True)
+    assert bf._M is None
+    assert rel(u, u_ref) < 1e-9, rel(u, u_ref)
+    ua, infoa = F.cg(A, bt, M=M, atol=1e-30, rtol=1e-11, returninfo=True)
+    assert abs(info["niter"] - infoa["niter"]) <= 1, (info, infoa)
+    assert rel(u, ua.cpu().numpy()) < 1e-9
+    # a COO operator goes to its CSR form
+    uc = F.cg(ba.assembly(format="coo"), bt, M=M, atol=1e-30, rtol=1e-11)
+    assert torch.equal(uc, ua)
