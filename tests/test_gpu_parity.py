@@ -132,6 +132,11 @@ def test_elasticity_p1(golden_dir):
     A = bf.assembly()
     assert same(A.crow, z["crow"]) and same(A.col, z["col"])
     assert rel_err(A.values, z["val"]) < VAL_TOL
+    # FEALPy's 'voigt' and 'fast' variants form the same matrix
+    for method in ("voigt", "fast"):
+        bv = BilinearForm(ts)
+        bv.add_integrator(LinearElasticityIntegrator(mat, q=4, method=method))
+        assert torch.equal(bv.assembly().values, A.values)
     lf = LinearForm(ts)
     lf.add_integrator(VectorSourceIntegrator(source=[0.0, 0.0, -1.0], q=4))
     Fv = lf.assembly()
