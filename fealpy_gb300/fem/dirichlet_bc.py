@@ -32,6 +32,7 @@ class DirichletBC:
     def check_matrix(self, matrix):
         if not isinstance(matrix, CSRTensor):
             raise ValueError("The type of matrix must be CSRTensor.")
+        matrix._single("DirichletBC.apply")
         if matrix.shape[0] != matrix.shape[1]:
             raise ValueError("The matrix must be a square matrix.")
         if matrix.shape[0] != self.gdof:

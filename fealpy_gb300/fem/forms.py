@@ -51,8 +51,8 @@ class _Form:
             space = tuple(space[0])
         if len(space) != 1:
             raise NotImplementedError("forms over two different spaces are not provided")
-        if batch_size != 0:
-            raise NotImplementedError("batched forms are not provided")
+        if batch_size < 0:
+            raise ValueError("batch_size must be non-negative")
         self._spaces = space
         self.integrators = {}
         self.splitters = {}
@@ -145,6 +145,8 @@ class BilinearForm(_Form):
         labelled CUDA events after each sub-stage (instrumentation)."""
         if format not in ("csr", "coo"):
             raise ValueError(f"Unsupported format {format}.")
+        if self.batch_size > 0:
+            return self._batched_assembly(format, dtype)
         space = self.space
         plan = self._plan()
         status = _lib.status_word(space.device)
@@ -203,6 +205,35 @@ class BilinearForm(_Form):
             M.node_block = 3
         if v32 is not None:
             M._f32 = v32
+        self._M = M
+        return M.tocoo() if format == "coo" else M
+
+    def _batched_assembly(self, format, dtype):
+        """A form with ``batch_size`` B (``fealpy/fem/bilinear_form.py:46-75``):
+        integrators with batched coefficients contribute member b's matrix to
+        batch member b, the others the same matrix to every member.  One
+        pattern for all members (with its slot map), one factor and one values
+        pass per member; the result holds values (B, nnz)."""
+        space = self.space
+        B = self.batch_size
+        for it in self.integrators.values():
+            nb = it.batch_size(space)
+            if nb not in (0, B):
+                raise ValueError(f"an integrator has {nb} batch members, the form {B}")
+        vals = []
+        for b in range(B):
+            member = BilinearForm(space, reuse_pattern=True)
+            for g, it in self.integrators.items():
+                member.integrators[g] = it.batch_member(space, b)
+            Mb = member.assembly(dtype=dtype)
+            if vals and not (Mb.crow is M0.crow and Mb.col is M0.col):
+                raise RuntimeError("batch members assembled on different patterns")
+            if not vals:
+                M0 = Mb
+            vals.append(Mb.values)
+        M = CSRTensor(M0.crow, M0.col, torch.stack(vals), M0.shape)
+        M.dof_blocks = M0.dof_blocks
+        M.node_block = M0.node_block
         self._M = M
         return M.tocoo() if format == "coo" else M
 
@@ -275,6 +306,8 @@ class LinearForm(_Form):
     into dofs by the deterministic adjacency gather."""
 
     def __init__(self, *space, batch_size: int = 0):
+        if batch_size != 0:
+            raise NotImplementedError("batched right-hand sides are not provided")
         super().__init__(*space, batch_size=batch_size)
         self._V = None
 

@@ -187,6 +187,17 @@ class Integrator:
 
     __iadd__ = __add__
 
+    # batched coefficients (``batched=True``: a leading batch axis on the
+    # coefficient, ``fealpy/functional.py:68-106``) -----------------------
+    def batch_size(self, space) -> int:
+        """Batch members of the coefficient (0: not batched)."""
+        return 0
+
+    def batch_member(self, space, b: int) -> "Integrator":
+        """The integrator of batch member ``b`` (unbatched); an unbatched
+        integrator is the same for every member."""
+        return self
+
     def __call__(self, *args, **kwargs):
         return self.assembly(*args, **kwargs)
 
@@ -207,7 +218,11 @@ class _OperatorIntegrator(Integrator):
 
     def assembly(self, space, /, indices=None):
         """Local matrices (NC, ldof, ldof), FP64 (a convenience; the CSR path
-        never materialises them)."""
+        never materialises them); (B, NC, ldof, ldof) with batched
+        coefficients."""
+        nb = self.batch_size(space)
+        if nb:
+            return torch.stack([self.batch_member(space, b).assembly(space, indices) for b in range(nb)])
         plan = self.plan(space)
         mesh = space.mesh
         coef = plan.coef_matrix()
@@ -218,13 +233,55 @@ class _OperatorIntegrator(Integrator):
         return out if indices is None else out[indices]
 
 
-class ScalarDiffusionIntegrator(_OperatorIntegrator):
+class _BatchedCoef:
+    """Batched coefficients of a scalar integrator: a number per member (B,),
+    a per-cell array (B, NC), values at the quadrature points (B, NC, NQ),
+    or a callable returning one of those at the quadrature points."""
+
+    def _batched_values(self, space) -> torch.Tensor:
+        coef = self.coef
+        mesh = space.mesh
+        if callable(coef) and not isinstance(coef, (torch.Tensor, np.ndarray)):
+            key = ("batched_coef", id(space))
+            if key not in self._cache:
+                q = space.p + 3 if self.q is None else self.q
+                bcs, _ = mesh.quadrature_formula(q).get_quadrature_points_and_weights()
+                cells = self.cell_selection(mesh)
+                index = _S if cells is None else cells
+                if getattr(coef, "coordtype", "barycentric") == "cartesian":
+                    val = coef(mesh.bc_to_point(bcs, index=index))
+                else:
+                    val = coef(torch.as_tensor(bcs, device=mesh.device), index=index)
+                self._cache[key] = torch.as_tensor(val, device=mesh.device)
+            return self._cache[key]
+        if isinstance(coef, (torch.Tensor, np.ndarray)):
+            return torch.as_tensor(coef, device=mesh.device)
+        raise ValueError("a batched coefficient is a tensor (or a callable) with the batch on its first axis")
+
+    def batch_size(self, space) -> int:
+        if not self.batched:
+            return 0
+        val = self._batched_values(space)
+        if val.ndim < 1 or val.shape[0] < 1:
+            raise ValueError("a batched coefficient has the batch on its first axis")
+        return int(val.shape[0])
+
+    def batch_member(self, space, b: int):
+        if not self.batched:
+            return self
+        import copy
+        member = copy.copy(self)
+        member._cache = {}
+        member.batched = False
+        member.coef = self._batched_values(space)[b]
+        return member
+
+
+class ScalarDiffusionIntegrator(_BatchedCoef, _OperatorIntegrator):
     """``(coef grad u, grad v)`` on simplex Lagrange spaces."""
 
     def __init__(self, coef=None, q: Optional[int] = None, *, region=None, batched: bool = False, method=None):
         super().__init__()
-        if batched:
-            raise NotImplementedError("batched coefficients are not provided")
         if method not in (None, "fast"):
             raise NotImplementedError(f"assembly variant {method!r} is not provided on the GB300 path")
         self.coef = coef
@@ -234,6 +291,8 @@ class ScalarDiffusionIntegrator(_OperatorIntegrator):
 
     def plan(self, space) -> ScalarPlan:
         self._check_region()
+        if self.batched:
+            raise ValueError("a batched integrator is assembled per batch member (a form with batch_size)")
         mesh = space.mesh
         TD = mesh.TD
         q = space.p + 3 if self.q is None else self.q
@@ -252,21 +311,22 @@ class ScalarDiffusionIntegrator(_OperatorIntegrator):
         return ScalarPlan(ch, coefs, sx.diffusion_tables(TD, space.p, q), cells)
 
 
-class ScalarMassIntegrator(_OperatorIntegrator):
+class ScalarMassIntegrator(_BatchedCoef, _OperatorIntegrator):
     """``(coef u, v)`` on simplex Lagrange spaces."""
 
     def __init__(self, coef=None, q: Optional[int] = None, *, index=_S, batched: bool = False, method=None):
         super().__init__()
-        if batched:
-            raise NotImplementedError("batched coefficients are not provided")
         if method is not None:
             raise NotImplementedError(f"assembly variant {method!r} is not provided on the GB300 path")
         self.coef = coef
         self.q = q
+        self.batched = batched
         self.index = index
 
     def plan(self, space) -> ScalarPlan:
         self._check_region()
+        if self.batched:
+            raise ValueError("a batched integrator is assembled per batch member (a form with batch_size)")
         mesh = space.mesh
         q = space.p + 3 if self.q is None else self.q
         cells = self.cell_selection(mesh)
@@ -383,6 +443,17 @@ class GroupIntegrator(Integrator):
     def to_global_dof(self, space, /, indices=None):
         return self.ints[0].to_global_dof(space, indices)
 
+    def batch_size(self, space) -> int:
+        sizes = {it.batch_size(space) for it in self.ints} - {0}
+        if len(sizes) > 1:
+            raise ValueError(f"grouped integrators have different batch sizes {sorted(sizes)}")
+        return sizes.pop() if sizes else 0
+
+    def batch_member(self, space, b: int):
+        if not self.batch_size(space):
+            return self
+        return GroupIntegrator(*[it.batch_member(space, b) for it in self.ints])
+
     def plan(self, space):
         plans = [it.plan(space) for it in self.ints]
         out = plans[0]
@@ -393,6 +464,9 @@ class GroupIntegrator(Integrator):
         return out
 
     def assembly(self, space, /, indices=None):
+        nb = self.batch_size(space)
+        if nb:
+            return torch.stack([self.batch_member(space, b).assembly(space, indices) for b in range(nb)])
         out = self.ints[0].assembly(space, indices)
         for it in self.ints[1:]:
             out = out + it.assembly(space, indices)

@@ -16,6 +16,12 @@ __all__ = ["cell_factors", "build_adjacency", "build_pattern", "assemble_scalar"
            "expand_blocks", "dirichlet_apply", "csr_spmv", "csr_diagonal", "pcg_f64", "pcg_mixed", "gather_sum"]
 
 
+def _values_1d(values, what: str):
+    """The C ABI takes one matrix: values (nnz,)."""
+    if values is not None and values.ndim != 1:
+        raise ValueError(f"{what} takes the values of one matrix, shaped (nnz,), got {tuple(values.shape)}")
+
+
 def _dev(mesh_or_tensor):
     d = mesh_or_tensor.device
     if d.type != "cuda":
@@ -247,6 +253,7 @@ def dirichlet_apply(indptr, indices, values, is_bd: torch.Tensor, f: Optional[to
                     uh: Optional[torch.Tensor], matrix: bool = True):
     """Returns (new_indptr, new_indices, new_values, f_new); entries not asked for are None.
     ``uh`` None with ``f`` given: all boundary values zero."""
+    _values_1d(values, "dirichlet_apply")
     dev = _dev(indptr)
     n = indptr.numel() - 1
     dt = values.dtype
@@ -275,6 +282,7 @@ def dirichlet_apply(indptr, indices, values, is_bd: torch.Tensor, f: Optional[to
 
 
 def csr_spmv(indptr, indices, values, x, lanes: int = 0, out: Optional[torch.Tensor] = None):
+    _values_1d(values, "csr_spmv")
     dev = _dev(indptr)
     n = indptr.numel() - 1
     x = x.to(dev, values.dtype).contiguous()
@@ -302,6 +310,7 @@ def residual_norm(indptr, indices, values, b, x):
 
 
 def csr_diagonal(indptr, indices, values):
+    _values_1d(values, "csr_diagonal")
     dev = _dev(indptr)
     n = indptr.numel() - 1
     d = torch.empty(n, dtype=values.dtype, device=dev)
@@ -312,6 +321,7 @@ def csr_diagonal(indptr, indices, values):
 
 
 def pcg_f64(indptr, indices, values, dinv, b, x, atol, rtol, maxit, check_every=16, lanes=0, norm=0, profile=False):
+    _values_1d(values, "pcg_f64")
     dev = _dev(indptr)
     n = indptr.numel() - 1
     lib = _lib.lib()
@@ -580,6 +590,8 @@ def sell_build(indptr, indices, values64=None, values32=None, want64=True, want3
     renumbering; without them the rows are ordered by their smallest column.
     ``triples``: node-triple copy for a vector space with three interleaved
     components (rows a multiple of 3; ``d16`` and ``d15`` ignored)."""
+    _values_1d(values64, "sell_build")
+    _values_1d(values32, "sell_build")
     dev = _dev(indptr)
     n = indptr.numel() - 1
     lib = _lib.lib()

@@ -188,6 +188,7 @@ def cg(A, b: torch.Tensor, x0: Optional[torch.Tensor] = None, M=None, *, batch_f
             raise TypeError(f"A must support matrix products, got {type(A).__name__}")
         x, info = _cg_operator(A, b, x0, M, atol, rtol, maxit, batch_first)
         return (x, info) if returninfo else x
+    A._single("cg")
     if stop not in ("preconditioned", "residual"):
         raise ValueError("stop must be 'preconditioned' or 'residual'")
     from .amg import GAMGSolver
@@ -250,6 +251,7 @@ def cg_mixed(A: CSRTensor, b: torch.Tensor, x0: Optional[torch.Tensor] = None, M
     assembly's FP32 rounding."""
     if not isinstance(A, CSRTensor):
         raise NotImplementedError("cg_mixed takes a CSRTensor matrix")
+    A._single("cg_mixed")
     dinv = _diag_inv_of(M)
     if dinv is None:
         dinv = A.diagonal_inverse()

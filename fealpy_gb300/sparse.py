@@ -11,8 +11,10 @@ __all__ = ["CSRTensor", "COOTensor", "spdiags"]
 
 class CSRTensor:
     """Compressed sparse rows: ``crow`` int64 (n+1), ``col`` int32 (nnz),
-    ``values`` (nnz,) float.  Matrices produced by this package are canonical
-    (columns strictly ascending within a row, duplicates summed)."""
+    ``values`` (nnz,) float, or (B, nnz) for a batch of B matrices on one
+    pattern (a form with batched coefficients).  Matrices produced by this
+    package are canonical (columns strictly ascending within a row,
+    duplicates summed)."""
 
     def __init__(self, crow: torch.Tensor, col: torch.Tensor, values: Optional[torch.Tensor],
                  spshape: Optional[Tuple[int, int]] = None):
@@ -59,12 +61,25 @@ class CSRTensor:
         return self._col.shape[-1]
 
     @property
+    def is_batched(self) -> bool:
+        return self._values is not None and self._values.ndim > 1
+
+    @property
+    def dense_shape(self):
+        return tuple(self._values.shape[:-1]) if self.is_batched else ()
+
+    @property
     def shape(self):
-        return self._spshape
+        return self.dense_shape + self._spshape
 
     @property
     def sparse_shape(self):
         return self._spshape
+
+    def _single(self, what: str):
+        if self.is_batched:
+            raise ValueError(f"{what} takes one matrix; a batched matrix's member b is "
+                             "CSRTensor(A.crow, A.col, A.values[b], A.sparse_shape)")
 
     @property
     def dtype(self):
@@ -91,11 +106,12 @@ class CSRTensor:
 
     # conversions ------------------------------------------------------------
     def to_dense(self):
-        out = torch.zeros(self._spshape, dtype=self._values.dtype, device=self.device)
-        out[self.row, self._col.long()] = self._values
+        out = torch.zeros(self.dense_shape + self._spshape, dtype=self._values.dtype, device=self.device)
+        out[..., self.row, self._col.long()] = self._values
         return out
 
     def to_scipy(self):
+        self._single("to_scipy")
         from scipy.sparse import csr_matrix
         return csr_matrix((self._values.cpu().numpy(), self._col.cpu().numpy(), self._crow.cpu().numpy()),
                           shape=self._spshape)
@@ -130,6 +146,7 @@ class CSRTensor:
     # arithmetic ---------------------------------------------------------------
     def values_f32(self) -> torch.Tensor:
         """Float copy of the values (computed once and cached)."""
+        self._single("the FP32 solver copy")
         if self._f32 is None:
             self._f32 = self._values.to(torch.float32)
         return self._f32
@@ -139,6 +156,18 @@ class CSRTensor:
             raise NotImplementedError("sparse-sparse products are not on the GB300 path")
         if not isinstance(other, torch.Tensor):
             raise TypeError(f"Unsupported type {type(other).__name__} in matmul")
+        if self.is_batched:
+            # one product per member: a vector for all members (B, n), or one
+            # vector per member (B, m) -> (B, n)
+            vals = self._values.reshape(-1, self.nnz)
+            if other.ndim == 1:
+                out = [K.csr_spmv(self._crow, self._col, v.contiguous(), other) for v in vals]
+            elif other.ndim == 2 and other.shape[0] == vals.shape[0] and other.shape[1] == self._spshape[1]:
+                out = [K.csr_spmv(self._crow, self._col, v.contiguous(), x.contiguous())
+                       for v, x in zip(vals, other)]
+            else:
+                raise ValueError("a batched matrix multiplies a vector (m,) or one vector per member (B, m)")
+            return torch.stack(out).reshape(self.dense_shape + (self._spshape[0],))
         if other.ndim == 1:
             return K.csr_spmv(self._crow, self._col, self._values, other)
         if other.ndim == 2:
@@ -152,6 +181,7 @@ class CSRTensor:
     def diags(self) -> "CSRTensor":
         """Diagonal part (FEALPy ``CSRTensor.diags``); every row of an
         assembled FE matrix has its diagonal entry."""
+        self._single("diags")
         d, _ = K.csr_diagonal(self._crow, self._col, self._values)
         n = self._spshape[0]
         crow = torch.arange(n + 1, dtype=torch.int64, device=self.device)
@@ -160,11 +190,14 @@ class CSRTensor:
         return out
 
     def diagonal_inverse(self) -> torch.Tensor:
+        self._single("diagonal_inverse")
         if self._dinv is None:
             _, self._dinv = K.csr_diagonal(self._crow, self._col, self._values)
         return self._dinv
 
     def is_diagonal(self) -> bool:
+        if self.is_batched:
+            return False
         n = self._spshape[0]
         if self.nnz != n or self._spshape[0] != self._spshape[1]:
             return False
@@ -304,8 +337,9 @@ class CSRTensor:
         if axis == 0:
             return self @ torch.ones(self._spshape[1], dtype=self._vals().dtype, device=self.device)
         if axis == 1:
-            out = torch.zeros(self._spshape[1], dtype=self._vals().dtype, device=self.device)
-            return out.index_add_(0, self._col.long(), self._vals())
+            v = self._vals()
+            out = torch.zeros(v.shape[:-1] + (self._spshape[1],), dtype=v.dtype, device=self.device)
+            return out.index_add_(-1, self._col.long(), v)
         raise ValueError("axis must be 0 or 1")
 
     @property
@@ -330,8 +364,8 @@ class COOTensor:
         if values is not None:
             if not isinstance(values, torch.Tensor):
                 raise TypeError(f"values must be a Tensor or None, but got {type(values)}")
-            if values.ndim != 1 or values.shape[0] != indices.shape[1]:
-                raise ValueError("values must be shaped (nnz,) like the indices")
+            if values.ndim < 1 or values.shape[-1] != indices.shape[1]:
+                raise ValueError("values must be shaped (..., nnz) like the indices")
         self._indices = indices
         self._values = values
         self.is_coalesced = is_coalesced
@@ -364,10 +398,16 @@ class COOTensor:
         return self._indices.shape[1]
 
     @property
-    def shape(self):
-        return self._spshape
+    def dense_shape(self):
+        return tuple(self._values.shape[:-1]) if self._values is not None else ()
 
-    sparse_shape = shape
+    @property
+    def shape(self):
+        return self.dense_shape + self._spshape
+
+    @property
+    def sparse_shape(self):
+        return self._spshape
 
     @property
     def dtype(self):
@@ -398,7 +438,8 @@ class COOTensor:
             return COOTensor(indices, None, self._spshape, is_coalesced=True)
         src = self._values if self._values is not None else torch.ones(self.nnz, dtype=torch.int64,
                                                                        device=self.device)
-        values = torch.zeros(uniq.numel(), dtype=src.dtype, device=self.device).index_add_(0, inv, src)
+        values = torch.zeros(src.shape[:-1] + (uniq.numel(),), dtype=src.dtype,
+                             device=self.device).index_add_(-1, inv, src)
         return COOTensor(indices, values, self._spshape, is_coalesced=True)
 
     def tocoo(self, *, copy=False):
@@ -418,9 +459,10 @@ class COOTensor:
     def to_dense(self):
         values = self._values if self._values is not None else torch.ones(self.nnz, dtype=torch.float64,
                                                                            device=self.device)
-        out = torch.zeros(self._spshape[0] * self._spshape[1], dtype=values.dtype, device=self.device)
-        out.index_add_(0, self._indices[0] * self._spshape[1] + self._indices[1], values)
-        return out.reshape(self._spshape)
+        out = torch.zeros(values.shape[:-1] + (self._spshape[0] * self._spshape[1],), dtype=values.dtype,
+                          device=self.device)
+        out.index_add_(-1, self._indices[0] * self._spshape[1] + self._indices[1], values)
+        return out.reshape(values.shape[:-1] + self._spshape)
 
     def copy(self):
         return COOTensor(self._indices.clone(), None if self._values is None else self._values.clone(),

@@ -6,6 +6,7 @@ Run in an environment where the reference checkout is importable:
     python tests/golden/make_golden.py /path/to/fealpy-checkout            # small cases, C1
     python tests/golden/make_golden.py --configs /path/to/fealpy-checkout  # mid-size config laws
     python tests/golden/make_golden.py --coef /path/to/fealpy-checkout     # (NC, NQ) coefficients
+    python tests/golden/make_golden.py --batched /path/to/fealpy-checkout  # batched coefficients
 
 The fixtures hold only inputs and outputs of the reference (meshes, dof maps,
 local matrices, CSR matrices, vectors, iteration counts, quadrature tables and
@@ -417,6 +418,47 @@ def coef_cases(ref_root):
     print("region", len(reg), mesh.number_of_cells(), A.nnz)
 
 
+def batched_cases(ref_root):
+    """A form with batched coefficients (``fealpy/fem/bilinear_form.py:46-75``,
+    ``fealpy/functional.py:68-106``): on P2 triangles (3x3 box, jittered),
+    batch size 3, a diffusion coefficient per member and cell (B, NC)
+    (lognormal) in one group and a mass coefficient per member (B,) in
+    another (the reference stacks groups without a batch over the batch, and
+    refuses batched and unbatched integrators in one group), q = 4.  The
+    fixture ``batched_tri_p2`` holds the inputs, the reference's batched
+    local diffusion matrices (B, NC, 6, 6) and its CSR with values (B, nnz)
+    in canonical order (the numpy backend has no product of a batched
+    matrix: ``fealpy/backend/numpy_backend.py:181-199``)."""
+    sys.path.insert(0, HERE)
+    import refshim
+    refshim.install(ref_root)
+    from fealpy.backend import backend_manager as bm
+    bm.set_backend("numpy")
+    from fealpy.mesh import TriangleMesh
+    from fealpy.functionspace import LagrangeFESpace
+    from fealpy.fem import BilinearForm, ScalarDiffusionIntegrator, ScalarMassIntegrator
+
+    rng = np.random.default_rng(20261205)
+    m0 = TriangleMesh.from_box([0, 1, 0, 1], 3, 3)
+    mesh = TriangleMesh(jitter(m0.node, m0.boundary_node_flag(), 1.0 / 3, 0.15, rng), m0.cell)
+    space = LagrangeFESpace(mesh, p=2)
+    B, NC = 3, mesh.number_of_cells()
+    kappa = np.exp(rng.normal(size=(B, NC)))
+    rho = rng.uniform(0.5, 2.0, size=B)
+    Kd = ScalarDiffusionIntegrator(coef=kappa, q=4, batched=True).assembly(space)
+    bf = BilinearForm(space, batch_size=B)
+    bf.add_integrator(ScalarDiffusionIntegrator(coef=kappa, q=4, batched=True))
+    bf.add_integrator(ScalarMassIntegrator(coef=rho, q=4, batched=True))
+    A = bf.assembly()
+    crow = np.asarray(A.crow, dtype=np.int64)
+    row = np.repeat(np.arange(len(crow) - 1), np.diff(crow))
+    order = np.lexsort((np.asarray(A.col), row))
+    np.savez_compressed(os.path.join(HERE, "batched_tri_p2.npz"), node=mesh.node, cell=mesh.cell, kappa=kappa,
+                        rho=rho, K_diff=Kd, crow=crow, col=np.asarray(A.col)[order].astype(np.int32),
+                        val=np.asarray(A.values)[:, order])
+    print("batched", B, NC, A.nnz, np.asarray(A.values).shape)
+
+
 def _reference_root(argv):
     root = argv[0] if argv else os.environ.get("FEALPY_REFERENCE")
     if not root:
@@ -431,5 +473,7 @@ if __name__ == "__main__":
         config_cases(_reference_root(args))
     elif "--coef" in sys.argv[1:]:
         coef_cases(_reference_root(args))
+    elif "--batched" in sys.argv[1:]:
+        batched_cases(_reference_root(args))
     else:
         main(_reference_root(args))

@@ -494,3 +494,55 @@ def test_forms_assembled_apart_add_to_the_grouped_form(golden_dir):
     T = S.T
     assert same(T.crow, z["crow"]) and same(T.col, z["col"])
     assert rel_err(T.values, z["val"]) < VAL_TOL
+
+
+def test_batched_form_against_reference(golden_dir):
+    """A form with batched coefficients (``BilinearForm(space, batch_size=3)``,
+    diffusion with a (B, NC) coefficient and mass with a (B,) coefficient,
+    both ``batched=True``) against the reference's batched CSR (values
+    (B, nnz)) and batched local matrices; products per member, COO output;
+    the single-matrix paths refuse the batch."""
+    dev = cuda()
+    import scipy.sparse as sps
+    import fealpy_gb300 as F
+    from fealpy_gb300.fem import BilinearForm, ScalarDiffusionIntegrator, ScalarMassIntegrator, DirichletBC
+    z = load(golden_dir, "batched_tri_p2.npz")
+    mesh = F.TriangleMesh(torch.as_tensor(z["node"], device=dev),
+                          torch.as_tensor(z["cell"], dtype=torch.int32, device=dev))
+    space = F.LagrangeFESpace(mesh, 2)
+    kappa = torch.as_tensor(z["kappa"], device=dev)
+    rho = torch.as_tensor(z["rho"], device=dev)
+    Kd = ScalarDiffusionIntegrator(coef=kappa, q=4, batched=True).assembly(space)
+    assert Kd.shape == z["K_diff"].shape and rel_err(Kd, z["K_diff"]) < VAL_TOL
+    bf = BilinearForm(space, batch_size=3)
+    bf.add_integrator(ScalarDiffusionIntegrator(coef=kappa, q=4, batched=True))
+    bf.add_integrator(ScalarMassIntegrator(coef=rho, q=4, batched=True))
+    A = bf.assembly()
+    n = space.number_of_global_dofs()
+    assert A.is_batched and tuple(A.shape) == (3, n, n) and A.values.shape == z["val"].shape
+    assert same(A.crow, z["crow"]) and same(A.col, z["col"])
+    assert rel_err(A.values, z["val"]) < VAL_TOL
+    # mixing a batched and an unbatched integrator in one group: the unbatched
+    # one repeats over the batch
+    bg = BilinearForm(space, batch_size=3)
+    bg.add_integrator(ScalarDiffusionIntegrator(coef=kappa, q=4, batched=True), ScalarMassIntegrator(coef=1.0, q=4))
+    Ag = bg.assembly()
+    for b in range(3):
+        bm_ = BilinearForm(space)
+        bm_.add_integrator(ScalarDiffusionIntegrator(coef=kappa[b], q=4), ScalarMassIntegrator(coef=1.0, q=4))
+        assert torch.equal(Ag.values[b], bm_.assembly().values)
+    # products per member: one vector for all, one vector per member
+    x = torch.as_tensor(np.random.default_rng(5).normal(size=(3, n)), device=dev)
+    y1 = A @ x[0]
+    yb = A @ x
+    for b in range(3):
+        Sb = sps.csr_matrix((z["val"][b], z["col"], z["crow"]), shape=(n, n))
+        assert rel_err(y1[b], Sb @ x[0].cpu().numpy()) < VAL_TOL
+        assert rel_err(yb[b], Sb @ x[b].cpu().numpy()) < VAL_TOL
+    C = bf.assembly(format="coo")
+    assert C.shape == (3, n, n) and torch.equal(C.values, A.values)
+    assert torch.equal(A.to_dense()[1], F.CSRTensor(A.crow, A.col, A.values[1], (n, n)).to_dense())
+    with pytest.raises(ValueError):
+        F.cg(A, x[0])
+    with pytest.raises(ValueError):
+        DirichletBC(space, gd=0.0).apply(A, x[0])

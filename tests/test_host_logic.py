@@ -282,3 +282,27 @@ def test_csr_arithmetic_matches_scipy():
     assert A.partial(mask).nnz == int(mask.sum())
     with pytest.raises(ValueError):
         A + CSRTensor.from_scipy(sps.random(30, 30, density=0.1, format="csr"), device="cpu")
+
+
+def test_batched_sparse_bookkeeping():
+    """Batched values (B, nnz) on one pattern (a form with batched
+    coefficients): dense form, COO round trip, coalescing per member."""
+    from fealpy_gb300.sparse import COOTensor, CSRTensor
+    crow = torch.tensor([0, 2, 3, 5])
+    col = torch.tensor([0, 2, 1, 0, 2], dtype=torch.int32)
+    vals = torch.arange(10, dtype=torch.float64).reshape(2, 5)
+    A = CSRTensor(crow, col, vals, (3, 3))
+    assert A.is_batched and A.shape == (2, 3, 3) and A.sparse_shape == (3, 3)
+    D = A.to_dense()
+    for b in range(2):
+        assert torch.equal(D[b], CSRTensor(crow, col, vals[b], (3, 3)).to_dense())
+    C = A.tocoo()
+    assert C.shape == (2, 3, 3) and torch.equal(C.to_dense(), D)
+    R = C.tocsr()
+    assert torch.equal(R.crow, crow) and torch.equal(R.values, vals)
+    # duplicates summed member by member
+    U = COOTensor(torch.tensor([[0, 0, 1], [1, 1, 0]]), torch.tensor([[1., 2., 3.], [4., 5., 6.]]), (2, 2))
+    c = U.coalesce()
+    assert torch.equal(c.values, torch.tensor([[3., 3.], [9., 6.]]))
+    with pytest.raises(ValueError):
+        A.diags()
