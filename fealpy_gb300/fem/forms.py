@@ -186,13 +186,27 @@ class BilinearForm(_Form):
             cell = mesh.cell if plan.cells is None else mesh.cell[plan.cells].contiguous()
             NN = mesh.number_of_nodes()
             adj_ptr, adj, nptr, nidx = self._symbolic(ss, cell, NN, marks, plan.cells is not None)
-            indptr, indices = K.expand_blocks(NN, plan.gd, space.dof_priority, nptr, nidx)
+            # the kernel writes the interleaved layout (3 node + component)
+            indptr, indices = K.expand_blocks(NN, plan.gd, False, nptr, nidx)
             n = space.number_of_global_dofs()
             fac = K.cell_factors(mesh, plan.channels, plan.coef_matrix(), dtype, status, cells=plan.cells)
             _mark(marks, "factors")
             values, v32 = K.assemble_elasticity_p1(plan.gd, adj_ptr, adj, cell, fac, nptr, nidx, indptr,
                                                    indices.numel(), values_f32=emit_f32 and dtype == torch.float64,
                                                    status=status)
+            if space.dof_priority:
+                # component-major layout (shape=(GD, -1)): row comp NN + node
+                # is the interleaved row GD node + comp; the permutation keeps
+                # every entry's value (the same sum) and sorts the columns
+                gd = plan.gd
+                k = torch.arange(n, device=space.device, dtype=torch.int64)
+                order = (k % NN) * gd + k // NN
+                inv = torch.empty_like(order)
+                inv[order] = k
+                _lib.check_status_word("assembly", status)
+                indptr, indices, values = K.csr_permute(indptr, indices, values, order, inv)
+                if v32 is not None:
+                    v32 = values.to(torch.float32)
             _mark(marks, "values")
         else:
             raise NotImplementedError

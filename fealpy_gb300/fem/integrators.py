@@ -341,8 +341,10 @@ class ScalarMassIntegrator(_BatchedCoef, _OperatorIntegrator):
 
 
 class LinearElasticityIntegrator(_OperatorIntegrator):
-    """Linear elasticity on a ``TensorFunctionSpace`` of P1 Lagrange functions,
-    interleaved components (``dof_priority=False``)."""
+    """Linear elasticity on a ``TensorFunctionSpace`` of P1 Lagrange functions:
+    interleaved components (``shape=(-1, GD)``, ``dof_priority=False``) or
+    component-major (``shape=(GD, -1)``; the form permutes the interleaved
+    matrix)."""
 
     def __init__(self, material, q: Optional[int] = None, *, index=_S, method=None):
         super().__init__()
@@ -372,8 +374,6 @@ class LinearElasticityIntegrator(_OperatorIntegrator):
         gd = mesh.GD
         if ss.p != 1:
             raise NotImplementedError("the GB300 elasticity kernel covers P1 spaces")
-        if space.dof_priority and not local:
-            raise NotImplementedError("the GB300 elasticity kernel covers the interleaved layout (shape=(-1, GD))")
         q = ss.p + 3 if self.q is None else self.q
         _, ws = mesh.quadrature_formula(q).get_quadrature_points_and_weights()
         wsum = float(np.sum(ws))

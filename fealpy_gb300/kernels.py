@@ -110,6 +110,30 @@ def expand_blocks(n_node: int, bs: int, dof_priority: bool, indptr, indices):
     return out_ptr, out_idx[: nnz_s * bs * bs]
 
 
+def csr_permute(indptr, indices, values, order: torch.Tensor, inv: torch.Tensor):
+    """P A P^T as a canonical CSR: row k of the result is row order[k] of A,
+    columns mapped through inv (inv[order[k]] = k) and sorted in each row;
+    the values (FP64 or FP32) move with their entries."""
+    _values_1d(values, "csr_permute")
+    dev = _dev(indptr)
+    n = indptr.numel() - 1
+    nnz = indices.numel()
+    lib = _lib.lib()
+    ws = workspace(lib.fgb_sell_d16_workspace_bytes(n), dev)
+    new_ptr = torch.empty(n + 1, dtype=torch.int64, device=dev)
+    new_idx = torch.empty(max(nnz, 1), dtype=torch.int32, device=dev)
+    new_val = torch.empty(max(nnz, 1), dtype=values.dtype, device=dev)
+    v64, v32 = (values, None) if values.dtype == torch.float64 else (None, values)
+    n64, n32 = (new_val, None) if values.dtype == torch.float64 else (None, new_val)
+    # the int32 copies are held until the launch is queued (a temporary freed
+    # before the call would hand its block to the next allocation)
+    o32 = order.to(torch.int32).contiguous()
+    i32 = inv.to(torch.int32).contiguous()
+    call("fgb_csr_permute", n, ptr(indptr), ptr(indices), ptr(v64), ptr(v32), ptr(o32), ptr(i32), ptr(new_ptr),
+         ptr(new_idx), ptr(n64), ptr(n32), ptr(ws), ws.numel(), stream_ptr(dev))
+    return new_ptr, new_idx[:nnz], new_val[:nnz]
+
+
 def assemble_scalar(adj_ptr, adj, c2d, tables: torch.Tensor, factors: torch.Tensor, indptr, indices,
                     values_f32: bool = False, status: Optional[torch.Tensor] = None,
                     accumulate_into: Optional[torch.Tensor] = None, positions: Optional[torch.Tensor] = None):

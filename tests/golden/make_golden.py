@@ -7,6 +7,7 @@ Run in an environment where the reference checkout is importable:
     python tests/golden/make_golden.py --configs /path/to/fealpy-checkout  # mid-size config laws
     python tests/golden/make_golden.py --coef /path/to/fealpy-checkout     # (NC, NQ) coefficients
     python tests/golden/make_golden.py --batched /path/to/fealpy-checkout  # batched coefficients
+    python tests/golden/make_golden.py --layouts /path/to/fealpy-checkout  # component-major elasticity
 
 The fixtures hold only inputs and outputs of the reference (meshes, dof maps,
 local matrices, CSR matrices, vectors, iteration counts, quadrature tables and
@@ -459,6 +460,45 @@ def batched_cases(ref_root):
     print("batched", B, NC, A.nnz, np.asarray(A.values).shape)
 
 
+def layout_cases(ref_root):
+    """P1 elasticity in the component-major layout (``TensorFunctionSpace``
+    ``shape=(3, -1)``, ``fealpy/functionspace/tensor_space.py:29-31``) on the
+    mesh, per-cell material scale and q of ``small_elasticity_tet_p1``: the
+    reference's local matrices and CSR (canonical order) in that layout."""
+    sys.path.insert(0, HERE)
+    import refshim
+    refshim.install(ref_root)
+    from fealpy.backend import backend_manager as bm
+    bm.set_backend("numpy")
+    from fealpy.mesh import TetrahedronMesh
+    from fealpy.functionspace import LagrangeFESpace, TensorFunctionSpace
+    from fealpy.material import LinearElasticMaterial
+    from fealpy.fem import BilinearForm, LinearElasticityIntegrator
+
+    z = np.load(os.path.join(HERE, "small_elasticity_tet_p1.npz"))
+    mesh = TetrahedronMesh(z["node"], z["cell"])
+    scale = z["scale"]
+
+    class ScaledMaterial(LinearElasticMaterial):
+        def __init__(self, s, **kw):
+            super().__init__(**kw)
+            self._s = s
+
+        def elastic_matrix(self, bcs=None):
+            return self._s[:, None, None, None] * super().elastic_matrix(bcs)
+
+    mat = ScaledMaterial(scale, name="m", lame_lambda=1.0, shear_modulus=0.5)
+    ts = TensorFunctionSpace(LagrangeFESpace(mesh, p=1), (3, -1))
+    KK = LinearElasticityIntegrator(mat, q=4).assembly(ts)
+    bf = BilinearForm(ts)
+    bf.add_integrator(LinearElasticityIntegrator(mat, q=4))
+    A = bf.assembly()
+    c0, c1, c2 = canonical(A.crow, A.col, A.values)
+    np.savez_compressed(os.path.join(HERE, "elasticity_component_major.npz"), cell2dof=ts.cell_to_dof(), KK=KK,
+                        crow=c0, col=c1, val=c2)
+    print("component-major elasticity", A.shape, A.nnz)
+
+
 def _reference_root(argv):
     root = argv[0] if argv else os.environ.get("FEALPY_REFERENCE")
     if not root:
@@ -475,5 +515,7 @@ if __name__ == "__main__":
         coef_cases(_reference_root(args))
     elif "--batched" in sys.argv[1:]:
         batched_cases(_reference_root(args))
+    elif "--layouts" in sys.argv[1:]:
+        layout_cases(_reference_root(args))
     else:
         main(_reference_root(args))

@@ -546,3 +546,37 @@ def test_batched_form_against_reference(golden_dir):
         F.cg(A, x[0])
     with pytest.raises(ValueError):
         DirichletBC(space, gd=0.0).apply(A, x[0])
+
+
+def test_elasticity_component_major_layout(golden_dir):
+    """P1 elasticity with ``shape=(3, -1)`` (component-major dofs): dof map,
+    local matrices and CSR against the reference in that layout; the solve
+    with the x = 0 clamp equals the interleaved solve with its dofs permuted."""
+    dev = cuda()
+    import fealpy_gb300 as F
+    from fealpy_gb300.fem import BilinearForm, LinearForm, LinearElasticityIntegrator, VectorSourceIntegrator, DirichletBC
+    z0 = load(golden_dir, "small_elasticity_tet_p1.npz")
+    z = load(golden_dir, "elasticity_component_major.npz")
+    mesh = F.TetrahedronMesh(torch.as_tensor(z0["node"], device=dev),
+                             torch.as_tensor(z0["cell"], dtype=torch.int32, device=dev))
+    mat = F.LinearElasticMaterial("m", lame_lambda=1.0, shear_modulus=0.5,
+                                  cell_scale=torch.as_tensor(z0["scale"], device=dev))
+    sols = {}
+    for shape in ((3, -1), (-1, 3)):
+        ts = F.TensorFunctionSpace(F.LagrangeFESpace(mesh, 1), shape)
+        bf = BilinearForm(ts)
+        bf.add_integrator(LinearElasticityIntegrator(mat, q=4))
+        A = bf.assembly()
+        if shape == (3, -1):
+            assert same(ts.cell_to_dof(), z["cell2dof"])
+            assert rel_err(LinearElasticityIntegrator(mat, q=4).assembly(ts), z["KK"]) < VAL_TOL
+            assert same(A.crow, z["crow"]) and same(A.col, z["col"])
+            assert rel_err(A.values, z["val"]) < VAL_TOL
+        lf = LinearForm(ts)
+        lf.add_integrator(VectorSourceIntegrator(source=[0.0, 0.0, -1.0], q=4))
+        bc = DirichletBC(ts, gd=0.0, threshold=lambda x: torch.abs(x[..., 0]) < 1e-12)
+        A2, F2 = bc.apply(A, lf.assembly())
+        sols[shape] = F.cg(A2, F2, M=F.JacobiPreconditioner().apply(A2), atol=1e-30, rtol=1e-12)
+    NN = mesh.number_of_nodes()
+    inter = sols[(-1, 3)].reshape(NN, 3)
+    assert rel_err(sols[(3, -1)], inter.T.reshape(-1).cpu().numpy()) < 1e-9
