@@ -113,6 +113,7 @@ _SIGNATURES = {
                                    c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "fgb_cell_apply": (c_i32, [c_i32, c_i64, c_i32, c_vp, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "fgb_csr_spmv": (c_i32, [c_i32, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_i32, c_vp]),
+    "fgb_csr_spmm_f64": (c_i32, [c_i64, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "fgb_residual_norm_workspace_bytes": (c_sz, []),
     "fgb_residual_norm": (c_i32, [c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_sz, c_vp]),
     "fgb_csr_diagonal": (c_i32, [c_i32, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
@@ -231,7 +232,7 @@ def check(fn_name, code):
 KERNELS_PER_CALL = {
     "fgb_cell_factors": 1, "fgb_adjacency_build": 6, "fgb_pattern_count": 5, "fgb_pattern_fill": 2, "fgb_pattern_build": 5, "fgb_pattern_compact": 2,
     "fgb_pattern_expand_blocks": 2, "fgb_assemble_scalar": 2, "fgb_assemble_scalar_acc": 2, "fgb_local_matrices": 1, "fgb_csr_split_blocks": 2, "fgb_residual_norm": 2, "fgb_source_local": 1, "fgb_source_gather": 1, "fgb_local_elasticity_p1": 1, "fgb_assemble_elasticity_p1": 2,
-    "fgb_dirichlet_count": 1, "fgb_exclusive_scan_i32": 3, "fgb_dirichlet_fill": 1, "fgb_csr_spmv": 1,
+    "fgb_dirichlet_count": 1, "fgb_exclusive_scan_i32": 3, "fgb_dirichlet_fill": 1, "fgb_csr_spmv": 1, "fgb_csr_spmm_f64": 1,
     "fgb_csr_diagonal": 1, "fgb_gather_sum": 1, "fgb_cell_apply": 1,
     "fgb_topology_count": 8, "fgb_topology_fill": 2, "fgb_cell_to_ipoint": 1, "fgb_sell_plan": 4, "fgb_sell_fill": 1, "fgb_sell_spmv": 1,
     "fgb_sell_renumber": 1, "fgb_csr_permute": 5, "fgb_sell_d16_indptr": 4, "fgb_sell_fill_d16": 1,

@@ -50,7 +50,8 @@ __device__ void mr_block_partials(double v, int k, double* sbuf, double* part) {
   for (int64_t i = static_cast<int64_t>(blockIdx.x) * rows_per_block + threadIdx.x / (k);             \
        lane_ok && i < (n); i += static_cast<int64_t>(gridDim.x) * rows_per_block)
 
-// mode 0: Y = B - A X ; mode 1: Y = A X with per-column partials of X.Y
+// mode 0: Y = B - A X ; mode 1: Y = A X with per-column partials of X.Y ;
+// mode 2: Y = A X (A of any width: X holds k values per column of A)
 __global__ void mr_spmm(int64_t n, int k, const int64_t* __restrict__ indptr, const int32_t* __restrict__ indices,
                         const double* __restrict__ values, const double* __restrict__ X,
                         const double* __restrict__ B, double* __restrict__ Y, int mode, double* part) {
@@ -64,10 +65,11 @@ __global__ void mr_spmm(int64_t n, int k, const int64_t* __restrict__ indptr, co
       Y[o] = B[o] - s;
     } else {
       Y[o] = s;
-      acc_dot += X[o] * s;
+      if (mode == 1) acc_dot += X[o] * s;
     }
   }
   if (mode == 1) mr_block_partials(acc_dot, k, sbuf, part);
+  (void)acc_dot;
 }
 
 // Z = D^-1 R (or R), P = Z, per-column partials of R.Z and of B.B
@@ -297,6 +299,14 @@ int32_t fgb_pcg_multi_f64(int64_t n, int32_t k, const int64_t* indptr, const int
   }
   if (reason == FGB_PCG_BREAKDOWN) return FGB_ERR_BREAKDOWN;
   if (reason == FGB_PCG_NONFINITE) return FGB_ERR_NONFINITE;
+  return launch_status();
+}
+
+int32_t fgb_csr_spmm_f64(int64_t n_row, int32_t k, const int64_t* indptr, const int32_t* indices,
+                         const double* values, const double* X, double* Y, void* stream) {
+  if (n_row <= 0 || k <= 0 || k > kMrMaxCols || !indptr || !indices || !values || !X || !Y) return FGB_ERR_ARG;
+  cudaStream_t st = as_stream(stream);
+  mr_spmm<<<mr_blocks(n_row, k), kMrThreads, 0, st>>>(n_row, k, indptr, indices, values, X, nullptr, Y, 2, nullptr);
   return launch_status();
 }
 

@@ -333,6 +333,19 @@ def residual_norm(indptr, indices, values, b, x):
     return rr ** 0.5, bb ** 0.5
 
 
+def csr_spmm(indptr, indices, values, X: torch.Tensor) -> torch.Tensor:
+    """Y = A X for X (m, k) row-major FP64, k <= 64, in one pass over the matrix."""
+    _values_1d(values, "csr_spmm")
+    dev = _dev(indptr)
+    n = indptr.numel() - 1
+    k = X.shape[1]
+    X = X.to(dev, torch.float64).contiguous()
+    Y = torch.empty((n, k), dtype=torch.float64, device=dev)
+    vals = values.contiguous()
+    call("fgb_csr_spmm_f64", n, k, ptr(indptr), ptr(indices), ptr(vals), ptr(X), ptr(Y), stream_ptr(dev))
+    return Y
+
+
 def csr_diagonal(indptr, indices, values):
     _values_1d(values, "csr_diagonal")
     dev = _dev(indptr)

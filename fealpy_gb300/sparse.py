@@ -171,6 +171,9 @@ class CSRTensor:
         if other.ndim == 1:
             return K.csr_spmv(self._crow, self._col, self._values, other)
         if other.ndim == 2:
+            if self._values.dtype == torch.float64 and 1 <= other.shape[1] <= 64:
+                # all columns in one pass over the matrix
+                return K.csr_spmm(self._crow, self._col, self._values, other)
             cols = [K.csr_spmv(self._crow, self._col, self._values, other[:, k].contiguous())
                     for k in range(other.shape[1])]
             return torch.stack(cols, dim=1)

@@ -337,6 +337,14 @@ int32_t fgb_csr_spmv(int32_t dtype, int64_t n_row, const int64_t* indptr, const 
                      const void* values, const void* x, void* y, int32_t lanes_per_row,
                      void* stream);
 
+/* Y = A X for k right-hand columns at once (the (n, batch) product of
+ * bm.csr_spmm, fealpy/backend/numpy_backend.py:181-199): X (n_col, k) and
+ * Y (n_row, k) row-major FP64, 1 <= k <= 64; the matrix is read once for all
+ * columns.  Every entry of Y is the same sum in the same order as
+ * fgb_csr_spmv with one lane per row. */
+int32_t fgb_csr_spmm_f64(int64_t n_row, int32_t k, const int64_t* indptr, const int32_t* indices,
+                         const double* values, const double* X, double* Y, void* stream);
+
 /* out2[0] = ||b - A x||^2, out2[1] = ||b||^2 (FP64 CSR, device scalars,
  * deterministic): the true residual of FEALPy's stopping test
  * (fealpy/solver/cg.py:99-113) as the restart loops of the FP32-refined

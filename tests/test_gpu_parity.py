@@ -170,6 +170,41 @@ def test_spmv_all_lane_widths(golden_dir):
         assert rel_err(y32, ref) < 1e-5
 
 
+def test_spmm_columns_in_one_pass(golden_dir):
+    """A @ X for X (n, k) (the (n, batch) product of bm.csr_spmm): one pass
+    over the matrix for all k columns, against scipy; each column the same
+    sum as the one-lane-per-row SpMV; k = 1, 3, 64 and a rectangular
+    matrix."""
+    dev = cuda()
+    import scipy.sparse as sp
+    import fealpy_gb300 as F
+    from fealpy_gb300 import kernels as K
+    z = load(golden_dir, "cfg_c2_tet_p2_8.npz")
+    crow, col, val = z["crow"], z["col"], z["val"]
+    n = len(crow) - 1
+    S = sp.csr_matrix((val, col, crow), shape=(n, n))
+    A = F.CSRTensor(torch.as_tensor(crow, device=dev), torch.as_tensor(col, device=dev),
+                    torch.as_tensor(val, device=dev), (n, n))
+    rng = np.random.default_rng(3)
+    for k in (1, 3, 64):
+        X = rng.normal(size=(n, k))
+        Y = A @ torch.as_tensor(X, device=dev)
+        assert Y.shape == (n, k) and rel_err(Y, S @ X) < 1e-14
+        y0 = K.csr_spmv(A.crow, A.col, A.values, torch.as_tensor(X[:, 0].copy(), device=dev), 1)
+        assert torch.equal(Y[:, 0], y0)
+    # wider than 64 columns: one product per column
+    X = rng.normal(size=(n, 65))
+    assert rel_err(A @ torch.as_tensor(X, device=dev), S @ X) < 1e-14
+    # a rectangular matrix (the first 100 columns of A)
+    R = S[:, :100].tocsr()
+    R.sort_indices()
+    Ar = F.CSRTensor(torch.as_tensor(R.indptr, dtype=torch.int64, device=dev),
+                     torch.as_tensor(R.indices, dtype=torch.int32, device=dev),
+                     torch.as_tensor(R.data, device=dev), R.shape)
+    X = rng.normal(size=(100, 5))
+    assert rel_err(Ar @ torch.as_tensor(X, device=dev), R @ X) < 1e-14
+
+
 def test_determinism_bitwise(golden_dir):
     dev = cuda()
     import fealpy_gb300 as F
