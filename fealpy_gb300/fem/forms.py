@@ -106,7 +106,23 @@ class BilinearForm(_Form):
 
     @property
     def shape(self):
-        return self.sparse_shape
+        return ((self.batch_size,) if self.batch_size > 0 else ()) + tuple(self.sparse_shape)
+
+    def _members(self):
+        """Unbatched forms of the batch members (kept for repeated matrix-free
+        products; rebuilt when integrators are added)."""
+        cached = getattr(self, "_member_forms", None)
+        key = tuple((g, id(it)) for g, it in self.integrators.items())
+        if cached is None or cached[0] != key:
+            forms = []
+            for b in range(self.batch_size):
+                f = BilinearForm(self.space)
+                for g, it in self.integrators.items():
+                    f.integrators[g] = it.batch_member(self.space, b)
+                forms.append(f)
+            cached = (key, forms)
+            self._member_forms = cached
+        return cached[1]
 
     def _plan(self):
         plans = [it.plan(self.space) for it in self.integrators.values()]
@@ -262,6 +278,14 @@ class BilinearForm(_Form):
             return self._M @ u
         if not isinstance(u, torch.Tensor):
             raise TypeError("u must be a torch tensor")
+        if self.batch_size > 0:
+            # batched coefficients: (B, n) out, u (n,) or one vector per member (B, n)
+            members = self._members()
+            if u.ndim == 1:
+                return torch.stack([f._matfree(u) for f in members])
+            if u.ndim == 2 and u.shape[0] == self.batch_size:
+                return torch.stack([f._matfree(v) for f, v in zip(members, u)])
+            raise ValueError(f"a batched form multiplies (n,) or ({self.batch_size}, n) vectors")
         if u.ndim >= 2:
             return torch.stack([self._matfree(v) for v in u.reshape(-1, u.shape[-1])]).reshape(
                 u.shape[:-1] + (self.shape[0],))

@@ -574,6 +574,14 @@ def test_batched_form_against_reference(golden_dir):
         Sb = sps.csr_matrix((z["val"][b], z["col"], z["crow"]), shape=(n, n))
         assert rel_err(y1[b], Sb @ x[0].cpu().numpy()) < VAL_TOL
         assert rel_err(yb[b], Sb @ x[b].cpu().numpy()) < VAL_TOL
+    # matrix free before assembly (fealpy/fem/bilinear_form.py:126-158): (B, n)
+    bu = BilinearForm(space, batch_size=3)
+    bu.add_integrator(ScalarDiffusionIntegrator(coef=kappa, q=4, batched=True))
+    bu.add_integrator(ScalarMassIntegrator(coef=rho, q=4, batched=True))
+    assert bu.shape == (3, n, n)
+    m1, mb = bu @ x[0], bu @ x
+    assert bu._M is None and m1.shape == (3, n) and mb.shape == (3, n)
+    assert rel_err(m1, y1.cpu().numpy()) < VAL_TOL and rel_err(mb, yb.cpu().numpy()) < VAL_TOL
     C = bf.assembly(format="coo")
     assert C.shape == (3, n, n) and torch.equal(C.values, A.values)
     assert torch.equal(A.to_dense()[1], F.CSRTensor(A.crow, A.col, A.values[1], (n, n)).to_dense())
