@@ -344,12 +344,25 @@ class LinearForm(_Form):
     into dofs by the deterministic adjacency gather."""
 
     def __init__(self, *space, batch_size: int = 0):
-        if batch_size != 0:
-            raise NotImplementedError("batched right-hand sides are not provided")
         super().__init__(*space, batch_size=batch_size)
         self._V = None
 
     def assembly(self, *, format="dense") -> torch.Tensor:
+        if self.batch_size > 0:
+            # batched sources (fealpy/fem/linear_form.py:36-60): one vector per
+            # member, (B, n); unbatched integrators repeat over the batch
+            space = self.space
+            out = []
+            for b in range(self.batch_size):
+                member = LinearForm(space)
+                for g, it in self.integrators.items():
+                    nb = it.batch_size(space)
+                    if nb not in (0, self.batch_size):
+                        raise ValueError(f"an integrator has {nb} batch members, the form {self.batch_size}")
+                    member.integrators[g] = it.batch_member(space, b)
+                out.append(member.assembly(format=format))
+            self._V = torch.stack(out)
+            return self._V
         space = self.space
         mesh = space.scalar_space.mesh if hasattr(space, "scalar_space") else space.mesh
         n = space.number_of_global_dofs()

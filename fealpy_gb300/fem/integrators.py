@@ -234,12 +234,15 @@ class _OperatorIntegrator(Integrator):
 
 
 class _BatchedCoef:
-    """Batched coefficients of a scalar integrator: a number per member (B,),
-    a per-cell array (B, NC), values at the quadrature points (B, NC, NQ),
-    or a callable returning one of those at the quadrature points."""
+    """Batched coefficients of a scalar integrator (the attribute named by
+    ``_batched_attr``: the coefficient, or a source's values): a number per
+    member (B,), a per-cell array (B, NC), values at the quadrature points
+    (B, NC, NQ), or a callable returning one of those at the quadrature
+    points."""
+    _batched_attr = "coef"
 
     def _batched_values(self, space) -> torch.Tensor:
-        coef = self.coef
+        coef = getattr(self, self._batched_attr)
         mesh = space.mesh
         if callable(coef) and not isinstance(coef, (torch.Tensor, np.ndarray)):
             key = ("batched_coef", id(space))
@@ -273,7 +276,7 @@ class _BatchedCoef:
         member = copy.copy(self)
         member._cache = {}
         member.batched = False
-        member.coef = self._batched_values(space)[b]
+        setattr(member, self._batched_attr, self._batched_values(space)[b])
         return member
 
 
@@ -492,19 +495,25 @@ def _source_values(source, mesh, bcs, index=_S):
     raise TypeError(f"source should be int, float, TensorLike or callable, but got {type(source)}")
 
 
-class ScalarSourceIntegrator(Integrator):
-    """``(f, v)`` (``fealpy/fem/scalar_source_integrator.py:13-90``)."""
+class ScalarSourceIntegrator(_BatchedCoef, Integrator):
+    """``(f, v)`` (``fealpy/fem/scalar_source_integrator.py:13-90``); with
+    ``batched=True`` the source has a leading batch axis (a form with
+    ``batch_size``)."""
+    _batched_attr = "source"
 
     def __init__(self, source=None, q: Optional[int] = None, *, region=None, batched: bool = False, method=None):
         super().__init__()
         self.source = source
         self.q = q
+        self.batched = batched
         self.set_region(region)
 
     def source_data(self, space):
         """(cells or None, signed measures, mode, number, values, w phi table,
         its column sums) of this source for ``fgb_source_local/gather``:
         mode 0 a number, 1 one value per cell, 2 one per quadrature point."""
+        if self.batched:
+            raise ValueError("a batched source is assembled per batch member (a form with batch_size)")
         mesh = space.mesh
         q = space.p + 3 if self.q is None else self.q
         bcs, ws = mesh.quadrature_formula(q).get_quadrature_points_and_weights()

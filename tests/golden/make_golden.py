@@ -427,9 +427,10 @@ def batched_cases(ref_root):
     another (the reference stacks groups without a batch over the batch, and
     refuses batched and unbatched integrators in one group), q = 4.  The
     fixture ``batched_tri_p2`` holds the inputs, the reference's batched
-    local diffusion matrices (B, NC, 6, 6) and its CSR with values (B, nnz)
-    in canonical order (the numpy backend has no product of a batched
-    matrix: ``fealpy/backend/numpy_backend.py:181-199``)."""
+    local diffusion matrices (B, NC, 6, 6), its CSR with values (B, nnz) in
+    canonical order (the numpy backend has no product of a batched matrix:
+    ``fealpy/backend/numpy_backend.py:181-199``), and the batched right-hand
+    side (B, n) of a source given per member and cell."""
     sys.path.insert(0, HERE)
     import refshim
     refshim.install(ref_root)
@@ -454,10 +455,16 @@ def batched_cases(ref_root):
     crow = np.asarray(A.crow, dtype=np.int64)
     row = np.repeat(np.arange(len(crow) - 1), np.diff(crow))
     order = np.lexsort((np.asarray(A.col), row))
+    # batched right-hand side: a source per member and cell (B, NC)
+    from fealpy.fem import LinearForm, ScalarSourceIntegrator
+    fsrc = rng.normal(size=(B, NC))
+    lf = LinearForm(space, batch_size=B)
+    lf.add_integrator(ScalarSourceIntegrator(source=fsrc, q=4, batched=True))
+    Fb = lf.assembly()
     np.savez_compressed(os.path.join(HERE, "batched_tri_p2.npz"), node=mesh.node, cell=mesh.cell, kappa=kappa,
                         rho=rho, K_diff=Kd, crow=crow, col=np.asarray(A.col)[order].astype(np.int32),
-                        val=np.asarray(A.values)[:, order])
-    print("batched", B, NC, A.nnz, np.asarray(A.values).shape)
+                        val=np.asarray(A.values)[:, order], source=fsrc, F=np.asarray(Fb))
+    print("batched", B, NC, A.nnz, np.asarray(A.values).shape, np.asarray(Fb).shape)
 
 
 def layout_cases(ref_root):

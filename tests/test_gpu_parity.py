@@ -535,8 +535,9 @@ def test_batched_form_against_reference(golden_dir):
     """A form with batched coefficients (``BilinearForm(space, batch_size=3)``,
     diffusion with a (B, NC) coefficient and mass with a (B,) coefficient,
     both ``batched=True``) against the reference's batched CSR (values
-    (B, nnz)) and batched local matrices; products per member, COO output;
-    the single-matrix paths refuse the batch."""
+    (B, nnz)), batched local matrices and batched right-hand side; products
+    per member (assembled and matrix free), COO output; the single-matrix
+    paths refuse the batch."""
     dev = cuda()
     import scipy.sparse as sps
     import fealpy_gb300 as F
@@ -585,6 +586,12 @@ def test_batched_form_against_reference(golden_dir):
     C = bf.assembly(format="coo")
     assert C.shape == (3, n, n) and torch.equal(C.values, A.values)
     assert torch.equal(A.to_dense()[1], F.CSRTensor(A.crow, A.col, A.values[1], (n, n)).to_dense())
+    # batched right-hand side (fealpy/fem/linear_form.py:36-60)
+    from fealpy_gb300.fem import LinearForm, ScalarSourceIntegrator
+    lf = LinearForm(space, batch_size=3)
+    lf.add_integrator(ScalarSourceIntegrator(source=torch.as_tensor(z["source"], device=dev), q=4, batched=True))
+    Fb = lf.assembly()
+    assert Fb.shape == (3, n) and rel_err(Fb, z["F"]) < VAL_TOL
     with pytest.raises(ValueError):
         F.cg(A, x[0])
     with pytest.raises(ValueError):
