@@ -169,3 +169,47 @@ def test_config_law_elasticity_case(golden_dir):
     assert rel_err(out["bc_F"], z["bc_F"]) < RTOL
     assert abs(out["info"]["niter"] - int(z["niter"])) <= 1
     assert rel_err(out["x"], z["uh"]) < 1e-9
+
+
+def test_batched_form_case(golden_dir):
+    """The oracle, member by member, against the reference's batched form:
+    a batch member's matrix is the unbatched assembly with that member's
+    coefficients (``fealpy/functional.py:68-106``), the batched right-hand
+    side likewise."""
+    z = load(golden_dir, "batched_tri_p2.npz")
+    node, cell = z["node"], z["cell"]
+    topo = O.construct(cell)
+    NN = node.shape[0]
+    c2d = O.cell_to_dof(cell, topo, NN, 2)
+    n = O.n_global_dofs(cell, topo, NN, 2)
+    Kd = np.stack([O.diffusion_local(node, cell, 2, 4, k) for k in z["kappa"]])
+    assert rel_err(Kd, z["K_diff"]) < RTOL
+    NQ = O._rule(2, 2, 4)[1].shape[0]
+    for b in range(z["kappa"].shape[0]):
+        K = O.diffusion_local(node, cell, 2, 4, z["kappa"][b]) + O.mass_local(node, cell, 2, 4, z["rho"][b])
+        crow, col, val = O.coalesce_to_csr(c2d, K, n)
+        assert np.array_equal(crow, z["crow"]) and np.array_equal(col, z["col"])
+        assert rel_err(val, z["val"][b]) < RTOL
+        fq = np.repeat(z["source"][b][:, None], NQ, axis=1)
+        assert rel_err(O.source_vector(node, cell, c2d, 2, n, fq, q=4), z["F"][b]) < RTOL
+
+
+def test_elasticity_component_major_case(golden_dir):
+    """The oracle's interleaved elasticity matrix with rows and columns
+    renumbered component-major (dof comp NN + node) against the reference's
+    shape=(3, -1) matrix."""
+    z0 = load(golden_dir, "small_elasticity_tet_p1.npz")
+    z = load(golden_dir, "elasticity_component_major.npz")
+    node, cell, s = z0["node"], z0["cell"], z0["scale"]
+    NN = node.shape[0]
+    KK = O.elasticity_local(node, cell, 1.0 * s, 0.5 * s, q=4)
+    crow, col, val = O.coalesce_to_csr(O.vector_elasticity_dofs(cell), KK, 3 * NN)
+    new_of = (np.arange(3 * NN) % 3) * NN + np.arange(3 * NN) // 3      # interleaved -> component-major
+    c2d_cm = new_of[O.vector_elasticity_dofs(cell)]
+    assert np.array_equal(np.sort(c2d_cm, axis=1), np.sort(z["cell2dof"], axis=1))
+    rows = new_of[np.repeat(np.arange(3 * NN), np.diff(crow))]
+    cols = new_of[col]
+    order = np.lexsort((cols, rows))
+    crow_cm = np.concatenate([[0], np.cumsum(np.bincount(rows, minlength=3 * NN))])
+    assert np.array_equal(crow_cm, z["crow"]) and np.array_equal(cols[order], z["col"])
+    assert rel_err(val[order], z["val"]) < RTOL
