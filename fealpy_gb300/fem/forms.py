@@ -13,7 +13,8 @@ import torch
 from ..sparse import CSRTensor
 from .. import _lib
 from .. import kernels as K
-from .integrators import (ElasticityPlan, GroupIntegrator, Integrator, ScalarPlan, ScalarSourceIntegrator)
+from .integrators import (ElasticityPlan, GroupIntegrator, Integrator, ScalarPlan, ScalarSourceIntegrator,
+                          _same_cells)
 
 __all__ = ["BilinearForm", "LinearForm", "symbolic_structure"]
 
@@ -125,16 +126,26 @@ class BilinearForm(_Form):
         return cached[1]
 
     def _plan(self):
+        """The merged plan of the form's integrators; scalar integrators over
+        different cells (a region per integrator group,
+        ``fealpy/fem/integrator.py:141-162``) give a list of plans, one per
+        distinct cell set."""
         plans = [it.plan(self.space) for it in self.integrators.values()]
         if not plans:
             raise RuntimeError("no integrator added to the form")
-        out = plans[0]
-        for p in plans[1:]:
-            if isinstance(out, ScalarPlan) and isinstance(p, ScalarPlan):
-                out = out + p
-            else:
+        if not all(isinstance(p, ScalarPlan) for p in plans):
+            if len(plans) > 1:
                 raise NotImplementedError("only several scalar integrators can share one form")
-        return out
+            return plans[0]
+        merged = []
+        for p in plans:
+            for k, m in enumerate(merged):
+                if _same_cells(m.cells, p.cells):
+                    merged[k] = m + p
+                    break
+            else:
+                merged.append(p)
+        return merged[0] if len(merged) == 1 else merged
 
     def _symbolic(self, space, c2d, n, marks=None, sub: bool = False, positions: bool = False):
         key = ("symbolic", n, positions)
@@ -167,7 +178,30 @@ class BilinearForm(_Form):
         plan = self._plan()
         status = _lib.status_word(space.device)
         _mark(marks, "start")
-        if isinstance(plan, ScalarPlan):
+        if isinstance(plan, list):
+            # several cell sets: the pattern of their union, then each set's
+            # values added into it (its own adjacency, column search)
+            full = space.cell_to_dof()
+            c2ds = [full if p.cells is None else full[p.cells].contiguous() for p in plan]
+            n = space.number_of_global_dofs()
+            adj_ptr, adj, indptr, indices = symbolic_structure(torch.cat(c2ds).contiguous(), n, marks=marks)
+            mesh = space.mesh
+            values = v32 = None
+            for g, (p, c2d) in enumerate(zip(plan, c2ds)):
+                st = _lib.status_word(space.device)
+                g_ptr, g_adj, _ = K.build_adjacency(c2d, n, st)
+                _lib.check_status_word("adjacency", st)
+                coef = p.coef_matrix()
+                passes = p.passes()
+                for k, (chans, tabs) in enumerate(passes):
+                    fac = K.cell_factors(mesh, chans, coef, dtype, status, cells=p.cells)
+                    tab = torch.as_tensor(tabs, dtype=dtype, device=space.device)
+                    last = g == len(plan) - 1 and k == len(passes) - 1
+                    values, v32 = K.assemble_scalar(g_ptr, g_adj, c2d, tab, fac, indptr, indices,
+                                                    values_f32=emit_f32 and dtype == torch.float64 and last,
+                                                    status=status, accumulate_into=values)
+            _mark(marks, "values")
+        elif isinstance(plan, ScalarPlan):
             c2d = space.cell_to_dof()
             sub = plan.cells is not None
             if sub:
@@ -291,8 +325,36 @@ class BilinearForm(_Form):
                 u.shape[:-1] + (self.shape[0],))
         return self._matfree(u)
 
+    def _region_forms(self):
+        """One form per distinct cell set of the integrator groups (kept for
+        repeated matrix-free products)."""
+        key = tuple((g, id(it)) for g, it in self.integrators.items())
+        cached = getattr(self, "_region_cache", None)
+        if cached is None or cached[0] != key:
+            forms = []
+            for g, it in self.integrators.items():
+                cells = it.plan(self.space).cells
+                for f, c in forms:
+                    if _same_cells(c, cells):
+                        f.integrators[g] = it
+                        break
+                else:
+                    f = BilinearForm(self.space)
+                    f.integrators[g] = it
+                    forms.append((f, cells))
+            cached = (key, [f for f, _ in forms])
+            self._region_cache = cached
+        return cached[1]
+
     def _matfree(self, u):
         plan = self._plan()
+        if isinstance(plan, list):
+            # integrator groups over different cells: the sum of their products
+            out = None
+            for f in self._region_forms():
+                y = f._matfree(u)
+                out = y if out is None else out + y
+            return out
         if not isinstance(plan, ScalarPlan):
             raise NotImplementedError("matrix-free products are provided for scalar integrators")
         space = self.space

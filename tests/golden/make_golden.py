@@ -8,6 +8,7 @@ Run in an environment where the reference checkout is importable:
     python tests/golden/make_golden.py --coef /path/to/fealpy-checkout     # (NC, NQ) coefficients
     python tests/golden/make_golden.py --batched /path/to/fealpy-checkout  # batched coefficients
     python tests/golden/make_golden.py --layouts /path/to/fealpy-checkout  # component-major elasticity
+    python tests/golden/make_golden.py --regions /path/to/fealpy-checkout  # groups over different regions
 
 The fixtures hold only inputs and outputs of the reference (meshes, dof maps,
 local matrices, CSR matrices, vectors, iteration counts, quadrature tables and
@@ -506,6 +507,46 @@ def layout_cases(ref_root):
     print("component-major elasticity", A.shape, A.nnz)
 
 
+def multi_region_cases(ref_root):
+    """Integrator groups over different regions of one form
+    (``fealpy/fem/integrator.py:141-162``, ``fealpy/fem/form.py:92-122``): on
+    P2 triangles (5x4 box, jittered), a diffusion group with a cartesian
+    coefficient over the cells with centroid x < 0.55, a diffusion group
+    (coefficient 3) over the cells with centroid x > 0.35 (the regions
+    overlap) and a mass group (coefficient 2, ``index=``; the reference's
+    mass integrator takes no ``region``) over the same cells, q = 4.  The fixture ``multi_region_tri_p2`` holds
+    the inputs and the reference's CSR (canonical order)."""
+    sys.path.insert(0, HERE)
+    import refshim
+    refshim.install(ref_root)
+    from fealpy.backend import backend_manager as bm
+    bm.set_backend("numpy")
+    from fealpy.mesh import TriangleMesh
+    from fealpy.functionspace import LagrangeFESpace
+    from fealpy.fem import BilinearForm, ScalarDiffusionIntegrator, ScalarMassIntegrator
+    from fealpy.decorator import cartesian
+
+    @cartesian
+    def kappa(p):
+        return 1.0 + p[..., 0] ** 2 + p[..., 1]
+
+    rng = np.random.default_rng(20261206)
+    m0 = TriangleMesh.from_box([0, 1, 0, 1], 5, 4)
+    mesh = TriangleMesh(jitter(m0.node, m0.boundary_node_flag(), 0.2, 0.15, rng), m0.cell)
+    xc = mesh.entity_barycenter("cell")[:, 0]
+    reg1, reg2 = np.nonzero(xc < 0.55)[0], np.nonzero(xc > 0.35)[0]
+    space = LagrangeFESpace(mesh, p=2)
+    bf = BilinearForm(space)
+    bf.add_integrator(ScalarDiffusionIntegrator(coef=kappa, q=4), region=reg1)
+    bf.add_integrator(ScalarDiffusionIntegrator(coef=3.0, q=4), region=reg2)
+    bf.add_integrator(ScalarMassIntegrator(coef=2.0, q=4, index=reg2))
+    A = bf.assembly()
+    c0, c1, c2 = canonical(A.crow, A.col, A.values)
+    np.savez_compressed(os.path.join(HERE, "multi_region_tri_p2.npz"), node=mesh.node, cell=mesh.cell, reg1=reg1,
+                        reg2=reg2, crow=c0, col=c1, val=c2)
+    print("multi-region", len(reg1), len(reg2), mesh.number_of_cells(), A.nnz)
+
+
 def _reference_root(argv):
     root = argv[0] if argv else os.environ.get("FEALPY_REFERENCE")
     if not root:
@@ -524,5 +565,7 @@ if __name__ == "__main__":
         batched_cases(_reference_root(args))
     elif "--layouts" in sys.argv[1:]:
         layout_cases(_reference_root(args))
+    elif "--regions" in sys.argv[1:]:
+        multi_region_cases(_reference_root(args))
     else:
         main(_reference_root(args))

@@ -113,3 +113,33 @@ def test_region_source_and_elasticity_consistency(golden_dir):
     KK = LinearElasticityIntegrator(mat, q=4, index=treg).assembly(ts)
     KA = LinearElasticityIntegrator(mat, q=4).assembly(ts)
     assert KK.shape[0] == treg.numel() and rel(KK, KA[treg]) < 1e-13
+
+
+def test_groups_over_different_regions_against_reference(golden_dir):
+    """Integrator groups over different (overlapping) regions of one form
+    (fealpy/fem/integrator.py:141-162): the pattern of the union of the
+    regions, each group's values added into it, against the reference's CSR;
+    the matrix-free product (the sum of the groups' products) against the
+    assembled one."""
+    dev = cuda()
+    import fealpy_gb300 as F
+    from fealpy_gb300.fem import BilinearForm, ScalarDiffusionIntegrator, ScalarMassIntegrator
+    z = np.load(os.path.join(golden_dir, "multi_region_tri_p2.npz"))
+    mesh = F.TriangleMesh(torch.as_tensor(z["node"], device=dev), torch.as_tensor(z["cell"], device=dev))
+    space = F.LagrangeFESpace(mesh, p=2)
+    reg1 = torch.as_tensor(z["reg1"], device=dev)
+    reg2 = torch.as_tensor(z["reg2"], device=dev)
+
+    def form():
+        bf = BilinearForm(space)
+        bf.add_integrator(ScalarDiffusionIntegrator(coef=_kappa, q=4), region=reg1)
+        bf.add_integrator(ScalarDiffusionIntegrator(coef=3.0, q=4), region=reg2)
+        bf.add_integrator(ScalarMassIntegrator(coef=2.0, q=4, index=reg2))
+        return bf
+
+    A = form().assembly()
+    assert np.array_equal(A.crow.cpu().numpy(), z["crow"]) and np.array_equal(A.col.cpu().numpy(), z["col"])
+    assert rel(A.values, z["val"]) < 1e-12
+    bf = form()
+    u = torch.rand(space.number_of_global_dofs(), dtype=torch.float64, device=dev)
+    assert rel(bf @ u, (A @ u).cpu().numpy()) < 1e-12 and bf._M is None
