@@ -193,13 +193,14 @@ class BilinearForm(_Form):
                 _lib.check_status_word("adjacency", st)
                 coef = p.coef_matrix()
                 passes = p.passes()
-                for k, (chans, tabs) in enumerate(passes):
+                for chans, tabs in passes:
                     fac = K.cell_factors(mesh, chans, coef, dtype, status, cells=p.cells)
                     tab = torch.as_tensor(tabs, dtype=dtype, device=space.device)
-                    last = g == len(plan) - 1 and k == len(passes) - 1
-                    values, v32 = K.assemble_scalar(g_ptr, g_adj, c2d, tab, fac, indptr, indices,
-                                                    values_f32=emit_f32 and dtype == torch.float64 and last,
-                                                    status=status, accumulate_into=values)
+                    values, _ = K.assemble_scalar(g_ptr, g_adj, c2d, tab, fac, indptr, indices,
+                                                  status=status, accumulate_into=values)
+            # the float copy of the totals (a cell set's pass covers its own rows only)
+            if emit_f32 and dtype == torch.float64:
+                v32 = values.to(torch.float32)
             _mark(marks, "values")
         elif isinstance(plan, ScalarPlan):
             c2d = space.cell_to_dof()
