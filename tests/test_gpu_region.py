@@ -143,3 +143,6 @@ def test_groups_over_different_regions_against_reference(golden_dir):
     bf = form()
     u = torch.rand(space.number_of_global_dofs(), dtype=torch.float64, device=dev)
     assert rel(bf @ u, (A @ u).cpu().numpy()) < 1e-12 and bf._M is None
+    # the FP32 copy for the mixed-precision solver covers every row
+    A2 = form().assembly(emit_f32=True)
+    assert torch.equal(A2.values, A.values) and torch.equal(A2._f32, A.values.to(torch.float32))
