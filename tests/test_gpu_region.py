@@ -7,6 +7,8 @@ ScalarSource, ``index=`` of ScalarMass / LinearElasticity;
   holds only the region's couplings, bit-exact; values 1e-12.  The region as
   indices, as a boolean mask and as a callable of the mesh give the same.
 * The matrix-free product over the region equals the region CSR product.
+* Integrator groups over two overlapping regions of one form against the
+  reference's CSR (``multi_region_tri_p2.npz``, ``make_golden.py --regions``).
 * Cases the reference itself cannot run (its source integrator ignores the
   region in its dof map; its elasticity integrator sizes local matrices by all
   cells) are checked for consistency: a region source equals the full source
