@@ -246,7 +246,8 @@ class CSRTensor:
                 raise ValueError(f"shapes {self.shape} and {tuple(other.shape)} do not match")
             out = other * alpha
             out = out.to(torch.promote_types(out.dtype, self._vals().dtype)).clone()
-            out.index_put_(self.nonzero_slice, self._vals().to(out.dtype), accumulate=True)
+            nz = (Ellipsis,) + self.nonzero_slice     # (row, col) of every member; no duplicates
+            out[nz] = out[nz] + self._vals().to(out.dtype)
             return out
         if isinstance(other, (int, float)):
             return CSRTensor(self._crow.clone(), self._col.clone(), self._vals() + alpha * other, self._spshape)
@@ -273,7 +274,7 @@ class CSRTensor:
         if isinstance(other, torch.Tensor):
             if tuple(other.shape) != tuple(self.shape):
                 raise ValueError(f"shapes {self.shape} and {tuple(other.shape)} do not match")
-            vals = other[self.nonzero_slice]
+            vals = other[(Ellipsis,) + self.nonzero_slice]
             if self._values is not None:
                 vals = self._values * vals
             return CSRTensor(self._crow, self._col, vals, self._spshape)
@@ -299,7 +300,8 @@ class CSRTensor:
                     return CSRTensor(self._crow, self._col, self._values / other[self._col.long()], self._spshape)
             if tuple(other.shape) != tuple(self.shape):
                 raise ValueError(f"shapes {self.shape} and {tuple(other.shape)} do not match")
-            return CSRTensor(self._crow, self._col, self._values / other[self.nonzero_slice], self._spshape)
+            return CSRTensor(self._crow, self._col, self._values / other[(Ellipsis,) + self.nonzero_slice],
+                             self._spshape)
         raise TypeError(f"Unsupported type {type(other).__name__} in division")
 
     __truediv__ = div
@@ -312,7 +314,8 @@ class CSRTensor:
         if isinstance(other, torch.Tensor):
             if tuple(other.shape) != tuple(self.shape):
                 raise ValueError(f"shapes {self.shape} and {tuple(other.shape)} do not match")
-            return CSRTensor(self._crow, self._col, self._values ** other[self.nonzero_slice], self._spshape)
+            return CSRTensor(self._crow, self._col, self._values ** other[(Ellipsis,) + self.nonzero_slice],
+                             self._spshape)
         raise TypeError(f"Unsupported type {type(other).__name__} in power")
 
     __pow__ = pow

@@ -306,3 +306,20 @@ def test_batched_sparse_bookkeeping():
     assert torch.equal(c.values, torch.tensor([[3., 3.], [9., 6.]]))
     with pytest.raises(ValueError):
         A.diags()
+
+
+def test_batched_csr_dense_operands():
+    """Dense operands of a batched CSR (values (B, nnz)) act member by member."""
+    from fealpy_gb300.sparse import CSRTensor
+    crow = torch.tensor([0, 2, 3, 5])
+    col = torch.tensor([0, 2, 1, 0, 2], dtype=torch.int32)
+    vals = torch.arange(1, 11, dtype=torch.float64).reshape(2, 5)
+    A = CSRTensor(crow, col, vals, (3, 3))
+    D = torch.rand(2, 3, 3, dtype=torch.float64, generator=torch.Generator().manual_seed(2))
+    dense = A.to_dense()
+    assert torch.allclose(A + D, dense + D, rtol=0, atol=1e-15)
+    assert torch.allclose(A.mul(D).to_dense(), dense * D * (dense != 0), rtol=0, atol=1e-15)
+    for b in range(2):
+        Ab = CSRTensor(crow, col, vals[b], (3, 3))
+        assert torch.allclose(A.div(D).values[b], Ab.div(D[b]).values, rtol=0, atol=1e-15)
+        assert torch.allclose((A ** D).values[b], (Ab ** D[b]).values, rtol=0, atol=1e-15)
